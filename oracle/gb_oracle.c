@@ -1,0 +1,1165 @@
+/*
+ * gb_oracle.c -- CPU oracle for GraphBrew's algorithm-12 mapping path.
+ *
+ * TEST INFRASTRUCTURE ONLY: a plain-C restatement of the reference algorithm,
+ * used by the tests to check the CUDA path and by the benchmark as the CPU
+ * baseline.  The product library never links or loads this file.
+ *
+ * Reference file paths below are relative to the GraphBrew project root;
+ * RG = bench/include/graphbrew/reorder/reorder_graphbrew.h,
+ * RT = bench/include/graphbrew/reorder/reorder_types.h,
+ * BH = bench/include/external/gapbs/builder.h.
+ *
+ * Floating point: every Delta-modularity expression keeps the reference's
+ * association and is compiled with -ffp-contract=off, so each product, sum and
+ * quotient is one IEEE double operation, exactly as in the reference.
+ */
+#include "gb_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define ORC_NONE ((uint32_t)0xFFFFFFFFu)
+
+static double now_seconds(void)
+{
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+int orc_max_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+static inline int64_t degree_of(const orc_graph *g, int64_t u)
+{
+    return g->row_ptr[u + 1] - g->row_ptr[u];
+}
+
+/* ------------------------------------------------------------------------ */
+/* Auto resolution: RT:2743-2780.                                            */
+/* ------------------------------------------------------------------------ */
+double orc_auto_resolution(const orc_graph *g)
+{
+    const int64_t n = g->n;
+    if (n == 0) return 1.0;
+    /* num_edges() of an undirected CSRGraph is the directed count / 2. */
+    const int64_t m = (g->row_ptr[n] - g->row_ptr[0]) / 2;
+    const double avg_degree = (double)m / (double)n;
+    double sum_sq = 0.0;
+    for (int64_t v = 0; v < n; ++v) {
+        const double d = (double)degree_of(g, v);
+        const double diff = d - avg_degree;
+        sum_sq += diff * diff;
+    }
+    const double variance = sum_sq / (double)n;
+    const double cv = (avg_degree > 0) ? sqrt(variance) / avg_degree : 0.0;
+    double resolution = 0.5 + 0.25 * log10(avg_degree + 1);
+    resolution = fmax(0.5, fmin(1.2, resolution));
+    if (cv > 2.0) {
+        const double factor = 2.0 / fmax(2.0, sqrt(cv));
+        resolution = fmax(0.5, resolution * factor);
+    }
+    return resolution;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Dense accumulator with a touched list.  The reference keeps a sparse     */
+/* open-addressing table (RG:1133-1232); the selection below is independent */
+/* of key iteration order, so a dense table gives the same answers.         */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+    double *val;       /* capacity entries, all 0 between uses */
+    uint32_t *keys;    /* touched keys */
+    int64_t nkeys;
+} orc_acc;
+
+static int acc_init(orc_acc *a, int64_t capacity, int64_t max_keys)
+{
+    a->val = (double *)calloc((size_t)(capacity > 0 ? capacity : 1), sizeof(double));
+    a->keys = (uint32_t *)malloc((size_t)(max_keys > 0 ? max_keys : 1) * sizeof(uint32_t));
+    a->nkeys = 0;
+    return (a->val && a->keys) ? ORC_OK : ORC_ENOMEM;
+}
+
+static void acc_free(orc_acc *a)
+{
+    free(a->val);
+    free(a->keys);
+}
+
+static inline void acc_add(orc_acc *a, uint32_t k, double w)
+{
+    /* A key is "touched" when first added; weights here are always > 0. */
+    if (a->val[k] == 0.0) a->keys[a->nkeys++] = k;
+    a->val[k] += w;
+}
+
+static inline void acc_clear(orc_acc *a)
+{
+    for (int64_t i = 0; i < a->nkeys; ++i) a->val[a->keys[i]] = 0.0;
+    a->nkeys = 0;
+}
+
+/* deltaModularity (RG:1295-1298). */
+static inline double delta_modularity(double k_u_c, double k_u_d, double k_u,
+                                      double sigma_c, double sigma_d,
+                                      double M, double R)
+{
+    return (k_u_c - k_u_d) / M - R * k_u * (sigma_c - sigma_d + k_u) / (2.0 * M * M);
+}
+
+/* chooseCommunityGreedy (RG:1494-1527): the candidate with the largest
+ * positive delta; equal deltas go to the smaller community id. */
+static inline uint32_t choose_community(const orc_acc *a, uint32_t d, double k_u,
+                                        const double *ctot, double M, double R,
+                                        double *best_delta_out)
+{
+    uint32_t best_c = d;
+    double best_delta = 0.0;
+    int found = 0;
+    const double k_u_d = a->val[d];
+    const double sigma_d = ctot[d];
+    for (int64_t i = 0; i < a->nkeys; ++i) {
+        const uint32_t c = a->keys[i];
+        if (c == d) continue;
+        const double delta = delta_modularity(a->val[c], k_u_d, k_u, ctot[c], sigma_d, M, R);
+        if (delta > best_delta || (found && delta == best_delta && c < best_c)) {
+            best_delta = delta;
+            best_c = c;
+            found = 1;
+        }
+    }
+    *best_delta_out = best_delta;
+    return best_c;
+}
+
+/* localMovingPhase<false> in serial order (RG:1588-1734 with one thread). */
+static int local_move_serial(const orc_graph *g, uint32_t *vcom, double *ctot,
+                             char *vaff, const double *vtot, double M, double R,
+                             double tolerance, int max_iterations, orc_acc *acc)
+{
+    const int64_t n = g->n;
+    int iterations = 0;
+    for (int iter = 0; iter < max_iterations; ++iter) {
+        double total_delta = 0.0;
+        for (int64_t u = 0; u < n; ++u) {
+            if (!vaff[u]) continue;
+            const uint32_t d = vcom[u];
+            acc_clear(acc);
+            for (int64_t e = g->row_ptr[u]; e < g->row_ptr[u + 1]; ++e) {
+                const int32_t v = g->col[e];
+                if (v == u) continue;
+                acc_add(acc, vcom[v], 1.0);
+            }
+            double delta;
+            const uint32_t best_c = choose_community(acc, d, vtot[u], ctot, M, R, &delta);
+            if (best_c != d) {
+                ctot[d] -= vtot[u];
+                ctot[best_c] += vtot[u];
+                vcom[u] = best_c;
+                for (int64_t e = g->row_ptr[u]; e < g->row_ptr[u + 1]; ++e)
+                    vaff[g->col[e]] = 1;
+            }
+            vaff[u] = 0;
+            total_delta += delta;
+        }
+        ++iterations;
+        if (total_delta <= tolerance) break;
+    }
+    return iterations;
+}
+
+#ifdef _OPENMP
+/* localMovingPhase<false> as the reference runs it with several threads:
+ * dynamic chunks of 4096 vertices (DEFAULT_TILE_SIZE), racy reads of vcom and
+ * ctot, atomic ctot updates (RG:1538-1573, :1655-1724). */
+static int local_move_parallel(const orc_graph *g, uint32_t *vcom, double *ctot,
+                               char *vaff, const double *vtot, double M, double R,
+                               double tolerance, int max_iterations,
+                               orc_acc *accs)
+{
+    const int64_t n = g->n;
+    int iterations = 0;
+    for (int iter = 0; iter < max_iterations; ++iter) {
+        double total_delta = 0.0;
+#pragma omp parallel reduction(+ : total_delta)
+        {
+            orc_acc *acc = &accs[omp_get_thread_num()];
+#pragma omp for schedule(dynamic, 4096)
+            for (int64_t u = 0; u < n; ++u) {
+                if (!__atomic_load_n(&vaff[u], __ATOMIC_RELAXED)) continue;
+                const uint32_t d = __atomic_load_n(&vcom[u], __ATOMIC_RELAXED);
+                acc_clear(acc);
+                for (int64_t e = g->row_ptr[u]; e < g->row_ptr[u + 1]; ++e) {
+                    const int32_t v = g->col[e];
+                    if (v == u) continue;
+                    acc_add(acc, __atomic_load_n(&vcom[v], __ATOMIC_RELAXED), 1.0);
+                }
+                double delta;
+                const uint32_t best_c = choose_community(acc, d, vtot[u], ctot, M, R, &delta);
+                if (best_c != d) {
+#pragma omp atomic
+                    ctot[d] -= vtot[u];
+#pragma omp atomic
+                    ctot[best_c] += vtot[u];
+                    __atomic_store_n(&vcom[u], best_c, __ATOMIC_RELAXED);
+                    for (int64_t e = g->row_ptr[u]; e < g->row_ptr[u + 1]; ++e)
+                        __atomic_store_n(&vaff[g->col[e]], (char)1, __ATOMIC_RELAXED);
+                }
+                __atomic_store_n(&vaff[u], (char)0, __ATOMIC_RELAXED);
+                total_delta += delta;
+            }
+        }
+        ++iterations;
+        if (total_delta <= tolerance) break;
+    }
+    return iterations;
+}
+#endif
+
+/* countCommunities (RG:1843-1865). */
+static int64_t count_communities(const uint32_t *vcom, int64_t n, uint32_t *exists)
+{
+    memset(exists, 0, (size_t)n * sizeof(uint32_t));
+    int64_t count = 0;
+    for (int64_t u = 0; u < n; ++u) {
+        if (!exists[vcom[u]]) {
+            exists[vcom[u]] = 1;
+            ++count;
+        }
+    }
+    return count;
+}
+
+/* renumberCommunities (RG:1870-1889): increasing old id. */
+static int64_t renumber_communities(uint32_t *vcom, int64_t n, uint32_t *cmap)
+{
+    uint32_t next = 0;
+    for (int64_t i = 0; i < n; ++i)
+        if (cmap[i]) cmap[i] = next++;
+    for (int64_t u = 0; u < n; ++u) vcom[u] = cmap[vcom[u]];
+    return next;
+}
+
+/* aggregateGVEStyle (RG:2156-2439).  vcom holds renumbered ids < C on entry;
+ * on exit it holds the merged, first-occurrence renumbered ids and ctot their
+ * totals.  Returns the merged community count. */
+static int64_t aggregate_gve(const orc_graph *g, uint32_t *vcom, double *ctot,
+                             const double *vtot, int64_t C, double M, double R,
+                             int max_iterations, int batch, int parallel,
+                             orc_leiden_stats *stats)
+{
+    const int64_t n = g->n;
+    int64_t result = -1;
+    double *super_weight = (double *)calloc((size_t)(C > 0 ? C : 1), sizeof(double));
+    int64_t *coff = (int64_t *)calloc((size_t)C + 1, sizeof(int64_t));
+    uint32_t *cvtx = (uint32_t *)malloc((size_t)(n > 0 ? n : 1) * sizeof(uint32_t));
+    int64_t *adj_off = (int64_t *)calloc((size_t)C + 1, sizeof(int64_t));
+    uint32_t *super_comm = (uint32_t *)malloc((size_t)(C > 0 ? C : 1) * sizeof(uint32_t));
+    double *super_ctot = (double *)malloc((size_t)(C > 0 ? C : 1) * sizeof(double));
+    uint32_t *proposed = (uint32_t *)malloc((size_t)(C > 0 ? C : 1) * sizeof(uint32_t));
+    double *proposed_delta = (double *)malloc((size_t)(C > 0 ? C : 1) * sizeof(double));
+    uint32_t *adj_c = NULL;
+    double *adj_w = NULL;
+    orc_acc acc = {0};
+    orc_acc *taccs = NULL;
+    int ntacc = 0;
+    if (!super_weight || !coff || !cvtx || !adj_off || !super_comm || !super_ctot ||
+        !proposed || !proposed_delta || acc_init(&acc, C, C) != ORC_OK)
+        goto done;
+#ifdef _OPENMP
+    if (parallel) {
+        ntacc = omp_get_max_threads();
+        taccs = (orc_acc *)calloc((size_t)ntacc, sizeof(orc_acc));
+        if (!taccs) goto done;
+        for (int i = 0; i < ntacc; ++i)
+            if (acc_init(&taccs[i], C, C) != ORC_OK) goto done;
+    }
+#endif
+
+    /* super_weight (RG:2173-2178). */
+    for (int64_t v = 0; v < n; ++v) super_weight[vcom[v]] += vtot[v];
+
+    /* buildCommunityVertices (RG:1912-1942): stable counting sort. */
+    for (int64_t u = 0; u < n; ++u) coff[vcom[u] + 1]++;
+    for (int64_t c = 0; c < C; ++c) coff[c + 1] += coff[c];
+    {
+        int64_t *pos = (int64_t *)malloc((size_t)(C > 0 ? C : 1) * sizeof(int64_t));
+        if (!pos) goto done;
+        memcpy(pos, coff, (size_t)C * sizeof(int64_t));
+        for (int64_t u = 0; u < n; ++u) cvtx[pos[vcom[u]]++] = (uint32_t)u;
+        free(pos);
+    }
+
+    /* Super-graph adjacency: inter-community edges only (RG:2184-2224). */
+    {
+        /* First pass: count distinct neighbour communities per community. */
+        for (int64_t c = 0; c < C; ++c) {
+            acc_clear(&acc);
+            for (int64_t i = coff[c]; i < coff[c + 1]; ++i) {
+                const uint32_t u = cvtx[i];
+                for (int64_t e = g->row_ptr[u]; e < g->row_ptr[u + 1]; ++e) {
+                    const uint32_t cv = vcom[g->col[e]];
+                    if (cv != (uint32_t)c) acc_add(&acc, cv, 1.0);
+                }
+            }
+            adj_off[c + 1] = adj_off[c] + acc.nkeys;
+        }
+        acc_clear(&acc);
+        adj_c = (uint32_t *)malloc((size_t)(adj_off[C] > 0 ? adj_off[C] : 1) * sizeof(uint32_t));
+        adj_w = (double *)malloc((size_t)(adj_off[C] > 0 ? adj_off[C] : 1) * sizeof(double));
+        if (!adj_c || !adj_w) goto done;
+        for (int64_t c = 0; c < C; ++c) {
+            acc_clear(&acc);
+            for (int64_t i = coff[c]; i < coff[c + 1]; ++i) {
+                const uint32_t u = cvtx[i];
+                for (int64_t e = g->row_ptr[u]; e < g->row_ptr[u + 1]; ++e) {
+                    const uint32_t cv = vcom[g->col[e]];
+                    if (cv != (uint32_t)c) acc_add(&acc, cv, 1.0);
+                }
+            }
+            for (int64_t k = 0; k < acc.nkeys; ++k) {
+                adj_c[adj_off[c] + k] = acc.keys[k];
+                adj_w[adj_off[c] + k] = acc.val[acc.keys[k]];
+            }
+        }
+        acc_clear(&acc);
+    }
+
+    /* Batched super-move (RG:2226-2380).  A batch of 1 is the sequential
+     * variant (RG:2325-2380): both propose from the state before the vertex's
+     * own batch and commit moves with a positive delta in id order. */
+    for (int64_t c = 0; c < C; ++c) {
+        super_comm[c] = (uint32_t)c;
+        super_ctot[c] = super_weight[c];
+    }
+    const int super_max_iter = max_iterations < 3 ? max_iterations : 3;
+    const int64_t bs = batch > 1 ? batch : 1;
+    int iters_run = 0;
+    for (int iter = 0; iter < super_max_iter; ++iter) {
+        int64_t moves = 0;
+        ++iters_run;
+        for (int64_t begin = 0; begin < C; begin += bs) {
+            const int64_t end = begin + bs < C ? begin + bs : C;
+#ifdef _OPENMP
+#pragma omp parallel if (parallel && end - begin > 256)
+#endif
+            {
+                orc_acc *a = &acc;
+#ifdef _OPENMP
+                if (taccs) a = &taccs[omp_get_thread_num()];
+#pragma omp for schedule(static)
+#endif
+                for (int64_t c = begin; c < end; ++c) {
+                    const uint32_t d = super_comm[c];
+                    const double kc = super_weight[c];
+                    const double sigma_d = super_ctot[d];
+                    const double delta_removal = R * kc * (sigma_d - kc) / M;
+                    acc_clear(a);
+                    for (int64_t k = adj_off[c]; k < adj_off[c + 1]; ++k)
+                        acc_add(a, super_comm[adj_c[k]], adj_w[k]);
+                    const double kc_to_d = a->val[d];
+                    uint32_t best_comm = d;
+                    double best_delta = 0.0;
+                    for (int64_t k = 0; k < a->nkeys; ++k) {
+                        const uint32_t e = a->keys[k];
+                        const double kc_to_e = a->val[e];
+                        const double delta_addition = e == d
+                            ? kc_to_d - delta_removal
+                            : kc_to_e - R * kc * super_ctot[e] / M;
+                        const double delta = delta_addition - delta_removal + kc_to_d;
+                        if (delta > best_delta || (delta == best_delta && e < best_comm)) {
+                            best_delta = delta;
+                            best_comm = e;
+                        }
+                    }
+                    acc_clear(a);
+                    proposed[c] = best_comm;
+                    proposed_delta[c] = best_delta;
+                }
+            }
+            for (int64_t c = begin; c < end; ++c) {
+                const uint32_t d = super_comm[c];
+                const uint32_t best_comm = proposed[c];
+                if (best_comm == d || proposed_delta[c] <= 0.0) continue;
+                const double kc = super_weight[c];
+                super_ctot[d] -= kc;
+                super_ctot[best_comm] += kc;
+                super_comm[c] = best_comm;
+                ++moves;
+            }
+        }
+        stats->super_moves += moves;
+        if (moves == 0) break;
+    }
+    stats->super_move_iterations += iters_run;
+
+    /* Remap and first-occurrence renumber (RG:2389-2419). */
+    for (int64_t v = 0; v < n; ++v) vcom[v] = super_comm[vcom[v]];
+    {
+        uint32_t max_c = 0;
+        for (int64_t v = 0; v < n; ++v) if (vcom[v] > max_c) max_c = vcom[v];
+        uint32_t *renum = (uint32_t *)malloc(((size_t)max_c + 1) * sizeof(uint32_t));
+        if (!renum) goto done;
+        for (uint32_t c = 0; c <= max_c; ++c) renum[c] = ORC_NONE;
+        uint32_t next = 0;
+        for (int64_t v = 0; v < n; ++v)
+            if (renum[vcom[v]] == ORC_NONE) renum[vcom[v]] = next++;
+        for (int64_t v = 0; v < n; ++v) vcom[v] = renum[vcom[v]];
+        free(renum);
+        result = next;
+    }
+    /* ctot of the merged communities (RG:2421-2428); ctot has n entries. */
+    for (int64_t v = 0; v < n; ++v) ctot[v] = 0.0;
+    for (int64_t v = 0; v < n; ++v) ctot[vcom[v]] += vtot[v];
+
+done:
+    free(super_weight);
+    free(coff);
+    free(cvtx);
+    free(adj_off);
+    free(adj_c);
+    free(adj_w);
+    free(super_comm);
+    free(super_ctot);
+    free(proposed);
+    free(proposed_delta);
+    acc_free(&acc);
+    if (taccs) {
+        for (int i = 0; i < ntacc; ++i) acc_free(&taccs[i]);
+        free(taccs);
+    }
+    return result;
+}
+
+int orc_leiden(const orc_graph *g, const orc_leiden_cfg *cfg,
+               uint32_t *membership, orc_leiden_stats *stats)
+{
+    if (!g || !cfg || !membership || g->n < 0) return ORC_EINVAL;
+    orc_leiden_stats local_stats;
+    if (!stats) stats = &local_stats;
+    memset(stats, 0, sizeof(*stats));
+    const int64_t n = g->n;
+    if (n == 0) return ORC_OK;
+    const int64_t m = (g->row_ptr[n] - g->row_ptr[0]) / 2;
+    /* RG:7246-7248. */
+    const double M = cfg->total_edges_m ? fmax(1.0, (double)m) : (double)m / 2.0;
+    const double R = cfg->resolution;
+
+    int rc = ORC_ENOMEM;
+    double *vtot = (double *)malloc((size_t)n * sizeof(double));
+    double *ctot = (double *)malloc((size_t)n * sizeof(double));
+    char *vaff = (char *)malloc((size_t)n);
+    uint32_t *cmap = (uint32_t *)malloc((size_t)n * sizeof(uint32_t));
+    orc_acc *accs = NULL;
+    int nacc = 1;
+#ifdef _OPENMP
+    if (cfg->parallel) {
+        if (cfg->threads > 0) omp_set_num_threads(cfg->threads);
+        nacc = omp_get_max_threads();
+    }
+#endif
+    accs = (orc_acc *)calloc((size_t)nacc, sizeof(orc_acc));
+    if (!vtot || !ctot || !vaff || !cmap || !accs) goto done;
+    for (int i = 0; i < nacc; ++i)
+        if (acc_init(&accs[i], n, n) != ORC_OK) goto done;
+
+    /* computeVertexWeights / initializeCommunities (RG:1307-1381). */
+    for (int64_t u = 0; u < n; ++u) {
+        vtot[u] = (double)degree_of(g, u);
+        membership[u] = (uint32_t)u;
+        ctot[u] = vtot[u];
+        vaff[u] = 1;
+    }
+
+    double tolerance = cfg->tolerance;
+    int64_t prev_communities = n;
+    int pass = 0;
+    for (; pass < cfg->max_passes && M > 0; ++pass) {
+        double t0 = now_seconds();
+        int iters;
+#ifdef _OPENMP
+        if (cfg->parallel)
+            iters = local_move_parallel(g, membership, ctot, vaff, vtot, M, R,
+                                        tolerance, cfg->max_iterations, accs);
+        else
+#endif
+            iters = local_move_serial(g, membership, ctot, vaff, vtot, M, R,
+                                      tolerance, cfg->max_iterations, &accs[0]);
+        stats->local_move_seconds += now_seconds() - t0;
+        if (pass < 16) stats->pass_iterations[pass] = iters;
+        stats->iterations += iters;
+
+        const int64_t nc = count_communities(membership, n, cmap);
+        if (pass == 0) stats->pass0_communities = nc;
+        /* GVE mode checks convergence only after aggregation (RG:7400-7421). */
+        if (pass >= cfg->max_passes - 1) break;
+
+        t0 = now_seconds();
+        const int64_t C = renumber_communities(membership, n, cmap);
+        const int64_t merged = aggregate_gve(g, membership, ctot, vtot, C, M, R,
+                                             cfg->max_iterations, cfg->super_move_batch,
+                                             cfg->parallel, stats);
+        stats->aggregate_seconds += now_seconds() - t0;
+        if (merged < 0) goto done;
+        stats->aggregated_communities = merged;
+        /* RG:7436-7452. */
+        if (merged >= prev_communities || merged == 1) break;
+        if ((double)merged / (double)prev_communities >= cfg->aggregation_tolerance) break;
+        prev_communities = merged;
+        for (int64_t v = 0; v < n; ++v) vaff[v] = 1;
+        tolerance /= cfg->tolerance_drop;
+    }
+    stats->passes = pass + 1;
+    {
+        const int64_t distinct = count_communities(membership, n, cmap);
+        stats->communities = distinct;
+    }
+    rc = ORC_OK;
+done:
+    free(vtot);
+    free(ctot);
+    free(vaff);
+    free(cmap);
+    if (accs) {
+        for (int i = 0; i < nacc; ++i) acc_free(&accs[i]);
+        free(accs);
+    }
+    return rc;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Intra-community primitives.                                               */
+/* ------------------------------------------------------------------------ */
+
+/* intraBFSFromHub (RG:3929-3984): FIFO BFS from the first max-degree vertex,
+ * neighbours in row order restricted to the community, unreached vertices
+ * appended in vertex order. */
+static void intra_bfs(const orc_graph *g, const uint32_t *verts, int64_t sz, uint32_t c,
+                      const uint32_t *memb, const uint32_t *deg, const int64_t *v2l,
+                      uint32_t *local_ids, char *visited, uint32_t *queue)
+{
+    if (sz == 0) return;
+    if (sz == 1) { local_ids[verts[0]] = 0; return; }
+    memset(visited, 0, (size_t)sz);
+    uint32_t start = verts[0];
+    uint32_t max_deg = deg[verts[0]];
+    for (int64_t i = 0; i < sz; ++i)
+        if (deg[verts[i]] > max_deg) { max_deg = deg[verts[i]]; start = verts[i]; }
+    uint32_t local_id = 0;
+    int64_t head = 0, tail = 0;
+    queue[tail++] = start;
+    visited[v2l[start]] = 1;
+    while (head < tail) {
+        const uint32_t u = queue[head++];
+        local_ids[u] = local_id++;
+        for (int64_t e = g->row_ptr[u]; e < g->row_ptr[u + 1]; ++e) {
+            const int32_t v = g->col[e];
+            if (memb[v] != c) continue;
+            const int64_t li = v2l[v];
+            if (li != -1 && !visited[li]) {
+                visited[li] = 1;
+                queue[tail++] = (uint32_t)v;
+            }
+        }
+    }
+    for (int64_t i = 0; i < sz; ++i)
+        if (!visited[i]) local_ids[verts[i]] = local_id++;
+}
+
+typedef struct { uint32_t deg, v; } orc_pair;
+
+static int pair_cmp(const void *a, const void *b)
+{
+    const orc_pair *x = (const orc_pair *)a, *y = (const orc_pair *)b;
+    if (x->deg != y->deg) return x->deg < y->deg ? -1 : 1;
+    if (x->v != y->v) return x->v < y->v ? -1 : 1;
+    return 0;
+}
+
+/* intraRCM (RG:4000-4134): min-degree start (ties -> smaller id), up to 3
+ * George-Liu steps for sz > 32, Cuthill-McKee BFS with children sorted by
+ * (degree, id), reversal of the reached part, unreached tail in input order. */
+static void intra_rcm(const orc_graph *g, const uint32_t *verts, int64_t sz, uint32_t c,
+                      const uint32_t *memb, const uint32_t *deg, const int64_t *v2l,
+                      uint32_t *local_ids, char *visited, uint32_t *queue,
+                      uint32_t *level_a, uint32_t *level_b, orc_pair *cand)
+{
+    if (sz == 0) return;
+    if (sz == 1) { local_ids[verts[0]] = 0; return; }
+    uint32_t start = verts[0];
+    uint32_t min_deg = deg[verts[0]];
+    for (int64_t i = 0; i < sz; ++i) {
+        const uint32_t v = verts[i];
+        if (deg[v] < min_deg || (deg[v] == min_deg && v < start)) { min_deg = deg[v]; start = v; }
+    }
+    const int max_gl = sz <= 32 ? 0 : 3;
+    if (max_gl > 0) {
+        uint32_t gl_node = start;
+        int64_t prev_ecc = 0;
+        for (int it = 0; it < max_gl; ++it) {
+            memset(visited, 0, (size_t)sz);
+            uint32_t *cur = level_a, *nxt = level_b;
+            int64_t ncur = 1, nnxt;
+            cur[0] = gl_node;
+            int64_t ecc = 0;
+            /* The George-Liu sweep does not mark its start vertex visited. */
+            for (;;) {
+                nnxt = 0;
+                for (int64_t i = 0; i < ncur; ++i) {
+                    const uint32_t u = cur[i];
+                    for (int64_t e = g->row_ptr[u]; e < g->row_ptr[u + 1]; ++e) {
+                        const int32_t v = g->col[e];
+                        if (memb[v] != c) continue;
+                        const int64_t li = v2l[v];
+                        if (li != -1 && !visited[li]) { visited[li] = 1; nxt[nnxt++] = (uint32_t)v; }
+                    }
+                }
+                if (nnxt == 0) break;
+                ++ecc;
+                uint32_t *t = cur; cur = nxt; nxt = t; ncur = nnxt;
+            }
+            if (ecc <= prev_ecc) break;
+            prev_ecc = ecc;
+            uint32_t best_v = cur[0];
+            uint32_t best_deg = deg[cur[0]];
+            for (int64_t i = 1; i < ncur; ++i)
+                if (deg[cur[i]] < best_deg) { best_deg = deg[cur[i]]; best_v = cur[i]; }
+            gl_node = best_v;
+        }
+        start = gl_node;
+    }
+    memset(visited, 0, (size_t)sz);
+    int64_t head = 0, tail = 0, nord = 0;
+    uint32_t *order = level_a; /* cmOrder */
+    const int64_t sli = v2l[start];
+    if (sli >= 0 && sli < sz) { queue[tail++] = start; visited[sli] = 1; }
+    while (head < tail) {
+        const uint32_t u = queue[head++];
+        order[nord++] = u;
+        int64_t nc = 0;
+        for (int64_t e = g->row_ptr[u]; e < g->row_ptr[u + 1]; ++e) {
+            const int32_t v = g->col[e];
+            if (memb[v] != c) continue;
+            const int64_t li = v2l[v];
+            if (li != -1 && !visited[li]) {
+                visited[li] = 1;
+                cand[nc].deg = deg[v];
+                cand[nc].v = (uint32_t)v;
+                ++nc;
+            }
+        }
+        qsort(cand, (size_t)nc, sizeof(orc_pair), pair_cmp);
+        for (int64_t i = 0; i < nc; ++i) queue[tail++] = cand[i].v;
+    }
+    const int64_t main_size = nord;
+    for (int64_t i = 0; i < sz; ++i)
+        if (!visited[i]) order[nord++] = verts[i];
+    for (int64_t i = 0; i < main_size; ++i) local_ids[order[i]] = (uint32_t)(main_size - 1 - i);
+    for (int64_t i = main_size; i < nord; ++i) local_ids[order[i]] = (uint32_t)i;
+}
+
+/* intraGorderGreedy (RG:4420-4587): relaxed Gorder with a UnitHeap.  The
+ * linked list keeps buckets contiguous in descending key order; each bucket
+ * is LIFO (insert at front), extract-max takes the front of the highest
+ * non-empty bucket.  The heap's "top" cursor never reaches the output, so it
+ * is not kept. */
+typedef struct {
+    int *key, *prev, *next;   /* per local vertex */
+    int *bfirst, *bsecond;    /* per bucket */
+    int64_t *ladj_off;        /* local adjacency */
+    int64_t *ladj;
+    uint32_t *placed;
+    int64_t cap_v, cap_e, cap_b;
+} orc_gorder_ws;
+
+static int gorder_ws_reserve(orc_gorder_ws *w, int64_t sz, int64_t ne, int64_t nb)
+{
+    if (sz > w->cap_v) {
+        free(w->key); free(w->prev); free(w->next); free(w->ladj_off); free(w->placed);
+        w->key = (int *)malloc((size_t)sz * sizeof(int));
+        w->prev = (int *)malloc((size_t)sz * sizeof(int));
+        w->next = (int *)malloc((size_t)sz * sizeof(int));
+        w->ladj_off = (int64_t *)malloc(((size_t)sz + 1) * sizeof(int64_t));
+        w->placed = (uint32_t *)malloc((size_t)sz * sizeof(uint32_t));
+        w->cap_v = sz;
+        if (!w->key || !w->prev || !w->next || !w->ladj_off || !w->placed) return ORC_ENOMEM;
+    }
+    if (ne > w->cap_e) {
+        free(w->ladj);
+        w->ladj = (int64_t *)malloc((size_t)(ne > 0 ? ne : 1) * sizeof(int64_t));
+        w->cap_e = ne;
+        if (!w->ladj) return ORC_ENOMEM;
+    }
+    if (nb > w->cap_b) {
+        free(w->bfirst); free(w->bsecond);
+        w->bfirst = (int *)malloc((size_t)nb * sizeof(int));
+        w->bsecond = (int *)malloc((size_t)nb * sizeof(int));
+        w->cap_b = nb;
+        if (!w->bfirst || !w->bsecond) return ORC_ENOMEM;
+    }
+    return ORC_OK;
+}
+
+static void gorder_ws_free(orc_gorder_ws *w)
+{
+    free(w->key); free(w->prev); free(w->next); free(w->ladj_off); free(w->placed);
+    free(w->ladj); free(w->bfirst); free(w->bsecond);
+    memset(w, 0, sizeof(*w));
+}
+
+typedef struct {
+    orc_gorder_ws *w;
+    int max_key;
+} orc_unitheap;
+
+static void uh_unlink(orc_unitheap *h, int idx)
+{
+    orc_gorder_ws *w = h->w;
+    const int p = w->prev[idx], nx = w->next[idx];
+    if (p >= 0) w->next[p] = nx;
+    if (nx >= 0) w->prev[nx] = p;
+    const int k = w->key[idx];
+    if (w->bfirst[k] == idx && w->bsecond[k] == idx) {
+        w->bfirst[k] = w->bsecond[k] = -1;
+    } else if (w->bfirst[k] == idx) {
+        w->bfirst[k] = nx;
+    } else if (w->bsecond[k] == idx) {
+        w->bsecond[k] = p;
+    }
+}
+
+static void uh_link_front(orc_unitheap *h, int idx, int k)
+{
+    orc_gorder_ws *w = h->w;
+    w->key[idx] = k;
+    if (w->bfirst[k] < 0) {
+        int after = -1;
+        for (int bk = k - 1; bk >= 0; --bk)
+            if (w->bfirst[bk] >= 0) { after = w->bfirst[bk]; break; }
+        int before = -1;
+        for (int bk = k + 1; bk <= h->max_key; ++bk)
+            if (w->bsecond[bk] >= 0) { before = w->bsecond[bk]; break; }
+        w->prev[idx] = before;
+        w->next[idx] = after;
+        if (before >= 0) w->next[before] = idx;
+        if (after >= 0) w->prev[after] = idx;
+        w->bfirst[k] = w->bsecond[k] = idx;
+    } else {
+        const int old_first = w->bfirst[k];
+        const int before_old = w->prev[old_first];
+        w->prev[idx] = before_old;
+        w->next[idx] = old_first;
+        w->prev[old_first] = idx;
+        if (before_old >= 0) w->next[before_old] = idx;
+        w->bfirst[k] = idx;
+    }
+    if (k > h->max_key) h->max_key = k;
+}
+
+static void uh_delete(orc_unitheap *h, int idx)
+{
+    orc_gorder_ws *w = h->w;
+    uh_unlink(h, idx);
+    w->prev[idx] = w->next[idx] = -1;
+    w->key[idx] = -1;
+    while (h->max_key > 0 && w->bfirst[h->max_key] < 0) h->max_key--;
+}
+
+static int uh_extract_max(orc_unitheap *h)
+{
+    orc_gorder_ws *w = h->w;
+    while (h->max_key > 0 && w->bfirst[h->max_key] < 0) h->max_key--;
+    const int idx = w->bfirst[h->max_key];
+    if (idx >= 0) uh_delete(h, idx);
+    return idx;
+}
+
+static int intra_gorder(const orc_graph *g, const uint32_t *verts, int64_t sz, uint32_t c,
+                        const uint32_t *memb, const uint32_t *deg, const int64_t *v2l,
+                        int window, uint32_t *local_ids, orc_gorder_ws *w)
+{
+    if (sz == 0) return ORC_OK;
+    if (sz == 1) { local_ids[verts[0]] = 0; return ORC_OK; }
+    if (sz <= 3) {
+        for (int64_t i = 0; i < sz; ++i) local_ids[verts[i]] = (uint32_t)i;
+        return ORC_OK;
+    }
+    int64_t ne = 0;
+    for (int64_t i = 0; i < sz; ++i) ne += degree_of(g, verts[i]);
+    /* A key never exceeds a vertex's local degree (< sz); 16 mirrors the
+     * reference's initial bucket count. */
+    const int64_t nb = (sz + 1 > 16 ? sz + 1 : 16);
+    if (gorder_ws_reserve(w, sz, ne, nb) != ORC_OK) return ORC_ENOMEM;
+
+    int64_t pos = 0;
+    for (int64_t i = 0; i < sz; ++i) {
+        w->ladj_off[i] = pos;
+        const uint32_t u = verts[i];
+        for (int64_t e = g->row_ptr[u]; e < g->row_ptr[u + 1]; ++e) {
+            const int32_t v = g->col[e];
+            if (memb[v] != c) continue;
+            const int64_t li = v2l[v];
+            if (li != -1 && li < sz) w->ladj[pos++] = li;
+        }
+    }
+    w->ladj_off[sz] = pos;
+
+    for (int64_t i = 0; i < sz; ++i) {
+        w->key[i] = 0;
+        w->prev[i] = (int)i - 1;
+        w->next[i] = (i + 1 < sz) ? (int)(i + 1) : -1;
+    }
+    for (int64_t b = 0; b < nb; ++b) w->bfirst[b] = w->bsecond[b] = -1;
+    w->bfirst[0] = 0;
+    w->bsecond[0] = (int)(sz - 1);
+    orc_unitheap h = {w, 0};
+
+    int64_t seed = 0;
+    uint32_t seed_deg = deg[verts[0]];
+    for (int64_t i = 1; i < sz; ++i)
+        if (deg[verts[i]] > seed_deg) { seed_deg = deg[verts[i]]; seed = i; }
+
+    uh_delete(&h, (int)seed);
+    int64_t nplaced = 0;
+    w->placed[nplaced++] = (uint32_t)seed;
+    local_ids[verts[seed]] = 0;
+    for (int64_t k = w->ladj_off[seed]; k < w->ladj_off[seed + 1]; ++k) {
+        const int64_t nb_i = w->ladj[k];
+        if (w->key[nb_i] >= 0) {
+            const int old = w->key[nb_i];
+            uh_unlink(&h, (int)nb_i);
+            uh_link_front(&h, (int)nb_i, old + 1);
+        }
+    }
+    for (uint32_t local_id = 1; local_id < (uint32_t)sz; ++local_id) {
+        const int best = uh_extract_max(&h);
+        if (best < 0) {
+            for (int64_t i = 0; i < sz && local_id < (uint32_t)sz; ++i) {
+                if (w->key[i] >= 0) {
+                    uh_delete(&h, (int)i);
+                    local_ids[verts[i]] = local_id++;
+                }
+            }
+            break;
+        }
+        w->placed[nplaced++] = (uint32_t)best;
+        local_ids[verts[best]] = local_id;
+        for (int64_t k = w->ladj_off[best]; k < w->ladj_off[best + 1]; ++k) {
+            const int64_t nb_i = w->ladj[k];
+            if (w->key[nb_i] >= 0) {
+                const int old = w->key[nb_i];
+                uh_unlink(&h, (int)nb_i);
+                uh_link_front(&h, (int)nb_i, old + 1);
+            }
+        }
+        if (nplaced > window) {
+            const uint32_t old_v = w->placed[nplaced - 1 - window];
+            for (int64_t k = w->ladj_off[old_v]; k < w->ladj_off[old_v + 1]; ++k) {
+                const int64_t nb_i = w->ladj[k];
+                if (w->key[nb_i] >= 0) {
+                    const int old = w->key[nb_i];
+                    if (old <= 0) continue;
+                    uh_unlink(&h, (int)nb_i);
+                    uh_link_front(&h, (int)nb_i, old - 1);
+                }
+            }
+        }
+    }
+    return ORC_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* orderCompose (RG:6286-7087), super-graph order "none".                    */
+/* ------------------------------------------------------------------------ */
+typedef struct { int64_t key; uint32_t c; } orc_sortrec;
+
+static int sortrec_cmp(const void *a, const void *b)
+{
+    /* Ascending key; equal keys keep community-id order, which is what the
+     * reference's std::stable_sort over iota(0..C) yields. */
+    const orc_sortrec *x = (const orc_sortrec *)a, *y = (const orc_sortrec *)b;
+    if (x->key != y->key) return x->key < y->key ? -1 : 1;
+    return x->c < y->c ? -1 : (x->c > y->c);
+}
+
+int orc_compose(const orc_graph *g, const uint32_t *membership,
+                const orc_compose_cfg *cfg, int32_t *new_ids,
+                orc_compose_stats *stats)
+{
+    if (!g || !membership || !cfg || !new_ids) return ORC_EINVAL;
+    orc_compose_stats local_stats;
+    if (!stats) stats = &local_stats;
+    memset(stats, 0, sizeof(*stats));
+    const int64_t n = g->n;
+    if (n == 0) return ORC_OK;
+    if (cfg->intra_order == ORC_INTRA_GORDER && cfg->gorder_window <= 0) return ORC_EINVAL;
+    if (cfg->intra_order != ORC_INTRA_BFS && cfg->intra_order != ORC_INTRA_RCM &&
+        cfg->intra_order != ORC_INTRA_GORDER)
+        return ORC_EUNSUPPORTED;
+
+    int rc = ORC_ENOMEM;
+    uint32_t num_comm = 0;
+    for (int64_t v = 0; v < n; ++v)
+        if (membership[v] + 1 > num_comm) num_comm = membership[v] + 1;
+    stats->num_communities = num_comm;
+
+    uint32_t *deg = (uint32_t *)malloc((size_t)n * sizeof(uint32_t));
+    int64_t *csize = (int64_t *)calloc((size_t)num_comm + 1, sizeof(int64_t));
+    int64_t *cstart = (int64_t *)calloc((size_t)num_comm + 1, sizeof(int64_t));
+    uint32_t *cverts = (uint32_t *)malloc((size_t)n * sizeof(uint32_t));
+    orc_sortrec *recs = (orc_sortrec *)malloc((size_t)num_comm * sizeof(orc_sortrec));
+    int64_t *offsets = (int64_t *)calloc((size_t)num_comm + 1, sizeof(int64_t));
+    int64_t *v2l = (int64_t *)malloc((size_t)n * sizeof(int64_t));
+    uint32_t *local_ids = (uint32_t *)calloc((size_t)n, sizeof(uint32_t));
+    if (!deg || !csize || !cstart || !cverts || !recs || !offsets || !v2l || !local_ids)
+        goto done;
+    for (int64_t v = 0; v < n; ++v) deg[v] = (uint32_t)degree_of(g, v);
+
+    /* Grouping: non-isolated vertices per community in vertex order. */
+    int64_t isolated = 0;
+    for (int64_t v = 0; v < n; ++v) {
+        if (deg[v] == 0) ++isolated;
+        else csize[membership[v]]++;
+    }
+    stats->isolated = isolated;
+    for (uint32_t c = 0; c < num_comm; ++c) cstart[c + 1] = cstart[c] + csize[c];
+    {
+        int64_t *cur = (int64_t *)malloc(((size_t)num_comm + 1) * sizeof(int64_t));
+        if (!cur) goto done;
+        memcpy(cur, cstart, ((size_t)num_comm + 1) * sizeof(int64_t));
+        for (int64_t v = 0; v < n; ++v)
+            if (deg[v] != 0) cverts[cur[membership[v]]++] = (uint32_t)v;
+        free(cur);
+    }
+
+    /* Community order: stable sort of 0..C-1 (RG:6438-6502). */
+    for (uint32_t c = 0; c < num_comm; ++c) {
+        int64_t key = 0;
+        int64_t tdeg = 0;
+        if (cfg->community_order == ORC_COMM_DEGREE_DESC || cfg->community_order == ORC_COMM_DEGREE_ASC)
+            for (int64_t i = cstart[c]; i < cstart[c + 1]; ++i) tdeg += deg[cverts[i]];
+        switch (cfg->community_order) {
+        case ORC_COMM_SIZE_DESC: key = -csize[c]; break;
+        case ORC_COMM_SIZE_ASC: key = csize[c]; break;
+        case ORC_COMM_DEGREE_DESC: key = -tdeg; break;
+        case ORC_COMM_DEGREE_ASC: key = tdeg; break;
+        case ORC_COMM_IDENTITY: key = 0; break;
+        default: rc = ORC_EUNSUPPORTED; goto done;
+        }
+        recs[c].key = key;
+        recs[c].c = c;
+    }
+    qsort(recs, num_comm, sizeof(orc_sortrec), sortrec_cmp);
+    for (uint32_t i = 0; i < num_comm; ++i) offsets[i + 1] = offsets[i] + csize[recs[i].c];
+
+    for (int64_t v = 0; v < n; ++v) v2l[v] = -1;
+    for (uint32_t c = 0; c < num_comm; ++c)
+        for (int64_t i = cstart[c]; i < cstart[c + 1]; ++i) v2l[cverts[i]] = i - cstart[c];
+
+    if (cfg->intra_order == ORC_INTRA_GORDER) {
+        for (uint32_t i = 0; i < num_comm; ++i) {
+            const int64_t sz = csize[recs[i].c];
+            if (cfg->gorder_fallback > 0 && sz > cfg->gorder_fallback) {
+                stats->fallback_communities++;
+                stats->fallback_vertices += sz;
+                continue;
+            }
+            if (sz <= 3) continue;
+            stats->gorder_communities++;
+            stats->gorder_vertices += sz;
+            if (sz > stats->gorder_max_community) stats->gorder_max_community = sz;
+        }
+    }
+    for (uint32_t c = 0; c < num_comm; ++c)
+        if (csize[c] > stats->largest_community) stats->largest_community = csize[c];
+
+    /* Per-community intra order, one community per task as in the reference
+     * (RG:6680-6962, schedule(dynamic, 1)); every task writes only its own
+     * vertices' local ids. */
+    {
+        int failed = 0;
+        const int64_t max_sz = stats->largest_community > 0 ? stats->largest_community : 1;
+#ifdef _OPENMP
+#pragma omp parallel if (cfg->threads != 1)
+#endif
+        {
+            char *t_visited = (char *)malloc((size_t)max_sz);
+            uint32_t *t_queue = (uint32_t *)malloc((size_t)max_sz * sizeof(uint32_t));
+            uint32_t *t_la = (uint32_t *)malloc((size_t)max_sz * sizeof(uint32_t));
+            uint32_t *t_lb = (uint32_t *)malloc((size_t)max_sz * sizeof(uint32_t));
+            orc_pair *t_cand = (orc_pair *)malloc((size_t)max_sz * sizeof(orc_pair));
+            orc_gorder_ws t_ws;
+            memset(&t_ws, 0, sizeof(t_ws));
+            const int ok = t_visited && t_queue && t_la && t_lb && t_cand;
+            if (!ok) {
+#ifdef _OPENMP
+#pragma omp atomic write
+#endif
+                failed = 1;
+            }
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 1)
+#endif
+            for (int64_t i = 0; i < (int64_t)num_comm; ++i) {
+                if (!ok) continue;
+                const uint32_t c = recs[i].c;
+                const uint32_t *verts = cverts + cstart[c];
+                const int64_t sz = csize[c];
+                if (cfg->intra_order == ORC_INTRA_RCM) {
+                    intra_rcm(g, verts, sz, c, membership, deg, v2l, local_ids, t_visited,
+                              t_queue, t_la, t_lb, t_cand);
+                } else if (cfg->intra_order == ORC_INTRA_GORDER &&
+                           !(cfg->gorder_fallback > 0 && sz > cfg->gorder_fallback)) {
+                    if (intra_gorder(g, verts, sz, c, membership, deg, v2l, cfg->gorder_window,
+                                     local_ids, &t_ws) != ORC_OK) {
+#ifdef _OPENMP
+#pragma omp atomic write
+#endif
+                        failed = 1;
+                    }
+                } else {
+                    intra_bfs(g, verts, sz, c, membership, deg, v2l, local_ids, t_visited,
+                              t_queue);
+                }
+            }
+            free(t_visited); free(t_queue); free(t_la); free(t_lb); free(t_cand);
+            gorder_ws_free(&t_ws);
+        }
+        if (failed) goto done;
+    }
+
+    /* Final assign (RG:7003-7017). */
+    for (uint32_t i = 0; i < num_comm; ++i) {
+        const uint32_t c = recs[i].c;
+        for (int64_t k = cstart[c]; k < cstart[c + 1]; ++k) {
+            const uint32_t v = cverts[k];
+            new_ids[v] = (int32_t)(offsets[i] + local_ids[v]);
+        }
+    }
+    {
+        int64_t tail = offsets[num_comm];
+        for (int64_t v = 0; v < n; ++v)
+            if (deg[v] == 0) new_ids[v] = (int32_t)(tail++);
+    }
+    rc = ORC_OK;
+done:
+    free(deg); free(csize); free(cstart); free(cverts); free(recs); free(offsets);
+    free(v2l); free(local_ids);
+    return rc;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Validation, fingerprint, relabel, modularity.                            */
+/* ------------------------------------------------------------------------ */
+int orc_validate_permutation(const int32_t *ids, int64_t n)
+{
+    if (n == 0) return 0;
+    unsigned char *seen = (unsigned char *)calloc((size_t)n, 1);
+    if (!seen) return ORC_ENOMEM;
+    int rc = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        const int64_t v = ids[i];
+        if (v < 0 || v >= n) { rc = 1; break; }
+        if (seen[v]) { rc = 2; break; }
+        seen[v] = 1;
+    }
+    free(seen);
+    return rc;
+}
+
+uint64_t orc_fingerprint(const int32_t *ids, int64_t n)
+{
+    uint64_t h = UINT64_C(1469598103934665603);
+    for (int64_t i = 0; i < n; ++i) {
+        h ^= (uint64_t)i;
+        h *= UINT64_C(1099511628211);
+        h ^= (uint64_t)(int64_t)ids[i];
+        h *= UINT64_C(1099511628211);
+    }
+    return h;
+}
+
+/* Ascending in-place sort of a row: insertion sort for short runs,
+ * median-of-three quicksort (recursing into the smaller side) above that. */
+static void sort_i32(int32_t *a, int64_t n)
+{
+    while (n > 24) {
+        int32_t x = a[0], y = a[n / 2], z = a[n - 1];
+        int32_t p = x < y ? (y < z ? y : (x < z ? z : x)) : (x < z ? x : (y < z ? z : y));
+        int64_t i = 0, j = n - 1;
+        for (;;) {
+            while (a[i] < p) ++i;
+            while (a[j] > p) --j;
+            if (i >= j) break;
+            int32_t t = a[i]; a[i] = a[j]; a[j] = t;
+            ++i; --j;
+        }
+        /* [0, j] <= p <= [j + 1, n) */
+        if (j + 1 < n - j - 1) { sort_i32(a, j + 1); a += j + 1; n -= j + 1; }
+        else { sort_i32(a + j + 1, n - j - 1); n = j + 1; }
+    }
+    for (int64_t i = 1; i < n; ++i) {
+        int32_t v = a[i];
+        int64_t k = i - 1;
+        while (k >= 0 && a[k] > v) { a[k + 1] = a[k]; --k; }
+        a[k + 1] = v;
+    }
+}
+
+int orc_relabel(const orc_graph *g, const int32_t *new_ids,
+                int64_t *out_row_ptr, int32_t *out_col, int threads)
+{
+    const int64_t n = g->n;
+    (void)threads;
+    out_row_ptr[0] = 0;
+    if (n == 0) return ORC_OK;
+    int64_t *deg = (int64_t *)malloc((size_t)n * sizeof(int64_t));
+    if (!deg) return ORC_ENOMEM;
+    for (int64_t v = 0; v < n; ++v) deg[new_ids[v]] = degree_of(g, v);
+    for (int64_t v = 0; v < n; ++v) out_row_ptr[v + 1] = out_row_ptr[v] + deg[v];
+    free(deg);
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel for schedule(dynamic, 1024)
+#endif
+    for (int64_t u = 0; u < n; ++u) {
+        const int64_t base = out_row_ptr[new_ids[u]];
+        int64_t k = 0;
+        for (int64_t e = g->row_ptr[u]; e < g->row_ptr[u + 1]; ++e) out_col[base + k++] = new_ids[g->col[e]];
+        sort_i32(out_col + base, k);
+    }
+    return ORC_OK;
+}
+
+double orc_modularity(const orc_graph *g, const uint32_t *membership, double resolution)
+{
+    const int64_t n = g->n;
+    if (n == 0) return 0.0;
+    const double M = (double)((g->row_ptr[n] - g->row_ptr[0]) / 2);
+    if (M == 0) return 0.0;
+    double Q = 0.0;
+    for (int64_t u = 0; u < n; ++u) {
+        const uint32_t cu = membership[u];
+        const double du = (double)degree_of(g, u);
+        for (int64_t e = g->row_ptr[u]; e < g->row_ptr[u + 1]; ++e) {
+            const int32_t v = g->col[e];
+            if (membership[v] == cu)
+                Q += 1.0 - resolution * du * (double)degree_of(g, v) / (2.0 * M);
+        }
+    }
+    return Q / (2.0 * M);
+}

@@ -1,0 +1,135 @@
+/*
+ * gb_oracle.h -- CPU oracle for the algorithm-12 mapping path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of GraphBrew's
+ * algorithm-12 pipeline (GVE-style Leiden -> COMPOSE placement -> per-community
+ * Gorder / BFS / RCM -> relabel).  It exists to check the CUDA implementation
+ * and to serve as the timed CPU baseline.  Only tests, the smoke check and the
+ * benchmark's CPU-baseline leg may load it; the product library never links it.
+ *
+ * Each function cites the reference code it follows (paths relative to the
+ * GraphBrew project root).
+ */
+#ifndef GB_ORACLE_H_
+#define GB_ORACLE_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    ORC_OK = 0,
+    ORC_EINVAL = -1,
+    ORC_ENOMEM = -2,
+    ORC_EUNSUPPORTED = -3
+};
+
+/* Undirected CSR: rows hold every neighbour once per direction. */
+typedef struct {
+    int64_t n;
+    const int64_t *row_ptr; /* n + 1 entries */
+    const int32_t *col;     /* row_ptr[n] entries */
+} orc_graph;
+
+/* computeAutoResolution (bench/include/graphbrew/reorder/reorder_types.h:2743-2780),
+ * with the degree variance summed serially in vertex order. */
+double orc_auto_resolution(const orc_graph *g);
+
+typedef struct {
+    double resolution;
+    double tolerance;             /* DEFAULT_TOLERANCE 1e-2 */
+    double aggregation_tolerance; /* DEFAULT_AGGREGATION_TOLERANCE 0.8 */
+    double tolerance_drop;        /* DEFAULT_TOLERANCE_DROP 10 */
+    int max_iterations;
+    int max_passes;
+    int total_edges_m;            /* 1: M = max(1, m) (totalm); 0: M = m / 2 */
+    int super_move_batch;         /* sgmb<k>; 1 = sequential super-move */
+    int parallel;                 /* 0: cd_serial semantics; 1: racy OpenMP (cd_parallel) */
+    int threads;                  /* OpenMP threads for parallel=1 (0 = runtime default) */
+} orc_leiden_cfg;
+
+typedef struct {
+    int passes;                   /* GraphBrewResult::totalPasses */
+    int iterations;               /* local-moving iterations, all passes */
+    int pass_iterations[16];      /* per pass */
+    int64_t pass0_communities;    /* communities after pass-0 local moving */
+    int64_t aggregated_communities; /* after the GVE super-move merge (0 if none) */
+    int super_move_iterations;
+    int64_t super_moves;
+    int64_t communities;          /* distinct ids in the final membership */
+    double local_move_seconds, aggregate_seconds;
+} orc_leiden_stats;
+
+/* runGraphBrew in GVE_CSR mode without refinement
+ * (bench/include/graphbrew/reorder/reorder_graphbrew.h:7238-7571), with
+ * localMovingPhase<false> (:1588-1734), countCommunities/renumberCommunities
+ * (:1843-1889), buildCommunityVertices (:1912-1942), aggregateGVEStyle
+ * (:2156-2439).  membership: n entries. */
+int orc_leiden(const orc_graph *g, const orc_leiden_cfg *cfg,
+               uint32_t *membership, orc_leiden_stats *stats);
+
+/* Community-order axis (CommunityOrder, reorder_graphbrew.h:286-297). */
+enum {
+    ORC_COMM_SIZE_DESC = 0,
+    ORC_COMM_SIZE_ASC = 1,
+    ORC_COMM_DEGREE_DESC = 2,
+    ORC_COMM_DEGREE_ASC = 3,
+    ORC_COMM_IDENTITY = 6
+};
+/* Intra-community axis (IntraCommunityOrder, reorder_graphbrew.h:302-378).
+ * Only the primitives whose order is fully specified are restated; HubSort
+ * and DegreeAsc use an unstable std::sort whose tie order is not. */
+enum {
+    ORC_INTRA_BFS = 0,
+    ORC_INTRA_RCM = 1,
+    ORC_INTRA_GORDER = 4
+};
+
+typedef struct {
+    int community_order;
+    int intra_order;
+    int gorder_window;    /* gw<k> */
+    int gorder_fallback;  /* gordf<k>; 0 = no fallback */
+    int threads;          /* 1 = serial; otherwise the OpenMP default */
+} orc_compose_cfg;
+
+typedef struct {
+    int64_t num_communities;   /* max(membership) + 1 */
+    int64_t isolated;
+    int64_t gorder_communities, gorder_vertices, gorder_max_community;
+    int64_t fallback_communities, fallback_vertices;
+    int64_t largest_community;
+} orc_compose_stats;
+
+/* orderCompose (reorder_graphbrew.h:6286-7087) for super-graph order "none".
+ * new_ids: n entries, forward map old -> new. */
+int orc_compose(const orc_graph *g, const uint32_t *membership,
+                const orc_compose_cfg *cfg, int32_t *new_ids,
+                orc_compose_stats *stats);
+
+/* ValidatePermutationOrThrow (bench/include/external/gapbs/builder.h:2056-2080):
+ * 0 = valid, 1 = out-of-range id, 2 = duplicate id. */
+int orc_validate_permutation(const int32_t *new_ids, int64_t n);
+
+/* MappingFingerprint (builder.h:1398-1411): FNV-1a-64 over (old, new) pairs. */
+uint64_t orc_fingerprint(const int32_t *new_ids, int64_t n);
+
+/* RelabelByMapping, undirected branch (builder.h:1046-1206, :1168-1201):
+ * out_row_ptr n + 1 entries, out_col row_ptr[n] entries, rows sorted. */
+int orc_relabel(const orc_graph *g, const int32_t *new_ids,
+                int64_t *out_row_ptr, int32_t *out_col, int threads);
+
+/* computeModularityCSR (reorder_types.h:3211-3291), summed in vertex order. */
+double orc_modularity(const orc_graph *g, const uint32_t *membership,
+                      double resolution);
+
+/* Number of OpenMP threads the library was built to use (1 without OpenMP). */
+int orc_max_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GB_ORACLE_H_ */

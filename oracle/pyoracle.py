@@ -1,0 +1,279 @@
+"""ctypes bindings for the CPU oracle (and, where it was built, the reference harness).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, ``__graft_entry__.smoke()`` and
+the CPU-baseline leg of ``bench.py``.  The product package never imports it.
+
+``load()`` returns the plain-C oracle (``_build/libgborc.so``, built by
+``make`` in this directory).  ``load_reference()`` returns the harness over the
+GraphBrew reference headers (``_ref/libgbref.so``) or ``None`` where it was not
+built (it needs the reference sources, which only the development container
+has).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "libgborc.so")
+REF_SO = os.path.join(HERE, "_ref", "libgbref.so")
+
+_i64p = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
+_i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_u32p = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
+
+# Algorithm-12 defaults (reorder_types.h:213-226) for the GVE-style path.
+DEFAULT_TOLERANCE = 1e-2
+DEFAULT_AGGREGATION_TOLERANCE = 0.8
+DEFAULT_TOLERANCE_DROP = 10.0
+
+COMM_ORDERS = {"size-desc": 0, "size-asc": 1, "degree-desc": 2, "degree-asc": 3, "identity": 6}
+INTRA_ORDERS = {"bfs": 0, "rcm": 1, "gorder": 4}
+
+
+class Graph(C.Structure):
+    _fields_ = [("n", C.c_int64), ("row_ptr", C.c_void_p), ("col", C.c_void_p)]
+
+
+class LeidenCfg(C.Structure):
+    _fields_ = [("resolution", C.c_double), ("tolerance", C.c_double),
+                ("aggregation_tolerance", C.c_double), ("tolerance_drop", C.c_double),
+                ("max_iterations", C.c_int), ("max_passes", C.c_int),
+                ("total_edges_m", C.c_int), ("super_move_batch", C.c_int),
+                ("parallel", C.c_int), ("threads", C.c_int)]
+
+
+class LeidenStats(C.Structure):
+    _fields_ = [("passes", C.c_int), ("iterations", C.c_int),
+                ("pass_iterations", C.c_int * 16), ("pass0_communities", C.c_int64),
+                ("aggregated_communities", C.c_int64), ("super_move_iterations", C.c_int),
+                ("super_moves", C.c_int64), ("communities", C.c_int64),
+                ("local_move_seconds", C.c_double), ("aggregate_seconds", C.c_double)]
+
+
+class ComposeCfg(C.Structure):
+    _fields_ = [("community_order", C.c_int), ("intra_order", C.c_int),
+                ("gorder_window", C.c_int), ("gorder_fallback", C.c_int),
+                ("threads", C.c_int)]
+
+
+class ComposeStats(C.Structure):
+    _fields_ = [("num_communities", C.c_int64), ("isolated", C.c_int64),
+                ("gorder_communities", C.c_int64), ("gorder_vertices", C.c_int64),
+                ("gorder_max_community", C.c_int64), ("fallback_communities", C.c_int64),
+                ("fallback_vertices", C.c_int64), ("largest_community", C.c_int64)]
+
+
+def build() -> str:
+    """Compile the plain-C oracle (seconds)."""
+    subprocess.run(["make", "-s", "-C", HERE, "_build/libgborc.so"], check=True)
+    return ORACLE_SO
+
+
+_lib = None
+_ref = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(ORACLE_SO):
+            build()
+        lib = C.CDLL(ORACLE_SO)
+        lib.orc_auto_resolution.restype = C.c_double
+        lib.orc_auto_resolution.argtypes = [C.POINTER(Graph)]
+        lib.orc_leiden.argtypes = [C.POINTER(Graph), C.POINTER(LeidenCfg), _u32p, C.POINTER(LeidenStats)]
+        lib.orc_compose.argtypes = [C.POINTER(Graph), _u32p, C.POINTER(ComposeCfg), _i32p, C.POINTER(ComposeStats)]
+        lib.orc_validate_permutation.argtypes = [_i32p, C.c_int64]
+        lib.orc_fingerprint.restype = C.c_uint64
+        lib.orc_fingerprint.argtypes = [_i32p, C.c_int64]
+        lib.orc_relabel.argtypes = [C.POINTER(Graph), _i32p, _i64p, _i32p, C.c_int]
+        lib.orc_modularity.restype = C.c_double
+        lib.orc_modularity.argtypes = [C.POINTER(Graph), _u32p, C.c_double]
+        lib.orc_max_threads.restype = C.c_int
+        _lib = lib
+    return _lib
+
+
+def load_reference():
+    """The reference harness, or None where it was not built here."""
+    global _ref
+    if _ref is None and os.path.exists(REF_SO):
+        lib = C.CDLL(REF_SO)
+        lib.ref_auto_resolution.restype = C.c_double
+        lib.ref_auto_resolution.argtypes = [C.c_int64, _i64p, _i32p]
+        lib.ref_effective_config_json.argtypes = [C.c_char_p, C.c_double, C.c_char_p, C.c_size_t]
+        lib.ref_run_graphbrew.argtypes = [C.c_int64, _i64p, _i32p, C.c_char_p, C.c_double, _u32p,
+                                          _i64p, C.c_int, C.c_char_p, C.c_size_t]
+        lib.ref_order_compose.argtypes = [C.c_int64, _i64p, _i32p, _u32p, C.c_char_p, C.c_double,
+                                          _i32p, _i64p, C.c_int, C.c_char_p, C.c_size_t]
+        lib.ref_generate_mapping.argtypes = [C.c_int64, _i64p, _i32p, C.c_char_p, C.c_double, _i32p,
+                                             C.c_int, C.c_char_p, C.c_size_t]
+        lib.ref_relabel.argtypes = [C.c_int64, _i64p, _i32p, _i32p, _i64p, _i32p, _i32p, C.c_int]
+        lib.ref_modularity.restype = C.c_double
+        lib.ref_modularity.argtypes = [C.c_int64, _i64p, _i32p, _u32p, C.c_double]
+        lib.ref_gorder_kat.argtypes = [C.c_int64, _i64p, _i32p, C.c_int, _i32p]
+        lib.ref_gapbs_generate.restype = C.c_int64
+        lib.ref_gapbs_generate.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int64), C.c_int]
+        lib.ref_last_graph_copy.argtypes = [_i64p, _i32p]
+        lib.ref_set_threads.argtypes = [C.c_int]
+        _ref = lib
+    return _ref
+
+
+def _as_graph(row_ptr, col):
+    row_ptr = np.ascontiguousarray(row_ptr, dtype=np.int64)
+    col = np.ascontiguousarray(col, dtype=np.int32)
+    g = Graph(len(row_ptr) - 1, row_ptr.ctypes.data, col.ctypes.data)
+    return g, (row_ptr, col)
+
+
+# --------------------------------------------------------------------------
+# Oracle API
+# --------------------------------------------------------------------------
+
+def auto_resolution(row_ptr, col) -> float:
+    g, keep = _as_graph(row_ptr, col)
+    return load().orc_auto_resolution(C.byref(g))
+
+
+def leiden(row_ptr, col, resolution, max_iterations=2, max_passes=2, super_move_batch=4096,
+           parallel=False, threads=0, total_edges_m=True):
+    g, keep = _as_graph(row_ptr, col)
+    cfg = LeidenCfg(resolution, DEFAULT_TOLERANCE, DEFAULT_AGGREGATION_TOLERANCE,
+                    DEFAULT_TOLERANCE_DROP, max_iterations, max_passes, int(total_edges_m),
+                    super_move_batch, int(parallel), threads)
+    memb = np.zeros(g.n, dtype=np.uint32)
+    st = LeidenStats()
+    rc = load().orc_leiden(C.byref(g), C.byref(cfg), memb, C.byref(st))
+    if rc != 0:
+        raise RuntimeError(f"orc_leiden failed: {rc}")
+    return memb, st
+
+
+def compose(row_ptr, col, membership, community_order="size-desc", intra_order="gorder",
+            gorder_window=8, gorder_fallback=5000, threads=0):
+    g, keep = _as_graph(row_ptr, col)
+    cfg = ComposeCfg(COMM_ORDERS[community_order], INTRA_ORDERS[intra_order], gorder_window,
+                     gorder_fallback, threads)
+    memb = np.ascontiguousarray(membership, dtype=np.uint32)
+    out = np.zeros(g.n, dtype=np.int32)
+    st = ComposeStats()
+    rc = load().orc_compose(C.byref(g), memb, C.byref(cfg), out, C.byref(st))
+    if rc != 0:
+        raise RuntimeError(f"orc_compose failed: {rc}")
+    return out, st
+
+
+def validate_permutation(new_ids) -> int:
+    ids = np.ascontiguousarray(new_ids, dtype=np.int32)
+    return load().orc_validate_permutation(ids, len(ids))
+
+
+def fingerprint(new_ids) -> str:
+    ids = np.ascontiguousarray(new_ids, dtype=np.int32)
+    return "%016x" % load().orc_fingerprint(ids, len(ids))
+
+
+def relabel(row_ptr, col, new_ids, threads=0):
+    g, keep = _as_graph(row_ptr, col)
+    ids = np.ascontiguousarray(new_ids, dtype=np.int32)
+    out_rp = np.zeros(g.n + 1, dtype=np.int64)
+    out_col = np.zeros(len(keep[1]), dtype=np.int32)
+    rc = load().orc_relabel(C.byref(g), ids, out_rp, out_col, threads)
+    if rc != 0:
+        raise RuntimeError(f"orc_relabel failed: {rc}")
+    return out_rp, out_col
+
+
+def modularity(row_ptr, col, membership, resolution=1.0) -> float:
+    g, keep = _as_graph(row_ptr, col)
+    return load().orc_modularity(C.byref(g), np.ascontiguousarray(membership, dtype=np.uint32),
+                                 resolution)
+
+
+def map_graph(row_ptr, col, resolution, parallel=False, threads=0, max_iterations=2,
+              max_passes=2, super_move_batch=4096, gorder_window=8, gorder_fallback=5000,
+              intra_order="gorder", community_order="size-desc"):
+    """The whole FastLeiden-Gorder8 recipe: Leiden, then COMPOSE."""
+    memb, lst = leiden(row_ptr, col, resolution, max_iterations, max_passes, super_move_batch,
+                       parallel, threads)
+    ids, cst = compose(row_ptr, col, memb, community_order, intra_order, gorder_window,
+                       gorder_fallback, 0 if parallel else 1)
+    return ids, memb, lst, cst
+
+
+# --------------------------------------------------------------------------
+# Reference harness API (development container only)
+# --------------------------------------------------------------------------
+
+def ref_effective_config(opts: str, auto_res: float):
+    buf = C.create_string_buffer(8192)
+    rc = load_reference().ref_effective_config_json(opts.encode(), auto_res, buf, len(buf))
+    return rc, buf.value.decode()
+
+
+def ref_leiden(row_ptr, col, opts, auto_res, threads=1):
+    ref = load_reference()
+    ref.ref_set_threads(threads)
+    rp = np.ascontiguousarray(row_ptr, dtype=np.int64)
+    cl = np.ascontiguousarray(col, dtype=np.int32)
+    memb = np.zeros(len(rp) - 1, dtype=np.uint32)
+    summ = np.zeros(3, dtype=np.int64)
+    err = C.create_string_buffer(1024)
+    rc = ref.ref_run_graphbrew(len(rp) - 1, rp, cl, opts.encode(), auto_res, memb, summ, 1, err, 1024)
+    if rc != 0:
+        raise RuntimeError(err.value.decode())
+    return memb, summ
+
+
+def ref_compose(row_ptr, col, membership, opts, auto_res, threads=1):
+    ref = load_reference()
+    ref.ref_set_threads(threads)
+    rp = np.ascontiguousarray(row_ptr, dtype=np.int64)
+    cl = np.ascontiguousarray(col, dtype=np.int32)
+    ids = np.zeros(len(rp) - 1, dtype=np.int32)
+    st = np.zeros(5, dtype=np.int64)
+    err = C.create_string_buffer(1024)
+    rc = ref.ref_order_compose(len(rp) - 1, rp, cl, np.ascontiguousarray(membership, dtype=np.uint32),
+                               opts.encode(), auto_res, ids, st, 1, err, 1024)
+    if rc != 0:
+        raise RuntimeError(err.value.decode())
+    return ids, st
+
+
+def ref_generate_mapping(row_ptr, col, opts, auto_res, threads=1):
+    ref = load_reference()
+    ref.ref_set_threads(threads)
+    rp = np.ascontiguousarray(row_ptr, dtype=np.int64)
+    cl = np.ascontiguousarray(col, dtype=np.int32)
+    ids = np.zeros(len(rp) - 1, dtype=np.int32)
+    err = C.create_string_buffer(1024)
+    rc = ref.ref_generate_mapping(len(rp) - 1, rp, cl, opts.encode(), auto_res, ids, 1, err, 1024)
+    if rc != 0:
+        raise RuntimeError(err.value.decode())
+    return ids
+
+
+def ref_relabel(row_ptr, col, new_ids):
+    ref = load_reference()
+    rp = np.ascontiguousarray(row_ptr, dtype=np.int64)
+    cl = np.ascontiguousarray(col, dtype=np.int32)
+    out_rp = np.zeros(len(rp), dtype=np.int64)
+    out_col = np.zeros(len(cl), dtype=np.int32)
+    org = np.zeros(len(rp) - 1, dtype=np.int32)
+    ref.ref_relabel(len(rp) - 1, rp, cl, np.ascontiguousarray(new_ids, dtype=np.int32), out_rp, out_col, org, 1)
+    return out_rp, out_col, org
+
+
+def ref_gapbs_graph(scale, degree=16, uniform=False):
+    ref = load_reference()
+    nnz = C.c_int64(0)
+    n = ref.ref_gapbs_generate(scale, degree, int(uniform), C.byref(nnz), 1)
+    rp = np.zeros(n + 1, dtype=np.int64)
+    cl = np.zeros(nnz.value, dtype=np.int32)
+    ref.ref_last_graph_copy(rp, cl)
+    return rp, cl
