@@ -1,0 +1,345 @@
+"""Benchmark: algorithm-12 mapping construction (FastLeiden-Gorder8) on one GB300.
+
+Workload: RMAT scale 22, edge factor 16 (a/b/c = 0.57/0.19/0.19), seeded,
+symmetrized int32 CSR (4.19M vertices, ~128M directed entries) and the recipe
+``-o 12:leiden:compose:sg_none:comm_size_desc:intra_gorder:gw8:cd_parallel:
+sgmb4096:gordf5000:norefine:2:2``.  One step = the builder's mapping
+lifecycle: GraphBrew core (Leiden + COMPOSE) + permutation validation + CSR
+relabel ("Reorder End-to-End Time", builder.h:881-892).
+
+metric  Medges/s = directed CSR entries / end-to-end mapping seconds.
+value   device-resident graph, CUDA events on the library's stream.
+e2e     same metric through the public C ABI with host (pinned) buffers:
+        the CSR copied in and the permutation plus relabelled CSR copied out
+        inside every step.
+
+``--impl reference`` times the CPU restatement of the reference's path (the
+oracle, OpenMP on every host core) on the same workload; the reference's own
+sources are not present on the GPU host, so it cannot be compiled there.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+RECIPE = ("leiden:compose:sg_none:comm_size_desc:intra_gorder:gw8:cd_parallel:"
+          "sgmb4096:gordf5000:norefine:2:2")
+METRIC = "GPU reorder Medges/s vs host CPU; map+kernel time, learned vs frozen rule"
+SCALE = 22
+EDGE_FACTOR = 16
+SEED = 27491095
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--scale", type=int, default=SCALE)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def host_cores():
+    return os.cpu_count() or 1
+
+
+# ---------------------------------------------------------------------------
+# CPU legs (oracle restatement of the reference path)
+# ---------------------------------------------------------------------------
+def cpu_mapping_seconds(rp, col, threads):
+    """One end-to-end mapping on the host cores: Leiden (cd_parallel, OpenMP),
+    COMPOSE, validation, relabel.  Returns (seconds, new_ids)."""
+    import pyoracle as po
+    ar = po.auto_resolution(rp, col)
+    t0 = time.perf_counter()
+    ids, _, _, _ = po.map_graph(rp, col, ar, parallel=True, threads=threads)
+    rc = po.validate_permutation(ids)
+    po.relabel(rp, col, ids, threads=threads)
+    t1 = time.perf_counter()
+    assert rc == 0
+    return t1 - t0, ids
+
+
+def run_reference_arm(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    from graphbrew_gb300 import graphgen as gg
+    po.build()
+    threads = host_cores()
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    # Bound the run: full scale while the step count is small, else a scale-20 sample.
+    scale = args.scale if (args.steps + args.warmup) <= 12 else min(args.scale, 20)
+    rp_t, col_t = gg.rmat(scale, EDGE_FACTOR, seed=SEED)
+    rp, col = rp_t.numpy(), col_t.numpy()
+    nnz = len(col)
+    for _ in range(args.warmup):
+        cpu_mapping_seconds(rp, col, threads)
+    times = [cpu_mapping_seconds(rp, col, threads)[0] for _ in range(args.steps)]
+    total = sum(times)
+    value = nnz * len(times) / total / 1e6
+    sample = f"RMAT scale {scale} ef {EDGE_FACTOR}, {nnz} directed entries, full mapping+validation+relabel per step"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Medges/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total / len(times) * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded RMAT)",
+        "config": {"workload": f"rmat{scale}_ef{EDGE_FACTOR}_fastleiden_gorder8", "recipe": "12:" + RECIPE,
+                   "scale": scale, "edge_factor": EDGE_FACTOR, "directed_entries": nnz},
+        "cpu_baseline": {"value": value, "unit": "Medges/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "Medges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def relabel_bytes(n, nnz):
+    # read col + gather new_ids + write out_col (4 B each per entry),
+    # inverse map and row offsets (per vertex: read old offsets 16 B,
+    # inverse 4 B, write new offsets 8 B, scan read+write 16 B).
+    return 12 * nnz + 44 * n
+
+
+def local_move_bytes(n, nnz):
+    # per iteration: row offsets 16 B + vaff 1 B + vcom 4 B + ctot 8 B per vertex;
+    # col 4 B + neighbour community 4 B + community total 8 B per entry.
+    return 16 * nnz + 29 * n
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference_arm(args)
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from graphbrew_gb300 import build as gbuild
+    gbuild.build()
+    import graphbrew_gb300 as gb
+    from graphbrew_gb300 import graphgen as gg
+
+    # Every rank maps its own replica (the path does not shard; no collective).
+    rp, col = gg.rmat(args.scale, EDGE_FACTOR, seed=SEED, device="cuda")
+    n, nnz = rp.numel() - 1, col.numel()
+    ctx = gb.Context(local)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+
+    def step():
+        ids, orp, ocol, st = ctx.map_and_relabel(rp, col, RECIPE)
+        return ids, orp, ocol, st
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    sampler = ClockSampler(local)
+    sampler.start()
+    stats = []
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        ids, orp, ocol, st = step()
+        stats.append(st)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    if world > 1:
+        dist.barrier()
+    ms_total = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms_total], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms_step = ms_total / args.steps
+    value = nnz * world * args.steps / (ms_total / 1e3) / 1e6
+
+    # Correctness of what was timed: a valid permutation.
+    assert ctx.validate_permutation(ids) == 0
+
+    # End to end through the C ABI with pinned host buffers.
+    e2e = None
+    if not args.no_e2e:
+        h_rp = rp.cpu().pin_memory()
+        h_col = col.cpu().pin_memory()
+        h_ids = torch.empty(n, dtype=torch.int32).pin_memory()
+        h_orp = torch.empty(n + 1, dtype=torch.int64).pin_memory()
+        h_ocol = torch.empty(nnz, dtype=torch.int32).pin_memory()
+        lib = gb.library()
+        opts = RECIPE.encode()
+
+        def host_step():
+            s = gb.GbgpuStats()
+            rc = lib.gbgpu_map_and_relabel(ctx.handle, h_rp.data_ptr(), h_col.data_ptr(), n, nnz, opts, -1.0,
+                                           h_ids.data_ptr(), h_orp.data_ptr(), h_ocol.data_ptr(),
+                                           gb.C.byref(s), 0)
+            assert rc == 0, lib.gbgpu_last_error(ctx.handle)
+            return s
+
+        for _ in range(2):
+            host_step()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            host_step()
+        t1 = time.perf_counter()
+        e2e_s = (t1 - t0) / args.steps
+        e2e = {"value": nnz * world / e2e_s / 1e6, "unit": "Medges/s",
+               "h2d_bytes_per_step": 8 * (n + 1) + 4 * nnz,
+               "d2h_bytes_per_step": 4 * n + 8 * (n + 1) + 4 * nnz,
+               "ms_per_step": e2e_s * 1e3}
+
+    # Stage split and the roofline of the dominant stage.
+    def avg(key):
+        return sum(s[key] for s in stats) / len(stats)
+    stage_ms = {k: avg(k) for k in ("leiden_ms", "local_move_ms", "aggregate_ms", "compose_ms", "intra_ms",
+                                    "validate_ms", "relabel_ms", "total_ms")}
+    iters = avg("iterations")
+    peak, peak_kind = load_peaks()
+    lm_bytes = local_move_bytes(n, nnz) * iters
+    rl_bytes = relabel_bytes(n, nnz)
+    cand = {"local_move": (lm_bytes, stage_ms["local_move_ms"]), "relabel": (rl_bytes, stage_ms["relabel_ms"])}
+    dom = max(cand, key=lambda k: cand[k][1])
+    b, ms = cand[dom]
+    achieved = b / (ms / 1e3) / 1e9 if ms > 0 else 0.0
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                "algorithmic_bytes_per_launch": b}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle as po
+        po.build()
+        threads = host_cores()
+        secs, cpu_ids = cpu_mapping_seconds(rp.cpu().numpy(), col.cpu().numpy(), threads)
+        cpu = {"value": nnz / secs / 1e6, "unit": "Medges/s", "cores": threads, "kind": "port",
+               "sample": f"one full mapping+validation+relabel of the same RMAT scale {args.scale} graph "
+                         f"({secs:.1f} s, OpenMP cd_parallel restatement)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "Medges/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded RMAT, generated on device)",
+            "config": {"workload": f"rmat{args.scale}_ef{EDGE_FACTOR}_fastleiden_gorder8",
+                       "recipe": "12:" + RECIPE, "scale": args.scale, "edge_factor": EDGE_FACTOR,
+                       "vertices": n, "directed_entries": nnz, "parallelism": f"replicas{world}",
+                       "l2": "inputs larger than L2 (CSR 0.55 GB vs 129 MB L2)"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "clocks": clocks,
+            "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
+            "stages_ms": stage_ms,
+            "mapping": {"passes": stats[-1]["passes"], "iterations": stats[-1]["iterations"],
+                        "communities": stats[-1]["communities"],
+                        "largest_community": stats[-1]["largest_community"],
+                        "bfs_levels": stats[-1]["bfs_levels"], "isolated": stats[-1]["isolated"],
+                        "gorder_communities": stats[-1]["gorder_communities"],
+                        "fallback_communities": stats[-1]["fallback_communities"]},
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

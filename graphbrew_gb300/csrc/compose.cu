@@ -1,0 +1,839 @@
+// compose.cu -- COMPOSE placement and intra-community ordering on the device.
+//
+// Follows graphbrew::orderCompose (bench/include/graphbrew/reorder/reorder_graphbrew.h:6286-7087)
+// with super-graph order "none":
+//   * vertices of degree 0 go to the global tail in id order (:6336-6386);
+//   * communities are stable-sorted by the community-order key (:6438-6502);
+//   * each community's vertices keep vertex-id order (commVertices, :6373-6386);
+//   * intra order: Gorder with window w for 4..fallback vertices
+//     (intraGorderGreedy, :4420-4587), BFS from the hub above the fallback
+//     (intraBFSFromHub, :3929-3984), identity for <= 3 vertices;
+//   * newIds[v] = offset(community) + localId[v] (:7003-7017).
+//
+// Layout in HBM (n vertices): one stable radix sort of (rank(community), v)
+// gives the whole placement skeleton: position p in [0, n) holds the vertex
+// placed p-th before intra ordering, isolated vertices last.  Every later
+// kernel indexes communities by their contiguous position range.
+#include <algorithm>
+#include <type_traits>
+
+#include "gb_common.cuh"
+#include "gb_stages.h"
+
+namespace gb {
+
+namespace {
+
+enum CommunityOrderOrd { kSizeDesc = 0, kSizeAsc = 1, kDegreeDesc = 2, kDegreeAsc = 3, kIdentity = 6 };
+enum IntraOrd { kIntraBFS = 0, kIntraDendrogram = 3, kIntraGorder = 4 };
+
+constexpr int kT = 256;
+
+__global__ void k_max_u32(const uint32_t* __restrict__ a, int64_t n, uint32_t* __restrict__ out) {
+    uint32_t m = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        m = max(m, a[i]);
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+// Community sizes over non-isolated vertices, optional degree totals.
+__global__ void k_comm_sizes(const int64_t* __restrict__ rp, const uint32_t* __restrict__ memb, int64_t n,
+                             uint32_t* __restrict__ csize, unsigned long long* __restrict__ cdeg) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t d = rp[v + 1] - rp[v];
+        if (d != 0) {
+            atomicAdd(&csize[memb[v]], 1u);
+            if (cdeg) atomicAdd(&cdeg[memb[v]], (unsigned long long)d);
+        }
+    }
+}
+
+__global__ void k_max_u32_u64(const uint32_t* __restrict__ a, const unsigned long long* __restrict__ b, int64_t n,
+                              uint32_t* __restrict__ out_a, unsigned long long* __restrict__ out_b) {
+    uint32_t ma = 0;
+    unsigned long long mb = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        ma = max(ma, a[i]);
+        if (b) mb = max(mb, b[i]);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        ma = max(ma, __shfl_xor_sync(0xFFFFFFFFu, ma, o));
+        mb = max(mb, __shfl_xor_sync(0xFFFFFFFFu, mb, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(out_a, ma);
+        if (b) atomicMax(out_b, mb);
+    }
+}
+
+__global__ void k_comm_keys(int order, const uint32_t* __restrict__ csize, const unsigned long long* __restrict__ cdeg,
+                            int64_t C, uint32_t max_size, unsigned long long max_deg,
+                            uint64_t* __restrict__ keys, uint32_t* __restrict__ ids) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C; c += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t k = 0;
+        switch (order) {
+            case kSizeDesc: k = (uint64_t)(max_size - csize[c]); break;
+            case kSizeAsc: k = csize[c]; break;
+            case kDegreeDesc: k = max_deg - cdeg[c]; break;
+            case kDegreeAsc: k = cdeg[c]; break;
+            default: k = 0; break;
+        }
+        keys[c] = k;
+        ids[c] = (uint32_t)c;
+    }
+}
+
+// rank[c] and sorted sizes.
+__global__ void k_rank(const uint32_t* __restrict__ order, const uint32_t* __restrict__ csize, int64_t C,
+                       uint32_t* __restrict__ rank, int64_t* __restrict__ ssize) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < C; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t c = order[i];
+        rank[c] = (uint32_t)i;
+        ssize[i] = csize[c];
+    }
+}
+
+// Sort keys for the placement skeleton: rank of the vertex's community, or C
+// for isolated vertices (they sort last, in id order).
+__global__ void k_vertex_keys(const int64_t* __restrict__ rp, const uint32_t* __restrict__ memb,
+                              const uint32_t* __restrict__ rank, int64_t n, uint32_t C,
+                              uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        keys[v] = (rp[v + 1] == rp[v]) ? C : rank[memb[v]];
+        vals[v] = (uint32_t)v;
+    }
+}
+
+// pos_of[v], local index (identity intra order) per vertex.
+__global__ void k_positions(const uint32_t* __restrict__ order_v, const uint32_t* __restrict__ keys_sorted,
+                            const int64_t* __restrict__ offs, int64_t n, uint32_t C,
+                            int64_t* __restrict__ pos_of, uint32_t* __restrict__ local) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t v = order_v[p];
+        const uint32_t r = keys_sorted[p];
+        pos_of[v] = p;
+        local[v] = (r < C) ? (uint32_t)(p - offs[r]) : 0u;
+    }
+}
+
+// Community classes: 1 = Gorder (thread), 2 = Gorder (warp, shared memory),
+// 3 = Gorder (warp, global workspace), 4 = BFS.  Lists hold ranks.
+struct ClassCounts {
+    int32_t n[5];
+    unsigned long long gorder_communities, gorder_vertices, fallback_communities, fallback_vertices;
+    uint32_t gorder_max, largest;
+};
+
+constexpr int kThreadGorderMax = 32;
+constexpr int kSmemGorderMax = 4096;
+
+__global__ void k_classify(const int64_t* __restrict__ ssize, int64_t C, int intra, int fallback,
+                           int32_t* __restrict__ lists, ClassCounts* __restrict__ cc) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < C; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t sz = ssize[i];
+        if (sz == 0) continue;
+        atomicMax(&cc->largest, (uint32_t)sz);
+        int cls = 0;
+        if (intra == kIntraGorder) {
+            if (fallback > 0 && sz > fallback) {
+                atomicAdd(&cc->fallback_communities, 1ull);
+                atomicAdd(&cc->fallback_vertices, (unsigned long long)sz);
+                cls = 4;
+            } else if (sz > 3) {
+                atomicAdd(&cc->gorder_communities, 1ull);
+                atomicAdd(&cc->gorder_vertices, (unsigned long long)sz);
+                atomicMax(&cc->gorder_max, (uint32_t)sz);
+                cls = sz <= kThreadGorderMax ? 1 : (sz <= kSmemGorderMax ? 2 : 3);
+            }
+        } else {
+            cls = sz >= 2 ? 4 : 0;
+        }
+        if (cls) {
+            const int32_t slot = atomicAdd(&cc->n[cls], 1);
+            lists[(int64_t)cls * C + slot] = (int32_t)i;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Local adjacency for Gorder communities: for each position p, the local
+// indices of in-community neighbours in row order.
+// ---------------------------------------------------------------------------
+__global__ void k_mark_gorder_positions(const int32_t* __restrict__ list, const int32_t* __restrict__ count_p,
+                                        const int64_t* __restrict__ offs, const int64_t* __restrict__ ssize,
+                                        uint8_t* __restrict__ mark) {
+    const int32_t count = *count_p;
+    for (int32_t j = blockIdx.x; j < count; j += gridDim.x) {
+        const int32_t r = list[j];
+        const int64_t b = offs[r], sz = ssize[r];
+        for (int64_t k = threadIdx.x; k < sz; k += blockDim.x) mark[b + k] = 1;
+    }
+}
+
+__global__ void k_local_count(const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
+                              const uint32_t* __restrict__ memb, const uint32_t* __restrict__ order_v,
+                              const uint8_t* __restrict__ mark, int64_t nn, int64_t* __restrict__ cnt) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nn; p += (int64_t)gridDim.x * blockDim.x) {
+        int64_t c = 0;
+        if (mark[p]) {
+            const uint32_t u = order_v[p];
+            const uint32_t cu = memb[u];
+            for (int64_t e = rp[u]; e < rp[u + 1]; ++e) c += (memb[col[e]] == cu);
+        }
+        cnt[p] = c;
+    }
+}
+
+__global__ void k_local_fill(const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
+                             const uint32_t* __restrict__ memb, const uint32_t* __restrict__ order_v,
+                             const uint8_t* __restrict__ mark, const uint32_t* __restrict__ local,
+                             const int64_t* __restrict__ loff, int64_t nn, uint16_t* __restrict__ ladj16,
+                             uint32_t* __restrict__ ladj32) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nn; p += (int64_t)gridDim.x * blockDim.x) {
+        if (!mark[p]) continue;
+        const uint32_t u = order_v[p];
+        const uint32_t cu = memb[u];
+        int64_t o = loff[p];
+        for (int64_t e = rp[u]; e < rp[u + 1]; ++e) {
+            const int32_t w = col[e];
+            if (memb[w] == cu) {
+                if (ladj32) ladj32[o++] = local[w];
+                else ladj16[o++] = (uint16_t)local[w];
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// UnitHeap replica (intraGorderGreedy).  The list keeps buckets contiguous in
+// descending key order; insertion is at the bucket front; extract-max takes
+// the front of the highest non-empty bucket.  Storage is abstracted so one
+// body serves thread-private arrays, shared memory and global workspaces.
+// ---------------------------------------------------------------------------
+struct HeapView {
+    int* key;
+    int* prev;
+    int* next;
+    int* bfirst;
+    int* bsecond;
+    int max_key;
+
+    __device__ __forceinline__ void unlink(int idx) {
+        const int p = prev[idx], nx = next[idx];
+        if (p >= 0) next[p] = nx;
+        if (nx >= 0) prev[nx] = p;
+        const int k = key[idx];
+        if (bfirst[k] == idx && bsecond[k] == idx) {
+            bfirst[k] = bsecond[k] = -1;
+        } else if (bfirst[k] == idx) {
+            bfirst[k] = nx;
+        } else if (bsecond[k] == idx) {
+            bsecond[k] = p;
+        }
+    }
+    __device__ __forceinline__ void link_front(int idx, int k) {
+        key[idx] = k;
+        if (bfirst[k] < 0) {
+            int after = -1;
+            for (int bk = k - 1; bk >= 0; --bk)
+                if (bfirst[bk] >= 0) { after = bfirst[bk]; break; }
+            int before = -1;
+            for (int bk = k + 1; bk <= max_key; ++bk)
+                if (bsecond[bk] >= 0) { before = bsecond[bk]; break; }
+            prev[idx] = before;
+            next[idx] = after;
+            if (before >= 0) next[before] = idx;
+            if (after >= 0) prev[after] = idx;
+            bfirst[k] = bsecond[k] = idx;
+        } else {
+            const int old_first = bfirst[k];
+            const int before_old = prev[old_first];
+            prev[idx] = before_old;
+            next[idx] = old_first;
+            prev[old_first] = idx;
+            if (before_old >= 0) next[before_old] = idx;
+            bfirst[k] = idx;
+        }
+        if (k > max_key) max_key = k;
+    }
+    __device__ __forceinline__ void remove(int idx) {
+        unlink(idx);
+        prev[idx] = next[idx] = -1;
+        key[idx] = -1;
+        while (max_key > 0 && bfirst[max_key] < 0) --max_key;
+    }
+    __device__ __forceinline__ int extract_max() {
+        while (max_key > 0 && bfirst[max_key] < 0) --max_key;
+        const int idx = bfirst[max_key];
+        if (idx >= 0) remove(idx);
+        return idx;
+    }
+    __device__ __forceinline__ void bump(int idx, int delta) {
+        const int old = key[idx];
+        if (old < 0) return;
+        if (delta < 0 && old <= 0) return;
+        unlink(idx);
+        link_front(idx, old + delta);
+    }
+};
+
+// Runs the greedy placement of one community of sz vertices (local indices
+// 0..sz-1 in vertex-id order).  ladj/loff give local adjacency; seed_deg the
+// degrees for seeding; out_local receives local ids by local index.
+template <typename LAdj>
+__device__ void gorder_run(HeapView& h, int sz, int nbuckets, int window, const LAdj* __restrict__ ladj,
+                           const int64_t* __restrict__ loff, const uint32_t* __restrict__ degs,
+                           int* __restrict__ placed, uint32_t* __restrict__ out_local) {
+    for (int i = 0; i < sz; ++i) {
+        h.key[i] = 0;
+        h.prev[i] = i - 1;
+        h.next[i] = (i + 1 < sz) ? i + 1 : -1;
+    }
+    for (int b = 0; b < nbuckets; ++b) h.bfirst[b] = h.bsecond[b] = -1;
+    h.bfirst[0] = 0;
+    h.bsecond[0] = sz - 1;
+    h.max_key = 0;
+    int seed = 0;
+    uint32_t seed_deg = degs[0];
+    for (int i = 1; i < sz; ++i)
+        if (degs[i] > seed_deg) { seed_deg = degs[i]; seed = i; }
+    h.remove(seed);
+    int nplaced = 0;
+    placed[nplaced++] = seed;
+    out_local[seed] = 0;
+    for (int64_t k = loff[seed]; k < loff[seed + 1]; ++k) h.bump((int)ladj[k], +1);
+    for (int lid = 1; lid < sz; ++lid) {
+        const int best = h.extract_max();
+        if (best < 0) {
+            for (int i = 0; i < sz && lid < sz; ++i) {
+                if (h.key[i] >= 0) {
+                    h.remove(i);
+                    out_local[i] = (uint32_t)lid++;
+                }
+            }
+            break;
+        }
+        placed[nplaced++] = best;
+        out_local[best] = (uint32_t)lid;
+        for (int64_t k = loff[best]; k < loff[best + 1]; ++k) h.bump((int)ladj[k], +1);
+        if (nplaced > window) {
+            const int old_v = placed[nplaced - 1 - window];
+            for (int64_t k = loff[old_v]; k < loff[old_v + 1]; ++k) h.bump((int)ladj[k], -1);
+        }
+    }
+}
+
+// One thread per community of 4..32 vertices; state in thread-private arrays.
+template <typename LAdj>
+__global__ void k_gorder_thread(const int32_t* __restrict__ list, const int32_t* __restrict__ count_p,
+                                const int64_t* __restrict__ offs, const int64_t* __restrict__ ssize,
+                                const uint32_t* __restrict__ order_v, const int64_t* __restrict__ rp,
+                                const LAdj* __restrict__ ladj, const int64_t* __restrict__ loff,
+                                int window, uint32_t* __restrict__ local_by_pos) {
+    constexpr int kMaxB = 102 + 8;  // window <= 100
+    const int32_t count = *count_p;
+    for (int32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < count; j += gridDim.x * blockDim.x) {
+        const int32_t r = list[j];
+        const int64_t base = offs[r];
+        const int sz = (int)ssize[r];
+        int key[kThreadGorderMax], prev[kThreadGorderMax], next[kThreadGorderMax], placed[kThreadGorderMax];
+        int bf[kMaxB], bs[kMaxB];
+        uint32_t degs[kThreadGorderMax];
+        for (int i = 0; i < sz; ++i) {
+            const uint32_t u = order_v[base + i];
+            degs[i] = (uint32_t)(rp[u + 1] - rp[u]);
+        }
+        HeapView h{key, prev, next, bf, bs, 0};
+        const int nb = min(window + 2, kMaxB);
+        gorder_run<LAdj>(h, sz, nb, window, ladj, loff + base, degs, placed, local_by_pos + base);
+    }
+}
+
+// One warp per community; heap in shared memory (lane 0 runs it, the warp
+// stages degrees).  Global variant for communities too large for shared memory.
+template <typename LAdj, bool kShared>
+__global__ void k_gorder_warp(const int32_t* __restrict__ list, const int32_t* __restrict__ count_p,
+                              const int64_t* __restrict__ offs, const int64_t* __restrict__ ssize,
+                              const uint32_t* __restrict__ order_v, const int64_t* __restrict__ rp,
+                              const LAdj* __restrict__ ladj, const int64_t* __restrict__ loff, int window,
+                              uint32_t* __restrict__ local_by_pos, int* __restrict__ gws, int64_t gcap,
+                              uint32_t* __restrict__ gdeg) {
+    extern __shared__ int smem[];
+    const int32_t count = *count_p;
+    const int lane = threadIdx.x & 31;
+    const int nb = window + 2;
+    for (int32_t j = blockIdx.x; j < count; j += gridDim.x) {
+        const int32_t r = list[j];
+        const int64_t base = offs[r];
+        const int sz = (int)ssize[r];
+        int* ws;
+        uint32_t* degs;
+        if (kShared) {
+            ws = smem;
+            degs = reinterpret_cast<uint32_t*>(smem + 4 * kSmemGorderMax + 2 * nb);
+        } else {
+            ws = gws + (int64_t)blockIdx.x * (4 * gcap + 2 * nb);
+            degs = gdeg + (int64_t)blockIdx.x * gcap;
+        }
+        const int cap = kShared ? kSmemGorderMax : (int)gcap;
+        for (int i = lane; i < sz; i += 32) {
+            const uint32_t u = order_v[base + i];
+            degs[i] = (uint32_t)(rp[u + 1] - rp[u]);
+        }
+        __syncwarp();
+        if (lane == 0) {
+            HeapView h{ws, ws + cap, ws + 2 * cap, ws + 4 * cap, ws + 4 * cap + nb, 0};
+            gorder_run<LAdj>(h, sz, nb, window, ladj, loff + base, degs, ws + 3 * cap, local_by_pos + base);
+        }
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Exact-order BFS from the hub (intraBFSFromHub), level-synchronous over all
+// BFS communities at once.  Within one community the reference's FIFO order
+// is reproduced: a vertex is discovered by the earliest frontier vertex (queue
+// position) that reaches it and, within that parent, in row order.  Claims are
+// atomicMin of (frontier index << 32 | row offset); the children of a level
+// are then written in (frontier index, row offset) order by an exclusive scan
+// over per-edge flags.
+// ---------------------------------------------------------------------------
+__global__ void k_bfs_slots(const int32_t* __restrict__ list, const int32_t* __restrict__ count_p,
+                            const uint32_t* __restrict__ order_v, const int64_t* __restrict__ offs,
+                            const uint32_t* __restrict__ memb, int32_t* __restrict__ slot_of_comm,
+                            int64_t* __restrict__ slot_base, int64_t* __restrict__ slot_size,
+                            const int64_t* __restrict__ ssize) {
+    const int32_t count = *count_p;
+    for (int32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < count; j += gridDim.x * blockDim.x) {
+        const int32_t r = list[j];
+        const uint32_t c = memb[order_v[offs[r]]];
+        slot_of_comm[c] = j;
+        slot_base[j] = offs[r];
+        slot_size[j] = ssize[r];
+    }
+}
+
+// Hub = max degree, first in vertex-id (= position) order.
+__global__ void k_bfs_hubs(const int64_t* __restrict__ slot_base, const int64_t* __restrict__ slot_size, int32_t nslots,
+                           const uint32_t* __restrict__ order_v, const int64_t* __restrict__ rp,
+                           unsigned long long* __restrict__ hubkey) {
+    // grid-stride over (slot, position) flattened per slot: one block per slot chunk
+    for (int32_t j = blockIdx.y; j < nslots; j += gridDim.y) {
+        const int64_t b = slot_base[j], sz = slot_size[j];
+        unsigned long long best = 0;
+        for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < sz; k += (int64_t)gridDim.x * blockDim.x) {
+            const uint32_t u = order_v[b + k];
+            const uint64_t d = (uint64_t)(rp[u + 1] - rp[u]);
+            const unsigned long long key = (d << 32) | (0xFFFFFFFFull - (uint64_t)k);
+            best = key > best ? key : best;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long t = __shfl_xor_sync(0xFFFFFFFFu, best, o);
+            best = t > best ? t : best;
+        }
+        if ((threadIdx.x & 31) == 0) atomicMax(&hubkey[j], best);
+    }
+}
+
+__global__ void k_bfs_init(const unsigned long long* __restrict__ hubkey, const int64_t* __restrict__ slot_base,
+                           int32_t nslots, const uint32_t* __restrict__ order_v, int32_t* __restrict__ frontier,
+                           uint8_t* __restrict__ visited, uint32_t* __restrict__ local, int64_t* __restrict__ qlen,
+                           int64_t* __restrict__ fs, int64_t* __restrict__ fe) {
+    for (int32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < nslots; j += gridDim.x * blockDim.x) {
+        const int64_t k = (int64_t)(0xFFFFFFFFull - (hubkey[j] & 0xFFFFFFFFull));
+        const uint32_t hub = order_v[slot_base[j] + k];
+        frontier[j] = (int32_t)hub;
+        visited[hub] = 1;
+        local[hub] = 0;
+        qlen[j] = 1;
+        fs[j] = j;
+        fe[j] = j + 1;
+    }
+}
+
+__global__ void k_frontier_degrees(const int32_t* __restrict__ F, int64_t nf, const int64_t* __restrict__ rp,
+                                   int64_t* __restrict__ fdeg) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nf; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t u = F[i];
+        fdeg[i] = rp[u + 1] - rp[u];
+    }
+}
+
+__device__ __forceinline__ int64_t upper_index(const int64_t* __restrict__ D, int64_t nf, int64_t e) {
+    // largest i in [0, nf) with D[i] <= e
+    int64_t lo = 0, hi = nf - 1;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi + 1) >> 1;
+        if (D[mid] <= e) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void k_bfs_claim(const int32_t* __restrict__ F, int64_t nf, const int64_t* __restrict__ D, int64_t T,
+                            const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
+                            const uint32_t* __restrict__ memb, const uint8_t* __restrict__ visited,
+                            unsigned long long* __restrict__ claim) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < T; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = upper_index(D, nf, e);
+        const int64_t k = e - D[i];
+        const int32_t u = F[i];
+        const int32_t w = col[rp[u] + k];
+        if (memb[w] == memb[u] && !visited[w])
+            atomicMin(&claim[w], ((unsigned long long)i << 32) | (unsigned long long)k);
+    }
+}
+
+__global__ void k_bfs_flag(const int32_t* __restrict__ F, int64_t nf, const int64_t* __restrict__ D, int64_t T,
+                           const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
+                           const uint32_t* __restrict__ memb, const uint8_t* __restrict__ visited,
+                           const unsigned long long* __restrict__ claim, int32_t* __restrict__ flag) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < T; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = upper_index(D, nf, e);
+        const int64_t k = e - D[i];
+        const int32_t u = F[i];
+        const int32_t w = col[rp[u] + k];
+        flag[e] = (memb[w] == memb[u] && !visited[w] &&
+                   claim[w] == (((unsigned long long)i << 32) | (unsigned long long)k)) ? 1 : 0;
+    }
+}
+
+// Per community: where its children start in the next frontier this level.
+__global__ void k_bfs_bases(int32_t nslots, const int64_t* __restrict__ fs, const int64_t* __restrict__ fe,
+                            const int64_t* __restrict__ D, const int64_t* __restrict__ P,
+                            int64_t* __restrict__ base, int64_t* __restrict__ end) {
+    for (int32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < nslots; j += gridDim.x * blockDim.x) {
+        base[j] = P[D[fs[j]]];
+        end[j] = P[D[fe[j]]];
+    }
+}
+
+__global__ void k_bfs_write(const int32_t* __restrict__ F, int64_t nf, const int64_t* __restrict__ D, int64_t T,
+                            const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
+                            const uint32_t* __restrict__ memb, const int32_t* __restrict__ flag,
+                            const int64_t* __restrict__ P, const int32_t* __restrict__ slot_of_comm,
+                            const int64_t* __restrict__ qlen, const int64_t* __restrict__ base,
+                            int32_t* __restrict__ nextF, uint8_t* __restrict__ visited, uint32_t* __restrict__ local) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < T; e += (int64_t)gridDim.x * blockDim.x) {
+        if (!flag[e]) continue;
+        const int64_t i = upper_index(D, nf, e);
+        const int64_t k = e - D[i];
+        const int32_t u = F[i];
+        const int32_t w = col[rp[u] + k];
+        const int64_t p = P[e];
+        const int32_t j = slot_of_comm[memb[u]];
+        nextF[p] = w;
+        visited[w] = 1;
+        local[w] = (uint32_t)(qlen[j] + (p - base[j]));
+    }
+}
+
+__global__ void k_bfs_advance(int32_t nslots, int64_t* __restrict__ qlen, int64_t* __restrict__ fs,
+                              int64_t* __restrict__ fe, const int64_t* __restrict__ base,
+                              const int64_t* __restrict__ end) {
+    for (int32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < nslots; j += gridDim.x * blockDim.x) {
+        qlen[j] += end[j] - base[j];
+        fs[j] = base[j];
+        fe[j] = end[j];
+    }
+}
+
+// Unreached vertices of BFS communities, in vertex order after the BFS order.
+__global__ void k_bfs_left_flags(const uint32_t* __restrict__ order_v, int64_t nn, const uint32_t* __restrict__ memb,
+                                 const int32_t* __restrict__ slot_of_comm, const uint8_t* __restrict__ visited,
+                                 int32_t* __restrict__ flag) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nn; p += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t v = order_v[p];
+        flag[p] = (slot_of_comm[memb[v]] >= 0 && !visited[v]) ? 1 : 0;
+    }
+}
+
+__global__ void k_bfs_left_assign(const uint32_t* __restrict__ order_v, int64_t nn, const uint32_t* __restrict__ memb,
+                                  const int32_t* __restrict__ slot_of_comm, const int32_t* __restrict__ flag,
+                                  const int64_t* __restrict__ R, const int64_t* __restrict__ slot_base,
+                                  const int64_t* __restrict__ qlen, uint32_t* __restrict__ local) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nn; p += (int64_t)gridDim.x * blockDim.x) {
+        if (!flag[p]) continue;
+        const uint32_t v = order_v[p];
+        const int32_t j = slot_of_comm[memb[v]];
+        local[v] = (uint32_t)(qlen[j] + (R[p] - R[slot_base[j]]));
+    }
+}
+
+__global__ void k_gather_local(const uint32_t* __restrict__ order_v, const uint32_t* __restrict__ local_by_pos,
+                               const uint8_t* __restrict__ mark, int64_t nn, uint32_t* __restrict__ local) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nn; p += (int64_t)gridDim.x * blockDim.x)
+        if (mark[p]) local[order_v[p]] = local_by_pos[p];
+}
+
+__global__ void k_final_assign(const uint32_t* __restrict__ order_v, const uint32_t* __restrict__ keys_sorted,
+                               const int64_t* __restrict__ offs, const uint32_t* __restrict__ local, int64_t n,
+                               uint32_t C, int32_t* __restrict__ new_ids) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t v = order_v[p];
+        const uint32_t r = keys_sorted[p];
+        new_ids[v] = (r < C) ? (int32_t)(offs[r] + local[v]) : (int32_t)p;
+    }
+}
+
+template <typename T>
+T read_dev(const T* p, cudaStream_t s) {
+    T h;
+    GB_CUDA(cudaMemcpyAsync(&h, p, sizeof(T), cudaMemcpyDeviceToHost, s));
+    GB_CUDA(cudaStreamSynchronize(s));
+    return h;
+}
+
+}  // namespace
+
+void compose_device(const DeviceCSR& g, const uint32_t* memb, const ComposeParams& p, int32_t* new_ids,
+                    gbgpu_stats* st, cudaStream_t s) {
+    const int64_t n = g.n;
+    if (n == 0) return;
+    int intra = p.intra_order;
+    if (intra == kIntraDendrogram) intra = kIntraBFS;  // Leiden has no Rabbit dendrogram (:6668-6677)
+    GB_REQUIRE(intra == kIntraBFS || intra == kIntraGorder, GBGPU_E_UNSUPPORTED,
+               "intra-community order not available on the GPU path");
+    const int co = p.community_order;
+    GB_REQUIRE(co == kSizeDesc || co == kSizeAsc || co == kDegreeDesc || co == kDegreeAsc || co == kIdentity,
+               GBGPU_E_UNSUPPORTED, "community order not available on the GPU path");
+    GB_REQUIRE(intra != kIntraGorder || p.gorder_window > 0, GBGPU_E_INVALID,
+               "Local Gorder requires a positive window");
+    GB_REQUIRE(p.gorder_window <= 100, GBGPU_E_INVALID, "Gorder window above 100");
+    int64_t launches = 0;
+    cudaEvent_t ev0, ev1;
+    GB_CUDA(cudaEventCreate(&ev0));
+    GB_CUDA(cudaEventCreate(&ev1));
+    GB_CUDA(cudaEventRecord(ev0, s));
+
+    // numComm = max(membership) + 1 (:6338-6343).
+    DevBuf<uint32_t> scal(4, s);
+    GB_CUDA(cudaMemsetAsync(scal, 0, 4 * sizeof(uint32_t), s));
+    k_max_u32<<<grid_for(n, kT), kT, 0, s>>>(memb, n, scal.get());
+    GB_LAUNCH_CHECK();
+    const int64_t C = (int64_t)read_dev(scal.get(), s) + 1;
+    GB_REQUIRE(C <= n, GBGPU_E_INVALID, "membership ids must be < n");
+
+    DevBuf<uint32_t> csize(C, s);
+    GB_CUDA(cudaMemsetAsync(csize, 0, C * sizeof(uint32_t), s));
+    const bool need_deg = (co == kDegreeDesc || co == kDegreeAsc);
+    DevBuf<unsigned long long> cdeg(need_deg ? C : 0, s);
+    if (need_deg) GB_CUDA(cudaMemsetAsync(cdeg, 0, C * sizeof(unsigned long long), s));
+    k_comm_sizes<<<grid_for(n, kT), kT, 0, s>>>(g.row_ptr, memb, n, csize, need_deg ? cdeg.get() : nullptr);
+    GB_LAUNCH_CHECK();
+
+    // Community order: stable sort of 0..C-1 by the order key.
+    DevBuf<uint32_t> comm_order(C, s);
+    {
+        DevBuf<unsigned long long> maxdeg(1, s);
+        GB_CUDA(cudaMemsetAsync(scal, 0, sizeof(uint32_t), s));
+        GB_CUDA(cudaMemsetAsync(maxdeg, 0, sizeof(unsigned long long), s));
+        k_max_u32_u64<<<grid_for(C, kT), kT, 0, s>>>(csize, need_deg ? cdeg.get() : nullptr, C, scal.get(), maxdeg.get());
+        GB_LAUNCH_CHECK();
+        const uint32_t max_size = read_dev(scal.get(), s);
+        const unsigned long long max_deg = read_dev(maxdeg.get(), s);
+        DevBuf<uint64_t> keys(C, s);
+        k_comm_keys<<<grid_for(C, kT), kT, 0, s>>>(co, csize, need_deg ? cdeg.get() : nullptr, C, max_size, max_deg,
+                                                   keys, comm_order);
+        GB_LAUNCH_CHECK();
+        int kbits = 0;
+        if (co == kSizeDesc || co == kSizeAsc) kbits = bits_for(max_size);
+        else if (co == kDegreeDesc || co == kDegreeAsc) kbits = bits_for(max_deg);
+        radix_sort_pairs_u64(keys, comm_order, C, kbits, s);
+        launches += 4 + 3 * ((kbits + 7) / 8);
+    }
+    DevBuf<uint32_t> rank(C, s);
+    DevBuf<int64_t> ssize(C, s);
+    DevBuf<int64_t> offs(C + 1, s);
+    k_rank<<<grid_for(C, kT), kT, 0, s>>>(comm_order, csize, C, rank, ssize);
+    GB_LAUNCH_CHECK();
+    exclusive_scan_i64_total(ssize, offs, C, offs.get() + C, s);
+    const int64_t nn = read_dev(offs.get() + C, s);  // non-isolated vertices
+
+    // Placement skeleton: stable sort of (rank(community) | C for isolated, v).
+    DevBuf<uint32_t> vkeys(n, s), order_v(n, s);
+    k_vertex_keys<<<grid_for(n, kT), kT, 0, s>>>(g.row_ptr, memb, rank, n, (uint32_t)C, vkeys, order_v);
+    GB_LAUNCH_CHECK();
+    const int vbits = bits_for((uint64_t)C);
+    radix_sort_pairs_u32(vkeys, order_v, n, vbits, s);
+    DevBuf<int64_t> pos_of(n, s);
+    DevBuf<uint32_t> local(n, s);
+    k_positions<<<grid_for(n, kT), kT, 0, s>>>(order_v, vkeys, offs, n, (uint32_t)C, pos_of, local);
+    GB_LAUNCH_CHECK();
+    launches += 6 + 3 * ((vbits + 7) / 8);
+
+    // Classify communities.
+    DevBuf<int32_t> lists(5 * C, s);
+    DevBuf<ClassCounts> cc(1, s);
+    GB_CUDA(cudaMemsetAsync(cc, 0, sizeof(ClassCounts), s));
+    k_classify<<<grid_for(C, kT), kT, 0, s>>>(ssize, C, intra, p.gorder_fallback, lists, cc);
+    GB_LAUNCH_CHECK();
+    ClassCounts hc = read_dev(cc.get(), s);
+    launches += 1;
+
+    cudaEvent_t ev_intra0, ev_intra1;
+    GB_CUDA(cudaEventCreate(&ev_intra0));
+    GB_CUDA(cudaEventCreate(&ev_intra1));
+    GB_CUDA(cudaEventRecord(ev_intra0, s));
+
+    // ---- Gorder communities ----
+    const int32_t ng = hc.n[1] + hc.n[2] + hc.n[3];
+    if (ng > 0) {
+        DevBuf<uint8_t> mark(nn, s);
+        GB_CUDA(cudaMemsetAsync(mark, 0, nn, s));
+        for (int cls = 1; cls <= 3; ++cls) {
+            if (hc.n[cls] == 0) continue;
+            k_mark_gorder_positions<<<kNumSMs * 8, kT, 0, s>>>(lists.get() + cls * C, cc.get()->n + cls, offs, ssize, mark);
+            GB_LAUNCH_CHECK();
+            ++launches;
+        }
+        DevBuf<int64_t> loff(nn + 1, s);
+        k_local_count<<<grid_for(nn, kT), kT, 0, s>>>(g.row_ptr, g.col, memb, order_v, mark, nn, loff);
+        GB_LAUNCH_CHECK();
+        exclusive_scan_i64_total(loff, loff, nn, loff.get() + nn, s);
+        const int64_t ltot = read_dev(loff.get() + nn, s);
+        const bool wide = hc.gorder_max > 65535;
+        DevBuf<uint16_t> l16(wide ? 0 : (ltot > 0 ? ltot : 1), s);
+        DevBuf<uint32_t> l32(wide ? (ltot > 0 ? ltot : 1) : 0, s);
+        k_local_fill<<<grid_for(nn, kT), kT, 0, s>>>(g.row_ptr, g.col, memb, order_v, mark, local, loff, nn,
+                                                     l16.get(), wide ? l32.get() : nullptr);
+        GB_LAUNCH_CHECK();
+        DevBuf<uint32_t> local_by_pos(nn, s);
+        GB_CUDA(cudaMemsetAsync(local_by_pos, 0, nn * sizeof(uint32_t), s));
+        launches += 5;
+        auto run = [&](auto* ladj) {
+            using LT = std::remove_pointer_t<decltype(ladj)>;
+            if (hc.n[1] > 0) {
+                k_gorder_thread<LT><<<grid_for(hc.n[1], 64), 64, 0, s>>>(lists.get() + 1 * C, cc.get()->n + 1, offs,
+                                                                          ssize, order_v, g.row_ptr, ladj, loff,
+                                                                          p.gorder_window, local_by_pos);
+                GB_LAUNCH_CHECK();
+                ++launches;
+            }
+            if (hc.n[2] > 0) {
+                const int nb = p.gorder_window + 2;
+                const int smem = (int)sizeof(int) * (5 * kSmemGorderMax + 2 * nb);
+                GB_CUDA(cudaFuncSetAttribute(k_gorder_warp<LT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+                const int grid = std::min<int>(hc.n[2], kNumSMs * 16);
+                k_gorder_warp<LT, true><<<grid, 32, smem, s>>>(lists.get() + 2 * C, cc.get()->n + 2, offs, ssize,
+                                                               order_v, g.row_ptr, ladj, loff, p.gorder_window,
+                                                               local_by_pos, nullptr, 0, nullptr);
+                GB_LAUNCH_CHECK();
+                ++launches;
+            }
+            if (hc.n[3] > 0) {
+                const int grid = std::min<int>(hc.n[3], kNumSMs * 4);
+                const int64_t cap = hc.gorder_max;
+                const int nb = p.gorder_window + 2;
+                DevBuf<int> gws((int64_t)grid * (4 * cap + 2 * nb), s);
+                DevBuf<uint32_t> gdeg((int64_t)grid * cap, s);
+                k_gorder_warp<LT, false><<<grid, 32, 0, s>>>(lists.get() + 3 * C, cc.get()->n + 3, offs, ssize,
+                                                             order_v, g.row_ptr, ladj, loff, p.gorder_window,
+                                                             local_by_pos, gws, cap, gdeg);
+                GB_LAUNCH_CHECK();
+                ++launches;
+            }
+        };
+        if (wide) run(l32.get()); else run(l16.get());
+        k_gather_local<<<grid_for(nn, kT), kT, 0, s>>>(order_v, local_by_pos, mark, nn, local);
+        GB_LAUNCH_CHECK();
+        ++launches;
+    }
+
+    // ---- BFS communities ----
+    const int32_t nbfs = hc.n[4];
+    int64_t levels = 0;
+    if (nbfs > 0) {
+        const int32_t* blist = lists.get() + 4 * C;
+        DevBuf<int32_t> slot_of_comm(C, s);
+        GB_CUDA(cudaMemsetAsync(slot_of_comm, 0xFF, C * sizeof(int32_t), s));
+        DevBuf<int64_t> slot_base(nbfs, s), slot_size(nbfs, s), qlen(nbfs, s), fs(nbfs, s), fe(nbfs, s),
+            bbase(nbfs, s), bend(nbfs, s);
+        k_bfs_slots<<<grid_for(nbfs, kT), kT, 0, s>>>(blist, cc.get()->n + 4, order_v, offs, memb, slot_of_comm,
+                                                      slot_base, slot_size, ssize);
+        GB_LAUNCH_CHECK();
+        DevBuf<unsigned long long> hubkey(nbfs, s);
+        GB_CUDA(cudaMemsetAsync(hubkey, 0, nbfs * sizeof(unsigned long long), s));
+        {
+            dim3 grid((unsigned)std::min<int64_t>(ceil_div(hc.largest, kT), 64), (unsigned)std::min(nbfs, 65535));
+            k_bfs_hubs<<<grid, kT, 0, s>>>(slot_base, slot_size, nbfs, order_v, g.row_ptr, hubkey);
+            GB_LAUNCH_CHECK();
+        }
+        DevBuf<uint8_t> visited(n, s);
+        GB_CUDA(cudaMemsetAsync(visited, 0, n, s));
+        DevBuf<unsigned long long> claim(n, s);
+        GB_CUDA(cudaMemsetAsync(claim, 0xFF, n * sizeof(unsigned long long), s));
+        DevBuf<int32_t> F(nn + 1, s), NF(nn + 1, s);
+        k_bfs_init<<<grid_for(nbfs, kT), kT, 0, s>>>(hubkey, slot_base, nbfs, order_v, F, visited, local, qlen, fs, fe);
+        GB_LAUNCH_CHECK();
+        launches += 3;
+        int64_t nf = nbfs;
+        DevBuf<int64_t> D(nn + 1, s);
+        while (nf > 0) {
+            ++levels;
+            k_frontier_degrees<<<grid_for(nf, kT), kT, 0, s>>>(F, nf, g.row_ptr, D);
+            GB_LAUNCH_CHECK();
+            exclusive_scan_i64_total(D, D, nf, D.get() + nf, s);
+            const int64_t T = read_dev(D.get() + nf, s);
+            if (T == 0) break;
+            DevBuf<int32_t> flag(T, s);
+            DevBuf<int64_t> P(T + 1, s);
+            k_bfs_claim<<<grid_for(T, kT), kT, 0, s>>>(F, nf, D, T, g.row_ptr, g.col, memb, visited, claim);
+            GB_LAUNCH_CHECK();
+            k_bfs_flag<<<grid_for(T, kT), kT, 0, s>>>(F, nf, D, T, g.row_ptr, g.col, memb, visited, claim, flag);
+            GB_LAUNCH_CHECK();
+            exclusive_scan_i32_to_i64(flag, P, T, P.get() + T, s);
+            k_bfs_bases<<<grid_for(nbfs, kT), kT, 0, s>>>(nbfs, fs, fe, D, P, bbase, bend);
+            GB_LAUNCH_CHECK();
+            k_bfs_write<<<grid_for(T, kT), kT, 0, s>>>(F, nf, D, T, g.row_ptr, g.col, memb, flag, P, slot_of_comm,
+                                                       qlen, bbase, NF, visited, local);
+            GB_LAUNCH_CHECK();
+            k_bfs_advance<<<grid_for(nbfs, kT), kT, 0, s>>>(nbfs, qlen, fs, fe, bbase, bend);
+            GB_LAUNCH_CHECK();
+            const int64_t next = read_dev(P.get() + T, s);
+            launches += 10;
+            std::swap(F.ptr, NF.ptr);
+            nf = next;
+        }
+        // Unreached vertices keep vertex order after the BFS order (:3978-3983).
+        DevBuf<int32_t> lflag(nn, s);
+        DevBuf<int64_t> R(nn + 1, s);
+        k_bfs_left_flags<<<grid_for(nn, kT), kT, 0, s>>>(order_v, nn, memb, slot_of_comm, visited, lflag);
+        GB_LAUNCH_CHECK();
+        exclusive_scan_i32_to_i64(lflag, R, nn, R.get() + nn, s);
+        k_bfs_left_assign<<<grid_for(nn, kT), kT, 0, s>>>(order_v, nn, memb, slot_of_comm, lflag, R, slot_base, qlen,
+                                                          local);
+        GB_LAUNCH_CHECK();
+        launches += 5;
+    }
+    GB_CUDA(cudaEventRecord(ev_intra1, s));
+
+    k_final_assign<<<grid_for(n, kT), kT, 0, s>>>(order_v, vkeys, offs, local, n, (uint32_t)C, new_ids);
+    GB_LAUNCH_CHECK();
+    launches += 1;
+    GB_CUDA(cudaEventRecord(ev1, s));
+    GB_CUDA(cudaEventSynchronize(ev1));
+    if (st) {
+        float ms = 0, ims = 0;
+        cudaEventElapsedTime(&ms, ev0, ev1);
+        cudaEventElapsedTime(&ims, ev_intra0, ev_intra1);
+        st->compose_ms += ms;
+        st->intra_ms += ims;
+        st->num_communities = C;
+        st->isolated = n - nn;
+        st->gorder_communities = (int64_t)hc.gorder_communities;
+        st->gorder_vertices = (int64_t)hc.gorder_vertices;
+        st->gorder_max_community = hc.gorder_max;
+        st->fallback_communities = (int64_t)hc.fallback_communities;
+        st->fallback_vertices = (int64_t)hc.fallback_vertices;
+        st->largest_community = hc.largest;
+        st->bfs_levels = levels;
+        st->kernel_launches += launches;
+    }
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+    cudaEventDestroy(ev_intra0);
+    cudaEventDestroy(ev_intra1);
+}
+
+}  // namespace gb

@@ -1,0 +1,49 @@
+// gb_stages.h -- internal stage entry points shared by the C ABI (api.cu).
+#pragma once
+
+#include "gb_common.cuh"
+
+namespace gb {
+
+// ---- relabel.cu ----
+// 0 valid, 1 out-of-range, 2 duplicate.  inv_out (n entries, may be null)
+// receives the inverse permutation when valid.  *bad_index: first failing index.
+int validate_permutation_device(const int32_t* ids, int64_t n, int32_t* inv_out, cudaStream_t s,
+                                int64_t* bad_index);
+void relabel_csr_device(const DeviceCSR& g, const int32_t* new_ids, const int32_t* inv,
+                        int64_t* out_rp, int32_t* out_col, cudaStream_t s, int64_t* launches);
+// Rejects graphs that are not squished CSR (every kernel relies on in-range
+// ids; the Gorder heap relies on duplicate-free rows).
+void check_graph_device(const DeviceCSR& g, cudaStream_t s);
+
+// ---- compose.cu ----
+struct ComposeParams {
+    int community_order = 0;   // CommunityOrder ordinal
+    int intra_order = 4;       // IntraCommunityOrder ordinal
+    int gorder_window = 8;
+    int gorder_fallback = 5000;
+};
+void compose_device(const DeviceCSR& g, const uint32_t* membership, const ComposeParams& p,
+                    int32_t* new_ids, gbgpu_stats* st, cudaStream_t s);
+
+// ---- leiden.cu ----
+struct LeidenParams {
+    double resolution = 1.0;
+    double tolerance = 1e-2;
+    double aggregation_tolerance = 0.8;
+    double tolerance_drop = 10.0;
+    int max_iterations = 10;
+    int max_passes = 10;
+    bool total_edges_m = true;
+    int super_move_batch = 1;
+    bool deterministic = false;
+    int chunk_vertices = 1 << 16;   // local-moving launch granularity (parallel mode)
+    int64_t super_single_cta_max_edges = 1 << 18;  // super-move in one persistent CTA up to this size
+};
+void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* membership, gbgpu_stats* st,
+                   cudaStream_t s);
+
+// Degree-distribution auto resolution (reorder_types.h:2743-2780).
+double auto_resolution_device(const int64_t* row_ptr, int64_t n, int64_t nnz, cudaStream_t s);
+
+}  // namespace gb

@@ -1,0 +1,958 @@
+// leiden.cu -- GVE-style Leiden community detection on the device.
+//
+// Follows graphbrew::runGraphBrew in GVE_CSR mode without refinement
+// (bench/include/graphbrew/reorder/reorder_graphbrew.h:7238-7571):
+//   pass loop: local moving on the original graph (localMovingPhase<false>,
+//   :1588-1734), community count and renumber (:1843-1889), GVE aggregation
+//   with the batched super-graph move (aggregateGVEStyle, :2156-2439),
+//   convergence checks (:7436-7452), tolerance drop per pass.
+//
+// Numerics: all edge weights are 1, so every community total and neighbour
+// weight is an exact integer; they are kept as int64 / uint32 and converted to
+// double only inside Delta-modularity, which is evaluated with explicitly
+// rounded IEEE operations in the reference's association (no FMA contraction),
+// so every delta equals the reference's bit for bit.
+//
+// Local moving (cd_parallel): asynchronous like the reference's OpenMP loop --
+// vertices are processed in id order in launches of `chunk_vertices`; a warp
+// per vertex accumulates neighbour communities (registers + __match_any_sync
+// up to 32 neighbours, a shared-memory hash table up to 1024), a CTA per hub
+// (a shared-memory or global hash table), community totals are updated with
+// integer atomics, and later launches see every earlier move.
+//
+// Super-graph move (sgmb<k>): batches of k communities in id order; proposals
+// read only the state before their batch and commits are commutative integer
+// adds, so the result is independent of thread scheduling.  The whole move
+// runs in one persistent CTA when the super-graph is small, otherwise one
+// launch pair per batch.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "gb_common.cuh"
+#include "gb_stages.h"
+
+namespace gb {
+
+namespace {
+
+constexpr int kT = 256;
+constexpr int kWarpMaxDeg = 1024;      // warp path up to this degree
+constexpr int kWarpHash = 2048;        // per-warp shared table slots
+constexpr int kLmWarpsPerBlock = 4;
+constexpr int kHubThreads = 512;
+constexpr int kHubSmemSlots = 16384;   // hub table in shared memory up to 8192 neighbours
+
+__device__ __forceinline__ uint32_t hash_u32(uint32_t x) {
+    return (uint32_t)(((uint64_t)x * 0x9E3779B97F4A7C15ull) >> 32);
+}
+
+// deltaModularity (:1295-1298) with the reference's association.
+__device__ __forceinline__ double delta_q(double kuc, double kud, double ku, double sc, double sd, double M, double R) {
+    const double a = __ddiv_rn(__dsub_rn(kuc, kud), M);
+    const double t = __dadd_rn(__dsub_rn(sc, sd), ku);
+    const double b = __dmul_rn(__dmul_rn(R, ku), t);
+    const double den = __dmul_rn(__dmul_rn(2.0, M), M);
+    return __dsub_rn(a, __ddiv_rn(b, den));
+}
+
+// (delta, id) ordering: larger delta first, then smaller id.
+__device__ __forceinline__ bool better(double da, uint32_t ia, double db, uint32_t ib) {
+    return da > db || (da == db && ia < ib);
+}
+
+__device__ __forceinline__ void warp_argmax(double& d, uint32_t& c) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double od = __shfl_xor_sync(0xFFFFFFFFu, d, o);
+        const uint32_t oc = __shfl_xor_sync(0xFFFFFFFFu, c, o);
+        if (better(od, oc, d, c)) { d = od; c = oc; }
+    }
+}
+
+// Shared-memory open-addressing insert (keys kNone = empty).
+__device__ __forceinline__ void table_add(uint32_t* keys, uint32_t* vals, uint32_t mask, uint32_t k, uint32_t w) {
+    uint32_t h = hash_u32(k) & mask;
+    while (true) {
+        const uint32_t prev = atomicCAS(&keys[h], kNone, k);
+        if (prev == kNone || prev == k) {
+            atomicAdd(&vals[h], w);
+            return;
+        }
+        h = (h + 1) & mask;
+    }
+}
+
+__device__ __forceinline__ uint32_t table_get(const uint32_t* keys, const uint32_t* vals, uint32_t mask, uint32_t k) {
+    uint32_t h = hash_u32(k) & mask;
+    while (true) {
+        const uint32_t s = keys[h];
+        if (s == k) return vals[h];
+        if (s == kNone) return 0;
+        h = (h + 1) & mask;
+    }
+}
+
+struct LmArgs {
+    const int64_t* rp;
+    const int32_t* col;
+    uint32_t* vcom;
+    unsigned long long* ctot;   // int64 totals, two's complement adds
+    uint8_t* vaff;
+    double M, R;
+    double* total_delta;
+    unsigned long long* moves;
+};
+
+// Warp per vertex, degree <= kWarpMaxDeg.
+__global__ void __launch_bounds__(kLmWarpsPerBlock * 32)
+k_local_move_warp(LmArgs a, int64_t begin, int64_t end) {
+    extern __shared__ uint32_t lm_smem[];  // kLmWarpsPerBlock x (keys, vals) x kWarpHash
+    __shared__ double sdelta[kLmWarpsPerBlock];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t* tk = lm_smem + (size_t)w * 2 * kWarpHash;
+    uint32_t* tv = tk + kWarpHash;
+    double acc_delta = 0.0;
+    unsigned long long acc_moves = 0;
+    const int64_t warps_total = (int64_t)gridDim.x * kLmWarpsPerBlock;
+    for (int64_t u = begin + (int64_t)blockIdx.x * kLmWarpsPerBlock + w; u < end; u += warps_total) {
+        const int64_t rb = a.rp[u];
+        const int deg = (int)(a.rp[u + 1] - rb);
+        if (deg > kWarpMaxDeg) continue;  // hub kernel
+        if (!a.vaff[u]) continue;
+        const uint32_t d = a.vcom[u];
+        const double ku = (double)deg;
+        double best_d = 0.0;
+        uint32_t best_c = kNone;
+        if (deg <= 32) {
+            uint32_t c = kNone;
+            if (lane < deg) {
+                const int32_t v = a.col[rb + lane];
+                if (v != (int32_t)u) c = a.vcom[v];
+            }
+            const unsigned peers = __match_any_sync(0xFFFFFFFFu, c);
+            const unsigned dmask = __ballot_sync(0xFFFFFFFFu, c == d);
+            const double kud = (double)__popc(dmask);
+            const bool leader = (c != kNone) && (lane == __ffs(peers) - 1) && c != d;
+            if (leader) {
+                const double sd = (double)(long long)a.ctot[d];
+                const double sc = (double)(long long)a.ctot[c];
+                const double dl = delta_q((double)__popc(peers), kud, ku, sc, sd, a.M, a.R);
+                if (dl > 0.0) { best_d = dl; best_c = c; }
+            }
+        } else {
+            uint32_t H = 64;
+            while (H < 2u * (uint32_t)deg) H <<= 1;
+            const uint32_t mask = H - 1;
+            for (uint32_t i = lane; i < H; i += 32) { tk[i] = kNone; tv[i] = 0; }
+            __syncwarp();
+            for (int base = 0; base < deg; base += 32) {
+                uint32_t c = kNone;
+                if (base + lane < deg) {
+                    const int32_t v = a.col[rb + base + lane];
+                    if (v != (int32_t)u) c = a.vcom[v];
+                }
+                const unsigned peers = __match_any_sync(0xFFFFFFFFu, c);
+                if (c != kNone && lane == __ffs(peers) - 1) table_add(tk, tv, mask, c, (uint32_t)__popc(peers));
+            }
+            __syncwarp();
+            const double kud = (double)table_get(tk, tv, mask, d);
+            const double sd = (double)(long long)a.ctot[d];
+            for (uint32_t i = lane; i < H; i += 32) {
+                const uint32_t c = tk[i];
+                if (c == kNone || c == d) continue;
+                const double sc = (double)(long long)a.ctot[c];
+                const double dl = delta_q((double)tv[i], kud, ku, sc, sd, a.M, a.R);
+                if (dl > 0.0 && better(dl, c, best_d, best_c)) { best_d = dl; best_c = c; }
+            }
+            __syncwarp();
+        }
+        warp_argmax(best_d, best_c);
+        if (best_d > 0.0 && best_c != d && best_c != kNone) {
+            if (lane == 0) {
+                atomicAdd(&a.ctot[d], (unsigned long long)(-(long long)deg));
+                atomicAdd(&a.ctot[best_c], (unsigned long long)(long long)deg);
+                a.vcom[u] = best_c;
+                acc_moves += 1;
+            }
+            for (int i = lane; i < deg; i += 32) a.vaff[a.col[rb + i]] = 1;
+            __syncwarp();
+        } else {
+            best_d = 0.0;
+        }
+        if (lane == 0) {
+            a.vaff[u] = 0;
+            acc_delta += best_d;
+        }
+    }
+    if (lane == 0) sdelta[w] = acc_delta;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int i = 0; i < kLmWarpsPerBlock; ++i) s += sdelta[i];
+        if (s != 0.0) atomicAdd(a.total_delta, s);
+    }
+    if (lane == 0 && acc_moves) atomicAdd(a.moves, acc_moves);
+}
+
+// CTA per hub vertex (degree > kWarpMaxDeg).  Table in shared memory when it
+// fits, otherwise in this CTA's slice of a global workspace.
+__global__ void __launch_bounds__(kHubThreads)
+k_local_move_hub(LmArgs a, const uint32_t* __restrict__ hubs, int64_t hub_begin, int64_t hub_end,
+                 uint32_t* __restrict__ gkeys, uint32_t* __restrict__ gvals, int64_t gcap) {
+    extern __shared__ uint32_t sm[];
+    __shared__ double red_d[kHubThreads / 32];
+    __shared__ uint32_t red_c[kHubThreads / 32];
+    __shared__ uint32_t s_kud;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int64_t hi = hub_begin + blockIdx.x; hi < hub_end; hi += gridDim.x) {
+        const uint32_t u = hubs[hi];
+        if (!a.vaff[u]) continue;
+        const int64_t rb = a.rp[u];
+        const int64_t deg = a.rp[u + 1] - rb;
+        uint32_t H = 1024;
+        while ((int64_t)H < 2 * deg) H <<= 1;
+        uint32_t *tk, *tv;
+        if (H <= (uint32_t)kHubSmemSlots) { tk = sm; tv = sm + kHubSmemSlots; }
+        else { tk = gkeys + (int64_t)blockIdx.x * gcap; tv = gvals + (int64_t)blockIdx.x * gcap; }
+        const uint32_t mask = H - 1;
+        for (uint32_t i = threadIdx.x; i < H; i += blockDim.x) { tk[i] = kNone; tv[i] = 0; }
+        __syncthreads();
+        const uint32_t d = a.vcom[u];
+        for (int64_t base = 0; base < deg; base += blockDim.x) {
+            uint32_t c = kNone;
+            if (base + threadIdx.x < deg) {
+                const int32_t v = a.col[rb + base + threadIdx.x];
+                if (v != (int32_t)u) c = a.vcom[v];
+            }
+            const unsigned peers = __match_any_sync(0xFFFFFFFFu, c);
+            if (c != kNone && lane == __ffs(peers) - 1) table_add(tk, tv, mask, c, (uint32_t)__popc(peers));
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) s_kud = table_get(tk, tv, mask, d);
+        __syncthreads();
+        const double kud = (double)s_kud;
+        const double ku = (double)deg;
+        const double sd = (double)(long long)a.ctot[d];
+        double best_d = 0.0;
+        uint32_t best_c = kNone;
+        for (uint32_t i = threadIdx.x; i < H; i += blockDim.x) {
+            const uint32_t c = tk[i];
+            if (c == kNone || c == d) continue;
+            const double sc = (double)(long long)a.ctot[c];
+            const double dl = delta_q((double)tv[i], kud, ku, sc, sd, a.M, a.R);
+            if (dl > 0.0 && better(dl, c, best_d, best_c)) { best_d = dl; best_c = c; }
+        }
+        warp_argmax(best_d, best_c);
+        if (lane == 0) { red_d[w] = best_d; red_c[w] = best_c; }
+        __syncthreads();
+        if (w == 0) {
+            best_d = lane < (int)(blockDim.x / 32) ? red_d[lane] : 0.0;
+            best_c = lane < (int)(blockDim.x / 32) ? red_c[lane] : kNone;
+            warp_argmax(best_d, best_c);
+            if (lane == 0) { red_d[0] = best_d; red_c[0] = best_c; }
+        }
+        __syncthreads();
+        best_d = red_d[0];
+        best_c = red_c[0];
+        const bool move = best_d > 0.0 && best_c != d && best_c != kNone;
+        if (move) {
+            if (threadIdx.x == 0) {
+                atomicAdd(&a.ctot[d], (unsigned long long)(-(long long)deg));
+                atomicAdd(&a.ctot[best_c], (unsigned long long)(long long)deg);
+                a.vcom[u] = best_c;
+                atomicAdd(a.moves, 1ull);
+            }
+            for (int64_t i = threadIdx.x; i < deg; i += blockDim.x) a.vaff[a.col[rb + i]] = 1;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            a.vaff[u] = 0;
+            if (move) atomicAdd(a.total_delta, best_d);
+        }
+        __syncthreads();
+    }
+}
+
+// ---- counting / renumbering ----
+__global__ void k_mark_exists(const uint32_t* __restrict__ vcom, int64_t n, int32_t* __restrict__ exists) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
+        exists[vcom[v]] = 1;
+}
+
+// cmap (exclusive scan of exists) -> renumbered vcom; super weights.
+__global__ void k_apply_renumber(uint32_t* __restrict__ vcom, int64_t n, const int64_t* __restrict__ cmap) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
+        vcom[v] = (uint32_t)cmap[vcom[v]];
+}
+
+__global__ void k_super_weights(const int32_t* __restrict__ exists, const int64_t* __restrict__ cmap,
+                                const unsigned long long* __restrict__ ctot, int64_t n,
+                                long long* __restrict__ sweight) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x)
+        if (exists[c]) sweight[cmap[c]] = (long long)ctot[c];
+}
+
+// Inter-community edges: counts per vertex, then keys in CSR order.
+__global__ void k_inter_count(const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
+                              const uint32_t* __restrict__ vcom, int64_t n, int32_t* __restrict__ cnt) {
+    const int lane = threadIdx.x & 31;
+    const int64_t wid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t u = wid; u < n; u += nw) {
+        const uint32_t cu = vcom[u];
+        int c = 0;
+        for (int64_t e = rp[u] + lane; e < rp[u + 1]; e += 32) c += (vcom[col[e]] != cu);
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xFFFFFFFFu, c, o);
+        if (lane == 0) cnt[u] = c;
+    }
+}
+
+__global__ void k_inter_fill(const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
+                             const uint32_t* __restrict__ vcom, int64_t n, const int64_t* __restrict__ off,
+                             uint64_t* __restrict__ keys) {
+    const int lane = threadIdx.x & 31;
+    const int64_t wid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    for (int64_t u = wid; u < n; u += nw) {
+        const uint32_t cu = vcom[u];
+        int64_t o = off[u];
+        for (int64_t e0 = rp[u]; e0 < rp[u + 1]; e0 += 32) {
+            const int64_t e = e0 + lane;
+            uint32_t cv = cu;
+            if (e < rp[u + 1]) cv = vcom[col[e]];
+            const bool hit = cv != cu;
+            const unsigned m = __ballot_sync(0xFFFFFFFFu, hit);
+            if (hit) keys[o + __popc(m & lt)] = ((uint64_t)cu << 32) | cv;
+            o += __popc(m);
+        }
+    }
+}
+
+// Run-length encode sorted keys: unique flags.
+__global__ void k_rle_flags(const uint64_t* __restrict__ keys, int64_t m, int32_t* __restrict__ flag) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
+        flag[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1 : 0;
+}
+
+__global__ void k_rle_emit(const uint64_t* __restrict__ keys, int64_t m, const int32_t* __restrict__ flag,
+                           const int64_t* __restrict__ pos, int64_t nuniq, uint32_t* __restrict__ snbr,
+                           uint32_t* __restrict__ sw, int32_t* __restrict__ sdeg, int64_t* __restrict__ start) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        if (!flag[i]) continue;
+        const int64_t p = pos[i];
+        snbr[p] = (uint32_t)(keys[i] & 0xFFFFFFFFull);
+        start[p] = i;
+        atomicAdd(&sdeg[keys[i] >> 32], 1);
+    }
+}
+
+__global__ void k_rle_weights(const int64_t* __restrict__ start, int64_t nuniq, int64_t m, uint32_t* __restrict__ sw) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nuniq; p += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = (p + 1 < nuniq) ? start[p + 1] : m;
+        sw[p] = (uint32_t)(e - start[p]);
+    }
+}
+
+// Active communities (super-degree > 0), in id order.
+__global__ void k_active_flags(const int32_t* __restrict__ sdeg, int64_t C, int32_t* __restrict__ flag) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C; c += (int64_t)gridDim.x * blockDim.x)
+        flag[c] = sdeg[c] > 0 ? 1 : 0;
+}
+
+__global__ void k_active_emit(const int32_t* __restrict__ flag, const int64_t* __restrict__ pos, int64_t C,
+                              uint32_t* __restrict__ active) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C; c += (int64_t)gridDim.x * blockDim.x)
+        if (flag[c]) active[pos[c]] = (uint32_t)c;
+}
+
+// Start index in `active` of every batch of `batch` communities.
+__global__ void k_batch_starts(const uint32_t* __restrict__ active, int64_t na, int64_t nbatch, int64_t batch,
+                               int64_t* __restrict__ bstart) {
+    for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b <= nbatch; b += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t lo_c = (uint64_t)(b * batch);
+        int64_t lo = 0, hi = na;
+        while (lo < hi) {
+            const int64_t mid = (lo + hi) >> 1;
+            if ((uint64_t)active[mid] < lo_c) lo = mid + 1; else hi = mid;
+        }
+        bstart[b] = lo;
+    }
+}
+
+struct SmArgs {
+    const int64_t* soff;
+    const uint32_t* snbr;
+    const uint32_t* sw;
+    const long long* sweight;     // kc per community
+    uint32_t* scomm;
+    unsigned long long* sctot;    // int64 totals
+    const uint32_t* active;
+    const int64_t* bstart;
+    int64_t nbatch;
+    uint32_t* proposed;
+    double* pdelta;
+    double M, R;
+    uint32_t* gkeys;              // per-warp global tables for big super-nodes
+    uint32_t* gvals;
+    int64_t gcap;
+};
+
+constexpr int kSmSmall = 256;     // per-warp shared table slots
+
+// Proposal for super-node c by one warp (proposals of :2264-2302).
+__device__ void super_propose(const SmArgs& a, uint32_t c, uint32_t* tk, uint32_t* tv, uint32_t* gk, uint32_t* gv) {
+    const int lane = threadIdx.x & 31;
+    const int64_t b = a.soff[c], e = a.soff[c + 1];
+    const int64_t deg = e - b;
+    uint32_t H = 64;
+    while ((int64_t)H < 2 * deg) H <<= 1;
+    uint32_t *k = tk, *v = tv;
+    if (H > (uint32_t)kSmSmall) { k = gk; v = gv; }
+    const uint32_t mask = H - 1;
+    for (uint32_t i = lane; i < H; i += 32) { k[i] = kNone; v[i] = 0; }
+    __syncwarp();
+    for (int64_t i0 = b; i0 < e; i0 += 32) {
+        uint32_t key = kNone, wgt = 0;
+        if (i0 + lane < e) {
+            key = a.scomm[a.snbr[i0 + lane]];
+            wgt = a.sw[i0 + lane];
+        }
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, key);
+        uint32_t sum = wgt;
+        // sum weights of peers (small groups): leader gathers by shuffles
+        for (int l = 0; l < 32; ++l) {
+            const uint32_t ow = __shfl_sync(0xFFFFFFFFu, wgt, l);
+            if (l != lane && ((peers >> l) & 1u)) sum += ow;
+        }
+        if (key != kNone && lane == __ffs(peers) - 1) table_add(k, v, mask, key, sum);
+    }
+    __syncwarp();
+    const uint32_t d = a.scomm[c];
+    const double kc = (double)a.sweight[c];
+    const double sigma_d = (double)(long long)a.sctot[d];
+    const double removal = __ddiv_rn(__dmul_rn(__dmul_rn(a.R, kc), __dsub_rn(sigma_d, kc)), a.M);
+    const double kc_to_d = (double)table_get(k, v, mask, d);
+    double best_d = 0.0;
+    uint32_t best_c = d;
+    for (uint32_t i = lane; i < H; i += 32) {
+        const uint32_t ek = k[i];
+        if (ek == kNone) continue;
+        const double kce = (double)v[i];
+        double add;
+        if (ek == d) {
+            add = __dsub_rn(kc_to_d, removal);
+        } else {
+            const double se = (double)(long long)a.sctot[ek];
+            add = __dsub_rn(kce, __ddiv_rn(__dmul_rn(__dmul_rn(a.R, kc), se), a.M));
+        }
+        const double dl = __dadd_rn(__dsub_rn(add, removal), kc_to_d);
+        if (better(dl, ek, best_d, best_c)) { best_d = dl; best_c = ek; }
+    }
+    warp_argmax(best_d, best_c);
+    if (lane == 0) {
+        a.proposed[c] = best_c;
+        a.pdelta[c] = best_d;
+    }
+    __syncwarp();
+}
+
+__device__ __forceinline__ void super_commit(const SmArgs& a, uint32_t c, int* moves) {
+    const uint32_t d = a.scomm[c];
+    const uint32_t best = a.proposed[c];
+    if (best == d || !(a.pdelta[c] > 0.0)) return;
+    const long long kc = a.sweight[c];
+    atomicAdd(&a.sctot[d], (unsigned long long)(-kc));
+    atomicAdd(&a.sctot[best], (unsigned long long)kc);
+    a.scomm[c] = best;
+    atomicAdd(moves, 1);
+}
+
+// Whole super-move in one CTA: batches in order, propose / barrier / commit /
+// barrier; iterations stop early when a full iteration moves nothing.
+__global__ void __launch_bounds__(1024)
+k_super_move_single(SmArgs a, int max_iter, int* iters_out, long long* moves_out) {
+    extern __shared__ uint32_t sm_smem[];  // 32 warps x (keys, vals) x kSmSmall
+    __shared__ int moves;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    long long total_moves = 0;
+    int it = 0;
+    for (; it < max_iter; ++it) {
+        if (threadIdx.x == 0) moves = 0;
+        __syncthreads();
+        for (int64_t bt = 0; bt < a.nbatch; ++bt) {
+            const int64_t lo = a.bstart[bt], hi = a.bstart[bt + 1];
+            if (lo == hi) continue;
+            uint32_t* tk = sm_smem + (size_t)w * 2 * kSmSmall;
+            for (int64_t i = lo + w; i < hi; i += nw)
+                super_propose(a, a.active[i], tk, tk + kSmSmall, a.gkeys + (int64_t)w * a.gcap,
+                              a.gvals + (int64_t)w * a.gcap);
+            __syncthreads();
+            for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) super_commit(a, a.active[i], &moves);
+            __syncthreads();
+        }
+        const int m = moves;
+        total_moves += m;
+        __syncthreads();
+        if (m == 0) { ++it; break; }
+    }
+    (void)lane;
+    if (threadIdx.x == 0) {
+        *iters_out = it;
+        *moves_out = total_moves;
+    }
+}
+
+// Multi-CTA variant: one launch pair per batch.
+__global__ void k_super_propose_batch(SmArgs a, int64_t bt) {
+    __shared__ uint32_t tk[8][kSmSmall];
+    __shared__ uint32_t tv[8][kSmSmall];
+    const int w = threadIdx.x >> 5;
+    const int64_t lo = a.bstart[bt], hi = a.bstart[bt + 1];
+    const int64_t gw = (int64_t)blockIdx.x * 8 + w;
+    const int64_t nwt = (int64_t)gridDim.x * 8;
+    for (int64_t i = lo + gw; i < hi; i += nwt)
+        super_propose(a, a.active[i], tk[w], tv[w], a.gkeys + gw * a.gcap, a.gvals + gw * a.gcap);
+}
+
+__global__ void k_super_commit_batch(SmArgs a, int64_t bt, int* moves) {
+    const int64_t lo = a.bstart[bt], hi = a.bstart[bt + 1];
+    for (int64_t i = lo + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < hi; i += (int64_t)gridDim.x * blockDim.x)
+        super_commit(a, a.active[i], moves);
+}
+
+// Map back and first-occurrence renumber (:2389-2419).
+__global__ void k_remap(uint32_t* __restrict__ vcom, int64_t n, const uint32_t* __restrict__ scomm,
+                        int32_t* __restrict__ firstpos) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t c = scomm[vcom[v]];
+        vcom[v] = c;
+        atomicMin(&firstpos[c], (int32_t)v);
+    }
+}
+
+__global__ void k_first_flags(const uint32_t* __restrict__ vcom, int64_t n, const int32_t* __restrict__ firstpos,
+                              int32_t* __restrict__ flag) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
+        flag[v] = firstpos[vcom[v]] == (int32_t)v ? 1 : 0;
+}
+
+__global__ void k_first_apply(uint32_t* __restrict__ vcom, int64_t n, const int32_t* __restrict__ firstpos,
+                              const int64_t* __restrict__ rk) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
+        vcom[v] = (uint32_t)rk[firstpos[vcom[v]]];
+}
+
+__global__ void k_ctot_from_members(const int64_t* __restrict__ rp, const uint32_t* __restrict__ vcom, int64_t n,
+                                    unsigned long long* __restrict__ ctot) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t d = rp[v + 1] - rp[v];
+        if (d) atomicAdd(&ctot[vcom[v]], (unsigned long long)d);
+    }
+}
+
+__global__ void k_init_state(const int64_t* __restrict__ rp, int64_t n, uint32_t* __restrict__ vcom,
+                             unsigned long long* __restrict__ ctot, uint8_t* __restrict__ vaff) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        vcom[v] = (uint32_t)v;
+        ctot[v] = (unsigned long long)(rp[v + 1] - rp[v]);
+        vaff[v] = 1;
+    }
+}
+
+__global__ void k_max_degree(const int64_t* __restrict__ rp, int64_t n, unsigned long long* __restrict__ out) {
+    unsigned long long m = 0;
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned long long d = (unsigned long long)(rp[v + 1] - rp[v]);
+        m = d > m ? d : m;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long t = __shfl_xor_sync(0xFFFFFFFFu, m, o);
+        m = t > m ? t : m;
+    }
+    if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+__global__ void k_hub_flags(const int64_t* __restrict__ rp, int64_t n, int32_t* __restrict__ flag) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
+        flag[v] = (rp[v + 1] - rp[v]) > kWarpMaxDeg ? 1 : 0;
+}
+
+__global__ void k_hub_emit(const int32_t* __restrict__ flag, const int64_t* __restrict__ pos, int64_t n,
+                           uint32_t* __restrict__ hubs) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
+        if (flag[v]) hubs[pos[v]] = (uint32_t)v;
+}
+
+template <typename T>
+T read_dev(const T* p, cudaStream_t s) {
+    T h;
+    GB_CUDA(cudaMemcpyAsync(&h, p, sizeof(T), cudaMemcpyDeviceToHost, s));
+    GB_CUDA(cudaStreamSynchronize(s));
+    return h;
+}
+
+float elapsed(cudaEvent_t a, cudaEvent_t b) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+}
+
+}  // namespace
+
+double auto_resolution_device(const int64_t* row_ptr, int64_t n, int64_t nnz, cudaStream_t s);
+
+void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gbgpu_stats* st, cudaStream_t s) {
+    const int64_t n = g.n;
+    if (n == 0) return;
+    GB_REQUIRE(n < (int64_t)0x7FFFFFFF, GBGPU_E_OVERFLOW, "graph has more vertices than int32 ids can name");
+    int64_t launches = 0;
+    const int64_t m = g.nnz / 2;
+    const double M = p.total_edges_m ? std::max(1.0, (double)m) : (double)m / 2.0;
+    const double R = p.resolution;
+
+    cudaEvent_t e0, e1, ea, eb;
+    GB_CUDA(cudaEventCreate(&e0));
+    GB_CUDA(cudaEventCreate(&e1));
+    GB_CUDA(cudaEventCreate(&ea));
+    GB_CUDA(cudaEventCreate(&eb));
+    GB_CUDA(cudaEventRecord(e0, s));
+    double lm_ms = 0.0, agg_ms = 0.0;
+
+    DevBuf<unsigned long long> ctot(n, s);
+    DevBuf<uint8_t> vaff(n, s);
+    DevBuf<double> dacc(1, s);
+    DevBuf<unsigned long long> macc(1, s);
+    k_init_state<<<grid_for(n, kT), kT, 0, s>>>(g.row_ptr, n, vcom, ctot, vaff);
+    GB_LAUNCH_CHECK();
+    ++launches;
+
+    // Hub list (degree > kWarpMaxDeg), id order; host copy for chunk ranges.
+    std::vector<uint32_t> hubs_h;
+    DevBuf<uint32_t> hubs;
+    int64_t max_hub_deg = 0;
+    {
+        DevBuf<int32_t> flag(n, s);
+        DevBuf<int64_t> pos(n + 1, s);
+        k_hub_flags<<<grid_for(n, kT), kT, 0, s>>>(g.row_ptr, n, flag);
+        GB_LAUNCH_CHECK();
+        exclusive_scan_i32_to_i64(flag, pos, n, pos.get() + n, s);
+        const int64_t nh = read_dev(pos.get() + n, s);
+        launches += 4;
+        if (nh > 0) {
+            hubs.alloc(nh, s);
+            k_hub_emit<<<grid_for(n, kT), kT, 0, s>>>(flag, pos, n, hubs);
+            GB_LAUNCH_CHECK();
+            ++launches;
+            hubs_h.resize(nh);
+            GB_CUDA(cudaMemcpyAsync(hubs_h.data(), hubs.get(), nh * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+            DevBuf<unsigned long long> md(1, s);
+            GB_CUDA(cudaMemsetAsync(md, 0, sizeof(unsigned long long), s));
+            k_max_degree<<<grid_for(n, kT), kT, 0, s>>>(g.row_ptr, n, md);
+            GB_LAUNCH_CHECK();
+            max_hub_deg = (int64_t)read_dev(md.get(), s);
+            launches += 1;
+        }
+    }
+    int64_t hub_gcap = 0;
+    if (max_hub_deg * 2 > kHubSmemSlots) {
+        hub_gcap = 1024;
+        while (hub_gcap < 2 * max_hub_deg) hub_gcap <<= 1;
+    }
+    const int hub_grid = (int)std::min<int64_t>(std::max<int64_t>(1, (int64_t)hubs_h.size()), kNumSMs);
+    DevBuf<uint32_t> hub_gk(hub_gcap ? hub_grid * hub_gcap : 0, s), hub_gv(hub_gcap ? hub_grid * hub_gcap : 0, s);
+    const int hub_smem = 2 * kHubSmemSlots * (int)sizeof(uint32_t);
+    GB_CUDA(cudaFuncSetAttribute(k_local_move_hub, cudaFuncAttributeMaxDynamicSharedMemorySize, hub_smem));
+    const int lm_smem = kLmWarpsPerBlock * 2 * kWarpHash * (int)sizeof(uint32_t);
+    GB_CUDA(cudaFuncSetAttribute(k_local_move_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, lm_smem));
+    const int sm_smem = 32 * 2 * kSmSmall * (int)sizeof(uint32_t);
+    GB_CUDA(cudaFuncSetAttribute(k_super_move_single, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_smem));
+
+    LmArgs la{g.row_ptr, g.col, vcom, ctot, vaff, M, R, dacc, macc};
+    const int64_t chunk = p.chunk_vertices > 0 ? p.chunk_vertices : n;
+
+    auto local_move = [&](double tolerance) -> int {
+        int iters = 0;
+        for (int it = 0; it < p.max_iterations; ++it) {
+            GB_CUDA(cudaMemsetAsync(dacc, 0, sizeof(double), s));
+            GB_CUDA(cudaMemsetAsync(macc, 0, sizeof(unsigned long long), s));
+            size_t hcur = 0;
+            for (int64_t b = 0; b < n; b += chunk) {
+                const int64_t e = std::min(n, b + chunk);
+                const int64_t warps = e - b;
+                const int grid = (int)std::min<int64_t>(ceil_div(warps, kLmWarpsPerBlock), (int64_t)kNumSMs * 16);
+                k_local_move_warp<<<grid, kLmWarpsPerBlock * 32, lm_smem, s>>>(la, b, e);
+                GB_LAUNCH_CHECK();
+                ++launches;
+                const size_t h0 = hcur;
+                while (hcur < hubs_h.size() && (int64_t)hubs_h[hcur] < e) ++hcur;
+                if (hcur > h0) {
+                    const int hg = (int)std::min<size_t>(hcur - h0, (size_t)hub_grid);
+                    k_local_move_hub<<<hg, kHubThreads, hub_smem, s>>>(la, hubs, (int64_t)h0, (int64_t)hcur, hub_gk,
+                                                                       hub_gv, hub_gcap);
+                    GB_LAUNCH_CHECK();
+                    ++launches;
+                }
+            }
+            ++iters;
+            const double total = read_dev(dacc.get(), s);
+            if (total <= tolerance) break;
+        }
+        return iters;
+    };
+
+    double tolerance = p.tolerance;
+    int64_t prev = n;
+    int pass = 0;
+    int total_iters = 0;
+    int64_t pass0_comms = 0, aggregated = 0, super_moves = 0;
+    int super_iters = 0;
+    DevBuf<int32_t> exists(n, s);
+    DevBuf<int64_t> cmap(n + 1, s);
+    for (; pass < p.max_passes && M > 0; ++pass) {
+        GB_CUDA(cudaEventRecord(ea, s));
+        const int iters = local_move(tolerance);
+        GB_CUDA(cudaEventRecord(eb, s));
+        GB_CUDA(cudaEventSynchronize(eb));
+        lm_ms += elapsed(ea, eb);
+        total_iters += iters;
+
+        // countCommunities + renumber.
+        GB_CUDA(cudaMemsetAsync(exists, 0, n * sizeof(int32_t), s));
+        k_mark_exists<<<grid_for(n, kT), kT, 0, s>>>(vcom, n, exists);
+        GB_LAUNCH_CHECK();
+        exclusive_scan_i32_to_i64(exists, cmap, n, cmap.get() + n, s);
+        const int64_t C = read_dev(cmap.get() + n, s);
+        launches += 4;
+        if (pass == 0) pass0_comms = C;
+        if (pass >= p.max_passes - 1) break;
+
+        GB_CUDA(cudaEventRecord(ea, s));
+        DevBuf<long long> sweight(C, s);
+        k_super_weights<<<grid_for(n, kT), kT, 0, s>>>(exists, cmap, ctot, n, sweight);
+        GB_LAUNCH_CHECK();
+        k_apply_renumber<<<grid_for(n, kT), kT, 0, s>>>(vcom, n, cmap);
+        GB_LAUNCH_CHECK();
+        launches += 2;
+
+        // Super-graph adjacency (inter-community edges only, :2184-2224).
+        DevBuf<int32_t> icnt(n, s);
+        DevBuf<int64_t> ioff(n + 1, s);
+        k_inter_count<<<grid_for(n * 32, kT), kT, 0, s>>>(g.row_ptr, g.col, vcom, n, icnt);
+        GB_LAUNCH_CHECK();
+        exclusive_scan_i32_to_i64(icnt, ioff, n, ioff.get() + n, s);
+        const int64_t ninter = read_dev(ioff.get() + n, s);
+        launches += 4;
+        DevBuf<uint64_t> ikeys(ninter, s);
+        DevBuf<int32_t> sdeg(C, s);
+        DevBuf<int64_t> soff(C + 1, s);
+        GB_CUDA(cudaMemsetAsync(sdeg, 0, C * sizeof(int32_t), s));
+        DevBuf<uint32_t> snbr, sw;
+        int64_t nuniq = 0;
+        if (ninter > 0) {
+            k_inter_fill<<<grid_for(n * 32, kT), kT, 0, s>>>(g.row_ptr, g.col, vcom, n, ioff, ikeys);
+            GB_LAUNCH_CHECK();
+            const int cb = bits_for((uint64_t)(C > 0 ? C - 1 : 0));
+            radix_sort_keys_u64(ikeys, ninter, 32 + cb, s);
+            DevBuf<int32_t> uflag(ninter, s);
+            DevBuf<int64_t> upos(ninter + 1, s);
+            k_rle_flags<<<grid_for(ninter, kT), kT, 0, s>>>(ikeys, ninter, uflag);
+            GB_LAUNCH_CHECK();
+            exclusive_scan_i32_to_i64(uflag, upos, ninter, upos.get() + ninter, s);
+            nuniq = read_dev(upos.get() + ninter, s);
+            snbr.alloc(nuniq, s);
+            sw.alloc(nuniq, s);
+            DevBuf<int64_t> ustart(nuniq, s);
+            k_rle_emit<<<grid_for(ninter, kT), kT, 0, s>>>(ikeys, ninter, uflag, upos, nuniq, snbr, sw, sdeg, ustart);
+            GB_LAUNCH_CHECK();
+            k_rle_weights<<<grid_for(nuniq, kT), kT, 0, s>>>(ustart, nuniq, ninter, sw);
+            GB_LAUNCH_CHECK();
+            launches += 8 + 3 * ((32 + cb + 7) / 8);
+        }
+        {
+            // soff = exclusive scan of sdeg (int32 -> int64)
+            exclusive_scan_i32_to_i64(sdeg, soff, C, soff.get() + C, s);
+            launches += 3;
+        }
+
+        // Batched super-move.
+        DevBuf<uint32_t> scomm(C, s);
+        DevBuf<unsigned long long> sctot(C, s);
+        iota_u32(scomm, C, s);
+        GB_CUDA(cudaMemcpyAsync(sctot, sweight, C * sizeof(long long), cudaMemcpyDeviceToDevice, s));
+        DevBuf<int32_t> aflag(C, s);
+        DevBuf<int64_t> apos(C + 1, s);
+        k_active_flags<<<grid_for(C, kT), kT, 0, s>>>(sdeg, C, aflag);
+        GB_LAUNCH_CHECK();
+        exclusive_scan_i32_to_i64(aflag, apos, C, apos.get() + C, s);
+        const int64_t na = read_dev(apos.get() + C, s);
+        launches += 5;
+        const int super_max_iter = std::min(3, p.max_iterations);
+        if (na > 0 && super_max_iter > 0) {
+            DevBuf<uint32_t> active(na, s);
+            k_active_emit<<<grid_for(C, kT), kT, 0, s>>>(aflag, apos, C, active);
+            GB_LAUNCH_CHECK();
+            const int64_t batch = std::max(1, p.super_move_batch);
+            const int64_t nbatch = ceil_div(C, batch);
+            DevBuf<int64_t> bstart(nbatch + 1, s);
+            k_batch_starts<<<grid_for(nbatch + 1, kT), kT, 0, s>>>(active, na, nbatch, batch, bstart);
+            GB_LAUNCH_CHECK();
+            DevBuf<uint32_t> proposed(C, s);
+            DevBuf<double> pdelta(C, s);
+            // Largest super-degree decides the per-warp global table size.
+            int32_t max_sdeg = 0;
+            {
+                std::vector<int32_t> sd(C);
+                GB_CUDA(cudaMemcpyAsync(sd.data(), sdeg.get(), C * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+                GB_CUDA(cudaStreamSynchronize(s));
+                for (int32_t v : sd) max_sdeg = std::max(max_sdeg, v);
+            }
+            int64_t gcap = 64;
+            while (gcap < 2 * (int64_t)max_sdeg) gcap <<= 1;
+            const bool single = nuniq <= p.super_single_cta_max_edges;
+            // Per-warp global tables for super-nodes above kSmSmall / 2 neighbours,
+            // capped at 512 MB in total.
+            int64_t nwarps_total = single ? 32 : (int64_t)kNumSMs * 4 * 8;
+            if (!single && gcap > kSmSmall)
+                nwarps_total = std::max<int64_t>(8, std::min<int64_t>(nwarps_total, ((int64_t)1 << 26) / gcap) / 8 * 8);
+            DevBuf<uint32_t> gk(gcap > kSmSmall ? nwarps_total * gcap : 1, s);
+            DevBuf<uint32_t> gv(gcap > kSmSmall ? nwarps_total * gcap : 1, s);
+            SmArgs sa{soff, snbr, sw, sweight, scomm, sctot, active, bstart, nbatch, proposed, pdelta, M, R,
+                      gk, gv, gcap > kSmSmall ? gcap : 0};
+            DevBuf<int> iters_d(1, s);
+            DevBuf<long long> moves_d(1, s);
+            launches += 2;
+            if (single) {
+                k_super_move_single<<<1, 1024, sm_smem, s>>>(sa, super_max_iter, iters_d, moves_d);
+                GB_LAUNCH_CHECK();
+                ++launches;
+                super_iters += read_dev(iters_d.get(), s);
+                super_moves += read_dev(moves_d.get(), s);
+            } else {
+                std::vector<int64_t> bs(nbatch + 1);
+                GB_CUDA(cudaMemcpyAsync(bs.data(), bstart.get(), (nbatch + 1) * sizeof(int64_t),
+                                        cudaMemcpyDeviceToHost, s));
+                GB_CUDA(cudaStreamSynchronize(s));
+                DevBuf<int> mv(1, s);
+                for (int it = 0; it < super_max_iter; ++it) {
+                    GB_CUDA(cudaMemsetAsync(mv, 0, sizeof(int), s));
+                    for (int64_t bt = 0; bt < nbatch; ++bt) {
+                        const int64_t cnt = bs[bt + 1] - bs[bt];
+                        if (cnt == 0) continue;
+                        const int grid = (int)std::min<int64_t>(ceil_div(cnt, 8), nwarps_total / 8);
+                        k_super_propose_batch<<<grid, 256, 0, s>>>(sa, bt);
+                        GB_LAUNCH_CHECK();
+                        k_super_commit_batch<<<(int)std::min<int64_t>(ceil_div(cnt, 256), 1024), 256, 0, s>>>(sa, bt, mv);
+                        GB_LAUNCH_CHECK();
+                        launches += 2;
+                    }
+                    ++super_iters;
+                    const int moved = read_dev(mv.get(), s);
+                    super_moves += moved;
+                    if (moved == 0) break;
+                }
+            }
+        }
+
+        // Remap, first-occurrence renumber, community totals.
+        DevBuf<int32_t> firstpos(C, s);
+        fill_u32(reinterpret_cast<uint32_t*>(firstpos.get()), 0x7FFFFFFFu, C, s);
+        k_remap<<<grid_for(n, kT), kT, 0, s>>>(vcom, n, scomm, firstpos);
+        GB_LAUNCH_CHECK();
+        DevBuf<int32_t> fflag(n, s);
+        DevBuf<int64_t> rk(n + 1, s);
+        k_first_flags<<<grid_for(n, kT), kT, 0, s>>>(vcom, n, firstpos, fflag);
+        GB_LAUNCH_CHECK();
+        exclusive_scan_i32_to_i64(fflag, rk, n, rk.get() + n, s);
+        const int64_t merged = read_dev(rk.get() + n, s);
+        k_first_apply<<<grid_for(n, kT), kT, 0, s>>>(vcom, n, firstpos, rk);
+        GB_LAUNCH_CHECK();
+        GB_CUDA(cudaMemsetAsync(ctot, 0, n * sizeof(unsigned long long), s));
+        k_ctot_from_members<<<grid_for(n, kT), kT, 0, s>>>(g.row_ptr, vcom, n, ctot);
+        GB_LAUNCH_CHECK();
+        launches += 8;
+        GB_CUDA(cudaEventRecord(eb, s));
+        GB_CUDA(cudaEventSynchronize(eb));
+        agg_ms += elapsed(ea, eb);
+        aggregated = merged;
+        if (merged >= prev || merged == 1) break;
+        if ((double)merged / (double)prev >= p.aggregation_tolerance) break;
+        prev = merged;
+        GB_CUDA(cudaMemsetAsync(vaff, 1, n, s));
+        tolerance /= p.tolerance_drop;
+    }
+    // distinct final communities
+    GB_CUDA(cudaMemsetAsync(exists, 0, n * sizeof(int32_t), s));
+    k_mark_exists<<<grid_for(n, kT), kT, 0, s>>>(vcom, n, exists);
+    GB_LAUNCH_CHECK();
+    exclusive_scan_i32_to_i64(exists, cmap, n, cmap.get() + n, s);
+    const int64_t distinct = read_dev(cmap.get() + n, s);
+    launches += 4;
+    GB_CUDA(cudaEventRecord(e1, s));
+    GB_CUDA(cudaEventSynchronize(e1));
+    if (st) {
+        st->leiden_ms += elapsed(e0, e1);
+        st->local_move_ms += lm_ms;
+        st->aggregate_ms += agg_ms;
+        st->passes = pass + 1;
+        st->iterations = total_iters;
+        st->super_move_iterations = super_iters;
+        st->super_moves = super_moves;
+        st->pass0_communities = pass0_comms;
+        st->aggregated_communities = aggregated;
+        st->communities = distinct;
+        st->resolution = R;
+        st->kernel_launches += launches;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaEventDestroy(ea);
+    cudaEventDestroy(eb);
+}
+
+// ---- auto resolution ----
+namespace {
+__global__ void k_degree_moments(const int64_t* __restrict__ rp, int64_t n, double avg, double* __restrict__ partial) {
+    double s = 0.0;
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        const double diff = (double)(rp[v + 1] - rp[v]) - avg;
+        s += diff * diff;
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o);
+    __shared__ double ws[32];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += ws[i];
+        partial[blockIdx.x] = t;
+    }
+}
+}  // namespace
+
+double auto_resolution_device(const int64_t* row_ptr, int64_t n, int64_t nnz, cudaStream_t s) {
+    if (n == 0) return 1.0;
+    const int64_t m = nnz / 2;
+    const double avg = (double)m / (double)n;
+    const int grid = 1024;
+    DevBuf<double> partial(grid, s);
+    k_degree_moments<<<grid, kT, 0, s>>>(row_ptr, n, avg, partial);
+    GB_LAUNCH_CHECK();
+    std::vector<double> h(grid);
+    GB_CUDA(cudaMemcpyAsync(h.data(), partial.get(), grid * sizeof(double), cudaMemcpyDeviceToHost, s));
+    GB_CUDA(cudaStreamSynchronize(s));
+    double sum_sq = 0.0;
+    for (double x : h) sum_sq += x;
+    const double variance = sum_sq / (double)n;
+    const double cv = (avg > 0) ? std::sqrt(variance) / avg : 0.0;
+    double resolution = 0.5 + 0.25 * std::log10(avg + 1);
+    resolution = std::max(0.5, std::min(1.2, resolution));
+    if (cv > 2.0) {
+        const double factor = 2.0 / std::max(2.0, std::sqrt(cv));
+        resolution = std::max(0.5, resolution * factor);
+    }
+    return resolution;
+}
+
+}  // namespace gb

@@ -1,0 +1,314 @@
+// relabel.cu -- permutation validation and CSR relabel on the device.
+//
+// Validation follows BuilderBase::ValidatePermutationOrThrow
+// (bench/include/external/gapbs/builder.h:2056-2080): the reported failure is
+// the one the reference's in-order scan would meet first (an out-of-range id
+// or the second occurrence of a repeated id).  The same pass produces the
+// inverse permutation, which the relabel uses.
+//
+// Relabel follows RelabelByMapping's undirected branch (builder.h:1168-1206):
+// new row x = sorted { new_ids[v] : v in N(old(x)) }.  Remap and sort are
+// fused per row; rows are bucketed by length: one thread (<= 16 entries),
+// one warp with a shared-memory bitonic sort (<= 256), one CTA with a
+// shared-memory bitonic sort (<= 16384), and a global segmented radix sort
+// for the few longer rows.
+#include "gb_common.cuh"
+#include "gb_stages.h"
+
+namespace gb {
+
+namespace {
+
+constexpr int32_t kIntMax = 0x7FFFFFFF;
+
+__global__ void k_first_index(const int32_t* __restrict__ ids, int64_t n, int32_t* __restrict__ first,
+                              int64_t* __restrict__ oor_min) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t v = ids[i];
+        if (v < 0 || (int64_t)v >= n) {
+            atomicMin((unsigned long long*)oor_min, (unsigned long long)i);
+        } else {
+            atomicMin(&first[v], (int32_t)i);
+        }
+    }
+}
+
+__global__ void k_dup_index(const int32_t* __restrict__ ids, int64_t n, const int32_t* __restrict__ first,
+                            int64_t* __restrict__ dup_min) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t v = ids[i];
+        if (v >= 0 && (int64_t)v < n && first[v] != (int32_t)i)
+            atomicMin((unsigned long long*)dup_min, (unsigned long long)i);
+    }
+}
+
+__global__ void k_new_degrees(const int64_t* __restrict__ rp, const int32_t* __restrict__ inv, int64_t n,
+                              int64_t* __restrict__ deg_new) {
+    for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t u = inv[x];
+        deg_new[x] = rp[u + 1] - rp[u];
+    }
+}
+
+constexpr int kThreadRowMax = 16;
+constexpr int kWarpRowMax = 256;
+constexpr int kBlockRowMax = 16384;
+
+__global__ void k_relabel_rows_small(const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
+                                     const int32_t* __restrict__ new_ids, const int32_t* __restrict__ inv,
+                                     const int64_t* __restrict__ out_rp, int32_t* __restrict__ out_col,
+                                     int64_t n, int32_t* __restrict__ lists, int32_t* __restrict__ counts) {
+    // counts[0..2]: warp, block, huge list sizes; lists: 3 x n entries.
+    for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t u = inv[x];
+        const int64_t b = rp[u], d = rp[u + 1] - b;
+        if (d <= kThreadRowMax) {
+            int32_t a[kThreadRowMax];
+            for (int i = 0; i < d; ++i) {
+                const int32_t v = new_ids[col[b + i]];
+                int j = i - 1;
+                while (j >= 0 && a[j] > v) { a[j + 1] = a[j]; --j; }
+                a[j + 1] = v;
+            }
+            const int64_t o = out_rp[x];
+            for (int i = 0; i < d; ++i) out_col[o + i] = a[i];
+        } else {
+            const int which = d <= kWarpRowMax ? 0 : (d <= kBlockRowMax ? 1 : 2);
+            const int32_t slot = atomicAdd(&counts[which], 1);
+            lists[(int64_t)which * n + slot] = (int32_t)x;
+        }
+    }
+}
+
+__global__ void k_relabel_rows_warp(const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
+                                    const int32_t* __restrict__ new_ids, const int32_t* __restrict__ inv,
+                                    const int64_t* __restrict__ out_rp, int32_t* __restrict__ out_col,
+                                    const int32_t* __restrict__ list, const int32_t* __restrict__ count) {
+    constexpr int kWarps = 8;
+    __shared__ int32_t sh[kWarps][kWarpRowMax];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int32_t* s = sh[w];
+    const int32_t total = *count;
+    for (int64_t r = (int64_t)blockIdx.x * kWarps + w; r < total; r += (int64_t)gridDim.x * kWarps) {
+        const int32_t x = list[r];
+        const int32_t u = inv[x];
+        const int64_t b = rp[u];
+        const int d = (int)(rp[u + 1] - b);
+        int p = 32;
+        while (p < d) p <<= 1;
+        for (int i = lane; i < p; i += 32) s[i] = i < d ? new_ids[col[b + i]] : kIntMax;
+        __syncwarp();
+        for (int k = 2; k <= p; k <<= 1) {
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int i = lane; i < p; i += 32) {
+                    const int ixj = i ^ j;
+                    if (ixj > i) {
+                        const int32_t a = s[i], c = s[ixj];
+                        const bool asc = (i & k) == 0;
+                        if ((a > c) == asc) { s[i] = c; s[ixj] = a; }
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        const int64_t o = out_rp[x];
+        for (int i = lane; i < d; i += 32) out_col[o + i] = s[i];
+        __syncwarp();
+    }
+}
+
+__global__ void k_relabel_rows_block(const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
+                                     const int32_t* __restrict__ new_ids, const int32_t* __restrict__ inv,
+                                     const int64_t* __restrict__ out_rp, int32_t* __restrict__ out_col,
+                                     const int32_t* __restrict__ list, const int32_t* __restrict__ count) {
+    extern __shared__ int32_t s[];
+    const int32_t total = *count;
+    for (int64_t r = blockIdx.x; r < total; r += gridDim.x) {
+        const int32_t x = list[r];
+        const int32_t u = inv[x];
+        const int64_t b = rp[u];
+        const int d = (int)(rp[u + 1] - b);
+        int p = 512;
+        while (p < d) p <<= 1;
+        for (int i = threadIdx.x; i < p; i += blockDim.x) s[i] = i < d ? new_ids[col[b + i]] : kIntMax;
+        __syncthreads();
+        for (int k = 2; k <= p; k <<= 1) {
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int i = threadIdx.x; i < p; i += blockDim.x) {
+                    const int ixj = i ^ j;
+                    if (ixj > i) {
+                        const int32_t a = s[i], c = s[ixj];
+                        const bool asc = (i & k) == 0;
+                        if ((a > c) == asc) { s[i] = c; s[ixj] = a; }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        const int64_t o = out_rp[x];
+        for (int i = threadIdx.x; i < d; i += blockDim.x) out_col[o + i] = s[i];
+        __syncthreads();
+    }
+}
+
+// Long rows: keys (list index << vbits | new id) in one buffer, sorted by a
+// global radix sort, then written back per row.
+__global__ void k_huge_gather(const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
+                              const int32_t* __restrict__ new_ids, const int32_t* __restrict__ inv,
+                              const int32_t* __restrict__ list, const int64_t* __restrict__ hoff,
+                              int32_t count, int vbits, uint64_t* __restrict__ keys) {
+    for (int32_t r = blockIdx.x; r < count; r += gridDim.x) {
+        const int32_t u = inv[list[r]];
+        const int64_t b = rp[u], d = rp[u + 1] - b, o = hoff[r];
+        for (int64_t i = threadIdx.x; i < d; i += blockDim.x)
+            keys[o + i] = ((uint64_t)r << vbits) | (uint32_t)new_ids[col[b + i]];
+    }
+}
+
+__global__ void k_huge_scatter(const int32_t* __restrict__ list, const int64_t* __restrict__ hoff,
+                               const int64_t* __restrict__ out_rp, int32_t count, int vbits,
+                               const uint64_t* __restrict__ keys, int32_t* __restrict__ out_col) {
+    const uint64_t mask = (vbits >= 64) ? ~0ull : ((1ull << vbits) - 1ull);
+    for (int32_t r = blockIdx.x; r < count; r += gridDim.x) {
+        const int64_t o = out_rp[list[r]], h = hoff[r], d = hoff[r + 1] - h;
+        for (int64_t i = threadIdx.x; i < d; i += blockDim.x) out_col[o + i] = (int32_t)(keys[h + i] & mask);
+    }
+}
+
+__global__ void k_huge_degrees(const int64_t* __restrict__ rp, const int32_t* __restrict__ inv,
+                               const int32_t* __restrict__ list, int32_t count, int64_t* __restrict__ hdeg) {
+    for (int32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < count; r += gridDim.x * blockDim.x) {
+        const int32_t u = inv[list[r]];
+        hdeg[r] = rp[u + 1] - rp[u];
+    }
+}
+
+__global__ void k_set_last(int64_t* p, int64_t n, int64_t v) { p[n] = v; }
+
+// Squished-CSR check: offsets non-decreasing from 0, neighbour ids in range,
+// rows strictly increasing (sorted, no duplicates).  bad[0]: offsets,
+// bad[1]: ids out of range, bad[2]: unsorted or duplicate.
+__global__ void k_check_graph(const int64_t* __restrict__ rp, const int32_t* __restrict__ col, int64_t n,
+                              int64_t nnz, int32_t* __restrict__ bad) {
+    const int lane = threadIdx.x & 31;
+    const int64_t wid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t u = wid; u < n; u += nw) {
+        const int64_t b = rp[u], e = rp[u + 1];
+        if (lane == 0 && (b > e || b < 0 || e > nnz || (u == 0 && b != 0))) atomicOr(&bad[0], 1);
+        if (b > e || b < 0 || e > nnz) continue;
+        for (int64_t i = b + lane; i < e; i += 32) {
+            const int32_t v = col[i];
+            if (v < 0 || (int64_t)v >= n) atomicOr(&bad[1], 1);
+            if (i > b && col[i - 1] >= v) atomicOr(&bad[2], 1);
+        }
+    }
+}
+
+}  // namespace
+
+void check_graph_device(const DeviceCSR& g, cudaStream_t s) {
+    if (g.n == 0) return;
+    DevBuf<int32_t> bad(3, s);
+    GB_CUDA(cudaMemsetAsync(bad, 0, 3 * sizeof(int32_t), s));
+    k_check_graph<<<grid_for(g.n * 32, 256), 256, 0, s>>>(g.row_ptr, g.col, g.n, g.nnz, bad);
+    GB_LAUNCH_CHECK();
+    int32_t h[3];
+    GB_CUDA(cudaMemcpyAsync(h, bad.get(), sizeof(h), cudaMemcpyDeviceToHost, s));
+    GB_CUDA(cudaStreamSynchronize(s));
+    GB_REQUIRE(!h[0], GBGPU_E_INVALID, "row offsets are not a non-decreasing sequence from 0 to nnz");
+    GB_REQUIRE(!h[1], GBGPU_E_INVALID, "neighbour id out of range");
+    GB_REQUIRE(!h[2], GBGPU_E_INVALID, "rows must be sorted ascending without duplicates (squished CSR)");
+}
+
+int validate_permutation_device(const int32_t* ids, int64_t n, int32_t* inv_out, cudaStream_t s,
+                                int64_t* bad_index) {
+    if (n == 0) return 0;
+    GB_REQUIRE(n <= (int64_t)kIntMax, GBGPU_E_OVERFLOW, "graph has more vertices than int32 ids can name");
+    DevBuf<int32_t> first_local;
+    int32_t* first = inv_out;
+    if (!first) {
+        first_local.alloc(n, s);
+        first = first_local.get();
+    }
+    DevBuf<int64_t> mins(2, s);
+    fill_u32(reinterpret_cast<uint32_t*>(first), (uint32_t)kIntMax, n, s);
+    fill_i64(mins, INT64_MAX, 2, s);
+    k_first_index<<<grid_for(n, 256), 256, 0, s>>>(ids, n, first, mins.get());
+    GB_LAUNCH_CHECK();
+    k_dup_index<<<grid_for(n, 256), 256, 0, s>>>(ids, n, first, mins.get() + 1);
+    GB_LAUNCH_CHECK();
+    int64_t h[2];
+    GB_CUDA(cudaMemcpyAsync(h, mins.get(), sizeof(h), cudaMemcpyDeviceToHost, s));
+    GB_CUDA(cudaStreamSynchronize(s));
+    if (h[0] == INT64_MAX && h[1] == INT64_MAX) return 0;
+    if (h[0] < h[1]) {
+        if (bad_index) *bad_index = h[0];
+        return 1;
+    }
+    if (bad_index) *bad_index = h[1];
+    return 2;
+}
+
+void relabel_csr_device(const DeviceCSR& g, const int32_t* new_ids, const int32_t* inv,
+                        int64_t* out_rp, int32_t* out_col, cudaStream_t s, int64_t* launches) {
+    const int64_t n = g.n;
+    if (n == 0) {
+        GB_CUDA(cudaMemsetAsync(out_rp, 0, sizeof(int64_t), s));
+        return;
+    }
+    int64_t nl = 0;
+    {
+        DevBuf<int64_t> deg_new(n, s);
+        k_new_degrees<<<grid_for(n, 256), 256, 0, s>>>(g.row_ptr, inv, n, deg_new);
+        GB_LAUNCH_CHECK();
+        exclusive_scan_i64(deg_new, out_rp, n, s);
+        k_set_last<<<1, 1, 0, s>>>(out_rp, n, g.nnz);
+        GB_LAUNCH_CHECK();
+        nl += 3;
+    }
+    DevBuf<int32_t> lists(3 * n, s);
+    DevBuf<int32_t> counts(3, s);
+    GB_CUDA(cudaMemsetAsync(counts, 0, 3 * sizeof(int32_t), s));
+    k_relabel_rows_small<<<grid_for(n, 256), 256, 0, s>>>(g.row_ptr, g.col, new_ids, inv, out_rp, out_col, n,
+                                                          lists, counts);
+    GB_LAUNCH_CHECK();
+    k_relabel_rows_warp<<<kNumSMs * 8, 256, 0, s>>>(g.row_ptr, g.col, new_ids, inv, out_rp, out_col, lists.get(),
+                                                    counts.get());
+    GB_LAUNCH_CHECK();
+    const int block_smem = kBlockRowMax * (int)sizeof(int32_t);
+    static bool attr_set = false;
+    if (!attr_set) {
+        GB_CUDA(cudaFuncSetAttribute(k_relabel_rows_block, cudaFuncAttributeMaxDynamicSharedMemorySize, block_smem));
+        attr_set = true;
+    }
+    k_relabel_rows_block<<<kNumSMs * 2, 1024, block_smem, s>>>(g.row_ptr, g.col, new_ids, inv, out_rp, out_col,
+                                                               lists.get() + n, counts.get() + 1);
+    GB_LAUNCH_CHECK();
+    nl += 3;
+    int32_t huge = 0;
+    GB_CUDA(cudaMemcpyAsync(&huge, counts.get() + 2, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    GB_CUDA(cudaStreamSynchronize(s));
+    if (huge > 0) {
+        const int32_t* hlist = lists.get() + 2 * n;
+        DevBuf<int64_t> hoff(huge + 1, s);
+        k_huge_degrees<<<grid_for(huge, 256), 256, 0, s>>>(g.row_ptr, inv, hlist, huge, hoff);
+        GB_LAUNCH_CHECK();
+        exclusive_scan_i64_total(hoff, hoff, huge, hoff.get() + huge, s);
+        int64_t total = 0;
+        GB_CUDA(cudaMemcpyAsync(&total, hoff.get() + huge, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        GB_CUDA(cudaStreamSynchronize(s));
+        const int vbits = bits_for((uint64_t)(n > 1 ? n - 1 : 1));
+        const int kbits = vbits + bits_for((uint64_t)huge);
+        DevBuf<uint64_t> keys(total, s);
+        k_huge_gather<<<kNumSMs * 4, 256, 0, s>>>(g.row_ptr, g.col, new_ids, inv, hlist, hoff, huge, vbits, keys);
+        GB_LAUNCH_CHECK();
+        radix_sort_keys_u64(keys, total, kbits, s);
+        k_huge_scatter<<<kNumSMs * 4, 256, 0, s>>>(hlist, hoff, out_rp, huge, vbits, keys, out_col);
+        GB_LAUNCH_CHECK();
+        nl += 6 + 3 * ((kbits + 7) / 8);
+    }
+    if (launches) *launches += nl;
+}
+
+}  // namespace gb

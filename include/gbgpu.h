@@ -1,0 +1,191 @@
+/*
+ * gbgpu.h -- C ABI of the GB300 implementation of GraphBrew's algorithm-12
+ * mapping path ("-o 12:leiden:compose:...").
+ *
+ * Every entry point takes plain pointers and sizes and returns a gbgpu_status.
+ * Graph inputs are undirected CSR graphs as the GAPBS builder produces them
+ * (int64 row offsets, int32 neighbour ids, each undirected edge stored in both
+ * rows, rows sorted ascending, no duplicates, no self-loops).  Pointers are
+ * host pointers unless GBGPU_DEVICE_POINTERS is set in `flags`, in which case
+ * every array argument of that call is a device pointer on the context's
+ * device and the call does no host<->device copies.
+ *
+ * A context owns one CUDA stream and a stream-ordered memory pool.  Calls on
+ * one context are not thread-safe; use one context per host thread.
+ *
+ * Reference interfaces replaced (paths relative to the GraphBrew project root):
+ *   gbgpu_generate_mapping  -> graphbrew::generateGraphBrewMapping<uint32_t>
+ *                              (bench/include/graphbrew/reorder/reorder_graphbrew.h:7836-8013),
+ *                              reached from BuilderBase::GenerateGraphBrewMappingUnified
+ *                              (bench/include/external/gapbs/builder.h:3669-3783)
+ *   gbgpu_leiden            -> graphbrew::runGraphBrew (reorder_graphbrew.h:7238-7571)
+ *   gbgpu_compose           -> graphbrew::orderCompose (reorder_graphbrew.h:6286-7087)
+ *   gbgpu_relabel_csr       -> BuilderBase::RelabelByMapping (builder.h:1046-1206)
+ *   gbgpu_validate_permutation -> BuilderBase::ValidatePermutationOrThrow (builder.h:2042-2081)
+ *   gbgpu_parse_config      -> graphbrew::parseGraphBrewCliConfig + graphBrewEffectiveConfigJson
+ *                              (reorder_graphbrew_parser.h:714-912, reorder_graphbrew.h:693-775)
+ *   gbgpu_auto_resolution   -> computeAutoResolution (reorder_types.h:2743-2780)
+ *   gbgpu_fingerprint       -> BuilderBase::MappingFingerprint (builder.h:1398-1411)
+ */
+#ifndef GBGPU_H_
+#define GBGPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    GBGPU_OK = 0,
+    GBGPU_E_INVALID = 1,        /* malformed argument or graph (std::invalid_argument) */
+    GBGPU_E_UNSUPPORTED = 2,    /* option valid in the grammar but not on this path */
+    GBGPU_E_CUDA = 3,           /* CUDA runtime error */
+    GBGPU_E_NOMEM = 4,          /* device or host allocation failed */
+    GBGPU_E_NOT_PERMUTATION = 5,/* validation failed (std::runtime_error) */
+    GBGPU_E_PARSE = 6,          /* option grammar rejected a token (std::invalid_argument) */
+    GBGPU_E_OVERFLOW = 7,       /* size beyond a documented limit (std::overflow_error) */
+    GBGPU_E_TIMEOUT = 8         /* a bounded device wait gave up */
+} gbgpu_status;
+
+/* flags */
+#define GBGPU_DEVICE_POINTERS 0x1u   /* all array arguments are device pointers */
+#define GBGPU_QUIET 0x2u             /* no stdout progress lines */
+
+typedef struct gbgpu_ctx gbgpu_ctx;
+
+/* Algorithm-12 configuration after option parsing (the fields of
+ * GraphBrewConfig that the mapping path reads, reorder_graphbrew.h:398-603). */
+typedef struct {
+    double resolution;
+    double tolerance;
+    double aggregation_tolerance;
+    double tolerance_drop;
+    int32_t max_iterations;
+    int32_t max_passes;
+    int32_t total_edges_m;          /* totalm */
+    int32_t gve_aggregation;        /* gvecsr */
+    int32_t use_refinement;
+    int32_t refinement_depth;
+    int32_t deterministic;          /* cd_serial (1) / cd_parallel (0) */
+    int32_t super_move_batch;       /* sgmb<k> */
+    int32_t ordering;               /* OrderingStrategy ordinal */
+    int32_t super_graph_order;      /* SuperGraphOrder ordinal */
+    int32_t community_order;        /* CommunityOrder ordinal */
+    int32_t intra_order;            /* IntraCommunityOrder ordinal */
+    int32_t refinement_pass;        /* RefinementPass ordinal */
+    int32_t gorder_window;
+    int32_t gorder_fallback;
+    int32_t algorithm;              /* 0 Leiden, 1 Rabbit */
+} gbgpu_config;
+
+/* Per-call statistics; times are device (CUDA event) milliseconds. */
+typedef struct {
+    double total_ms;
+    double leiden_ms;
+    double local_move_ms;
+    double aggregate_ms;
+    double compose_ms;
+    double intra_ms;
+    double validate_ms;
+    double relabel_ms;
+    double h2d_ms;
+    double d2h_ms;
+    int32_t passes;
+    int32_t iterations;
+    int32_t super_move_iterations;
+    int32_t reserved0;
+    int64_t super_moves;
+    int64_t pass0_communities;
+    int64_t aggregated_communities;
+    int64_t communities;            /* distinct ids in the final membership */
+    int64_t num_communities;        /* max id + 1 (orderCompose's numComm) */
+    int64_t isolated;
+    int64_t gorder_communities;
+    int64_t gorder_vertices;
+    int64_t gorder_max_community;
+    int64_t fallback_communities;
+    int64_t fallback_vertices;
+    int64_t largest_community;
+    int64_t bfs_levels;
+    int64_t kernel_launches;        /* kernels this call launched */
+    double resolution;              /* resolution used */
+} gbgpu_stats;
+
+/* Context lifetime.  device < 0 selects the current device. */
+int gbgpu_ctx_create(gbgpu_ctx** out, int device);
+void gbgpu_ctx_destroy(gbgpu_ctx* ctx);
+/* Message of the last failing call on this context ("" if none). */
+const char* gbgpu_last_error(const gbgpu_ctx* ctx);
+/* Use a caller-owned cudaStream_t (NULL restores the context's own stream). */
+int gbgpu_set_stream(gbgpu_ctx* ctx, void* cuda_stream);
+/* Block until the context's stream is idle. */
+int gbgpu_synchronize(gbgpu_ctx* ctx);
+
+/* Parse the tokens after "12:" ("leiden:compose:...:2:2").  On success the
+ * effective-config JSON (graphbrew_config/v3, byte-identical to the
+ * reference's) is written to json_out when json_cap > 0.  On failure the
+ * reference's exception text is written there instead. */
+int gbgpu_parse_config(const char* opts, double auto_resolution, gbgpu_config* out,
+                       char* json_out, size_t json_cap);
+
+/* Automatic resolution from the degree distribution.  The variance is summed
+ * on the device in a fixed order, so the result may differ from a serial sum
+ * in the last bits. */
+int gbgpu_auto_resolution(gbgpu_ctx* ctx, const int64_t* row_ptr, int64_t n, int64_t nnz,
+                          uint32_t flags, double* out);
+
+/* Full algorithm-12 mapping: Leiden, COMPOSE placement, intra-community order.
+ * new_ids_out: n entries, forward map old id -> new id.  auto_resolution < 0
+ * computes it with gbgpu_auto_resolution.  stats may be NULL. */
+int gbgpu_generate_mapping(gbgpu_ctx* ctx, const int64_t* row_ptr, const int32_t* col,
+                           int64_t n, int64_t nnz, const char* opts, double auto_resolution,
+                           int32_t* new_ids_out, gbgpu_stats* stats, uint32_t flags);
+
+/* Community detection stage only (membership_out: n entries).  The final
+ * membership is not renumbered after the last local-moving pass, exactly as
+ * the reference returns it. */
+int gbgpu_leiden(gbgpu_ctx* ctx, const int64_t* row_ptr, const int32_t* col, int64_t n,
+                 int64_t nnz, const char* opts, double resolution, uint32_t* membership_out,
+                 gbgpu_stats* stats, uint32_t flags);
+
+/* COMPOSE stage only, from a given membership (n entries). */
+int gbgpu_compose(gbgpu_ctx* ctx, const int64_t* row_ptr, const int32_t* col, int64_t n,
+                  int64_t nnz, const uint32_t* membership, const char* opts,
+                  int32_t* new_ids_out, gbgpu_stats* stats, uint32_t flags);
+
+/* Check that new_ids is a permutation of 0..n-1.  *result: 0 valid,
+ * 1 out-of-range id, 2 duplicate id (ValidatePermutationOrThrow's cases). */
+int gbgpu_validate_permutation(gbgpu_ctx* ctx, const int32_t* new_ids, int64_t n,
+                               uint32_t flags, int32_t* result);
+
+/* Rebuild the CSR under new_ids: out_row_ptr n + 1 entries, out_col nnz
+ * entries, every row sorted ascending.  org_ids_out (n entries, may be NULL)
+ * receives the inverse map new -> old (the graph's org ids after
+ * update_org_ids on a freshly built graph).  new_ids must be a permutation. */
+int gbgpu_relabel_csr(gbgpu_ctx* ctx, const int64_t* row_ptr, const int32_t* col, int64_t n,
+                      int64_t nnz, const int32_t* new_ids, int64_t* out_row_ptr,
+                      int32_t* out_col, int32_t* org_ids_out, uint32_t flags);
+
+/* The builder's mapping lifecycle after GenerateMapping (builder.h:829-940):
+ * mapping, device-side validation, relabel.  Equivalent to the three calls
+ * above on one resident copy of the graph.  out_row_ptr / out_col may be NULL
+ * to skip the relabel. */
+int gbgpu_map_and_relabel(gbgpu_ctx* ctx, const int64_t* row_ptr, const int32_t* col,
+                          int64_t n, int64_t nnz, const char* opts, double auto_resolution,
+                          int32_t* new_ids_out, int64_t* out_row_ptr, int32_t* out_col,
+                          gbgpu_stats* stats, uint32_t flags);
+
+/* FNV-1a-64 fingerprint of a forward map, on the host, as the builder prints
+ * it ("Mapping Fingerprint"). */
+uint64_t gbgpu_fingerprint(const int32_t* new_ids, int64_t n);
+
+/* Library version string. */
+const char* gbgpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBGPU_H_ */

@@ -1,0 +1,221 @@
+"""CUDA path against the oracle and the reference's golden outputs (GB300).
+
+Integer work is bit-exact: orderCompose (placement, Gorder, BFS fallback),
+RelabelByMapping, validation and the fingerprint must equal the reference's
+outputs on the same membership.  Community detection in cd_parallel mode is
+nondeterministic in the reference itself, so it is judged by invariants
+(a valid membership whose community totals match, a valid permutation) and
+by modularity against the reference's own run-to-run spread.
+"""
+import numpy as np
+import pytest
+import torch
+
+import pyoracle as po
+import graphbrew_gb300 as gb
+from graphbrew_gb300 import graphgen as gg
+from conftest import case_names
+
+pytestmark = pytest.mark.gpu
+
+SERIAL = ("leiden:compose:sg_none:comm_size_desc:intra_gorder:gw8:cd_serial:"
+          "sgmb4096:gordf5000:norefine:2:2")
+PARALLEL = SERIAL.replace("cd_serial", "cd_parallel")
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    assert torch.cuda.is_available(), "GPU tests need CUDA"
+    c = gb.Context(0)
+    yield c
+    c.close()
+
+
+def graph(g, name):
+    return g[f"{name}/row_ptr"], g[f"{name}/col"]
+
+
+def to_dev(*arrays):
+    return [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in arrays]
+
+
+@pytest.mark.parametrize("name", case_names())
+def test_compose_bit_exact(ctx, name, manifest, golden_arrays):
+    rp, col = graph(golden_arrays, name)
+    memb = golden_arrays[f"{name}/membership_serial"]
+    for key, recipe in manifest["compose_recipes"].items():
+        ids, st = ctx.order_compose(rp, col, memb, recipe)
+        np.testing.assert_array_equal(ids, golden_arrays[f"{name}/compose_{key}"], err_msg=f"{name}/{key}")
+        if "intra_gorder" in recipe:
+            gst = manifest["cases"][name]["compose"][key]["gorder_stats"]
+            assert [st["gorder_communities"], st["gorder_vertices"], st["gorder_max_community"],
+                    st["fallback_communities"], st["fallback_vertices"]] == gst
+
+
+@pytest.mark.parametrize("name", case_names())
+def test_compose_device_pointers(ctx, name, golden_arrays):
+    rp, col = graph(golden_arrays, name)
+    memb = golden_arrays[f"{name}/membership_serial"].astype(np.int32)
+    drp, dcol, dmemb = to_dev(rp, col, memb)
+    ids, _ = ctx.order_compose(drp, dcol, dmemb, SERIAL)
+    assert ids.is_cuda
+    np.testing.assert_array_equal(ids.cpu().numpy(), golden_arrays[f"{name}/compose_gorder8_f5000"])
+
+
+@pytest.mark.parametrize("name", case_names())
+def test_relabel_bit_exact(ctx, name, golden_arrays):
+    rp, col = graph(golden_arrays, name)
+    ids = golden_arrays[f"{name}/new_ids_serial"]
+    orp, ocol, org = ctx.relabel_by_mapping(rp, col, ids)
+    np.testing.assert_array_equal(orp, golden_arrays[f"{name}/relabel_row_ptr"])
+    np.testing.assert_array_equal(ocol, golden_arrays[f"{name}/relabel_col"])
+    np.testing.assert_array_equal(org, golden_arrays[f"{name}/relabel_org_ids"])
+
+
+def test_validate_permutation(ctx):
+    assert ctx.validate_permutation(np.array([2, 0, 1], dtype=np.int32)) == 0
+    assert ctx.validate_permutation(np.array([2, 3, 1], dtype=np.int32)) == 1
+    assert ctx.validate_permutation(np.array([2, 2, 1], dtype=np.int32)) == 2
+    assert ctx.validate_permutation(np.array([0, 0, 5], dtype=np.int32)) == 2
+    assert ctx.validate_permutation(np.array([5, 0, 0], dtype=np.int32)) == 1
+    assert ctx.validate_permutation(np.array([-1, 0, 1], dtype=np.int32)) == 1
+    assert ctx.validate_permutation(np.array([], dtype=np.int32)) == 0
+    big = np.random.default_rng(0).permutation(1 << 20).astype(np.int32)
+    assert ctx.validate_permutation(torch.from_numpy(big).cuda()) == 0
+    big[12345] = big[777]
+    assert ctx.validate_permutation(big) == 2
+
+
+def test_relabel_rejects_non_permutation(ctx):
+    rp = np.array([0, 1, 2], dtype=np.int64)
+    col = np.array([1, 0], dtype=np.int32)
+    with pytest.raises(RuntimeError, match="duplicate"):
+        ctx.relabel_by_mapping(rp, col, np.array([0, 0], dtype=np.int32))
+
+
+@pytest.mark.parametrize("name", case_names())
+def test_auto_resolution(ctx, name, manifest, golden_arrays):
+    rp, col = graph(golden_arrays, name)
+    assert ctx.auto_resolution(rp, col) == pytest.approx(manifest["cases"][name]["auto_resolution"], rel=1e-12)
+
+
+def _check_membership(rp, col, memb):
+    n = len(rp) - 1
+    assert memb.shape == (n,)
+    assert (memb.astype(np.int64) < n).all()
+
+
+@pytest.mark.parametrize("name", case_names())
+def test_parallel_leiden_and_mapping(ctx, name, manifest, golden_arrays):
+    rp, col = graph(golden_arrays, name)
+    case = manifest["cases"][name]
+    ar = case["auto_resolution"]
+    memb, st = ctx.run_graphbrew(rp, col, PARALLEL, ar)
+    _check_membership(rp, col, memb)
+    assert st["passes"] <= 2
+    q = po.modularity(rp, col, memb, 1.0)
+    ref_q = case["parallel_modularity_samples"] + [case["serial_modularity"]]
+    # The reference's own parallel runs spread widely on some graphs; the GPU
+    # result must not fall meaningfully below the worst of them.
+    assert q >= min(ref_q) - 0.02, (q, ref_q)
+    # Given the GPU membership, COMPOSE is exact against the oracle.
+    ids_gpu, _ = ctx.order_compose(rp, col, memb, PARALLEL)
+    ids_orc, _ = po.compose(rp, col, memb)
+    np.testing.assert_array_equal(ids_gpu, ids_orc)
+    ids, st2 = ctx.generate_mapping(rp, col, PARALLEL, ar)
+    assert po.validate_permutation(ids) == 0
+
+
+@pytest.mark.parametrize("scale,fallback", [(14, 5000), (16, 5000), (16, 300), (18, 5000)])
+def test_seeded_rmat_against_oracle(ctx, scale, fallback):
+    rp_t, col_t = gg.rmat(scale, 16, seed=100 + scale, device="cuda")
+    rp, col = rp_t.cpu().numpy(), col_t.cpu().numpy()
+    recipe = PARALLEL.replace("gordf5000", f"gordf{fallback}")
+    ar = po.auto_resolution(rp, col)
+    memb, st = ctx.run_graphbrew(rp_t, col_t, recipe, ar)
+    memb = memb.cpu().numpy().view(np.uint32)
+    _check_membership(rp, col, memb)
+    ids_gpu, cst = ctx.order_compose(rp_t, col_t, torch.from_numpy(memb.view(np.int32)).cuda(), recipe)
+    ids_orc, ost = po.compose(rp, col, memb, gorder_fallback=fallback)
+    np.testing.assert_array_equal(ids_gpu.cpu().numpy(), ids_orc)
+    assert cst["fallback_communities"] == ost.fallback_communities
+    orp, ocol, _ = ctx.relabel_by_mapping(rp_t, col_t, ids_gpu)
+    erp, ecol = po.relabel(rp, col, ids_orc)
+    np.testing.assert_array_equal(orp.cpu().numpy(), erp)
+    np.testing.assert_array_equal(ocol.cpu().numpy(), ecol)
+    q_gpu = po.modularity(rp, col, memb, 1.0)
+    m_ser, _ = po.leiden(rp, col, ar)
+    q_ser = po.modularity(rp, col, m_ser, 1.0)
+    assert q_gpu >= q_ser - 0.03, (q_gpu, q_ser)
+
+
+def test_edge_cases(ctx):
+    # empty graph
+    ids, _ = ctx.generate_mapping(np.zeros(1, dtype=np.int64), np.zeros(0, dtype=np.int32), PARALLEL, 1.0)
+    assert len(ids) == 0
+    # all isolated
+    ids, _ = ctx.generate_mapping(np.zeros(6, dtype=np.int64), np.zeros(0, dtype=np.int32), PARALLEL, 1.0)
+    assert list(ids) == [0, 1, 2, 3, 4]
+    # one edge + isolated tail
+    rp, col = gg.from_edges(4, [(1, 2)])
+    ids, _ = ctx.generate_mapping(rp.numpy(), col.numpy(), PARALLEL, 1.0)
+    memb, _ = ctx.run_graphbrew(rp.numpy(), col.numpy(), PARALLEL, 1.0)
+    np.testing.assert_array_equal(ids, po.compose(rp.numpy(), col.numpy(), memb)[0])
+
+
+@pytest.mark.parametrize("hub_degree", [40, 700, 3000, 20000, 70000])
+def test_hub_vertices(ctx, hub_degree):
+    # A star plus a ring: exercises register, shared-table and global-table
+    # accumulation, the CTA row sort and the long-row radix sort.
+    n = hub_degree + 1
+    edges = [(0, i) for i in range(1, n)] + [(i, i + 1) for i in range(1, n - 1)]
+    rp_t, col_t = gg.from_edges(n, edges)
+    rp, col = rp_t.numpy(), col_t.numpy()
+    memb, _ = ctx.run_graphbrew(rp, col, PARALLEL, 1.0)
+    ids_gpu, _ = ctx.order_compose(rp, col, memb, PARALLEL.replace("gordf5000", "gordf100"))
+    ids_orc, _ = po.compose(rp, col, memb, gorder_fallback=100)
+    np.testing.assert_array_equal(ids_gpu, ids_orc)
+    orp, ocol, _ = ctx.relabel_by_mapping(rp, col, ids_orc)
+    erp, ecol = po.relabel(rp, col, ids_orc)
+    np.testing.assert_array_equal(orp, erp)
+    np.testing.assert_array_equal(ocol, ecol)
+
+
+def test_large_community_gorder_paths(ctx):
+    # Communities of 20..6000 vertices: thread, shared-memory and global
+    # UnitHeap variants, against the oracle.
+    rp_t, col_t, planted = gg.planted_partition(60000, 12, degree=10, mixing=0.02, seed=9)
+    rp, col = rp_t.numpy(), col_t.numpy()
+    memb = planted.numpy().astype(np.uint32)
+    for fallback in (8000, 100000):
+        recipe = PARALLEL.replace("gordf5000", f"gordf{fallback}")
+        ids_gpu, st = ctx.order_compose(rp, col, memb, recipe)
+        ids_orc, ost = po.compose(rp, col, memb, gorder_fallback=fallback)
+        np.testing.assert_array_equal(ids_gpu, ids_orc)
+        assert st["gorder_max_community"] == ost.gorder_max_community
+
+
+def test_unsupported_and_bad_options(ctx):
+    rp, col = gg.from_edges(3, [(0, 1), (1, 2)])
+    with pytest.raises(NotImplementedError):
+        ctx.generate_mapping(rp.numpy(), col.numpy(), "leiden", 1.0)  # LAYER ordering
+    with pytest.raises(ValueError):
+        ctx.generate_mapping(rp.numpy(), col.numpy(), "leiden:compose:sgmb0", 1.0)
+    with pytest.raises(ValueError):
+        ctx.generate_mapping(np.array([0, 5], dtype=np.int64), np.zeros(1, dtype=np.int32), PARALLEL, 1.0)
+
+
+def test_graph_generator_cpu_gpu_identical():
+    a = gg.rmat(12, 8, seed=3)
+    b = gg.rmat(12, 8, seed=3, device="cuda")
+    assert torch.equal(a[0], b[0].cpu()) and torch.equal(a[1], b[1].cpu())
+
+
+def test_map_and_relabel_lifecycle(ctx, golden_arrays):
+    rp, col = graph(golden_arrays, "rmat12")
+    ids, orp, ocol, st = ctx.map_and_relabel(rp, col, PARALLEL)
+    assert po.validate_permutation(ids) == 0
+    erp, ecol = po.relabel(rp, col, ids)
+    np.testing.assert_array_equal(orp, erp)
+    np.testing.assert_array_equal(ocol, ecol)
+    assert st["total_ms"] > 0 and st["kernel_launches"] > 0
