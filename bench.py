@@ -48,7 +48,14 @@ def parse_args():
     ap.add_argument("--scale", type=int, default=SCALE)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    return ap.parse_args()
+    ap.add_argument("--engine", default="auto", choices=["auto", "exact", "async"],
+                    help="local-moving engine for cd_parallel: serial-order (exact), asynchronous, or by size")
+    a = ap.parse_args()
+    if a.engine == "exact":
+        os.environ["GBGPU_EXACT_MAX_VERTICES"] = str(1 << 62)
+    elif a.engine == "async":
+        os.environ["GBGPU_EXACT_MAX_VERTICES"] = "0"
+    return a
 
 
 def dist_env():
@@ -322,6 +329,7 @@ def main():
             "config": {"workload": f"rmat{args.scale}_ef{EDGE_FACTOR}_fastleiden_gorder8",
                        "recipe": "12:" + RECIPE, "scale": args.scale, "edge_factor": EDGE_FACTOR,
                        "vertices": n, "directed_entries": nnz, "parallelism": f"replicas{world}",
+                       "local_move_engine": args.engine,
                        "l2": "inputs larger than L2 (CSR 0.55 GB vs 129 MB L2)"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "clocks": clocks,

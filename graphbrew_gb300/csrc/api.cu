@@ -4,7 +4,9 @@
 // the message for gbgpu_last_error(); nothing here falls back to a CPU path.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <new>
@@ -139,6 +141,10 @@ gb::LeidenParams leiden_params(const gb::Config& c) {
     p.total_edges_m = c.mComputation == gb::MComputation::TotalEdges;
     p.super_move_batch = c.superGraphMoveBatch;
     p.deterministic = c.deterministicCommunityDetection;
+    // Schedule knobs (the autotuner's choices; defaults otherwise).
+    if (const char* v = std::getenv("GBGPU_EXACT_MAX_VERTICES")) p.exact_max_vertices = std::atoll(v);
+    if (const char* v = std::getenv("GBGPU_EXACT_WINDOW")) p.exact_window = std::max(32LL, std::atoll(v));
+    if (const char* v = std::getenv("GBGPU_ASYNC_CHUNK")) p.chunk_vertices = std::max(32, std::atoi(v));
     return p;
 }
 

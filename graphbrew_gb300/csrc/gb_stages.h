@@ -37,8 +37,10 @@ struct LeidenParams {
     bool total_edges_m = true;
     int super_move_batch = 1;
     bool deterministic = false;
-    int chunk_vertices = 1 << 16;   // local-moving launch granularity (parallel mode)
+    int chunk_vertices = 2048;      // asynchronous engine: vertices per launch
     int64_t super_single_cta_max_edges = 1 << 18;  // super-move in one persistent CTA up to this size
+    int64_t exact_max_vertices = 1 << 20;   // cd_parallel uses the serial-order engine up to this size
+    int64_t exact_window = 16384;           // speculative window of the serial-order engine
 };
 void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* membership, gbgpu_stats* st,
                    cudaStream_t s);

@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "gb_common.cuh"
+#include "gb_leiden_internal.cuh"
 #include "gb_stages.h"
 
 namespace gb {
@@ -37,62 +38,7 @@ namespace gb {
 namespace {
 
 constexpr int kT = 256;
-constexpr int kWarpMaxDeg = 1024;      // warp path up to this degree
-constexpr int kWarpHash = 2048;        // per-warp shared table slots
 constexpr int kLmWarpsPerBlock = 4;
-constexpr int kHubThreads = 512;
-constexpr int kHubSmemSlots = 16384;   // hub table in shared memory up to 8192 neighbours
-
-__device__ __forceinline__ uint32_t hash_u32(uint32_t x) {
-    return (uint32_t)(((uint64_t)x * 0x9E3779B97F4A7C15ull) >> 32);
-}
-
-// deltaModularity (:1295-1298) with the reference's association.
-__device__ __forceinline__ double delta_q(double kuc, double kud, double ku, double sc, double sd, double M, double R) {
-    const double a = __ddiv_rn(__dsub_rn(kuc, kud), M);
-    const double t = __dadd_rn(__dsub_rn(sc, sd), ku);
-    const double b = __dmul_rn(__dmul_rn(R, ku), t);
-    const double den = __dmul_rn(__dmul_rn(2.0, M), M);
-    return __dsub_rn(a, __ddiv_rn(b, den));
-}
-
-// (delta, id) ordering: larger delta first, then smaller id.
-__device__ __forceinline__ bool better(double da, uint32_t ia, double db, uint32_t ib) {
-    return da > db || (da == db && ia < ib);
-}
-
-__device__ __forceinline__ void warp_argmax(double& d, uint32_t& c) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const double od = __shfl_xor_sync(0xFFFFFFFFu, d, o);
-        const uint32_t oc = __shfl_xor_sync(0xFFFFFFFFu, c, o);
-        if (better(od, oc, d, c)) { d = od; c = oc; }
-    }
-}
-
-// Shared-memory open-addressing insert (keys kNone = empty).
-__device__ __forceinline__ void table_add(uint32_t* keys, uint32_t* vals, uint32_t mask, uint32_t k, uint32_t w) {
-    uint32_t h = hash_u32(k) & mask;
-    while (true) {
-        const uint32_t prev = atomicCAS(&keys[h], kNone, k);
-        if (prev == kNone || prev == k) {
-            atomicAdd(&vals[h], w);
-            return;
-        }
-        h = (h + 1) & mask;
-    }
-}
-
-__device__ __forceinline__ uint32_t table_get(const uint32_t* keys, const uint32_t* vals, uint32_t mask, uint32_t k) {
-    uint32_t h = hash_u32(k) & mask;
-    while (true) {
-        const uint32_t s = keys[h];
-        if (s == k) return vals[h];
-        if (s == kNone) return 0;
-        h = (h + 1) & mask;
-    }
-}
-
 struct LmArgs {
     const int64_t* rp;
     const int32_t* col;
@@ -672,7 +618,27 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
     LmArgs la{g.row_ptr, g.col, vcom, ctot, vaff, M, R, dacc, macc};
     const int64_t chunk = p.chunk_vertices > 0 ? p.chunk_vertices : n;
 
+    // Serial-order engine: cd_serial always; cd_parallel below the size where
+    // the asynchronous engine is both faster and statistically equivalent.
+    const bool exact = p.deterministic || n <= p.exact_max_vertices;
+    LocalMoveContext lmc;
+    lmc.g = g;
+    lmc.vcom = vcom;
+    lmc.ctot = ctot;
+    lmc.vaff = vaff;
+    lmc.M = M;
+    lmc.R = R;
+    lmc.hubs_h = hubs_h;
+    lmc.hubs = hubs.get();
+    lmc.hub_grid = hub_grid;
+    lmc.hub_gk = hub_gk.get();
+    lmc.hub_gv = hub_gv.get();
+    lmc.hub_gcap = hub_gcap;
+    int64_t exact_rounds = 0;
+
     auto local_move = [&](double tolerance) -> int {
+        if (exact)
+            return local_move_exact(lmc, tolerance, p.max_iterations, p.exact_window, s, &launches, &exact_rounds);
         int iters = 0;
         for (int it = 0; it < p.max_iterations; ++it) {
             GB_CUDA(cudaMemsetAsync(dacc, 0, sizeof(double), s));

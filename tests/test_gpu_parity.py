@@ -99,6 +99,57 @@ def test_auto_resolution(ctx, name, manifest, golden_arrays):
     assert ctx.auto_resolution(rp, col) == pytest.approx(manifest["cases"][name]["auto_resolution"], rel=1e-12)
 
 
+@pytest.mark.parametrize("name", case_names())
+def test_serial_leiden_bit_exact(ctx, name, manifest, golden_arrays):
+    """cd_serial community detection equals the reference's, id for id."""
+    rp, col = graph(golden_arrays, name)
+    case = manifest["cases"][name]
+    memb, st = ctx.run_graphbrew(rp, col, SERIAL, case["auto_resolution"])
+    np.testing.assert_array_equal(memb, golden_arrays[f"{name}/membership_serial"])
+    assert [st["passes"], st["iterations"], st["communities"]] == case["serial_summary"]
+
+
+@pytest.mark.parametrize("name", case_names())
+def test_serial_mapping_bit_exact(ctx, name, manifest, golden_arrays):
+    """The whole cd_serial mapping equals the reference's (and its fingerprint)."""
+    rp, col = graph(golden_arrays, name)
+    case = manifest["cases"][name]
+    ids, _ = ctx.generate_mapping(rp, col, SERIAL, case["auto_resolution"])
+    np.testing.assert_array_equal(ids, golden_arrays[f"{name}/new_ids_serial"])
+    assert gb.mapping_fingerprint(ids) == case["serial_fingerprint"]
+
+
+@pytest.mark.parametrize("scale,window", [(14, 16384), (16, 16384), (16, 1024), (18, 4096)])
+def test_serial_engine_against_oracle(ctx, scale, window, monkeypatch):
+    """Serial-order engine at larger sizes and window settings: bit-exact."""
+    monkeypatch.setenv("GBGPU_EXACT_WINDOW", str(window))
+    rp_t, col_t = gg.rmat(scale, 16, seed=200 + scale, device="cuda")
+    rp, col = rp_t.cpu().numpy(), col_t.cpu().numpy()
+    ar = po.auto_resolution(rp, col)
+    memb, st = ctx.run_graphbrew(rp_t, col_t, SERIAL, ar)
+    m_orc, ost = po.leiden(rp, col, ar)
+    np.testing.assert_array_equal(memb.cpu().numpy().view(np.uint32), m_orc)
+    assert [st["passes"], st["iterations"]] == [ost.passes, ost.iterations]
+    ids, _ = ctx.generate_mapping(rp_t, col_t, SERIAL, ar)
+    ids_orc, _ = po.compose(rp, col, m_orc)
+    np.testing.assert_array_equal(ids.cpu().numpy(), ids_orc)
+
+
+def test_async_engine_quality(ctx, monkeypatch):
+    """The asynchronous cd_parallel engine stays close to the serial result."""
+    monkeypatch.setenv("GBGPU_EXACT_MAX_VERTICES", "0")
+    rp_t, col_t = gg.rmat(17, 16, seed=5, device="cuda")
+    rp, col = rp_t.cpu().numpy(), col_t.cpu().numpy()
+    ar = po.auto_resolution(rp, col)
+    memb, _ = ctx.run_graphbrew(rp_t, col_t, PARALLEL, ar)
+    q = po.modularity(rp, col, memb.cpu().numpy().view(np.uint32), 1.0)
+    m_ser, _ = po.leiden(rp, col, ar)
+    q_ser = po.modularity(rp, col, m_ser, 1.0)
+    assert q >= q_ser - 0.02, (q, q_ser)
+    ids, _ = ctx.generate_mapping(rp_t, col_t, PARALLEL, ar)
+    assert ctx.validate_permutation(ids) == 0
+
+
 def _check_membership(rp, col, memb):
     n = len(rp) - 1
     assert memb.shape == (n,)
