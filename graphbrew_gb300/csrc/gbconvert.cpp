@@ -1,0 +1,376 @@
+// gbconvert.cpp -- GAPBS "converter" lifecycle on the GB300 mapping path.
+//
+// A drop-in for `converter -f G -s -o 12:<tokens> -q map.lo` (bench/src/converter.cc:14-47)
+// when the ordering is algorithm 12: the graph is built (loaded or generated,
+// symmetrized, squished), made resident on the GPU once, and for every -o
+// option the builder's mapping lifecycle runs (builder.h:829-940): mapping,
+// validation, fingerprint, relabel, with the same stdout labels the Python
+// orchestrator parses ("Reorder Core Time", "Mapping Fingerprint",
+// "Reorder End-to-End Time", ...).  Outputs: -q labels as text (.lo), -x labels
+// as raw int32 (.so), -b the relabelled graph (.sg), -e an edge list (.el),
+// in GAPBS's formats (writer.h:336-398).
+//
+// Flags: -f <file.el|.sg>  -g <scale>  -u <scale>  -k <degree>  -s
+//        -o 12:<tokens> (repeatable)  -q <out.lo>  -x <out.so>  -b <out.sg>
+//        -e <out.el>  -d <cuda device>  -r <seed>
+#include <cuda_runtime.h>
+#include <getopt.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "gbgpu.h"
+
+namespace {
+
+double now() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+void print_label(const std::string& label, const std::string& val) {
+    std::printf("%-21s%7s\n", (label + ":").c_str(), val.c_str());
+}
+
+void print_time(const std::string& s, double seconds) {
+    std::printf("%-21s%3.5lf\n", (s + ":").c_str(), seconds);
+}
+
+#define CU(x)                                                                                   \
+    do {                                                                                        \
+        cudaError_t e_ = (x);                                                                   \
+        if (e_ != cudaSuccess) throw std::runtime_error(std::string(#x) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+// ---- seeded generators: same SplitMix64 counter scheme as graphgen.py ----
+uint64_t mix64(uint64_t x) {
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+struct Draw {
+    uint64_t base;
+    Draw(uint64_t seed, uint64_t stream) : base(mix64(seed * 0x100000001B3ull + stream * 0x9E3779B1ull)) {}
+    uint64_t operator()(uint64_t i) const { return mix64(i ^ base); }
+};
+
+void radix_sort_u64(std::vector<uint64_t>& a, int bits) {
+    std::vector<uint64_t> tmp(a.size());
+    for (int shift = 0; shift < bits; shift += 16) {
+        std::vector<size_t> count(65537, 0);
+        for (uint64_t v : a) count[((v >> shift) & 0xFFFF) + 1]++;
+        for (int i = 0; i < 65536; ++i) count[i + 1] += count[i];
+        for (uint64_t v : a) tmp[count[(v >> shift) & 0xFFFF]++] = v;
+        a.swap(tmp);
+    }
+}
+
+struct HostGraph {
+    int64_t n = 0;
+    std::vector<int64_t> rp;
+    std::vector<int32_t> col;
+    std::vector<int32_t> org;
+};
+
+// Symmetrize, drop self-loops, sort and de-duplicate (builder.h:254-312).
+HostGraph squish(int64_t n, const std::vector<uint64_t>& src, const std::vector<uint64_t>& dst, bool symmetrize) {
+    std::vector<uint64_t> keys;
+    keys.reserve(src.size() * (symmetrize ? 2 : 1));
+    for (size_t i = 0; i < src.size(); ++i) {
+        if (src[i] == dst[i]) continue;
+        keys.push_back(src[i] * (uint64_t)n + dst[i]);
+        if (symmetrize) keys.push_back(dst[i] * (uint64_t)n + src[i]);
+    }
+    int bits = 0;
+    while (bits < 64 && ((uint64_t)n * (uint64_t)n >> bits) != 0) ++bits;
+    radix_sort_u64(keys, bits);
+    keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+    HostGraph g;
+    g.n = n;
+    g.rp.assign(n + 1, 0);
+    g.col.resize(keys.size());
+    for (size_t i = 0; i < keys.size(); ++i) {
+        g.rp[keys[i] / n + 1]++;
+        g.col[i] = (int32_t)(keys[i] % n);
+    }
+    for (int64_t v = 0; v < n; ++v) g.rp[v + 1] += g.rp[v];
+    g.org.resize(n);
+    for (int64_t v = 0; v < n; ++v) g.org[v] = (int32_t)v;
+    return g;
+}
+
+HostGraph gen_rmat(int scale, int degree, uint64_t seed) {
+    const int64_t n = int64_t(1) << scale, m = n * degree;
+    const uint64_t umax = 0xFFFFFFFFull;
+    const uint64_t A = (uint64_t)(0.57 * (double)umax), B = (uint64_t)(0.19 * (double)umax),
+                   C = (uint64_t)(0.19 * (double)umax);
+    const int words = (scale + 1) / 2;
+    Draw draw(seed, 1);
+    std::vector<uint64_t> src(m), dst(m);
+    for (int64_t e = 0; e < m; ++e) {
+        uint64_t s = 0, d = 0;
+        for (int j = 0; j < words; ++j) {
+            const uint64_t r64 = draw((uint64_t)e * words + j);
+            for (int half = 0; half < 2 && 2 * j + half < scale; ++half) {
+                const uint64_t r = half == 0 ? (r64 & 0xFFFFFFFFull) : (r64 >> 32);
+                s <<= 1;
+                d <<= 1;
+                if (r < A + B) {
+                    if (r > A) d++;
+                } else {
+                    s++;
+                    if (r > A + B + C) d++;
+                }
+            }
+        }
+        src[e] = s;
+        dst[e] = d;
+    }
+    // Seeded id permutation: rank of each id under a signed 64-bit hash key.
+    Draw pd(seed, 2);
+    std::vector<std::pair<int64_t, int64_t>> key(n);
+    for (int64_t v = 0; v < n; ++v) key[v] = {(int64_t)pd((uint64_t)v), v};
+    std::stable_sort(key.begin(), key.end(), [](auto& a, auto& b) { return a.first < b.first; });
+    std::vector<uint64_t> perm(n);
+    for (int64_t i = 0; i < n; ++i) perm[key[i].second] = (uint64_t)i;
+    for (int64_t e = 0; e < m; ++e) {
+        src[e] = perm[src[e]];
+        dst[e] = perm[dst[e]];
+    }
+    return squish(n, src, dst, true);
+}
+
+HostGraph gen_uniform(int scale, int degree, uint64_t seed) {
+    const int64_t n = int64_t(1) << scale, m = n * degree;
+    Draw draw(seed, 3);
+    std::vector<uint64_t> src(m), dst(m);
+    for (int64_t e = 0; e < m; ++e) {
+        src[e] = (draw(2 * (uint64_t)e) >> 1) % (uint64_t)n;
+        dst[e] = (draw(2 * (uint64_t)e + 1) >> 1) % (uint64_t)n;
+    }
+    return squish(n, src, dst, true);
+}
+
+HostGraph read_el(const std::string& path, bool symmetrize) {
+    std::ifstream in(path);
+    if (!in) throw std::runtime_error("Couldn't open file " + path);
+    std::vector<uint64_t> src, dst;
+    int64_t u, v, n = 0;
+    std::string line;
+    while (std::getline(in, line)) {
+        if (line.empty() || line[0] == '#' || line[0] == '%') continue;
+        if (std::sscanf(line.c_str(), "%ld %ld", &u, &v) != 2) continue;
+        src.push_back(u);
+        dst.push_back(v);
+        n = std::max(n, std::max(u, v) + 1);
+    }
+    return squish(n, src, dst, symmetrize);
+}
+
+HostGraph read_sg(const std::string& path) {
+    std::ifstream in(path, std::ios::binary);
+    if (!in) throw std::runtime_error("Couldn't open file " + path);
+    bool directed = false;
+    int64_t ne = 0, n = 0;
+    in.read(reinterpret_cast<char*>(&directed), sizeof(bool));
+    in.read(reinterpret_cast<char*>(&ne), sizeof(int64_t));
+    in.read(reinterpret_cast<char*>(&n), sizeof(int64_t));
+    if (directed) throw std::invalid_argument("the mapping path needs an undirected (symmetrized) .sg graph");
+    HostGraph g;
+    g.n = n;
+    g.rp.resize(n + 1);
+    g.col.resize(ne);
+    g.org.resize(n);
+    in.read(reinterpret_cast<char*>(g.rp.data()), (n + 1) * sizeof(int64_t));
+    in.read(reinterpret_cast<char*>(g.col.data()), ne * sizeof(int32_t));
+    in.read(reinterpret_cast<char*>(g.org.data()), n * sizeof(int32_t));
+    if (!in) throw std::runtime_error("Serialized graph is truncated");
+    return g;
+}
+
+void write_outputs(const HostGraph& g, const std::string& lo, const std::string& so, const std::string& sg,
+                   const std::string& el) {
+    if (!lo.empty()) {
+        std::ofstream out(lo);
+        for (int64_t v = 0; v < g.n; ++v) out << g.org[v] << '\n';
+    }
+    if (!so.empty()) {
+        std::ofstream out(so, std::ios::binary);
+        out.write(reinterpret_cast<const char*>(g.org.data()), g.n * sizeof(int32_t));
+    }
+    if (!sg.empty()) {
+        std::ofstream out(sg, std::ios::binary);
+        const bool directed = false;
+        const int64_t ne = (int64_t)g.col.size();
+        out.write(reinterpret_cast<const char*>(&directed), sizeof(bool));
+        out.write(reinterpret_cast<const char*>(&ne), sizeof(int64_t));
+        out.write(reinterpret_cast<const char*>(&g.n), sizeof(int64_t));
+        out.write(reinterpret_cast<const char*>(g.rp.data()), (g.n + 1) * sizeof(int64_t));
+        out.write(reinterpret_cast<const char*>(g.col.data()), ne * sizeof(int32_t));
+        out.write(reinterpret_cast<const char*>(g.org.data()), g.n * sizeof(int32_t));
+    }
+    if (!el.empty()) {
+        std::ofstream out(el);
+        for (int64_t u = 0; u < g.n; ++u)
+            for (int64_t e = g.rp[u]; e < g.rp[u + 1]; ++e) out << u << ' ' << g.col[e] << '\n';
+    }
+}
+
+int run(int argc, char** argv) {
+    std::string file, lo, so, sgout, elout;
+    int gscale = -1, uscale = -1, degree = 16, device = 0;
+    uint64_t seed = 27491095;
+    bool symmetrize = false;
+    std::vector<std::string> orders;
+    int c;
+    while ((c = getopt(argc, argv, "f:g:u:k:so:q:x:b:e:d:r:h")) != -1) {
+        switch (c) {
+            case 'f': file = optarg; break;
+            case 'g': gscale = std::atoi(optarg); break;
+            case 'u': uscale = std::atoi(optarg); break;
+            case 'k': degree = std::atoi(optarg); break;
+            case 's': symmetrize = true; break;
+            case 'o': orders.push_back(optarg); break;
+            case 'q': lo = optarg; break;
+            case 'x': so = optarg; break;
+            case 'b': sgout = optarg; break;
+            case 'e': elout = optarg; break;
+            case 'd': device = std::atoi(optarg); break;
+            case 'r': seed = std::strtoull(optarg, nullptr, 10); break;
+            default:
+                std::printf("gbconvert -f <file.el|.sg> | -g <scale> | -u <scale> [-k deg] [-s]\n"
+                            "          -o 12:<tokens> [-q out.lo] [-x out.so] [-b out.sg] [-e out.el] [-d dev]\n");
+                return c == 'h' ? 0 : 1;
+        }
+    }
+    if (file.empty() && gscale < 0 && uscale < 0) {
+        std::cout << "No graph input specified. (Use -h for help)" << std::endl;
+        return 1;
+    }
+    double t0 = now();
+    HostGraph g;
+    if (gscale >= 0) g = gen_rmat(gscale, degree, seed);
+    else if (uscale >= 0) g = gen_uniform(uscale, degree, seed);
+    else if (file.size() > 3 && file.substr(file.size() - 3) == ".sg") g = read_sg(file);
+    else g = read_el(file, symmetrize);
+    print_time("Build Time", now() - t0);
+    const int64_t nnz = (int64_t)g.col.size();
+    std::cout << "Graph has " << g.n << " nodes and " << nnz / 2 << " undirected edges for degree: "
+              << (g.n ? (nnz / 2) / g.n : 0) << std::endl;
+    if (orders.empty()) {  // conversion only
+        write_outputs(g, lo, so, sgout, elout);
+        return 0;
+    }
+
+    CU(cudaSetDevice(device));
+    gbgpu_ctx* ctx = nullptr;
+    if (gbgpu_ctx_create(&ctx, device) != GBGPU_OK) throw std::runtime_error("gbgpu_ctx_create failed");
+    int64_t *d_rp = nullptr, *d_orp = nullptr;
+    int32_t *d_col = nullptr, *d_ocol = nullptr, *d_ids = nullptr;
+    CU(cudaMalloc(&d_rp, (g.n + 1) * sizeof(int64_t)));
+    CU(cudaMalloc(&d_col, std::max<int64_t>(nnz, 1) * sizeof(int32_t)));
+    CU(cudaMalloc(&d_orp, (g.n + 1) * sizeof(int64_t)));
+    CU(cudaMalloc(&d_ocol, std::max<int64_t>(nnz, 1) * sizeof(int32_t)));
+    CU(cudaMalloc(&d_ids, std::max<int64_t>(g.n, 1) * sizeof(int32_t)));
+    CU(cudaMemcpy(d_rp, g.rp.data(), (g.n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(d_col, g.col.data(), nnz * sizeof(int32_t), cudaMemcpyHostToDevice));
+    double auto_res = -1.0;
+    gbgpu_auto_resolution(ctx, d_rp, g.n, nnz, GBGPU_DEVICE_POINTERS, &auto_res);
+
+    std::vector<int32_t> ids(g.n);
+    for (const std::string& o : orders) {
+        const size_t colon = o.find(':');
+        const std::string algo = o.substr(0, colon);
+        const std::string opts = colon == std::string::npos ? "" : o.substr(colon + 1);
+        if (algo != "12") throw std::invalid_argument("gbconvert runs reordering algorithm 12 only, got " + algo);
+        char json[16384];
+        gbgpu_config cfg;
+        int rc = gbgpu_parse_config(opts.c_str(), auto_res, &cfg, json, sizeof(json));
+        if (rc != GBGPU_OK) throw std::invalid_argument(json);
+        std::printf("GraphBrew Effective Config: %s\n", json);
+        std::printf("GraphBrew: resolution=%.4f (%s), maxIters=%d, maxPasses=%d\n", cfg.resolution, "fixed",
+                    cfg.max_iterations, cfg.max_passes);
+        std::printf("GraphBrew: community-detection=%s\n", cfg.deterministic ? "serial" : "parallel");
+        gbgpu_stats st;
+        double t = now();
+        rc = gbgpu_generate_mapping(ctx, d_rp, d_col, g.n, nnz, opts.c_str(), auto_res, d_ids, &st,
+                                    GBGPU_DEVICE_POINTERS);
+        const double core = now() - t;
+        if (rc != GBGPU_OK) throw std::runtime_error(gbgpu_last_error(ctx));
+        std::printf("GraphBrew: %d passes, %d iters, %ld communities, time=%.4fs\n", st.passes, st.iterations,
+                    (long)st.communities, st.leiden_ms / 1e3);
+        std::printf("  local-move: %.4fs, refine: %.4fs, aggregate: %.4fs\n", st.local_move_ms / 1e3, 0.0,
+                    st.aggregate_ms / 1e3);
+        std::printf("  compose: sg=none, %ld communities, %ld isolated, %.4fs\n", (long)st.num_communities,
+                    (long)st.isolated, st.compose_ms / 1e3);
+        std::printf("  compose gorder: communities=%ld, vertices=%ld, max-community=%ld, "
+                    "fallback-communities=%ld, fallback-vertices=%ld\n",
+                    (long)st.gorder_communities, (long)st.gorder_vertices, (long)st.gorder_max_community,
+                    (long)st.fallback_communities, (long)st.fallback_vertices);
+        std::cout << "=== Reorder Summary ===" << std::endl;
+        print_label("Algorithm", "GraphBrewOrder");
+        print_time("Reorder Core Time", core);
+        print_time("Reorder Time", core);
+        t = now();
+        int32_t valid = 0;
+        rc = gbgpu_validate_permutation(ctx, d_ids, g.n, GBGPU_DEVICE_POINTERS, &valid);
+        const double vtime = now() - t;
+        if (rc != GBGPU_OK) throw std::runtime_error(gbgpu_last_error(ctx));
+        if (valid == 1) throw std::runtime_error("generated mapping contains an out-of-range ID");
+        if (valid == 2) throw std::runtime_error("generated mapping contains a duplicate ID");
+        CU(cudaMemcpy(ids.data(), d_ids, g.n * sizeof(int32_t), cudaMemcpyDeviceToHost));
+        char fp[32];
+        std::snprintf(fp, sizeof(fp), "%016llx", (unsigned long long)gbgpu_fingerprint(ids.data(), g.n));
+        print_label("Mapping Fingerprint", fp);
+        t = now();
+        rc = gbgpu_relabel_csr(ctx, d_rp, d_col, g.n, nnz, d_ids, d_orp, d_ocol, nullptr, GBGPU_DEVICE_POINTERS);
+        if (rc != GBGPU_OK) throw std::runtime_error(gbgpu_last_error(ctx));
+        CU(cudaDeviceSynchronize());
+        const double apply = now() - t;
+        print_time("Reorder Validation Time", vtime);
+        print_time("Reorder Apply Time", apply);
+        print_time("Reorder End-to-End Time", core + vtime + apply);
+        // The relabelled graph becomes the current graph (update_org_ids).
+        std::swap(d_rp, d_orp);
+        std::swap(d_col, d_ocol);
+        std::vector<int32_t> org(g.n);
+        for (int64_t v = 0; v < g.n; ++v) org[ids[v]] = g.org[v];
+        g.org.swap(org);
+    }
+    if (!orders.empty() && (!sgout.empty() || !elout.empty())) {
+        CU(cudaMemcpy(g.rp.data(), d_rp, (g.n + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost));
+        CU(cudaMemcpy(g.col.data(), d_col, nnz * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    }
+    write_outputs(g, lo, so, sgout, elout);
+    cudaFree(d_rp);
+    cudaFree(d_col);
+    cudaFree(d_orp);
+    cudaFree(d_ocol);
+    cudaFree(d_ids);
+    gbgpu_ctx_destroy(ctx);
+    return 0;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    try {
+        return run(argc, argv);
+    } catch (const std::invalid_argument& e) {
+        std::fprintf(stderr, "Error: %s\n", e.what());
+        return 2;
+    } catch (const std::exception& e) {
+        std::fprintf(stderr, "Error: %s\n", e.what());
+        return 3;
+    }
+}
