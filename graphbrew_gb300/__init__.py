@@ -95,6 +95,7 @@ SIGNATURES = {
     "gbgpu_relabel_csr": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int64, _P, _P, _P, _P, C.c_uint32]),
     "gbgpu_map_and_relabel": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int64, C.c_char_p, C.c_double, _P, _P, _P,
                                         C.POINTER(GbgpuStats), C.c_uint32]),
+    "gbgpu_validate_permutation_noalloc": (C.c_int, [_P, _P, C.c_int64, C.POINTER(C.c_int32)]),
     "gbgpu_fingerprint": (C.c_uint64, [_P, C.c_int64]),
     "gbgpu_version": (C.c_char_p, []),
 }

@@ -508,6 +508,15 @@ int gbgpu_map_and_relabel(gbgpu_ctx* ctx, const int64_t* row_ptr, const int32_t*
     });
 }
 
+}  // extern "C"
+
+// Internal accessors for entry points defined in other translation units.
+cudaStream_t gb_ctx_stream(gbgpu_ctx* ctx) { return ctx->stream; }
+int gb_ctx_device(gbgpu_ctx* ctx) { return ctx->device; }
+void gb_ctx_set_error(gbgpu_ctx* ctx, const char* msg) { ctx->last_error = msg ? msg : ""; }
+
+extern "C" {
+
 uint64_t gbgpu_fingerprint(const int32_t* new_ids, int64_t n) {
     uint64_t h = UINT64_C(1469598103934665603);
     for (int64_t i = 0; i < n; ++i) {

@@ -177,6 +177,23 @@ int gbgpu_map_and_relabel(gbgpu_ctx* ctx, const int64_t* row_ptr, const int32_t*
                           int32_t* new_ids_out, int64_t* out_row_ptr, int32_t* out_col,
                           gbgpu_stats* stats, uint32_t flags);
 
+/* Largest n accepted by gbgpu_validate_permutation_noalloc. */
+#define GBGPU_NOALLOC_MAX_VERTICES (1 << 20)
+
+/* Permutation check that allocates no device memory.  No counterpart in the
+ * reference: it serves callers that cannot allocate device memory -- a process
+ * whose GPU memory is reserved by another framework's allocator, work issued
+ * inside a CUDA stream capture, or a latency-critical loop that cannot take
+ * cudaMalloc's implicit synchronisation.  Same *result codes as
+ * gbgpu_validate_permutation; new_ids_dev must be device memory; n at most
+ * GBGPU_NOALLOC_MAX_VERTICES (larger n returns GBGPU_E_OVERFLOW).  Scratch is a
+ * fixed 4 MiB array in the library's device image, held by every GPU that loads
+ * the library until exit and shared by all calls: calls whose GPU work
+ * overlaps race and must be serialised by the caller.  The first call on each
+ * device looks up that array's address, so make it before any stream capture. */
+int gbgpu_validate_permutation_noalloc(gbgpu_ctx* ctx, const int32_t* new_ids_dev, int64_t n,
+                                       int32_t* result);
+
 /* FNV-1a-64 fingerprint of a forward map, on the host, as the builder prints
  * it ("Mapping Fingerprint"). */
 uint64_t gbgpu_fingerprint(const int32_t* new_ids, int64_t n);
