@@ -643,7 +643,6 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
         for (int it = 0; it < p.max_iterations; ++it) {
             GB_CUDA(cudaMemsetAsync(dacc, 0, sizeof(double), s));
             GB_CUDA(cudaMemsetAsync(macc, 0, sizeof(unsigned long long), s));
-            size_t hcur = 0;
             for (int64_t b = 0; b < n; b += chunk) {
                 const int64_t e = std::min(n, b + chunk);
                 const int64_t warps = e - b;
@@ -651,15 +650,14 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
                 k_local_move_warp<<<grid, kLmWarpsPerBlock * 32, lm_smem, s>>>(la, b, e);
                 GB_LAUNCH_CHECK();
                 ++launches;
-                const size_t h0 = hcur;
-                while (hcur < hubs_h.size() && (int64_t)hubs_h[hcur] < e) ++hcur;
-                if (hcur > h0) {
-                    const int hg = (int)std::min<size_t>(hcur - h0, (size_t)hub_grid);
-                    k_local_move_hub<<<hg, kHubThreads, hub_smem, s>>>(la, hubs, (int64_t)h0, (int64_t)hcur, hub_gk,
-                                                                       hub_gv, hub_gcap);
-                    GB_LAUNCH_CHECK();
-                    ++launches;
-                }
+            }
+            // Hubs in one launch per iteration, one CTA each: they see the
+            // moves of every lower-degree vertex of this iteration.
+            if (!hubs_h.empty()) {
+                k_local_move_hub<<<hub_grid, kHubThreads, hub_smem, s>>>(la, hubs, 0, (int64_t)hubs_h.size(),
+                                                                         hub_gk, hub_gv, hub_gcap);
+                GB_LAUNCH_CHECK();
+                ++launches;
             }
             ++iters;
             const double total = read_dev(dacc.get(), s);

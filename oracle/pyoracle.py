@@ -277,3 +277,159 @@ def ref_gapbs_graph(scale, degree=16, uniform=False):
     cl = np.zeros(nnz.value, dtype=np.int32)
     ref.ref_last_graph_copy(rp, cl)
     return rp, cl
+
+
+# --------------------------------------------------------------------------
+# Timed consumers, the DBG arm, Tier-0 features and the MLP (numpy restatements)
+# --------------------------------------------------------------------------
+
+def dbg_mapping(row_ptr, col):
+    """GenerateDBGMapping (bench/include/graphbrew/reorder/reorder_hub.h:267-342):
+    8 degree buckets (avg/2, avg, 2avg, ..., 32avg, inf), highest bucket first,
+    vertex-id order inside a bucket."""
+    rp = np.asarray(row_ptr, dtype=np.int64)
+    n = len(rp) - 1
+    if n == 0:
+        return np.zeros(0, dtype=np.int32)
+    deg = np.diff(rp).astype(np.uint64)
+    avg = np.uint64((rp[-1]) // n)
+    th = [avg // np.uint64(2), avg, avg * np.uint64(2), avg * np.uint64(4), avg * np.uint64(8),
+          avg * np.uint64(16), avg * np.uint64(32)]
+    bucket = np.full(n, 7, dtype=np.int64)
+    for j in range(6, -1, -1):
+        bucket[deg <= th[j]] = j
+    order = np.argsort(7 - bucket, kind="stable")
+    ids = np.empty(n, dtype=np.int32)
+    ids[order] = np.arange(n, dtype=np.int32)
+    return ids
+
+
+def bfs_depths(row_ptr, col, source):
+    """BFS depth of every vertex from source (-1 unreached)."""
+    rp = np.asarray(row_ptr, dtype=np.int64)
+    cl = np.asarray(col)
+    n = len(rp) - 1
+    depth = np.full(n, -1, dtype=np.int32)
+    depth[source] = 0
+    frontier = [source]
+    level = 0
+    while frontier:
+        nxt = []
+        for u in frontier:
+            for v in cl[rp[u]:rp[u + 1]]:
+                if depth[v] < 0:
+                    depth[v] = level + 1
+                    nxt.append(int(v))
+        frontier = nxt
+        level += 1
+    return depth
+
+
+def cc_min_labels(row_ptr, col):
+    """Connected components labelled by their smallest vertex id."""
+    rp = np.asarray(row_ptr, dtype=np.int64)
+    cl = np.asarray(col)
+    n = len(rp) - 1
+    parent = np.arange(n)
+
+    def find(x):
+        while parent[x] != x:
+            parent[x] = parent[parent[x]]
+            x = parent[x]
+        return x
+    for u in range(n):
+        for v in cl[rp[u]:rp[u + 1]]:
+            a, b = find(u), find(int(v))
+            if a != b:
+                parent[max(a, b)] = min(a, b)
+    return np.array([find(x) for x in range(n)], dtype=np.int32)
+
+
+def pagerank(row_ptr, col, max_iters=20, epsilon=1e-4, damp=0.85):
+    """Pull PageRank (bench/src/pr.cc:40-90) as Jacobi sweeps in float64."""
+    rp = np.asarray(row_ptr, dtype=np.int64)
+    cl = np.asarray(col, dtype=np.int64)
+    n = len(rp) - 1
+    deg = np.diff(rp).astype(np.float64)
+    score = np.full(n, 1.0 / n)
+    src = np.repeat(np.arange(n), np.diff(rp))
+    for _ in range(max_iters):
+        contrib = np.where(deg > 0, score / np.maximum(deg, 1), 0.0)
+        incoming = np.bincount(src, weights=contrib[cl], minlength=n)
+        new = (1.0 - damp) / n + damp * incoming
+        err = np.abs(new - score).sum()
+        score = new
+        if err < epsilon:
+            break
+    return score
+
+
+def tier0_features(row_ptr, col):
+    """ComputeTier0SampledGraphFeatures (reorder_types.h:6066-6186) with sample seed 0."""
+    rp = np.asarray(row_ptr, dtype=np.int64)
+    cl = np.asarray(col, dtype=np.int64)
+    n = len(rp) - 1
+    s = max(1024, min(int(np.sqrt(float(n))), 8192))
+    s = min(s, n)
+    nodes = [((2 * i + 1) * n) // (2 * s) for i in range(s)]
+    degs = [int(rp[v + 1] - rp[v]) for v in nodes]
+    dsum = 0.0
+    for d in degs:
+        dsum += d
+    avg = dsum / s
+    var = 0.0
+    for d in degs:
+        var += (d - avg) * (d - avg)
+    variance = var / (s - 1) if s > 1 else 0.0
+    cv = np.sqrt(variance) / avg if avg > 0 else 0.0
+    pairs = sorted(zip(degs, nodes), key=lambda p: (-p[0], p[1]))
+    hub_count = max(1, s // 10)
+    hsum = 0.0
+    for d, _ in pairs[:hub_count]:
+        hsum += d
+    hubs = [v for _, v in pairs[:hub_count]]
+    lines = {v // 8 for v in hubs}
+    span, edges, window = 0.0, 0, 0
+    den = float(max(1, n - 1))
+    for _, v in pairs:
+        for d in cl[rp[v]:rp[v + 1]]:
+            span += abs(int(d) - v) / den
+            edges += 1
+            window += abs(int(d) // 8 - v // 8) <= 1
+    return {"num_nodes": float(n), "num_edges": float(rp[-1]), "avg_degree": avg, "degree_cv": cv,
+            "internal_density": avg / (n - 1) if n > 1 else 0.0,
+            "hub_concentration": hsum / dsum if dsum > 0 else 0.0,
+            "packing_factor": len(hubs) / len(lines) if lines else 0.0,
+            "normalized_edge_span": span / edges if edges else 0.0,
+            "window_neighbor_overlap": window / edges if edges else 0.0}
+
+
+def mlp_unpack(params, in_dim, hidden=64, out=3):
+    p = np.asarray(params, dtype=np.float64)
+    shapes = [(in_dim, hidden), (hidden,), (hidden, hidden), (hidden,), (hidden, out), (out,)]
+    res, o = [], 0
+    for sh in shapes:
+        k = int(np.prod(sh))
+        res.append(p[o:o + k].reshape(sh))
+        o += k
+    return res
+
+
+def mlp_loss_grad(params, X, T):
+    """float64 forward/backward of the in -> 64 -> 64 -> 3 ReLU MLP under mean squared error."""
+    X = np.asarray(X, dtype=np.float64)
+    T = np.asarray(T, dtype=np.float64)
+    W1, b1, W2, b2, W3, b3 = mlp_unpack(params, X.shape[1])
+    H1 = np.maximum(X @ W1 + b1, 0)
+    H2 = np.maximum(H1 @ W2 + b2, 0)
+    Y = H2 @ W3 + b3
+    B, O = Y.shape
+    loss = ((Y - T) ** 2).sum() / (B * O)
+    dY = 2 * (Y - T) / (B * O)
+    gW3, gb3 = H2.T @ dY, dY.sum(0)
+    dH2 = (dY @ W3.T) * (H2 > 0)
+    gW2, gb2 = H1.T @ dH2, dH2.sum(0)
+    dH1 = (dH2 @ W2.T) * (H1 > 0)
+    gW1, gb1 = X.T @ dH1, dH1.sum(0)
+    grad = np.concatenate([g.ravel() for g in (gW1, gb1, gW2, gb2, gW3, gb3)])
+    return loss, grad, Y
