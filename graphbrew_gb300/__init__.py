@@ -98,6 +98,19 @@ SIGNATURES = {
     "gbgpu_validate_permutation_noalloc": (C.c_int, [_P, _P, C.c_int64, C.POINTER(C.c_int32)]),
     "gbgpu_fingerprint": (C.c_uint64, [_P, C.c_int64]),
     "gbgpu_version": (C.c_char_p, []),
+    "gbgpu_pagerank": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int64, C.c_int32, C.c_double, _P,
+                                 C.POINTER(C.c_int32), C.POINTER(C.c_double), C.c_uint32]),
+    "gbgpu_bfs": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int64, C.c_int64, _P, C.POINTER(C.c_double), C.c_uint32]),
+    "gbgpu_connected_components": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int64, _P, C.POINTER(C.c_double),
+                                             C.c_uint32]),
+    "gbgpu_dbg_mapping": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int64, _P, C.POINTER(C.c_double), C.c_uint32]),
+    "gbgpu_tier0_features": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int64, C.POINTER(C.c_double), C.c_uint32]),
+    "gbgpu_mlp_param_count": (C.c_int, [C.c_int32]),
+    "gbgpu_mlp_forward": (C.c_int, [_P, _P, _P, C.c_int32, C.c_int32, _P, C.c_uint32]),
+    "gbgpu_mlp_gradient": (C.c_int, [_P, _P, _P, _P, C.c_int32, C.c_int32, _P, C.POINTER(C.c_float),
+                                     C.c_uint32]),
+    "gbgpu_mlp_train": (C.c_int, [_P, _P, _P, _P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_float,
+                                  C.c_uint64, C.POINTER(C.c_float), C.c_uint32]),
 }
 
 _lib = None
@@ -326,6 +339,83 @@ class Context:
         self._check(library().gbgpu_map_and_relabel(self._h, prp, pcl, n, nnz, opts.encode(), ar, pids, porp,
                                                        pocol, C.byref(st), DEVICE_POINTERS if dev else 0))
         return ids, orp, ocol, st.as_dict()
+
+    # -- consumers timed after a mapping, DBG arm, selector ---------------------
+    def _vertex_out(self, fn, row_ptr, col, dtype, *extra):
+        rp, cl, prp, pcl, n, nnz, dev = self._graph_args(row_ptr, col)
+        out, pout = self._out(n, dtype, dev, rp)
+        ms = C.c_double()
+        self._check(fn(self._h, prp, pcl, n, nnz, *extra, pout, C.byref(ms), DEVICE_POINTERS if dev else 0))
+        return out, ms.value
+
+    def pagerank(self, row_ptr, col, max_iters=20, epsilon=1e-4):
+        """PageRank scores (float32), sweeps run, kernel ms."""
+        rp, cl, prp, pcl, n, nnz, dev = self._graph_args(row_ptr, col)
+        if dev:
+            import torch
+            out = torch.empty(n, dtype=torch.float32, device=rp.device)
+            pout = out.data_ptr()
+        else:
+            out = np.zeros(n, dtype=np.float32)
+            pout = out.ctypes.data if n else 0
+        it, ms = C.c_int32(), C.c_double()
+        self._check(library().gbgpu_pagerank(self._h, prp, pcl, n, nnz, int(max_iters), float(epsilon), pout,
+                                               C.byref(it), C.byref(ms), DEVICE_POINTERS if dev else 0))
+        return out, it.value, ms.value
+
+    def bfs(self, row_ptr, col, source=0):
+        """BFS depth per vertex (-1 unreached) and kernel ms."""
+        return self._vertex_out(library().gbgpu_bfs, row_ptr, col, np.int32, C.c_int64(int(source)))
+
+    def connected_components(self, row_ptr, col):
+        """Smallest vertex id of each vertex's component, and kernel ms."""
+        return self._vertex_out(library().gbgpu_connected_components, row_ptr, col, np.int32)
+
+    def dbg_mapping(self, row_ptr, col):
+        """DBG forward map (algorithm 5) and kernel ms."""
+        return self._vertex_out(library().gbgpu_dbg_mapping, row_ptr, col, np.int32)
+
+    def tier0_features(self, row_ptr, col) -> np.ndarray:
+        """The nine Tier-0 sampled features (float64, host)."""
+        rp, cl, prp, pcl, n, nnz, dev = self._graph_args(row_ptr, col)
+        out = (C.c_double * 9)()
+        self._check(library().gbgpu_tier0_features(self._h, prp, pcl, n, nnz, out, DEVICE_POINTERS if dev else 0))
+        return np.array(out[:], dtype=np.float64)
+
+    @staticmethod
+    def mlp_param_count(in_dim: int) -> int:
+        return library().gbgpu_mlp_param_count(int(in_dim))
+
+    @staticmethod
+    def _f32(a):
+        return np.ascontiguousarray(_to_numpy(a), dtype=np.float32)
+
+    def mlp_forward(self, params, X):
+        p, x = self._f32(params), self._f32(X)
+        rows, in_dim = x.shape
+        y = np.zeros((rows, 3), dtype=np.float32)
+        self._check(library().gbgpu_mlp_forward(self._h, p.ctypes.data, x.ctypes.data, rows, in_dim,
+                                                  y.ctypes.data, 0))
+        return y
+
+    def mlp_gradient(self, params, X, T):
+        """(gradient packed like params, mean squared error)."""
+        p, x, t = self._f32(params), self._f32(X), self._f32(T)
+        rows, in_dim = x.shape
+        g = np.zeros_like(p)
+        loss = C.c_float()
+        self._check(library().gbgpu_mlp_gradient(self._h, p.ctypes.data, x.ctypes.data, t.ctypes.data, rows,
+                                                   in_dim, g.ctypes.data, C.byref(loss), 0))
+        return g, loss.value
+
+    def mlp_train(self, params, X, T, epochs=200, batch=64, lr=1e-3, seed=0):
+        """Adam on the GPU; returns (new params, last epoch's mean loss)."""
+        p, x, t = self._f32(params).copy(), self._f32(X), self._f32(T)
+        rows, in_dim = x.shape
+        loss = C.c_float()
+        self._check(library().gbgpu_mlp_train(self._h, p.ctypes.data, x.ctypes.data, t.ctypes.data, rows, in_dim,
+                                                int(epochs), int(batch), float(lr), int(seed), C.byref(loss), 0))
+        return p, loss.value
 
 
 _default_ctx = None

@@ -39,13 +39,20 @@ struct LeidenParams {
     bool deterministic = false;
     int chunk_vertices = 2048;      // asynchronous engine: vertices per launch
     int64_t super_single_cta_max_edges = 1 << 18;  // super-move in one persistent CTA up to this size
-    int64_t exact_max_vertices = 1 << 20;   // cd_parallel uses the serial-order engine up to this size
-    int64_t exact_window = 16384;           // speculative window of the serial-order engine
+    int64_t exact_max_vertices = INT64_MAX; // cd_parallel uses the serial-order engine up to this size
+    int64_t exact_window = 8192;            // speculative window of the serial-order engine
 };
 void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* membership, gbgpu_stats* st,
                    cudaStream_t s);
 
 // Degree-distribution auto resolution (reorder_types.h:2743-2780).
 double auto_resolution_device(const int64_t* row_ptr, int64_t n, int64_t nnz, cudaStream_t s);
+
+// ---- kernels.cu: timed consumers and the DBG arm; each returns device ms ----
+double pagerank_device(const DeviceCSR& g, int max_iters, double epsilon, float* score, int* iters_out,
+                       cudaStream_t s);
+double bfs_device(const DeviceCSR& g, int64_t source, int32_t* depth, cudaStream_t s);
+double cc_device(const DeviceCSR& g, int32_t* comp, cudaStream_t s);
+double dbg_mapping_device(const DeviceCSR& g, int32_t* new_ids, cudaStream_t s);
 
 }  // namespace gb

@@ -11,14 +11,21 @@
 //     state plus the D_prev moves of window vertices before u (neighbour
 //     communities, affected flags and community totals at "time u");
 //   * the first vertex x whose new decision differs from D_prev bounds the
-//     exact prefix: all of [P, x] was evaluated from exact inputs, so it is
-//     committed; the rest of the window carries its new decisions forward.
+//     exact prefix: all of [P, x] was evaluated from exact inputs (induction
+//     from P), so it is committed; the rest carries its new decisions forward.
 //
-// Community totals at time u come from an event table rebuilt every round:
-// each speculative move contributes (old, -k) and (new, +k) at its time; the
-// events are stably sorted by community slot and prefix-summed, and a lookup
-// binary-searches the community's events for the last time before u.  All
-// totals are exact integers, so every Delta-modularity equals the serial one.
+// Community totals at time u come from an event table rebuilt every round by
+// one CTA: each speculative move contributes (old, -k) and (new, +k) at its
+// time; events are stably radix-sorted by community slot in shared memory and
+// prefix-summed, and a lookup binary-searches the community's events for the
+// last time before u.  All totals are exact integers, so every
+// Delta-modularity equals the serial one.
+//
+// Vertices above kWarpMaxDeg ("hubs") are split into 4096-edge segments, each
+// accumulated by its own CTA into the hub's global table, then scanned in
+// 4096-slot segments; the last CTA of a hub reduces the partial maxima.  The
+// whole round reads its window bounds from a device control block, so the host
+// enqueues rounds without waiting and checks completion every few rounds.
 //
 // The iteration's totalDelta decides the tolerance break; it is summed in a
 // fixed tree order with a rigorous error bound and re-summed serially in
@@ -36,105 +43,338 @@ namespace {
 
 constexpr int kT = 256;
 constexpr uint8_t kUnknown = 2;
+constexpr int kWindowMax = 8192;              // window vertices (events <= 2 x window)
+constexpr int kEventsMax = 2 * kWindowMax;    // 16384 -> 14-bit event index
+constexpr int kTableSlots = 4 * kWindowMax;   // 32768 hash slots -> 15 bits (+1 for padding)
+constexpr int kEvThreads = 1024;
+constexpr int kHubSeg = 4096;                 // edges per hub-accumulation CTA
+constexpr int kTabSeg = 4096;                 // table slots per hub-selection CTA
+constexpr unsigned long long kNoChange = ~0ull;
 
-struct ExactArgs {
+struct Ctl {
+    long long P, E, n, B;
+    unsigned long long first_change;
+    long long es0, es1;       // hub edge-segment range of the window
+    long long ts0, ts1;       // hub table-segment range of the window
+    long long round;
+};
+
+struct HubSeg {
+    int32_t hub;      // index into the hub arrays
+    int32_t part;     // segment number within the hub
+};
+
+struct ExactState {
     const int64_t* rp;
     const int32_t* col;
-    const uint32_t* vcom;           // committed communities
-    const unsigned long long* ctot; // committed totals
-    const uint8_t* vaff;            // committed affected flags
-    const uint32_t* pbest;          // D_prev
-    const uint8_t* pact;
-    uint32_t* nbest;                // D_new
-    uint8_t* nact;
-    double* ndelta;
+    uint32_t* vcom;
+    unsigned long long* ctot;
+    uint8_t* vaff;
+    Ctl* ctl;
+    // decisions, double-buffered by round parity
+    uint32_t* best[2];
+    uint8_t* act[2];
+    double* delta[2];
+    double* final_delta;
     // event table
-    const uint32_t* hkey;           // hash slot -> community (kNone empty)
-    uint32_t hmask;
-    const int32_t* sstart;          // slot -> [start, end) in sorted events
-    const int32_t* send;
-    const uint32_t* etime;          // sorted event times
-    const long long* epre;          // inclusive prefix within the slot
-    int64_t P, E;
+    uint32_t* hkey;       // kTableSlots
+    int32_t* sstart;      // kTableSlots
+    int32_t* send;
+    uint32_t* etime_raw;  // kEventsMax (by event index)
+    long long* eval_raw;
+    uint32_t* stime;      // sorted
+    long long* epre;      // inclusive prefix within slot
+    long long* gscan;     // scratch: inclusive scan over all sorted events
+    // hubs
+    const uint32_t* hub_v;        // hub vertex ids (ascending)
+    const int64_t* hub_toff;      // table offset
+    const uint32_t* hub_tcap;     // table capacity (pow2)
+    const int32_t* hub_tfirst;    // first table segment index of each hub
+    const int32_t* hub_tcount;    // table segments of each hub
+    const HubSeg* eseg;           // edge segments (hub id order)
+    const uint32_t* eseg_v;       // hub vertex of each edge segment
+    long long n_eseg;
+    const HubSeg* tseg;           // table segments
+    const uint32_t* tseg_v;
+    long long n_tseg;
+    uint32_t* tkeys;              // hub tables (pool)
+    uint32_t* tvals;
+    int32_t* hub_any;
+    int32_t* hub_done;
+    double* part_d;               // per table segment
+    uint32_t* part_c;
     double M, R;
-    unsigned long long* first_change;
 };
 
 __device__ __forceinline__ uint32_t slot_hash(uint32_t c) {
     return (uint32_t)(((uint64_t)c * 0x9E3779B97F4A7C15ull) >> 40);
 }
 
-__device__ __forceinline__ int find_slot(const uint32_t* hkey, uint32_t mask, uint32_t c) {
-    uint32_t h = slot_hash(c) & mask;
+__device__ __forceinline__ int find_slot(const uint32_t* hkey, uint32_t c) {
+    uint32_t h = slot_hash(c) & (kTableSlots - 1);
     while (true) {
         const uint32_t k = hkey[h];
         if (k == c) return (int)h;
         if (k == kNone) return -1;
-        h = (h + 1) & mask;
+        h = (h + 1) & (kTableSlots - 1);
     }
 }
 
-// Community total at time u: committed total plus the speculative moves of
-// window vertices before u.
-__device__ __forceinline__ long long sigma_at(const ExactArgs& a, uint32_t c, uint32_t u) {
+// Community total at time u.
+__device__ __forceinline__ long long sigma_at(const ExactState& a, uint32_t c, uint32_t u) {
     long long s = (long long)a.ctot[c];
-    const int slot = find_slot(a.hkey, a.hmask, c);
+    const int slot = find_slot(a.hkey, c);
     if (slot < 0) return s;
-    int lo = a.sstart[slot], hi = a.send[slot];  // events sorted by time
-    // last index with time < u
+    int lo = a.sstart[slot], hi = a.send[slot];
     int l = lo, r = hi;
     while (l < r) {
         const int mid = (l + r) >> 1;
-        if (a.etime[mid] < u) l = mid + 1; else r = mid;
+        if (a.stime[mid] < u) l = mid + 1; else r = mid;
     }
     if (l > lo) s += a.epre[l - 1];
     return s;
 }
 
-__device__ __forceinline__ bool prev_mover(const ExactArgs& a, int64_t v) {
-    return a.pact[v] == 1 && a.pbest[v] != a.vcom[v];
+struct Round {
+    long long P, E;
+    const uint32_t* pbest;
+    const uint8_t* pact;
+    uint32_t* nbest;
+    uint8_t* nact;
+    double* ndelta;
+};
+
+__device__ __forceinline__ Round round_view(const ExactState& a) {
+    Round r;
+    r.P = a.ctl->P;
+    r.E = a.ctl->E;
+    const int par = (int)(a.ctl->round & 1);
+    r.pbest = a.best[par];
+    r.pact = a.act[par];
+    r.nbest = a.best[par ^ 1];
+    r.nact = a.act[par ^ 1];
+    r.ndelta = a.delta[par ^ 1];
+    return r;
 }
 
-// Community of neighbour v as seen at time u.
-__device__ __forceinline__ uint32_t comm_at(const ExactArgs& a, int64_t v, int64_t u) {
-    if (v >= a.P && v < u && prev_mover(a, v)) return a.pbest[v];
+__device__ __forceinline__ bool prev_mover(const ExactState& a, const Round& r, int64_t v) {
+    return r.pact[v] == 1 && r.pbest[v] != a.vcom[v];
+}
+
+__device__ __forceinline__ uint32_t comm_at(const ExactState& a, const Round& r, int64_t v, int64_t u) {
+    if (v >= r.P && v < u && prev_mover(a, r, v)) return r.pbest[v];
     return a.vcom[v];
 }
 
-__device__ __forceinline__ void record(const ExactArgs& a, int64_t u, uint8_t act, uint32_t best, double delta) {
-    a.nact[u] = act;
-    a.nbest[u] = best;
-    a.ndelta[u] = delta;
-    if (act != a.pact[u] || (act == 1 && best != a.pbest[u])) atomicMin(a.first_change, (unsigned long long)u);
+__device__ __forceinline__ void record(const ExactState& a, const Round& r, int64_t u, uint8_t act, uint32_t best,
+                                       double delta) {
+    r.nact[u] = act;
+    r.nbest[u] = best;
+    r.ndelta[u] = delta;
+    // Only the move itself is visible to later vertices: "inactive" and
+    // "evaluated, stays" are the same decision.
+    const uint32_t cur = a.vcom[u];
+    const uint8_t pa = r.pact[u];
+    const bool moves = act == 1 && best != cur;
+    const bool pmoves = pa == 1 && r.pbest[u] != cur;
+    if (pa == kUnknown || moves != pmoves || (moves && best != r.pbest[u]))
+        atomicMin(&a.ctl->first_change, (unsigned long long)u);
+}
+
+__device__ __forceinline__ long long lower_bound_u32(const uint32_t* a, long long n, uint32_t key) {
+    long long lo = 0, hi = n;
+    while (lo < hi) {
+        const long long mid = (lo + hi) >> 1;
+        if (a[mid] < key) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+// ---------------------------------------------------------------------------
+// Event table (one CTA): hash slots, stable sort by slot, prefix sums.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kEvThreads) k_ex_table(ExactState a) {
+    extern __shared__ uint32_t sm[];
+    uint32_t* bufA = sm;                               // kEventsMax
+    uint32_t* bufB = sm + kEventsMax;                  // kEventsMax
+    int32_t* wcnt = reinterpret_cast<int32_t*>(sm + 2 * kEventsMax);  // 32 x 257
+    __shared__ int32_t digit_off[256];
+    __shared__ long long warp_tot[32];
+    const long long P = a.ctl->P, E = a.ctl->E;
+    if (P >= a.ctl->n) return;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int W = (int)(E - P);
+    const int m = 2 * W;
+    const Round r = round_view(a);
+    for (int i = tid; i < kTableSlots; i += blockDim.x) a.hkey[i] = kNone;
+    if (tid == 0) {
+        a.ctl->first_change = kNoChange;
+        a.ctl->es0 = lower_bound_u32(a.eseg_v, a.n_eseg, (uint32_t)P);
+        a.ctl->es1 = lower_bound_u32(a.eseg_v, a.n_eseg, (uint32_t)E);
+        a.ctl->ts0 = lower_bound_u32(a.tseg_v, a.n_tseg, (uint32_t)P);
+        a.ctl->ts1 = lower_bound_u32(a.tseg_v, a.n_tseg, (uint32_t)E);
+    }
+    __syncthreads();
+    // Events of D_prev movers, packed as (slot << 14 | event index).
+    constexpr uint32_t kPad = (uint32_t)kTableSlots << 14;
+    for (int i = tid; i < W; i += blockDim.x) {
+        const int64_t wv = P + i;
+        uint32_t p0 = kPad | (uint32_t)(2 * i), p1 = kPad | (uint32_t)(2 * i + 1);
+        if (r.pact[wv] == 1 && r.pbest[wv] != a.vcom[wv]) {
+            const long long deg = (long long)(a.rp[wv + 1] - a.rp[wv]);
+            const uint32_t cs[2] = {a.vcom[wv], r.pbest[wv]};
+            uint32_t ks[2];
+            for (int j = 0; j < 2; ++j) {
+                uint32_t h = slot_hash(cs[j]) & (kTableSlots - 1);
+                while (true) {
+                    const uint32_t prev = atomicCAS(&a.hkey[h], kNone, cs[j]);
+                    if (prev == kNone || prev == cs[j]) break;
+                    h = (h + 1) & (kTableSlots - 1);
+                }
+                ks[j] = h;
+            }
+            p0 = (ks[0] << 14) | (uint32_t)(2 * i);
+            p1 = (ks[1] << 14) | (uint32_t)(2 * i + 1);
+            a.eval_raw[2 * i] = -deg;
+            a.eval_raw[2 * i + 1] = deg;
+        } else {
+            a.eval_raw[2 * i] = 0;
+            a.eval_raw[2 * i + 1] = 0;
+        }
+        a.etime_raw[2 * i] = (uint32_t)wv;
+        a.etime_raw[2 * i + 1] = (uint32_t)wv;
+        bufA[2 * i] = p0;
+        bufA[2 * i + 1] = p1;
+    }
+    __syncthreads();
+    // Stable LSD radix sort on the slot bits (14..29): two 8-bit passes.
+    // Warp w owns a contiguous chunk; inside it 32-element steps keep order.
+    const int chunk = (m + 31) / 32;
+    uint32_t* src = bufA;
+    uint32_t* dst = bufB;
+    for (int pass = 0; pass < 2; ++pass) {
+        const int shift = 14 + 8 * pass;
+        for (int i = tid; i < 32 * 257; i += blockDim.x) wcnt[i] = 0;
+        __syncthreads();
+        const int c0 = w * chunk, c1 = min(m, c0 + chunk);
+        for (int base = c0; base < c1; base += 32) {
+            const int idx = base + lane;
+            const int d = idx < c1 ? (int)((src[idx] >> shift) & 0xFF) : 256;
+            const unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
+            if (d < 256 && lane == __ffs(peers) - 1) wcnt[w * 257 + d] += __popc(peers);
+            __syncwarp();
+        }
+        __syncthreads();
+        if (tid < 256) {
+            int acc = 0;
+            for (int ww = 0; ww < 32; ++ww) {
+                const int t = wcnt[ww * 257 + tid];
+                wcnt[ww * 257 + tid] = acc;
+                acc += t;
+            }
+            digit_off[tid] = acc;  // digit total for now
+        }
+        __syncthreads();
+        if (tid == 0) {
+            int acc = 0;
+            for (int d = 0; d < 256; ++d) {
+                const int t = digit_off[d];
+                digit_off[d] = acc;
+                acc += t;
+            }
+        }
+        __syncthreads();
+        for (int base = c0; base < c1; base += 32) {
+            const int idx = base + lane;
+            const int d = idx < c1 ? (int)((src[idx] >> shift) & 0xFF) : 256;
+            const unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
+            const unsigned lt = (1u << lane) - 1u;
+            int before = 0;
+            if (d < 256) before = wcnt[w * 257 + d];
+            __syncwarp();
+            if (d < 256) dst[digit_off[d] + before + __popc(peers & lt)] = src[idx];
+            if (d < 256 && lane == __ffs(peers) - 1) wcnt[w * 257 + d] = before + __popc(peers);
+            __syncwarp();
+        }
+        __syncthreads();
+        uint32_t* t = src;
+        src = dst;
+        dst = t;
+    }
+    // src holds the sorted events.  Times, deltas and slot bounds.
+    for (int i = tid; i < m; i += blockDim.x) {
+        const uint32_t pk = src[i];
+        const uint32_t s = pk >> 14, e = pk & 0x3FFF;
+        a.stime[i] = a.etime_raw[e];
+        if (s < (uint32_t)kTableSlots) {
+            if (i == 0 || (src[i - 1] >> 14) != s) a.sstart[s] = i;
+            if (i == m - 1 || (src[i + 1] >> 14) != s) a.send[s] = i + 1;
+        }
+    }
+    // Inclusive scan of the deltas in sorted order (global G in epre), then
+    // per-slot prefix = G[i] - G[start] + val[start].
+    const int per = (m + blockDim.x - 1) / blockDim.x;
+    const int b0 = tid * per, b1 = min(m, b0 + per);
+    long long run = 0;
+    for (int i = b0; i < b1; ++i) run += a.eval_raw[src[i] & 0x3FFF];
+    long long incl = run;
+    for (int o = 1; o < 32; o <<= 1) {
+        const long long t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) warp_tot[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        long long v = warp_tot[lane];
+        long long vi = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long t = __shfl_up_sync(0xFFFFFFFFu, vi, o);
+            if (lane >= o) vi += t;
+        }
+        warp_tot[lane] = vi - v;
+    }
+    __syncthreads();
+    long long acc = warp_tot[w] + incl - run;
+    for (int i = b0; i < b1; ++i) {
+        acc += a.eval_raw[src[i] & 0x3FFF];
+        a.gscan[i] = acc;
+    }
+    __syncthreads();
+    for (int i = tid; i < m; i += blockDim.x) {
+        const uint32_t s = src[i] >> 14;
+        if (s >= (uint32_t)kTableSlots) continue;
+        const int st = a.sstart[s];
+        a.epre[i] = a.gscan[i] - (a.gscan[st] - a.eval_raw[src[st] & 0x3FFF]);
+    }
 }
 
 constexpr int kExWarpsPerBlock = 4;
 
 // Warp per window vertex (degree <= kWarpMaxDeg).
-__global__ void __launch_bounds__(kExWarpsPerBlock * 32)
-k_exact_eval_warp(ExactArgs a) {
+__global__ void __launch_bounds__(kExWarpsPerBlock * 32) k_ex_eval_warp(ExactState a) {
     extern __shared__ uint32_t ex_smem[];
+    if (a.ctl->P >= a.ctl->n) return;
+    const Round r = round_view(a);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     uint32_t* tk = ex_smem + (size_t)w * 2 * kWarpHash;
     uint32_t* tv = tk + kWarpHash;
     const int64_t nw = (int64_t)gridDim.x * kExWarpsPerBlock;
-    for (int64_t u = a.P + (int64_t)blockIdx.x * kExWarpsPerBlock + w; u < a.E; u += nw) {
+    for (int64_t u = r.P + (int64_t)blockIdx.x * kExWarpsPerBlock + w; u < r.E; u += nw) {
         const int64_t rb = a.rp[u];
         const int deg = (int)(a.rp[u + 1] - rb);
         if (deg > kWarpMaxDeg) continue;
-        // Affected at time u: committed flag, or a neighbour before u moved.
         bool act = a.vaff[u] != 0;
         if (!act) {
             bool any = false;
             for (int i = lane; i < deg && !any; i += 32) {
                 const int32_t v = a.col[rb + i];
-                any = (v >= a.P && v < u && prev_mover(a, v));
+                any = (v >= r.P && v < u && prev_mover(a, r, v));
             }
             act = __any_sync(0xFFFFFFFFu, any);
         }
         const uint32_t d = a.vcom[u];
         if (!act) {
-            if (lane == 0) record(a, u, 0, d, 0.0);
+            if (lane == 0) record(a, r, u, 0, d, 0.0);
             continue;
         }
         const double ku = (double)deg;
@@ -144,12 +384,12 @@ k_exact_eval_warp(ExactArgs a) {
             uint32_t c = kNone;
             if (lane < deg) {
                 const int32_t v = a.col[rb + lane];
-                if (v != (int32_t)u) c = comm_at(a, v, u);
+                if (v != (int32_t)u) c = comm_at(a, r, v, u);
             }
             const unsigned peers = __match_any_sync(0xFFFFFFFFu, c);
             const double kud = (double)__popc(__ballot_sync(0xFFFFFFFFu, c == d));
-            const double sd = (double)sigma_at(a, d, (uint32_t)u);
             if (c != kNone && c != d && lane == __ffs(peers) - 1) {
+                const double sd = (double)sigma_at(a, d, (uint32_t)u);
                 const double sc = (double)sigma_at(a, c, (uint32_t)u);
                 const double dl = delta_q((double)__popc(peers), kud, ku, sc, sd, a.M, a.R);
                 if (dl > 0.0) { best_d = dl; best_c = c; }
@@ -164,7 +404,7 @@ k_exact_eval_warp(ExactArgs a) {
                 uint32_t c = kNone;
                 if (base + lane < deg) {
                     const int32_t v = a.col[rb + base + lane];
-                    if (v != (int32_t)u) c = comm_at(a, v, u);
+                    if (v != (int32_t)u) c = comm_at(a, r, v, u);
                 }
                 const unsigned peers = __match_any_sync(0xFFFFFFFFu, c);
                 if (c != kNone && lane == __ffs(peers) - 1) table_add(tk, tv, mask, c, (uint32_t)__popc(peers));
@@ -183,201 +423,230 @@ k_exact_eval_warp(ExactArgs a) {
         }
         warp_argmax(best_d, best_c);
         if (lane == 0) {
-            if (best_d > 0.0 && best_c != kNone && best_c != d) record(a, u, 1, best_c, best_d);
-            else record(a, u, 1, d, 0.0);
+            if (best_d > 0.0 && best_c != kNone && best_c != d) record(a, r, u, 1, best_c, best_d);
+            else record(a, r, u, 1, d, 0.0);
         }
     }
 }
 
-// CTA per window hub (degree > kWarpMaxDeg).
-__global__ void __launch_bounds__(kHubThreads)
-k_exact_eval_hub(ExactArgs a, const uint32_t* __restrict__ hubs, int64_t h0, int64_t h1,
-                 uint32_t* __restrict__ gkeys, uint32_t* __restrict__ gvals, int64_t gcap) {
-    extern __shared__ uint32_t sm[];
-    __shared__ double red_d[kHubThreads / 32];
-    __shared__ uint32_t red_c[kHubThreads / 32];
-    __shared__ uint32_t s_kud;
+// Hub accumulation: one CTA per 4096-edge segment of a window hub.
+__global__ void __launch_bounds__(256) k_ex_hub_accum(ExactState a) {
+    if (a.ctl->P >= a.ctl->n) return;
+    const Round r = round_view(a);
+    const long long q0 = a.ctl->es0, q1 = a.ctl->es1;
+    const int lane = threadIdx.x & 31;
     __shared__ int s_any;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int64_t hi = h0 + blockIdx.x; hi < h1; hi += gridDim.x) {
-        const uint32_t u = hubs[hi];
-        const int64_t rb = a.rp[u];
-        const int64_t deg = a.rp[u + 1] - rb;
-        const uint32_t d = a.vcom[u];
-        if (threadIdx.x == 0) s_any = a.vaff[u] != 0;
+    for (long long q = q0 + blockIdx.x; q < q1; q += gridDim.x) {
+        const HubSeg sg = a.eseg[q];
+        const uint32_t h = a.hub_v[sg.hub];
+        const int64_t rb = a.rp[h], re = a.rp[h + 1];
+        const int64_t e0 = rb + (int64_t)sg.part * kHubSeg, e1 = min(re, e0 + kHubSeg);
+        uint32_t* tk = a.tkeys + a.hub_toff[sg.hub];
+        uint32_t* tv = a.tvals + a.hub_toff[sg.hub];
+        const uint32_t mask = a.hub_tcap[sg.hub] - 1;
+        if (threadIdx.x == 0) s_any = 0;
         __syncthreads();
-        if (!s_any) {
-            bool any = false;
-            for (int64_t i = threadIdx.x; i < deg; i += blockDim.x) {
-                const int32_t v = a.col[rb + i];
-                any = any || (v >= a.P && v < (int64_t)u && prev_mover(a, v));
-            }
-            if (any) atomicOr(&s_any, 1);
-        }
-        __syncthreads();
-        if (!s_any) {
-            if (threadIdx.x == 0) record(a, u, 0, d, 0.0);
-            __syncthreads();
-            continue;
-        }
-        uint32_t H = 1024;
-        while ((int64_t)H < 2 * deg) H <<= 1;
-        uint32_t *tk, *tv;
-        if (H <= (uint32_t)kHubSmemSlots) { tk = sm; tv = sm + kHubSmemSlots; }
-        else { tk = gkeys + (int64_t)blockIdx.x * gcap; tv = gvals + (int64_t)blockIdx.x * gcap; }
-        const uint32_t mask = H - 1;
-        for (uint32_t i = threadIdx.x; i < H; i += blockDim.x) { tk[i] = kNone; tv[i] = 0; }
-        __syncthreads();
-        for (int64_t base = 0; base < deg; base += blockDim.x) {
+        bool any = false;
+        for (int64_t b = e0; b < e1; b += blockDim.x) {
             uint32_t c = kNone;
-            if (base + threadIdx.x < deg) {
-                const int32_t v = a.col[rb + base + threadIdx.x];
-                if (v != (int32_t)u) c = comm_at(a, v, u);
+            const int64_t e = b + threadIdx.x;
+            if (e < e1) {
+                const int32_t v = a.col[e];
+                any = any || (v >= r.P && v < (int64_t)h && prev_mover(a, r, v));
+                if (v != (int32_t)h) c = comm_at(a, r, v, h);
             }
             const unsigned peers = __match_any_sync(0xFFFFFFFFu, c);
             if (c != kNone && lane == __ffs(peers) - 1) table_add(tk, tv, mask, c, (uint32_t)__popc(peers));
         }
+        if (any) s_any = 1;
         __syncthreads();
-        if (threadIdx.x == 0) s_kud = table_get(tk, tv, mask, d);
+        if (threadIdx.x == 0 && s_any) atomicOr(&a.hub_any[sg.hub], 1);
         __syncthreads();
-        const double kud = (double)s_kud, ku = (double)deg;
-        const double sd = (double)sigma_at(a, d, u);
+    }
+}
+
+// Hub selection: one CTA per 4096-slot segment of a window hub's table; the
+// last CTA of a hub reduces the partial maxima and records the decision.
+__global__ void __launch_bounds__(256) k_ex_hub_select(ExactState a) {
+    if (a.ctl->P >= a.ctl->n) return;
+    const Round r = round_view(a);
+    const long long q0 = a.ctl->ts0, q1 = a.ctl->ts1;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __shared__ double red_d[8];
+    __shared__ uint32_t red_c[8];
+    __shared__ int s_last;
+    for (long long q = q0 + blockIdx.x; q < q1; q += gridDim.x) {
+        const HubSeg sg = a.tseg[q];
+        const int j = sg.hub;
+        const uint32_t h = a.hub_v[j];
+        const uint32_t* tk = a.tkeys + a.hub_toff[j];
+        const uint32_t* tv = a.tvals + a.hub_toff[j];
+        const uint32_t cap = a.hub_tcap[j];
+        const uint32_t d = a.vcom[h];
+        const double ku = (double)(a.rp[h + 1] - a.rp[h]);
+        const double kud = (double)table_get(tk, tv, cap - 1, d);
+        const double sd = (double)sigma_at(a, d, h);
         double best_d = 0.0;
         uint32_t best_c = kNone;
-        for (uint32_t i = threadIdx.x; i < H; i += blockDim.x) {
+        const uint32_t s0 = (uint32_t)sg.part * kTabSeg, s1 = min(cap, s0 + kTabSeg);
+        for (uint32_t i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
             const uint32_t c = tk[i];
             if (c == kNone || c == d) continue;
-            const double sc = (double)sigma_at(a, c, u);
+            const double sc = (double)sigma_at(a, c, h);
             const double dl = delta_q((double)tv[i], kud, ku, sc, sd, a.M, a.R);
             if (dl > 0.0 && better(dl, c, best_d, best_c)) { best_d = dl; best_c = c; }
         }
         warp_argmax(best_d, best_c);
         if (lane == 0) { red_d[w] = best_d; red_c[w] = best_c; }
         __syncthreads();
-        if (w == 0) {
-            best_d = lane < (int)(blockDim.x / 32) ? red_d[lane] : 0.0;
-            best_c = lane < (int)(blockDim.x / 32) ? red_c[lane] : kNone;
-            warp_argmax(best_d, best_c);
-            if (lane == 0) {
-                if (best_d > 0.0 && best_c != kNone && best_c != d) record(a, u, 1, best_c, best_d);
-                else record(a, u, 1, d, 0.0);
+        if (threadIdx.x == 0) {
+            double bd = red_d[0];
+            uint32_t bc = red_c[0];
+            for (int k = 1; k < (int)(blockDim.x / 32); ++k)
+                if (better(red_d[k], red_c[k], bd, bc)) { bd = red_d[k]; bc = red_c[k]; }
+            a.part_d[q] = bd;
+            a.part_c[q] = bc;
+            __threadfence();
+            s_last = atomicAdd(&a.hub_done[j], 1) == a.hub_tcount[j] - 1;
+        }
+        __syncthreads();
+        if (s_last && threadIdx.x == 0) {
+            __threadfence();
+            double bd = 0.0;
+            uint32_t bc = kNone;
+            const int f = a.hub_tfirst[j];
+            for (int k = 0; k < a.hub_tcount[j]; ++k) {
+                const double pd = ((volatile double*)a.part_d)[f + k];
+                const uint32_t pc = ((volatile uint32_t*)a.part_c)[f + k];
+                if (better(pd, pc, bd, bc)) { bd = pd; bc = pc; }
             }
+            const bool act = a.vaff[h] != 0 || ((volatile int32_t*)a.hub_any)[j] != 0;
+            if (!act) record(a, r, h, 0, d, 0.0);
+            else if (bd > 0.0 && bc != kNone && bc != d) record(a, r, h, 1, bc, bd);
+            else record(a, r, h, 1, d, 0.0);
+            a.hub_done[j] = 0;
+            a.hub_any[j] = 0;
         }
         __syncthreads();
     }
 }
 
-// Event emission: two slots per window vertex (old, new), padding key = TS.
-__global__ void k_exact_events(const int64_t* __restrict__ rp, const uint32_t* __restrict__ vcom,
-                               const uint32_t* __restrict__ pbest, const uint8_t* __restrict__ pact, int64_t P,
-                               int64_t E, int64_t B, uint32_t* __restrict__ hkey, uint32_t hmask,
-                               uint32_t* __restrict__ ekey, uint32_t* __restrict__ eidx, uint32_t* __restrict__ etime,
-                               long long* __restrict__ eval) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < B; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t w = P + i;
-        uint32_t k0 = hmask + 1, k1 = hmask + 1;
-        if (w < E && pact[w] == 1 && pbest[w] != vcom[w]) {
-            const long long deg = (long long)(rp[w + 1] - rp[w]);
-            const uint32_t cs[2] = {vcom[w], pbest[w]};
-            uint32_t ks[2];
-            for (int j = 0; j < 2; ++j) {
-                uint32_t h = slot_hash(cs[j]) & hmask;
-                while (true) {
-                    const uint32_t prev = atomicCAS(&hkey[h], kNone, cs[j]);
-                    if (prev == kNone || prev == cs[j]) break;
-                    h = (h + 1) & hmask;
-                }
-                ks[j] = h;
-            }
-            k0 = ks[0];
-            k1 = ks[1];
-            eval[2 * i] = -deg;
-            eval[2 * i + 1] = deg;
-        } else {
-            eval[2 * i] = 0;
-            eval[2 * i + 1] = 0;
+__global__ void __launch_bounds__(256) k_ex_hub_clear(ExactState a) {
+    if (a.ctl->P >= a.ctl->n) return;
+    const long long q0 = a.ctl->ts0, q1 = a.ctl->ts1;
+    for (long long q = q0 + blockIdx.x; q < q1; q += gridDim.x) {
+        const HubSeg sg = a.tseg[q];
+        uint32_t* tk = a.tkeys + a.hub_toff[sg.hub];
+        uint32_t* tv = a.tvals + a.hub_toff[sg.hub];
+        const uint32_t s0 = (uint32_t)sg.part * kTabSeg, s1 = min(a.hub_tcap[sg.hub], s0 + kTabSeg);
+        for (uint32_t i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
+            tk[i] = kNone;
+            tv[i] = 0;
         }
-        ekey[2 * i] = k0;
-        ekey[2 * i + 1] = k1;
-        eidx[2 * i] = (uint32_t)(2 * i);
-        eidx[2 * i + 1] = (uint32_t)(2 * i + 1);
-        etime[2 * i] = (uint32_t)w;
-        etime[2 * i + 1] = (uint32_t)w;
     }
 }
 
-// After the stable sort by slot: gather times/deltas, segment bounds.
-__global__ void k_exact_segments(const uint32_t* __restrict__ skey, const uint32_t* __restrict__ sidx,
-                                 const uint32_t* __restrict__ etime, const long long* __restrict__ eval, int64_t m,
-                                 uint32_t TS, uint32_t* __restrict__ stime, long long* __restrict__ sval,
-                                 int32_t* __restrict__ sstart, int32_t* __restrict__ send) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t s = skey[i];
-        stime[i] = etime[sidx[i]];
-        sval[i] = eval[sidx[i]];
-        if (s >= TS) continue;
-        if (i == 0 || skey[i - 1] != s) sstart[s] = (int32_t)i;
-        if (i == m - 1 || skey[i + 1] != s) send[s] = (int32_t)(i + 1);
-    }
+__device__ __forceinline__ long long commit_end(const ExactState& a) {
+    const unsigned long long f = a.ctl->first_change;
+    const long long E = a.ctl->E;
+    return f == kNoChange ? E - 1 : min((long long)f, E - 1);
 }
 
-// Inclusive prefix within each slot from a global exclusive scan X of sval.
-__global__ void k_exact_prefix(const uint32_t* __restrict__ skey, const long long* __restrict__ sval,
-                               const int64_t* __restrict__ X, const int32_t* __restrict__ sstart, int64_t m,
-                               uint32_t TS, long long* __restrict__ epre) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t s = skey[i];
-        if (s >= TS) continue;
-        epre[i] = X[i] + sval[i] - X[sstart[s]];
-    }
-}
-
-// Commit [P, x]: totals and communities of movers; processed flags cleared.
-__global__ void k_exact_commit_a(const int64_t* __restrict__ rp, uint32_t* __restrict__ vcom,
-                                 unsigned long long* __restrict__ ctot, uint8_t* __restrict__ vaff,
-                                 const uint32_t* __restrict__ nbest, const uint8_t* __restrict__ nact,
-                                 const double* __restrict__ ndelta, double* __restrict__ final_delta, int64_t P,
-                                 int64_t x) {
-    for (int64_t u = P + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u <= x; u += (int64_t)gridDim.x * blockDim.x) {
+// Commit [P, x]: totals of movers, final deltas, processed flags cleared.
+__global__ void k_ex_commit_a(ExactState a) {
+    if (a.ctl->P >= a.ctl->n) return;
+    const Round r = round_view(a);
+    const long long x = commit_end(a);
+    for (long long u = r.P + blockIdx.x * (long long)blockDim.x + threadIdx.x; u <= x;
+         u += (long long)gridDim.x * blockDim.x) {
         double dl = 0.0;
-        if (nact[u] == 1 && nbest[u] != vcom[u]) {
-            const long long deg = (long long)(rp[u + 1] - rp[u]);
-            atomicAdd(&ctot[vcom[u]], (unsigned long long)(-deg));
-            atomicAdd(&ctot[nbest[u]], (unsigned long long)deg);
-            dl = ndelta[u];
+        if (r.nact[u] == 1 && r.nbest[u] != a.vcom[u]) {
+            const long long deg = (long long)(a.rp[u + 1] - a.rp[u]);
+            atomicAdd(&a.ctot[a.vcom[u]], (unsigned long long)(-deg));
+            atomicAdd(&a.ctot[r.nbest[u]], (unsigned long long)deg);
+            dl = r.ndelta[u];
         }
-        final_delta[u] = dl;
-        vaff[u] = 0;
+        a.final_delta[u] = dl;
+        a.vaff[u] = 0;
     }
 }
 
-// Affected flags set by the committed movers: every neighbour outside [P, x]
-// and every neighbour in [P, x] processed before the mover.
-__global__ void k_exact_commit_b(const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
-                                 uint32_t* __restrict__ vcom, uint8_t* __restrict__ vaff,
-                                 const uint32_t* __restrict__ nbest, const uint8_t* __restrict__ nact, int64_t P,
-                                 int64_t x) {
+// Affected flags from committed movers: every neighbour outside [P, x] and
+// every neighbour in [P, x] processed before the mover.  Non-hub movers here,
+// hub movers in k_ex_commit_hub.
+__global__ void k_ex_commit_b(ExactState a) {
+    if (a.ctl->P >= a.ctl->n) return;
+    const Round r = round_view(a);
+    const long long x = commit_end(a);
     const int lane = threadIdx.x & 31;
-    const int64_t wid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t w = P + wid; w <= x; w += nw) {
-        if (!(nact[w] == 1 && nbest[w] != vcom[w])) continue;
-        for (int64_t e = rp[w] + lane; e < rp[w + 1]; e += 32) {
-            const int32_t v = col[e];
-            if (v < P || v > x || v < w) vaff[v] = 1;
+    const long long wid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long w = r.P + wid; w <= x; w += nw) {
+        if (!(r.nact[w] == 1 && r.nbest[w] != a.vcom[w])) continue;
+        const int64_t rb = a.rp[w], re = a.rp[w + 1];
+        if (re - rb > kWarpMaxDeg) continue;
+        for (int64_t e = rb + lane; e < re; e += 32) {
+            const int32_t v = a.col[e];
+            if (v < r.P || v > x || v < w) a.vaff[v] = 1;
         }
     }
 }
 
-__global__ void k_exact_commit_c(uint32_t* __restrict__ vcom, const uint32_t* __restrict__ nbest,
-                                 const uint8_t* __restrict__ nact, int64_t P, int64_t x) {
-    for (int64_t u = P + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u <= x; u += (int64_t)gridDim.x * blockDim.x)
-        if (nact[u] == 1) vcom[u] = nbest[u];
+__global__ void __launch_bounds__(256) k_ex_commit_hub(ExactState a) {
+    if (a.ctl->P >= a.ctl->n) return;
+    const Round r = round_view(a);
+    const long long x = commit_end(a);
+    const long long q0 = a.ctl->es0;
+    const long long q1 = lower_bound_u32(a.eseg_v, a.n_eseg, (uint32_t)(x + 1));
+    for (long long q = q0 + blockIdx.x; q < q1; q += gridDim.x) {
+        const HubSeg sg = a.eseg[q];
+        const uint32_t h = a.hub_v[sg.hub];
+        if (!(r.nact[h] == 1 && r.nbest[h] != a.vcom[h])) continue;
+        const int64_t rb = a.rp[h], re = a.rp[h + 1];
+        const int64_t e0 = rb + (int64_t)sg.part * kHubSeg, e1 = min(re, e0 + kHubSeg);
+        for (int64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+            const int32_t v = a.col[e];
+            if (v < r.P || v > x || v < (int64_t)h) a.vaff[v] = 1;
+        }
+    }
 }
 
-__global__ void k_exact_mark_unknown(uint8_t* __restrict__ pact, int64_t a, int64_t b) {
-    for (int64_t u = a + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < b; u += (int64_t)gridDim.x * blockDim.x)
-        pact[u] = kUnknown;
+__global__ void k_ex_commit_c(ExactState a) {
+    if (a.ctl->P >= a.ctl->n) return;
+    const Round r = round_view(a);
+    const long long x = commit_end(a);
+    for (long long u = r.P + blockIdx.x * (long long)blockDim.x + threadIdx.x; u <= x;
+         u += (long long)gridDim.x * blockDim.x)
+        if (r.nact[u] == 1) a.vcom[u] = r.nbest[u];
+}
+
+// Slide the window: the new decisions become D_prev; entering vertices are unknown.
+__global__ void __launch_bounds__(1024) k_ex_advance(ExactState a) {
+    const long long P = a.ctl->P, E = a.ctl->E, n = a.ctl->n, B = a.ctl->B;
+    if (P >= n) return;
+    const long long x = commit_end(a);
+    const long long nP = x + 1, nE = min(n, nP + B);
+    const int par = (int)(a.ctl->round & 1);
+    uint8_t* next_prev_act = a.act[par ^ 1];
+    for (long long u = E + threadIdx.x; u < nE; u += blockDim.x) next_prev_act[u] = kUnknown;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        a.ctl->P = nP;
+        a.ctl->E = nE;
+        a.ctl->round = a.ctl->round + 1;
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_ex_init_iter(ExactState a) {
+    const long long n = a.ctl->n, B = a.ctl->B;
+    const long long E = min(n, B);
+    for (long long u = threadIdx.x; u < E; u += blockDim.x) a.act[0][u] = kUnknown;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        a.ctl->P = 0;
+        a.ctl->E = E;
+        a.ctl->round = 0;
+    }
 }
 
 // Deterministic tree sum of the iteration's committed deltas (and count).
@@ -387,7 +656,6 @@ __global__ void k_sum_deltas(const double* __restrict__ d, int64_t n, double* __
     unsigned long long c = 0;
     const int64_t per = (n + gridDim.x - 1) / gridDim.x;
     const int64_t b = blockIdx.x * per, e = min(n, b + per);
-    // fixed per-thread strided order inside the block's fixed range
     for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
         s += d[i];
         c += d[i] != 0.0;
@@ -419,6 +687,12 @@ __global__ void k_sum_serial(const double* __restrict__ d, int64_t n, double* __
     }
 }
 
+__global__ void k_hub_degrees(const int64_t* __restrict__ rp, const uint32_t* __restrict__ hubs, int64_t nh,
+                              int64_t* __restrict__ deg) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nh; j += (int64_t)gridDim.x * blockDim.x)
+        deg[j] = rp[hubs[j] + 1] - rp[hubs[j]];
+}
+
 template <typename T>
 T read_dev(const T* p, cudaStream_t s) {
     T h;
@@ -427,102 +701,166 @@ T read_dev(const T* p, cudaStream_t s) {
     return h;
 }
 
+template <typename T>
+DevBuf<T> upload(const std::vector<T>& v, cudaStream_t s) {
+    DevBuf<T> d(v.empty() ? 1 : v.size(), s);
+    if (!v.empty()) GB_CUDA(cudaMemcpyAsync(d.get(), v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    return d;
+}
+
 }  // namespace
 
 int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iterations, int64_t window,
                      cudaStream_t s, int64_t* launches, int64_t* rounds_out) {
     const int64_t n = ctx.g.n;
-    const int64_t B = std::max<int64_t>(32, std::min<int64_t>(window, n));
-    const int64_t m = 2 * B;
-    uint32_t TS = 1024;
-    while ((int64_t)TS < 2 * m) TS <<= 1;
-    const int sort_bits = bits_for(TS);
+    const int64_t B = std::max<int64_t>(32, std::min<int64_t>(std::min<int64_t>(window, kWindowMax), n));
 
-    DevBuf<uint32_t> pbest(n, s), nbest(n, s);
-    DevBuf<uint8_t> pact(n, s), nact(n, s);
-    DevBuf<double> ndelta(n, s), final_delta(n, s);
-    DevBuf<uint32_t> hkey(TS, s), ekey(m, s), eidx(m, s), etime(m, s), stime(m, s);
-    DevBuf<long long> eval(m, s), sval(m, s), epre(m, s);
-    DevBuf<int64_t> X(m, s);
-    DevBuf<int32_t> sstart(TS, s), send(TS, s);
-    DevBuf<unsigned long long> fc(1, s);
+    // ---- hub segment tables (once per call) ----
+    const int64_t nh = (int64_t)ctx.hubs_h.size();
+    std::vector<int64_t> hdeg(nh);
+    if (nh) {
+        DevBuf<int64_t> dd(nh, s);
+        k_hub_degrees<<<grid_for(nh, kT), kT, 0, s>>>(ctx.g.row_ptr, ctx.hubs, nh, dd);
+        GB_LAUNCH_CHECK();
+        GB_CUDA(cudaMemcpyAsync(hdeg.data(), dd.get(), nh * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        GB_CUDA(cudaStreamSynchronize(s));
+    }
+    std::vector<int64_t> toff(nh);
+    std::vector<uint32_t> tcap(nh);
+    std::vector<int32_t> tfirst(nh), tcount(nh);
+    std::vector<HubSeg> eseg, tseg;
+    std::vector<uint32_t> eseg_v, tseg_v;
+    int64_t pool = 0;
+    for (int64_t j = 0; j < nh; ++j) {
+        uint32_t cap = 64;
+        while ((int64_t)cap < 2 * hdeg[j]) cap <<= 1;
+        tcap[j] = cap;
+        toff[j] = pool;
+        pool += cap;
+        const int ne = (int)ceil_div(hdeg[j], kHubSeg);
+        for (int k = 0; k < ne; ++k) {
+            eseg.push_back({(int32_t)j, k});
+            eseg_v.push_back(ctx.hubs_h[j]);
+        }
+        const int nt = (int)ceil_div(cap, kTabSeg);
+        tfirst[j] = (int32_t)tseg.size();
+        tcount[j] = nt;
+        for (int k = 0; k < nt; ++k) {
+            tseg.push_back({(int32_t)j, k});
+            tseg_v.push_back(ctx.hubs_h[j]);
+        }
+    }
+    DevBuf<int64_t> d_toff = upload(toff, s);
+    DevBuf<uint32_t> d_tcap = upload(tcap, s);
+    DevBuf<int32_t> d_tfirst = upload(tfirst, s), d_tcount = upload(tcount, s);
+    DevBuf<HubSeg> d_eseg = upload(eseg, s), d_tseg = upload(tseg, s);
+    DevBuf<uint32_t> d_eseg_v = upload(eseg_v, s), d_tseg_v = upload(tseg_v, s);
+    DevBuf<uint32_t> tkeys(pool > 0 ? pool : 1, s), tvals(pool > 0 ? pool : 1, s);
+    GB_CUDA(cudaMemsetAsync(tkeys, 0xFF, (pool > 0 ? pool : 1) * sizeof(uint32_t), s));
+    GB_CUDA(cudaMemsetAsync(tvals, 0, (pool > 0 ? pool : 1) * sizeof(uint32_t), s));
+    DevBuf<int32_t> hub_any(nh > 0 ? nh : 1, s), hub_done(nh > 0 ? nh : 1, s);
+    GB_CUDA(cudaMemsetAsync(hub_any, 0, (nh > 0 ? nh : 1) * sizeof(int32_t), s));
+    GB_CUDA(cudaMemsetAsync(hub_done, 0, (nh > 0 ? nh : 1) * sizeof(int32_t), s));
+    DevBuf<double> part_d(tseg.empty() ? 1 : tseg.size(), s);
+    DevBuf<uint32_t> part_c(tseg.empty() ? 1 : tseg.size(), s);
+
+    // ---- round state ----
+    DevBuf<uint32_t> best0(n, s), best1(n, s);
+    DevBuf<uint8_t> act0(n, s), act1(n, s);
+    DevBuf<double> delta0(n, s), delta1(n, s), final_delta(n, s);
+    DevBuf<uint32_t> hkey(kTableSlots, s), etime_raw(kEventsMax, s), stime(kEventsMax, s);
+    DevBuf<int32_t> sstart(kTableSlots, s), send(kTableSlots, s);
+    DevBuf<long long> eval_raw(kEventsMax, s), epre(kEventsMax, s), gscan(kEventsMax, s);
+    DevBuf<Ctl> ctl(1, s);
+    Ctl* hctl = nullptr;
+    GB_CUDA(cudaMallocHost(&hctl, sizeof(Ctl)));
+    *hctl = Ctl{};
+    hctl->n = n;
+    hctl->B = B;
+    GB_CUDA(cudaMemcpyAsync(ctl.get(), hctl, sizeof(Ctl), cudaMemcpyHostToDevice, s));
     DevBuf<double> partial(1024, s), dsum(1, s);
     DevBuf<unsigned long long> nmov(1, s);
 
+    ExactState a{};
+    a.rp = ctx.g.row_ptr;
+    a.col = ctx.g.col;
+    a.vcom = ctx.vcom;
+    a.ctot = ctx.ctot;
+    a.vaff = ctx.vaff;
+    a.ctl = ctl.get();
+    a.best[0] = best0.get();
+    a.best[1] = best1.get();
+    a.act[0] = act0.get();
+    a.act[1] = act1.get();
+    a.delta[0] = delta0.get();
+    a.delta[1] = delta1.get();
+    a.final_delta = final_delta.get();
+    a.hkey = hkey.get();
+    a.sstart = sstart.get();
+    a.send = send.get();
+    a.etime_raw = etime_raw.get();
+    a.eval_raw = eval_raw.get();
+    a.stime = stime.get();
+    a.epre = epre.get();
+    a.gscan = gscan.get();
+    a.hub_v = ctx.hubs;
+    a.hub_toff = d_toff.get();
+    a.hub_tcap = d_tcap.get();
+    a.hub_tfirst = d_tfirst.get();
+    a.hub_tcount = d_tcount.get();
+    a.eseg = d_eseg.get();
+    a.eseg_v = d_eseg_v.get();
+    a.n_eseg = (long long)eseg.size();
+    a.tseg = d_tseg.get();
+    a.tseg_v = d_tseg_v.get();
+    a.n_tseg = (long long)tseg.size();
+    a.tkeys = tkeys.get();
+    a.tvals = tvals.get();
+    a.hub_any = hub_any.get();
+    a.hub_done = hub_done.get();
+    a.part_d = part_d.get();
+    a.part_c = part_c.get();
+    a.M = ctx.M;
+    a.R = ctx.R;
+
+    const int table_smem = (2 * kEventsMax + 32 * 257) * (int)sizeof(uint32_t);
+    GB_CUDA(cudaFuncSetAttribute(k_ex_table, cudaFuncAttributeMaxDynamicSharedMemorySize, table_smem));
     const int eval_smem = kExWarpsPerBlock * 2 * kWarpHash * (int)sizeof(uint32_t);
-    GB_CUDA(cudaFuncSetAttribute(k_exact_eval_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, eval_smem));
-    const int hub_smem = 2 * kHubSmemSlots * (int)sizeof(uint32_t);
-    GB_CUDA(cudaFuncSetAttribute(k_exact_eval_hub, cudaFuncAttributeMaxDynamicSharedMemorySize, hub_smem));
+    GB_CUDA(cudaFuncSetAttribute(k_ex_eval_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, eval_smem));
+    const int eval_grid = (int)std::min<int64_t>(ceil_div(B, kExWarpsPerBlock), (int64_t)kNumSMs * 16);
+    const int hub_grid = kNumSMs * 4;
+    const int commit_grid = (int)std::max<int64_t>(1, ceil_div(B, kT));
+    const int commit_b_grid = (int)std::max<int64_t>(1, ceil_div(B * 32, kT));
+    const int kBatch = 8;
 
     int iterations = 0;
     int64_t rounds = 0, nl = 0;
-    uint32_t* pb = pbest.get();
-    uint32_t* nb = nbest.get();
-    uint8_t* pa = pact.get();
-    uint8_t* na = nact.get();
     for (int it = 0; it < max_iterations; ++it) {
-        int64_t P = 0;
-        int64_t E = std::min(n, P + B);
-        k_exact_mark_unknown<<<grid_for(E, kT), kT, 0, s>>>(pa, 0, E);
+        k_ex_init_iter<<<1, 1024, 0, s>>>(a);
         GB_LAUNCH_CHECK();
         ++nl;
-        size_t hcur = 0;
-        while (P < n) {
-            ++rounds;
-            // Event table from D_prev.
-            GB_CUDA(cudaMemsetAsync(hkey, 0xFF, TS * sizeof(uint32_t), s));
-            k_exact_events<<<grid_for(B, kT), kT, 0, s>>>(ctx.g.row_ptr, ctx.vcom, pb, pa, P, E, B, hkey, TS - 1,
-                                                         ekey, eidx, etime, eval);
-            GB_LAUNCH_CHECK();
-            radix_sort_pairs_u32(ekey, eidx, m, sort_bits, s);
-            k_exact_segments<<<grid_for(m, kT), kT, 0, s>>>(ekey, eidx, etime, eval, m, TS, stime, sval, sstart,
-                                                           send);
-            GB_LAUNCH_CHECK();
-            exclusive_scan_i64(reinterpret_cast<const int64_t*>(sval.get()), X, m, s);
-            k_exact_prefix<<<grid_for(m, kT), kT, 0, s>>>(ekey, sval, X, sstart, m, TS, epre);
-            GB_LAUNCH_CHECK();
-            // Evaluate the window.
-            GB_CUDA(cudaMemsetAsync(fc, 0xFF, sizeof(unsigned long long), s));
-            ExactArgs a{ctx.g.row_ptr, ctx.g.col, ctx.vcom, ctx.ctot, ctx.vaff, pb, pa, nb, na, ndelta,
-                        hkey, TS - 1, sstart, send, stime, epre, P, E, ctx.M, ctx.R, fc};
-            const int grid = (int)std::min<int64_t>(ceil_div(E - P, kExWarpsPerBlock), (int64_t)kNumSMs * 16);
-            k_exact_eval_warp<<<grid, kExWarpsPerBlock * 32, eval_smem, s>>>(a);
-            GB_LAUNCH_CHECK();
-            while (hcur < ctx.hubs_h.size() && (int64_t)ctx.hubs_h[hcur] < P) ++hcur;
-            size_t hend = hcur;
-            while (hend < ctx.hubs_h.size() && (int64_t)ctx.hubs_h[hend] < E) ++hend;
-            if (hend > hcur) {
-                const int hg = (int)std::min<size_t>(hend - hcur, (size_t)ctx.hub_grid);
-                k_exact_eval_hub<<<hg, kHubThreads, hub_smem, s>>>(a, ctx.hubs, (int64_t)hcur, (int64_t)hend,
-                                                                   ctx.hub_gk, ctx.hub_gv, ctx.hub_gcap);
+        while (true) {
+            for (int b = 0; b < kBatch; ++b) {
+                k_ex_table<<<1, kEvThreads, table_smem, s>>>(a);
+                k_ex_eval_warp<<<eval_grid, kExWarpsPerBlock * 32, eval_smem, s>>>(a);
+                if (nh) {
+                    k_ex_hub_accum<<<hub_grid, 256, 0, s>>>(a);
+                    k_ex_hub_select<<<hub_grid, 256, 0, s>>>(a);
+                    k_ex_hub_clear<<<hub_grid, 256, 0, s>>>(a);
+                }
+                k_ex_commit_a<<<commit_grid, kT, 0, s>>>(a);
+                k_ex_commit_b<<<commit_b_grid, kT, 0, s>>>(a);
+                if (nh) k_ex_commit_hub<<<hub_grid, 256, 0, s>>>(a);
+                k_ex_commit_c<<<commit_grid, kT, 0, s>>>(a);
+                k_ex_advance<<<1, 1024, 0, s>>>(a);
                 GB_LAUNCH_CHECK();
-                ++nl;
+                nl += nh ? 10 : 6;
             }
-            const unsigned long long first = read_dev(fc.get(), s);
-            const int64_t x = (first == ~0ull) ? E - 1 : (int64_t)first;
-            // Commit [P, x].
-            k_exact_commit_a<<<grid_for(x - P + 1, kT), kT, 0, s>>>(ctx.g.row_ptr, ctx.vcom, ctx.ctot, ctx.vaff,
-                                                                   nb, na, ndelta, final_delta, P, x);
-            GB_LAUNCH_CHECK();
-            k_exact_commit_b<<<grid_for((x - P + 1) * 32, kT), kT, 0, s>>>(ctx.g.row_ptr, ctx.g.col, ctx.vcom,
-                                                                           ctx.vaff, nb, na, P, x);
-            GB_LAUNCH_CHECK();
-            k_exact_commit_c<<<grid_for(x - P + 1, kT), kT, 0, s>>>(ctx.vcom, nb, na, P, x);
-            GB_LAUNCH_CHECK();
-            nl += 9 + 3 * ((sort_bits + 7) / 8) + 3;
-            // Slide: new decisions become D_prev; vertices entering are unknown.
-            std::swap(pb, nb);
-            std::swap(pa, na);
-            const int64_t newP = x + 1;
-            const int64_t newE = std::min(n, newP + B);
-            if (newE > E) {
-                k_exact_mark_unknown<<<grid_for(newE - E, kT), kT, 0, s>>>(pa, E, newE);
-                GB_LAUNCH_CHECK();
-                ++nl;
-            }
-            P = newP;
-            E = newE;
+            GB_CUDA(cudaMemcpyAsync(hctl, ctl.get(), sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+            GB_CUDA(cudaStreamSynchronize(s));
+            if (hctl->P >= n) break;
         }
+        rounds += hctl->round;
         ++iterations;
         // totalDelta <= tolerance, decided exactly.
         const int sb = 1024;
@@ -548,6 +886,7 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
         nl += 2;
         if (stop) break;
     }
+    cudaFreeHost(hctl);
     if (launches) *launches += nl;
     if (rounds_out) *rounds_out += rounds;
     return iterations;

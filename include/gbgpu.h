@@ -198,6 +198,50 @@ int gbgpu_validate_permutation_noalloc(gbgpu_ctx* ctx, const int32_t* new_ids_de
  * it ("Mapping Fingerprint"). */
 uint64_t gbgpu_fingerprint(const int32_t* new_ids, int64_t n);
 
+/* ---- Consumers timed after a mapping, and the selector's other arm ----
+ * The reference's "map + kernel" end-to-end time is the mapping plus runs of
+ * a benchmark kernel on the relabelled graph.  *ms_out (may be NULL) receives
+ * the device time of the kernel itself.
+ *   gbgpu_pagerank   -> PageRank pull form (bench/src/pr.cc:40-90): damping 0.85,
+ *                       Jacobi sweeps until the L1 change < epsilon or max_iters;
+ *                       scores agree with a float64 restatement to float tolerance
+ *   gbgpu_bfs        -> BFS depths from `source` (bench/src/bfs.cc), -1 = unreached
+ *   gbgpu_connected_components -> component = smallest vertex id in it (bench/src/cc.cc)
+ *   gbgpu_dbg_mapping -> GenerateDBGMapping (bench/include/graphbrew/reorder/
+ *                       reorder_hub.h:267-342), bit-exact */
+int gbgpu_pagerank(gbgpu_ctx* ctx, const int64_t* row_ptr, const int32_t* col, int64_t n, int64_t nnz,
+                   int32_t max_iters, double epsilon, float* scores_out, int32_t* iters_out, double* ms_out,
+                   uint32_t flags);
+int gbgpu_bfs(gbgpu_ctx* ctx, const int64_t* row_ptr, const int32_t* col, int64_t n, int64_t nnz,
+              int64_t source, int32_t* depth_out, double* ms_out, uint32_t flags);
+int gbgpu_connected_components(gbgpu_ctx* ctx, const int64_t* row_ptr, const int32_t* col, int64_t n,
+                               int64_t nnz, int32_t* comp_out, double* ms_out, uint32_t flags);
+int gbgpu_dbg_mapping(gbgpu_ctx* ctx, const int64_t* row_ptr, const int32_t* col, int64_t n, int64_t nnz,
+                      int32_t* new_ids_out, double* ms_out, uint32_t flags);
+
+/* ---- Selector ----
+ * gbgpu_tier0_features -> ComputeTier0SampledGraphFeatures
+ *   (bench/include/graphbrew/reorder/reorder_types.h:6066-6186).  features_out
+ *   is always a HOST array of 9 doubles: num_nodes, num_edges, avg_degree,
+ *   degree_cv, internal_density, hub_concentration, packing_factor,
+ *   normalized_edge_span, window_neighbor_overlap.
+ * The learned selector is a float32 MLP in_dim -> 64 -> 64 -> 3 (ReLU) whose
+ * outputs are predicted log end-to-end times of the arms (algorithm 12, DBG,
+ * original order).  Parameters are packed W1[in x 64], b1, W2[64 x 64], b2,
+ * W3[64 x 3], b3 (row-major, input index first).  Loss is the mean squared
+ * error over rows x 3 outputs; gbgpu_mlp_train runs Adam (0.9, 0.999, 1e-8) on
+ * minibatches of a seeded shuffle and returns the last epoch's mean loss. */
+int gbgpu_tier0_features(gbgpu_ctx* ctx, const int64_t* row_ptr, const int32_t* col, int64_t n, int64_t nnz,
+                         double* features_out, uint32_t flags);
+int gbgpu_mlp_param_count(int32_t in_dim);
+int gbgpu_mlp_forward(gbgpu_ctx* ctx, const float* params, const float* X, int32_t rows, int32_t in_dim,
+                      float* Y, uint32_t flags);
+int gbgpu_mlp_gradient(gbgpu_ctx* ctx, const float* params, const float* X, const float* T, int32_t rows,
+                       int32_t in_dim, float* grad_out, float* loss_out, uint32_t flags);
+int gbgpu_mlp_train(gbgpu_ctx* ctx, float* params_inout, const float* X, const float* T, int32_t rows,
+                    int32_t in_dim, int32_t epochs, int32_t batch, float lr, uint64_t seed, float* loss_out,
+                    uint32_t flags);
+
 /* Library version string. */
 const char* gbgpu_version(void);
 

@@ -120,6 +120,8 @@ def load_reference():
         lib.ref_gapbs_generate.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int64), C.c_int]
         lib.ref_last_graph_copy.argtypes = [_i64p, _i32p]
         lib.ref_set_threads.argtypes = [C.c_int]
+        lib.ref_dbg_mapping.argtypes = [C.c_int64, _i64p, _i32p, _i32p]
+        lib.ref_tier0_features.argtypes = [C.c_int64, _i64p, _i32p, C.POINTER(C.c_double)]
         _ref = lib
     return _ref
 
@@ -277,6 +279,28 @@ def ref_gapbs_graph(scale, degree=16, uniform=False):
     cl = np.zeros(nnz.value, dtype=np.int32)
     ref.ref_last_graph_copy(rp, cl)
     return rp, cl
+
+
+def ref_dbg_mapping(row_ptr, col):
+    ref = load_reference()
+    rp = np.ascontiguousarray(row_ptr, dtype=np.int64)
+    cl = np.ascontiguousarray(col, dtype=np.int32)
+    out = np.zeros(len(rp) - 1, dtype=np.int32)
+    ref.ref_dbg_mapping(len(rp) - 1, rp, cl, out)
+    return out
+
+
+def ref_tier0_features(row_ptr, col):
+    ref = load_reference()
+    rp = np.ascontiguousarray(row_ptr, dtype=np.int64)
+    cl = np.ascontiguousarray(col, dtype=np.int32)
+    out = (C.c_double * 9)()
+    ref.ref_tier0_features(len(rp) - 1, rp, cl, out)
+    return dict(zip(TIER0_KEYS, list(out)))
+
+
+TIER0_KEYS = ("num_nodes", "num_edges", "avg_degree", "degree_cv", "internal_density", "hub_concentration",
+              "packing_factor", "normalized_edge_span", "window_neighbor_overlap")
 
 
 # --------------------------------------------------------------------------

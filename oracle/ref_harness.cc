@@ -273,4 +273,26 @@ void ref_last_graph_copy(int64_t* row_ptr, int32_t* col) {
     }
 }
 
+// GenerateDBGMapping (reorder_hub.h:267-342) on out-degrees.
+void ref_dbg_mapping(int64_t n, const int64_t* row_ptr, const int32_t* col, int32_t* new_ids) {
+    QuietStdout q(true);
+    Graph g = MakeGraph(n, row_ptr, col);
+    pvector<NodeID> ids(n);
+    ::GenerateDBGMapping(g, ids, true);
+    for (int64_t i = 0; i < n; ++i) new_ids[i] = ids[i];
+}
+
+// ComputeTier0SampledGraphFeatures (reorder_types.h:6066-6186), sample seed 0;
+// out = num_nodes, num_edges, avg_degree, degree_variance (cv), internal_density,
+// hub_concentration, packing_factor, avg_reuse_distance (normalised span),
+// window_neighbor_overlap.
+void ref_tier0_features(int64_t n, const int64_t* row_ptr, const int32_t* col, double* out) {
+    Graph g = MakeGraph(n, row_ptr, col);
+    const CommunityFeatures f = ComputeTier0SampledGraphFeatures(g);
+    const double v[9] = {(double)f.num_nodes, (double)f.num_edges, f.avg_degree, f.degree_variance,
+                         f.internal_density, f.hub_concentration, f.packing_factor, f.avg_reuse_distance,
+                         f.window_neighbor_overlap};
+    for (int i = 0; i < 9; ++i) out[i] = v[i];
+}
+
 }  // extern "C"

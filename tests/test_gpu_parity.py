@@ -119,7 +119,7 @@ def test_serial_mapping_bit_exact(ctx, name, manifest, golden_arrays):
     assert gb.mapping_fingerprint(ids) == case["serial_fingerprint"]
 
 
-@pytest.mark.parametrize("scale,window", [(14, 16384), (16, 16384), (16, 1024), (18, 4096)])
+@pytest.mark.parametrize("scale,window", [(14, 8192), (16, 8192), (16, 1024), (18, 4096), (20, 8192)])
 def test_serial_engine_against_oracle(ctx, scale, window, monkeypatch):
     """Serial-order engine at larger sizes and window settings: bit-exact."""
     monkeypatch.setenv("GBGPU_EXACT_WINDOW", str(window))
@@ -133,6 +133,20 @@ def test_serial_engine_against_oracle(ctx, scale, window, monkeypatch):
     ids, _ = ctx.generate_mapping(rp_t, col_t, SERIAL, ar)
     ids_orc, _ = po.compose(rp, col, m_orc)
     np.testing.assert_array_equal(ids.cpu().numpy(), ids_orc)
+
+
+def test_parallel_recipe_is_serial_order(ctx):
+    """cd_parallel runs the serial-order engine: same membership as cd_serial
+    and as the oracle's serial sweep, on a graph with multi-segment hubs."""
+    rp_t, col_t = gg.rmat(19, 16, seed=77, device="cuda")
+    rp, col = rp_t.cpu().numpy(), col_t.cpu().numpy()
+    assert np.diff(rp).max() > 4 * 4096
+    ar = po.auto_resolution(rp, col)
+    m_par, _ = ctx.run_graphbrew(rp_t, col_t, PARALLEL, ar)
+    m_ser, _ = ctx.run_graphbrew(rp_t, col_t, SERIAL, ar)
+    np.testing.assert_array_equal(m_par.cpu().numpy(), m_ser.cpu().numpy())
+    m_orc, _ = po.leiden(rp, col, ar)
+    np.testing.assert_array_equal(m_par.cpu().numpy().view(np.uint32), m_orc)
 
 
 def test_async_engine_quality(ctx, monkeypatch):
