@@ -69,7 +69,8 @@ class GbgpuStats(C.Structure):
                 ("gorder_communities", C.c_int64), ("gorder_vertices", C.c_int64),
                 ("gorder_max_community", C.c_int64), ("fallback_communities", C.c_int64),
                 ("fallback_vertices", C.c_int64), ("largest_community", C.c_int64),
-                ("bfs_levels", C.c_int64), ("kernel_launches", C.c_int64), ("resolution", C.c_double)]
+                ("bfs_levels", C.c_int64), ("kernel_launches", C.c_int64), ("resolution", C.c_double),
+                ("local_move_rounds", C.c_int64), ("local_move_evaluations", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved0"}
@@ -222,8 +223,7 @@ class Context:
         self._check(library().gbgpu_synchronize(self._h))
 
     # -- argument marshalling ------------------------------------------------
-    @staticmethod
-    def _graph_args(row_ptr, col):
+    def _graph_args(self, row_ptr, col):
         dev = _is_cuda(row_ptr)
         if dev != _is_cuda(col):
             raise ValueError("row_ptr and col must both be host arrays or both CUDA tensors")
@@ -232,10 +232,25 @@ class Context:
             if row_ptr.dtype != torch.int64 or col.dtype != torch.int32:
                 raise ValueError("row_ptr must be int64 and col int32")
             row_ptr, col = row_ptr.contiguous(), col.contiguous()
+            self._follow_torch_stream(row_ptr)
             return row_ptr, col, row_ptr.data_ptr(), col.data_ptr(), row_ptr.numel() - 1, col.numel(), True
         rp = np.ascontiguousarray(_to_numpy(row_ptr), dtype=np.int64)
         cl = np.ascontiguousarray(_to_numpy(col), dtype=np.int32)
         return rp, cl, rp.ctypes.data, cl.ctypes.data if len(cl) else 0, len(rp) - 1, len(cl), False
+
+    def _follow_torch_stream(self, t):
+        """Device-tensor calls run on torch's current stream of the tensor's
+        device, so they are ordered after the kernels that produced the inputs
+        and before whatever consumes the outputs."""
+        import torch
+        st = torch.cuda.current_stream(t.device)
+        if st.cuda_stream == 0:
+            # The legacy default stream has no handle to order against the
+            # context's non-blocking stream: wait for it instead.
+            st.synchronize()
+            self.set_stream(None)
+        else:
+            self.set_stream(st.cuda_stream)
 
     @staticmethod
     def _out(n, dtype, dev, like=None):
@@ -301,6 +316,7 @@ class Context:
         dev = _is_cuda(new_ids)
         if dev:
             ids = new_ids.contiguous()
+            self._follow_torch_stream(ids)
             p, n = ids.data_ptr(), ids.numel()
         else:
             ids = np.ascontiguousarray(_to_numpy(new_ids), dtype=np.int32)

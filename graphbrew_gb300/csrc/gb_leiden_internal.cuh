@@ -80,6 +80,6 @@ struct LocalMoveContext {
 
 // Serial-order local moving (leiden_exact.cu).  Returns the iterations run.
 int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iterations, int64_t window,
-                     cudaStream_t s, int64_t* launches, int64_t* rounds_out);
+                     cudaStream_t s, int64_t* launches, int64_t* rounds_out, int64_t* evals_out);
 
 }  // namespace gb

@@ -634,11 +634,12 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
     lmc.hub_gk = hub_gk.get();
     lmc.hub_gv = hub_gv.get();
     lmc.hub_gcap = hub_gcap;
-    int64_t exact_rounds = 0;
+    int64_t exact_rounds = 0, exact_evals = 0;
 
     auto local_move = [&](double tolerance) -> int {
         if (exact)
-            return local_move_exact(lmc, tolerance, p.max_iterations, p.exact_window, s, &launches, &exact_rounds);
+            return local_move_exact(lmc, tolerance, p.max_iterations, p.exact_window, s, &launches, &exact_rounds,
+                                    &exact_evals);
         int iters = 0;
         for (int it = 0; it < p.max_iterations; ++it) {
             GB_CUDA(cudaMemsetAsync(dacc, 0, sizeof(double), s));
@@ -868,6 +869,8 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
         st->communities = distinct;
         st->resolution = R;
         st->kernel_launches += launches;
+        st->local_move_rounds = exact_rounds;
+        st->local_move_evaluations = exact_evals;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

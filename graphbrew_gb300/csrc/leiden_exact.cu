@@ -31,6 +31,7 @@
 // fixed tree order with a rigorous error bound and re-summed serially in
 // vertex order only when the bound cannot settle the comparison.
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <vector>
 
@@ -47,8 +48,9 @@ constexpr int kWindowMax = 8192;              // window vertices (events <= 2 x 
 constexpr int kEventsMax = 2 * kWindowMax;    // 16384 -> 14-bit event index
 constexpr int kTableSlots = 4 * kWindowMax;   // 32768 hash slots -> 15 bits (+1 for padding)
 constexpr int kEvThreads = 1024;
-constexpr int kHubSeg = 4096;                 // edges per hub-accumulation CTA
-constexpr int kTabSeg = 4096;                 // table slots per hub-selection CTA
+constexpr int kHubThreads2 = 256;             // threads of the hub kernels
+constexpr int kHubSeg = 4 * kHubThreads2;     // edges per hub-accumulation CTA (4 per thread)
+constexpr int kTabSeg = kHubThreads2;         // table slots per hub-selection CTA (1 per thread)
 constexpr unsigned long long kNoChange = ~0ull;
 
 struct Ctl {
@@ -56,7 +58,18 @@ struct Ctl {
     unsigned long long first_change;
     long long es0, es1;       // hub edge-segment range of the window
     long long ts0, ts1;       // hub table-segment range of the window
+    long long ms0, ms1;       // mid-degree list range of the window
     long long round;
+    long long evals;          // window vertices evaluated in this iteration
+    long long max_rounds;     // bound on rounds per iteration (n + 1 always suffices)
+    long long error;          // nonzero: the round loop stopped without finishing
+};
+
+struct __align__(16) SlotMeta {
+    uint32_t key;     // community id (kNone = empty)
+    int32_t start;    // first sorted event of the slot
+    int32_t end;      // one past its last event
+    int32_t pad;
 };
 
 struct HubSeg {
@@ -77,14 +90,9 @@ struct ExactState {
     double* delta[2];
     double* final_delta;
     // event table
-    uint32_t* hkey;       // kTableSlots
-    int32_t* sstart;      // kTableSlots
-    int32_t* send;
-    uint32_t* etime_raw;  // kEventsMax (by event index)
-    long long* eval_raw;
+    SlotMeta* slots;      // kTableSlots: community key and its sorted-event range
     uint32_t* stime;      // sorted
     long long* epre;      // inclusive prefix within slot
-    long long* gscan;     // scratch: inclusive scan over all sorted events
     // hubs
     const uint32_t* hub_v;        // hub vertex ids (ascending)
     const int64_t* hub_toff;      // table offset
@@ -101,8 +109,14 @@ struct ExactState {
     uint32_t* tvals;
     int32_t* hub_any;
     int32_t* hub_done;
+    uint32_t* hub_kud;            // edges of the hub into its own community (accumulated)
+    double* hub_sd;               // sigma of its own community at the hub's time
     double* part_d;               // per table segment
     uint32_t* part_c;
+    const uint32_t* mid_v;        // vertices with 32 < degree <= kWarpMaxDeg (ascending)
+    long long n_mid;
+    cudaGraphConditionalHandle cond;  // while-node condition (graph-driven rounds)
+    int use_cond;
     double M, R;
 };
 
@@ -110,22 +124,21 @@ __device__ __forceinline__ uint32_t slot_hash(uint32_t c) {
     return (uint32_t)(((uint64_t)c * 0x9E3779B97F4A7C15ull) >> 40);
 }
 
-__device__ __forceinline__ int find_slot(const uint32_t* hkey, uint32_t c) {
+// Community total at time u: the committed total plus the speculative
+// events of c before u (one 16-byte probe per hash step, then a binary
+// search over the slot's time-sorted events).
+__device__ __forceinline__ long long sigma_at(const ExactState& a, uint32_t c, uint32_t u) {
+    const long long base = (long long)a.ctot[c];
     uint32_t h = slot_hash(c) & (kTableSlots - 1);
+    SlotMeta sm;
     while (true) {
-        const uint32_t k = hkey[h];
-        if (k == c) return (int)h;
-        if (k == kNone) return -1;
+        sm = a.slots[h];
+        if (sm.key == c) break;
+        if (sm.key == kNone) return base;
         h = (h + 1) & (kTableSlots - 1);
     }
-}
-
-// Community total at time u.
-__device__ __forceinline__ long long sigma_at(const ExactState& a, uint32_t c, uint32_t u) {
-    long long s = (long long)a.ctot[c];
-    const int slot = find_slot(a.hkey, c);
-    if (slot < 0) return s;
-    int lo = a.sstart[slot], hi = a.send[slot];
+    long long s = base;
+    const int lo = sm.start, hi = sm.end;
     int l = lo, r = hi;
     while (l < r) {
         const int mid = (l + r) >> 1;
@@ -171,13 +184,13 @@ __device__ __forceinline__ void record(const ExactState& a, const Round& r, int6
     r.nact[u] = act;
     r.nbest[u] = best;
     r.ndelta[u] = delta;
-    // Only the move itself is visible to later vertices: "inactive" and
-    // "evaluated, stays" are the same decision.
+    // Only the move itself is visible to later vertices: "inactive",
+    // "evaluated, stays" and "not yet evaluated" (kUnknown) are the same
+    // input to them, so only a different move is a change.
     const uint32_t cur = a.vcom[u];
-    const uint8_t pa = r.pact[u];
     const bool moves = act == 1 && best != cur;
-    const bool pmoves = pa == 1 && r.pbest[u] != cur;
-    if (pa == kUnknown || moves != pmoves || (moves && best != r.pbest[u]))
+    const bool pmoves = r.pact[u] == 1 && r.pbest[u] != cur;
+    if (moves != pmoves || (moves && best != r.pbest[u]))
         atomicMin(&a.ctl->first_change, (unsigned long long)u);
 }
 
@@ -190,62 +203,129 @@ __device__ __forceinline__ long long lower_bound_u32(const uint32_t* a, long lon
     return lo;
 }
 
+// First index i in the ascending array a[0, n) with a[i] >= key, searched by
+// one warp: 32 samples per step narrow the range 32-fold (4 steps for 2^20).
+__device__ __forceinline__ long long warp_lower_bound_u32(const uint32_t* a, long long n, uint32_t key,
+                                                         int lane) {
+    long long lo = 0, hi = n;   // a[0, lo) < key; a[hi] >= key or hi == n
+    while (hi - lo > 32) {
+        const long long step = (hi - lo + 31) / 32;
+        const long long p = lo + (long long)lane * step;
+        const bool ge = p < hi ? a[p] >= key : true;
+        const unsigned b = __ballot_sync(0xFFFFFFFFu, ge);   // lanes at or past hi vote true
+        if (b == 0) {   // every sample < key: the bound lies past the last sample
+            lo = lo + 31 * step + 1;
+            continue;
+        }
+        const int f = __ffs(b) - 1;
+        if (f == 0) return lo;
+        const long long pf = lo + (long long)f * step;
+        lo = lo + (long long)(f - 1) * step + 1;
+        hi = min(hi, pf);
+    }
+    const long long p = lo + lane;
+    const bool ge = p < hi ? a[p] >= key : true;
+    const unsigned b = __ballot_sync(0xFFFFFFFFu, ge);
+    return b ? lo + (__ffs(b) - 1) : hi;
+}
+
 // ---------------------------------------------------------------------------
 // Event table (one CTA): hash slots, stable sort by slot, prefix sums.
+// Everything between the window loads and the table stores stays in shared
+// memory: the hash is built there and published, the packed events are
+// radix-sorted there, and the per-slot prefix sums are one segmented scan.
 // ---------------------------------------------------------------------------
+constexpr int kPerThread = kWindowMax / kEvThreads;      // window vertices per thread
+constexpr int kTableSmemWords = kEventsMax + kTableSlots + kWindowMax;
+
+struct SegSum {
+    long long v;
+    int head;   // a segment starts inside this range
+};
+
+__device__ __forceinline__ SegSum seg_combine(SegSum a, SegSum b) {
+    return SegSum{b.head ? b.v : a.v + b.v, a.head | b.head};
+}
+
 __global__ void __launch_bounds__(kEvThreads) k_ex_table(ExactState a) {
     extern __shared__ uint32_t sm[];
-    uint32_t* bufA = sm;                               // kEventsMax
-    uint32_t* bufB = sm + kEventsMax;                  // kEventsMax
-    int32_t* wcnt = reinterpret_cast<int32_t*>(sm + 2 * kEventsMax);  // 32 x 257
+    uint32_t* bufA = sm;                               // kEventsMax packed events
+    uint32_t* shash = sm + kEventsMax;                 // kTableSlots while inserting
+    uint32_t* bufB = sm + kEventsMax;                  // kEventsMax, after insertion
+    int32_t* wcnt = reinterpret_cast<int32_t*>(sm + 2 * kEventsMax);  // 32 x 257, after insertion
+    int32_t* wdeg = reinterpret_cast<int32_t*>(sm + kEventsMax + kTableSlots);  // mover degree or 0
     __shared__ int32_t digit_off[256];
-    __shared__ long long warp_tot[32];
+    __shared__ long long warp_v[32];
+    __shared__ int warp_h[32];
     const long long P = a.ctl->P, E = a.ctl->E;
     if (P >= a.ctl->n) return;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int W = (int)(E - P);
     const int m = 2 * W;
     const Round r = round_view(a);
-    for (int i = tid; i < kTableSlots; i += blockDim.x) a.hkey[i] = kNone;
-    if (tid == 0) {
-        a.ctl->first_change = kNoChange;
-        a.ctl->es0 = lower_bound_u32(a.eseg_v, a.n_eseg, (uint32_t)P);
-        a.ctl->es1 = lower_bound_u32(a.eseg_v, a.n_eseg, (uint32_t)E);
-        a.ctl->ts0 = lower_bound_u32(a.tseg_v, a.n_tseg, (uint32_t)P);
-        a.ctl->ts1 = lower_bound_u32(a.tseg_v, a.n_tseg, (uint32_t)E);
+    for (int i = tid; i < kTableSlots; i += blockDim.x) shash[i] = kNone;
+    if (tid == 0) a.ctl->first_change = kNoChange;
+    // Window ranges of the hub segment lists and the mid-degree list: six
+    // searches on six warps.
+    if (w < 6) {
+        const uint32_t* arr = w < 2 ? a.eseg_v : (w < 4 ? a.tseg_v : a.mid_v);
+        const long long len = w < 2 ? a.n_eseg : (w < 4 ? a.n_tseg : a.n_mid);
+        const long long pos = warp_lower_bound_u32(arr, len, (uint32_t)((w & 1) ? E : P), lane);
+        if (lane == 0) {
+            long long* dst[6] = {&a.ctl->es0, &a.ctl->es1, &a.ctl->ts0, &a.ctl->ts1, &a.ctl->ms0, &a.ctl->ms1};
+            *dst[w] = pos;
+        }
+    }
+    // Window state: all loads of a thread issued before any use.
+    uint8_t pa[kPerThread];
+    uint32_t pb[kPerThread], vc[kPerThread];
+    int64_t r0[kPerThread], r1[kPerThread];
+#pragma unroll
+    for (int k = 0; k < kPerThread; ++k) {
+        const int i = tid + k * kEvThreads;
+        if (i < W) {
+            const int64_t wv = P + i;
+            pa[k] = r.pact[wv];
+            pb[k] = r.pbest[wv];
+            vc[k] = a.vcom[wv];
+            r0[k] = a.rp[wv];
+            r1[k] = a.rp[wv + 1];
+        }
     }
     __syncthreads();
-    // Events of D_prev movers, packed as (slot << 14 | event index).
+    // Events of D_prev movers, packed as (slot << 14 | event index); the
+    // event index is 2 x window offset (+1 for the arrival), so it is time order.
     constexpr uint32_t kPad = (uint32_t)kTableSlots << 14;
-    for (int i = tid; i < W; i += blockDim.x) {
-        const int64_t wv = P + i;
+#pragma unroll
+    for (int k = 0; k < kPerThread; ++k) {
+        const int i = tid + k * kEvThreads;
+        if (i >= W) continue;
         uint32_t p0 = kPad | (uint32_t)(2 * i), p1 = kPad | (uint32_t)(2 * i + 1);
-        if (r.pact[wv] == 1 && r.pbest[wv] != a.vcom[wv]) {
-            const long long deg = (long long)(a.rp[wv + 1] - a.rp[wv]);
-            const uint32_t cs[2] = {a.vcom[wv], r.pbest[wv]};
-            uint32_t ks[2];
-            for (int j = 0; j < 2; ++j) {
-                uint32_t h = slot_hash(cs[j]) & (kTableSlots - 1);
-                while (true) {
-                    const uint32_t prev = atomicCAS(&a.hkey[h], kNone, cs[j]);
-                    if (prev == kNone || prev == cs[j]) break;
-                    h = (h + 1) & (kTableSlots - 1);
-                }
-                ks[j] = h;
+        int dg = 0;
+        if (pa[k] == 1 && pb[k] != vc[k]) {
+            dg = (int)(r1[k] - r0[k]);
+            uint32_t h0 = slot_hash(vc[k]) & (kTableSlots - 1);
+            while (true) {
+                const uint32_t prev = atomicCAS(&shash[h0], kNone, vc[k]);
+                if (prev == kNone || prev == vc[k]) break;
+                h0 = (h0 + 1) & (kTableSlots - 1);
             }
-            p0 = (ks[0] << 14) | (uint32_t)(2 * i);
-            p1 = (ks[1] << 14) | (uint32_t)(2 * i + 1);
-            a.eval_raw[2 * i] = -deg;
-            a.eval_raw[2 * i + 1] = deg;
-        } else {
-            a.eval_raw[2 * i] = 0;
-            a.eval_raw[2 * i + 1] = 0;
+            uint32_t h1 = slot_hash(pb[k]) & (kTableSlots - 1);
+            while (true) {
+                const uint32_t prev = atomicCAS(&shash[h1], kNone, pb[k]);
+                if (prev == kNone || prev == pb[k]) break;
+                h1 = (h1 + 1) & (kTableSlots - 1);
+            }
+            p0 = (h0 << 14) | (uint32_t)(2 * i);
+            p1 = (h1 << 14) | (uint32_t)(2 * i + 1);
         }
-        a.etime_raw[2 * i] = (uint32_t)wv;
-        a.etime_raw[2 * i + 1] = (uint32_t)wv;
+        wdeg[i] = dg;
         bufA[2 * i] = p0;
         bufA[2 * i + 1] = p1;
     }
+    __syncthreads();
+    // Publish the slot keys for lookups; the shared hash area becomes bufB.
+    for (int i = tid; i < kTableSlots; i += blockDim.x) a.slots[i].key = shash[i];
     __syncthreads();
     // Stable LSD radix sort on the slot bits (14..29): two 8-bit passes.
     // Warp w owns a contiguous chunk; inside it 32-element steps keep order.
@@ -275,13 +355,19 @@ __global__ void __launch_bounds__(kEvThreads) k_ex_table(ExactState a) {
             digit_off[tid] = acc;  // digit total for now
         }
         __syncthreads();
-        if (tid == 0) {
-            int acc = 0;
-            for (int d = 0; d < 256; ++d) {
-                const int t = digit_off[d];
-                digit_off[d] = acc;
-                acc += t;
+        if (w == 0) {
+            // exclusive scan of the 256 digit totals, 8 per lane
+            int v[8], t = 0;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) { v[k] = digit_off[lane * 8 + k]; t += v[k]; }
+            int incl = t;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                if (lane >= o) incl += y;
             }
+            int run = incl - t;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) { digit_off[lane * 8 + k] = run; run += v[k]; }
         }
         __syncthreads();
         for (int base = c0; base < c1; base += 32) {
@@ -301,136 +387,202 @@ __global__ void __launch_bounds__(kEvThreads) k_ex_table(ExactState a) {
         src = dst;
         dst = t;
     }
-    // src holds the sorted events.  Times, deltas and slot bounds.
-    for (int i = tid; i < m; i += blockDim.x) {
-        const uint32_t pk = src[i];
-        const uint32_t s = pk >> 14, e = pk & 0x3FFF;
-        a.stime[i] = a.etime_raw[e];
-        if (s < (uint32_t)kTableSlots) {
-            if (i == 0 || (src[i - 1] >> 14) != s) a.sstart[s] = i;
-            if (i == m - 1 || (src[i + 1] >> 14) != s) a.send[s] = i + 1;
-        }
-    }
-    // Inclusive scan of the deltas in sorted order (global G in epre), then
-    // per-slot prefix = G[i] - G[start] + val[start].
+    // src holds the sorted events.  Per-slot inclusive prefix sums of the
+    // signed degrees: a segmented scan, each thread over a contiguous range.
     const int per = (m + blockDim.x - 1) / blockDim.x;
-    const int b0 = tid * per, b1 = min(m, b0 + per);
-    long long run = 0;
-    for (int i = b0; i < b1; ++i) run += a.eval_raw[src[i] & 0x3FFF];
-    long long incl = run;
-    for (int o = 1; o < 32; o <<= 1) {
-        const long long t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-        if (lane >= o) incl += t;
+    const int b0 = min(m, tid * per), b1 = min(m, b0 + per);
+    SegSum own{0, 0};
+    for (int i = b0; i < b1; ++i) {
+        const uint32_t pk = src[i];
+        const uint32_t sl = pk >> 14, e = pk & 0x3FFF;
+        const int head = (i == 0 || (src[i - 1] >> 14) != sl);
+        const long long v = sl < (uint32_t)kTableSlots ? ((e & 1) ? wdeg[e >> 1] : -(long long)wdeg[e >> 1]) : 0;
+        own = seg_combine(own, SegSum{v, head});
     }
-    if (lane == 31) warp_tot[w] = incl;
+    // exclusive scan of the thread aggregates (warp shuffles, then warps)
+    SegSum inc = own;
+    for (int o = 1; o < 32; o <<= 1) {
+        SegSum y{__shfl_up_sync(0xFFFFFFFFu, inc.v, o), __shfl_up_sync(0xFFFFFFFFu, inc.head, o)};
+        if (lane >= o) inc = seg_combine(y, inc);
+    }
+    if (lane == 31) { warp_v[w] = inc.v; warp_h[w] = inc.head; }
     __syncthreads();
     if (w == 0) {
-        long long v = warp_tot[lane];
-        long long vi = v;
+        SegSum x{warp_v[lane], warp_h[lane]};
+        SegSum xi = x;
         for (int o = 1; o < 32; o <<= 1) {
-            const long long t = __shfl_up_sync(0xFFFFFFFFu, vi, o);
-            if (lane >= o) vi += t;
+            SegSum y{__shfl_up_sync(0xFFFFFFFFu, xi.v, o), __shfl_up_sync(0xFFFFFFFFu, xi.head, o)};
+            if (lane >= o) xi = seg_combine(y, xi);
         }
-        warp_tot[lane] = vi - v;
+        // exclusive value for warp `lane`
+        SegSum ex{__shfl_up_sync(0xFFFFFFFFu, xi.v, 1), __shfl_up_sync(0xFFFFFFFFu, xi.head, 1)};
+        if (lane == 0) ex = SegSum{0, 0};
+        warp_v[lane] = ex.v;
+        warp_h[lane] = ex.head;
     }
     __syncthreads();
-    long long acc = warp_tot[w] + incl - run;
+    SegSum ex_thread{__shfl_up_sync(0xFFFFFFFFu, inc.v, 1), __shfl_up_sync(0xFFFFFFFFu, inc.head, 1)};
+    if (lane == 0) ex_thread = SegSum{0, 0};
+    const SegSum carry = seg_combine(SegSum{warp_v[w], warp_h[w]}, ex_thread);
+    long long run = carry.v;
     for (int i = b0; i < b1; ++i) {
-        acc += a.eval_raw[src[i] & 0x3FFF];
-        a.gscan[i] = acc;
-    }
-    __syncthreads();
-    for (int i = tid; i < m; i += blockDim.x) {
-        const uint32_t s = src[i] >> 14;
-        if (s >= (uint32_t)kTableSlots) continue;
-        const int st = a.sstart[s];
-        a.epre[i] = a.gscan[i] - (a.gscan[st] - a.eval_raw[src[st] & 0x3FFF]);
+        const uint32_t pk = src[i];
+        const uint32_t sl = pk >> 14, e = pk & 0x3FFF;
+        a.stime[i] = (uint32_t)(P + (e >> 1));
+        if (sl >= (uint32_t)kTableSlots) continue;
+        const long long v = (e & 1) ? wdeg[e >> 1] : -(long long)wdeg[e >> 1];
+        const bool head = (i == 0 || (src[i - 1] >> 14) != sl);
+        run = head ? v : run + v;
+        a.epre[i] = run;
+        if (head) a.slots[sl].start = i;
+        if (i == m - 1 || (src[i + 1] >> 14) != sl) a.slots[sl].end = i + 1;
     }
 }
 
-constexpr int kExWarpsPerBlock = 4;
+constexpr int kMidWarpsPerBlock = 4;
+constexpr int kSmallWarpsPerBlock = 8;
+constexpr int kSmallMaxDeg = 32;
 
-// Warp per window vertex (degree <= kWarpMaxDeg).
-__global__ void __launch_bounds__(kExWarpsPerBlock * 32) k_ex_eval_warp(ExactState a) {
-    extern __shared__ uint32_t ex_smem[];
+// One window vertex by one warp.  Small rows (deg <= 32) hold one neighbour
+// per lane and rank communities with __match_any_sync; mid rows
+// (32 < deg <= kWarpMaxDeg) accumulate into the warp's shared-memory table.
+template <bool kMid>
+__device__ __forceinline__ void eval_vertex(const ExactState& a, const Round& r, int64_t u, int lane, uint32_t* tk,
+                                            uint32_t* tv) {
+    const int64_t rb = a.rp[u];
+    const int deg = (int)(a.rp[u + 1] - rb);
+    bool act = a.vaff[u] != 0;
+    if (!act) {
+        bool any = false;
+        for (int i = lane; i < deg && !any; i += 32) {
+            const int32_t v = a.col[rb + i];
+            any = (v >= r.P && v < u && prev_mover(a, r, v));
+        }
+        act = __any_sync(0xFFFFFFFFu, any);
+    }
+    const uint32_t d = a.vcom[u];
+    if (!act) {
+        if (lane == 0) record(a, r, u, 0, d, 0.0);
+        return;
+    }
+    const double ku = (double)deg;
+    double best_d = 0.0;
+    uint32_t best_c = kNone;
+    if (!kMid) {
+        uint32_t c = kNone;
+        if (lane < deg) {
+            const int32_t v = a.col[rb + lane];
+            if (v != (int32_t)u) c = comm_at(a, r, v, u);
+        }
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, c);
+        const double kud = (double)__popc(__ballot_sync(0xFFFFFFFFu, c == d));
+        if (c != kNone && c != d && lane == __ffs(peers) - 1) {
+            const double sd = (double)sigma_at(a, d, (uint32_t)u);
+            const double sc = (double)sigma_at(a, c, (uint32_t)u);
+            const double dl = delta_q((double)__popc(peers), kud, ku, sc, sd, a.M, a.R);
+            if (dl > 0.0) { best_d = dl; best_c = c; }
+        }
+    } else {
+        uint32_t H = 64;
+        while (H < 2u * (uint32_t)deg) H <<= 1;
+        const uint32_t mask = H - 1;
+        for (uint32_t i = lane; i < H; i += 32) { tk[i] = kNone; tv[i] = 0; }
+        __syncwarp();
+        // Neighbour communities, four 32-edge batches in flight per step.
+        for (int base = 0; base < deg; base += 128) {
+            uint32_t c[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int e = base + 32 * k + lane;
+                c[k] = kNone;
+                if (e < deg) {
+                    const int32_t v = a.col[rb + e];
+                    if (v != (int32_t)u) c[k] = comm_at(a, r, v, u);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const unsigned peers = __match_any_sync(0xFFFFFFFFu, c[k]);
+                if (c[k] != kNone && lane == __ffs(peers) - 1)
+                    table_add(tk, tv, mask, c[k], (uint32_t)__popc(peers));
+            }
+        }
+        __syncwarp();
+        const double kud = (double)table_get(tk, tv, mask, d);
+        // Compact the candidate communities (c != d) to the front of the
+        // table, so the selection runs ceil(candidates / 32) lookup rounds.
+        uint32_t cnt = 0;
+        for (uint32_t i0 = 0; i0 < H; i0 += 32) {
+            const uint32_t c = tk[i0 + lane], v = tv[i0 + lane];
+            const bool occ = c != kNone && c != d;
+            const unsigned bal = __ballot_sync(0xFFFFFFFFu, occ);
+            __syncwarp();
+            if (occ) {
+                const uint32_t pos = cnt + __popc(bal & ((1u << lane) - 1u));
+                tk[pos] = c;
+                tv[pos] = v;
+            }
+            cnt += __popc(bal);
+            __syncwarp();
+        }
+        const double sd = (double)sigma_at(a, d, (uint32_t)u);
+        for (uint32_t i = lane; i < cnt; i += 32) {
+            const uint32_t c = tk[i];
+            const double sc = (double)sigma_at(a, c, (uint32_t)u);
+            const double dl = delta_q((double)tv[i], kud, ku, sc, sd, a.M, a.R);
+            if (dl > 0.0 && better(dl, c, best_d, best_c)) { best_d = dl; best_c = c; }
+        }
+        __syncwarp();
+    }
+    warp_argmax(best_d, best_c);
+    if (lane == 0) {
+        if (best_d > 0.0 && best_c != kNone && best_c != d) record(a, r, u, 1, best_c, best_d);
+        else record(a, r, u, 1, d, 0.0);
+    }
+}
+
+// Small rows: one warp per window vertex, no shared memory (full occupancy).
+__global__ void __launch_bounds__(kSmallWarpsPerBlock * 32) k_ex_eval_small(ExactState a) {
     if (a.ctl->P >= a.ctl->n) return;
     const Round r = round_view(a);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    uint32_t* tk = ex_smem + (size_t)w * 2 * kWarpHash;
-    uint32_t* tv = tk + kWarpHash;
-    const int64_t nw = (int64_t)gridDim.x * kExWarpsPerBlock;
-    for (int64_t u = r.P + (int64_t)blockIdx.x * kExWarpsPerBlock + w; u < r.E; u += nw) {
-        const int64_t rb = a.rp[u];
-        const int deg = (int)(a.rp[u + 1] - rb);
-        if (deg > kWarpMaxDeg) continue;
-        bool act = a.vaff[u] != 0;
-        if (!act) {
-            bool any = false;
-            for (int i = lane; i < deg && !any; i += 32) {
-                const int32_t v = a.col[rb + i];
-                any = (v >= r.P && v < u && prev_mover(a, r, v));
-            }
-            act = __any_sync(0xFFFFFFFFu, any);
-        }
-        const uint32_t d = a.vcom[u];
-        if (!act) {
-            if (lane == 0) record(a, r, u, 0, d, 0.0);
-            continue;
-        }
-        const double ku = (double)deg;
-        double best_d = 0.0;
-        uint32_t best_c = kNone;
-        if (deg <= 32) {
-            uint32_t c = kNone;
-            if (lane < deg) {
-                const int32_t v = a.col[rb + lane];
-                if (v != (int32_t)u) c = comm_at(a, r, v, u);
-            }
-            const unsigned peers = __match_any_sync(0xFFFFFFFFu, c);
-            const double kud = (double)__popc(__ballot_sync(0xFFFFFFFFu, c == d));
-            if (c != kNone && c != d && lane == __ffs(peers) - 1) {
-                const double sd = (double)sigma_at(a, d, (uint32_t)u);
-                const double sc = (double)sigma_at(a, c, (uint32_t)u);
-                const double dl = delta_q((double)__popc(peers), kud, ku, sc, sd, a.M, a.R);
-                if (dl > 0.0) { best_d = dl; best_c = c; }
-            }
-        } else {
-            uint32_t H = 64;
-            while (H < 2u * (uint32_t)deg) H <<= 1;
-            const uint32_t mask = H - 1;
-            for (uint32_t i = lane; i < H; i += 32) { tk[i] = kNone; tv[i] = 0; }
-            __syncwarp();
-            for (int base = 0; base < deg; base += 32) {
-                uint32_t c = kNone;
-                if (base + lane < deg) {
-                    const int32_t v = a.col[rb + base + lane];
-                    if (v != (int32_t)u) c = comm_at(a, r, v, u);
-                }
-                const unsigned peers = __match_any_sync(0xFFFFFFFFu, c);
-                if (c != kNone && lane == __ffs(peers) - 1) table_add(tk, tv, mask, c, (uint32_t)__popc(peers));
-            }
-            __syncwarp();
-            const double kud = (double)table_get(tk, tv, mask, d);
-            const double sd = (double)sigma_at(a, d, (uint32_t)u);
-            for (uint32_t i = lane; i < H; i += 32) {
-                const uint32_t c = tk[i];
-                if (c == kNone || c == d) continue;
-                const double sc = (double)sigma_at(a, c, (uint32_t)u);
-                const double dl = delta_q((double)tv[i], kud, ku, sc, sd, a.M, a.R);
-                if (dl > 0.0 && better(dl, c, best_d, best_c)) { best_d = dl; best_c = c; }
-            }
-            __syncwarp();
-        }
-        warp_argmax(best_d, best_c);
-        if (lane == 0) {
-            if (best_d > 0.0 && best_c != kNone && best_c != d) record(a, r, u, 1, best_c, best_d);
-            else record(a, r, u, 1, d, 0.0);
-        }
+    const int64_t nw = (int64_t)gridDim.x * kSmallWarpsPerBlock;
+    for (int64_t u = r.P + (int64_t)blockIdx.x * kSmallWarpsPerBlock + w; u < r.E; u += nw) {
+        if (a.rp[u + 1] - a.rp[u] > kSmallMaxDeg) continue;
+        eval_vertex<false>(a, r, u, lane, nullptr, nullptr);
     }
 }
 
-// Hub accumulation: one CTA per 4096-edge segment of a window hub.
-__global__ void __launch_bounds__(256) k_ex_hub_accum(ExactState a) {
+// Mid rows of the window (from the ascending list of mid-degree vertices).
+__global__ void __launch_bounds__(kMidWarpsPerBlock * 32) k_ex_eval_mid(ExactState a) {
+    extern __shared__ uint32_t ex_smem[];
+    if (a.ctl->P >= a.ctl->n) return;
+    const Round r = round_view(a);
+    const long long m0 = a.ctl->ms0, m1 = a.ctl->ms1;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t* tk = ex_smem + (size_t)w * 2 * kWarpHash;
+    uint32_t* tv = tk + kWarpHash;
+    const long long nw = (long long)gridDim.x * kMidWarpsPerBlock;
+    for (long long i = m0 + (long long)blockIdx.x * kMidWarpsPerBlock + w; i < m1; i += nw)
+        eval_vertex<true>(a, r, a.mid_v[i], lane, tk, tv);
+}
+
+__global__ void k_mid_flags(const int64_t* __restrict__ rp, int64_t n, int32_t* __restrict__ flag) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t d = rp[v + 1] - rp[v];
+        flag[v] = d > kSmallMaxDeg && d <= kWarpMaxDeg;
+    }
+}
+
+__global__ void k_mid_scatter(const int32_t* __restrict__ flag, const int64_t* __restrict__ pos, int64_t n,
+                              uint32_t* __restrict__ out) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
+        if (flag[v]) out[pos[v]] = (uint32_t)v;
+}
+
+// Hub accumulation: one CTA per kHubSeg-edge segment of a window hub, four
+// edges per thread in flight.
+__global__ void __launch_bounds__(kHubThreads2) k_ex_hub_accum(ExactState a) {
     if (a.ctl->P >= a.ctl->n) return;
     const Round r = round_view(a);
     const long long q0 = a.ctl->es0, q1 = a.ctl->es1;
@@ -444,20 +596,30 @@ __global__ void __launch_bounds__(256) k_ex_hub_accum(ExactState a) {
         uint32_t* tk = a.tkeys + a.hub_toff[sg.hub];
         uint32_t* tv = a.tvals + a.hub_toff[sg.hub];
         const uint32_t mask = a.hub_tcap[sg.hub] - 1;
+        const uint32_t d = a.vcom[h];
         if (threadIdx.x == 0) s_any = 0;
+        if (threadIdx.x == 0 && sg.part == 0) a.hub_sd[sg.hub] = (double)sigma_at(a, d, h);
         __syncthreads();
         bool any = false;
-        for (int64_t b = e0; b < e1; b += blockDim.x) {
-            uint32_t c = kNone;
-            const int64_t e = b + threadIdx.x;
+        uint32_t c[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int64_t e = e0 + k * kHubThreads2 + threadIdx.x;
+            c[k] = kNone;
             if (e < e1) {
                 const int32_t v = a.col[e];
                 any = any || (v >= r.P && v < (int64_t)h && prev_mover(a, r, v));
-                if (v != (int32_t)h) c = comm_at(a, r, v, h);
+                if (v != (int32_t)h) c[k] = comm_at(a, r, v, h);
             }
-            const unsigned peers = __match_any_sync(0xFFFFFFFFu, c);
-            if (c != kNone && lane == __ffs(peers) - 1) table_add(tk, tv, mask, c, (uint32_t)__popc(peers));
         }
+        uint32_t own = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const unsigned peers = __match_any_sync(0xFFFFFFFFu, c[k]);
+            if (c[k] != kNone && lane == __ffs(peers) - 1) table_add(tk, tv, mask, c[k], (uint32_t)__popc(peers));
+            own += __popc(__ballot_sync(0xFFFFFFFFu, c[k] == d));
+        }
+        if (lane == 0 && own) atomicAdd(&a.hub_kud[sg.hub], own);
         if (any) s_any = 1;
         __syncthreads();
         if (threadIdx.x == 0 && s_any) atomicOr(&a.hub_any[sg.hub], 1);
@@ -465,9 +627,10 @@ __global__ void __launch_bounds__(256) k_ex_hub_accum(ExactState a) {
     }
 }
 
-// Hub selection: one CTA per 4096-slot segment of a window hub's table; the
-// last CTA of a hub reduces the partial maxima and records the decision.
-__global__ void __launch_bounds__(256) k_ex_hub_select(ExactState a) {
+// Hub selection: one CTA per kTabSeg-slot segment of a window hub's table,
+// one slot per thread; the last CTA of a hub reduces the partial maxima and
+// records the decision.
+__global__ void __launch_bounds__(kHubThreads2) k_ex_hub_select(ExactState a) {
     if (a.ctl->P >= a.ctl->n) return;
     const Round r = round_view(a);
     const long long q0 = a.ctl->ts0, q1 = a.ctl->ts1;
@@ -484,8 +647,8 @@ __global__ void __launch_bounds__(256) k_ex_hub_select(ExactState a) {
         const uint32_t cap = a.hub_tcap[j];
         const uint32_t d = a.vcom[h];
         const double ku = (double)(a.rp[h + 1] - a.rp[h]);
-        const double kud = (double)table_get(tk, tv, cap - 1, d);
-        const double sd = (double)sigma_at(a, d, h);
+        const double kud = (double)a.hub_kud[j];
+        const double sd = a.hub_sd[j];
         double best_d = 0.0;
         uint32_t best_c = kNone;
         const uint32_t s0 = (uint32_t)sg.part * kTabSeg, s1 = min(cap, s0 + kTabSeg);
@@ -510,28 +673,40 @@ __global__ void __launch_bounds__(256) k_ex_hub_select(ExactState a) {
             s_last = atomicAdd(&a.hub_done[j], 1) == a.hub_tcount[j] - 1;
         }
         __syncthreads();
-        if (s_last && threadIdx.x == 0) {
+        if (s_last) {
+            // The whole CTA reduces the hub's partial maxima.
             __threadfence();
             double bd = 0.0;
             uint32_t bc = kNone;
-            const int f = a.hub_tfirst[j];
-            for (int k = 0; k < a.hub_tcount[j]; ++k) {
+            const int f = a.hub_tfirst[j], nt = a.hub_tcount[j];
+            for (int k = threadIdx.x; k < nt; k += blockDim.x) {
                 const double pd = ((volatile double*)a.part_d)[f + k];
                 const uint32_t pc = ((volatile uint32_t*)a.part_c)[f + k];
                 if (better(pd, pc, bd, bc)) { bd = pd; bc = pc; }
             }
-            const bool act = a.vaff[h] != 0 || ((volatile int32_t*)a.hub_any)[j] != 0;
-            if (!act) record(a, r, h, 0, d, 0.0);
-            else if (bd > 0.0 && bc != kNone && bc != d) record(a, r, h, 1, bc, bd);
-            else record(a, r, h, 1, d, 0.0);
-            a.hub_done[j] = 0;
-            a.hub_any[j] = 0;
+            warp_argmax(bd, bc);
+            __syncthreads();
+            if (lane == 0) { red_d[w] = bd; red_c[w] = bc; }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                bd = red_d[0];
+                bc = red_c[0];
+                for (int k = 1; k < (int)(blockDim.x / 32); ++k)
+                    if (better(red_d[k], red_c[k], bd, bc)) { bd = red_d[k]; bc = red_c[k]; }
+                const bool act = a.vaff[h] != 0 || ((volatile int32_t*)a.hub_any)[j] != 0;
+                if (!act) record(a, r, h, 0, d, 0.0);
+                else if (bd > 0.0 && bc != kNone && bc != d) record(a, r, h, 1, bc, bd);
+                else record(a, r, h, 1, d, 0.0);
+                a.hub_done[j] = 0;
+                a.hub_any[j] = 0;
+                a.hub_kud[j] = 0;
+            }
         }
         __syncthreads();
     }
 }
 
-__global__ void __launch_bounds__(256) k_ex_hub_clear(ExactState a) {
+__global__ void __launch_bounds__(kHubThreads2) k_ex_hub_clear(ExactState a) {
     if (a.ctl->P >= a.ctl->n) return;
     const long long q0 = a.ctl->ts0, q1 = a.ctl->ts1;
     for (long long q = q0 + blockIdx.x; q < q1; q += gridDim.x) {
@@ -592,15 +767,15 @@ __global__ void k_ex_commit_b(ExactState a) {
     }
 }
 
-__global__ void __launch_bounds__(256) k_ex_commit_hub(ExactState a) {
+__global__ void __launch_bounds__(kHubThreads2) k_ex_commit_hub(ExactState a) {
     if (a.ctl->P >= a.ctl->n) return;
     const Round r = round_view(a);
     const long long x = commit_end(a);
-    const long long q0 = a.ctl->es0;
-    const long long q1 = lower_bound_u32(a.eseg_v, a.n_eseg, (uint32_t)(x + 1));
+    const long long q0 = a.ctl->es0, q1 = a.ctl->es1;
     for (long long q = q0 + blockIdx.x; q < q1; q += gridDim.x) {
         const HubSeg sg = a.eseg[q];
         const uint32_t h = a.hub_v[sg.hub];
+        if ((long long)h > x) continue;   // segments are in hub order: block-uniform skip
         if (!(r.nact[h] == 1 && r.nbest[h] != a.vcom[h])) continue;
         const int64_t rb = a.rp[h], re = a.rp[h + 1];
         const int64_t e0 = rb + (int64_t)sg.part * kHubSeg, e1 = min(re, e0 + kHubSeg);
@@ -623,7 +798,10 @@ __global__ void k_ex_commit_c(ExactState a) {
 // Slide the window: the new decisions become D_prev; entering vertices are unknown.
 __global__ void __launch_bounds__(1024) k_ex_advance(ExactState a) {
     const long long P = a.ctl->P, E = a.ctl->E, n = a.ctl->n, B = a.ctl->B;
-    if (P >= n) return;
+    if (P >= n) {
+        if (threadIdx.x == 0 && a.use_cond) cudaGraphSetConditional(a.cond, 0u);
+        return;
+    }
     const long long x = commit_end(a);
     const long long nP = x + 1, nE = min(n, nP + B);
     const int par = (int)(a.ctl->round & 1);
@@ -631,9 +809,20 @@ __global__ void __launch_bounds__(1024) k_ex_advance(ExactState a) {
     for (long long u = E + threadIdx.x; u < nE; u += blockDim.x) next_prev_act[u] = kUnknown;
     __syncthreads();
     if (threadIdx.x == 0) {
+        const long long rnd = a.ctl->round + 1;
+        a.ctl->evals = a.ctl->evals + (E - P);
         a.ctl->P = nP;
         a.ctl->E = nE;
-        a.ctl->round = a.ctl->round + 1;
+        a.ctl->round = rnd;
+        // Every round commits at least vertex P, so the loop ends within n
+        // rounds; the bound only guards against a broken invariant.
+        bool more = nP < n;
+        if (nP <= P || (more && rnd >= a.ctl->max_rounds)) {
+            a.ctl->error = 1;
+            a.ctl->P = n;
+            more = false;
+        }
+        if (a.use_cond) cudaGraphSetConditional(a.cond, more ? 1u : 0u);
     }
 }
 
@@ -646,6 +835,7 @@ __global__ void __launch_bounds__(1024) k_ex_init_iter(ExactState a) {
         a.ctl->P = 0;
         a.ctl->E = E;
         a.ctl->round = 0;
+        a.ctl->evals = 0;
     }
 }
 
@@ -711,7 +901,7 @@ DevBuf<T> upload(const std::vector<T>& v, cudaStream_t s) {
 }  // namespace
 
 int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iterations, int64_t window,
-                     cudaStream_t s, int64_t* launches, int64_t* rounds_out) {
+                     cudaStream_t s, int64_t* launches, int64_t* rounds_out, int64_t* evals_out) {
     const int64_t n = ctx.g.n;
     const int64_t B = std::max<int64_t>(32, std::min<int64_t>(std::min<int64_t>(window, kWindowMax), n));
 
@@ -761,22 +951,43 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     DevBuf<int32_t> hub_any(nh > 0 ? nh : 1, s), hub_done(nh > 0 ? nh : 1, s);
     GB_CUDA(cudaMemsetAsync(hub_any, 0, (nh > 0 ? nh : 1) * sizeof(int32_t), s));
     GB_CUDA(cudaMemsetAsync(hub_done, 0, (nh > 0 ? nh : 1) * sizeof(int32_t), s));
+    DevBuf<uint32_t> hub_kud(nh > 0 ? nh : 1, s);
+    DevBuf<double> hub_sd(nh > 0 ? nh : 1, s);
+    GB_CUDA(cudaMemsetAsync(hub_kud, 0, (nh > 0 ? nh : 1) * sizeof(uint32_t), s));
     DevBuf<double> part_d(tseg.empty() ? 1 : tseg.size(), s);
     DevBuf<uint32_t> part_c(tseg.empty() ? 1 : tseg.size(), s);
+
+    // ---- mid-degree list (ascending vertex ids) ----
+    int64_t n_mid = 0;
+    DevBuf<uint32_t> mid_v;
+    {
+        DevBuf<int32_t> flag(n, s);
+        DevBuf<int64_t> pos(n, s), tot(1, s);
+        k_mid_flags<<<grid_for(n, kT), kT, 0, s>>>(ctx.g.row_ptr, n, flag);
+        GB_LAUNCH_CHECK();
+        exclusive_scan_i32_to_i64(flag, pos, n, tot, s);
+        n_mid = read_dev(tot.get(), s);
+        mid_v.alloc(n_mid > 0 ? n_mid : 1, s);
+        if (n_mid) {
+            k_mid_scatter<<<grid_for(n, kT), kT, 0, s>>>(flag, pos, n, mid_v);
+            GB_LAUNCH_CHECK();
+        }
+    }
 
     // ---- round state ----
     DevBuf<uint32_t> best0(n, s), best1(n, s);
     DevBuf<uint8_t> act0(n, s), act1(n, s);
     DevBuf<double> delta0(n, s), delta1(n, s), final_delta(n, s);
-    DevBuf<uint32_t> hkey(kTableSlots, s), etime_raw(kEventsMax, s), stime(kEventsMax, s);
-    DevBuf<int32_t> sstart(kTableSlots, s), send(kTableSlots, s);
-    DevBuf<long long> eval_raw(kEventsMax, s), epre(kEventsMax, s), gscan(kEventsMax, s);
+    DevBuf<SlotMeta> slots(kTableSlots, s);
+    DevBuf<uint32_t> stime(kEventsMax, s);
+    DevBuf<long long> epre(kEventsMax, s);
     DevBuf<Ctl> ctl(1, s);
     Ctl* hctl = nullptr;
     GB_CUDA(cudaMallocHost(&hctl, sizeof(Ctl)));
     *hctl = Ctl{};
     hctl->n = n;
     hctl->B = B;
+    hctl->max_rounds = n + 2;
     GB_CUDA(cudaMemcpyAsync(ctl.get(), hctl, sizeof(Ctl), cudaMemcpyHostToDevice, s));
     DevBuf<double> partial(1024, s), dsum(1, s);
     DevBuf<unsigned long long> nmov(1, s);
@@ -795,14 +1006,9 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     a.delta[0] = delta0.get();
     a.delta[1] = delta1.get();
     a.final_delta = final_delta.get();
-    a.hkey = hkey.get();
-    a.sstart = sstart.get();
-    a.send = send.get();
-    a.etime_raw = etime_raw.get();
-    a.eval_raw = eval_raw.get();
+    a.slots = slots.get();
     a.stime = stime.get();
     a.epre = epre.get();
-    a.gscan = gscan.get();
     a.hub_v = ctx.hubs;
     a.hub_toff = d_toff.get();
     a.hub_tcap = d_tcap.get();
@@ -817,50 +1023,110 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     a.tkeys = tkeys.get();
     a.tvals = tvals.get();
     a.hub_any = hub_any.get();
+    a.hub_kud = hub_kud.get();
+    a.hub_sd = hub_sd.get();
     a.hub_done = hub_done.get();
     a.part_d = part_d.get();
     a.part_c = part_c.get();
+    a.mid_v = mid_v.get();
+    a.n_mid = n_mid;
     a.M = ctx.M;
     a.R = ctx.R;
 
-    const int table_smem = (2 * kEventsMax + 32 * 257) * (int)sizeof(uint32_t);
+    static_assert(kEventsMax + 32 * 257 <= kTableSlots + kEventsMax, "sort scratch fits the hash area");
+    const int table_smem = kTableSmemWords * (int)sizeof(uint32_t);
     GB_CUDA(cudaFuncSetAttribute(k_ex_table, cudaFuncAttributeMaxDynamicSharedMemorySize, table_smem));
-    const int eval_smem = kExWarpsPerBlock * 2 * kWarpHash * (int)sizeof(uint32_t);
-    GB_CUDA(cudaFuncSetAttribute(k_ex_eval_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, eval_smem));
-    const int eval_grid = (int)std::min<int64_t>(ceil_div(B, kExWarpsPerBlock), (int64_t)kNumSMs * 16);
+    const int mid_smem = kMidWarpsPerBlock * 2 * kWarpHash * (int)sizeof(uint32_t);
+    GB_CUDA(cudaFuncSetAttribute(k_ex_eval_mid, cudaFuncAttributeMaxDynamicSharedMemorySize, mid_smem));
+    const int small_grid = (int)std::max<int64_t>(1, ceil_div(B, kSmallWarpsPerBlock));
+    const int mid_grid = kNumSMs * 3;
     const int hub_grid = kNumSMs * 4;
     const int commit_grid = (int)std::max<int64_t>(1, ceil_div(B, kT));
     const int commit_b_grid = (int)std::max<int64_t>(1, ceil_div(B * 32, kT));
+    const int per_round = (nh ? 10 : 6) + (n_mid ? 1 : 0);
+    auto enqueue_round = [&](cudaStream_t st) {
+        k_ex_table<<<1, kEvThreads, table_smem, st>>>(a);
+        k_ex_eval_small<<<small_grid, kSmallWarpsPerBlock * 32, 0, st>>>(a);
+        if (n_mid) k_ex_eval_mid<<<mid_grid, kMidWarpsPerBlock * 32, mid_smem, st>>>(a);
+        if (nh) {
+            k_ex_hub_accum<<<hub_grid, kHubThreads2, 0, st>>>(a);
+            k_ex_hub_select<<<hub_grid, kHubThreads2, 0, st>>>(a);
+            k_ex_hub_clear<<<hub_grid, kHubThreads2, 0, st>>>(a);
+        }
+        k_ex_commit_a<<<commit_grid, kT, 0, st>>>(a);
+        k_ex_commit_b<<<commit_b_grid, kT, 0, st>>>(a);
+        if (nh) k_ex_commit_hub<<<hub_grid, kHubThreads2, 0, st>>>(a);
+        k_ex_commit_c<<<commit_grid, kT, 0, st>>>(a);
+        k_ex_advance<<<1, 1024, 0, st>>>(a);
+        GB_LAUNCH_CHECK();
+    };
+
+    // One local-moving iteration as one graph: the init kernel, then a
+    // device-side while loop over rounds whose condition the advance kernel
+    // sets.  GBGPU_EXACT_GRAPH=0 enqueues rounds from the host instead.
+    const char* genv = std::getenv("GBGPU_EXACT_GRAPH");
+    const bool use_graph = !(genv && genv[0] == '0');
+    struct GraphGuard {
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t e = nullptr;
+        cudaStream_t cs = nullptr;
+        ~GraphGuard() {
+            if (e) cudaGraphExecDestroy(e);
+            if (g) cudaGraphDestroy(g);
+            if (cs) cudaStreamDestroy(cs);
+        }
+    } gg;
+    if (use_graph) {
+        GB_CUDA(cudaStreamCreateWithFlags(&gg.cs, cudaStreamNonBlocking));
+        GB_CUDA(cudaGraphCreate(&gg.g, 0));
+        cudaGraphConditionalHandle cond;
+        GB_CUDA(cudaGraphConditionalHandleCreate(&cond, gg.g, 1, cudaGraphCondAssignDefault));
+        a.cond = cond;
+        a.use_cond = 1;
+        GB_CUDA(cudaStreamBeginCaptureToGraph(gg.cs, gg.g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        k_ex_init_iter<<<1, 1024, 0, gg.cs>>>(a);
+        GB_LAUNCH_CHECK();
+        GB_CUDA(cudaStreamEndCapture(gg.cs, &gg.g));
+        cudaGraphNode_t init_node;
+        size_t nn = 1;
+        GB_CUDA(cudaGraphGetNodes(gg.g, &init_node, &nn));
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = cond;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t loop_node;
+        GB_CUDA(cudaGraphAddNode(&loop_node, gg.g, &init_node, nullptr, 1, &cp));
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        GB_CUDA(cudaStreamBeginCaptureToGraph(gg.cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        enqueue_round(gg.cs);
+        GB_CUDA(cudaStreamEndCapture(gg.cs, &body));
+        GB_CUDA(cudaGraphInstantiate(&gg.e, gg.g, 0));
+    }
     const int kBatch = 8;
 
     int iterations = 0;
-    int64_t rounds = 0, nl = 0;
+    int64_t rounds = 0, nl = 0, evals = 0;
     for (int it = 0; it < max_iterations; ++it) {
-        k_ex_init_iter<<<1, 1024, 0, s>>>(a);
-        GB_LAUNCH_CHECK();
-        ++nl;
-        while (true) {
-            for (int b = 0; b < kBatch; ++b) {
-                k_ex_table<<<1, kEvThreads, table_smem, s>>>(a);
-                k_ex_eval_warp<<<eval_grid, kExWarpsPerBlock * 32, eval_smem, s>>>(a);
-                if (nh) {
-                    k_ex_hub_accum<<<hub_grid, 256, 0, s>>>(a);
-                    k_ex_hub_select<<<hub_grid, 256, 0, s>>>(a);
-                    k_ex_hub_clear<<<hub_grid, 256, 0, s>>>(a);
-                }
-                k_ex_commit_a<<<commit_grid, kT, 0, s>>>(a);
-                k_ex_commit_b<<<commit_b_grid, kT, 0, s>>>(a);
-                if (nh) k_ex_commit_hub<<<hub_grid, 256, 0, s>>>(a);
-                k_ex_commit_c<<<commit_grid, kT, 0, s>>>(a);
-                k_ex_advance<<<1, 1024, 0, s>>>(a);
-                GB_LAUNCH_CHECK();
-                nl += nh ? 10 : 6;
-            }
+        if (use_graph) {
+            GB_CUDA(cudaGraphLaunch(gg.e, s));
             GB_CUDA(cudaMemcpyAsync(hctl, ctl.get(), sizeof(Ctl), cudaMemcpyDeviceToHost, s));
             GB_CUDA(cudaStreamSynchronize(s));
-            if (hctl->P >= n) break;
+        } else {
+            k_ex_init_iter<<<1, 1024, 0, s>>>(a);
+            GB_LAUNCH_CHECK();
+            while (true) {
+                for (int b = 0; b < kBatch; ++b) enqueue_round(s);
+                GB_CUDA(cudaMemcpyAsync(hctl, ctl.get(), sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+                GB_CUDA(cudaStreamSynchronize(s));
+                if (hctl->P >= n) break;
+            }
         }
+        if (hctl->error)
+            throw Error(GBGPU_E_CUDA, "serial-order local moving: round loop stopped without progress");
+        nl += 1 + hctl->round * per_round;
         rounds += hctl->round;
+        evals += hctl->evals;
         ++iterations;
         // totalDelta <= tolerance, decided exactly.
         const int sb = 1024;
@@ -889,6 +1155,7 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     cudaFreeHost(hctl);
     if (launches) *launches += nl;
     if (rounds_out) *rounds_out += rounds;
+    if (evals_out) *evals_out += evals;
     return iterations;
 }
 

@@ -66,8 +66,9 @@ k_tier0(const int64_t* __restrict__ rp, const int32_t* __restrict__ col, int64_t
         const double avg = sum / s;
         double var = 0.0;
         for (int i = 0; i < s; ++i) {
-            const double d = (double)e[i].deg - avg;
-            var += d * d;
+            // explicit rounding: no fused multiply-add, as in the reference's sum
+            const double d = __dsub_rn((double)e[i].deg, avg);
+            var = __dadd_rn(var, __dmul_rn(d, d));
         }
         const double variance = s > 1 ? var / (s - 1) : 0.0;
         out[0] = (double)n;

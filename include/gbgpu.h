@@ -111,6 +111,8 @@ typedef struct {
     int64_t bfs_levels;
     int64_t kernel_launches;        /* kernels this call launched */
     double resolution;              /* resolution used */
+    int64_t local_move_rounds;      /* speculative rounds of the serial-order engine */
+    int64_t local_move_evaluations; /* vertex evaluations in those rounds */
 } gbgpu_stats;
 
 /* Context lifetime.  device < 0 selects the current device. */

@@ -135,6 +135,18 @@ def test_serial_engine_against_oracle(ctx, scale, window, monkeypatch):
     np.testing.assert_array_equal(ids.cpu().numpy(), ids_orc)
 
 
+def test_serial_engine_host_driven_rounds(ctx, monkeypatch):
+    """Rounds enqueued from the host (no device-side loop): same membership."""
+    monkeypatch.setenv("GBGPU_EXACT_GRAPH", "0")
+    rp_t, col_t = gg.rmat(16, 16, seed=216, device="cuda")
+    rp, col = rp_t.cpu().numpy(), col_t.cpu().numpy()
+    ar = po.auto_resolution(rp, col)
+    memb, st = ctx.run_graphbrew(rp_t, col_t, SERIAL, ar)
+    m_orc, _ = po.leiden(rp, col, ar)
+    np.testing.assert_array_equal(memb.cpu().numpy().view(np.uint32), m_orc)
+    assert st["local_move_rounds"] > 0
+
+
 def test_parallel_recipe_is_serial_order(ctx):
     """cd_parallel runs the serial-order engine: same membership as cd_serial
     and as the oracle's serial sweep, on a graph with multi-segment hubs."""
