@@ -7,8 +7,8 @@
 
 namespace gb {
 
-constexpr int kWarpMaxDeg = 1024;      // warp path up to this degree
-constexpr int kWarpHash = 2048;        // per-warp shared table slots
+constexpr int kWarpMaxDeg = 512;       // warp path up to this degree
+constexpr int kWarpHash = 1024;        // per-warp shared table slots (>= 2 x kWarpMaxDeg)
 constexpr int kHubThreads = 512;
 constexpr int kHubSmemSlots = 16384;   // hub table in shared memory up to 8192 neighbours
 

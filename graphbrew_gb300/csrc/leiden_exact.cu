@@ -50,7 +50,7 @@ constexpr int kTableSlots = 4 * kWindowMax;   // 32768 hash slots -> 15 bits (+1
 constexpr int kEvThreads = 1024;
 constexpr int kHubThreads2 = 256;             // threads of the hub kernels
 constexpr int kHubSeg = 4 * kHubThreads2;     // edges per hub-accumulation CTA (4 per thread)
-constexpr int kTabSeg = kHubThreads2;         // table slots per hub-selection CTA (1 per thread)
+constexpr int kTabSeg = 4 * kHubThreads2;     // table slots per hub-selection CTA (4 per thread)
 constexpr unsigned long long kNoChange = ~0ull;
 
 struct Ctl {
@@ -61,6 +61,9 @@ struct Ctl {
     long long ms0, ms1;       // mid-degree list range of the window
     long long round;
     long long evals;          // window vertices evaluated in this iteration
+    long long cP, cX;         // committed range of the last decided window
+    long long c_es0, c_es1;   // its hub edge-segment range
+    long long c_ts0, c_ts1;   // its hub table-segment range
     long long max_rounds;     // bound on rounds per iteration (n + 1 always suffices)
     long long error;          // nonzero: the round loop stopped without finishing
 };
@@ -83,6 +86,7 @@ struct ExactState {
     uint32_t* vcom;
     unsigned long long* ctot;
     uint8_t* vaff;
+    uint8_t* mv;          // committed vertex moved (read by the affected-flag kernels)
     Ctl* ctl;
     // decisions, double-buffered by round parity
     uint32_t* best[2];
@@ -124,28 +128,67 @@ __device__ __forceinline__ uint32_t slot_hash(uint32_t c) {
     return (uint32_t)(((uint64_t)c * 0x9E3779B97F4A7C15ull) >> 40);
 }
 
-// Community total at time u: the committed total plus the speculative
-// events of c before u (one 16-byte probe per hash step, then a binary
-// search over the slot's time-sorted events).
-__device__ __forceinline__ long long sigma_at(const ExactState& a, uint32_t c, uint32_t u) {
-    const long long base = (long long)a.ctot[c];
-    uint32_t h = slot_hash(c) & (kTableSlots - 1);
-    SlotMeta sm;
-    while (true) {
-        sm = a.slots[h];
-        if (sm.key == c) break;
-        if (sm.key == kNone) return base;
-        h = (h + 1) & (kTableSlots - 1);
+// Community totals at time u for K communities: the committed total plus the
+// speculative events of c before u -- a 16-byte probe per hash step, then a
+// binary search over the slot's time-sorted events.  The K probe chains and
+// searches advance in lockstep so their loads are in flight together.
+// valid[k] = false entries return 0.
+template <int K>
+__device__ __forceinline__ void sigma_at_k(const ExactState& a, const uint32_t (&c)[K], const bool (&valid)[K],
+                                           uint32_t u, long long (&out)[K]) {
+    uint32_t h[K];
+    int lo[K], l[K], r[K];
+    bool pending[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        out[k] = valid[k] ? (long long)a.ctot[c[k]] : 0;
+        h[k] = slot_hash(c[k]) & (kTableSlots - 1);
+        pending[k] = valid[k];
+        lo[k] = l[k] = r[k] = 0;
     }
-    long long s = base;
-    const int lo = sm.start, hi = sm.end;
-    int l = lo, r = hi;
-    while (l < r) {
-        const int mid = (l + r) >> 1;
-        if (a.stime[mid] < u) l = mid + 1; else r = mid;
+    bool any = true;
+    while (any) {
+        SlotMeta sm[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            if (pending[k]) sm[k] = a.slots[h[k]];
+        any = false;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            if (!pending[k]) continue;
+            if (sm[k].key == c[k]) {
+                lo[k] = l[k] = sm[k].start;
+                r[k] = sm[k].end;
+                pending[k] = false;
+            } else if (sm[k].key == kNone) {
+                pending[k] = false;
+            } else {
+                h[k] = (h[k] + 1) & (kTableSlots - 1);
+                any = true;
+            }
+        }
     }
-    if (l > lo) s += a.epre[l - 1];
-    return s;
+    any = true;
+    while (any) {
+        uint32_t t[K];
+        int mid[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            mid[k] = (l[k] + r[k]) >> 1;
+            if (l[k] < r[k]) t[k] = a.stime[mid[k]];
+        }
+        any = false;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            if (l[k] < r[k]) {
+                if (t[k] < u) l[k] = mid[k] + 1; else r[k] = mid[k];
+                any = any || l[k] < r[k];
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+        if (l[k] > lo[k]) out[k] += a.epre[l[k] - 1];
 }
 
 struct Round {
@@ -272,8 +315,14 @@ __global__ void __launch_bounds__(kEvThreads) k_ex_table(ExactState a) {
         const long long len = w < 2 ? a.n_eseg : (w < 4 ? a.n_tseg : a.n_mid);
         const long long pos = warp_lower_bound_u32(arr, len, (uint32_t)((w & 1) ? E : P), lane);
         if (lane == 0) {
-            long long* dst[6] = {&a.ctl->es0, &a.ctl->es1, &a.ctl->ts0, &a.ctl->ts1, &a.ctl->ms0, &a.ctl->ms1};
-            *dst[w] = pos;
+            switch (w) {
+                case 0: a.ctl->es0 = pos; break;
+                case 1: a.ctl->es1 = pos; break;
+                case 2: a.ctl->ts0 = pos; break;
+                case 3: a.ctl->ts1 = pos; break;
+                case 4: a.ctl->ms0 = pos; break;
+                default: a.ctl->ms1 = pos; break;
+            }
         }
     }
     // Window state: all loads of a thread issued before any use.
@@ -477,9 +526,11 @@ __device__ __forceinline__ void eval_vertex(const ExactState& a, const Round& r,
         const unsigned peers = __match_any_sync(0xFFFFFFFFu, c);
         const double kud = (double)__popc(__ballot_sync(0xFFFFFFFFu, c == d));
         if (c != kNone && c != d && lane == __ffs(peers) - 1) {
-            const double sd = (double)sigma_at(a, d, (uint32_t)u);
-            const double sc = (double)sigma_at(a, c, (uint32_t)u);
-            const double dl = delta_q((double)__popc(peers), kud, ku, sc, sd, a.M, a.R);
+            const uint32_t cc[2] = {c, d};
+            const bool vv[2] = {true, true};
+            long long sg[2];
+            sigma_at_k<2>(a, cc, vv, (uint32_t)u, sg);
+            const double dl = delta_q((double)__popc(peers), kud, ku, (double)sg[0], (double)sg[1], a.M, a.R);
             if (dl > 0.0) { best_d = dl; best_c = c; }
         }
     } else {
@@ -525,12 +576,30 @@ __device__ __forceinline__ void eval_vertex(const ExactState& a, const Round& r,
             cnt += __popc(bal);
             __syncwarp();
         }
-        const double sd = (double)sigma_at(a, d, (uint32_t)u);
-        for (uint32_t i = lane; i < cnt; i += 32) {
-            const uint32_t c = tk[i];
-            const double sc = (double)sigma_at(a, c, (uint32_t)u);
-            const double dl = delta_q((double)tv[i], kud, ku, sc, sd, a.M, a.R);
-            if (dl > 0.0 && better(dl, c, best_d, best_c)) { best_d = dl; best_c = c; }
+        // Four candidates per lane per step, interleaved; the first step also
+        // looks up sigma of d.
+        double sd = 0.0;
+        for (uint32_t i0 = 0;; i0 += 128) {
+            uint32_t cc[5];
+            bool vv[5];
+            long long sg[5];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const uint32_t i = i0 + 32 * k + lane;
+                vv[k] = i < cnt;
+                cc[k] = vv[k] ? tk[i] : kNone;
+            }
+            cc[4] = d;
+            vv[4] = i0 == 0;
+            sigma_at_k<5>(a, cc, vv, (uint32_t)u, sg);
+            if (i0 == 0) sd = (double)sg[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (!vv[k]) continue;
+                const double dl = delta_q((double)tv[i0 + 32 * k + lane], kud, ku, (double)sg[k], sd, a.M, a.R);
+                if (dl > 0.0 && better(dl, cc[k], best_d, best_c)) { best_d = dl; best_c = cc[k]; }
+            }
+            if (i0 + 128 >= cnt) break;
         }
         __syncwarp();
     }
@@ -598,7 +667,13 @@ __global__ void __launch_bounds__(kHubThreads2) k_ex_hub_accum(ExactState a) {
         const uint32_t mask = a.hub_tcap[sg.hub] - 1;
         const uint32_t d = a.vcom[h];
         if (threadIdx.x == 0) s_any = 0;
-        if (threadIdx.x == 0 && sg.part == 0) a.hub_sd[sg.hub] = (double)sigma_at(a, d, h);
+        if (threadIdx.x == 0 && sg.part == 0) {
+            const uint32_t c1[1] = {d};
+            const bool v1[1] = {true};
+            long long s1[1];
+            sigma_at_k<1>(a, c1, v1, h, s1);
+            a.hub_sd[sg.hub] = (double)s1[0];
+        }
         __syncthreads();
         bool any = false;
         uint32_t c[4];
@@ -652,12 +727,23 @@ __global__ void __launch_bounds__(kHubThreads2) k_ex_hub_select(ExactState a) {
         double best_d = 0.0;
         uint32_t best_c = kNone;
         const uint32_t s0 = (uint32_t)sg.part * kTabSeg, s1 = min(cap, s0 + kTabSeg);
-        for (uint32_t i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
-            const uint32_t c = tk[i];
-            if (c == kNone || c == d) continue;
-            const double sc = (double)sigma_at(a, c, h);
-            const double dl = delta_q((double)tv[i], kud, ku, sc, sd, a.M, a.R);
-            if (dl > 0.0 && better(dl, c, best_d, best_c)) { best_d = dl; best_c = c; }
+        // kTabSeg = 4 x blockDim: four slots per thread, lookups interleaved.
+        uint32_t cc[4], cw[4];
+        bool vv[4];
+        long long sgm[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t i = s0 + (uint32_t)k * blockDim.x + threadIdx.x;
+            cc[k] = i < s1 ? tk[i] : kNone;
+            cw[k] = i < s1 ? tv[i] : 0;
+            vv[k] = cc[k] != kNone && cc[k] != d;
+        }
+        sigma_at_k<4>(a, cc, vv, h, sgm);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (!vv[k]) continue;
+            const double dl = delta_q((double)cw[k], kud, ku, (double)sgm[k], sd, a.M, a.R);
+            if (dl > 0.0 && better(dl, cc[k], best_d, best_c)) { best_d = dl; best_c = cc[k]; }
         }
         warp_argmax(best_d, best_c);
         if (lane == 0) { red_d[w] = best_d; red_c[w] = best_c; }
@@ -706,9 +792,56 @@ __global__ void __launch_bounds__(kHubThreads2) k_ex_hub_select(ExactState a) {
     }
 }
 
-__global__ void __launch_bounds__(kHubThreads2) k_ex_hub_clear(ExactState a) {
-    if (a.ctl->P >= a.ctl->n) return;
-    const long long q0 = a.ctl->ts0, q1 = a.ctl->ts1;
+__device__ __forceinline__ long long commit_end(const ExactState& a) {
+    const unsigned long long f = a.ctl->first_change;
+    const long long E = a.ctl->E;
+    return f == kNoChange ? E - 1 : min((long long)f, E - 1);
+}
+
+// The window just decided, as the commit kernels see it after the advance:
+// [cP, cX] is committed (empty when cX < cP); the decisions are the new
+// round's "previous" buffers.
+struct CommitView {
+    long long P, x;
+    const uint8_t* act;
+    const uint32_t* best;
+    const double* delta;
+};
+
+__device__ __forceinline__ CommitView commit_view(const ExactState& a) {
+    CommitView c;
+    c.P = a.ctl->cP;
+    c.x = a.ctl->cX;
+    const int par = (int)(a.ctl->round & 1);
+    c.act = a.act[par];
+    c.best = a.best[par];
+    c.delta = a.delta[par];
+    return c;
+}
+
+// Commit [cP, cX]: totals and memberships of movers, final deltas, processed
+// flags cleared, move flags for the affected-flag kernels; and the decided
+// window's hub tables cleared for the next round.
+__global__ void k_ex_commit_a(ExactState a) {
+    const CommitView c = commit_view(a);
+    if (c.x < c.P) return;
+    for (long long u = c.P + blockIdx.x * (long long)blockDim.x + threadIdx.x; u <= c.x;
+         u += (long long)gridDim.x * blockDim.x) {
+        double dl = 0.0;
+        const uint32_t cur = a.vcom[u], nb = c.best[u];
+        const bool moves = c.act[u] == 1 && nb != cur;
+        if (moves) {
+            const long long deg = (long long)(a.rp[u + 1] - a.rp[u]);
+            atomicAdd(&a.ctot[cur], (unsigned long long)(-deg));
+            atomicAdd(&a.ctot[nb], (unsigned long long)deg);
+            dl = c.delta[u];
+            a.vcom[u] = nb;
+        }
+        a.mv[u] = moves;
+        a.final_delta[u] = dl;
+        a.vaff[u] = 0;
+    }
+    const long long q0 = a.ctl->c_ts0, q1 = a.ctl->c_ts1;
     for (long long q = q0 + blockIdx.x; q < q1; q += gridDim.x) {
         const HubSeg sg = a.tseg[q];
         uint32_t* tk = a.tkeys + a.hub_toff[sg.hub];
@@ -721,85 +854,58 @@ __global__ void __launch_bounds__(kHubThreads2) k_ex_hub_clear(ExactState a) {
     }
 }
 
-__device__ __forceinline__ long long commit_end(const ExactState& a) {
-    const unsigned long long f = a.ctl->first_change;
-    const long long E = a.ctl->E;
-    return f == kNoChange ? E - 1 : min((long long)f, E - 1);
-}
-
-// Commit [P, x]: totals of movers, final deltas, processed flags cleared.
-__global__ void k_ex_commit_a(ExactState a) {
-    if (a.ctl->P >= a.ctl->n) return;
-    const Round r = round_view(a);
-    const long long x = commit_end(a);
-    for (long long u = r.P + blockIdx.x * (long long)blockDim.x + threadIdx.x; u <= x;
-         u += (long long)gridDim.x * blockDim.x) {
-        double dl = 0.0;
-        if (r.nact[u] == 1 && r.nbest[u] != a.vcom[u]) {
-            const long long deg = (long long)(a.rp[u + 1] - a.rp[u]);
-            atomicAdd(&a.ctot[a.vcom[u]], (unsigned long long)(-deg));
-            atomicAdd(&a.ctot[r.nbest[u]], (unsigned long long)deg);
-            dl = r.ndelta[u];
-        }
-        a.final_delta[u] = dl;
-        a.vaff[u] = 0;
-    }
-}
-
-// Affected flags from committed movers: every neighbour outside [P, x] and
-// every neighbour in [P, x] processed before the mover.  Non-hub movers here,
-// hub movers in k_ex_commit_hub.
+// Affected flags from committed movers: every neighbour outside [cP, cX] and
+// every neighbour in [cP, cX] processed before the mover.  Non-hub movers
+// here, hub movers in k_ex_commit_hub.
 __global__ void k_ex_commit_b(ExactState a) {
-    if (a.ctl->P >= a.ctl->n) return;
-    const Round r = round_view(a);
-    const long long x = commit_end(a);
+    const CommitView c = commit_view(a);
+    if (c.x < c.P) return;
     const int lane = threadIdx.x & 31;
     const long long wid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
     const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long w = r.P + wid; w <= x; w += nw) {
-        if (!(r.nact[w] == 1 && r.nbest[w] != a.vcom[w])) continue;
+    for (long long w = c.P + wid; w <= c.x; w += nw) {
+        if (!a.mv[w]) continue;
         const int64_t rb = a.rp[w], re = a.rp[w + 1];
         if (re - rb > kWarpMaxDeg) continue;
         for (int64_t e = rb + lane; e < re; e += 32) {
             const int32_t v = a.col[e];
-            if (v < r.P || v > x || v < w) a.vaff[v] = 1;
+            if (v < c.P || v > c.x || v < w) a.vaff[v] = 1;
         }
     }
 }
 
 __global__ void __launch_bounds__(kHubThreads2) k_ex_commit_hub(ExactState a) {
-    if (a.ctl->P >= a.ctl->n) return;
-    const Round r = round_view(a);
-    const long long x = commit_end(a);
-    const long long q0 = a.ctl->es0, q1 = a.ctl->es1;
+    const CommitView c = commit_view(a);
+    if (c.x < c.P) return;
+    const long long q0 = a.ctl->c_es0, q1 = a.ctl->c_es1;
     for (long long q = q0 + blockIdx.x; q < q1; q += gridDim.x) {
         const HubSeg sg = a.eseg[q];
         const uint32_t h = a.hub_v[sg.hub];
-        if ((long long)h > x) continue;   // segments are in hub order: block-uniform skip
-        if (!(r.nact[h] == 1 && r.nbest[h] != a.vcom[h])) continue;
+        if ((long long)h > c.x) continue;   // segments are in hub order: block-uniform skip
+        if (!a.mv[h]) continue;
         const int64_t rb = a.rp[h], re = a.rp[h + 1];
         const int64_t e0 = rb + (int64_t)sg.part * kHubSeg, e1 = min(re, e0 + kHubSeg);
         for (int64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
             const int32_t v = a.col[e];
-            if (v < r.P || v > x || v < (int64_t)h) a.vaff[v] = 1;
+            if (v < c.P || v > c.x || v < (int64_t)h) a.vaff[v] = 1;
         }
     }
 }
 
-__global__ void k_ex_commit_c(ExactState a) {
-    if (a.ctl->P >= a.ctl->n) return;
-    const Round r = round_view(a);
-    const long long x = commit_end(a);
-    for (long long u = r.P + blockIdx.x * (long long)blockDim.x + threadIdx.x; u <= x;
-         u += (long long)gridDim.x * blockDim.x)
-        if (r.nact[u] == 1) a.vcom[u] = r.nbest[u];
-}
-
-// Slide the window: the new decisions become D_prev; entering vertices are unknown.
+// After the window's decisions: fix the committed prefix [P, x] for the commit
+// kernels, slide the window (the new decisions become D_prev; entering
+// vertices are unknown) and tell the graph's loop whether to go on.  The next
+// window's event table and this window's commits then run concurrently: they
+// touch disjoint vertices.
 __global__ void __launch_bounds__(1024) k_ex_advance(ExactState a) {
     const long long P = a.ctl->P, E = a.ctl->E, n = a.ctl->n, B = a.ctl->B;
     if (P >= n) {
-        if (threadIdx.x == 0 && a.use_cond) cudaGraphSetConditional(a.cond, 0u);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            a.ctl->cP = 1;   // nothing to commit
+            a.ctl->cX = 0;
+            if (a.use_cond) cudaGraphSetConditional(a.cond, 0u);
+        }
         return;
     }
     const long long x = commit_end(a);
@@ -810,6 +916,12 @@ __global__ void __launch_bounds__(1024) k_ex_advance(ExactState a) {
     __syncthreads();
     if (threadIdx.x == 0) {
         const long long rnd = a.ctl->round + 1;
+        a.ctl->cP = P;
+        a.ctl->cX = x;
+        a.ctl->c_es0 = a.ctl->es0;
+        a.ctl->c_es1 = a.ctl->es1;
+        a.ctl->c_ts0 = a.ctl->ts0;
+        a.ctl->c_ts1 = a.ctl->ts1;
         a.ctl->evals = a.ctl->evals + (E - P);
         a.ctl->P = nP;
         a.ctl->E = nE;
@@ -836,6 +948,8 @@ __global__ void __launch_bounds__(1024) k_ex_init_iter(ExactState a) {
         a.ctl->E = E;
         a.ctl->round = 0;
         a.ctl->evals = 0;
+        a.ctl->cP = 1;
+        a.ctl->cX = 0;
     }
 }
 
@@ -978,6 +1092,7 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     DevBuf<uint32_t> best0(n, s), best1(n, s);
     DevBuf<uint8_t> act0(n, s), act1(n, s);
     DevBuf<double> delta0(n, s), delta1(n, s), final_delta(n, s);
+    DevBuf<uint8_t> mv(n, s);
     DevBuf<SlotMeta> slots(kTableSlots, s);
     DevBuf<uint32_t> stime(kEventsMax, s);
     DevBuf<long long> epre(kEventsMax, s);
@@ -998,6 +1113,7 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     a.vcom = ctx.vcom;
     a.ctot = ctx.ctot;
     a.vaff = ctx.vaff;
+    a.mv = mv.get();
     a.ctl = ctl.get();
     a.best[0] = best0.get();
     a.best[1] = best1.get();
@@ -1039,25 +1155,67 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     const int mid_smem = kMidWarpsPerBlock * 2 * kWarpHash * (int)sizeof(uint32_t);
     GB_CUDA(cudaFuncSetAttribute(k_ex_eval_mid, cudaFuncAttributeMaxDynamicSharedMemorySize, mid_smem));
     const int small_grid = (int)std::max<int64_t>(1, ceil_div(B, kSmallWarpsPerBlock));
-    const int mid_grid = kNumSMs * 3;
+    const int mid_grid = kNumSMs * 5;       // resident blocks at 96 registers per thread
+    const int select_grid = kNumSMs * 3;    // resident blocks at 79 registers per thread
     const int hub_grid = kNumSMs * 4;
     const int commit_grid = (int)std::max<int64_t>(1, ceil_div(B, kT));
     const int commit_b_grid = (int)std::max<int64_t>(1, ceil_div(B * 32, kT));
-    const int per_round = (nh ? 10 : 6) + (n_mid ? 1 : 0);
-    auto enqueue_round = [&](cudaStream_t st) {
-        k_ex_table<<<1, kEvThreads, table_smem, st>>>(a);
-        k_ex_eval_small<<<small_grid, kSmallWarpsPerBlock * 32, 0, st>>>(a);
-        if (n_mid) k_ex_eval_mid<<<mid_grid, kMidWarpsPerBlock * 32, mid_smem, st>>>(a);
-        if (nh) {
-            k_ex_hub_accum<<<hub_grid, kHubThreads2, 0, st>>>(a);
-            k_ex_hub_select<<<hub_grid, kHubThreads2, 0, st>>>(a);
-            k_ex_hub_clear<<<hub_grid, kHubThreads2, 0, st>>>(a);
+    const int per_round = 5 + (n_mid ? 1 : 0) + (nh ? 3 : 0);
+    const int commit_a_grid = std::max(commit_grid, nh ? hub_grid : 0);
+    // Side streams and events for the fork/join shape of a captured round:
+    struct Fork {
+        cudaStream_t s1 = nullptr, s2 = nullptr;
+        cudaEvent_t ev[7] = {};
+        ~Fork() {
+            for (cudaEvent_t e : ev)
+                if (e) cudaEventDestroy(e);
+            if (s1) cudaStreamDestroy(s1);
+            if (s2) cudaStreamDestroy(s2);
         }
-        k_ex_commit_a<<<commit_grid, kT, 0, st>>>(a);
-        k_ex_commit_b<<<commit_b_grid, kT, 0, st>>>(a);
-        if (nh) k_ex_commit_hub<<<hub_grid, kHubThreads2, 0, st>>>(a);
-        k_ex_commit_c<<<commit_grid, kT, 0, st>>>(a);
+    } fk;
+    // One round: decide the window, advance, then build the next window's
+    // event table while this window commits.  Forked shape (graph capture):
+    //   { eval_small | eval_mid | hub_accum -> hub_select } -> advance
+    //   -> { table(next) | commit_a -> { commit_b | commit_hub } }
+    // The round before the first needs the first window's table only.
+    auto enqueue_round = [&](cudaStream_t st, bool fork) {
+        cudaStream_t sm = fork ? fk.s1 : st, sh = fork ? fk.s2 : st;
+        if (fork) {
+            GB_CUDA(cudaEventRecord(fk.ev[0], st));
+            GB_CUDA(cudaStreamWaitEvent(sm, fk.ev[0], 0));
+            GB_CUDA(cudaStreamWaitEvent(sh, fk.ev[0], 0));
+        }
+        k_ex_eval_small<<<small_grid, kSmallWarpsPerBlock * 32, 0, st>>>(a);
+        if (n_mid) k_ex_eval_mid<<<mid_grid, kMidWarpsPerBlock * 32, mid_smem, sm>>>(a);
+        if (nh) {
+            k_ex_hub_accum<<<hub_grid, kHubThreads2, 0, sh>>>(a);
+            k_ex_hub_select<<<select_grid, kHubThreads2, 0, sh>>>(a);
+        }
+        if (fork) {
+            GB_CUDA(cudaEventRecord(fk.ev[1], sm));
+            GB_CUDA(cudaEventRecord(fk.ev[2], sh));
+            GB_CUDA(cudaStreamWaitEvent(st, fk.ev[1], 0));
+            GB_CUDA(cudaStreamWaitEvent(st, fk.ev[2], 0));
+        }
         k_ex_advance<<<1, 1024, 0, st>>>(a);
+        if (fork) {
+            GB_CUDA(cudaEventRecord(fk.ev[3], st));
+            GB_CUDA(cudaStreamWaitEvent(sm, fk.ev[3], 0));
+        }
+        k_ex_table<<<1, kEvThreads, table_smem, sm>>>(a);
+        k_ex_commit_a<<<commit_a_grid, kT, 0, st>>>(a);
+        if (fork) {
+            GB_CUDA(cudaEventRecord(fk.ev[4], st));
+            GB_CUDA(cudaStreamWaitEvent(sh, fk.ev[4], 0));
+        }
+        k_ex_commit_b<<<commit_b_grid, kT, 0, st>>>(a);
+        if (nh) k_ex_commit_hub<<<hub_grid, kHubThreads2, 0, sh>>>(a);
+        if (fork) {
+            GB_CUDA(cudaEventRecord(fk.ev[5], sm));
+            GB_CUDA(cudaEventRecord(fk.ev[6], sh));
+            GB_CUDA(cudaStreamWaitEvent(st, fk.ev[5], 0));
+            GB_CUDA(cudaStreamWaitEvent(st, fk.ev[6], 0));
+        }
         GB_LAUNCH_CHECK();
     };
 
@@ -1083,13 +1241,20 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
         GB_CUDA(cudaGraphConditionalHandleCreate(&cond, gg.g, 1, cudaGraphCondAssignDefault));
         a.cond = cond;
         a.use_cond = 1;
-        GB_CUDA(cudaStreamBeginCaptureToGraph(gg.cs, gg.g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-        k_ex_init_iter<<<1, 1024, 0, gg.cs>>>(a);
-        GB_LAUNCH_CHECK();
-        GB_CUDA(cudaStreamEndCapture(gg.cs, &gg.g));
-        cudaGraphNode_t init_node;
-        size_t nn = 1;
-        GB_CUDA(cudaGraphGetNodes(gg.g, &init_node, &nn));
+        // init -> first window's table -> while(rounds)
+        void* kargs[] = {&a};
+        cudaKernelNodeParams kp = {};
+        kp.func = (void*)k_ex_init_iter;
+        kp.gridDim = dim3(1);
+        kp.blockDim = dim3(1024);
+        kp.sharedMemBytes = 0;
+        kp.kernelParams = kargs;
+        cudaGraphNode_t n_init, init_node;
+        GB_CUDA(cudaGraphAddKernelNode(&n_init, gg.g, nullptr, 0, &kp));
+        kp.func = (void*)k_ex_table;
+        kp.blockDim = dim3(kEvThreads);
+        kp.sharedMemBytes = table_smem;
+        GB_CUDA(cudaGraphAddKernelNode(&init_node, gg.g, &n_init, 1, &kp));
         cudaGraphNodeParams cp = {};
         cp.type = cudaGraphNodeTypeConditional;
         cp.conditional.handle = cond;
@@ -1098,8 +1263,11 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
         cudaGraphNode_t loop_node;
         GB_CUDA(cudaGraphAddNode(&loop_node, gg.g, &init_node, nullptr, 1, &cp));
         cudaGraph_t body = cp.conditional.phGraph_out[0];
+        GB_CUDA(cudaStreamCreateWithFlags(&fk.s1, cudaStreamNonBlocking));
+        GB_CUDA(cudaStreamCreateWithFlags(&fk.s2, cudaStreamNonBlocking));
+        for (cudaEvent_t& e : fk.ev) GB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         GB_CUDA(cudaStreamBeginCaptureToGraph(gg.cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-        enqueue_round(gg.cs);
+        enqueue_round(gg.cs, true);
         GB_CUDA(cudaStreamEndCapture(gg.cs, &body));
         GB_CUDA(cudaGraphInstantiate(&gg.e, gg.g, 0));
     }
@@ -1114,9 +1282,10 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
             GB_CUDA(cudaStreamSynchronize(s));
         } else {
             k_ex_init_iter<<<1, 1024, 0, s>>>(a);
+            k_ex_table<<<1, kEvThreads, table_smem, s>>>(a);
             GB_LAUNCH_CHECK();
             while (true) {
-                for (int b = 0; b < kBatch; ++b) enqueue_round(s);
+                for (int b = 0; b < kBatch; ++b) enqueue_round(s, false);
                 GB_CUDA(cudaMemcpyAsync(hctl, ctl.get(), sizeof(Ctl), cudaMemcpyDeviceToHost, s));
                 GB_CUDA(cudaStreamSynchronize(s));
                 if (hctl->P >= n) break;
@@ -1124,7 +1293,7 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
         }
         if (hctl->error)
             throw Error(GBGPU_E_CUDA, "serial-order local moving: round loop stopped without progress");
-        nl += 1 + hctl->round * per_round;
+        nl += 2 + hctl->round * per_round;
         rounds += hctl->round;
         evals += hctl->evals;
         ++iterations;
