@@ -44,10 +44,18 @@ namespace {
 
 constexpr int kT = 256;
 constexpr uint8_t kUnknown = 2;
-constexpr int kWindowMax = 8192;              // window vertices (events <= 2 x window)
-constexpr int kEventsMax = 2 * kWindowMax;    // 16384 -> 14-bit event index
-constexpr int kTableSlots = 4 * kWindowMax;   // 32768 hash slots -> 15 bits (+1 for padding)
-constexpr int kEvThreads = 1024;
+constexpr int kWindowMax = 32768;             // window vertices (events <= 2 x window)
+constexpr int kEventsMax = 2 * kWindowMax;    // event index = 2 x window offset (+1): 16 bits
+constexpr int kSlotBits = 17;
+constexpr int kTableSlots = 1 << kSlotBits;   // hash slots, >= 2 x events
+constexpr int kCoarseBits = 9;                // event grouping: 512 coarse buckets of slots
+constexpr int kCoarse = 1 << kCoarseBits;
+constexpr int kFineBits = kSlotBits - kCoarseBits;
+constexpr int kTbThreads = 1024;              // table insert / group: one window vertex per thread
+constexpr int kTbChunks = kWindowMax / kTbThreads;
+constexpr int kTbFinishThreads = 1024;        // table finish: one CTA per coarse bucket
+constexpr uint32_t kPadSlot = 0xFFFFFFFFu;
+static_assert(kTableSlots >= 2 * kEventsMax, "hash load factor <= 1/2");
 constexpr int kHubThreads2 = 256;             // threads of the hub kernels
 constexpr int kHubSeg = 4 * kHubThreads2;     // edges per hub-accumulation CTA (4 per thread)
 constexpr int kTabSeg = 4 * kHubThreads2;     // table slots per hub-selection CTA (4 per thread)
@@ -66,13 +74,13 @@ struct Ctl {
     long long c_ts0, c_ts1;   // its hub table-segment range
     long long max_rounds;     // bound on rounds per iteration (n + 1 always suffices)
     long long error;          // nonzero: the round loop stopped without finishing
+    unsigned long long tag;   // generation of the event table (slots of older tags are empty)
 };
 
 struct __align__(16) SlotMeta {
-    uint32_t key;     // community id (kNone = empty)
-    int32_t start;    // first sorted event of the slot
-    int32_t end;      // one past its last event
-    int32_t pad;
+    unsigned long long tkey;  // table generation << 32 | community id
+    int32_t start;            // first sorted event of the slot
+    int32_t end;              // one past its last event
 };
 
 struct HubSeg {
@@ -95,8 +103,15 @@ struct ExactState {
     double* final_delta;
     // event table
     SlotMeta* slots;      // kTableSlots: community key and its sorted-event range
-    uint32_t* stime;      // sorted
-    long long* epre;      // inclusive prefix within slot
+    uint32_t* stime;      // event times (vertex ids), sorted by slot then time
+    long long* epre;      // inclusive prefix of the signed degrees within the slot
+    uint32_t* tb_s0;      // per window offset: slot of the departure event (kPadSlot: none)
+    uint32_t* tb_s1;      // slot of the arrival event
+    int32_t* wdeg;        // degree of a window mover, 0 otherwise
+    int32_t* tb_hist;     // coarse bucket x insert chunk counts
+    int32_t* tb_bstart;   // coarse bucket starts (kCoarse + 1)
+    unsigned long long* ev1;  // events grouped by coarse bucket: slot << 32 | event index
+    unsigned long long* ev2;  // events sorted by slot
     // hubs
     const uint32_t* hub_v;        // hub vertex ids (ascending)
     const int64_t* hub_toff;      // table offset
@@ -134,8 +149,8 @@ __device__ __forceinline__ uint32_t slot_hash(uint32_t c) {
 // searches advance in lockstep so their loads are in flight together.
 // valid[k] = false entries return 0.
 template <int K>
-__device__ __forceinline__ void sigma_at_k(const ExactState& a, const uint32_t (&c)[K], const bool (&valid)[K],
-                                           uint32_t u, long long (&out)[K]) {
+__device__ __forceinline__ void sigma_at_k(const ExactState& a, unsigned long long tag, const uint32_t (&c)[K],
+                                           const bool (&valid)[K], uint32_t u, long long (&out)[K]) {
     uint32_t h[K];
     int lo[K], l[K], r[K];
     bool pending[K];
@@ -156,11 +171,11 @@ __device__ __forceinline__ void sigma_at_k(const ExactState& a, const uint32_t (
 #pragma unroll
         for (int k = 0; k < K; ++k) {
             if (!pending[k]) continue;
-            if (sm[k].key == c[k]) {
+            if (sm[k].tkey == (tag << 32 | c[k])) {
                 lo[k] = l[k] = sm[k].start;
                 r[k] = sm[k].end;
                 pending[k] = false;
-            } else if (sm[k].key == kNone) {
+            } else if ((sm[k].tkey >> 32) != tag) {   // a slot of an older table: empty
                 pending[k] = false;
             } else {
                 h[k] = (h[k] + 1) & (kTableSlots - 1);
@@ -193,6 +208,7 @@ __device__ __forceinline__ void sigma_at_k(const ExactState& a, const uint32_t (
 
 struct Round {
     long long P, E;
+    unsigned long long tag;
     const uint32_t* pbest;
     const uint8_t* pact;
     uint32_t* nbest;
@@ -204,6 +220,7 @@ __device__ __forceinline__ Round round_view(const ExactState& a) {
     Round r;
     r.P = a.ctl->P;
     r.E = a.ctl->E;
+    r.tag = a.ctl->tag;
     const int par = (int)(a.ctl->round & 1);
     r.pbest = a.best[par];
     r.pact = a.act[par];
@@ -273,14 +290,19 @@ __device__ __forceinline__ long long warp_lower_bound_u32(const uint32_t* a, lon
 }
 
 // ---------------------------------------------------------------------------
-// Event table (one CTA): hash slots, stable sort by slot, prefix sums.
-// Everything between the window loads and the table stores stays in shared
-// memory: the hash is built there and published, the packed events are
-// radix-sorted there, and the per-slot prefix sums are one segmented scan.
+// Event table.  Each D_prev mover w of the window contributes two events at
+// time w: (old community, -deg w) and (new community, +deg w).  A lookup needs,
+// per community, its events in time order with inclusive prefix sums.  Built
+// in three kernels:
+//   insert: one thread per window vertex; movers insert both communities into
+//           the generation-tagged hash (no clearing between rounds) and count
+//           their events per coarse bucket (high slot bits) per chunk;
+//   group:  each chunk scatters its events, in time order, to its coarse
+//           buckets' ranges (a stable counting pass);
+//   finish: one CTA per coarse bucket sorts its events by the low slot bits
+//           (stable, so time order holds inside a slot) and runs the
+//           segmented prefix sum, filling each slot's event range.
 // ---------------------------------------------------------------------------
-constexpr int kPerThread = kWindowMax / kEvThreads;      // window vertices per thread
-constexpr int kTableSmemWords = kEventsMax + kTableSlots + kWindowMax;
-
 struct SegSum {
     long long v;
     int head;   // a segment starts inside this range
@@ -290,165 +312,239 @@ __device__ __forceinline__ SegSum seg_combine(SegSum a, SegSum b) {
     return SegSum{b.head ? b.v : a.v + b.v, a.head | b.head};
 }
 
-__global__ void __launch_bounds__(kEvThreads) k_ex_table(ExactState a) {
-    extern __shared__ uint32_t sm[];
-    uint32_t* bufA = sm;                               // kEventsMax packed events
-    uint32_t* shash = sm + kEventsMax;                 // kTableSlots while inserting
-    uint32_t* bufB = sm + kEventsMax;                  // kEventsMax, after insertion
-    int32_t* wcnt = reinterpret_cast<int32_t*>(sm + 2 * kEventsMax);  // 32 x 257, after insertion
-    int32_t* wdeg = reinterpret_cast<int32_t*>(sm + kEventsMax + kTableSlots);  // mover degree or 0
-    __shared__ int32_t digit_off[256];
-    __shared__ long long warp_v[32];
-    __shared__ int warp_h[32];
+// Slot of community c in the generation-`tag` table, inserting it if absent.
+__device__ __forceinline__ uint32_t table_insert(SlotMeta* slots, unsigned long long tag, uint32_t c) {
+    const unsigned long long want = tag << 32 | c;
+    uint32_t h = slot_hash(c) & (kTableSlots - 1);
+    while (true) {
+        unsigned long long cur = ((volatile unsigned long long*)&slots[h].tkey)[0];
+        if (cur == want) return h;
+        if ((cur >> 32) != tag) {
+            const unsigned long long prev = atomicCAS(&slots[h].tkey, cur, want);
+            if (prev == cur || prev == want) return h;
+            continue;   // another community took the slot: look at it again
+        }
+        h = (h + 1) & (kTableSlots - 1);
+    }
+}
+
+__global__ void __launch_bounds__(kTbThreads) k_tb_insert(ExactState a) {
+    __shared__ int32_t hist[kCoarse];
+    const long long P = a.ctl->P, E = a.ctl->E;
+    if (P >= a.ctl->n) return;
+    const Round r = round_view(a);
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    for (int b = tid; b < kCoarse; b += blockDim.x) hist[b] = 0;
+    if (blockIdx.x == 0) {
+        if (tid == 0) a.ctl->first_change = kNoChange;
+        // Window ranges of the hub segment lists and the mid-degree list:
+        // six searches on six warps.
+        if (w < 6) {
+            const uint32_t* arr = w < 2 ? a.eseg_v : (w < 4 ? a.tseg_v : a.mid_v);
+            const long long len = w < 2 ? a.n_eseg : (w < 4 ? a.n_tseg : a.n_mid);
+            const long long pos = warp_lower_bound_u32(arr, len, (uint32_t)((w & 1) ? E : P), lane);
+            if (lane == 0) {
+                switch (w) {
+                    case 0: a.ctl->es0 = pos; break;
+                    case 1: a.ctl->es1 = pos; break;
+                    case 2: a.ctl->ts0 = pos; break;
+                    case 3: a.ctl->ts1 = pos; break;
+                    case 4: a.ctl->ms0 = pos; break;
+                    default: a.ctl->ms1 = pos; break;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    const int W = (int)(E - P);
+    const int i = blockIdx.x * blockDim.x + tid;
+    if (i < W) {
+        const int64_t wv = P + i;
+        const uint8_t pa = r.pact[wv];
+        const uint32_t pb = r.pbest[wv], vc = a.vcom[wv];
+        const int64_t r0 = a.rp[wv], r1 = a.rp[wv + 1];
+        uint32_t s0 = kPadSlot, s1 = kPadSlot;
+        int dg = 0;
+        if (pa == 1 && pb != vc) {
+            dg = (int)(r1 - r0);
+            s0 = table_insert(a.slots, r.tag, vc);
+            s1 = table_insert(a.slots, r.tag, pb);
+            atomicAdd(&hist[s0 >> kFineBits], 1);
+            atomicAdd(&hist[s1 >> kFineBits], 1);
+        }
+        a.tb_s0[i] = s0;
+        a.tb_s1[i] = s1;
+        a.wdeg[i] = dg;
+    }
+    __syncthreads();
+    for (int b = tid; b < kCoarse; b += blockDim.x) a.tb_hist[b * kTbChunks + blockIdx.x] = hist[b];
+}
+
+// Stable scatter of each chunk's events to their coarse buckets.  Warp w of a
+// chunk owns its 32 consecutive vertices, i.e. 64 consecutive events.
+__global__ void __launch_bounds__(kTbThreads) k_tb_group(ExactState a) {
+    __shared__ int32_t base[kCoarse];
+    __shared__ int32_t warp_sum[32];
+    extern __shared__ int32_t wcnt[];   // 32 warps x kCoarse
     const long long P = a.ctl->P, E = a.ctl->E;
     if (P >= a.ctl->n) return;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int W = (int)(E - P);
-    const int m = 2 * W;
-    const Round r = round_view(a);
-    for (int i = tid; i < kTableSlots; i += blockDim.x) shash[i] = kNone;
-    if (tid == 0) a.ctl->first_change = kNoChange;
-    // Window ranges of the hub segment lists and the mid-degree list: six
-    // searches on six warps.
-    if (w < 6) {
-        const uint32_t* arr = w < 2 ? a.eseg_v : (w < 4 ? a.tseg_v : a.mid_v);
-        const long long len = w < 2 ? a.n_eseg : (w < 4 ? a.n_tseg : a.n_mid);
-        const long long pos = warp_lower_bound_u32(arr, len, (uint32_t)((w & 1) ? E : P), lane);
-        if (lane == 0) {
-            switch (w) {
-                case 0: a.ctl->es0 = pos; break;
-                case 1: a.ctl->es1 = pos; break;
-                case 2: a.ctl->ts0 = pos; break;
-                case 3: a.ctl->ts1 = pos; break;
-                case 4: a.ctl->ms0 = pos; break;
-                default: a.ctl->ms1 = pos; break;
-            }
+    const int chunks = gridDim.x;
+    // Bucket totals over all chunks and this chunk's offset inside each bucket.
+    int tot = 0, pre = 0;
+    if (tid < kCoarse) {
+        const int32_t* h = a.tb_hist + tid * kTbChunks;
+        for (int c = 0; c < chunks; ++c) {
+            const int v = h[c];
+            tot += v;
+            if (c < (int)blockIdx.x) pre += v;
         }
     }
-    // Window state: all loads of a thread issued before any use.
-    uint8_t pa[kPerThread];
-    uint32_t pb[kPerThread], vc[kPerThread];
-    int64_t r0[kPerThread], r1[kPerThread];
+    // Exclusive scan of the totals (kCoarse = 512 <= threads).
+    int incl = tot;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) warp_sum[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        const int v = warp_sum[lane];
+        int vi = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xFFFFFFFFu, vi, o);
+            if (lane >= o) vi += y;
+        }
+        warp_sum[lane] = vi - v;
+    }
+    __syncthreads();
+    const int excl = warp_sum[w] + incl - tot;
+    if (tid < kCoarse) {
+        base[tid] = excl + pre;
+        if (blockIdx.x == 0) {
+            a.tb_bstart[tid] = excl;
+            if (tid == kCoarse - 1) a.tb_bstart[kCoarse] = excl + tot;
+        }
+    }
+    for (int k = tid; k < 32 * kCoarse; k += blockDim.x) wcnt[k] = 0;
+    __syncthreads();
+    // Count per warp, then turn counts into per-warp offsets (exclusive over warps).
+    const int v0 = blockIdx.x * kTbThreads + w * 32;   // first window offset of this warp
+    uint32_t sl[2];
 #pragma unroll
-    for (int k = 0; k < kPerThread; ++k) {
-        const int i = tid + k * kEvThreads;
-        if (i < W) {
-            const int64_t wv = P + i;
-            pa[k] = r.pact[wv];
-            pb[k] = r.pbest[wv];
-            vc[k] = a.vcom[wv];
-            r0[k] = a.rp[wv];
-            r1[k] = a.rp[wv + 1];
+    for (int st = 0; st < 2; ++st) {
+        const int e = 2 * v0 + st * 32 + lane;    // event index (time order)
+        const int i = e >> 1;
+        sl[st] = i < W ? ((e & 1) ? a.tb_s1[i] : a.tb_s0[i]) : kPadSlot;
+        const int b = sl[st] == kPadSlot ? kCoarse : (int)(sl[st] >> kFineBits);
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, b);
+        if (b < kCoarse && lane == __ffs(peers) - 1) wcnt[w * kCoarse + b] += __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    for (int b = tid; b < kCoarse; b += blockDim.x) {
+        int acc = base[b];
+        for (int ww = 0; ww < 32; ++ww) {
+            const int t = wcnt[ww * kCoarse + b];
+            wcnt[ww * kCoarse + b] = acc;
+            acc += t;
         }
     }
     __syncthreads();
-    // Events of D_prev movers, packed as (slot << 14 | event index); the
-    // event index is 2 x window offset (+1 for the arrival), so it is time order.
-    constexpr uint32_t kPad = (uint32_t)kTableSlots << 14;
 #pragma unroll
-    for (int k = 0; k < kPerThread; ++k) {
-        const int i = tid + k * kEvThreads;
-        if (i >= W) continue;
-        uint32_t p0 = kPad | (uint32_t)(2 * i), p1 = kPad | (uint32_t)(2 * i + 1);
-        int dg = 0;
-        if (pa[k] == 1 && pb[k] != vc[k]) {
-            dg = (int)(r1[k] - r0[k]);
-            uint32_t h0 = slot_hash(vc[k]) & (kTableSlots - 1);
-            while (true) {
-                const uint32_t prev = atomicCAS(&shash[h0], kNone, vc[k]);
-                if (prev == kNone || prev == vc[k]) break;
-                h0 = (h0 + 1) & (kTableSlots - 1);
-            }
-            uint32_t h1 = slot_hash(pb[k]) & (kTableSlots - 1);
-            while (true) {
-                const uint32_t prev = atomicCAS(&shash[h1], kNone, pb[k]);
-                if (prev == kNone || prev == pb[k]) break;
-                h1 = (h1 + 1) & (kTableSlots - 1);
-            }
-            p0 = (h0 << 14) | (uint32_t)(2 * i);
-            p1 = (h1 << 14) | (uint32_t)(2 * i + 1);
+    for (int st = 0; st < 2; ++st) {
+        const int e = 2 * v0 + st * 32 + lane;
+        const int b = sl[st] == kPadSlot ? kCoarse : (int)(sl[st] >> kFineBits);
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, b);
+        int pos = 0;
+        if (b < kCoarse) pos = wcnt[w * kCoarse + b] + __popc(peers & ((1u << lane) - 1u));
+        __syncwarp();
+        if (b < kCoarse) {
+            a.ev1[pos] = (unsigned long long)sl[st] << 32 | (unsigned)e;
+            if (lane == __ffs(peers) - 1) wcnt[w * kCoarse + b] += __popc(peers);
         }
-        wdeg[i] = dg;
-        bufA[2 * i] = p0;
-        bufA[2 * i + 1] = p1;
+        __syncwarp();
+    }
+}
+
+// One CTA per coarse bucket: stable pass on the fine slot bits, then the
+// segmented inclusive scan of signed degrees; writes times, prefixes and the
+// slots' event ranges.
+__global__ void __launch_bounds__(kTbFinishThreads) k_tb_finish(ExactState a) {
+    __shared__ int32_t wcnt[32 * 257];
+    __shared__ int32_t digit[256];
+    __shared__ long long warp_v[32];
+    __shared__ int warp_h[32];
+    const long long P = a.ctl->P;
+    if (P >= a.ctl->n) return;
+    const int bs = a.tb_bstart[blockIdx.x], be = a.tb_bstart[blockIdx.x + 1];
+    const int cnt = be - bs;
+    if (cnt == 0) return;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int nwarps = blockDim.x >> 5;
+    constexpr int kFine = 1 << kFineBits;   // 256
+    static_assert(kFine == 256, "one 8-bit pass");
+    for (int k = tid; k < nwarps * 257; k += blockDim.x) wcnt[k] = 0;
+    __syncthreads();
+    const int chunk = (cnt + nwarps - 1) / nwarps;
+    const int c0 = bs + min(cnt, w * chunk), c1 = bs + min(cnt, (w + 1) * chunk);
+    for (int base = c0; base < c1; base += 32) {
+        const int idx = base + lane;
+        const int d = idx < c1 ? (int)((a.ev1[idx] >> 32) & (kFine - 1)) : kFine;
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
+        if (d < kFine && lane == __ffs(peers) - 1) wcnt[w * 257 + d] += __popc(peers);
+        __syncwarp();
     }
     __syncthreads();
-    // Publish the slot keys for lookups; the shared hash area becomes bufB.
-    for (int i = tid; i < kTableSlots; i += blockDim.x) a.slots[i].key = shash[i];
-    __syncthreads();
-    // Stable LSD radix sort on the slot bits (14..29): two 8-bit passes.
-    // Warp w owns a contiguous chunk; inside it 32-element steps keep order.
-    const int chunk = (m + 31) / 32;
-    uint32_t* src = bufA;
-    uint32_t* dst = bufB;
-    for (int pass = 0; pass < 2; ++pass) {
-        const int shift = 14 + 8 * pass;
-        for (int i = tid; i < 32 * 257; i += blockDim.x) wcnt[i] = 0;
-        __syncthreads();
-        const int c0 = w * chunk, c1 = min(m, c0 + chunk);
-        for (int base = c0; base < c1; base += 32) {
-            const int idx = base + lane;
-            const int d = idx < c1 ? (int)((src[idx] >> shift) & 0xFF) : 256;
-            const unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
-            if (d < 256 && lane == __ffs(peers) - 1) wcnt[w * 257 + d] += __popc(peers);
-            __syncwarp();
+    if (tid < kFine) {
+        int acc = 0;
+        for (int ww = 0; ww < nwarps; ++ww) {
+            const int t = wcnt[ww * 257 + tid];
+            wcnt[ww * 257 + tid] = acc;
+            acc += t;
         }
-        __syncthreads();
-        if (tid < 256) {
-            int acc = 0;
-            for (int ww = 0; ww < 32; ++ww) {
-                const int t = wcnt[ww * 257 + tid];
-                wcnt[ww * 257 + tid] = acc;
-                acc += t;
-            }
-            digit_off[tid] = acc;  // digit total for now
-        }
-        __syncthreads();
-        if (w == 0) {
-            // exclusive scan of the 256 digit totals, 8 per lane
-            int v[8], t = 0;
-#pragma unroll
-            for (int k = 0; k < 8; ++k) { v[k] = digit_off[lane * 8 + k]; t += v[k]; }
-            int incl = t;
-            for (int o = 1; o < 32; o <<= 1) {
-                const int y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-                if (lane >= o) incl += y;
-            }
-            int run = incl - t;
-#pragma unroll
-            for (int k = 0; k < 8; ++k) { digit_off[lane * 8 + k] = run; run += v[k]; }
-        }
-        __syncthreads();
-        for (int base = c0; base < c1; base += 32) {
-            const int idx = base + lane;
-            const int d = idx < c1 ? (int)((src[idx] >> shift) & 0xFF) : 256;
-            const unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
-            const unsigned lt = (1u << lane) - 1u;
-            int before = 0;
-            if (d < 256) before = wcnt[w * 257 + d];
-            __syncwarp();
-            if (d < 256) dst[digit_off[d] + before + __popc(peers & lt)] = src[idx];
-            if (d < 256 && lane == __ffs(peers) - 1) wcnt[w * 257 + d] = before + __popc(peers);
-            __syncwarp();
-        }
-        __syncthreads();
-        uint32_t* t = src;
-        src = dst;
-        dst = t;
+        digit[tid] = acc;
     }
-    // src holds the sorted events.  Per-slot inclusive prefix sums of the
-    // signed degrees: a segmented scan, each thread over a contiguous range.
-    const int per = (m + blockDim.x - 1) / blockDim.x;
-    const int b0 = min(m, tid * per), b1 = min(m, b0 + per);
+    __syncthreads();
+    if (w == 0) {
+        int v[8], t = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) { v[k] = digit[lane * 8 + k]; t += v[k]; }
+        int incl = t;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        int run = incl - t;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) { digit[lane * 8 + k] = run; run += v[k]; }
+    }
+    __syncthreads();
+    for (int base = c0; base < c1; base += 32) {
+        const int idx = base + lane;
+        const unsigned long long key = idx < c1 ? a.ev1[idx] : 0ull;
+        const int d = idx < c1 ? (int)((key >> 32) & (kFine - 1)) : kFine;
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
+        int before = 0;
+        if (d < kFine) before = wcnt[w * 257 + d];
+        __syncwarp();
+        if (d < kFine) a.ev2[bs + digit[d] + before + __popc(peers & ((1u << lane) - 1u))] = key;
+        if (d < kFine && lane == __ffs(peers) - 1) wcnt[w * 257 + d] = before + __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    // Segmented inclusive scan over ev2[bs, be), each thread a contiguous range.
+    const int per = (cnt + blockDim.x - 1) / blockDim.x;
+    const int b0 = bs + min(cnt, tid * per), b1 = bs + min(cnt, tid * per + per);
     SegSum own{0, 0};
-    for (int i = b0; i < b1; ++i) {
-        const uint32_t pk = src[i];
-        const uint32_t sl = pk >> 14, e = pk & 0x3FFF;
-        const int head = (i == 0 || (src[i - 1] >> 14) != sl);
-        const long long v = sl < (uint32_t)kTableSlots ? ((e & 1) ? wdeg[e >> 1] : -(long long)wdeg[e >> 1]) : 0;
+    for (int k = b0; k < b1; ++k) {
+        const unsigned long long key = a.ev2[k];
+        const uint32_t sl = (uint32_t)(key >> 32), e = (uint32_t)key;
+        const int head = (k == bs || (uint32_t)(a.ev2[k - 1] >> 32) != sl);
+        const long long v = (e & 1) ? a.wdeg[e >> 1] : -(long long)a.wdeg[e >> 1];
         own = seg_combine(own, SegSum{v, head});
     }
-    // exclusive scan of the thread aggregates (warp shuffles, then warps)
     SegSum inc = own;
     for (int o = 1; o < 32; o <<= 1) {
         SegSum y{__shfl_up_sync(0xFFFFFFFFu, inc.v, o), __shfl_up_sync(0xFFFFFFFFu, inc.head, o)};
@@ -457,34 +553,31 @@ __global__ void __launch_bounds__(kEvThreads) k_ex_table(ExactState a) {
     if (lane == 31) { warp_v[w] = inc.v; warp_h[w] = inc.head; }
     __syncthreads();
     if (w == 0) {
-        SegSum x{warp_v[lane], warp_h[lane]};
+        SegSum x = lane < nwarps ? SegSum{warp_v[lane], warp_h[lane]} : SegSum{0, 0};
         SegSum xi = x;
         for (int o = 1; o < 32; o <<= 1) {
             SegSum y{__shfl_up_sync(0xFFFFFFFFu, xi.v, o), __shfl_up_sync(0xFFFFFFFFu, xi.head, o)};
             if (lane >= o) xi = seg_combine(y, xi);
         }
-        // exclusive value for warp `lane`
         SegSum ex{__shfl_up_sync(0xFFFFFFFFu, xi.v, 1), __shfl_up_sync(0xFFFFFFFFu, xi.head, 1)};
         if (lane == 0) ex = SegSum{0, 0};
-        warp_v[lane] = ex.v;
-        warp_h[lane] = ex.head;
+        if (lane < nwarps) { warp_v[lane] = ex.v; warp_h[lane] = ex.head; }
     }
     __syncthreads();
     SegSum ex_thread{__shfl_up_sync(0xFFFFFFFFu, inc.v, 1), __shfl_up_sync(0xFFFFFFFFu, inc.head, 1)};
     if (lane == 0) ex_thread = SegSum{0, 0};
     const SegSum carry = seg_combine(SegSum{warp_v[w], warp_h[w]}, ex_thread);
     long long run = carry.v;
-    for (int i = b0; i < b1; ++i) {
-        const uint32_t pk = src[i];
-        const uint32_t sl = pk >> 14, e = pk & 0x3FFF;
-        a.stime[i] = (uint32_t)(P + (e >> 1));
-        if (sl >= (uint32_t)kTableSlots) continue;
-        const long long v = (e & 1) ? wdeg[e >> 1] : -(long long)wdeg[e >> 1];
-        const bool head = (i == 0 || (src[i - 1] >> 14) != sl);
+    for (int k = b0; k < b1; ++k) {
+        const unsigned long long key = a.ev2[k];
+        const uint32_t sl = (uint32_t)(key >> 32), e = (uint32_t)key;
+        const long long v = (e & 1) ? a.wdeg[e >> 1] : -(long long)a.wdeg[e >> 1];
+        const bool head = (k == bs || (uint32_t)(a.ev2[k - 1] >> 32) != sl);
         run = head ? v : run + v;
-        a.epre[i] = run;
-        if (head) a.slots[sl].start = i;
-        if (i == m - 1 || (src[i + 1] >> 14) != sl) a.slots[sl].end = i + 1;
+        a.stime[k] = (uint32_t)(P + (e >> 1));
+        a.epre[k] = run;
+        if (head) a.slots[sl].start = k;
+        if (k == be - 1 || (uint32_t)(a.ev2[k + 1] >> 32) != sl) a.slots[sl].end = k + 1;
     }
 }
 
@@ -529,7 +622,7 @@ __device__ __forceinline__ void eval_vertex(const ExactState& a, const Round& r,
             const uint32_t cc[2] = {c, d};
             const bool vv[2] = {true, true};
             long long sg[2];
-            sigma_at_k<2>(a, cc, vv, (uint32_t)u, sg);
+            sigma_at_k<2>(a, r.tag, cc, vv, (uint32_t)u, sg);
             const double dl = delta_q((double)__popc(peers), kud, ku, (double)sg[0], (double)sg[1], a.M, a.R);
             if (dl > 0.0) { best_d = dl; best_c = c; }
         }
@@ -591,7 +684,7 @@ __device__ __forceinline__ void eval_vertex(const ExactState& a, const Round& r,
             }
             cc[4] = d;
             vv[4] = i0 == 0;
-            sigma_at_k<5>(a, cc, vv, (uint32_t)u, sg);
+            sigma_at_k<5>(a, r.tag, cc, vv, (uint32_t)u, sg);
             if (i0 == 0) sd = (double)sg[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
@@ -671,7 +764,7 @@ __global__ void __launch_bounds__(kHubThreads2) k_ex_hub_accum(ExactState a) {
             const uint32_t c1[1] = {d};
             const bool v1[1] = {true};
             long long s1[1];
-            sigma_at_k<1>(a, c1, v1, h, s1);
+            sigma_at_k<1>(a, r.tag, c1, v1, h, s1);
             a.hub_sd[sg.hub] = (double)s1[0];
         }
         __syncthreads();
@@ -738,7 +831,7 @@ __global__ void __launch_bounds__(kHubThreads2) k_ex_hub_select(ExactState a) {
             cw[k] = i < s1 ? tv[i] : 0;
             vv[k] = cc[k] != kNone && cc[k] != d;
         }
-        sigma_at_k<4>(a, cc, vv, h, sgm);
+        sigma_at_k<4>(a, r.tag, cc, vv, h, sgm);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             if (!vv[k]) continue;
@@ -926,6 +1019,7 @@ __global__ void __launch_bounds__(1024) k_ex_advance(ExactState a) {
         a.ctl->P = nP;
         a.ctl->E = nE;
         a.ctl->round = rnd;
+        a.ctl->tag = a.ctl->tag + 1;
         // Every round commits at least vertex P, so the loop ends within n
         // rounds; the bound only guards against a broken invariant.
         bool more = nP < n;
@@ -950,6 +1044,7 @@ __global__ void __launch_bounds__(1024) k_ex_init_iter(ExactState a) {
         a.ctl->evals = 0;
         a.ctl->cP = 1;
         a.ctl->cX = 0;
+        a.ctl->tag = a.ctl->tag + 1;
     }
 }
 
@@ -1094,8 +1189,11 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     DevBuf<double> delta0(n, s), delta1(n, s), final_delta(n, s);
     DevBuf<uint8_t> mv(n, s);
     DevBuf<SlotMeta> slots(kTableSlots, s);
-    DevBuf<uint32_t> stime(kEventsMax, s);
+    GB_CUDA(cudaMemsetAsync(slots, 0xFF, kTableSlots * sizeof(SlotMeta), s));   // no generation yet
+    DevBuf<uint32_t> stime(kEventsMax, s), tb_s0(kWindowMax, s), tb_s1(kWindowMax, s);
     DevBuf<long long> epre(kEventsMax, s);
+    DevBuf<int32_t> wdeg(kWindowMax, s), tb_hist(kCoarse * kTbChunks, s), tb_bstart(kCoarse + 1, s);
+    DevBuf<unsigned long long> ev1(kEventsMax, s), ev2(kEventsMax, s);
     DevBuf<Ctl> ctl(1, s);
     Ctl* hctl = nullptr;
     GB_CUDA(cudaMallocHost(&hctl, sizeof(Ctl)));
@@ -1123,6 +1221,13 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     a.delta[1] = delta1.get();
     a.final_delta = final_delta.get();
     a.slots = slots.get();
+    a.tb_s0 = tb_s0.get();
+    a.tb_s1 = tb_s1.get();
+    a.wdeg = wdeg.get();
+    a.tb_hist = tb_hist.get();
+    a.tb_bstart = tb_bstart.get();
+    a.ev1 = ev1.get();
+    a.ev2 = ev2.get();
     a.stime = stime.get();
     a.epre = epre.get();
     a.hub_v = ctx.hubs;
@@ -1150,17 +1255,23 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     a.R = ctx.R;
 
     static_assert(kEventsMax + 32 * 257 <= kTableSlots + kEventsMax, "sort scratch fits the hash area");
-    const int table_smem = kTableSmemWords * (int)sizeof(uint32_t);
-    GB_CUDA(cudaFuncSetAttribute(k_ex_table, cudaFuncAttributeMaxDynamicSharedMemorySize, table_smem));
+    const int group_smem = 32 * kCoarse * (int)sizeof(int32_t);
+    GB_CUDA(cudaFuncSetAttribute(k_tb_group, cudaFuncAttributeMaxDynamicSharedMemorySize, group_smem));
+    const int tb_grid = (int)ceil_div(B, kTbThreads);
+    auto enqueue_table = [&](cudaStream_t st) {
+        k_tb_insert<<<tb_grid, kTbThreads, 0, st>>>(a);
+        k_tb_group<<<tb_grid, kTbThreads, group_smem, st>>>(a);
+        k_tb_finish<<<kCoarse, kTbFinishThreads, 0, st>>>(a);
+    };
     const int mid_smem = kMidWarpsPerBlock * 2 * kWarpHash * (int)sizeof(uint32_t);
     GB_CUDA(cudaFuncSetAttribute(k_ex_eval_mid, cudaFuncAttributeMaxDynamicSharedMemorySize, mid_smem));
     const int small_grid = (int)std::max<int64_t>(1, ceil_div(B, kSmallWarpsPerBlock));
-    const int mid_grid = kNumSMs * 5;       // resident blocks at 96 registers per thread
+    const int mid_grid = kNumSMs * 4;       // resident blocks at ~105 registers per thread
     const int select_grid = kNumSMs * 3;    // resident blocks at 79 registers per thread
     const int hub_grid = kNumSMs * 4;
     const int commit_grid = (int)std::max<int64_t>(1, ceil_div(B, kT));
     const int commit_b_grid = (int)std::max<int64_t>(1, ceil_div(B * 32, kT));
-    const int per_round = 5 + (n_mid ? 1 : 0) + (nh ? 3 : 0);
+    const int per_round = 7 + (n_mid ? 1 : 0) + (nh ? 3 : 0);
     const int commit_a_grid = std::max(commit_grid, nh ? hub_grid : 0);
     // Side streams and events for the fork/join shape of a captured round:
     struct Fork {
@@ -1202,7 +1313,7 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
             GB_CUDA(cudaEventRecord(fk.ev[3], st));
             GB_CUDA(cudaStreamWaitEvent(sm, fk.ev[3], 0));
         }
-        k_ex_table<<<1, kEvThreads, table_smem, sm>>>(a);
+        enqueue_table(sm);
         k_ex_commit_a<<<commit_a_grid, kT, 0, st>>>(a);
         if (fork) {
             GB_CUDA(cudaEventRecord(fk.ev[4], st));
@@ -1241,20 +1352,26 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
         GB_CUDA(cudaGraphConditionalHandleCreate(&cond, gg.g, 1, cudaGraphCondAssignDefault));
         a.cond = cond;
         a.use_cond = 1;
-        // init -> first window's table -> while(rounds)
-        void* kargs[] = {&a};
-        cudaKernelNodeParams kp = {};
-        kp.func = (void*)k_ex_init_iter;
-        kp.gridDim = dim3(1);
-        kp.blockDim = dim3(1024);
-        kp.sharedMemBytes = 0;
-        kp.kernelParams = kargs;
-        cudaGraphNode_t n_init, init_node;
-        GB_CUDA(cudaGraphAddKernelNode(&n_init, gg.g, nullptr, 0, &kp));
-        kp.func = (void*)k_ex_table;
-        kp.blockDim = dim3(kEvThreads);
-        kp.sharedMemBytes = table_smem;
-        GB_CUDA(cudaGraphAddKernelNode(&init_node, gg.g, &n_init, 1, &kp));
+        // init -> first window's table (captured) -> while(rounds)
+        GB_CUDA(cudaStreamBeginCaptureToGraph(gg.cs, gg.g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        k_ex_init_iter<<<1, 1024, 0, gg.cs>>>(a);
+        enqueue_table(gg.cs);
+        GB_LAUNCH_CHECK();
+        GB_CUDA(cudaStreamEndCapture(gg.cs, &gg.g));
+        // The captured chain's last node (the one no other node depends on).
+        cudaGraphNode_t init_node = nullptr;
+        {
+            size_t nn = 0;
+            GB_CUDA(cudaGraphGetNodes(gg.g, nullptr, &nn));
+            std::vector<cudaGraphNode_t> nodes(nn);
+            GB_CUDA(cudaGraphGetNodes(gg.g, nodes.data(), &nn));
+            for (cudaGraphNode_t nd : nodes) {
+                size_t nd_out = 0;
+                GB_CUDA(cudaGraphNodeGetDependentNodes(nd, nullptr, nullptr, &nd_out));
+                if (nd_out == 0) init_node = nd;
+            }
+            if (!init_node) throw Error(GBGPU_E_CUDA, "serial-order local moving: empty init graph");
+        }
         cudaGraphNodeParams cp = {};
         cp.type = cudaGraphNodeTypeConditional;
         cp.conditional.handle = cond;
@@ -1282,7 +1399,7 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
             GB_CUDA(cudaStreamSynchronize(s));
         } else {
             k_ex_init_iter<<<1, 1024, 0, s>>>(a);
-            k_ex_table<<<1, kEvThreads, table_smem, s>>>(a);
+            enqueue_table(s);
             GB_LAUNCH_CHECK();
             while (true) {
                 for (int b = 0; b < kBatch; ++b) enqueue_round(s, false);
@@ -1293,7 +1410,7 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
         }
         if (hctl->error)
             throw Error(GBGPU_E_CUDA, "serial-order local moving: round loop stopped without progress");
-        nl += 2 + hctl->round * per_round;
+        nl += 4 + hctl->round * per_round;
         rounds += hctl->round;
         evals += hctl->evals;
         ++iterations;

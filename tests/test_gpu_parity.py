@@ -119,7 +119,8 @@ def test_serial_mapping_bit_exact(ctx, name, manifest, golden_arrays):
     assert gb.mapping_fingerprint(ids) == case["serial_fingerprint"]
 
 
-@pytest.mark.parametrize("scale,window", [(14, 8192), (16, 8192), (16, 1024), (18, 4096), (20, 8192)])
+@pytest.mark.parametrize("scale,window", [(14, 8192), (16, 32768), (16, 1024), (18, 4096), (20, 8192),
+                                          (20, 32768)])
 def test_serial_engine_against_oracle(ctx, scale, window, monkeypatch):
     """Serial-order engine at larger sizes and window settings: bit-exact."""
     monkeypatch.setenv("GBGPU_EXACT_WINDOW", str(window))
