@@ -766,15 +766,17 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
             DevBuf<uint32_t> proposed(C, s);
             DevBuf<double> pdelta(C, s);
             // Largest super-degree decides the per-warp global table size.
-            int32_t max_sdeg = 0;
+            int64_t max_sdeg = 0;
             {
-                std::vector<int32_t> sd(C);
-                GB_CUDA(cudaMemcpyAsync(sd.data(), sdeg.get(), C * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-                GB_CUDA(cudaStreamSynchronize(s));
-                for (int32_t v : sd) max_sdeg = std::max(max_sdeg, v);
+                DevBuf<unsigned long long> md(1, s);
+                GB_CUDA(cudaMemsetAsync(md, 0, sizeof(unsigned long long), s));
+                k_max_degree<<<grid_for(C, kT), kT, 0, s>>>(soff, C, md);
+                GB_LAUNCH_CHECK();
+                max_sdeg = (int64_t)read_dev(md.get(), s);
+                ++launches;
             }
             int64_t gcap = 64;
-            while (gcap < 2 * (int64_t)max_sdeg) gcap <<= 1;
+            while (gcap < 2 * max_sdeg) gcap <<= 1;
             const bool single = nuniq <= p.super_single_cta_max_edges;
             // Per-warp global tables for super-nodes above kSmSmall / 2 neighbours,
             // capped at 512 MB in total.

@@ -129,7 +129,9 @@ struct ExactState {
     int32_t* hub_any;
     int32_t* hub_done;
     uint32_t* hub_kud;            // edges of the hub into its own community (accumulated)
-    double* hub_sd;               // sigma of its own community at the hub's time
+    uint32_t* hub_occ;            // per hub (pool offsets): slots of its table in insertion order
+    uint32_t* hub_occn;           // per hub: occupied slots
+    int32_t* hub_clr;             // per hub: table segments cleared this round
     double* part_d;               // per table segment
     uint32_t* part_c;
     const uint32_t* mid_v;        // vertices with 32 < degree <= kWarpMaxDeg (ascending)
@@ -289,6 +291,26 @@ __device__ __forceinline__ long long warp_lower_bound_u32(const uint32_t* a, lon
     return b ? lo + (__ffs(b) - 1) : hi;
 }
 
+// Window ranges of the hub segment lists and the mid-degree list for the
+// window [P, E): six searches on warps 0-5 of the calling CTA.
+__device__ __forceinline__ void window_ranges(const ExactState& a, long long P, long long E) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (w >= 6) return;
+    const uint32_t* arr = w < 2 ? a.eseg_v : (w < 4 ? a.tseg_v : a.mid_v);
+    const long long len = w < 2 ? a.n_eseg : (w < 4 ? a.n_tseg : a.n_mid);
+    const long long pos = warp_lower_bound_u32(arr, len, (uint32_t)((w & 1) ? E : P), lane);
+    if (lane == 0) {
+        switch (w) {
+            case 0: a.ctl->es0 = pos; break;
+            case 1: a.ctl->es1 = pos; break;
+            case 2: a.ctl->ts0 = pos; break;
+            case 3: a.ctl->ts1 = pos; break;
+            case 4: a.ctl->ms0 = pos; break;
+            default: a.ctl->ms1 = pos; break;
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Event table.  Each D_prev mover w of the window contributes two events at
 // time w: (old community, -deg w) and (new community, +deg w).  A lookup needs,
@@ -335,26 +357,9 @@ __global__ void __launch_bounds__(kTbThreads) k_tb_insert(ExactState a) {
     const Round r = round_view(a);
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     for (int b = tid; b < kCoarse; b += blockDim.x) hist[b] = 0;
-    if (blockIdx.x == 0) {
-        if (tid == 0) a.ctl->first_change = kNoChange;
-        // Window ranges of the hub segment lists and the mid-degree list:
-        // six searches on six warps.
-        if (w < 6) {
-            const uint32_t* arr = w < 2 ? a.eseg_v : (w < 4 ? a.tseg_v : a.mid_v);
-            const long long len = w < 2 ? a.n_eseg : (w < 4 ? a.n_tseg : a.n_mid);
-            const long long pos = warp_lower_bound_u32(arr, len, (uint32_t)((w & 1) ? E : P), lane);
-            if (lane == 0) {
-                switch (w) {
-                    case 0: a.ctl->es0 = pos; break;
-                    case 1: a.ctl->es1 = pos; break;
-                    case 2: a.ctl->ts0 = pos; break;
-                    case 3: a.ctl->ts1 = pos; break;
-                    case 4: a.ctl->ms0 = pos; break;
-                    default: a.ctl->ms1 = pos; break;
-                }
-            }
-        }
-    }
+    if (blockIdx.x == 0 && tid == 0) a.ctl->first_change = kNoChange;
+    (void)lane;
+    (void)w;
     __syncthreads();
     const int W = (int)(E - P);
     const int i = blockIdx.x * blockDim.x + tid;
@@ -743,7 +748,8 @@ __global__ void k_mid_scatter(const int32_t* __restrict__ flag, const int64_t* _
 }
 
 // Hub accumulation: one CTA per kHubSeg-edge segment of a window hub, four
-// edges per thread in flight.
+// edges per thread in flight.  Needs no event table: it runs while the
+// previous window commits its affected flags and the event table is built.
 __global__ void __launch_bounds__(kHubThreads2) k_ex_hub_accum(ExactState a) {
     if (a.ctl->P >= a.ctl->n) return;
     const Round r = round_view(a);
@@ -758,15 +764,10 @@ __global__ void __launch_bounds__(kHubThreads2) k_ex_hub_accum(ExactState a) {
         uint32_t* tk = a.tkeys + a.hub_toff[sg.hub];
         uint32_t* tv = a.tvals + a.hub_toff[sg.hub];
         const uint32_t mask = a.hub_tcap[sg.hub] - 1;
+        uint32_t* occ = a.hub_occ + a.hub_toff[sg.hub];
+        uint32_t* occn = a.hub_occn + sg.hub;
         const uint32_t d = a.vcom[h];
         if (threadIdx.x == 0) s_any = 0;
-        if (threadIdx.x == 0 && sg.part == 0) {
-            const uint32_t c1[1] = {d};
-            const bool v1[1] = {true};
-            long long s1[1];
-            sigma_at_k<1>(a, r.tag, c1, v1, h, s1);
-            a.hub_sd[sg.hub] = (double)s1[0];
-        }
         __syncthreads();
         bool any = false;
         uint32_t c[4];
@@ -784,7 +785,19 @@ __global__ void __launch_bounds__(kHubThreads2) k_ex_hub_accum(ExactState a) {
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             const unsigned peers = __match_any_sync(0xFFFFFFFFu, c[k]);
-            if (c[k] != kNone && lane == __ffs(peers) - 1) table_add(tk, tv, mask, c[k], (uint32_t)__popc(peers));
+            if (c[k] != kNone && lane == __ffs(peers) - 1) {
+                // insert-or-add; a new key also goes on the hub's occupied list
+                uint32_t hh = hash_u32(c[k]) & mask;
+                while (true) {
+                    const uint32_t prev = atomicCAS(&tk[hh], kNone, c[k]);
+                    if (prev == kNone) occ[atomicAdd(occn, 1u)] = hh;
+                    if (prev == kNone || prev == c[k]) {
+                        atomicAdd(&tv[hh], (uint32_t)__popc(peers));
+                        break;
+                    }
+                    hh = (hh + 1) & mask;
+                }
+            }
             own += __popc(__ballot_sync(0xFFFFFFFFu, c[k] == d));
         }
         if (lane == 0 && own) atomicAdd(&a.hub_kud[sg.hub], own);
@@ -812,31 +825,38 @@ __global__ void __launch_bounds__(kHubThreads2) k_ex_hub_select(ExactState a) {
         const uint32_t h = a.hub_v[j];
         const uint32_t* tk = a.tkeys + a.hub_toff[j];
         const uint32_t* tv = a.tvals + a.hub_toff[j];
-        const uint32_t cap = a.hub_tcap[j];
+        const uint32_t* occ = a.hub_occ + a.hub_toff[j];
+        const uint32_t nocc = a.hub_occn[j];
         const uint32_t d = a.vcom[h];
         const double ku = (double)(a.rp[h + 1] - a.rp[h]);
         const double kud = (double)a.hub_kud[j];
-        const double sd = a.hub_sd[j];
         double best_d = 0.0;
         uint32_t best_c = kNone;
-        const uint32_t s0 = (uint32_t)sg.part * kTabSeg, s1 = min(cap, s0 + kTabSeg);
-        // kTabSeg = 4 x blockDim: four slots per thread, lookups interleaved.
-        uint32_t cc[4], cw[4];
-        bool vv[4];
-        long long sgm[4];
+        // Segment `part` covers occupied-list positions [s0, s0 + kTabSeg):
+        // four per thread, lookups interleaved with the one for d.
+        const uint32_t s0 = (uint32_t)sg.part * kTabSeg, s1 = min(nocc, s0 + kTabSeg);
+        if (s0 < s1) {
+            uint32_t cc[5], cw[4];
+            bool vv[5];
+            long long sgm[5];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const uint32_t i = s0 + (uint32_t)k * blockDim.x + threadIdx.x;
-            cc[k] = i < s1 ? tk[i] : kNone;
-            cw[k] = i < s1 ? tv[i] : 0;
-            vv[k] = cc[k] != kNone && cc[k] != d;
-        }
-        sigma_at_k<4>(a, r.tag, cc, vv, h, sgm);
+            for (int k = 0; k < 4; ++k) {
+                const uint32_t i = s0 + (uint32_t)k * blockDim.x + threadIdx.x;
+                const uint32_t slot = i < s1 ? occ[i] : 0u;
+                cc[k] = i < s1 ? tk[slot] : kNone;
+                cw[k] = i < s1 ? tv[slot] : 0;
+                vv[k] = cc[k] != kNone && cc[k] != d;
+            }
+            cc[4] = d;
+            vv[4] = true;
+            sigma_at_k<5>(a, r.tag, cc, vv, h, sgm);
+            const double sd = (double)sgm[4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            if (!vv[k]) continue;
-            const double dl = delta_q((double)cw[k], kud, ku, (double)sgm[k], sd, a.M, a.R);
-            if (dl > 0.0 && better(dl, cc[k], best_d, best_c)) { best_d = dl; best_c = cc[k]; }
+            for (int k = 0; k < 4; ++k) {
+                if (!vv[k]) continue;
+                const double dl = delta_q((double)cw[k], kud, ku, (double)sgm[k], sd, a.M, a.R);
+                if (dl > 0.0 && better(dl, cc[k], best_d, best_c)) { best_d = dl; best_c = cc[k]; }
+            }
         }
         warp_argmax(best_d, best_c);
         if (lane == 0) { red_d[w] = best_d; red_c[w] = best_c; }
@@ -935,14 +955,27 @@ __global__ void k_ex_commit_a(ExactState a) {
         a.vaff[u] = 0;
     }
     const long long q0 = a.ctl->c_ts0, q1 = a.ctl->c_ts1;
+    __shared__ int s_last;
     for (long long q = q0 + blockIdx.x; q < q1; q += gridDim.x) {
         const HubSeg sg = a.tseg[q];
-        uint32_t* tk = a.tkeys + a.hub_toff[sg.hub];
-        uint32_t* tv = a.tvals + a.hub_toff[sg.hub];
-        const uint32_t s0 = (uint32_t)sg.part * kTabSeg, s1 = min(a.hub_tcap[sg.hub], s0 + kTabSeg);
+        const int j = sg.hub;
+        uint32_t* tk = a.tkeys + a.hub_toff[j];
+        uint32_t* tv = a.tvals + a.hub_toff[j];
+        const uint32_t* occ = a.hub_occ + a.hub_toff[j];
+        const uint32_t s0 = (uint32_t)sg.part * kTabSeg, s1 = min(a.hub_occn[j], s0 + kTabSeg);
         for (uint32_t i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
-            tk[i] = kNone;
-            tv[i] = 0;
+            const uint32_t slot = occ[i];
+            tk[slot] = kNone;
+            tv[slot] = 0;
+        }
+        __syncthreads();
+        // The hub's last clearing CTA empties its occupied list (every CTA has
+        // read the count before it arrives here).
+        if (threadIdx.x == 0) s_last = atomicAdd(&a.hub_clr[j], 1) == a.hub_tcount[j] - 1;
+        __syncthreads();
+        if (s_last && threadIdx.x == 0) {
+            a.hub_occn[j] = 0;
+            a.hub_clr[j] = 0;
         }
     }
 }
@@ -1006,15 +1039,18 @@ __global__ void __launch_bounds__(1024) k_ex_advance(ExactState a) {
     const int par = (int)(a.ctl->round & 1);
     uint8_t* next_prev_act = a.act[par ^ 1];
     for (long long u = E + threadIdx.x; u < nE; u += blockDim.x) next_prev_act[u] = kUnknown;
-    __syncthreads();
     if (threadIdx.x == 0) {
-        const long long rnd = a.ctl->round + 1;
-        a.ctl->cP = P;
-        a.ctl->cX = x;
         a.ctl->c_es0 = a.ctl->es0;
         a.ctl->c_es1 = a.ctl->es1;
         a.ctl->c_ts0 = a.ctl->ts0;
         a.ctl->c_ts1 = a.ctl->ts1;
+    }
+    __syncthreads();
+    window_ranges(a, nP, nE);
+    if (threadIdx.x == 0) {
+        const long long rnd = a.ctl->round + 1;
+        a.ctl->cP = P;
+        a.ctl->cX = x;
         a.ctl->evals = a.ctl->evals + (E - P);
         a.ctl->P = nP;
         a.ctl->E = nE;
@@ -1036,6 +1072,7 @@ __global__ void __launch_bounds__(1024) k_ex_init_iter(ExactState a) {
     const long long n = a.ctl->n, B = a.ctl->B;
     const long long E = min(n, B);
     for (long long u = threadIdx.x; u < E; u += blockDim.x) a.act[0][u] = kUnknown;
+    window_ranges(a, 0, E);
     __syncthreads();
     if (threadIdx.x == 0) {
         a.ctl->P = 0;
@@ -1141,7 +1178,7 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
             eseg.push_back({(int32_t)j, k});
             eseg_v.push_back(ctx.hubs_h[j]);
         }
-        const int nt = (int)ceil_div(cap, kTabSeg);
+        const int nt = (int)std::max<int64_t>(1, ceil_div(hdeg[j], kTabSeg));   // occupied slots <= degree
         tfirst[j] = (int32_t)tseg.size();
         tcount[j] = nt;
         for (int k = 0; k < nt; ++k) {
@@ -1160,8 +1197,11 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     DevBuf<int32_t> hub_any(nh > 0 ? nh : 1, s), hub_done(nh > 0 ? nh : 1, s);
     GB_CUDA(cudaMemsetAsync(hub_any, 0, (nh > 0 ? nh : 1) * sizeof(int32_t), s));
     GB_CUDA(cudaMemsetAsync(hub_done, 0, (nh > 0 ? nh : 1) * sizeof(int32_t), s));
-    DevBuf<uint32_t> hub_kud(nh > 0 ? nh : 1, s);
-    DevBuf<double> hub_sd(nh > 0 ? nh : 1, s);
+    DevBuf<uint32_t> hub_kud(nh > 0 ? nh : 1, s), hub_occn(nh > 0 ? nh : 1, s);
+    DevBuf<int32_t> hub_clr(nh > 0 ? nh : 1, s);
+    DevBuf<uint32_t> hub_occ(pool > 0 ? pool : 1, s);
+    GB_CUDA(cudaMemsetAsync(hub_occn, 0, (nh > 0 ? nh : 1) * sizeof(uint32_t), s));
+    GB_CUDA(cudaMemsetAsync(hub_clr, 0, (nh > 0 ? nh : 1) * sizeof(int32_t), s));
     GB_CUDA(cudaMemsetAsync(hub_kud, 0, (nh > 0 ? nh : 1) * sizeof(uint32_t), s));
     DevBuf<double> part_d(tseg.empty() ? 1 : tseg.size(), s);
     DevBuf<uint32_t> part_c(tseg.empty() ? 1 : tseg.size(), s);
@@ -1245,7 +1285,9 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     a.tvals = tvals.get();
     a.hub_any = hub_any.get();
     a.hub_kud = hub_kud.get();
-    a.hub_sd = hub_sd.get();
+    a.hub_occ = hub_occ.get();
+    a.hub_occn = hub_occn.get();
+    a.hub_clr = hub_clr.get();
     a.hub_done = hub_done.get();
     a.part_d = part_d.get();
     a.part_c = part_c.get();
@@ -1271,26 +1313,28 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     const int hub_grid = kNumSMs * 4;
     const int commit_grid = (int)std::max<int64_t>(1, ceil_div(B, kT));
     const int commit_b_grid = (int)std::max<int64_t>(1, ceil_div(B * 32, kT));
-    const int per_round = 7 + (n_mid ? 1 : 0) + (nh ? 3 : 0);
+    const int per_round = 7 + (n_mid ? 1 : 0) + (nh ? 3 : 0);   // table = 3 kernels
     const int commit_a_grid = std::max(commit_grid, nh ? hub_grid : 0);
     // Side streams and events for the fork/join shape of a captured round:
     struct Fork {
-        cudaStream_t s1 = nullptr, s2 = nullptr;
-        cudaEvent_t ev[7] = {};
+        cudaStream_t s1 = nullptr, s2 = nullptr, s3 = nullptr;
+        cudaEvent_t ev[8] = {};
         ~Fork() {
             for (cudaEvent_t e : ev)
                 if (e) cudaEventDestroy(e);
             if (s1) cudaStreamDestroy(s1);
             if (s2) cudaStreamDestroy(s2);
+            if (s3) cudaStreamDestroy(s3);
         }
     } fk;
-    // One round: decide the window, advance, then build the next window's
-    // event table while this window commits.  Forked shape (graph capture):
-    //   { eval_small | eval_mid | hub_accum -> hub_select } -> advance
-    //   -> { table(next) | commit_a -> { commit_b | commit_hub } }
-    // The round before the first needs the first window's table only.
+    // One round: decide the window, advance, then prepare the next window
+    // while this one commits.  Forked shape (graph capture):
+    //   { eval_small | eval_mid | hub_select } -> advance
+    //   -> { table(next) | commit_a -> { commit_b | commit_hub | hub_accum(next) } }
+    // hub_accum needs the committed memberships but no event table; the
+    // round before the first needs the first window's table and accumulation.
     auto enqueue_round = [&](cudaStream_t st, bool fork) {
-        cudaStream_t sm = fork ? fk.s1 : st, sh = fork ? fk.s2 : st;
+        cudaStream_t sm = fork ? fk.s1 : st, sh = fork ? fk.s2 : st, sa = fork ? fk.s3 : st;
         if (fork) {
             GB_CUDA(cudaEventRecord(fk.ev[0], st));
             GB_CUDA(cudaStreamWaitEvent(sm, fk.ev[0], 0));
@@ -1298,10 +1342,7 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
         }
         k_ex_eval_small<<<small_grid, kSmallWarpsPerBlock * 32, 0, st>>>(a);
         if (n_mid) k_ex_eval_mid<<<mid_grid, kMidWarpsPerBlock * 32, mid_smem, sm>>>(a);
-        if (nh) {
-            k_ex_hub_accum<<<hub_grid, kHubThreads2, 0, sh>>>(a);
-            k_ex_hub_select<<<select_grid, kHubThreads2, 0, sh>>>(a);
-        }
+        if (nh) k_ex_hub_select<<<select_grid, kHubThreads2, 0, sh>>>(a);
         if (fork) {
             GB_CUDA(cudaEventRecord(fk.ev[1], sm));
             GB_CUDA(cudaEventRecord(fk.ev[2], sh));
@@ -1318,16 +1359,27 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
         if (fork) {
             GB_CUDA(cudaEventRecord(fk.ev[4], st));
             GB_CUDA(cudaStreamWaitEvent(sh, fk.ev[4], 0));
+            GB_CUDA(cudaStreamWaitEvent(sa, fk.ev[4], 0));
         }
         k_ex_commit_b<<<commit_b_grid, kT, 0, st>>>(a);
-        if (nh) k_ex_commit_hub<<<hub_grid, kHubThreads2, 0, sh>>>(a);
+        if (nh) {
+            k_ex_commit_hub<<<hub_grid, kHubThreads2, 0, sh>>>(a);
+            k_ex_hub_accum<<<hub_grid, kHubThreads2, 0, sa>>>(a);
+        }
         if (fork) {
             GB_CUDA(cudaEventRecord(fk.ev[5], sm));
             GB_CUDA(cudaEventRecord(fk.ev[6], sh));
+            GB_CUDA(cudaEventRecord(fk.ev[7], sa));
             GB_CUDA(cudaStreamWaitEvent(st, fk.ev[5], 0));
             GB_CUDA(cudaStreamWaitEvent(st, fk.ev[6], 0));
+            GB_CUDA(cudaStreamWaitEvent(st, fk.ev[7], 0));
         }
         GB_LAUNCH_CHECK();
+    };
+    auto enqueue_first = [&](cudaStream_t st) {
+        k_ex_init_iter<<<1, 1024, 0, st>>>(a);
+        enqueue_table(st);
+        if (nh) k_ex_hub_accum<<<hub_grid, kHubThreads2, 0, st>>>(a);
     };
 
     // One local-moving iteration as one graph: the init kernel, then a
@@ -1354,8 +1406,7 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
         a.use_cond = 1;
         // init -> first window's table (captured) -> while(rounds)
         GB_CUDA(cudaStreamBeginCaptureToGraph(gg.cs, gg.g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-        k_ex_init_iter<<<1, 1024, 0, gg.cs>>>(a);
-        enqueue_table(gg.cs);
+        enqueue_first(gg.cs);
         GB_LAUNCH_CHECK();
         GB_CUDA(cudaStreamEndCapture(gg.cs, &gg.g));
         // The captured chain's last node (the one no other node depends on).
@@ -1382,6 +1433,7 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
         cudaGraph_t body = cp.conditional.phGraph_out[0];
         GB_CUDA(cudaStreamCreateWithFlags(&fk.s1, cudaStreamNonBlocking));
         GB_CUDA(cudaStreamCreateWithFlags(&fk.s2, cudaStreamNonBlocking));
+        GB_CUDA(cudaStreamCreateWithFlags(&fk.s3, cudaStreamNonBlocking));
         for (cudaEvent_t& e : fk.ev) GB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         GB_CUDA(cudaStreamBeginCaptureToGraph(gg.cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
         enqueue_round(gg.cs, true);
@@ -1398,8 +1450,7 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
             GB_CUDA(cudaMemcpyAsync(hctl, ctl.get(), sizeof(Ctl), cudaMemcpyDeviceToHost, s));
             GB_CUDA(cudaStreamSynchronize(s));
         } else {
-            k_ex_init_iter<<<1, 1024, 0, s>>>(a);
-            enqueue_table(s);
+            enqueue_first(s);
             GB_LAUNCH_CHECK();
             while (true) {
                 for (int b = 0; b < kBatch; ++b) enqueue_round(s, false);
@@ -1410,7 +1461,7 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
         }
         if (hctl->error)
             throw Error(GBGPU_E_CUDA, "serial-order local moving: round loop stopped without progress");
-        nl += 4 + hctl->round * per_round;
+        nl += 4 + (nh ? 1 : 0) + hctl->round * per_round;
         rounds += hctl->round;
         evals += hctl->evals;
         ++iterations;
