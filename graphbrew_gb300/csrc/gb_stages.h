@@ -38,7 +38,7 @@ struct LeidenParams {
     int super_move_batch = 1;
     bool deterministic = false;
     int chunk_vertices = 2048;      // asynchronous engine: vertices per launch
-    int64_t super_single_cta_max_edges = 1 << 18;  // super-move in one persistent CTA up to this size
+    int64_t super_single_cta_max_edges = 1 << 24;  // super-move in one thread-block cluster up to this size
     int64_t exact_max_vertices = INT64_MAX; // cd_parallel uses the serial-order engine up to this size
     int64_t exact_window = 32768;           // speculative window of the serial-order engine
 };

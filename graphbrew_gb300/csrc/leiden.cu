@@ -415,36 +415,42 @@ __device__ __forceinline__ void super_commit(const SmArgs& a, uint32_t c, int* m
     atomicAdd(moves, 1);
 }
 
-// Whole super-move in one CTA: batches in order, propose / barrier / commit /
-// barrier; iterations stop early when a full iteration moves nothing.
+// Whole super-move in one thread-block cluster: batches in order, propose /
+// cluster barrier / commit / cluster barrier; iterations stop early when a
+// full iteration moves nothing.  The cluster barrier is the hardware
+// barrier.cluster (release / acquire), so the CTAs' global writes of one
+// phase are visible to the next.
+constexpr int kSmCluster = 8;
+
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
+    asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+
 __global__ void __launch_bounds__(1024)
-k_super_move_single(SmArgs a, int max_iter, int* iters_out, long long* moves_out) {
+k_super_move_cluster(SmArgs a, int max_iter, int* iters_out, long long* moves_out, int* gmoves) {
     extern __shared__ uint32_t sm_smem[];  // 32 warps x (keys, vals) x kSmSmall
-    __shared__ int moves;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int64_t gw = (int64_t)blockIdx.x * nw + w, gnw = (int64_t)gridDim.x * nw;
+    const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, gnt = (int64_t)gridDim.x * blockDim.x;
+    uint32_t* tk = sm_smem + (size_t)w * 2 * kSmSmall;
     long long total_moves = 0;
     int it = 0;
     for (; it < max_iter; ++it) {
-        if (threadIdx.x == 0) moves = 0;
-        __syncthreads();
         for (int64_t bt = 0; bt < a.nbatch; ++bt) {
             const int64_t lo = a.bstart[bt], hi = a.bstart[bt + 1];
             if (lo == hi) continue;
-            uint32_t* tk = sm_smem + (size_t)w * 2 * kSmSmall;
-            for (int64_t i = lo + w; i < hi; i += nw)
-                super_propose(a, a.active[i], tk, tk + kSmSmall, a.gkeys + (int64_t)w * a.gcap,
-                              a.gvals + (int64_t)w * a.gcap);
-            __syncthreads();
-            for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) super_commit(a, a.active[i], &moves);
-            __syncthreads();
+            for (int64_t i = lo + gw; i < hi; i += gnw)
+                super_propose(a, a.active[i], tk, tk + kSmSmall, a.gkeys + gw * a.gcap, a.gvals + gw * a.gcap);
+            cluster_sync_all();
+            for (int64_t i = lo + gt; i < hi; i += gnt) super_commit(a, a.active[i], &gmoves[it]);
+            cluster_sync_all();
         }
-        const int m = moves;
+        const int m = atomicAdd(&gmoves[it], 0);
         total_moves += m;
-        __syncthreads();
         if (m == 0) { ++it; break; }
     }
-    (void)lane;
-    if (threadIdx.x == 0) {
+    if (gt == 0) {
         *iters_out = it;
         *moves_out = total_moves;
     }
@@ -613,7 +619,7 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
     const int lm_smem = kLmWarpsPerBlock * 2 * kWarpHash * (int)sizeof(uint32_t);
     GB_CUDA(cudaFuncSetAttribute(k_local_move_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, lm_smem));
     const int sm_smem = 32 * 2 * kSmSmall * (int)sizeof(uint32_t);
-    GB_CUDA(cudaFuncSetAttribute(k_super_move_single, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_smem));
+    GB_CUDA(cudaFuncSetAttribute(k_super_move_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_smem));
 
     LmArgs la{g.row_ptr, g.col, vcom, ctot, vaff, M, R, dacc, macc};
     const int64_t chunk = p.chunk_vertices > 0 ? p.chunk_vertices : n;
@@ -780,18 +786,34 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
             const bool single = nuniq <= p.super_single_cta_max_edges;
             // Per-warp global tables for super-nodes above kSmSmall / 2 neighbours,
             // capped at 512 MB in total.
-            int64_t nwarps_total = single ? 32 : (int64_t)kNumSMs * 4 * 8;
+            int64_t nwarps_total = single ? (int64_t)kSmCluster * 32 : (int64_t)kNumSMs * 4 * 8;
             if (!single && gcap > kSmSmall)
                 nwarps_total = std::max<int64_t>(8, std::min<int64_t>(nwarps_total, ((int64_t)1 << 26) / gcap) / 8 * 8);
             DevBuf<uint32_t> gk(gcap > kSmSmall ? nwarps_total * gcap : 1, s);
             DevBuf<uint32_t> gv(gcap > kSmSmall ? nwarps_total * gcap : 1, s);
             SmArgs sa{soff, snbr, sw, sweight, scomm, sctot, active, bstart, nbatch, proposed, pdelta, M, R,
                       gk, gv, gcap > kSmSmall ? gcap : 0};
-            DevBuf<int> iters_d(1, s);
+            DevBuf<int> iters_d(1, s), gmoves(super_max_iter, s);
             DevBuf<long long> moves_d(1, s);
             launches += 2;
             if (single) {
-                k_super_move_single<<<1, 1024, sm_smem, s>>>(sa, super_max_iter, iters_d, moves_d);
+                GB_CUDA(cudaMemsetAsync(gmoves, 0, super_max_iter * sizeof(int), s));
+                cudaLaunchConfig_t cfg = {};
+                cfg.gridDim = dim3(kSmCluster);
+                cfg.blockDim = dim3(1024);
+                cfg.dynamicSmemBytes = sm_smem;
+                cfg.stream = s;
+                cudaLaunchAttribute attr[1];
+                attr[0].id = cudaLaunchAttributeClusterDimension;
+                attr[0].val.clusterDim.x = kSmCluster;
+                attr[0].val.clusterDim.y = 1;
+                attr[0].val.clusterDim.z = 1;
+                cfg.attrs = attr;
+                cfg.numAttrs = 1;
+                int* gm = gmoves.get();
+                int* itp = iters_d.get();
+                long long* mvp = moves_d.get();
+                GB_CUDA(cudaLaunchKernelEx(&cfg, k_super_move_cluster, sa, super_max_iter, itp, mvp, gm));
                 GB_LAUNCH_CHECK();
                 ++launches;
                 super_iters += read_dev(iters_d.get(), s);

@@ -44,11 +44,11 @@ namespace {
 
 constexpr int kT = 256;
 constexpr uint8_t kUnknown = 2;
-constexpr int kWindowMax = 32768;             // window vertices (events <= 2 x window)
-constexpr int kEventsMax = 2 * kWindowMax;    // event index = 2 x window offset (+1): 16 bits
-constexpr int kSlotBits = 17;
+constexpr int kWindowMax = 65536;             // window vertices (events <= 2 x window)
+constexpr int kEventsMax = 2 * kWindowMax;    // event index = 2 x window offset (+1)
+constexpr int kSlotBits = 18;
 constexpr int kTableSlots = 1 << kSlotBits;   // hash slots, >= 2 x events
-constexpr int kCoarseBits = 9;                // event grouping: 512 coarse buckets of slots
+constexpr int kCoarseBits = 10;               // event grouping: 1024 coarse buckets of slots
 constexpr int kCoarse = 1 << kCoarseBits;
 constexpr int kFineBits = kSlotBits - kCoarseBits;
 constexpr int kTbThreads = 1024;              // table insert / group: one window vertex per thread
@@ -56,6 +56,16 @@ constexpr int kTbChunks = kWindowMax / kTbThreads;
 constexpr int kTbFinishThreads = 1024;        // table finish: one CTA per coarse bucket
 constexpr uint32_t kPadSlot = 0xFFFFFFFFu;
 static_assert(kTableSlots >= 2 * kEventsMax, "hash load factor <= 1/2");
+static_assert(kCoarse <= kTbThreads, "one coarse bucket per grouping thread");
+// Slots with many events ("hot": a community that many window vertices join
+// or leave) get a time-bucket index: bidx[b] = first event at time >= P + 16 b,
+// so a lookup searches at most 16 events instead of the whole slot.
+constexpr int kHotMin = 128;                  // events that make a slot hot
+constexpr int kBucketV = 16;                  // window vertices per time bucket
+constexpr int kHotStride = kWindowMax / kBucketV + 1;
+constexpr int kHotMax = 2 * kEventsMax / kHotMin;
+constexpr int kEndBits = 18;                  // SlotMeta.endh: end | (hot id + 1) << kEndBits
+static_assert(kEventsMax < (1 << kEndBits), "event positions fit the end field");
 constexpr int kHubThreads2 = 256;             // threads of the hub kernels
 constexpr int kHubSeg = 4 * kHubThreads2;     // edges per hub-accumulation CTA (4 per thread)
 constexpr int kTabSeg = 4 * kHubThreads2;     // table slots per hub-selection CTA (4 per thread)
@@ -75,12 +85,13 @@ struct Ctl {
     long long max_rounds;     // bound on rounds per iteration (n + 1 always suffices)
     long long error;          // nonzero: the round loop stopped without finishing
     unsigned long long tag;   // generation of the event table (slots of older tags are empty)
+    unsigned int nhot;        // hot slots of the current table
 };
 
 struct __align__(16) SlotMeta {
     unsigned long long tkey;  // table generation << 32 | community id
     int32_t start;            // first sorted event of the slot
-    int32_t end;              // one past its last event
+    uint32_t endh;            // one past its last event | (hot index + 1) << kEndBits
 };
 
 struct HubSeg {
@@ -112,6 +123,7 @@ struct ExactState {
     int32_t* tb_bstart;   // coarse bucket starts (kCoarse + 1)
     unsigned long long* ev1;  // events grouped by coarse bucket: slot << 32 | event index
     unsigned long long* ev2;  // events sorted by slot
+    int32_t* hot_bidx;        // kHotMax x kHotStride time-bucket starts of hot slots
     // hubs
     const uint32_t* hub_v;        // hub vertex ids (ascending)
     const int64_t* hub_toff;      // table offset
@@ -151,9 +163,10 @@ __device__ __forceinline__ uint32_t slot_hash(uint32_t c) {
 // searches advance in lockstep so their loads are in flight together.
 // valid[k] = false entries return 0.
 template <int K>
-__device__ __forceinline__ void sigma_at_k(const ExactState& a, unsigned long long tag, const uint32_t (&c)[K],
-                                           const bool (&valid)[K], uint32_t u, long long (&out)[K]) {
-    uint32_t h[K];
+__device__ __forceinline__ void sigma_at_k(const ExactState& a, unsigned long long tag, long long P,
+                                           const uint32_t (&c)[K], const bool (&valid)[K], uint32_t u,
+                                           long long (&out)[K]) {
+    uint32_t h[K], hot[K];
     int lo[K], l[K], r[K];
     bool pending[K];
 #pragma unroll
@@ -162,6 +175,7 @@ __device__ __forceinline__ void sigma_at_k(const ExactState& a, unsigned long lo
         h[k] = slot_hash(c[k]) & (kTableSlots - 1);
         pending[k] = valid[k];
         lo[k] = l[k] = r[k] = 0;
+        hot[k] = 0;
     }
     bool any = true;
     while (any) {
@@ -175,7 +189,8 @@ __device__ __forceinline__ void sigma_at_k(const ExactState& a, unsigned long lo
             if (!pending[k]) continue;
             if (sm[k].tkey == (tag << 32 | c[k])) {
                 lo[k] = l[k] = sm[k].start;
-                r[k] = sm[k].end;
+                r[k] = (int)(sm[k].endh & ((1u << kEndBits) - 1u));
+                hot[k] = sm[k].endh >> kEndBits;
                 pending[k] = false;
             } else if ((sm[k].tkey >> 32) != tag) {   // a slot of an older table: empty
                 pending[k] = false;
@@ -184,6 +199,21 @@ __device__ __forceinline__ void sigma_at_k(const ExactState& a, unsigned long lo
                 any = true;
             }
         }
+    }
+    // Hot slots: narrow [l, r) to u's time bucket.
+    {
+        int bl[K], br[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            if (hot[k]) {
+                const int32_t* bx = a.hot_bidx + (size_t)(hot[k] - 1) * kHotStride + (int)((u - P) / kBucketV);
+                bl[k] = bx[0];
+                br[k] = bx[1];
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            if (hot[k]) { l[k] = bl[k]; r[k] = br[k]; }
     }
     any = true;
     while (any) {
@@ -357,7 +387,10 @@ __global__ void __launch_bounds__(kTbThreads) k_tb_insert(ExactState a) {
     const Round r = round_view(a);
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     for (int b = tid; b < kCoarse; b += blockDim.x) hist[b] = 0;
-    if (blockIdx.x == 0 && tid == 0) a.ctl->first_change = kNoChange;
+    if (blockIdx.x == 0 && tid == 0) {
+        a.ctl->first_change = kNoChange;
+        a.ctl->nhot = 0;
+    }
     (void)lane;
     (void)w;
     __syncthreads();
@@ -406,7 +439,7 @@ __global__ void __launch_bounds__(kTbThreads) k_tb_group(ExactState a) {
             if (c < (int)blockIdx.x) pre += v;
         }
     }
-    // Exclusive scan of the totals (kCoarse = 512 <= threads).
+    // Exclusive scan of the totals (kCoarse <= threads).
     int incl = tot;
     for (int o = 1; o < 32; o <<= 1) {
         const int y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
@@ -582,7 +615,34 @@ __global__ void __launch_bounds__(kTbFinishThreads) k_tb_finish(ExactState a) {
         a.stime[k] = (uint32_t)(P + (e >> 1));
         a.epre[k] = run;
         if (head) a.slots[sl].start = k;
-        if (k == be - 1 || (uint32_t)(a.ev2[k + 1] >> 32) != sl) a.slots[sl].end = k + 1;
+        if (k == be - 1 || (uint32_t)(a.ev2[k + 1] >> 32) != sl) a.slots[sl].endh = (uint32_t)(k + 1);
+    }
+    __syncthreads();
+    // Hot slots of this bucket: an index each, then their time-bucket starts.
+    const int nb = (int)((a.ctl->E - P + kBucketV - 1) / kBucketV);
+    for (int k = b0; k < b1; ++k) {
+        const uint32_t sl = (uint32_t)(a.ev2[k] >> 32);
+        if (!(k == bs || (uint32_t)(a.ev2[k - 1] >> 32) != sl)) continue;
+        const int32_t st = a.slots[sl].start;
+        const uint32_t en = a.slots[sl].endh;
+        if ((int)en - st < kHotMin) continue;
+        const unsigned id = atomicAdd(&a.ctl->nhot, 1u);
+        if (id < (unsigned)kHotMax) a.slots[sl].endh = en | ((id + 1) << kEndBits);
+    }
+    __syncthreads();
+    for (int k = b0; k < b1; ++k) {
+        const unsigned long long key = a.ev2[k];
+        const uint32_t sl = (uint32_t)(key >> 32), e = (uint32_t)key;
+        const uint32_t eh = a.slots[sl].endh;
+        const uint32_t hid = eh >> kEndBits;
+        if (!hid) continue;
+        const int end = (int)(eh & ((1u << kEndBits) - 1u));
+        int32_t* bx = a.hot_bidx + (size_t)(hid - 1) * kHotStride;
+        const int bk = (int)(e >> 1) / kBucketV;
+        const int bprev = k == a.slots[sl].start ? -1 : (int)((uint32_t)a.ev2[k - 1] >> 1) / kBucketV;
+        for (int b = bprev + 1; b <= bk; ++b) bx[b] = k;
+        if (k == end - 1)
+            for (int b = bk + 1; b <= nb; ++b) bx[b] = end;
     }
 }
 
@@ -627,7 +687,7 @@ __device__ __forceinline__ void eval_vertex(const ExactState& a, const Round& r,
             const uint32_t cc[2] = {c, d};
             const bool vv[2] = {true, true};
             long long sg[2];
-            sigma_at_k<2>(a, r.tag, cc, vv, (uint32_t)u, sg);
+            sigma_at_k<2>(a, r.tag, r.P, cc, vv, (uint32_t)u, sg);
             const double dl = delta_q((double)__popc(peers), kud, ku, (double)sg[0], (double)sg[1], a.M, a.R);
             if (dl > 0.0) { best_d = dl; best_c = c; }
         }
@@ -689,7 +749,7 @@ __device__ __forceinline__ void eval_vertex(const ExactState& a, const Round& r,
             }
             cc[4] = d;
             vv[4] = i0 == 0;
-            sigma_at_k<5>(a, r.tag, cc, vv, (uint32_t)u, sg);
+            sigma_at_k<5>(a, r.tag, r.P, cc, vv, (uint32_t)u, sg);
             if (i0 == 0) sd = (double)sg[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
@@ -708,15 +768,83 @@ __device__ __forceinline__ void eval_vertex(const ExactState& a, const Round& r,
     }
 }
 
-// Small rows: one warp per window vertex, no shared memory (full occupancy).
+// Small rows, no shared memory.  A warp takes four consecutive window
+// vertices: rows of degree <= 8 are evaluated together by four 8-lane groups
+// (one neighbour per lane), rows of degree 9..32 then one at a time by the
+// whole warp.
+constexpr int kTinyDeg = 8;
+
 __global__ void __launch_bounds__(kSmallWarpsPerBlock * 32) k_ex_eval_small(ExactState a) {
     if (a.ctl->P >= a.ctl->n) return;
     const Round r = round_view(a);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int g = lane >> 3, j = lane & 7;
+    const unsigned gmask = 0xFFu << (g * 8);
     const int64_t nw = (int64_t)gridDim.x * kSmallWarpsPerBlock;
-    for (int64_t u = r.P + (int64_t)blockIdx.x * kSmallWarpsPerBlock + w; u < r.E; u += nw) {
-        if (a.rp[u + 1] - a.rp[u] > kSmallMaxDeg) continue;
-        eval_vertex<false>(a, r, u, lane, nullptr, nullptr);
+    for (int64_t u0 = r.P + 4 * ((int64_t)blockIdx.x * kSmallWarpsPerBlock + w); u0 < r.E; u0 += 4 * nw) {
+        const int64_t u = u0 + g;
+        const bool inwin = u < r.E;
+        int64_t rb = 0;
+        int deg = 0;
+        if (inwin) {
+            rb = a.rp[u];
+            deg = (int)(a.rp[u + 1] - rb);
+        }
+        const bool tiny = inwin && deg <= kTinyDeg;
+        // One load round for the row, its vertex state and its neighbours' states.
+        int32_t v = -1;
+        uint32_t d = kNone;
+        bool aff = false;
+        if (tiny) {
+            if (j < deg) v = a.col[rb + j];
+            d = a.vcom[u];
+            aff = a.vaff[u] != 0;
+        }
+        bool pm = false;
+        uint32_t cv = kNone;
+        if (v >= 0) {
+            const uint32_t vc = a.vcom[v];
+            cv = vc;
+            if (v >= r.P && v < u) {
+                pm = r.pact[v] == 1 && r.pbest[v] != vc;
+                if (pm) cv = r.pbest[v];
+            }
+            if (v == (int32_t)u) cv = kNone;   // self loops never count
+        }
+        const unsigned pmb = __ballot_sync(0xFFFFFFFFu, pm);
+        const bool act = tiny && (aff || (pmb & gmask) != 0);
+        const uint32_t c = act ? cv : kNone;
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, ((unsigned long long)g << 32) | c);
+        const unsigned eqd = __ballot_sync(0xFFFFFFFFu, act && c != kNone && c == d) & gmask;
+        double best_d = 0.0;
+        uint32_t best_c = kNone;
+        if (act && c != kNone && c != d && lane == __ffs(peers) - 1) {
+            const uint32_t cc[2] = {c, d};
+            const bool vv[2] = {true, true};
+            long long sg[2];
+            sigma_at_k<2>(a, r.tag, r.P, cc, vv, (uint32_t)u, sg);
+            const double dl = delta_q((double)__popc(peers), (double)__popc(eqd), (double)deg, (double)sg[0],
+                                      (double)sg[1], a.M, a.R);
+            if (dl > 0.0) { best_d = dl; best_c = c; }
+        }
+#pragma unroll
+        for (int o = 4; o > 0; o >>= 1) {   // argmax inside each 8-lane group
+            const double od = __shfl_xor_sync(0xFFFFFFFFu, best_d, o);
+            const uint32_t oc = __shfl_xor_sync(0xFFFFFFFFu, best_c, o);
+            if (better(od, oc, best_d, best_c)) { best_d = od; best_c = oc; }
+        }
+        if (tiny && j == 0) {
+            if (!act) record(a, r, u, 0, d, 0.0);
+            else if (best_d > 0.0 && best_c != kNone && best_c != d) record(a, r, u, 1, best_c, best_d);
+            else record(a, r, u, 1, d, 0.0);
+        }
+        // Rows of degree 9..32: the whole warp, one row at a time.
+#pragma unroll 1
+        for (int k = 0; k < 4; ++k) {
+            const int dk = __shfl_sync(0xFFFFFFFFu, deg, k * 8);
+            const int ik = __shfl_sync(0xFFFFFFFFu, (int)inwin, k * 8);
+            if (ik && dk > kTinyDeg && dk <= kSmallMaxDeg) eval_vertex<false>(a, r, u0 + k, lane, nullptr, nullptr);
+        }
     }
 }
 
@@ -849,7 +977,7 @@ __global__ void __launch_bounds__(kHubThreads2) k_ex_hub_select(ExactState a) {
             }
             cc[4] = d;
             vv[4] = true;
-            sigma_at_k<5>(a, r.tag, cc, vv, h, sgm);
+            sigma_at_k<5>(a, r.tag, r.P, cc, vv, h, sgm);
             const double sd = (double)sgm[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
@@ -1234,6 +1362,7 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     DevBuf<long long> epre(kEventsMax, s);
     DevBuf<int32_t> wdeg(kWindowMax, s), tb_hist(kCoarse * kTbChunks, s), tb_bstart(kCoarse + 1, s);
     DevBuf<unsigned long long> ev1(kEventsMax, s), ev2(kEventsMax, s);
+    DevBuf<int32_t> hot_bidx((size_t)kHotMax * kHotStride, s);
     DevBuf<Ctl> ctl(1, s);
     Ctl* hctl = nullptr;
     GB_CUDA(cudaMallocHost(&hctl, sizeof(Ctl)));
@@ -1268,6 +1397,7 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     a.tb_bstart = tb_bstart.get();
     a.ev1 = ev1.get();
     a.ev2 = ev2.get();
+    a.hot_bidx = hot_bidx.get();
     a.stime = stime.get();
     a.epre = epre.get();
     a.hub_v = ctx.hubs;
@@ -1307,10 +1437,20 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     };
     const int mid_smem = kMidWarpsPerBlock * 2 * kWarpHash * (int)sizeof(uint32_t);
     GB_CUDA(cudaFuncSetAttribute(k_ex_eval_mid, cudaFuncAttributeMaxDynamicSharedMemorySize, mid_smem));
-    const int small_grid = (int)std::max<int64_t>(1, ceil_div(B, kSmallWarpsPerBlock));
-    const int mid_grid = kNumSMs * 4;       // resident blocks at ~105 registers per thread
-    const int select_grid = kNumSMs * 3;    // resident blocks at 79 registers per thread
-    const int hub_grid = kNumSMs * 4;
+    const int small_grid = (int)std::max<int64_t>(1, ceil_div(B, 4 * kSmallWarpsPerBlock));
+    // Grid-stride kernels: one resident wave (blocks per SM from the occupancy
+    // of the compiled kernel x the SM count).
+    auto resident = [&](const void* fn, int threads, int smem) {
+        int per_sm = 0;
+        GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem));
+        int dev = 0, sms = kNumSMs;
+        GB_CUDA(cudaGetDevice(&dev));
+        GB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        return std::max(1, per_sm) * sms;
+    };
+    const int mid_grid = resident((const void*)k_ex_eval_mid, kMidWarpsPerBlock * 32, mid_smem);
+    const int select_grid = resident((const void*)k_ex_hub_select, kHubThreads2, 0);
+    const int hub_grid = resident((const void*)k_ex_hub_accum, kHubThreads2, 0);
     const int commit_grid = (int)std::max<int64_t>(1, ceil_div(B, kT));
     const int commit_b_grid = (int)std::max<int64_t>(1, ceil_div(B * 32, kT));
     const int per_round = 7 + (n_mid ? 1 : 0) + (nh ? 3 : 0);   // table = 3 kernels

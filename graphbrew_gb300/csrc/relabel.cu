@@ -9,9 +9,9 @@
 // Relabel follows RelabelByMapping's undirected branch (builder.h:1168-1206):
 // new row x = sorted { new_ids[v] : v in N(old(x)) }.  Remap and sort are
 // fused per row; rows are bucketed by length: one thread (<= 16 entries),
-// one warp with a shared-memory bitonic sort (<= 256), one CTA with a
-// shared-memory bitonic sort (<= 16384), and a global segmented radix sort
-// for the few longer rows.
+// one warp with a shared-memory bitonic sort (<= 256), one 256-thread CTA
+// (<= 2048) or one 1024-thread CTA (<= 16384) with a shared-memory bitonic
+// sort, and a global segmented radix sort for the few longer rows.
 #include "gb_common.cuh"
 #include "gb_stages.h"
 
@@ -52,13 +52,15 @@ __global__ void k_new_degrees(const int64_t* __restrict__ rp, const int32_t* __r
 
 constexpr int kThreadRowMax = 16;
 constexpr int kWarpRowMax = 256;
-constexpr int kBlockRowMax = 16384;
+constexpr int kMidRowMax = 2048;      // 256-thread CTA, 8 KB shared memory
+constexpr int kBlockRowMax = 16384;   // 1024-thread CTA, 64 KB shared memory
+constexpr int kRowLists = 4;          // warp, mid-CTA, CTA, huge
 
 __global__ void k_relabel_rows_small(const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
                                      const int32_t* __restrict__ new_ids, const int32_t* __restrict__ inv,
                                      const int64_t* __restrict__ out_rp, int32_t* __restrict__ out_col,
                                      int64_t n, int32_t* __restrict__ lists, int32_t* __restrict__ counts) {
-    // counts[0..2]: warp, block, huge list sizes; lists: 3 x n entries.
+    // counts[0..3]: warp, mid-CTA, CTA, huge list sizes; lists: 4 x n entries.
     for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
         const int32_t u = inv[x];
         const int64_t b = rp[u], d = rp[u + 1] - b;
@@ -73,7 +75,7 @@ __global__ void k_relabel_rows_small(const int64_t* __restrict__ rp, const int32
             const int64_t o = out_rp[x];
             for (int i = 0; i < d; ++i) out_col[o + i] = a[i];
         } else {
-            const int which = d <= kWarpRowMax ? 0 : (d <= kBlockRowMax ? 1 : 2);
+            const int which = d <= kWarpRowMax ? 0 : (d <= kMidRowMax ? 1 : (d <= kBlockRowMax ? 2 : 3));
             const int32_t slot = atomicAdd(&counts[which], 1);
             lists[(int64_t)which * n + slot] = (int32_t)x;
         }
@@ -117,10 +119,14 @@ __global__ void k_relabel_rows_warp(const int64_t* __restrict__ rp, const int32_
     }
 }
 
-__global__ void k_relabel_rows_block(const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
-                                     const int32_t* __restrict__ new_ids, const int32_t* __restrict__ inv,
-                                     const int64_t* __restrict__ out_rp, int32_t* __restrict__ out_col,
-                                     const int32_t* __restrict__ list, const int32_t* __restrict__ count) {
+// One CTA per row: remap into shared memory, bitonic sort, write back.
+// kThreads = 256 for rows up to kMidRowMax, 1024 up to kBlockRowMax.
+template <int kThreads>
+__global__ void __launch_bounds__(kThreads)
+k_relabel_rows_block(const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
+                     const int32_t* __restrict__ new_ids, const int32_t* __restrict__ inv,
+                     const int64_t* __restrict__ out_rp, int32_t* __restrict__ out_col,
+                     const int32_t* __restrict__ list, const int32_t* __restrict__ count) {
     extern __shared__ int32_t s[];
     const int32_t total = *count;
     for (int64_t r = blockIdx.x; r < total; r += gridDim.x) {
@@ -128,7 +134,7 @@ __global__ void k_relabel_rows_block(const int64_t* __restrict__ rp, const int32
         const int32_t u = inv[x];
         const int64_t b = rp[u];
         const int d = (int)(rp[u + 1] - b);
-        int p = 512;
+        int p = 2 * kThreads;
         while (p < d) p <<= 1;
         for (int i = threadIdx.x; i < p; i += blockDim.x) s[i] = i < d ? new_ids[col[b + i]] : kIntMax;
         __syncthreads();
@@ -267,30 +273,31 @@ void relabel_csr_device(const DeviceCSR& g, const int32_t* new_ids, const int32_
         GB_LAUNCH_CHECK();
         nl += 3;
     }
-    DevBuf<int32_t> lists(3 * n, s);
-    DevBuf<int32_t> counts(3, s);
-    GB_CUDA(cudaMemsetAsync(counts, 0, 3 * sizeof(int32_t), s));
+    DevBuf<int32_t> lists(kRowLists * n, s);
+    DevBuf<int32_t> counts(kRowLists, s);
+    GB_CUDA(cudaMemsetAsync(counts, 0, kRowLists * sizeof(int32_t), s));
     k_relabel_rows_small<<<grid_for(n, 256), 256, 0, s>>>(g.row_ptr, g.col, new_ids, inv, out_rp, out_col, n,
                                                           lists, counts);
     GB_LAUNCH_CHECK();
     k_relabel_rows_warp<<<kNumSMs * 8, 256, 0, s>>>(g.row_ptr, g.col, new_ids, inv, out_rp, out_col, lists.get(),
                                                     counts.get());
     GB_LAUNCH_CHECK();
+    const int mid_smem = kMidRowMax * (int)sizeof(int32_t);
     const int block_smem = kBlockRowMax * (int)sizeof(int32_t);
-    static bool attr_set = false;
-    if (!attr_set) {
-        GB_CUDA(cudaFuncSetAttribute(k_relabel_rows_block, cudaFuncAttributeMaxDynamicSharedMemorySize, block_smem));
-        attr_set = true;
-    }
-    k_relabel_rows_block<<<kNumSMs * 2, 1024, block_smem, s>>>(g.row_ptr, g.col, new_ids, inv, out_rp, out_col,
-                                                               lists.get() + n, counts.get() + 1);
+    GB_CUDA(cudaFuncSetAttribute(k_relabel_rows_block<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 block_smem));
+    k_relabel_rows_block<256><<<kNumSMs * 8, 256, mid_smem, s>>>(g.row_ptr, g.col, new_ids, inv, out_rp, out_col,
+                                                                 lists.get() + n, counts.get() + 1);
     GB_LAUNCH_CHECK();
-    nl += 3;
+    k_relabel_rows_block<1024><<<kNumSMs * 2, 1024, block_smem, s>>>(g.row_ptr, g.col, new_ids, inv, out_rp,
+                                                                     out_col, lists.get() + 2 * n, counts.get() + 2);
+    GB_LAUNCH_CHECK();
+    nl += 4;
     int32_t huge = 0;
-    GB_CUDA(cudaMemcpyAsync(&huge, counts.get() + 2, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    GB_CUDA(cudaMemcpyAsync(&huge, counts.get() + 3, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     GB_CUDA(cudaStreamSynchronize(s));
     if (huge > 0) {
-        const int32_t* hlist = lists.get() + 2 * n;
+        const int32_t* hlist = lists.get() + 3 * n;
         DevBuf<int64_t> hoff(huge + 1, s);
         k_huge_degrees<<<grid_for(huge, 256), 256, 0, s>>>(g.row_ptr, inv, hlist, huge, hoff);
         GB_LAUNCH_CHECK();
