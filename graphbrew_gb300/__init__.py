@@ -57,6 +57,15 @@ class GbgpuConfig(C.Structure):
                 ("gorder_fallback", C.c_int32), ("algorithm", C.c_int32)]
 
 
+class GbgpuGraph(C.Structure):
+    _fields_ = [("row_ptr", C.c_void_p), ("col", C.c_void_p), ("n", C.c_int64), ("nnz", C.c_int64),
+                ("new_ids_out", C.c_void_p)]
+
+
+class GbgpuSchedule(C.Structure):
+    _fields_ = [("streams", C.c_int32), ("order", C.c_int32), ("exact_window", C.c_int64)]
+
+
 class GbgpuStats(C.Structure):
     _fields_ = [("total_ms", C.c_double), ("leiden_ms", C.c_double), ("local_move_ms", C.c_double),
                 ("aggregate_ms", C.c_double), ("compose_ms", C.c_double), ("intra_ms", C.c_double),
@@ -99,6 +108,8 @@ SIGNATURES = {
     "gbgpu_validate_permutation_noalloc": (C.c_int, [_P, _P, C.c_int64, C.POINTER(C.c_int32)]),
     "gbgpu_fingerprint": (C.c_uint64, [_P, C.c_int64]),
     "gbgpu_version": (C.c_char_p, []),
+    "gbgpu_generate_mappings_batched": (C.c_int, [_P, C.POINTER(GbgpuGraph), C.c_int32, C.c_char_p,
+                                                  C.POINTER(GbgpuSchedule), _P, C.POINTER(C.c_double), C.c_uint32]),
     "gbgpu_pagerank": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int64, C.c_int32, C.c_double, _P,
                                  C.POINTER(C.c_int32), C.POINTER(C.c_double), C.c_uint32]),
     "gbgpu_bfs": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int64, C.c_int64, _P, C.POINTER(C.c_double), C.c_uint32]),
@@ -355,6 +366,34 @@ class Context:
         self._check(library().gbgpu_map_and_relabel(self._h, prp, pcl, n, nnz, opts.encode(), ar, pids, porp,
                                                        pocol, C.byref(st), DEVICE_POINTERS if dev else 0))
         return ids, orp, ocol, st.as_dict()
+
+    def generate_mappings_batched(self, graphs, options=DEFAULT_RECIPE, streams=4, order=1, exact_window=0):
+        """Map many graphs (list of (row_ptr, col) torch CUDA tensor pairs)
+        concurrently.  Returns (list of new_ids tensors, list of stats dicts,
+        wall ms)."""
+        import torch
+        count = len(graphs)
+        arr = (GbgpuGraph * max(1, count))()
+        outs, keep = [], []
+        for i, (rp, col) in enumerate(graphs):
+            if not (_is_cuda(rp) and _is_cuda(col)):
+                raise ValueError("batched mapping takes CUDA tensors")
+            rp, col = rp.contiguous(), col.contiguous()
+            keep.append((rp, col))
+            n = rp.numel() - 1
+            ids = torch.empty(max(n, 0), dtype=torch.int32, device=rp.device)
+            outs.append(ids)
+            arr[i] = GbgpuGraph(rp.data_ptr(), col.data_ptr(), n, col.numel(), ids.data_ptr() if n else 0)
+        if keep:
+            torch.cuda.current_stream(keep[0][0].device).synchronize()
+        sts = (GbgpuStats * max(1, count))()
+        sched = GbgpuSchedule(int(streams), int(order), int(exact_window))
+        wall = C.c_double()
+        opts = options if isinstance(options, str) else ":".join(options)
+        self._check(library().gbgpu_generate_mappings_batched(self._h, arr, count, opts.encode(), C.byref(sched),
+                                                                C.cast(sts, C.c_void_p), C.byref(wall),
+                                                                DEVICE_POINTERS))
+        return outs, [sts[i].as_dict() for i in range(count)], wall.value
 
     # -- consumers timed after a mapping, DBG arm, selector ---------------------
     def _vertex_out(self, fn, row_ptr, col, dtype, *extra):

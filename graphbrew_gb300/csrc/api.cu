@@ -5,12 +5,16 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <new>
 #include <string>
+#include <thread>
+#include <vector>
 
 #include "gb_common.cuh"
 #include "gb_config.h"
@@ -22,6 +26,8 @@ struct gbgpu_ctx {
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
     std::string last_error;
+    int64_t exact_window = 0;               // serial-order engine window (0: default)
+    std::vector<gbgpu_ctx*> workers;        // batched calls: one context per worker stream
 };
 
 namespace {
@@ -29,9 +35,13 @@ namespace {
 using gb::DevBuf;
 using gb::Error;
 
+// Schedule of the call running on this host thread (set from its context).
+thread_local int64_t tl_exact_window = 0;
+
 template <typename F>
 int guarded(gbgpu_ctx* ctx, F&& f) {
     try {
+        tl_exact_window = ctx ? ctx->exact_window : 0;
         if (ctx) GB_CUDA(cudaSetDevice(ctx->device));
         f();
         if (ctx) ctx->last_error.clear();
@@ -144,6 +154,7 @@ gb::LeidenParams leiden_params(const gb::Config& c) {
     // Schedule knobs (the autotuner's choices; defaults otherwise).
     if (const char* v = std::getenv("GBGPU_EXACT_MAX_VERTICES")) p.exact_max_vertices = std::atoll(v);
     if (const char* v = std::getenv("GBGPU_EXACT_WINDOW")) p.exact_window = std::max(32LL, std::atoll(v));
+    if (tl_exact_window > 0) p.exact_window = std::max<int64_t>(32, tl_exact_window);
     if (const char* v = std::getenv("GBGPU_ASYNC_CHUNK")) p.chunk_vertices = std::max(32, std::atoi(v));
     return p;
 }
@@ -230,6 +241,7 @@ int gbgpu_ctx_create(gbgpu_ctx** out, int device) {
 
 void gbgpu_ctx_destroy(gbgpu_ctx* ctx) {
     if (!ctx) return;
+    for (gbgpu_ctx* w : ctx->workers) gbgpu_ctx_destroy(w);
     cudaSetDevice(ctx->device);
     if (ctx->own_stream) {
         cudaStreamSynchronize(ctx->own_stream);
@@ -319,6 +331,66 @@ int gbgpu_generate_mapping(gbgpu_ctx* ctx, const int64_t* row_ptr, const int32_t
         cudaEventDestroy(t0);
         cudaEventDestroy(t1);
     });
+}
+
+int gbgpu_generate_mappings_batched(gbgpu_ctx* ctx, const gbgpu_graph* graphs, int32_t count, const char* opts,
+                                    const gbgpu_schedule* schedule, gbgpu_stats* stats, double* wall_ms,
+                                    uint32_t flags) {
+    if (!ctx || count < 0 || (count > 0 && !graphs)) return GBGPU_E_INVALID;
+    const int streams = schedule && schedule->streams > 0 ? std::min(schedule->streams, 64) : 4;
+    const int order = schedule ? schedule->order : 1;
+    const int64_t window = schedule ? schedule->exact_window : 0;
+    // Worker contexts (one stream each), created once and kept by the context.
+    int rc = guarded(ctx, [&] {
+        while ((int)ctx->workers.size() < streams) {
+            gbgpu_ctx* w = nullptr;
+            const int wrc = gbgpu_ctx_create(&w, ctx->device);
+            if (wrc != GBGPU_OK) throw Error(wrc, "worker context creation failed");
+            ctx->workers.push_back(w);
+        }
+        GB_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+    if (rc != GBGPU_OK) return rc;
+    // Order: as given, or largest graph first (longest-processing-time first
+    // over the worker streams).
+    std::vector<int32_t> idx(count);
+    for (int32_t i = 0; i < count; ++i) idx[i] = i;
+    if (order == 1)
+        std::stable_sort(idx.begin(), idx.end(),
+                         [&](int32_t x, int32_t y) { return graphs[x].nnz + graphs[x].n > graphs[y].nnz + graphs[y].n; });
+    std::atomic<int32_t> next{0};
+    std::atomic<int> first_rc{GBGPU_OK};
+    std::vector<std::string> errs(streams);
+    const auto t0 = std::chrono::steady_clock::now();
+    std::vector<std::thread> pool;
+    for (int wi = 0; wi < streams; ++wi) {
+        pool.emplace_back([&, wi] {
+            gbgpu_ctx* w = ctx->workers[wi];
+            w->exact_window = window;
+            while (first_rc.load() == GBGPU_OK) {
+                const int32_t k = next.fetch_add(1);
+                if (k >= count) break;
+                const gbgpu_graph& g = graphs[idx[k]];
+                const int r = gbgpu_generate_mapping(w, g.row_ptr, g.col, g.n, g.nnz, opts, -1.0, g.new_ids_out,
+                                                     stats ? &stats[idx[k]] : nullptr, flags);
+                if (r != GBGPU_OK) {
+                    int expect = GBGPU_OK;
+                    if (first_rc.compare_exchange_strong(expect, r)) errs[wi] = w->last_error;
+                }
+            }
+        });
+    }
+    for (std::thread& t : pool) t.join();
+    const auto t1 = std::chrono::steady_clock::now();
+    if (wall_ms) *wall_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    const int r = first_rc.load();
+    if (r != GBGPU_OK) {
+        for (const std::string& e : errs)
+            if (!e.empty()) ctx->last_error = e;
+        return r;
+    }
+    ctx->last_error.clear();
+    return GBGPU_OK;
 }
 
 int gbgpu_leiden(gbgpu_ctx* ctx, const int64_t* row_ptr, const int32_t* col, int64_t n, int64_t nnz,

@@ -142,9 +142,17 @@ def measure_graph(ctx: Context, rp, col, recipe: str = DEFAULT_RECIPE, repeats: 
     return np.asarray(tier0, dtype=np.float64), map_ms, kms
 
 
-def collect(ctx: Context, seeds, log=None):
+def collect(ctx: Context, seeds, log=None, checkpoint=None):
+    """Measure every seed's graph; `checkpoint(records)` is called every 100
+    graphs with what has been measured so far."""
     import torch
     recs = {"seed": [], "family": [], "scale": [], "tier0": [], "map_ms": [], "kernel_ms": []}
+    l2 = np.int64(torch.cuda.get_device_properties(0).L2_cache_size)
+
+    def snapshot():
+        out = {k: np.asarray(v) for k, v in recs.items()}
+        out["l2_bytes"] = l2
+        return out
     t0 = time.time()
     for i, seed in enumerate(seeds):
         fam, scale, rp, col = random_graph(seed)
@@ -152,11 +160,12 @@ def collect(ctx: Context, seeds, log=None):
         for k, v in (("seed", seed), ("family", FAMILIES.index(fam)), ("scale", scale), ("tier0", tier0),
                      ("map_ms", map_ms), ("kernel_ms", kms)):
             recs[k].append(v)
-        if log and (i + 1) % 100 == 0:
-            log(f"{i + 1} graphs, {time.time() - t0:.0f} s")
-    out = {k: np.asarray(v) for k, v in recs.items()}
-    out["l2_bytes"] = np.int64(torch.cuda.get_device_properties(0).L2_cache_size)
-    return out
+        if (i + 1) % 100 == 0:
+            if log:
+                log(f"{i + 1} graphs, {time.time() - t0:.0f} s")
+            if checkpoint:
+                checkpoint(snapshot())
+    return snapshot()
 
 
 # ---------------------------------------------------------------------------
@@ -280,7 +289,8 @@ def main(argv=None):
     a = ap.parse_args(argv)
     ctx = Context(0)
     if a.cmd == "collect":
-        data = collect(ctx, range(a.first, a.first + a.count), log=lambda m: print(m, file=sys.stderr))
+        data = collect(ctx, range(a.first, a.first + a.count), log=lambda m: print(m, file=sys.stderr),
+                       checkpoint=lambda d: np.savez_compressed(a.out, **d))
         np.savez_compressed(a.out, **data)
         print(json.dumps({"graphs": int(len(data["seed"]))}))
     elif a.cmd == "train":

@@ -179,6 +179,36 @@ int gbgpu_map_and_relabel(gbgpu_ctx* ctx, const int64_t* row_ptr, const int32_t*
                           int32_t* new_ids_out, int64_t* out_row_ptr, int32_t* out_col,
                           gbgpu_stats* stats, uint32_t flags);
 
+/* ---- Batched mode ----
+ * No counterpart in the reference (it maps one graph per process).  Many
+ * graphs are mapped with one recipe; graphs run concurrently on `streams`
+ * worker streams of the context's device (each worker has its own context,
+ * created on first use and kept until the parent is destroyed), so the
+ * latency-bound stages of small graphs overlap.  Every graph's result equals
+ * gbgpu_generate_mapping's on that graph.  Host pointers unless
+ * GBGPU_DEVICE_POINTERS. */
+typedef struct {
+    const int64_t* row_ptr;
+    const int32_t* col;
+    int64_t n;
+    int64_t nnz;
+    int32_t* new_ids_out;           /* n entries */
+} gbgpu_graph;
+
+typedef struct {
+    int32_t streams;                /* concurrent graphs (1..64); 0 = 4 */
+    int32_t order;                  /* 0 = as given, 1 = largest graph first */
+    int64_t exact_window;           /* serial-order engine window; 0 = library default */
+} gbgpu_schedule;
+
+/* stats (may be NULL): one entry per graph, in the given order; *wall_ms
+ * (may be NULL): host wall time of the whole batch.  schedule may be NULL
+ * (4 streams, largest first, default window).  Stops at the first failing
+ * graph and returns its status. */
+int gbgpu_generate_mappings_batched(gbgpu_ctx* ctx, const gbgpu_graph* graphs, int32_t count, const char* opts,
+                                    const gbgpu_schedule* schedule, gbgpu_stats* stats, double* wall_ms,
+                                    uint32_t flags);
+
 /* Largest n accepted by gbgpu_validate_permutation_noalloc. */
 #define GBGPU_NOALLOC_MAX_VERTICES (1 << 20)
 
