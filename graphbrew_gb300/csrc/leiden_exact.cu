@@ -48,12 +48,12 @@ constexpr int kWindowMax = 65536;             // window vertices (events <= 2 x 
 constexpr int kEventsMax = 2 * kWindowMax;    // event index = 2 x window offset (+1)
 constexpr int kSlotBits = 18;
 constexpr int kTableSlots = 1 << kSlotBits;   // hash slots, >= 2 x events
-constexpr int kCoarseBits = 10;               // event grouping: 1024 coarse buckets of slots
+constexpr int kCoarseBits = 9;                // event grouping: 512 coarse buckets of slots
 constexpr int kCoarse = 1 << kCoarseBits;
 constexpr int kFineBits = kSlotBits - kCoarseBits;
 constexpr int kTbThreads = 1024;              // table insert / group: one window vertex per thread
 constexpr int kTbChunks = kWindowMax / kTbThreads;
-constexpr int kTbFinishThreads = 1024;        // table finish: one CTA per coarse bucket
+constexpr int kTbFinishThreads = 512;         // table finish: one CTA per coarse bucket
 constexpr uint32_t kPadSlot = 0xFFFFFFFFu;
 static_assert(kTableSlots >= 2 * kEventsMax, "hash load factor <= 1/2");
 static_assert(kCoarse <= kTbThreads, "one coarse bucket per grouping thread");
@@ -510,8 +510,11 @@ __global__ void __launch_bounds__(kTbThreads) k_tb_group(ExactState a) {
 // segmented inclusive scan of signed degrees; writes times, prefixes and the
 // slots' event ranges.
 __global__ void __launch_bounds__(kTbFinishThreads) k_tb_finish(ExactState a) {
-    __shared__ int32_t wcnt[32 * 257];
-    __shared__ int32_t digit[256];
+    constexpr int kFine = 1 << kFineBits;
+    constexpr int kW = kTbFinishThreads / 32;
+    constexpr int kRow = kFine + 1;          // padded row of per-warp digit counts
+    __shared__ int32_t wcnt[kW * kRow];
+    __shared__ int32_t digit[kFine];
     __shared__ long long warp_v[32];
     __shared__ int warp_h[32];
     const long long P = a.ctl->P;
@@ -521,34 +524,41 @@ __global__ void __launch_bounds__(kTbFinishThreads) k_tb_finish(ExactState a) {
     if (cnt == 0) return;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int nwarps = blockDim.x >> 5;
-    constexpr int kFine = 1 << kFineBits;   // 256
-    static_assert(kFine == 256, "one 8-bit pass");
-    for (int k = tid; k < nwarps * 257; k += blockDim.x) wcnt[k] = 0;
+    static_assert(kFine % 32 == 0 && kFine <= kTbFinishThreads, "digit scan layout");
+    for (int k = tid; k < nwarps * kRow; k += blockDim.x) wcnt[k] = 0;
     __syncthreads();
+    // Stable pass on the fine slot bits: warp w owns a contiguous range; the
+    // next 32 keys are loaded while the current ones are ranked.
     const int chunk = (cnt + nwarps - 1) / nwarps;
     const int c0 = bs + min(cnt, w * chunk), c1 = bs + min(cnt, (w + 1) * chunk);
-    for (int base = c0; base < c1; base += 32) {
-        const int idx = base + lane;
-        const int d = idx < c1 ? (int)((a.ev1[idx] >> 32) & (kFine - 1)) : kFine;
-        const unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
-        if (d < kFine && lane == __ffs(peers) - 1) wcnt[w * 257 + d] += __popc(peers);
-        __syncwarp();
+    {
+        unsigned long long nxt = c0 + lane < c1 ? a.ev1[c0 + lane] : 0ull;
+        for (int base = c0; base < c1; base += 32) {
+            const int idx = base + lane;
+            const unsigned long long key = nxt;
+            if (base + 32 + lane < c1) nxt = a.ev1[base + 32 + lane];
+            const int d = idx < c1 ? (int)((key >> 32) & (kFine - 1)) : kFine;
+            const unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
+            if (d < kFine && lane == __ffs(peers) - 1) wcnt[w * kRow + d] += __popc(peers);
+            __syncwarp();
+        }
     }
     __syncthreads();
     if (tid < kFine) {
         int acc = 0;
         for (int ww = 0; ww < nwarps; ++ww) {
-            const int t = wcnt[ww * 257 + tid];
-            wcnt[ww * 257 + tid] = acc;
+            const int t = wcnt[ww * kRow + tid];
+            wcnt[ww * kRow + tid] = acc;
             acc += t;
         }
         digit[tid] = acc;
     }
     __syncthreads();
     if (w == 0) {
-        int v[8], t = 0;
+        constexpr int kPer = kFine / 32;
+        int v[kPer], t = 0;
 #pragma unroll
-        for (int k = 0; k < 8; ++k) { v[k] = digit[lane * 8 + k]; t += v[k]; }
+        for (int k = 0; k < kPer; ++k) { v[k] = digit[lane * kPer + k]; t += v[k]; }
         int incl = t;
         for (int o = 1; o < 32; o <<= 1) {
             const int y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
@@ -556,20 +566,24 @@ __global__ void __launch_bounds__(kTbFinishThreads) k_tb_finish(ExactState a) {
         }
         int run = incl - t;
 #pragma unroll
-        for (int k = 0; k < 8; ++k) { digit[lane * 8 + k] = run; run += v[k]; }
+        for (int k = 0; k < kPer; ++k) { digit[lane * kPer + k] = run; run += v[k]; }
     }
     __syncthreads();
-    for (int base = c0; base < c1; base += 32) {
-        const int idx = base + lane;
-        const unsigned long long key = idx < c1 ? a.ev1[idx] : 0ull;
-        const int d = idx < c1 ? (int)((key >> 32) & (kFine - 1)) : kFine;
-        const unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
-        int before = 0;
-        if (d < kFine) before = wcnt[w * 257 + d];
-        __syncwarp();
-        if (d < kFine) a.ev2[bs + digit[d] + before + __popc(peers & ((1u << lane) - 1u))] = key;
-        if (d < kFine && lane == __ffs(peers) - 1) wcnt[w * 257 + d] = before + __popc(peers);
-        __syncwarp();
+    {
+        unsigned long long nxt = c0 + lane < c1 ? a.ev1[c0 + lane] : 0ull;
+        for (int base = c0; base < c1; base += 32) {
+            const int idx = base + lane;
+            const unsigned long long key = nxt;
+            if (base + 32 + lane < c1) nxt = a.ev1[base + 32 + lane];
+            const int d = idx < c1 ? (int)((key >> 32) & (kFine - 1)) : kFine;
+            const unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
+            int before = 0;
+            if (d < kFine) before = wcnt[w * kRow + d];
+            __syncwarp();
+            if (d < kFine) a.ev2[bs + digit[d] + before + __popc(peers & ((1u << lane) - 1u))] = key;
+            if (d < kFine && lane == __ffs(peers) - 1) wcnt[w * kRow + d] = before + __popc(peers);
+            __syncwarp();
+        }
     }
     __syncthreads();
     // Segmented inclusive scan over ev2[bs, be), each thread a contiguous range.
