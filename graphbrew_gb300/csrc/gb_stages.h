@@ -40,7 +40,7 @@ struct LeidenParams {
     int chunk_vertices = 2048;      // asynchronous engine: vertices per launch
     int64_t super_single_cta_max_edges = 1 << 24;  // super-move in one thread-block cluster up to this size
     int64_t exact_max_vertices = INT64_MAX; // cd_parallel uses the serial-order engine up to this size
-    int64_t exact_window = 32768;           // speculative window of the serial-order engine
+    int64_t exact_window = 65536;           // speculative window of the serial-order engine
 };
 void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* membership, gbgpu_stats* st,
                    cudaStream_t s);

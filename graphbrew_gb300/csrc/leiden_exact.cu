@@ -67,6 +67,9 @@ constexpr int kHotMax = 2 * kEventsMax / kHotMin;
 constexpr int kEndBits = 18;                  // SlotMeta.endh: end | (hot id + 1) << kEndBits
 static_assert(kEventsMax < (1 << kEndBits), "event positions fit the end field");
 constexpr int kHubThreads2 = 256;             // threads of the hub kernels
+constexpr int kBigMaxDeg = 2048;              // rows above kWarpMaxDeg up to this: one CTA each
+constexpr int kBigThreads = 256;
+constexpr int kBigSlots = 2 * kBigMaxDeg;     // shared table of a big row
 constexpr int kHubSeg = 4 * kHubThreads2;     // edges per hub-accumulation CTA (4 per thread)
 constexpr int kTabSeg = 4 * kHubThreads2;     // table slots per hub-selection CTA (4 per thread)
 constexpr unsigned long long kNoChange = ~0ull;
@@ -77,6 +80,8 @@ struct Ctl {
     long long es0, es1;       // hub edge-segment range of the window
     long long ts0, ts1;       // hub table-segment range of the window
     long long ms0, ms1;       // mid-degree list range of the window
+    long long bs0, bs1;       // big-row list range of the window
+    long long c_bs0, c_bs1;   // big-row range of the last decided window
     long long round;
     long long evals;          // window vertices evaluated in this iteration
     long long cP, cX;         // committed range of the last decided window
@@ -148,6 +153,8 @@ struct ExactState {
     uint32_t* part_c;
     const uint32_t* mid_v;        // vertices with 32 < degree <= kWarpMaxDeg (ascending)
     long long n_mid;
+    const uint32_t* big_v;        // vertices with kWarpMaxDeg < degree <= kBigMaxDeg (ascending)
+    long long n_big;
     cudaGraphConditionalHandle cond;  // while-node condition (graph-driven rounds)
     int use_cond;
     double M, R;
@@ -321,13 +328,13 @@ __device__ __forceinline__ long long warp_lower_bound_u32(const uint32_t* a, lon
     return b ? lo + (__ffs(b) - 1) : hi;
 }
 
-// Window ranges of the hub segment lists and the mid-degree list for the
-// window [P, E): six searches on warps 0-5 of the calling CTA.
+// Window ranges of the hub segment lists, the mid-degree list and the
+// big-row list for the window [P, E): eight searches on warps 0-7.
 __device__ __forceinline__ void window_ranges(const ExactState& a, long long P, long long E) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (w >= 6) return;
-    const uint32_t* arr = w < 2 ? a.eseg_v : (w < 4 ? a.tseg_v : a.mid_v);
-    const long long len = w < 2 ? a.n_eseg : (w < 4 ? a.n_tseg : a.n_mid);
+    if (w >= 8) return;
+    const uint32_t* arr = w < 2 ? a.eseg_v : (w < 4 ? a.tseg_v : (w < 6 ? a.mid_v : a.big_v));
+    const long long len = w < 2 ? a.n_eseg : (w < 4 ? a.n_tseg : (w < 6 ? a.n_mid : a.n_big));
     const long long pos = warp_lower_bound_u32(arr, len, (uint32_t)((w & 1) ? E : P), lane);
     if (lane == 0) {
         switch (w) {
@@ -336,7 +343,9 @@ __device__ __forceinline__ void window_ranges(const ExactState& a, long long P, 
             case 2: a.ctl->ts0 = pos; break;
             case 3: a.ctl->ts1 = pos; break;
             case 4: a.ctl->ms0 = pos; break;
-            default: a.ctl->ms1 = pos; break;
+            case 5: a.ctl->ms1 = pos; break;
+            case 6: a.ctl->bs0 = pos; break;
+            default: a.ctl->bs1 = pos; break;
         }
     }
 }
@@ -357,11 +366,17 @@ __device__ __forceinline__ void window_ranges(const ExactState& a, long long P, 
 // ---------------------------------------------------------------------------
 struct SegSum {
     long long v;
+    int cnt;    // elements since the last segment start
     int head;   // a segment starts inside this range
 };
 
 __device__ __forceinline__ SegSum seg_combine(SegSum a, SegSum b) {
-    return SegSum{b.head ? b.v : a.v + b.v, a.head | b.head};
+    return b.head ? b : SegSum{a.v + b.v, a.cnt + b.cnt, a.head};
+}
+
+__device__ __forceinline__ SegSum seg_shfl_up(SegSum x, int o) {
+    return SegSum{__shfl_up_sync(0xFFFFFFFFu, x.v, o), __shfl_up_sync(0xFFFFFFFFu, x.cnt, o),
+                  __shfl_up_sync(0xFFFFFFFFu, x.head, o)};
 }
 
 // Slot of community c in the generation-`tag` table, inserting it if absent.
@@ -432,11 +447,17 @@ __global__ void __launch_bounds__(kTbThreads) k_tb_group(ExactState a) {
     // Bucket totals over all chunks and this chunk's offset inside each bucket.
     int tot = 0, pre = 0;
     if (tid < kCoarse) {
+        // Eight chunk counts in flight per step.
         const int32_t* h = a.tb_hist + tid * kTbChunks;
-        for (int c = 0; c < chunks; ++c) {
-            const int v = h[c];
-            tot += v;
-            if (c < (int)blockIdx.x) pre += v;
+        for (int c0 = 0; c0 < chunks; c0 += 8) {
+            int v[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) v[k] = c0 + k < chunks ? h[c0 + k] : 0;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                tot += v[k];
+                if (c0 + k < (int)blockIdx.x) pre += v[k];
+            }
         }
     }
     // Exclusive scan of the totals (kCoarse <= threads).
@@ -586,77 +607,115 @@ __global__ void __launch_bounds__(kTbFinishThreads) k_tb_finish(ExactState a) {
         }
     }
     __syncthreads();
-    // Segmented inclusive scan over ev2[bs, be), each thread a contiguous range.
+    // Segmented inclusive scan over ev2[bs, be), each thread a contiguous
+    // range read eight events at a time (keys, then degrees, in flight
+    // together).  The tail of each slot knows the slot's length from the scan
+    // and marks it hot.
+    __shared__ int s_cnt_w[32];
     const int per = (cnt + blockDim.x - 1) / blockDim.x;
     const int b0 = bs + min(cnt, tid * per), b1 = bs + min(cnt, tid * per + per);
-    SegSum own{0, 0};
-    for (int k = b0; k < b1; ++k) {
-        const unsigned long long key = a.ev2[k];
-        const uint32_t sl = (uint32_t)(key >> 32), e = (uint32_t)key;
-        const int head = (k == bs || (uint32_t)(a.ev2[k - 1] >> 32) != sl);
-        const long long v = (e & 1) ? a.wdeg[e >> 1] : -(long long)a.wdeg[e >> 1];
-        own = seg_combine(own, SegSum{v, head});
+    SegSum own{0, 0, 0};
+    {
+        uint32_t psl = b0 > bs ? (uint32_t)(a.ev2[b0 - 1] >> 32) : kPadSlot;
+        for (int k0 = b0; k0 < b1; k0 += 8) {
+            unsigned long long key[8];
+            int32_t dg[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) key[j] = k0 + j < b1 ? a.ev2[k0 + j] : 0ull;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) dg[j] = k0 + j < b1 ? a.wdeg[(uint32_t)key[j] >> 1] : 0;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                if (k0 + j >= b1) break;
+                const uint32_t sl = (uint32_t)(key[j] >> 32), e = (uint32_t)key[j];
+                const long long v = (e & 1) ? dg[j] : -(long long)dg[j];
+                own = seg_combine(own, SegSum{v, 1, sl != psl});
+                psl = sl;
+            }
+        }
     }
     SegSum inc = own;
     for (int o = 1; o < 32; o <<= 1) {
-        SegSum y{__shfl_up_sync(0xFFFFFFFFu, inc.v, o), __shfl_up_sync(0xFFFFFFFFu, inc.head, o)};
+        const SegSum y = seg_shfl_up(inc, o);
         if (lane >= o) inc = seg_combine(y, inc);
     }
-    if (lane == 31) { warp_v[w] = inc.v; warp_h[w] = inc.head; }
+    if (lane == 31) { warp_v[w] = inc.v; s_cnt_w[w] = inc.cnt; warp_h[w] = inc.head; }
     __syncthreads();
     if (w == 0) {
-        SegSum x = lane < nwarps ? SegSum{warp_v[lane], warp_h[lane]} : SegSum{0, 0};
+        const SegSum x = lane < nwarps ? SegSum{warp_v[lane], s_cnt_w[lane], warp_h[lane]} : SegSum{0, 0, 0};
         SegSum xi = x;
         for (int o = 1; o < 32; o <<= 1) {
-            SegSum y{__shfl_up_sync(0xFFFFFFFFu, xi.v, o), __shfl_up_sync(0xFFFFFFFFu, xi.head, o)};
+            const SegSum y = seg_shfl_up(xi, o);
             if (lane >= o) xi = seg_combine(y, xi);
         }
-        SegSum ex{__shfl_up_sync(0xFFFFFFFFu, xi.v, 1), __shfl_up_sync(0xFFFFFFFFu, xi.head, 1)};
-        if (lane == 0) ex = SegSum{0, 0};
-        if (lane < nwarps) { warp_v[lane] = ex.v; warp_h[lane] = ex.head; }
+        SegSum ex = seg_shfl_up(xi, 1);
+        if (lane == 0) ex = SegSum{0, 0, 0};
+        if (lane < nwarps) { warp_v[lane] = ex.v; s_cnt_w[lane] = ex.cnt; warp_h[lane] = ex.head; }
     }
     __syncthreads();
-    SegSum ex_thread{__shfl_up_sync(0xFFFFFFFFu, inc.v, 1), __shfl_up_sync(0xFFFFFFFFu, inc.head, 1)};
-    if (lane == 0) ex_thread = SegSum{0, 0};
-    const SegSum carry = seg_combine(SegSum{warp_v[w], warp_h[w]}, ex_thread);
-    long long run = carry.v;
-    for (int k = b0; k < b1; ++k) {
-        const unsigned long long key = a.ev2[k];
-        const uint32_t sl = (uint32_t)(key >> 32), e = (uint32_t)key;
-        const long long v = (e & 1) ? a.wdeg[e >> 1] : -(long long)a.wdeg[e >> 1];
-        const bool head = (k == bs || (uint32_t)(a.ev2[k - 1] >> 32) != sl);
-        run = head ? v : run + v;
-        a.stime[k] = (uint32_t)(P + (e >> 1));
-        a.epre[k] = run;
-        if (head) a.slots[sl].start = k;
-        if (k == be - 1 || (uint32_t)(a.ev2[k + 1] >> 32) != sl) a.slots[sl].endh = (uint32_t)(k + 1);
+    SegSum ex_thread = seg_shfl_up(inc, 1);
+    if (lane == 0) ex_thread = SegSum{0, 0, 0};
+    const SegSum carry = seg_combine(SegSum{warp_v[w], s_cnt_w[w], warp_h[w]}, ex_thread);
+    {
+        long long run = carry.v;
+        int runc = carry.cnt;
+        uint32_t psl = b0 > bs ? (uint32_t)(a.ev2[b0 - 1] >> 32) : kPadSlot;
+        for (int k0 = b0; k0 < b1; k0 += 8) {
+            unsigned long long key[9];
+            int32_t dg[8];
+#pragma unroll
+            for (int j = 0; j < 9; ++j) key[j] = k0 + j < be ? a.ev2[k0 + j] : ~0ull;   // one past for the tail test
+#pragma unroll
+            for (int j = 0; j < 8; ++j) dg[j] = k0 + j < b1 ? a.wdeg[(uint32_t)key[j] >> 1] : 0;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int k = k0 + j;
+                if (k >= b1) break;
+                const uint32_t sl = (uint32_t)(key[j] >> 32), e = (uint32_t)key[j];
+                const long long v = (e & 1) ? dg[j] : -(long long)dg[j];
+                const bool head = sl != psl;
+                run = head ? v : run + v;
+                runc = head ? 1 : runc + 1;
+                psl = sl;
+                a.stime[k] = (uint32_t)(P + (e >> 1));
+                a.epre[k] = run;
+                if (head) a.slots[sl].start = k;
+                if (k == be - 1 || (uint32_t)(key[j + 1] >> 32) != sl) {
+                    uint32_t endh = (uint32_t)(k + 1);
+                    if (runc >= kHotMin) {
+                        const unsigned id = atomicAdd(&a.ctl->nhot, 1u);
+                        if (id < (unsigned)kHotMax) endh |= (id + 1) << kEndBits;
+                    }
+                    a.slots[sl].endh = endh;
+                }
+            }
+        }
     }
     __syncthreads();
-    // Hot slots of this bucket: an index each, then their time-bucket starts.
+    // Hot slots: their time-bucket starts (bidx[b] = first event at a time
+    // >= P + kBucketV * b).
     const int nb = (int)((a.ctl->E - P + kBucketV - 1) / kBucketV);
-    for (int k = b0; k < b1; ++k) {
-        const uint32_t sl = (uint32_t)(a.ev2[k] >> 32);
-        if (!(k == bs || (uint32_t)(a.ev2[k - 1] >> 32) != sl)) continue;
-        const int32_t st = a.slots[sl].start;
-        const uint32_t en = a.slots[sl].endh;
-        if ((int)en - st < kHotMin) continue;
-        const unsigned id = atomicAdd(&a.ctl->nhot, 1u);
-        if (id < (unsigned)kHotMax) a.slots[sl].endh = en | ((id + 1) << kEndBits);
-    }
-    __syncthreads();
-    for (int k = b0; k < b1; ++k) {
-        const unsigned long long key = a.ev2[k];
-        const uint32_t sl = (uint32_t)(key >> 32), e = (uint32_t)key;
-        const uint32_t eh = a.slots[sl].endh;
-        const uint32_t hid = eh >> kEndBits;
-        if (!hid) continue;
-        const int end = (int)(eh & ((1u << kEndBits) - 1u));
-        int32_t* bx = a.hot_bidx + (size_t)(hid - 1) * kHotStride;
-        const int bk = (int)(e >> 1) / kBucketV;
-        const int bprev = k == a.slots[sl].start ? -1 : (int)((uint32_t)a.ev2[k - 1] >> 1) / kBucketV;
-        for (int b = bprev + 1; b <= bk; ++b) bx[b] = k;
-        if (k == end - 1)
-            for (int b = bk + 1; b <= nb; ++b) bx[b] = end;
+    for (int k0 = b0; k0 < b1; k0 += 8) {
+        unsigned long long key[8];
+        uint32_t eh[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) key[j] = k0 + j < b1 ? a.ev2[k0 + j] : 0ull;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) eh[j] = k0 + j < b1 ? a.slots[(uint32_t)(key[j] >> 32)].endh : 0u;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int k = k0 + j;
+            const uint32_t hid = eh[j] >> kEndBits;
+            if (k >= b1 || !hid) continue;
+            const uint32_t sl = (uint32_t)(key[j] >> 32), e = (uint32_t)key[j];
+            const int end = (int)(eh[j] & ((1u << kEndBits) - 1u));
+            int32_t* bx = a.hot_bidx + (size_t)(hid - 1) * kHotStride;
+            const int bk = (int)(e >> 1) / kBucketV;
+            const int bprev = k == a.slots[sl].start ? -1 : (int)((uint32_t)a.ev2[k - 1] >> 1) / kBucketV;
+            for (int b = bprev + 1; b <= bk; ++b) bx[b] = k;
+            if (k == end - 1)
+                for (int b = bk + 1; b <= nb; ++b) bx[b] = end;
+        }
     }
 }
 
@@ -859,6 +918,123 @@ __global__ void __launch_bounds__(kSmallWarpsPerBlock * 32) k_ex_eval_small(Exac
             const int ik = __shfl_sync(0xFFFFFFFFu, (int)inwin, k * 8);
             if (ik && dk > kTinyDeg && dk <= kSmallMaxDeg) eval_vertex<false>(a, r, u0 + k, lane, nullptr, nullptr);
         }
+    }
+}
+
+// Big rows (kWarpMaxDeg < degree <= kBigMaxDeg): one CTA per row, table in
+// shared memory, candidates compacted, lookups of four per thread interleaved.
+__global__ void __launch_bounds__(kBigThreads) k_ex_eval_big(ExactState a) {
+    extern __shared__ uint32_t big_smem[];
+    uint32_t* tk = big_smem;                      // kBigSlots keys
+    uint32_t* tv = tk + kBigSlots;                // kBigSlots counts
+    uint32_t* cand_c = tv + kBigSlots;            // kBigMaxDeg compacted candidates
+    uint32_t* cand_w = cand_c + kBigMaxDeg;
+    __shared__ int s_any;
+    __shared__ uint32_t s_cnt;
+    __shared__ double red_d[kBigThreads / 32];
+    __shared__ uint32_t red_c[kBigThreads / 32];
+    if (a.ctl->P >= a.ctl->n) return;
+    const Round r = round_view(a);
+    const long long b0 = a.ctl->bs0, b1 = a.ctl->bs1;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    for (long long bi = b0 + blockIdx.x; bi < b1; bi += gridDim.x) {
+        const uint32_t u = a.big_v[bi];
+        const int64_t rb = a.rp[u], re = a.rp[u + 1];
+        const int deg = (int)(re - rb);
+        const uint32_t d = a.vcom[u];
+        uint32_t H = 64;
+        while (H < 2u * (uint32_t)deg) H <<= 1;
+        const uint32_t mask = H - 1;
+        for (uint32_t i = tid; i < H; i += blockDim.x) { tk[i] = kNone; tv[i] = 0; }
+        if (tid == 0) {
+            s_any = a.vaff[u] != 0;
+            s_cnt = 0;
+        }
+        __syncthreads();
+        bool any = false;
+        for (int64_t base = rb; base < re; base += 4 * (int64_t)blockDim.x) {
+            uint32_t c[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int64_t e = base + k * (int64_t)blockDim.x + tid;
+                c[k] = kNone;
+                if (e < re) {
+                    const int32_t v = a.col[e];
+                    any = any || (v >= r.P && v < (int64_t)u && prev_mover(a, r, v));
+                    if (v != (int32_t)u) c[k] = comm_at(a, r, v, u);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const unsigned peers = __match_any_sync(0xFFFFFFFFu, c[k]);
+                if (c[k] != kNone && lane == __ffs(peers) - 1) table_add(tk, tv, mask, c[k], (uint32_t)__popc(peers));
+            }
+        }
+        if (any) s_any = 1;
+        __syncthreads();
+        if (!s_any) {
+            if (tid == 0) record(a, r, u, 0, d, 0.0);
+            __syncthreads();
+            continue;
+        }
+        const double ku = (double)deg;
+        const double kud = (double)table_get(tk, tv, mask, d);
+        // Compact the candidates (c != d); their order does not matter, the
+        // selection is a total order.
+        for (uint32_t i0 = 0; i0 < H; i0 += blockDim.x) {
+            const uint32_t i = i0 + tid;
+            const uint32_t c = i < H ? tk[i] : kNone;
+            const bool occ = c != kNone && c != d;
+            const unsigned bal = __ballot_sync(0xFFFFFFFFu, occ);
+            uint32_t base = 0;
+            if (lane == 0 && bal) base = atomicAdd(&s_cnt, (uint32_t)__popc(bal));
+            base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            if (occ) {
+                const uint32_t pos = base + __popc(bal & ((1u << lane) - 1u));
+                cand_c[pos] = c;
+                cand_w[pos] = tv[i];
+            }
+        }
+        __syncthreads();
+        const uint32_t cnt = s_cnt;
+        double best_d = 0.0;
+        uint32_t best_c = kNone;
+        double sd = 0.0;
+        for (uint32_t i0 = 0;; i0 += 4 * blockDim.x) {
+            uint32_t cc[5];
+            bool vv[5];
+            long long sg[5];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const uint32_t i = i0 + k * blockDim.x + tid;
+                vv[k] = i < cnt;
+                cc[k] = vv[k] ? cand_c[i] : kNone;
+            }
+            cc[4] = d;
+            vv[4] = i0 == 0;
+            sigma_at_k<5>(a, r.tag, r.P, cc, vv, u, sg);
+            if (i0 == 0) sd = (double)sg[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (!vv[k]) continue;
+                const double dl = delta_q((double)cand_w[i0 + k * blockDim.x + tid], kud, ku, (double)sg[k], sd,
+                                          a.M, a.R);
+                if (dl > 0.0 && better(dl, cc[k], best_d, best_c)) { best_d = dl; best_c = cc[k]; }
+            }
+            if (i0 + 4 * blockDim.x >= cnt) break;
+        }
+        warp_argmax(best_d, best_c);
+        if (lane == 0) { red_d[w] = best_d; red_c[w] = best_c; }
+        __syncthreads();
+        if (tid == 0) {
+            double bd = red_d[0];
+            uint32_t bc = red_c[0];
+            for (int k = 1; k < (int)(blockDim.x / 32); ++k)
+                if (better(red_d[k], red_c[k], bd, bc)) { bd = red_d[k]; bc = red_c[k]; }
+            if (bd > 0.0 && bc != kNone && bc != d) record(a, r, u, 1, bc, bd);
+            else record(a, r, u, 1, d, 0.0);
+        }
+        __syncthreads();
     }
 }
 
@@ -1145,14 +1321,24 @@ __global__ void k_ex_commit_b(ExactState a) {
 __global__ void __launch_bounds__(kHubThreads2) k_ex_commit_hub(ExactState a) {
     const CommitView c = commit_view(a);
     if (c.x < c.P) return;
+    // Work items: the decided window's hub edge segments, then its big rows.
     const long long q0 = a.ctl->c_es0, q1 = a.ctl->c_es1;
-    for (long long q = q0 + blockIdx.x; q < q1; q += gridDim.x) {
-        const HubSeg sg = a.eseg[q];
-        const uint32_t h = a.hub_v[sg.hub];
-        if ((long long)h > c.x) continue;   // segments are in hub order: block-uniform skip
-        if (!a.mv[h]) continue;
-        const int64_t rb = a.rp[h], re = a.rp[h + 1];
-        const int64_t e0 = rb + (int64_t)sg.part * kHubSeg, e1 = min(re, e0 + kHubSeg);
+    const long long g0 = a.ctl->c_bs0, g1 = a.ctl->c_bs1;
+    const long long nseg = q1 - q0, items = nseg + (g1 - g0);
+    for (long long q = blockIdx.x; q < items; q += gridDim.x) {
+        uint32_t h;
+        int64_t e0, e1;
+        if (q < nseg) {
+            const HubSeg sg = a.eseg[q0 + q];
+            h = a.hub_v[sg.hub];
+            e0 = a.rp[h] + (int64_t)sg.part * kHubSeg;
+            e1 = min(a.rp[h + 1], e0 + kHubSeg);
+        } else {
+            h = a.big_v[g0 + (q - nseg)];
+            e0 = a.rp[h];
+            e1 = a.rp[h + 1];
+        }
+        if ((long long)h > c.x || !a.mv[h]) continue;   // block-uniform
         for (int64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
             const int32_t v = a.col[e];
             if (v < c.P || v > c.x || v < (int64_t)h) a.vaff[v] = 1;
@@ -1186,6 +1372,8 @@ __global__ void __launch_bounds__(1024) k_ex_advance(ExactState a) {
         a.ctl->c_es1 = a.ctl->es1;
         a.ctl->c_ts0 = a.ctl->ts0;
         a.ctl->c_ts1 = a.ctl->ts1;
+        a.ctl->c_bs0 = a.ctl->bs0;
+        a.ctl->c_bs1 = a.ctl->bs1;
     }
     __syncthreads();
     window_ranges(a, nP, nE);
@@ -1294,15 +1482,28 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     const int64_t B = std::max<int64_t>(32, std::min<int64_t>(std::min<int64_t>(window, kWindowMax), n));
 
     // ---- hub segment tables (once per call) ----
-    const int64_t nh = (int64_t)ctx.hubs_h.size();
-    std::vector<int64_t> hdeg(nh);
-    if (nh) {
-        DevBuf<int64_t> dd(nh, s);
-        k_hub_degrees<<<grid_for(nh, kT), kT, 0, s>>>(ctx.g.row_ptr, ctx.hubs, nh, dd);
+    // Rows above kWarpMaxDeg: up to kBigMaxDeg one CTA each ("big"), above
+    // that segmented over CTAs ("hubs").
+    const int64_t nh_all = (int64_t)ctx.hubs_h.size();
+    std::vector<int64_t> hdeg_all(nh_all);
+    if (nh_all) {
+        DevBuf<int64_t> dd(nh_all, s);
+        k_hub_degrees<<<grid_for(nh_all, kT), kT, 0, s>>>(ctx.g.row_ptr, ctx.hubs, nh_all, dd);
         GB_LAUNCH_CHECK();
-        GB_CUDA(cudaMemcpyAsync(hdeg.data(), dd.get(), nh * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+        GB_CUDA(cudaMemcpyAsync(hdeg_all.data(), dd.get(), nh_all * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
         GB_CUDA(cudaStreamSynchronize(s));
     }
+    std::vector<uint32_t> big_h, hub_h;
+    std::vector<int64_t> hdeg;
+    for (int64_t j = 0; j < nh_all; ++j) {
+        if (hdeg_all[j] <= kBigMaxDeg) {
+            big_h.push_back(ctx.hubs_h[j]);
+        } else {
+            hub_h.push_back(ctx.hubs_h[j]);
+            hdeg.push_back(hdeg_all[j]);
+        }
+    }
+    const int64_t nh = (int64_t)hub_h.size(), n_big = (int64_t)big_h.size();
     std::vector<int64_t> toff(nh);
     std::vector<uint32_t> tcap(nh);
     std::vector<int32_t> tfirst(nh), tcount(nh);
@@ -1318,14 +1519,14 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
         const int ne = (int)ceil_div(hdeg[j], kHubSeg);
         for (int k = 0; k < ne; ++k) {
             eseg.push_back({(int32_t)j, k});
-            eseg_v.push_back(ctx.hubs_h[j]);
+            eseg_v.push_back(hub_h[j]);
         }
         const int nt = (int)std::max<int64_t>(1, ceil_div(hdeg[j], kTabSeg));   // occupied slots <= degree
         tfirst[j] = (int32_t)tseg.size();
         tcount[j] = nt;
         for (int k = 0; k < nt; ++k) {
             tseg.push_back({(int32_t)j, k});
-            tseg_v.push_back(ctx.hubs_h[j]);
+            tseg_v.push_back(hub_h[j]);
         }
     }
     DevBuf<int64_t> d_toff = upload(toff, s);
@@ -1333,6 +1534,7 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     DevBuf<int32_t> d_tfirst = upload(tfirst, s), d_tcount = upload(tcount, s);
     DevBuf<HubSeg> d_eseg = upload(eseg, s), d_tseg = upload(tseg, s);
     DevBuf<uint32_t> d_eseg_v = upload(eseg_v, s), d_tseg_v = upload(tseg_v, s);
+    DevBuf<uint32_t> d_hub_v = upload(hub_h, s), d_big_v = upload(big_h, s);
     DevBuf<uint32_t> tkeys(pool > 0 ? pool : 1, s), tvals(pool > 0 ? pool : 1, s);
     GB_CUDA(cudaMemsetAsync(tkeys, 0xFF, (pool > 0 ? pool : 1) * sizeof(uint32_t), s));
     GB_CUDA(cudaMemsetAsync(tvals, 0, (pool > 0 ? pool : 1) * sizeof(uint32_t), s));
@@ -1414,7 +1616,9 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     a.hot_bidx = hot_bidx.get();
     a.stime = stime.get();
     a.epre = epre.get();
-    a.hub_v = ctx.hubs;
+    a.hub_v = d_hub_v.get();
+    a.big_v = d_big_v.get();
+    a.n_big = n_big;
     a.hub_toff = d_toff.get();
     a.hub_tcap = d_tcap.get();
     a.hub_tfirst = d_tfirst.get();
@@ -1464,15 +1668,20 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     };
     const int mid_grid = resident((const void*)k_ex_eval_mid, kMidWarpsPerBlock * 32, mid_smem);
     const int select_grid = resident((const void*)k_ex_hub_select, kHubThreads2, 0);
+    const int big_smem = (2 * kBigSlots + 2 * kBigMaxDeg) * (int)sizeof(uint32_t);
+    GB_CUDA(cudaFuncSetAttribute(k_ex_eval_big, cudaFuncAttributeMaxDynamicSharedMemorySize, big_smem));
+    const int big_grid = resident((const void*)k_ex_eval_big, kBigThreads, big_smem);
     const int hub_grid = resident((const void*)k_ex_hub_accum, kHubThreads2, 0);
     const int commit_grid = (int)std::max<int64_t>(1, ceil_div(B, kT));
     const int commit_b_grid = (int)std::max<int64_t>(1, ceil_div(B * 32, kT));
-    const int per_round = 7 + (n_mid ? 1 : 0) + (nh ? 3 : 0);   // table = 3 kernels
+    // eval_small, advance, 3 table kernels, commit_a, commit_b; eval_mid;
+    // eval_big; hub_select + hub_accum; commit_hub (hubs or big rows).
+    const int per_round = 7 + (n_mid ? 1 : 0) + (n_big ? 1 : 0) + (nh ? 2 : 0) + ((nh || n_big) ? 1 : 0);
     const int commit_a_grid = std::max(commit_grid, nh ? hub_grid : 0);
     // Side streams and events for the fork/join shape of a captured round:
     struct Fork {
         cudaStream_t s1 = nullptr, s2 = nullptr, s3 = nullptr;
-        cudaEvent_t ev[8] = {};
+        cudaEvent_t ev[9] = {};
         ~Fork() {
             for (cudaEvent_t e : ev)
                 if (e) cudaEventDestroy(e);
@@ -1494,14 +1703,18 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
             GB_CUDA(cudaStreamWaitEvent(sm, fk.ev[0], 0));
             GB_CUDA(cudaStreamWaitEvent(sh, fk.ev[0], 0));
         }
+        if (fork) GB_CUDA(cudaStreamWaitEvent(sa, fk.ev[0], 0));
         k_ex_eval_small<<<small_grid, kSmallWarpsPerBlock * 32, 0, st>>>(a);
         if (n_mid) k_ex_eval_mid<<<mid_grid, kMidWarpsPerBlock * 32, mid_smem, sm>>>(a);
         if (nh) k_ex_hub_select<<<select_grid, kHubThreads2, 0, sh>>>(a);
+        if (n_big) k_ex_eval_big<<<big_grid, kBigThreads, big_smem, sa>>>(a);
         if (fork) {
             GB_CUDA(cudaEventRecord(fk.ev[1], sm));
             GB_CUDA(cudaEventRecord(fk.ev[2], sh));
+            GB_CUDA(cudaEventRecord(fk.ev[8], sa));
             GB_CUDA(cudaStreamWaitEvent(st, fk.ev[1], 0));
             GB_CUDA(cudaStreamWaitEvent(st, fk.ev[2], 0));
+            GB_CUDA(cudaStreamWaitEvent(st, fk.ev[8], 0));
         }
         k_ex_advance<<<1, 1024, 0, st>>>(a);
         if (fork) {
@@ -1516,10 +1729,8 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
             GB_CUDA(cudaStreamWaitEvent(sa, fk.ev[4], 0));
         }
         k_ex_commit_b<<<commit_b_grid, kT, 0, st>>>(a);
-        if (nh) {
-            k_ex_commit_hub<<<hub_grid, kHubThreads2, 0, sh>>>(a);
-            k_ex_hub_accum<<<hub_grid, kHubThreads2, 0, sa>>>(a);
-        }
+        if (nh || n_big) k_ex_commit_hub<<<hub_grid, kHubThreads2, 0, sh>>>(a);
+        if (nh) k_ex_hub_accum<<<hub_grid, kHubThreads2, 0, sa>>>(a);
         if (fork) {
             GB_CUDA(cudaEventRecord(fk.ev[5], sm));
             GB_CUDA(cudaEventRecord(fk.ev[6], sh));
