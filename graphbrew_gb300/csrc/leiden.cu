@@ -327,6 +327,20 @@ __global__ void k_batch_starts(const uint32_t* __restrict__ active, int64_t na, 
     }
 }
 
+__global__ void k_big_super_flags(const uint32_t* __restrict__ active, int64_t na, const int64_t* __restrict__ soff,
+                                  int64_t limit, int32_t* __restrict__ flag) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < na; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t c = active[i];
+        flag[i] = soff[c + 1] - soff[c] > limit;
+    }
+}
+
+__global__ void k_big_super_emit(const uint32_t* __restrict__ active, int64_t na, const int32_t* __restrict__ flag,
+                                 const int64_t* __restrict__ pos, uint32_t* __restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < na; i += (int64_t)gridDim.x * blockDim.x)
+        if (flag[i]) out[pos[i]] = active[i];
+}
+
 struct SmArgs {
     const int64_t* soff;
     const uint32_t* snbr;
@@ -343,6 +357,12 @@ struct SmArgs {
     uint32_t* gkeys;              // per-warp global tables for big super-nodes
     uint32_t* gvals;
     int64_t gcap;
+    // Super-nodes above kBigSuper neighbours: one CTA each (cluster kernel).
+    const uint32_t* big_active;   // ascending
+    const int64_t* bigstart;      // per batch
+    uint32_t* bkeys;              // per-CTA global tables
+    uint32_t* bvals;
+    int64_t bcap;
 };
 
 constexpr int kSmSmall = 256;     // per-warp shared table slots
@@ -419,38 +439,218 @@ __device__ __forceinline__ void super_commit(const SmArgs& a, uint32_t c, int* m
 // cluster barrier / commit / cluster barrier; iterations stop early when a
 // full iteration moves nothing.  The cluster barrier is the hardware
 // barrier.cluster (release / acquire), so the CTAs' global writes of one
-// phase are visible to the next.
+// phase are visible to the next.  A warp keeps its proposals in shared
+// memory and its lanes commit them after the barrier; small super-nodes use
+// a shared table that also caches each candidate's total at insertion.
 constexpr int kSmCluster = 8;
+constexpr int kSmPerWarp = 16;    // proposals a warp keeps per batch (4096 / (8 x 32))
+constexpr int kBigSuper = 1024;   // super-nodes with more neighbours: one CTA each
 
 __device__ __forceinline__ void cluster_sync_all() {
     asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
     asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
 }
 
+struct SmProposal {
+    uint32_t c, d, best, pad;
+    long long kc;
+    double delta;
+};
+
+// Proposal for super-node c (as super_propose) with a shared table whose
+// third array holds the candidates' totals, loaded by the inserting lane.
+__device__ void super_propose_cached(const SmArgs& a, uint32_t c, uint32_t* tk, uint32_t* tv,
+                                     unsigned long long* tt, uint32_t* gk, uint32_t* gv, SmProposal& out) {
+    const int lane = threadIdx.x & 31;
+    const int64_t b = a.soff[c], e = a.soff[c + 1];
+    const int64_t deg = e - b;
+    uint32_t H = 64;
+    while ((int64_t)H < 2 * deg) H <<= 1;
+    const bool shared = H <= (uint32_t)kSmSmall;
+    uint32_t *k = shared ? tk : gk, *v = shared ? tv : gv;
+    const uint32_t mask = H - 1;
+    for (uint32_t i = lane; i < H; i += 32) { k[i] = kNone; v[i] = 0; }
+    __syncwarp();
+    const uint32_t d = a.scomm[c];
+    const long long kcl = a.sweight[c];
+    const unsigned long long sd_raw = a.sctot[d];
+    for (int64_t i0 = b; i0 < e; i0 += 32) {
+        uint32_t key = kNone, wgt = 0;
+        if (i0 + lane < e) {
+            key = a.scomm[a.snbr[i0 + lane]];
+            wgt = a.sw[i0 + lane];
+        }
+        if (key != kNone) {
+            uint32_t h = hash_u32(key) & mask;
+            while (true) {
+                const uint32_t prev = atomicCAS(&k[h], kNone, key);
+                if (prev == kNone && shared) tt[h] = a.sctot[key];
+                if (prev == kNone || prev == key) {
+                    atomicAdd(&v[h], wgt);
+                    break;
+                }
+                h = (h + 1) & mask;
+            }
+        }
+    }
+    __syncwarp();
+    const double kc = (double)kcl;
+    const double sigma_d = (double)(long long)sd_raw;
+    const double removal = __ddiv_rn(__dmul_rn(__dmul_rn(a.R, kc), __dsub_rn(sigma_d, kc)), a.M);
+    const double kc_to_d = (double)table_get(k, v, mask, d);
+    double best_d = 0.0;
+    uint32_t best_c = d;
+    for (uint32_t i = lane; i < H; i += 32) {
+        const uint32_t ek = k[i];
+        if (ek == kNone) continue;
+        const double kce = (double)v[i];
+        double add;
+        if (ek == d) {
+            add = __dsub_rn(kc_to_d, removal);
+        } else {
+            const double se = (double)(long long)(shared ? tt[i] : a.sctot[ek]);
+            add = __dsub_rn(kce, __ddiv_rn(__dmul_rn(__dmul_rn(a.R, kc), se), a.M));
+        }
+        const double dl = __dadd_rn(__dsub_rn(add, removal), kc_to_d);
+        if (better(dl, ek, best_d, best_c)) { best_d = dl; best_c = ek; }
+    }
+    warp_argmax(best_d, best_c);
+    out.c = c;
+    out.d = d;
+    out.best = best_c;
+    out.kc = kcl;
+    out.delta = best_d;
+    __syncwarp();
+}
+
+// Proposal for a big super-node by the whole CTA (global table of the CTA).
+__device__ void super_propose_block(const SmArgs& a, uint32_t c, SmProposal* out, double* red_d, uint32_t* red_c) {
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int64_t b = a.soff[c], e = a.soff[c + 1];
+    const int64_t deg = e - b;
+    uint32_t H = 64;
+    while ((int64_t)H < 2 * deg) H <<= 1;
+    uint32_t* k = a.bkeys + (int64_t)blockIdx.x * a.bcap;
+    uint32_t* v = a.bvals + (int64_t)blockIdx.x * a.bcap;
+    const uint32_t mask = H - 1;
+    for (uint32_t i = tid; i < H; i += blockDim.x) { k[i] = kNone; v[i] = 0; }
+    const uint32_t d = a.scomm[c];
+    const long long kcl = a.sweight[c];
+    const double kc = (double)kcl;
+    const double sigma_d = (double)(long long)a.sctot[d];
+    __syncthreads();
+#pragma unroll 4
+    for (int64_t idx = b + tid; idx < e; idx += blockDim.x) table_add(k, v, mask, a.scomm[a.snbr[idx]], a.sw[idx]);
+    __syncthreads();
+    const double removal = __ddiv_rn(__dmul_rn(__dmul_rn(a.R, kc), __dsub_rn(sigma_d, kc)), a.M);
+    const double kc_to_d = (double)table_get(k, v, mask, d);
+    double best_d = 0.0;
+    uint32_t best_c = d;
+#pragma unroll 8
+    for (uint32_t i = tid; i < H; i += blockDim.x) {
+        const uint32_t ek = k[i];
+        if (ek == kNone) continue;
+        const double kce = (double)v[i];
+        double add;
+        if (ek == d) {
+            add = __dsub_rn(kc_to_d, removal);
+        } else {
+            const double se = (double)(long long)a.sctot[ek];
+            add = __dsub_rn(kce, __ddiv_rn(__dmul_rn(__dmul_rn(a.R, kc), se), a.M));
+        }
+        const double dl = __dadd_rn(__dsub_rn(add, removal), kc_to_d);
+        if (better(dl, ek, best_d, best_c)) { best_d = dl; best_c = ek; }
+    }
+    warp_argmax(best_d, best_c);
+    if (lane == 0) { red_d[w] = best_d; red_c[w] = best_c; }
+    __syncthreads();
+    if (tid == 0) {
+        double bd = red_d[0];
+        uint32_t bc = red_c[0];
+        for (int q = 1; q < (int)(blockDim.x >> 5); ++q)
+            if (better(red_d[q], red_c[q], bd, bc)) { bd = red_d[q]; bc = red_c[q]; }
+        out->c = c;
+        out->d = d;
+        out->best = bc;
+        out->kc = kcl;
+        out->delta = bd;
+    }
+    __syncthreads();
+}
+
 __global__ void __launch_bounds__(1024)
 k_super_move_cluster(SmArgs a, int max_iter, int* iters_out, long long* moves_out, int* gmoves) {
-    extern __shared__ uint32_t sm_smem[];  // 32 warps x (keys, vals) x kSmSmall
-    const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    extern __shared__ uint32_t sm_smem[];   // 32 warps x (keys, vals, totals) x kSmSmall
+    __shared__ SmProposal props[32][kSmPerWarp];
+    __shared__ SmProposal bprop;
+    __shared__ double red_d[32];
+    __shared__ uint32_t red_c[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int64_t gw = (int64_t)blockIdx.x * nw + w, gnw = (int64_t)gridDim.x * nw;
-    const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, gnt = (int64_t)gridDim.x * blockDim.x;
-    uint32_t* tk = sm_smem + (size_t)w * 2 * kSmSmall;
+    uint32_t* tk = sm_smem + (size_t)w * 4 * kSmSmall;
+    uint32_t* tv = tk + kSmSmall;
+    unsigned long long* tt = reinterpret_cast<unsigned long long*>(tv + kSmSmall);
     long long total_moves = 0;
     int it = 0;
     for (; it < max_iter; ++it) {
         for (int64_t bt = 0; bt < a.nbatch; ++bt) {
             const int64_t lo = a.bstart[bt], hi = a.bstart[bt + 1];
             if (lo == hi) continue;
-            for (int64_t i = lo + gw; i < hi; i += gnw)
-                super_propose(a, a.active[i], tk, tk + kSmSmall, a.gkeys + gw * a.gcap, a.gvals + gw * a.gcap);
+            // Warps: super-nodes up to kBigSuper neighbours.
+            int kept = 0;
+            for (int64_t i = lo + gw; i < hi; i += gnw) {
+                const uint32_t c = a.active[i];
+                if (a.soff[c + 1] - a.soff[c] > kBigSuper) continue;
+                SmProposal pr;
+                super_propose_cached(a, c, tk, tv, tt, a.gkeys + gw * a.gcap, a.gvals + gw * a.gcap, pr);
+                if (kept < kSmPerWarp) {
+                    if (lane == 0) props[w][kept] = pr;
+                } else if (lane == 0) {   // more than the warp keeps: through global memory
+                    a.proposed[pr.c] = pr.best;
+                    a.pdelta[pr.c] = pr.delta;
+                }
+                ++kept;
+            }
+            __syncwarp();
+            // CTAs: the batch's big super-nodes (proposals through global memory).
+            const int64_t blo = a.bigstart[bt], bhi = a.bigstart[bt + 1];
+            __syncthreads();
+            for (int64_t j = blo + blockIdx.x; j < bhi; j += gridDim.x) {
+                super_propose_block(a, a.big_active[j], &bprop, red_d, red_c);
+                if (threadIdx.x == 0) {
+                    a.proposed[bprop.c] = bprop.best;
+                    a.pdelta[bprop.c] = bprop.delta;
+                }
+            }
             cluster_sync_all();
-            for (int64_t i = lo + gt; i < hi; i += gnt) super_commit(a, a.active[i], &gmoves[it]);
+            if (lane < min(kept, kSmPerWarp)) {
+                const SmProposal pr = props[w][lane];
+                if (pr.best != pr.d && pr.delta > 0.0) {
+                    atomicAdd(&a.sctot[pr.d], (unsigned long long)(-pr.kc));
+                    atomicAdd(&a.sctot[pr.best], (unsigned long long)pr.kc);
+                    a.scomm[pr.c] = pr.best;
+                    atomicAdd(&gmoves[it], 1);
+                }
+            }
+            if (kept > kSmPerWarp) {
+                // The warp's nodes past kSmPerWarp, in the same order as proposed.
+                int seen = 0;
+                for (int64_t i = lo + gw; i < hi; i += gnw) {
+                    const uint32_t c = a.active[i];
+                    if (a.soff[c + 1] - a.soff[c] > kBigSuper) continue;
+                    if (seen++ < kSmPerWarp) continue;
+                    if (lane == 0) super_commit(a, c, &gmoves[it]);
+                }
+            }
+            if (threadIdx.x == 0)
+                for (int64_t j = blo + blockIdx.x; j < bhi; j += gridDim.x) super_commit(a, a.big_active[j], &gmoves[it]);
             cluster_sync_all();
         }
         const int m = atomicAdd(&gmoves[it], 0);
         total_moves += m;
         if (m == 0) { ++it; break; }
     }
-    if (gt == 0) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
         *iters_out = it;
         *moves_out = total_moves;
     }
@@ -618,7 +818,7 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
     GB_CUDA(cudaFuncSetAttribute(k_local_move_hub, cudaFuncAttributeMaxDynamicSharedMemorySize, hub_smem));
     const int lm_smem = kLmWarpsPerBlock * 2 * kWarpHash * (int)sizeof(uint32_t);
     GB_CUDA(cudaFuncSetAttribute(k_local_move_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, lm_smem));
-    const int sm_smem = 32 * 2 * kSmSmall * (int)sizeof(uint32_t);
+    const int sm_smem = 32 * 4 * kSmSmall * (int)sizeof(uint32_t);
     GB_CUDA(cudaFuncSetAttribute(k_super_move_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_smem));
 
     LmArgs la{g.row_ptr, g.col, vcom, ctot, vaff, M, R, dacc, macc};
@@ -781,9 +981,35 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
                 max_sdeg = (int64_t)read_dev(md.get(), s);
                 ++launches;
             }
-            int64_t gcap = 64;
-            while (gcap < 2 * max_sdeg) gcap <<= 1;
             const bool single = nuniq <= p.super_single_cta_max_edges;
+            // The cluster kernel gives super-nodes above kBigSuper neighbours a
+            // CTA each; warps then need tables for at most kBigSuper.
+            const int64_t warp_max = single ? std::min<int64_t>(max_sdeg, kBigSuper) : max_sdeg;
+            int64_t gcap = 64;
+            while (gcap < 2 * warp_max) gcap <<= 1;
+            int64_t bcap = 64;
+            while (bcap < 2 * max_sdeg) bcap <<= 1;
+            int64_t nbig = 0;
+            DevBuf<uint32_t> big_active;
+            DevBuf<int64_t> bigstart(nbatch + 1, s);
+            if (single) {
+                DevBuf<int32_t> bflag(na, s);
+                DevBuf<int64_t> bpos(na + 1, s);
+                k_big_super_flags<<<grid_for(na, kT), kT, 0, s>>>(active, na, soff, kBigSuper, bflag);
+                GB_LAUNCH_CHECK();
+                exclusive_scan_i32_to_i64(bflag, bpos, na, bpos.get() + na, s);
+                nbig = read_dev(bpos.get() + na, s);
+                big_active.alloc(nbig > 0 ? nbig : 1, s);
+                if (nbig) {
+                    k_big_super_emit<<<grid_for(na, kT), kT, 0, s>>>(active, na, bflag, bpos, big_active);
+                    GB_LAUNCH_CHECK();
+                }
+                k_batch_starts<<<grid_for(nbatch + 1, kT), kT, 0, s>>>(big_active, nbig, nbatch, batch, bigstart);
+                GB_LAUNCH_CHECK();
+                launches += 6;
+            }
+            DevBuf<uint32_t> bk(single && nbig ? (int64_t)kSmCluster * bcap : 1, s);
+            DevBuf<uint32_t> bv(single && nbig ? (int64_t)kSmCluster * bcap : 1, s);
             // Per-warp global tables for super-nodes above kSmSmall / 2 neighbours,
             // capped at 512 MB in total.
             int64_t nwarps_total = single ? (int64_t)kSmCluster * 32 : (int64_t)kNumSMs * 4 * 8;
@@ -792,7 +1018,8 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
             DevBuf<uint32_t> gk(gcap > kSmSmall ? nwarps_total * gcap : 1, s);
             DevBuf<uint32_t> gv(gcap > kSmSmall ? nwarps_total * gcap : 1, s);
             SmArgs sa{soff, snbr, sw, sweight, scomm, sctot, active, bstart, nbatch, proposed, pdelta, M, R,
-                      gk, gv, gcap > kSmSmall ? gcap : 0};
+                      gk, gv, gcap > kSmSmall ? gcap : 0, big_active.get(), bigstart.get(), bk.get(), bv.get(),
+                      bcap};
             DevBuf<int> iters_d(1, s), gmoves(super_max_iter, s);
             DevBuf<long long> moves_d(1, s);
             launches += 2;

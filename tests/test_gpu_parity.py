@@ -162,6 +162,38 @@ def test_parallel_recipe_is_serial_order(ctx):
     np.testing.assert_array_equal(m_par.cpu().numpy().view(np.uint32), m_orc)
 
 
+@pytest.mark.parametrize("family", ["urand", "grid"])
+def test_weak_structure_graphs_bit_exact(ctx, family):
+    """Uniform-random and grid graphs (weak community structure, long BFS
+    chains): the whole mapping equals the oracle's serial-order result."""
+    if family == "urand":
+        rp_t, col_t = gg.uniform(17, 16, seed=31, device="cuda")
+    else:
+        rp_t, col_t = gg.grid(400, 400, 0.05, seed=32, device="cuda")
+    rp, col = rp_t.cpu().numpy(), col_t.cpu().numpy()
+    ar = po.auto_resolution(rp, col)
+    memb, st = ctx.run_graphbrew(rp_t, col_t, PARALLEL, ar)
+    m_orc, ost = po.leiden(rp, col, ar)
+    np.testing.assert_array_equal(memb.cpu().numpy().view(np.uint32), m_orc)
+    ids, _ = ctx.generate_mapping(rp_t, col_t, PARALLEL, ar)
+    ids_orc, _ = po.compose(rp, col, m_orc)
+    np.testing.assert_array_equal(ids.cpu().numpy(), ids_orc)
+
+
+@pytest.mark.parametrize("family", ["urand23", "grid4096"])
+def test_full_size_weak_structure_graphs(ctx, family):
+    """The full-size uniform (2^23 vertices, degree 16) and 4096 x 4096 grid
+    graphs: a valid permutation, relabelled CSR with the same entry count."""
+    if family == "urand23":
+        rp_t, col_t = gg.uniform(23, 16, seed=27491095, device="cuda")
+    else:
+        rp_t, col_t = gg.grid(4096, 4096, 0.05, seed=27491095, device="cuda")
+    ids, orp, ocol, st = ctx.map_and_relabel(rp_t, col_t, PARALLEL)
+    assert ctx.validate_permutation(ids) == 0
+    assert int(orp[-1].item()) == col_t.numel() and ocol.numel() == col_t.numel()
+    assert st["passes"] <= 2 and st["communities"] > 1
+
+
 def test_async_engine_quality(ctx, monkeypatch):
     """The asynchronous cd_parallel engine stays close to the serial result."""
     monkeypatch.setenv("GBGPU_EXACT_MAX_VERTICES", "0")
