@@ -7,7 +7,8 @@
 //   * each community's vertices keep vertex-id order (commVertices, :6373-6386);
 //   * intra order: Gorder with window w for 4..fallback vertices
 //     (intraGorderGreedy, :4420-4587), BFS from the hub above the fallback
-//     (intraBFSFromHub, :3929-3984), identity for <= 3 vertices;
+//     (intraBFSFromHub, :3929-3984), identity for <= 3 vertices; or reverse
+//     Cuthill-McKee for every community (intraRCM, :4000-4134);
 //   * newIds[v] = offset(community) + localId[v] (:7003-7017).
 //
 // Layout in HBM (n vertices): one stable radix sort of (rank(community), v)
@@ -25,7 +26,7 @@ namespace gb {
 namespace {
 
 enum CommunityOrderOrd { kSizeDesc = 0, kSizeAsc = 1, kDegreeDesc = 2, kDegreeAsc = 3, kIdentity = 6 };
-enum IntraOrd { kIntraBFS = 0, kIntraDendrogram = 3, kIntraGorder = 4 };
+enum IntraOrd { kIntraBFS = 0, kIntraRCM = 1, kIntraDendrogram = 3, kIntraGorder = 4 };
 
 constexpr int kT = 256;
 
@@ -560,6 +561,183 @@ __global__ void k_bfs_left_assign(const uint32_t* __restrict__ order_v, int64_t 
     }
 }
 
+// ---------------------------------------------------------------------------
+// Reverse Cuthill-McKee (intraRCM, :4000-4134) over all communities at once,
+// level-synchronous like the BFS above:
+//   * start: minimum degree, ties to the smaller id;
+//   * communities above 32 vertices: up to three George-Liu sweeps, each a
+//     BFS from the current node whose start is *not* marked visited (so it
+//     reappears on level 2, as in the reference); while the eccentricity
+//     grows, the next node is the minimum-degree vertex of the last level,
+//     first in level order;
+//   * Cuthill-McKee BFS: a level's children are ordered by (parent position,
+//     degree, id) -- claims give (parent, row offset) order, a stable sort by
+//     (parent, degree) finishes it;
+//   * the reached part is reversed, unreached vertices follow in id order.
+// ---------------------------------------------------------------------------
+__global__ void k_rcm_start(const int64_t* __restrict__ slot_base, const int64_t* __restrict__ slot_size,
+                            int32_t nslots, const uint32_t* __restrict__ order_v, const int64_t* __restrict__ rp,
+                            unsigned long long* __restrict__ key) {
+    for (int32_t j = blockIdx.y; j < nslots; j += gridDim.y) {
+        const int64_t b = slot_base[j], sz = slot_size[j];
+        unsigned long long best = ~0ull;
+        for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < sz; k += (int64_t)gridDim.x * blockDim.x) {
+            const uint32_t u = order_v[b + k];
+            const unsigned long long kk = ((unsigned long long)(rp[u + 1] - rp[u]) << 32) | u;
+            best = kk < best ? kk : best;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long t = __shfl_xor_sync(0xFFFFFFFFu, best, o);
+            best = t < best ? t : best;
+        }
+        if ((threadIdx.x & 31) == 0) atomicMin(&key[j], best);
+    }
+}
+
+// Frontier of a sweep: one start per participating slot, in slot order.
+__global__ void k_rcm_frontier(int32_t nslots, const int32_t* __restrict__ part, const int64_t* __restrict__ pos,
+                               const uint32_t* __restrict__ start, int mark, int32_t* __restrict__ F,
+                               uint8_t* __restrict__ visited, int64_t* __restrict__ fs, int64_t* __restrict__ fe,
+                               int64_t* __restrict__ qlen, int32_t* __restrict__ ecc,
+                               unsigned long long* __restrict__ cand) {
+    for (int32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < nslots; j += gridDim.x * blockDim.x) {
+        fs[j] = pos[j];
+        fe[j] = pos[j] + part[j];
+        qlen[j] = part[j];
+        ecc[j] = 0;
+        cand[j] = ~0ull;
+        if (part[j]) {
+            F[pos[j]] = (int32_t)start[j];
+            if (mark) visited[start[j]] = 1;
+        }
+    }
+}
+
+// Children in (parent, row offset) order with their parent's frontier index.
+__global__ void k_rcm_write(const int32_t* __restrict__ F, int64_t nf, const int64_t* __restrict__ D, int64_t T,
+                            const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
+                            const int32_t* __restrict__ flag, const int64_t* __restrict__ P,
+                            int32_t* __restrict__ nextF, int64_t* __restrict__ parent, uint8_t* __restrict__ visited) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < T; e += (int64_t)gridDim.x * blockDim.x) {
+        if (!flag[e]) continue;
+        const int64_t i = upper_index(D, nf, e);
+        const int64_t k = e - D[i];
+        const int32_t w = col[rp[F[i]] + k];
+        const int64_t p = P[e];
+        nextF[p] = w;
+        parent[p] = i;
+        visited[w] = 1;
+    }
+}
+
+// Last level of a slot whose next level is empty: minimum degree, first in
+// level order.
+__global__ void k_rcm_last_level(const int32_t* __restrict__ F, int64_t nf, const int64_t* __restrict__ rp,
+                                 const uint32_t* __restrict__ memb, const int32_t* __restrict__ slot_of_comm,
+                                 const int64_t* __restrict__ bbase, const int64_t* __restrict__ bend,
+                                 unsigned long long* __restrict__ cand) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nf; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t u = F[i];
+        const int32_t j = slot_of_comm[memb[u]];
+        if (bend[j] != bbase[j]) continue;
+        atomicMin(&cand[j], ((unsigned long long)(rp[u + 1] - rp[u]) << 32) | (unsigned long long)i);
+    }
+}
+
+__global__ void k_rcm_level_done(int32_t nslots, const int64_t* __restrict__ fs, const int64_t* __restrict__ fe,
+                                 const int64_t* __restrict__ bbase, const int64_t* __restrict__ bend,
+                                 const int32_t* __restrict__ F, unsigned long long* __restrict__ cand,
+                                 uint32_t* __restrict__ last_node, int32_t* __restrict__ ecc) {
+    for (int32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < nslots; j += gridDim.x * blockDim.x) {
+        if (fe[j] == fs[j]) continue;
+        if (bend[j] > bbase[j]) {
+            ++ecc[j];
+        } else if (cand[j] != ~0ull) {
+            last_node[j] = (uint32_t)F[cand[j] & 0xFFFFFFFFull];
+            cand[j] = ~0ull;
+        }
+    }
+}
+
+// George-Liu step: keep sweeping while the eccentricity grows.
+__global__ void k_rcm_gl_step(int32_t nslots, int32_t* __restrict__ part, const int32_t* __restrict__ ecc,
+                              int32_t* __restrict__ prev_ecc, const uint32_t* __restrict__ last_node,
+                              uint32_t* __restrict__ start, int32_t* __restrict__ still) {
+    for (int32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < nslots; j += gridDim.x * blockDim.x) {
+        if (!part[j]) continue;
+        if (ecc[j] <= prev_ecc[j]) {
+            part[j] = 0;
+            continue;
+        }
+        prev_ecc[j] = ecc[j];
+        start[j] = last_node[j];
+        atomicAdd(still, 1);
+    }
+}
+
+__global__ void k_rcm_keys(const int32_t* __restrict__ NF, const int64_t* __restrict__ parent, int64_t cnt,
+                           const int64_t* __restrict__ rp, int degbits, uint64_t* __restrict__ keys,
+                           uint32_t* __restrict__ vals) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < cnt; p += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t w = NF[p];
+        keys[p] = ((uint64_t)parent[p] << degbits) | (uint64_t)(rp[w + 1] - rp[w]);
+        vals[p] = (uint32_t)w;
+    }
+}
+
+__global__ void k_rcm_assign(const uint32_t* __restrict__ sorted, int64_t cnt, const uint32_t* __restrict__ memb,
+                             const int32_t* __restrict__ slot_of_comm, const int64_t* __restrict__ qlen,
+                             const int64_t* __restrict__ bbase, int32_t* __restrict__ NF,
+                             uint32_t* __restrict__ local) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < cnt; p += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t w = sorted[p];
+        const int32_t j = slot_of_comm[memb[w]];
+        NF[p] = (int32_t)w;
+        local[w] = (uint32_t)(qlen[j] + (p - bbase[j]));
+    }
+}
+
+// Reverse the reached part: local = reached - 1 - Cuthill-McKee position.
+__global__ void k_rcm_reverse(const uint32_t* __restrict__ order_v, int64_t nn, const uint32_t* __restrict__ memb,
+                              const int32_t* __restrict__ slot_of_comm, const uint8_t* __restrict__ visited,
+                              const int64_t* __restrict__ qlen, uint32_t* __restrict__ local) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nn; p += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t v = order_v[p];
+        const int32_t j = slot_of_comm[memb[v]];
+        if (j >= 0 && visited[v]) local[v] = (uint32_t)(qlen[j] - 1 - local[v]);
+    }
+}
+
+__global__ void k_rcm_init_slots(int32_t nslots, const int64_t* __restrict__ slot_size,
+                                 const unsigned long long* __restrict__ key, uint32_t* __restrict__ start,
+                                 int32_t* __restrict__ part, int32_t* __restrict__ prev_ecc) {
+    for (int32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < nslots; j += gridDim.x * blockDim.x) {
+        start[j] = (uint32_t)(key[j] & 0xFFFFFFFFull);
+        part[j] = slot_size[j] > 32 ? 1 : 0;
+        prev_ecc[j] = 0;
+    }
+}
+
+__global__ void k_max_degree_of(const int32_t* __restrict__ list, int64_t cnt, const int64_t* __restrict__ rp,
+                                unsigned long long* __restrict__ out) {
+    unsigned long long m = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < cnt; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t u = list[i];
+        const unsigned long long d = (unsigned long long)(rp[u + 1] - rp[u]);
+        m = d > m ? d : m;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long t = __shfl_xor_sync(0xFFFFFFFFu, m, o);
+        m = t > m ? t : m;
+    }
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
+}
+
+__global__ void k_fill_i32(int32_t* p, int64_t n, int32_t v) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+
 __global__ void k_gather_local(const uint32_t* __restrict__ order_v, const uint32_t* __restrict__ local_by_pos,
                                const uint8_t* __restrict__ mark, int64_t nn, uint32_t* __restrict__ local) {
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nn; p += (int64_t)gridDim.x * blockDim.x)
@@ -586,13 +764,162 @@ T read_dev(const T* p, cudaStream_t s) {
 
 }  // namespace
 
+// Reverse Cuthill-McKee for the listed communities (see the kernels above).
+// Returns the number of BFS levels run.
+int64_t rcm_communities(const DeviceCSR& g, const uint32_t* memb, const int32_t* blist, const int32_t* count_p,
+                        int32_t nslots, const uint32_t* order_v, const int64_t* offs, const int64_t* ssize,
+                        int64_t C, int64_t nn, uint32_t largest, uint32_t* local, cudaStream_t s,
+                        int64_t* launches) {
+    const int64_t n = g.n;
+    DevBuf<int32_t> slot_of_comm(C, s);
+    GB_CUDA(cudaMemsetAsync(slot_of_comm, 0xFF, C * sizeof(int32_t), s));
+    DevBuf<int64_t> slot_base(nslots, s), slot_size(nslots, s), qlen(nslots, s), fs(nslots, s), fe(nslots, s),
+        bbase(nslots, s), bend(nslots, s), pos(nslots + 1, s);
+    k_bfs_slots<<<grid_for(nslots, kT), kT, 0, s>>>(blist, count_p, order_v, offs, memb, slot_of_comm, slot_base,
+                                                    slot_size, ssize);
+    GB_LAUNCH_CHECK();
+    DevBuf<unsigned long long> key(nslots, s), cand(nslots, s);
+    GB_CUDA(cudaMemsetAsync(key, 0xFF, nslots * sizeof(unsigned long long), s));
+    {
+        dim3 grid((unsigned)std::min<int64_t>(ceil_div(largest, kT), 64), (unsigned)std::min(nslots, 65535));
+        k_rcm_start<<<grid, kT, 0, s>>>(slot_base, slot_size, nslots, order_v, g.row_ptr, key);
+        GB_LAUNCH_CHECK();
+    }
+    DevBuf<uint32_t> start(nslots, s), last_node(nslots, s);
+    DevBuf<int32_t> part(nslots, s), prev_ecc(nslots, s), ecc(nslots, s), still(1, s);
+    k_rcm_init_slots<<<grid_for(nslots, kT), kT, 0, s>>>(nslots, slot_size, key, start, part, prev_ecc);
+    GB_LAUNCH_CHECK();
+    *launches += 4;
+    DevBuf<uint8_t> visited(n, s);
+    DevBuf<unsigned long long> claim(n, s);
+    DevBuf<int32_t> F(nn + 1, s), NF(nn + 1, s);
+    DevBuf<int64_t> D(nn + 1, s), parent(nn + 1, s);
+    int64_t levels = 0;
+    // One BFS over the participating slots; Cuthill-McKee ordering when cm.
+    auto sweep = [&](bool cm) -> void {
+        exclusive_scan_i32_to_i64(part, pos, nslots, pos.get() + nslots, s);
+        const int64_t np = read_dev(pos.get() + nslots, s);
+        GB_CUDA(cudaMemsetAsync(visited, 0, n, s));
+        GB_CUDA(cudaMemsetAsync(claim, 0xFF, n * sizeof(unsigned long long), s));
+        k_rcm_frontier<<<grid_for(nslots, kT), kT, 0, s>>>(nslots, part, pos, start, cm ? 1 : 0, F, visited, fs, fe,
+                                                           qlen, ecc, cand);
+        GB_LAUNCH_CHECK();
+        *launches += 4;
+        if (cm) {
+            // the start is Cuthill-McKee position 0 of its community
+            DevBuf<uint32_t> sorted(np > 0 ? np : 1, s);
+            GB_CUDA(cudaMemsetAsync(bbase, 0, nslots * sizeof(int64_t), s));
+            GB_CUDA(cudaMemcpyAsync(sorted, F.get(), np * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+            DevBuf<int64_t> zero(nslots, s);
+            GB_CUDA(cudaMemsetAsync(zero, 0, nslots * sizeof(int64_t), s));
+            k_rcm_assign<<<grid_for(np, kT), kT, 0, s>>>(sorted, np, memb, slot_of_comm, zero, pos, F, local);
+            GB_LAUNCH_CHECK();
+            *launches += 1;
+        }
+        int64_t nf = np;
+        while (nf > 0) {
+            ++levels;
+            k_frontier_degrees<<<grid_for(nf, kT), kT, 0, s>>>(F, nf, g.row_ptr, D);
+            GB_LAUNCH_CHECK();
+            exclusive_scan_i64_total(D, D, nf, D.get() + nf, s);
+            const int64_t T = read_dev(D.get() + nf, s);
+            DevBuf<int32_t> flag(T > 0 ? T : 1, s);
+            DevBuf<int64_t> P(T + 1, s);
+            if (T > 0) {
+                k_bfs_claim<<<grid_for(T, kT), kT, 0, s>>>(F, nf, D, T, g.row_ptr, g.col, memb, visited, claim);
+                GB_LAUNCH_CHECK();
+                k_bfs_flag<<<grid_for(T, kT), kT, 0, s>>>(F, nf, D, T, g.row_ptr, g.col, memb, visited, claim, flag);
+                GB_LAUNCH_CHECK();
+                exclusive_scan_i32_to_i64(flag, P, T, P.get() + T, s);
+            } else {
+                GB_CUDA(cudaMemsetAsync(P, 0, sizeof(int64_t), s));
+            }
+            k_bfs_bases<<<grid_for(nslots, kT), kT, 0, s>>>(nslots, fs, fe, D, P, bbase, bend);
+            GB_LAUNCH_CHECK();
+            if (T > 0) {
+                k_rcm_write<<<grid_for(T, kT), kT, 0, s>>>(F, nf, D, T, g.row_ptr, g.col, flag, P, NF, parent,
+                                                           visited);
+                GB_LAUNCH_CHECK();
+            }
+            const int64_t next = T > 0 ? read_dev(P.get() + T, s) : 0;
+            if (!cm) {
+                k_rcm_last_level<<<grid_for(nf, kT), kT, 0, s>>>(F, nf, g.row_ptr, memb, slot_of_comm, bbase, bend,
+                                                                 cand);
+                GB_LAUNCH_CHECK();
+                k_rcm_level_done<<<grid_for(nslots, kT), kT, 0, s>>>(nslots, fs, fe, bbase, bend, F, cand, last_node,
+                                                                     ecc);
+                GB_LAUNCH_CHECK();
+            } else if (next > 0) {
+                // Children of one parent by (degree, id): stable sort by (parent, degree).
+                unsigned long long md = 0;
+                {
+                    DevBuf<unsigned long long> mdd(1, s);
+                    GB_CUDA(cudaMemsetAsync(mdd, 0, sizeof(unsigned long long), s));
+                    k_max_degree_of<<<grid_for(next, kT), kT, 0, s>>>(NF, next, g.row_ptr, mdd);
+                    GB_LAUNCH_CHECK();
+                    md = read_dev(mdd.get(), s);
+                }
+                const int degbits = bits_for(md);
+                const int pbits = bits_for((uint64_t)(nf > 1 ? nf - 1 : 1));
+                DevBuf<uint64_t> keys(next, s);
+                DevBuf<uint32_t> vals(next, s);
+                k_rcm_keys<<<grid_for(next, kT), kT, 0, s>>>(NF, parent, next, g.row_ptr, degbits, keys, vals);
+                GB_LAUNCH_CHECK();
+                radix_sort_pairs_u64(keys, vals, next, degbits + pbits, s);
+                k_rcm_assign<<<grid_for(next, kT), kT, 0, s>>>(vals, next, memb, slot_of_comm, qlen, bbase, NF,
+                                                               local);
+                GB_LAUNCH_CHECK();
+                *launches += 4 + 3 * ((degbits + pbits + 7) / 8);
+            }
+            k_bfs_advance<<<grid_for(nslots, kT), kT, 0, s>>>(nslots, qlen, fs, fe, bbase, bend);
+            GB_LAUNCH_CHECK();
+            *launches += 8;
+            std::swap(F.ptr, NF.ptr);
+            nf = next;
+        }
+    };
+    // George-Liu sweeps (communities above 32 vertices), at most three.
+    for (int it = 0; it < 3; ++it) {
+        int32_t np_host = 0;
+        {
+            DevBuf<int64_t> tot(1, s);
+            exclusive_scan_i32_to_i64(part, pos, nslots, tot, s);
+            np_host = (int32_t)read_dev(tot.get(), s);
+        }
+        if (np_host == 0) break;
+        sweep(false);
+        GB_CUDA(cudaMemsetAsync(still, 0, sizeof(int32_t), s));
+        k_rcm_gl_step<<<grid_for(nslots, kT), kT, 0, s>>>(nslots, part, ecc, prev_ecc, last_node, start, still);
+        GB_LAUNCH_CHECK();
+        *launches += 2;
+        if (read_dev(still.get(), s) == 0) break;
+    }
+    // Cuthill-McKee BFS from the final starts, all communities.
+    k_fill_i32<<<grid_for(nslots, kT), kT, 0, s>>>(part, nslots, 1);
+    GB_LAUNCH_CHECK();
+    sweep(true);
+    // Reverse the reached part; unreached vertices follow in vertex order.
+    k_rcm_reverse<<<grid_for(nn, kT), kT, 0, s>>>(order_v, nn, memb, slot_of_comm, visited, qlen, local);
+    GB_LAUNCH_CHECK();
+    DevBuf<int32_t> lflag(nn, s);
+    DevBuf<int64_t> R(nn + 1, s);
+    k_bfs_left_flags<<<grid_for(nn, kT), kT, 0, s>>>(order_v, nn, memb, slot_of_comm, visited, lflag);
+    GB_LAUNCH_CHECK();
+    exclusive_scan_i32_to_i64(lflag, R, nn, R.get() + nn, s);
+    k_bfs_left_assign<<<grid_for(nn, kT), kT, 0, s>>>(order_v, nn, memb, slot_of_comm, lflag, R, slot_base, qlen,
+                                                      local);
+    GB_LAUNCH_CHECK();
+    *launches += 7;
+    return levels;
+}
+
 void compose_device(const DeviceCSR& g, const uint32_t* memb, const ComposeParams& p, int32_t* new_ids,
                     gbgpu_stats* st, cudaStream_t s) {
     const int64_t n = g.n;
     if (n == 0) return;
     int intra = p.intra_order;
     if (intra == kIntraDendrogram) intra = kIntraBFS;  // Leiden has no Rabbit dendrogram (:6668-6677)
-    GB_REQUIRE(intra == kIntraBFS || intra == kIntraGorder, GBGPU_E_UNSUPPORTED,
+    GB_REQUIRE(intra == kIntraBFS || intra == kIntraGorder || intra == kIntraRCM, GBGPU_E_UNSUPPORTED,
                "intra-community order not available on the GPU path");
     const int co = p.community_order;
     GB_REQUIRE(co == kSizeDesc || co == kSizeAsc || co == kDegreeDesc || co == kDegreeAsc || co == kIdentity,
@@ -740,10 +1067,15 @@ void compose_device(const DeviceCSR& g, const uint32_t* memb, const ComposeParam
         ++launches;
     }
 
-    // ---- BFS communities ----
+    // ---- RCM: every community of two or more vertices ----
     const int32_t nbfs = hc.n[4];
     int64_t levels = 0;
-    if (nbfs > 0) {
+    if (nbfs > 0 && intra == kIntraRCM) {
+        levels = rcm_communities(g, memb, lists.get() + 4 * C, cc.get()->n + 4, nbfs, order_v, offs, ssize, C, nn,
+                                 hc.largest, local, s, &launches);
+    }
+    // ---- BFS communities ----
+    if (nbfs > 0 && intra != kIntraRCM) {
         const int32_t* blist = lists.get() + 4 * C;
         DevBuf<int32_t> slot_of_comm(C, s);
         GB_CUDA(cudaMemsetAsync(slot_of_comm, 0xFF, C * sizeof(int32_t), s));
