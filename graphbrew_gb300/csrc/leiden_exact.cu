@@ -53,7 +53,7 @@ constexpr int kCoarse = 1 << kCoarseBits;
 constexpr int kFineBits = kSlotBits - kCoarseBits;
 constexpr int kTbThreads = 1024;              // table insert / group: one window vertex per thread
 constexpr int kTbChunks = kWindowMax / kTbThreads;
-constexpr int kTbFinishThreads = 512;         // table finish: one CTA per coarse bucket
+constexpr int kTbFinishThreads = 1024;        // table finish: one CTA per coarse bucket
 constexpr uint32_t kPadSlot = 0xFFFFFFFFu;
 static_assert(kTableSlots >= 2 * kEventsMax, "hash load factor <= 1/2");
 static_assert(kCoarse <= kTbThreads, "one coarse bucket per grouping thread");
@@ -91,6 +91,7 @@ struct Ctl {
     long long error;          // nonzero: the round loop stopped without finishing
     unsigned long long tag;   // generation of the event table (slots of older tags are empty)
     unsigned int nhot;        // hot slots of the current table
+    unsigned long long tb_big; // largest coarse bucket: size << 32 | bucket (its CTA starts first)
 };
 
 struct __align__(16) SlotMeta {
@@ -405,6 +406,7 @@ __global__ void __launch_bounds__(kTbThreads) k_tb_insert(ExactState a) {
     if (blockIdx.x == 0 && tid == 0) {
         a.ctl->first_change = kNoChange;
         a.ctl->nhot = 0;
+        a.ctl->tb_big = 0;
     }
     (void)lane;
     (void)w;
@@ -484,6 +486,7 @@ __global__ void __launch_bounds__(kTbThreads) k_tb_group(ExactState a) {
         if (blockIdx.x == 0) {
             a.tb_bstart[tid] = excl;
             if (tid == kCoarse - 1) a.tb_bstart[kCoarse] = excl + tot;
+            if (tot) atomicMax(&a.ctl->tb_big, ((unsigned long long)tot << 32) | (unsigned long long)tid);
         }
     }
     for (int k = tid; k < 32 * kCoarse; k += blockDim.x) wcnt[k] = 0;
@@ -534,13 +537,17 @@ __global__ void __launch_bounds__(kTbFinishThreads) k_tb_finish(ExactState a) {
     constexpr int kFine = 1 << kFineBits;
     constexpr int kW = kTbFinishThreads / 32;
     constexpr int kRow = kFine + 1;          // padded row of per-warp digit counts
-    __shared__ int32_t wcnt[kW * kRow];
+    extern __shared__ int32_t wcnt[];   // kW x kRow per-warp digit counts (dynamic: > 48 KB)
     __shared__ int32_t digit[kFine];
     __shared__ long long warp_v[32];
     __shared__ int warp_h[32];
     const long long P = a.ctl->P;
     if (P >= a.ctl->n) return;
-    const int bs = a.tb_bstart[blockIdx.x], be = a.tb_bstart[blockIdx.x + 1];
+    // The largest bucket (the one holding a community many window vertices
+    // join) goes to CTA 0, which the scheduler starts first.
+    const int big = (int)(a.ctl->tb_big & 0xFFFFFFFFull);
+    const int bucket = blockIdx.x == 0 ? big : ((int)blockIdx.x == big ? 0 : (int)blockIdx.x);
+    const int bs = a.tb_bstart[bucket], be = a.tb_bstart[bucket + 1];
     const int cnt = be - bs;
     if (cnt == 0) return;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -1648,10 +1655,12 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     const int group_smem = 32 * kCoarse * (int)sizeof(int32_t);
     GB_CUDA(cudaFuncSetAttribute(k_tb_group, cudaFuncAttributeMaxDynamicSharedMemorySize, group_smem));
     const int tb_grid = (int)ceil_div(B, kTbThreads);
+    const int finish_smem = (kTbFinishThreads / 32) * ((1 << kFineBits) + 1) * (int)sizeof(int32_t);
+    GB_CUDA(cudaFuncSetAttribute(k_tb_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, finish_smem));
     auto enqueue_table = [&](cudaStream_t st) {
         k_tb_insert<<<tb_grid, kTbThreads, 0, st>>>(a);
         k_tb_group<<<tb_grid, kTbThreads, group_smem, st>>>(a);
-        k_tb_finish<<<kCoarse, kTbFinishThreads, 0, st>>>(a);
+        k_tb_finish<<<kCoarse, kTbFinishThreads, finish_smem, st>>>(a);
     };
     const int mid_smem = kMidWarpsPerBlock * 2 * kWarpHash * (int)sizeof(uint32_t);
     GB_CUDA(cudaFuncSetAttribute(k_ex_eval_mid, cudaFuncAttributeMaxDynamicSharedMemorySize, mid_smem));
