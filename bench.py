@@ -296,14 +296,18 @@ def main():
         for _ in range(2):
             host_step()
         t0 = time.perf_counter()
-        for _ in range(args.steps):
-            host_step()
+        host_stats = [host_step() for _ in range(args.steps)]
         t1 = time.perf_counter()
         e2e_s = (t1 - t0) / args.steps
         e2e = {"value": nnz * world / e2e_s / 1e6, "unit": "Medges/s",
                "h2d_bytes_per_step": 8 * (n + 1) + 4 * nnz,
                "d2h_bytes_per_step": 4 * n + 8 * (n + 1) + 4 * nnz,
-               "ms_per_step": e2e_s * 1e3}
+               "ms_per_step": e2e_s * 1e3,
+               "h2d_ms": float(np.median([x.h2d_ms for x in host_stats])),
+               "d2h_ms": float(np.median([x.d2h_ms for x in host_stats])),
+               "call_device_ms": float(np.median([x.total_ms for x in host_stats])),
+               "call_stages_ms": {k: float(np.median([getattr(x, k) for x in host_stats]))
+                                  for k in ("local_move_ms", "aggregate_ms", "compose_ms", "relabel_ms")}}
 
     # Stage split and the roofline of the dominant stage.  The serial-order
     # local moving is a chain of short dependent rounds (latency-bound by

@@ -71,7 +71,7 @@ class GbgpuStats(C.Structure):
                 ("aggregate_ms", C.c_double), ("compose_ms", C.c_double), ("intra_ms", C.c_double),
                 ("validate_ms", C.c_double), ("relabel_ms", C.c_double), ("h2d_ms", C.c_double),
                 ("d2h_ms", C.c_double), ("passes", C.c_int32), ("iterations", C.c_int32),
-                ("super_move_iterations", C.c_int32), ("reserved0", C.c_int32),
+                ("super_move_iterations", C.c_int32), ("super_move_ctas", C.c_int32),
                 ("super_moves", C.c_int64), ("pass0_communities", C.c_int64),
                 ("aggregated_communities", C.c_int64), ("communities", C.c_int64),
                 ("num_communities", C.c_int64), ("isolated", C.c_int64),
@@ -82,7 +82,7 @@ class GbgpuStats(C.Structure):
                 ("local_move_rounds", C.c_int64), ("local_move_evaluations", C.c_int64)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved0"}
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 # Every entry point declared in include/gbgpu.h, with its ctypes signature.

@@ -41,12 +41,14 @@ __global__ void k_max_u32(const uint32_t* __restrict__ a, int64_t n, uint32_t* _
 // Community sizes over non-isolated vertices, optional degree totals.
 __global__ void k_comm_sizes(const int64_t* __restrict__ rp, const uint32_t* __restrict__ memb, int64_t n,
                              uint32_t* __restrict__ csize, unsigned long long* __restrict__ cdeg) {
-    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t d = rp[v + 1] - rp[v];
-        if (d != 0) {
-            atomicAdd(&csize[memb[v]], 1u);
-            if (cdeg) atomicAdd(&cdeg[memb[v]], (unsigned long long)d);
-        }
+    const int lane = threadIdx.x & 31;
+    for (int64_t v0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; v0 < n;
+         v0 += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t v = v0 + lane;
+        const int64_t d = v < n ? rp[v + 1] - rp[v] : 0;
+        const uint32_t c = d ? memb[v] : 0u;
+        warp_add_u32(csize, c, 1u, d != 0);
+        if (cdeg) warp_add_u64(cdeg, c, (unsigned long long)d, d != 0);
     }
 }
 
@@ -471,32 +473,52 @@ __device__ __forceinline__ int64_t upper_index(const int64_t* __restrict__ D, in
     return lo;
 }
 
+// Frontier edges in runs of kEdgeRun consecutive edge indices per thread:
+// one binary search for the run's first edge, then the owning frontier
+// vertex advances with the edge index.
+constexpr int kEdgeRun = 8;
+
+template <typename Fn>
+__device__ __forceinline__ void for_frontier_edges(const int64_t* __restrict__ D, int64_t nf, int64_t T, Fn&& fn) {
+    for (int64_t e0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) * kEdgeRun; e0 < T;
+         e0 += (int64_t)gridDim.x * blockDim.x * kEdgeRun) {
+        int64_t i = upper_index(D, nf, e0);
+        int64_t next = D[i + 1];
+        const int64_t e1 = min(T, e0 + kEdgeRun);
+        for (int64_t e = e0; e < e1; ++e) {
+            while (e >= next) {
+                ++i;
+                next = D[i + 1];
+            }
+            fn(i, e - D[i], e);
+        }
+    }
+}
+
+inline int edge_grid(int64_t T) { return grid_for(ceil_div(T, kEdgeRun), 256); }
+
 __global__ void k_bfs_claim(const int32_t* __restrict__ F, int64_t nf, const int64_t* __restrict__ D, int64_t T,
                             const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
                             const uint32_t* __restrict__ memb, const uint8_t* __restrict__ visited,
                             unsigned long long* __restrict__ claim) {
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < T; e += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = upper_index(D, nf, e);
-        const int64_t k = e - D[i];
+    for_frontier_edges(D, nf, T, [&](int64_t i, int64_t k, int64_t) {
         const int32_t u = F[i];
         const int32_t w = col[rp[u] + k];
         if (memb[w] == memb[u] && !visited[w])
             atomicMin(&claim[w], ((unsigned long long)i << 32) | (unsigned long long)k);
-    }
+    });
 }
 
 __global__ void k_bfs_flag(const int32_t* __restrict__ F, int64_t nf, const int64_t* __restrict__ D, int64_t T,
                            const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
                            const uint32_t* __restrict__ memb, const uint8_t* __restrict__ visited,
                            const unsigned long long* __restrict__ claim, int32_t* __restrict__ flag) {
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < T; e += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = upper_index(D, nf, e);
-        const int64_t k = e - D[i];
+    for_frontier_edges(D, nf, T, [&](int64_t i, int64_t k, int64_t e) {
         const int32_t u = F[i];
         const int32_t w = col[rp[u] + k];
         flag[e] = (memb[w] == memb[u] && !visited[w] &&
                    claim[w] == (((unsigned long long)i << 32) | (unsigned long long)k)) ? 1 : 0;
-    }
+    });
 }
 
 // Per community: where its children start in the next frontier this level.
@@ -515,10 +537,8 @@ __global__ void k_bfs_write(const int32_t* __restrict__ F, int64_t nf, const int
                             const int64_t* __restrict__ P, const int32_t* __restrict__ slot_of_comm,
                             const int64_t* __restrict__ qlen, const int64_t* __restrict__ base,
                             int32_t* __restrict__ nextF, uint8_t* __restrict__ visited, uint32_t* __restrict__ local) {
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < T; e += (int64_t)gridDim.x * blockDim.x) {
-        if (!flag[e]) continue;
-        const int64_t i = upper_index(D, nf, e);
-        const int64_t k = e - D[i];
+    for_frontier_edges(D, nf, T, [&](int64_t i, int64_t k, int64_t e) {
+        if (!flag[e]) return;
         const int32_t u = F[i];
         const int32_t w = col[rp[u] + k];
         const int64_t p = P[e];
@@ -526,7 +546,7 @@ __global__ void k_bfs_write(const int32_t* __restrict__ F, int64_t nf, const int
         nextF[p] = w;
         visited[w] = 1;
         local[w] = (uint32_t)(qlen[j] + (p - base[j]));
-    }
+    });
 }
 
 __global__ void k_bfs_advance(int32_t nslots, int64_t* __restrict__ qlen, int64_t* __restrict__ fs,
@@ -618,16 +638,14 @@ __global__ void k_rcm_write(const int32_t* __restrict__ F, int64_t nf, const int
                             const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
                             const int32_t* __restrict__ flag, const int64_t* __restrict__ P,
                             int32_t* __restrict__ nextF, int64_t* __restrict__ parent, uint8_t* __restrict__ visited) {
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < T; e += (int64_t)gridDim.x * blockDim.x) {
-        if (!flag[e]) continue;
-        const int64_t i = upper_index(D, nf, e);
-        const int64_t k = e - D[i];
+    for_frontier_edges(D, nf, T, [&](int64_t i, int64_t k, int64_t e) {
+        if (!flag[e]) return;
         const int32_t w = col[rp[F[i]] + k];
         const int64_t p = P[e];
         nextF[p] = w;
         parent[p] = i;
         visited[w] = 1;
-    }
+    });
 }
 
 // Last level of a slot whose next level is empty: minimum degree, first in
@@ -826,9 +844,9 @@ int64_t rcm_communities(const DeviceCSR& g, const uint32_t* memb, const int32_t*
             DevBuf<int32_t> flag(T > 0 ? T : 1, s);
             DevBuf<int64_t> P(T + 1, s);
             if (T > 0) {
-                k_bfs_claim<<<grid_for(T, kT), kT, 0, s>>>(F, nf, D, T, g.row_ptr, g.col, memb, visited, claim);
+                k_bfs_claim<<<edge_grid(T), 256, 0, s>>>(F, nf, D, T, g.row_ptr, g.col, memb, visited, claim);
                 GB_LAUNCH_CHECK();
-                k_bfs_flag<<<grid_for(T, kT), kT, 0, s>>>(F, nf, D, T, g.row_ptr, g.col, memb, visited, claim, flag);
+                k_bfs_flag<<<edge_grid(T), 256, 0, s>>>(F, nf, D, T, g.row_ptr, g.col, memb, visited, claim, flag);
                 GB_LAUNCH_CHECK();
                 exclusive_scan_i32_to_i64(flag, P, T, P.get() + T, s);
             } else {
@@ -837,7 +855,7 @@ int64_t rcm_communities(const DeviceCSR& g, const uint32_t* memb, const int32_t*
             k_bfs_bases<<<grid_for(nslots, kT), kT, 0, s>>>(nslots, fs, fe, D, P, bbase, bend);
             GB_LAUNCH_CHECK();
             if (T > 0) {
-                k_rcm_write<<<grid_for(T, kT), kT, 0, s>>>(F, nf, D, T, g.row_ptr, g.col, flag, P, NF, parent,
+                k_rcm_write<<<edge_grid(T), 256, 0, s>>>(F, nf, D, T, g.row_ptr, g.col, flag, P, NF, parent,
                                                            visited);
                 GB_LAUNCH_CHECK();
             }
@@ -1110,14 +1128,14 @@ void compose_device(const DeviceCSR& g, const uint32_t* memb, const ComposeParam
             if (T == 0) break;
             DevBuf<int32_t> flag(T, s);
             DevBuf<int64_t> P(T + 1, s);
-            k_bfs_claim<<<grid_for(T, kT), kT, 0, s>>>(F, nf, D, T, g.row_ptr, g.col, memb, visited, claim);
+            k_bfs_claim<<<edge_grid(T), 256, 0, s>>>(F, nf, D, T, g.row_ptr, g.col, memb, visited, claim);
             GB_LAUNCH_CHECK();
-            k_bfs_flag<<<grid_for(T, kT), kT, 0, s>>>(F, nf, D, T, g.row_ptr, g.col, memb, visited, claim, flag);
+            k_bfs_flag<<<edge_grid(T), 256, 0, s>>>(F, nf, D, T, g.row_ptr, g.col, memb, visited, claim, flag);
             GB_LAUNCH_CHECK();
             exclusive_scan_i32_to_i64(flag, P, T, P.get() + T, s);
             k_bfs_bases<<<grid_for(nbfs, kT), kT, 0, s>>>(nbfs, fs, fe, D, P, bbase, bend);
             GB_LAUNCH_CHECK();
-            k_bfs_write<<<grid_for(T, kT), kT, 0, s>>>(F, nf, D, T, g.row_ptr, g.col, memb, flag, P, slot_of_comm,
+            k_bfs_write<<<edge_grid(T), 256, 0, s>>>(F, nf, D, T, g.row_ptr, g.col, memb, flag, P, slot_of_comm,
                                                        qlen, bbase, NF, visited, local);
             GB_LAUNCH_CHECK();
             k_bfs_advance<<<grid_for(nbfs, kT), kT, 0, s>>>(nbfs, qlen, fs, fe, bbase, bend);

@@ -79,6 +79,48 @@ struct DevBuf {
     operator T*() const { return ptr; }
 };
 
+#ifdef __CUDACC__
+// Warp-aggregated atomics on arrays indexed by a key (a community id): lanes
+// holding the same key combine their values and the lowest such lane issues
+// the one atomic.  All 32 lanes of the warp call; a lane with nothing to add
+// passes active = false.
+__device__ __forceinline__ unsigned warp_key_peers(uint32_t key, bool active, bool* leader) {
+    const unsigned act = __ballot_sync(0xFFFFFFFFu, active);
+    if (!active) return 0u;
+    const unsigned peers = __match_any_sync(act, key);
+    *leader = (int)(threadIdx.x & 31) == __ffs(peers) - 1;
+    return peers;
+}
+
+__device__ __forceinline__ void warp_add_u32(uint32_t* arr, uint32_t key, uint32_t val, bool active) {
+    bool leader = false;
+    const unsigned peers = warp_key_peers(key, active, &leader);
+    if (!active) return;
+    const uint32_t sum = __reduce_add_sync(peers, val);
+    if (leader) atomicAdd(&arr[key], sum);
+}
+
+// Values below 2^32 each (degrees): summed in 16-bit halves so that 32 of
+// them cannot overflow the 32-bit warp reduction.
+__device__ __forceinline__ void warp_add_u64(unsigned long long* arr, uint32_t key, unsigned long long val,
+                                             bool active) {
+    bool leader = false;
+    const unsigned peers = warp_key_peers(key, active, &leader);
+    if (!active) return;
+    const uint32_t lo = __reduce_add_sync(peers, (uint32_t)(val & 0xFFFFull));
+    const uint32_t hi = __reduce_add_sync(peers, (uint32_t)(val >> 16));
+    if (leader) atomicAdd(&arr[key], ((unsigned long long)hi << 16) + lo);
+}
+
+// Minimum of values that increase with the lane (vertex ids of a warp-aligned
+// range): the leader's own value.
+__device__ __forceinline__ void warp_min_ordered_i32(int32_t* arr, uint32_t key, int32_t val, bool active) {
+    bool leader = false;
+    warp_key_peers(key, active, &leader);
+    if (leader) atomicMin(&arr[key], val);
+}
+#endif  // __CUDACC__
+
 // Read-only view of an undirected CSR graph resident in HBM.
 struct DeviceCSR {
     int64_t n = 0;

@@ -29,6 +29,7 @@
 #include <cmath>
 #include <vector>
 
+#include "gb_chunks.cuh"
 #include "gb_common.cuh"
 #include "gb_leiden_internal.cuh"
 #include "gb_stages.h"
@@ -239,40 +240,60 @@ __global__ void k_super_weights(const int32_t* __restrict__ exists, const int64_
         if (exists[c]) sweight[cmap[c]] = (long long)ctot[c];
 }
 
-// Inter-community edges: counts per vertex, then keys in CSR order.
-__global__ void k_inter_count(const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
-                              const uint32_t* __restrict__ vcom, int64_t n, int32_t* __restrict__ cnt) {
-    const int lane = threadIdx.x & 31;
-    const int64_t wid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t u = wid; u < n; u += nw) {
-        const uint32_t cu = vcom[u];
-        int c = 0;
-        for (int64_t e = rp[u] + lane; e < rp[u + 1]; e += 32) c += (vcom[col[e]] != cu);
-        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xFFFFFFFFu, c, o);
-        if (lane == 0) cnt[u] = c;
-    }
-}
+// Inter-community edges as keys (community(u) << 32 | community(v)), one
+// entry-parallel pass: each CTA compacts its chunk's hits warp by warp and
+// reserves their slots with one atomic on the cursor.  The keys are sorted
+// next, so the order in which CTAs reserve does not reach the result.
+constexpr int kInterThreads = 256;
 
-__global__ void k_inter_fill(const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
-                             const uint32_t* __restrict__ vcom, int64_t n, const int64_t* __restrict__ off,
-                             uint64_t* __restrict__ keys) {
-    const int lane = threadIdx.x & 31;
-    const int64_t wid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+__global__ void __launch_bounds__(kInterThreads)
+k_inter_edges(const int64_t* __restrict__ rp, const int32_t* __restrict__ col, const uint32_t* __restrict__ vcom,
+              int64_t n, int64_t nnz, const int32_t* __restrict__ chunk_row, uint64_t* __restrict__ keys,
+              unsigned long long* __restrict__ cursor) {
+    constexpr int kPer = kEdgeChunk / kInterThreads;
+    __shared__ int32_t srow[kEdgeChunkPadded];
+    __shared__ int32_t wmax[kInterThreads / 32];
+    __shared__ uint32_t wcnt[kInterThreads / 32];
+    __shared__ unsigned long long base;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     const unsigned lt = (1u << lane) - 1u;
-    for (int64_t u = wid; u < n; u += nw) {
-        const uint32_t cu = vcom[u];
-        int64_t o = off[u];
-        for (int64_t e0 = rp[u]; e0 < rp[u + 1]; e0 += 32) {
-            const int64_t e = e0 + lane;
-            uint32_t cv = cu;
-            if (e < rp[u + 1]) cv = vcom[col[e]];
-            const bool hit = cv != cu;
-            const unsigned m = __ballot_sync(0xFFFFFFFFu, hit);
-            if (hit) keys[o + __popc(m & lt)] = ((uint64_t)cu << 32) | cv;
-            o += __popc(m);
+    const int64_t chunks = (nnz + kEdgeChunk - 1) / kEdgeChunk;
+    for (int64_t c = blockIdx.x; c < chunks; c += gridDim.x) {
+        const int64_t e0 = c * kEdgeChunk, e1 = min(nnz, e0 + kEdgeChunk);
+        chunk_entry_rows<kInterThreads>(rp, n, chunk_row[c], e0, e1, srow, wmax);
+        uint64_t key[kPer];
+        unsigned hits[kPer];
+        uint32_t cnt = 0;
+#pragma unroll
+        for (int k = 0; k < kPer; ++k) {
+            const int i = k * kInterThreads + t;
+            bool hit = false;
+            key[k] = 0;
+            if (e0 + i < e1) {
+                const uint32_t cu = vcom[srow[chunk_pad(i)]];
+                const uint32_t cv = vcom[col[e0 + i]];
+                hit = cu != cv;
+                key[k] = ((uint64_t)cu << 32) | cv;
+            }
+            hits[k] = __ballot_sync(0xFFFFFFFFu, hit);
+            cnt += __popc(hits[k]);
         }
+        if (lane == 0) wcnt[warp] = cnt;
+        __syncthreads();
+        if (t == 0) {
+            unsigned long long tot = 0;
+            for (int w = 0; w < kInterThreads / 32; ++w) tot += wcnt[w];
+            base = tot ? atomicAdd(cursor, tot) : 0ull;
+        }
+        __syncthreads();
+        unsigned long long o = base;
+        for (int w = 0; w < warp; ++w) o += wcnt[w];
+#pragma unroll
+        for (int k = 0; k < kPer; ++k) {
+            if ((hits[k] >> lane) & 1u) keys[o + __popc(hits[k] & lt)] = key[k];
+            o += __popc(hits[k]);
+        }
+        __syncthreads();  // srow, wcnt and base are reused by the next chunk
     }
 }
 
@@ -341,6 +362,22 @@ __global__ void k_big_super_emit(const uint32_t* __restrict__ active, int64_t na
         if (flag[i]) out[pos[i]] = active[i];
 }
 
+// light[b] = 1 when batch b has at most kLightNodes super-nodes, each of
+// degree <= kLightDeg (constants defined with the cluster kernel).
+__global__ void k_batch_light(const uint32_t* __restrict__ active, const int64_t* __restrict__ bstart,
+                              const int64_t* __restrict__ soff, int64_t nbatch, int max_nodes, int max_deg,
+                              uint8_t* __restrict__ light) {
+    for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < nbatch; b += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t lo = bstart[b], hi = bstart[b + 1];
+        bool ok = hi - lo <= max_nodes;
+        for (int64_t i = lo; ok && i < hi; ++i) {
+            const uint32_t c = active[i];
+            ok = soff[c + 1] - soff[c] <= max_deg;
+        }
+        light[b] = ok ? 1 : 0;
+    }
+}
+
 struct SmArgs {
     const int64_t* soff;
     const uint32_t* snbr;
@@ -363,6 +400,9 @@ struct SmArgs {
     uint32_t* bkeys;              // per-CTA global tables
     uint32_t* bvals;
     int64_t bcap;
+    // Batches of at most kLightNodes super-nodes of degree <= kLightDeg: one
+    // thread per super-node on the cluster's first CTA.
+    const uint8_t* light;
 };
 
 constexpr int kSmSmall = 256;     // per-warp shared table slots
@@ -442,7 +482,8 @@ __device__ __forceinline__ void super_commit(const SmArgs& a, uint32_t c, int* m
 // phase are visible to the next.  A warp keeps its proposals in shared
 // memory and its lanes commit them after the barrier; small super-nodes use
 // a shared table that also caches each candidate's total at insertion.
-constexpr int kSmCluster = 8;
+constexpr int kSmCluster = 8;     // portable cluster size
+constexpr int kSmClusterMax = 16; // non-portable size, used where the GPU can place it
 constexpr int kSmPerWarp = 16;    // proposals a warp keeps per batch (4096 / (8 x 32))
 constexpr int kBigSuper = 1024;   // super-nodes with more neighbours: one CTA each
 
@@ -578,6 +619,74 @@ __device__ void super_propose_block(const SmArgs& a, uint32_t c, SmProposal* out
     __syncthreads();
 }
 
+constexpr int kLightDeg = 8;
+constexpr int kLightNodes = 1024;
+
+// Proposal for a super-node of degree <= kLightDeg by one thread: the same
+// candidates, weights, totals and arithmetic as super_propose_cached, with
+// the table replaced by a first-occurrence merge in registers.  scomm and
+// sctot are read through L2 (they change between batches of one CTA).
+__device__ void super_propose_light(const SmArgs& a, uint32_t c, SmProposal& out) {
+    const int64_t b = a.soff[c];
+    const int deg = (int)(a.soff[c + 1] - b);
+    const uint32_t d = __ldcg(&a.scomm[c]);
+    const long long kcl = a.sweight[c];
+    const unsigned long long sd_raw = __ldcg(&a.sctot[d]);
+    uint32_t key[kLightDeg], wsum[kLightDeg];
+#pragma unroll
+    for (int k = 0; k < kLightDeg; ++k) {
+        key[k] = kNone;
+        wsum[k] = 0;
+        if (k < deg) {
+            key[k] = __ldcg(&a.scomm[a.snbr[b + k]]);
+            wsum[k] = a.sw[b + k];
+        }
+    }
+    // Weights onto first occurrences; later duplicates become empty.
+#pragma unroll
+    for (int k = 1; k < kLightDeg; ++k) {
+#pragma unroll
+        for (int j = 0; j < k; ++j) {
+            if (key[k] != kNone && key[j] == key[k]) {
+                wsum[j] += wsum[k];
+                key[k] = kNone;
+            }
+        }
+    }
+    unsigned long long se_raw[kLightDeg];
+#pragma unroll
+    for (int k = 0; k < kLightDeg; ++k) se_raw[k] = key[k] != kNone && key[k] != d ? __ldcg(&a.sctot[key[k]]) : 0ull;
+    uint32_t kc_to_d_w = 0;
+#pragma unroll
+    for (int k = 0; k < kLightDeg; ++k)
+        if (key[k] == d) kc_to_d_w = wsum[k];
+    const double kc = (double)kcl;
+    const double sigma_d = (double)(long long)sd_raw;
+    const double removal = __ddiv_rn(__dmul_rn(__dmul_rn(a.R, kc), __dsub_rn(sigma_d, kc)), a.M);
+    const double kc_to_d = (double)kc_to_d_w;
+    double best_d = 0.0;
+    uint32_t best_c = d;
+#pragma unroll
+    for (int k = 0; k < kLightDeg; ++k) {
+        const uint32_t ek = key[k];
+        if (ek == kNone) continue;
+        double add;
+        if (ek == d) {
+            add = __dsub_rn(kc_to_d, removal);
+        } else {
+            const double se = (double)(long long)se_raw[k];
+            add = __dsub_rn((double)wsum[k], __ddiv_rn(__dmul_rn(__dmul_rn(a.R, kc), se), a.M));
+        }
+        const double dl = __dadd_rn(__dsub_rn(add, removal), kc_to_d);
+        if (better(dl, ek, best_d, best_c)) { best_d = dl; best_c = ek; }
+    }
+    out.c = c;
+    out.d = d;
+    out.best = best_c;
+    out.kc = kcl;
+    out.delta = best_d;
+}
+
 __global__ void __launch_bounds__(1024)
 k_super_move_cluster(SmArgs a, int max_iter, int* iters_out, long long* moves_out, int* gmoves) {
     extern __shared__ uint32_t sm_smem[];   // 32 warps x (keys, vals, totals) x kSmSmall
@@ -593,9 +702,33 @@ k_super_move_cluster(SmArgs a, int max_iter, int* iters_out, long long* moves_ou
     long long total_moves = 0;
     int it = 0;
     for (; it < max_iter; ++it) {
+        // Runs of light batches are done by CTA 0 alone, CTA barriers between
+        // propose and commit; the cluster barrier before the next heavy batch
+        // (or the iteration's move count) publishes them to the other CTAs.
+        bool light_pending = false;
         for (int64_t bt = 0; bt < a.nbatch; ++bt) {
             const int64_t lo = a.bstart[bt], hi = a.bstart[bt + 1];
             if (lo == hi) continue;
+            if (a.light[bt]) {
+                light_pending = true;
+                if (blockIdx.x != 0) continue;
+                SmProposal pr;
+                const int64_t i = lo + threadIdx.x;
+                if (i < hi) super_propose_light(a, a.active[i], pr);
+                __syncthreads();
+                if (i < hi && pr.best != pr.d && pr.delta > 0.0) {
+                    atomicAdd(&a.sctot[pr.d], (unsigned long long)(-pr.kc));
+                    atomicAdd(&a.sctot[pr.best], (unsigned long long)pr.kc);
+                    a.scomm[pr.c] = pr.best;
+                    atomicAdd(&gmoves[it], 1);
+                }
+                __syncthreads();
+                continue;
+            }
+            if (light_pending) {
+                cluster_sync_all();
+                light_pending = false;
+            }
             // Warps: super-nodes up to kBigSuper neighbours.
             int kept = 0;
             for (int64_t i = lo + gw; i < hi; i += gnw) {
@@ -646,6 +779,7 @@ k_super_move_cluster(SmArgs a, int max_iter, int* iters_out, long long* moves_ou
                 for (int64_t j = blo + blockIdx.x; j < bhi; j += gridDim.x) super_commit(a, a.big_active[j], &gmoves[it]);
             cluster_sync_all();
         }
+        if (light_pending) cluster_sync_all();
         const int m = atomicAdd(&gmoves[it], 0);
         total_moves += m;
         if (m == 0) { ++it; break; }
@@ -677,10 +811,16 @@ __global__ void k_super_commit_batch(SmArgs a, int64_t bt, int* moves) {
 // Map back and first-occurrence renumber (:2389-2419).
 __global__ void k_remap(uint32_t* __restrict__ vcom, int64_t n, const uint32_t* __restrict__ scomm,
                         int32_t* __restrict__ firstpos) {
-    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t c = scomm[vcom[v]];
-        vcom[v] = c;
-        atomicMin(&firstpos[c], (int32_t)v);
+    const int lane = threadIdx.x & 31;
+    for (int64_t v0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; v0 < n;
+         v0 += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t v = v0 + lane;
+        uint32_t c = 0;
+        if (v < n) {
+            c = scomm[vcom[v]];
+            vcom[v] = c;
+        }
+        warp_min_ordered_i32(firstpos, c, (int32_t)v, v < n);
     }
 }
 
@@ -698,9 +838,12 @@ __global__ void k_first_apply(uint32_t* __restrict__ vcom, int64_t n, const int3
 
 __global__ void k_ctot_from_members(const int64_t* __restrict__ rp, const uint32_t* __restrict__ vcom, int64_t n,
                                     unsigned long long* __restrict__ ctot) {
-    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t d = rp[v + 1] - rp[v];
-        if (d) atomicAdd(&ctot[vcom[v]], (unsigned long long)d);
+    const int lane = threadIdx.x & 31;
+    for (int64_t v0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; v0 < n;
+         v0 += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t v = v0 + lane;
+        const int64_t d = v < n ? rp[v + 1] - rp[v] : 0;
+        warp_add_u64(ctot, d ? vcom[v] : 0u, (unsigned long long)d, d != 0);
     }
 }
 
@@ -754,6 +897,38 @@ float elapsed(cudaEvent_t a, cudaEvent_t b) {
 }  // namespace
 
 double auto_resolution_device(const int64_t* row_ptr, int64_t n, int64_t nnz, cudaStream_t s);
+
+// Cluster size of the super-move: 16 CTAs where the GPU can place such a
+// cluster of 1,024-thread CTAs with this much shared memory, else 8.
+// The result does not depend on it (proposals read the batch's frozen state;
+// commits are integer atomics on distinct super-nodes).
+int probe_super_cluster_size(int smem) {
+    int size = kSmCluster;
+    if (cudaFuncSetAttribute(k_super_move_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+        cudaSuccess) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(kSmClusterMax);
+        cfg.blockDim = dim3(1024);
+        cfg.dynamicSmemBytes = smem;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = kSmClusterMax;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int clusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&clusters, k_super_move_cluster, &cfg) == cudaSuccess && clusters > 0)
+            size = kSmClusterMax;
+    }
+    cudaGetLastError();
+    return size;
+}
+
+int super_cluster_size(int smem) {
+    static const int size = probe_super_cluster_size(smem);   // smem is the same constant on every call
+    return size;
+}
 
 void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gbgpu_stats* st, cudaStream_t s) {
     const int64_t n = g.n;
@@ -879,8 +1054,13 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
     int total_iters = 0;
     int64_t pass0_comms = 0, aggregated = 0, super_moves = 0;
     int super_iters = 0;
+    int super_ctas = 0;
     DevBuf<int32_t> exists(n, s);
     DevBuf<int64_t> cmap(n + 1, s);
+    DevBuf<int32_t> chunk_row(std::max<int64_t>(1, edge_chunks(g.nnz)), s);
+    DevBuf<unsigned long long> inter_cursor(1, s);
+    chunk_rows_device(g.row_ptr, n, g.nnz, chunk_row, s);
+    ++launches;
     for (; pass < p.max_passes && M > 0; ++pass) {
         GB_CUDA(cudaEventRecord(ea, s));
         const int iters = local_move(tolerance);
@@ -908,22 +1088,22 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
         launches += 2;
 
         // Super-graph adjacency (inter-community edges only, :2184-2224).
-        DevBuf<int32_t> icnt(n, s);
-        DevBuf<int64_t> ioff(n + 1, s);
-        k_inter_count<<<grid_for(n * 32, kT), kT, 0, s>>>(g.row_ptr, g.col, vcom, n, icnt);
-        GB_LAUNCH_CHECK();
-        exclusive_scan_i32_to_i64(icnt, ioff, n, ioff.get() + n, s);
-        const int64_t ninter = read_dev(ioff.get() + n, s);
-        launches += 4;
-        DevBuf<uint64_t> ikeys(ninter, s);
+        DevBuf<uint64_t> ikeys(g.nnz > 0 ? g.nnz : 1, s);
+        int64_t ninter = 0;
+        if (g.nnz > 0) {
+            GB_CUDA(cudaMemsetAsync(inter_cursor, 0, sizeof(unsigned long long), s));
+            k_inter_edges<<<grid_for(edge_chunks(g.nnz), 1), kInterThreads, 0, s>>>(
+                g.row_ptr, g.col, vcom, n, g.nnz, chunk_row, ikeys, inter_cursor);
+            GB_LAUNCH_CHECK();
+            ninter = (int64_t)read_dev(inter_cursor.get(), s);
+            launches += 1;
+        }
         DevBuf<int32_t> sdeg(C, s);
         DevBuf<int64_t> soff(C + 1, s);
         GB_CUDA(cudaMemsetAsync(sdeg, 0, C * sizeof(int32_t), s));
         DevBuf<uint32_t> snbr, sw;
         int64_t nuniq = 0;
         if (ninter > 0) {
-            k_inter_fill<<<grid_for(n * 32, kT), kT, 0, s>>>(g.row_ptr, g.col, vcom, n, ioff, ikeys);
-            GB_LAUNCH_CHECK();
             const int cb = bits_for((uint64_t)(C > 0 ? C - 1 : 0));
             radix_sort_keys_u64(ikeys, ninter, 32 + cb, s);
             DevBuf<int32_t> uflag(ninter, s);
@@ -939,7 +1119,7 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
             GB_LAUNCH_CHECK();
             k_rle_weights<<<grid_for(nuniq, kT), kT, 0, s>>>(ustart, nuniq, ninter, sw);
             GB_LAUNCH_CHECK();
-            launches += 8 + 3 * ((32 + cb + 7) / 8);
+            launches += 7 + 3 * ((32 + cb + 7) / 8);
         }
         {
             // soff = exclusive scan of sdeg (int32 -> int64)
@@ -1008,31 +1188,39 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
                 GB_LAUNCH_CHECK();
                 launches += 6;
             }
-            DevBuf<uint32_t> bk(single && nbig ? (int64_t)kSmCluster * bcap : 1, s);
-            DevBuf<uint32_t> bv(single && nbig ? (int64_t)kSmCluster * bcap : 1, s);
+            const int cluster = super_cluster_size(sm_smem);
+            DevBuf<uint32_t> bk(single && nbig ? (int64_t)cluster * bcap : 1, s);
+            DevBuf<uint32_t> bv(single && nbig ? (int64_t)cluster * bcap : 1, s);
             // Per-warp global tables for super-nodes above kSmSmall / 2 neighbours,
             // capped at 512 MB in total.
-            int64_t nwarps_total = single ? (int64_t)kSmCluster * 32 : (int64_t)kNumSMs * 4 * 8;
+            int64_t nwarps_total = single ? (int64_t)cluster * 32 : (int64_t)kNumSMs * 4 * 8;
             if (!single && gcap > kSmSmall)
                 nwarps_total = std::max<int64_t>(8, std::min<int64_t>(nwarps_total, ((int64_t)1 << 26) / gcap) / 8 * 8);
             DevBuf<uint32_t> gk(gcap > kSmSmall ? nwarps_total * gcap : 1, s);
             DevBuf<uint32_t> gv(gcap > kSmSmall ? nwarps_total * gcap : 1, s);
+            DevBuf<uint8_t> light(nbatch, s);
+            if (single) {
+                k_batch_light<<<grid_for(nbatch, kT), kT, 0, s>>>(active, bstart, soff, nbatch, kLightNodes, kLightDeg,
+                                                                 light);
+                GB_LAUNCH_CHECK();
+                ++launches;
+            }
             SmArgs sa{soff, snbr, sw, sweight, scomm, sctot, active, bstart, nbatch, proposed, pdelta, M, R,
                       gk, gv, gcap > kSmSmall ? gcap : 0, big_active.get(), bigstart.get(), bk.get(), bv.get(),
-                      bcap};
+                      bcap, light.get()};
             DevBuf<int> iters_d(1, s), gmoves(super_max_iter, s);
             DevBuf<long long> moves_d(1, s);
             launches += 2;
             if (single) {
                 GB_CUDA(cudaMemsetAsync(gmoves, 0, super_max_iter * sizeof(int), s));
                 cudaLaunchConfig_t cfg = {};
-                cfg.gridDim = dim3(kSmCluster);
+                cfg.gridDim = dim3(cluster);
                 cfg.blockDim = dim3(1024);
                 cfg.dynamicSmemBytes = sm_smem;
                 cfg.stream = s;
                 cudaLaunchAttribute attr[1];
                 attr[0].id = cudaLaunchAttributeClusterDimension;
-                attr[0].val.clusterDim.x = kSmCluster;
+                attr[0].val.clusterDim.x = cluster;
                 attr[0].val.clusterDim.y = 1;
                 attr[0].val.clusterDim.z = 1;
                 cfg.attrs = attr;
@@ -1042,6 +1230,7 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
                 long long* mvp = moves_d.get();
                 GB_CUDA(cudaLaunchKernelEx(&cfg, k_super_move_cluster, sa, super_max_iter, itp, mvp, gm));
                 GB_LAUNCH_CHECK();
+                super_ctas = cluster;
                 ++launches;
                 super_iters += read_dev(iters_d.get(), s);
                 super_moves += read_dev(moves_d.get(), s);
@@ -1114,6 +1303,7 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
         st->passes = pass + 1;
         st->iterations = total_iters;
         st->super_move_iterations = super_iters;
+        st->super_move_ctas = super_ctas;
         st->super_moves = super_moves;
         st->pass0_communities = pass0_comms;
         st->aggregated_communities = aggregated;

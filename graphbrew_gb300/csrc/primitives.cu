@@ -3,6 +3,7 @@
 // All of these are bandwidth-bound integer passes: tiles of 2048 elements per
 // 256-thread CTA, coalesced loads, shared-memory staging, grid sizes set by
 // the element count.
+#include "gb_chunks.cuh"
 #include "gb_common.cuh"
 
 namespace gb {
@@ -247,7 +248,20 @@ __global__ void k_degrees(const int64_t* __restrict__ rp, int64_t* __restrict__ 
         deg[i] = rp[i + 1] - rp[i];
 }
 
+__global__ void k_chunk_rows(const int64_t* __restrict__ rp, int64_t n, int32_t* __restrict__ chunk_row) {
+    for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t b = rp[u], e = rp[u + 1];
+        for (int64_t c = (b + kEdgeChunk - 1) / kEdgeChunk; c * kEdgeChunk < e; ++c) chunk_row[c] = (int32_t)u;
+    }
+}
+
 }  // namespace
+
+void chunk_rows_device(const int64_t* row_ptr, int64_t n, int64_t nnz, int32_t* chunk_row, cudaStream_t s) {
+    if (n <= 0 || nnz <= 0) return;
+    k_chunk_rows<<<grid_for(n, 256), 256, 0, s>>>(row_ptr, n, chunk_row);
+    GB_LAUNCH_CHECK();
+}
 
 void exclusive_scan_i64(const int64_t* in, int64_t* out, int64_t n, cudaStream_t s) {
     exclusive_scan_impl<int64_t>(in, out, n, nullptr, s);

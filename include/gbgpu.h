@@ -95,7 +95,7 @@ typedef struct {
     int32_t passes;
     int32_t iterations;
     int32_t super_move_iterations;
-    int32_t reserved0;
+    int32_t super_move_ctas;      // CTAs of the super-move thread-block cluster (0: batched launches)
     int64_t super_moves;
     int64_t pass0_communities;
     int64_t aggregated_communities;

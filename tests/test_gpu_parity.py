@@ -86,11 +86,93 @@ def test_validate_permutation(ctx):
     assert ctx.validate_permutation(big) == 2
 
 
+def test_relabel_every_row_class(ctx):
+    """Rows on both sides of each relabel class boundary (thread 16, warp 256,
+    256-thread CTA 2,048, 1,024-thread CTA 16,384, global sort above)."""
+    rng = np.random.default_rng(11)
+    n = 60000
+    src, dst = [], []
+    for hub, d in enumerate([16, 17, 256, 257, 2048, 2049, 16384, 16385, 30000, 5000, 700]):
+        nb = rng.choice(np.arange(20, n), d, replace=False)
+        src.append(np.full(d, hub))
+        dst.append(nb)
+    e = rng.integers(20, n, size=(200000, 2))
+    src.append(e[:, 0])
+    dst.append(e[:, 1])
+    s_ = np.concatenate(src + dst)
+    d_ = np.concatenate(dst + src)
+    keep = s_ != d_
+    key = np.unique(s_[keep].astype(np.int64) * n + d_[keep])
+    rows, cols = key // n, (key % n).astype(np.int32)
+    rp = np.zeros(n + 1, dtype=np.int64)
+    np.add.at(rp, rows + 1, 1)
+    rp = np.cumsum(rp)
+    deg = np.diff(rp)
+    for d in (16, 17, 256, 257, 2048, 2049, 16384, 16385):
+        assert d in set(deg[:11].tolist())
+    ids = rng.permutation(n).astype(np.int32)
+    orp, ocol, _ = ctx.relabel_by_mapping(rp, cols, ids)
+    erp, ecol = po.relabel(rp, cols, ids)
+    np.testing.assert_array_equal(orp, erp)
+    np.testing.assert_array_equal(ocol, ecol)
+
+
 def test_relabel_rejects_non_permutation(ctx):
     rp = np.array([0, 1, 2], dtype=np.int64)
     col = np.array([1, 0], dtype=np.int32)
     with pytest.raises(RuntimeError, match="duplicate"):
         ctx.relabel_by_mapping(rp, col, np.array([0, 0], dtype=np.int32))
+
+
+def _chunked_graph():
+    """Valid squished CSR whose rows cross the input check's 4096-entry
+    chunks, with runs of empty rows and a row that starts exactly on a chunk
+    boundary after a row ending in a larger id."""
+    rng = np.random.default_rng(7)
+    n = 50000
+    deg = rng.integers(0, 40, n)
+    deg[100:5000] = 0
+    deg[7] = 9000
+    rp = np.zeros(n + 1, dtype=np.int64)
+    rp[1:] = np.cumsum(deg)
+    # Move degree so that some row begins at entry 4096 * 3.
+    k = int(np.searchsorted(rp, 4096 * 3))
+    shift = 4096 * 3 - int(rp[k - 1])
+    deg[k - 1] = shift
+    rp[1:] = np.cumsum(deg)
+    col = np.concatenate([np.sort(rng.choice(n, int(d), replace=False)) for d in deg]).astype(np.int32)
+    return rp, col, k - 1
+
+
+def test_input_check_accepts_and_rejects(ctx):
+    rp, col, row = _chunked_graph()
+    assert 4096 * 3 in set(rp.tolist())
+    ctx.connected_components(rp, col)
+    dcol = torch.from_numpy(col).cuda()
+    ctx.connected_components(torch.from_numpy(rp).cuda(), dcol)
+    # One descending pair inside a row, right across a chunk boundary.
+    assert 4096 * 5 not in set(rp.tolist())
+    bad = col.copy()
+    bad[4096 * 5] = bad[4096 * 5 - 1]
+    with pytest.raises(ValueError, match="sorted ascending"):
+        ctx.connected_components(rp, bad)
+    bad = col.copy()
+    bad[-1] = len(rp) - 1
+    with pytest.raises(ValueError, match="out of range"):
+        ctx.connected_components(rp, bad)
+    bad = col.copy()
+    bad[4096 * 2 + 5] = -3
+    with pytest.raises(ValueError, match="out of range"):
+        ctx.connected_components(rp, bad)
+    small = np.array([0, 2, 3, 4], dtype=np.int64)
+    with pytest.raises(ValueError, match="sorted ascending"):
+        ctx.connected_components(small, np.array([2, 1, 0, 0], dtype=np.int32))
+    with pytest.raises(ValueError, match="sorted ascending"):
+        ctx.connected_components(small, np.array([1, 1, 0, 0], dtype=np.int32))
+    with pytest.raises(ValueError, match="row offsets"):
+        ctx.connected_components(np.array([0, 3, 1, 4], dtype=np.int64), np.array([0, 1, 2, 0], dtype=np.int32))
+    with pytest.raises(ValueError, match="row offsets"):
+        ctx.connected_components(np.array([1, 2, 3, 4], dtype=np.int64), np.array([1, 2, 0, 0], dtype=np.int32))
 
 
 @pytest.mark.parametrize("name", case_names())
