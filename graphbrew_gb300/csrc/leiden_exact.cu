@@ -930,7 +930,8 @@ __global__ void __launch_bounds__(kSmallWarpsPerBlock * 32) k_ex_eval_small(Exac
 
 // Big rows (kWarpMaxDeg < degree <= kBigMaxDeg): one CTA per row, table in
 // shared memory, candidates compacted, lookups of four per thread interleaved.
-__global__ void __launch_bounds__(kBigThreads) k_ex_eval_big(ExactState a) {
+// Three CTAs per SM (registers capped near 80): more lookups in flight.
+__global__ void __launch_bounds__(kBigThreads, 3) k_ex_eval_big(ExactState a) {
     extern __shared__ uint32_t big_smem[];
     uint32_t* tk = big_smem;                      // kBigSlots keys
     uint32_t* tv = tk + kBigSlots;                // kBigSlots counts
@@ -1135,8 +1136,8 @@ __global__ void __launch_bounds__(kHubThreads2) k_ex_hub_accum(ExactState a) {
 
 // Hub selection: one CTA per kTabSeg-slot segment of a window hub's table,
 // one slot per thread; the last CTA of a hub reduces the partial maxima and
-// records the decision.
-__global__ void __launch_bounds__(kHubThreads2) k_ex_hub_select(ExactState a) {
+// records the decision.  Three CTAs per SM, as for the big rows.
+__global__ void __launch_bounds__(kHubThreads2, 3) k_ex_hub_select(ExactState a) {
     if (a.ctl->P >= a.ctl->n) return;
     const Round r = round_view(a);
     const long long q0 = a.ctl->ts0, q1 = a.ctl->ts1;

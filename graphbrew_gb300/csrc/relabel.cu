@@ -122,14 +122,28 @@ __global__ void k_relabel_rows_warp(const int64_t* __restrict__ rp, const int32_
 // One CTA per row: remap into shared memory, then a stable LSD radix sort of
 // the new ids in shared memory, 8 bits per pass.  Warp w owns the w-th
 // contiguous segment of the row; a pass counts each warp's digits
-// (match_any, no atomics), scans the digit-major / warp-minor counts, and
+// (no atomics), scans the digit-major / warp-minor counts, and
 // scatters every warp's segment in order, so equal digits keep their order.
+// Ranks among a warp's 32 lanes come from a ballot multisplit.
 // kThreads = 256 for rows up to kMidRowMax, 1024 up to kBlockRowMax.
 constexpr int kRadixBins = 256;
 
 template <int kThreads, int kMaxRow>
 constexpr int radix_row_smem() {
     return (2 * kMaxRow + kRadixBins * (kThreads / 32) * 33 / 32) * (int)sizeof(int32_t);
+}
+
+// Lanes of the warp holding the same 8-bit digit as this lane, by eight
+// ballots (a multisplit; cheaper than __match_any_sync here).
+__device__ __forceinline__ unsigned digit_peers8(int dig, unsigned valid) {
+    unsigned p = valid;
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+        const bool bit = (dig >> b) & 1;
+        const unsigned bal = __ballot_sync(0xFFFFFFFFu, bit);
+        p &= bit ? bal : ~bal;
+    }
+    return p;
 }
 
 // Counts are padded one word per 32 so that the scan's per-thread runs of
@@ -170,7 +184,7 @@ k_relabel_rows_block(const int64_t* __restrict__ rp, const int32_t* __restrict__
             for (int i0 = lo; i0 < hi; i0 += 32) {
                 const int i = i0 + lane;
                 const int dig = i < hi ? (src[i] >> shift) & (kRadixBins - 1) : -1;
-                const unsigned peers = __match_any_sync(0xFFFFFFFFu, dig);
+                const unsigned peers = digit_peers8(dig, __ballot_sync(0xFFFFFFFFu, dig >= 0));
                 if (dig >= 0 && lane == __ffs(peers) - 1) H[hpad(dig * kW + w)] += __popc(peers);
                 __syncwarp();
             }
@@ -203,7 +217,7 @@ k_relabel_rows_block(const int64_t* __restrict__ rp, const int32_t* __restrict__
                 const int i = i0 + lane;
                 const int32_t v = i < hi ? src[i] : 0;
                 const int dig = i < hi ? (v >> shift) & (kRadixBins - 1) : -1;
-                const unsigned peers = __match_any_sync(0xFFFFFFFFu, dig);
+                const unsigned peers = digit_peers8(dig, __ballot_sync(0xFFFFFFFFu, dig >= 0));
                 if (dig >= 0) dst[H[hpad(dig * kW + w)] + __popc(peers & lt)] = v;
                 __syncwarp();
                 if (dig >= 0 && lane == __ffs(peers) - 1) H[hpad(dig * kW + w)] += __popc(peers);

@@ -883,6 +883,323 @@ static int intra_gorder(const orc_graph *g, const uint32_t *verts, int64_t sz, u
 }
 
 /* ------------------------------------------------------------------------ */
+/* Sorted intra orders (RG:6759-6955): HubSort, DegreeAsc, Hub2, Alternate,  */
+/* BoundaryLast and CoreOrder each std::sort the community's vertices        */
+/* (vertex order to start with) by a per-vertex comparator.  std::sort is    */
+/* not stable, so the order of ties is whatever the standard library's       */
+/* sort leaves; the reference is built against libstdc++ (GCC 13), whose    */
+/* published algorithm is restated here (bits/stl_algo.h: __sort,           */
+/* __introsort_loop, __unguarded_partition_pivot, __move_median_to_first,   */
+/* __unguarded_partition, __final_insertion_sort, __insertion_sort,         */
+/* __unguarded_linear_insert; bits/stl_heap.h: __make_heap, __sort_heap,    */
+/* __adjust_heap, __push_heap): an introsort with a depth limit of          */
+/* 2 floor(log2 n), median-of-three pivot moved to the front, an unguarded  */
+/* Hoare partition, heap sort when the depth limit runs out, and a final    */
+/* insertion sort with threshold 16.  Each comparator is encoded as a       */
+/* 64-bit key with comp(a, b) = key[a] < key[b].                            */
+/* ------------------------------------------------------------------------ */
+#define LS_THRESHOLD 16
+
+static inline int ls_less(const uint64_t *key, uint32_t a, uint32_t b) { return key[a] < key[b]; }
+static inline void ls_swap(uint32_t *x, uint32_t *y) { const uint32_t t = *x; *x = *y; *y = t; }
+
+static void ls_move_median_to_first(uint32_t *result, uint32_t *a, uint32_t *b, uint32_t *c,
+                                    const uint64_t *key)
+{
+    if (ls_less(key, *a, *b)) {
+        if (ls_less(key, *b, *c)) ls_swap(result, b);
+        else if (ls_less(key, *a, *c)) ls_swap(result, c);
+        else ls_swap(result, a);
+    } else if (ls_less(key, *a, *c)) {
+        ls_swap(result, a);
+    } else if (ls_less(key, *b, *c)) {
+        ls_swap(result, c);
+    } else {
+        ls_swap(result, b);
+    }
+}
+
+static uint32_t *ls_unguarded_partition(uint32_t *first, uint32_t *last, const uint32_t *pivot,
+                                        const uint64_t *key)
+{
+    for (;;) {
+        while (ls_less(key, *first, *pivot)) ++first;
+        --last;
+        while (ls_less(key, *pivot, *last)) --last;
+        if (!(first < last)) return first;
+        ls_swap(first, last);
+        ++first;
+    }
+}
+
+static void ls_push_heap(uint32_t *first, int64_t hole, int64_t top, uint32_t value, const uint64_t *key)
+{
+    int64_t parent = (hole - 1) / 2;
+    while (hole > top && ls_less(key, first[parent], value)) {
+        first[hole] = first[parent];
+        hole = parent;
+        parent = (hole - 1) / 2;
+    }
+    first[hole] = value;
+}
+
+static void ls_adjust_heap(uint32_t *first, int64_t hole, int64_t len, uint32_t value, const uint64_t *key)
+{
+    const int64_t top = hole;
+    int64_t child = hole;
+    while (child < (len - 1) / 2) {
+        child = 2 * (child + 1);
+        if (ls_less(key, first[child], first[child - 1])) child--;
+        first[hole] = first[child];
+        hole = child;
+    }
+    if ((len & 1) == 0 && child == (len - 2) / 2) {
+        child = 2 * (child + 1);
+        first[hole] = first[child - 1];
+        hole = child - 1;
+    }
+    ls_push_heap(first, hole, top, value, key);
+}
+
+/* __partial_sort(first, last, last): make_heap, then sort_heap. */
+static void ls_heap_sort(uint32_t *first, uint32_t *last, const uint64_t *key)
+{
+    const int64_t len = last - first;
+    if (len >= 2) {
+        int64_t parent = (len - 2) / 2;
+        for (;;) {
+            ls_adjust_heap(first, parent, len, first[parent], key);
+            if (parent == 0) break;
+            parent--;
+        }
+    }
+    while (last - first > 1) {
+        --last;
+        const uint32_t value = *last;
+        *last = *first;
+        ls_adjust_heap(first, 0, last - first, value, key);
+    }
+}
+
+static void ls_introsort_loop(uint32_t *first, uint32_t *last, int64_t depth, const uint64_t *key)
+{
+    while (last - first > LS_THRESHOLD) {
+        if (depth == 0) {
+            ls_heap_sort(first, last, key);
+            return;
+        }
+        --depth;
+        uint32_t *mid = first + (last - first) / 2;
+        ls_move_median_to_first(first, first + 1, mid, last - 1, key);
+        uint32_t *cut = ls_unguarded_partition(first + 1, last, first, key);
+        ls_introsort_loop(cut, last, depth, key);
+        last = cut;
+    }
+}
+
+static void ls_unguarded_linear_insert(uint32_t *last, const uint64_t *key)
+{
+    const uint32_t val = *last;
+    uint32_t *next = last - 1;
+    while (ls_less(key, val, *next)) {
+        *last = *next;
+        last = next;
+        --next;
+    }
+    *last = val;
+}
+
+static void ls_insertion_sort(uint32_t *first, uint32_t *last, const uint64_t *key)
+{
+    if (first == last) return;
+    for (uint32_t *i = first + 1; i != last; ++i) {
+        if (ls_less(key, *i, *first)) {
+            const uint32_t val = *i;
+            memmove(first + 1, first, (size_t)(i - first) * sizeof(uint32_t));
+            *first = val;
+        } else {
+            ls_unguarded_linear_insert(i, key);
+        }
+    }
+}
+
+static void ls_sort(uint32_t *first, uint32_t *last, const uint64_t *key)
+{
+    if (first == last) return;
+    const int64_t n = last - first;
+    const int64_t lg = 63 - __builtin_clzll((unsigned long long)n);
+    ls_introsort_loop(first, last, 2 * lg, key);
+    if (last - first > LS_THRESHOLD) {
+        ls_insertion_sort(first, first + LS_THRESHOLD, key);
+        for (uint32_t *i = first + LS_THRESHOLD; i != last; ++i) ls_unguarded_linear_insert(i, key);
+    } else {
+        ls_insertion_sort(first, last, key);
+    }
+}
+
+int orc_libstdcxx_heap_sort(uint32_t *elems, int64_t count, const uint64_t *key)
+{
+    if (count < 0 || (count > 0 && (!elems || !key))) return ORC_EINVAL;
+    ls_heap_sort(elems, elems + count, key);
+    return ORC_OK;
+}
+
+int orc_libstdcxx_sort(uint32_t *elems, int64_t count, const uint64_t *key)
+{
+    if (count < 0 || (count > 0 && (!elems || !key))) return ORC_EINVAL;
+    ls_sort(elems, elems + count, key);
+    return ORC_OK;
+}
+
+/* Core numbers of every community's induced subgraph (RG:6881-6955): the
+ * internal degree counts neighbours in the same community (a self loop
+ * included); peeling in degree order (Batagelj-Zaversnik bins here, the
+ * reference's lazy buckets give the same, uniquely defined, numbers). */
+static int community_cores(const orc_graph *g, const uint32_t *membership, const uint32_t *cverts,
+                           const int64_t *cstart, uint32_t num_comm, const int64_t *v2l, uint32_t *core)
+{
+    const int64_t n = g->n;
+    uint32_t *d = (uint32_t *)malloc((size_t)n * sizeof(uint32_t));
+    int64_t *pos = (int64_t *)malloc((size_t)n * sizeof(int64_t));
+    uint32_t *vert = (uint32_t *)malloc((size_t)n * sizeof(uint32_t));
+    int64_t *bin = NULL;
+    int64_t bin_cap = 0;
+    int rc = ORC_ENOMEM;
+    if (!d || !pos || !vert) goto out;
+    for (uint32_t c = 0; c < num_comm; ++c) {
+        const uint32_t *verts = cverts + cstart[c];
+        const int64_t sz = cstart[c + 1] - cstart[c];
+        if (sz == 0) continue;
+        uint32_t md = 0;
+        for (int64_t i = 0; i < sz; ++i) {
+            const uint32_t v = verts[i];
+            uint32_t k = 0;
+            for (int64_t e = g->row_ptr[v]; e < g->row_ptr[v + 1]; ++e)
+                if (membership[g->col[e]] == c) ++k;
+            d[v] = k;
+            if (k > md) md = k;
+        }
+        if ((int64_t)md + 2 > bin_cap) {
+            free(bin);
+            bin_cap = (int64_t)md + 2;
+            bin = (int64_t *)malloc((size_t)bin_cap * sizeof(int64_t));
+            if (!bin) goto out;
+        }
+        memset(bin, 0, (size_t)(md + 2) * sizeof(int64_t));
+        for (int64_t i = 0; i < sz; ++i) bin[d[verts[i]]]++;
+        int64_t start = 0;
+        for (uint32_t k = 0; k <= md; ++k) {
+            const int64_t num = bin[k];
+            bin[k] = start;
+            start += num;
+        }
+        for (int64_t i = 0; i < sz; ++i) {
+            const uint32_t v = verts[i];
+            pos[v] = bin[d[v]];
+            vert[bin[d[v]]] = v;
+            bin[d[v]]++;
+        }
+        for (uint32_t k = md; k >= 1; --k) bin[k] = bin[k - 1];
+        bin[0] = 0;
+        for (int64_t i = 0; i < sz; ++i) {
+            const uint32_t v = vert[i];
+            core[v] = d[v];
+            for (int64_t e = g->row_ptr[v]; e < g->row_ptr[v + 1]; ++e) {
+                const uint32_t u = (uint32_t)g->col[e];
+                if (membership[u] != c || v2l[u] < 0) continue;
+                if (d[u] > d[v]) {
+                    const uint32_t du = d[u];
+                    const int64_t pu = pos[u], pw = bin[du];
+                    const uint32_t w = vert[pw];
+                    if (u != w) {
+                        pos[u] = pw;
+                        vert[pu] = w;
+                        pos[w] = pu;
+                        vert[pw] = u;
+                    }
+                    bin[du]++;
+                    d[u]--;
+                }
+            }
+        }
+    }
+    rc = ORC_OK;
+out:
+    free(d); free(pos); free(vert); free(bin);
+    return rc;
+}
+
+static int is_sorted_intra(int order)
+{
+    return order == ORC_INTRA_HUBSORT || order == ORC_INTRA_DEGREE_ASC || order == ORC_INTRA_HUB2 ||
+           order == ORC_INTRA_ALTERNATE || order == ORC_INTRA_BOUNDARY_LAST || order == ORC_INTRA_CORE;
+}
+
+/* Per-vertex sort keys of the sorted intra orders. */
+static int sorted_intra_keys(const orc_graph *g, const uint32_t *membership, const uint32_t *deg,
+                             const uint32_t *cverts, const int64_t *cstart, uint32_t num_comm,
+                             const int64_t *v2l, int order, uint64_t *key)
+{
+    const int64_t n = g->n;
+    const uint64_t m32 = 0xFFFFFFFFull;
+    if (order == ORC_INTRA_CORE) {
+        uint32_t *core = (uint32_t *)calloc((size_t)n, sizeof(uint32_t));
+        if (!core) return ORC_ENOMEM;
+        const int rc = community_cores(g, membership, cverts, cstart, num_comm, v2l, core);
+        if (rc == ORC_OK)
+            for (int64_t v = 0; v < n; ++v) key[v] = ((m32 - core[v]) << 32) | (m32 - deg[v]);
+        free(core);
+        return rc;
+    }
+    for (int64_t v = 0; v < n; ++v) {
+        switch (order) {
+        case ORC_INTRA_HUBSORT:
+        case ORC_INTRA_ALTERNATE: key[v] = m32 - deg[v]; break;
+        case ORC_INTRA_DEGREE_ASC: key[v] = deg[v]; break;
+        case ORC_INTRA_HUB2: {
+            uint64_t sc = 0;
+            for (int64_t e = g->row_ptr[v]; e < g->row_ptr[v + 1]; ++e) sc += deg[g->col[e]];
+            key[v] = ~sc;
+            break;
+        }
+        case ORC_INTRA_BOUNDARY_LAST: {
+            uint64_t ext = 0;
+            for (int64_t e = g->row_ptr[v]; e < g->row_ptr[v + 1]; ++e)
+                if (membership[g->col[e]] != membership[v]) ++ext;
+            key[v] = (ext << 32) | (m32 - deg[v]);
+            break;
+        }
+        default: return ORC_EUNSUPPORTED;
+        }
+    }
+    return ORC_OK;
+}
+
+/* One community of a sorted intra order; tmp holds sz entries. */
+static void intra_sorted(const uint32_t *verts, int64_t sz, int order, const uint64_t *key,
+                         uint32_t *local_ids, uint32_t *tmp)
+{
+    if (sz == 0) return;
+    if (sz == 1) {
+        local_ids[verts[0]] = 0;
+        return;
+    }
+    memcpy(tmp, verts, (size_t)sz * sizeof(uint32_t));
+    ls_sort(tmp, tmp + sz, key);
+    if (order == ORC_INTRA_ALTERNATE) {
+        /* Hubs and leaves interleaved from both ends (RG:6799-6818). */
+        const int64_t mid = (sz + 1) / 2;
+        int64_t lo = 0, hi = sz - 1, p = 0;
+        for (int64_t i = 0; i < mid; ++i) {
+            local_ids[tmp[lo++]] = (uint32_t)p++;
+            if (hi >= lo) local_ids[tmp[hi--]] = (uint32_t)p++;
+        }
+        return;
+    }
+    for (int64_t j = 0; j < sz; ++j) local_ids[tmp[j]] = (uint32_t)j;
+}
+
+/* ------------------------------------------------------------------------ */
 /* orderCompose (RG:6286-7087), super-graph order "none".                    */
 /* ------------------------------------------------------------------------ */
 typedef struct { int64_t key; uint32_t c; } orc_sortrec;
@@ -908,7 +1225,7 @@ int orc_compose(const orc_graph *g, const uint32_t *membership,
     if (n == 0) return ORC_OK;
     if (cfg->intra_order == ORC_INTRA_GORDER && cfg->gorder_window <= 0) return ORC_EINVAL;
     if (cfg->intra_order != ORC_INTRA_BFS && cfg->intra_order != ORC_INTRA_RCM &&
-        cfg->intra_order != ORC_INTRA_GORDER)
+        cfg->intra_order != ORC_INTRA_GORDER && !is_sorted_intra(cfg->intra_order))
         return ORC_EUNSUPPORTED;
 
     int rc = ORC_ENOMEM;
@@ -925,6 +1242,7 @@ int orc_compose(const orc_graph *g, const uint32_t *membership,
     int64_t *offsets = (int64_t *)calloc((size_t)num_comm + 1, sizeof(int64_t));
     int64_t *v2l = (int64_t *)malloc((size_t)n * sizeof(int64_t));
     uint32_t *local_ids = (uint32_t *)calloc((size_t)n, sizeof(uint32_t));
+    uint64_t *skey = NULL;   /* sort keys of the sorted intra orders */
     if (!deg || !csize || !cstart || !cverts || !recs || !offsets || !v2l || !local_ids)
         goto done;
     for (int64_t v = 0; v < n; ++v) deg[v] = (uint32_t)degree_of(g, v);
@@ -986,6 +1304,13 @@ int orc_compose(const orc_graph *g, const uint32_t *membership,
     }
     for (uint32_t c = 0; c < num_comm; ++c)
         if (csize[c] > stats->largest_community) stats->largest_community = csize[c];
+    if (is_sorted_intra(cfg->intra_order)) {
+        skey = (uint64_t *)malloc((size_t)n * sizeof(uint64_t));
+        if (!skey) goto done;
+        rc = sorted_intra_keys(g, membership, deg, cverts, cstart, num_comm, v2l, cfg->intra_order, skey);
+        if (rc != ORC_OK) goto done;
+        rc = ORC_ENOMEM;
+    }
 
     /* Per-community intra order, one community per task as in the reference
      * (RG:6680-6962, schedule(dynamic, 1)); every task writes only its own
@@ -1019,7 +1344,9 @@ int orc_compose(const orc_graph *g, const uint32_t *membership,
                 const uint32_t c = recs[i].c;
                 const uint32_t *verts = cverts + cstart[c];
                 const int64_t sz = csize[c];
-                if (cfg->intra_order == ORC_INTRA_RCM) {
+                if (skey) {
+                    intra_sorted(verts, sz, cfg->intra_order, skey, local_ids, t_la);
+                } else if (cfg->intra_order == ORC_INTRA_RCM) {
                     intra_rcm(g, verts, sz, c, membership, deg, v2l, local_ids, t_visited,
                               t_queue, t_la, t_lb, t_cand);
                 } else if (cfg->intra_order == ORC_INTRA_GORDER &&
@@ -1058,7 +1385,7 @@ int orc_compose(const orc_graph *g, const uint32_t *membership,
     rc = ORC_OK;
 done:
     free(deg); free(csize); free(cstart); free(cverts); free(recs); free(offsets);
-    free(v2l); free(local_ids);
+    free(v2l); free(local_ids); free(skey);
     return rc;
 }
 

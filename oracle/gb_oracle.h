@@ -79,13 +79,25 @@ enum {
     ORC_COMM_IDENTITY = 6
 };
 /* Intra-community axis (IntraCommunityOrder, reorder_graphbrew.h:302-378).
- * Only the primitives whose order is fully specified are restated; HubSort
- * and DegreeAsc use an unstable std::sort whose tie order is not. */
+ * The sorted orders (HubSort .. CoreOrder) sort with std::sort, whose tie
+ * order is that of the standard library; libstdc++'s (GCC 13) is restated. */
 enum {
     ORC_INTRA_BFS = 0,
     ORC_INTRA_RCM = 1,
-    ORC_INTRA_GORDER = 4
+    ORC_INTRA_GORDER = 4,
+    ORC_INTRA_HUBSORT = 6,
+    ORC_INTRA_DEGREE_ASC = 7,
+    ORC_INTRA_HUB2 = 8,
+    ORC_INTRA_ALTERNATE = 9,
+    ORC_INTRA_BOUNDARY_LAST = 11,
+    ORC_INTRA_CORE = 12
 };
+
+/* libstdc++ (GCC 13) std::sort of `count` element ids by comp(a, b) =
+ * key[a] < key[b]: the tie order the sorted intra orders inherit. */
+int orc_libstdcxx_sort(uint32_t *elems, int64_t count, const uint64_t *key);
+/* Its depth-limit fallback alone (__partial_sort(first, last, last)). */
+int orc_libstdcxx_heap_sort(uint32_t *elems, int64_t count, const uint64_t *key);
 
 typedef struct {
     int community_order;

@@ -31,7 +31,10 @@ DEFAULT_AGGREGATION_TOLERANCE = 0.8
 DEFAULT_TOLERANCE_DROP = 10.0
 
 COMM_ORDERS = {"size-desc": 0, "size-asc": 1, "degree-desc": 2, "degree-asc": 3, "identity": 6}
-INTRA_ORDERS = {"bfs": 0, "rcm": 1, "gorder": 4}
+INTRA_ORDERS = {"bfs": 0, "rcm": 1, "gorder": 4, "hubsort": 6, "degree-asc": 7, "hub2": 8, "alternate": 9,
+                "boundary-last": 11, "core": 12}
+_u64p = np.ctypeslib.ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")
+STDSORT_SO = os.path.join(HERE, "_build", "libstdsort.so")
 
 
 class Graph(C.Structure):
@@ -94,8 +97,52 @@ def load():
         lib.orc_modularity.restype = C.c_double
         lib.orc_modularity.argtypes = [C.POINTER(Graph), _u32p, C.c_double]
         lib.orc_max_threads.restype = C.c_int
+        lib.orc_libstdcxx_sort.argtypes = [_u32p, C.c_int64, _u64p]
+        lib.orc_libstdcxx_heap_sort.argtypes = [_u32p, C.c_int64, _u64p]
         _lib = lib
     return _lib
+
+
+def libstdcxx_sort(elems, key):
+    """The oracle's restatement of libstdc++ std::sort: elems (uint32 ids)
+    sorted by key[elem] ascending, ties left where introsort leaves them."""
+    e = np.array(elems, dtype=np.uint32)
+    k = np.ascontiguousarray(key, dtype=np.uint64)
+    if load().orc_libstdcxx_sort(e, len(e), k) != 0:
+        raise RuntimeError("orc_libstdcxx_sort failed")
+    return e
+
+
+def libstdcxx_heap_sort(elems, key):
+    """The restatement's depth-limit fallback (heap sort) alone."""
+    e = np.array(elems, dtype=np.uint32)
+    k = np.ascontiguousarray(key, dtype=np.uint64)
+    if load().orc_libstdcxx_heap_sort(e, len(e), k) != 0:
+        raise RuntimeError("orc_libstdcxx_heap_sort failed")
+    return e
+
+
+def _stdsort_lib():
+    if not os.path.exists(STDSORT_SO):
+        subprocess.run(["make", "-s", "-C", HERE, "_build/libstdsort.so"], check=True)
+    lib = C.CDLL(STDSORT_SO)
+    lib.pin_std_sort.argtypes = [_u32p, C.c_int64, _u64p]
+    lib.pin_std_heap_sort.argtypes = [_u32p, C.c_int64, _u64p]
+    return lib
+
+
+def std_sort(elems, key):
+    """The toolchain's own std::sort with the same comparator (pin)."""
+    e = np.array(elems, dtype=np.uint32)
+    _stdsort_lib().pin_std_sort(e, len(e), np.ascontiguousarray(key, dtype=np.uint64))
+    return e
+
+
+def std_heap_sort(elems, key):
+    """The toolchain's std::partial_sort over the whole range (pin)."""
+    e = np.array(elems, dtype=np.uint32)
+    _stdsort_lib().pin_std_heap_sort(e, len(e), np.ascontiguousarray(key, dtype=np.uint64))
+    return e
 
 
 def load_reference():
