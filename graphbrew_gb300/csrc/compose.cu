@@ -937,8 +937,9 @@ void compose_device(const DeviceCSR& g, const uint32_t* memb, const ComposeParam
     if (n == 0) return;
     int intra = p.intra_order;
     if (intra == kIntraDendrogram) intra = kIntraBFS;  // Leiden has no Rabbit dendrogram (:6668-6677)
-    GB_REQUIRE(intra == kIntraBFS || intra == kIntraGorder || intra == kIntraRCM, GBGPU_E_UNSUPPORTED,
-               "intra-community order not available on the GPU path");
+    const bool sorted_intra = is_sorted_intra_order(intra);
+    GB_REQUIRE(intra == kIntraBFS || intra == kIntraGorder || intra == kIntraRCM || sorted_intra,
+               GBGPU_E_UNSUPPORTED, "intra-community order not available on the GPU path");
     const int co = p.community_order;
     GB_REQUIRE(co == kSizeDesc || co == kSizeAsc || co == kDegreeDesc || co == kDegreeAsc || co == kIdentity,
                GBGPU_E_UNSUPPORTED, "community order not available on the GPU path");
@@ -1092,8 +1093,10 @@ void compose_device(const DeviceCSR& g, const uint32_t* memb, const ComposeParam
         levels = rcm_communities(g, memb, lists.get() + 4 * C, cc.get()->n + 4, nbfs, order_v, offs, ssize, C, nn,
                                  hc.largest, local, s, &launches);
     }
+    // ---- sorted orders: every community ----
+    if (sorted_intra) sorted_communities(g, memb, intra, order_v, vkeys, offs, ssize, nn, local, s, &launches);
     // ---- BFS communities ----
-    if (nbfs > 0 && intra != kIntraRCM) {
+    if (nbfs > 0 && intra != kIntraRCM && !sorted_intra) {
         const int32_t* blist = lists.get() + 4 * C;
         DevBuf<int32_t> slot_of_comm(C, s);
         GB_CUDA(cudaMemsetAsync(slot_of_comm, 0xFF, C * sizeof(int32_t), s));

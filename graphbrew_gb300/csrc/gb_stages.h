@@ -26,6 +26,15 @@ struct ComposeParams {
 void compose_device(const DeviceCSR& g, const uint32_t* membership, const ComposeParams& p,
                     int32_t* new_ids, gbgpu_stats* st, cudaStream_t s);
 
+// ---- compose_sorted.cu: HubSort, DegreeAsc, Hub2, Alternate, BoundaryLast, CoreOrder ----
+bool is_sorted_intra_order(int intra);
+// Local ids of every non-isolated vertex for a sorted intra order.  order_v /
+// ranks: the placement skeleton (vertex and community rank per position, nn
+// positions); offs / ssize: start and size of each ranked community.
+int64_t sorted_communities(const DeviceCSR& g, const uint32_t* memb, int intra, const uint32_t* order_v,
+                           const uint32_t* ranks, const int64_t* offs, const int64_t* ssize, int64_t nn,
+                           uint32_t* local, cudaStream_t s, int64_t* launches);
+
 // ---- leiden.cu ----
 struct LeidenParams {
     double resolution = 1.0;
