@@ -26,7 +26,7 @@ namespace gb {
 namespace {
 
 enum CommunityOrderOrd { kSizeDesc = 0, kSizeAsc = 1, kDegreeDesc = 2, kDegreeAsc = 3, kIdentity = 6 };
-enum IntraOrd { kIntraBFS = 0, kIntraRCM = 1, kIntraDendrogram = 3, kIntraGorder = 4 };
+enum IntraOrd { kIntraBFS = 0, kIntraRCM = 1, kIntraRCMpp = 2, kIntraDendrogram = 3, kIntraGorder = 4 };
 
 constexpr int kT = 256;
 
@@ -649,32 +649,80 @@ __global__ void k_rcm_write(const int32_t* __restrict__ F, int64_t nf, const int
 }
 
 // Last level of a slot whose next level is empty: minimum degree, first in
-// level order.
+// level order (RCM) or smallest id (RCM++).
 __global__ void k_rcm_last_level(const int32_t* __restrict__ F, int64_t nf, const int64_t* __restrict__ rp,
                                  const uint32_t* __restrict__ memb, const int32_t* __restrict__ slot_of_comm,
-                                 const int64_t* __restrict__ bbase, const int64_t* __restrict__ bend,
+                                 const int64_t* __restrict__ bbase, const int64_t* __restrict__ bend, int by_id,
                                  unsigned long long* __restrict__ cand) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nf; i += (int64_t)gridDim.x * blockDim.x) {
         const int32_t u = F[i];
         const int32_t j = slot_of_comm[memb[u]];
         if (bend[j] != bbase[j]) continue;
-        atomicMin(&cand[j], ((unsigned long long)(rp[u + 1] - rp[u]) << 32) | (unsigned long long)i);
+        const unsigned long long tie = by_id ? (unsigned long long)(uint32_t)u : (unsigned long long)i;
+        atomicMin(&cand[j], ((unsigned long long)(rp[u + 1] - rp[u]) << 32) | tie);
     }
 }
 
 __global__ void k_rcm_level_done(int32_t nslots, const int64_t* __restrict__ fs, const int64_t* __restrict__ fe,
                                  const int64_t* __restrict__ bbase, const int64_t* __restrict__ bend,
-                                 const int32_t* __restrict__ F, unsigned long long* __restrict__ cand,
+                                 const int32_t* __restrict__ F, int by_id, unsigned long long* __restrict__ cand,
                                  uint32_t* __restrict__ last_node, int32_t* __restrict__ ecc) {
     for (int32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < nslots; j += gridDim.x * blockDim.x) {
         if (fe[j] == fs[j]) continue;
         if (bend[j] > bbase[j]) {
             ++ecc[j];
         } else if (cand[j] != ~0ull) {
-            last_node[j] = (uint32_t)F[cand[j] & 0xFFFFFFFFull];
+            const uint32_t lo = (uint32_t)(cand[j] & 0xFFFFFFFFull);
+            last_node[j] = by_id ? lo : (uint32_t)F[lo];
             cand[j] = ~0ull;
         }
     }
+}
+
+// RCM++ start (RG:4185-4256): depth of each reached vertex from the seed.
+__global__ void k_rcm_depth(const int32_t* __restrict__ F, int64_t nf, uint32_t level, uint32_t* __restrict__ depth) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nf; i += (int64_t)gridDim.x * blockDim.x)
+        depth[F[i]] = level;
+}
+
+// Rank keys over the placement skeleton: (community rank, degree) or
+// (community rank, ~depth); a stable sort keeps vertex order for ties.
+__global__ void k_rcmpp_keys(const uint32_t* __restrict__ order_v, const uint32_t* __restrict__ ranks, int64_t nn,
+                             const int64_t* __restrict__ rp, const uint32_t* __restrict__ depth, int low_bits,
+                             uint32_t max_depth, int by_depth, uint64_t* __restrict__ keys,
+                             uint32_t* __restrict__ pos) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nn; p += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t v = order_v[p];
+        const uint64_t low = by_depth ? (uint64_t)(max_depth - depth[v]) : (uint64_t)(rp[v + 1] - rp[v]);
+        keys[p] = ((uint64_t)ranks[p] << low_bits) | low;
+        pos[p] = (uint32_t)p;
+    }
+}
+
+__global__ void k_rcmpp_rank(const uint32_t* __restrict__ sorted_pos, const uint32_t* __restrict__ ranks,
+                             const int64_t* __restrict__ offs, int64_t nn, int64_t* __restrict__ score) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nn; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t p = sorted_pos[i];
+        score[p] += i - offs[ranks[p]];
+    }
+}
+
+// Least degree rank + depth rank per participating slot, ties to the smaller id.
+__global__ void k_rcmpp_pick(const uint32_t* __restrict__ order_v, int64_t nn, const uint32_t* __restrict__ memb,
+                             const int32_t* __restrict__ slot_of_comm, const int32_t* __restrict__ part,
+                             const int64_t* __restrict__ score, unsigned long long* __restrict__ best) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nn; p += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t v = order_v[p];
+        const int32_t j = slot_of_comm[memb[v]];
+        if (j < 0 || !part[j]) continue;
+        atomicMin(&best[j], ((unsigned long long)score[p] << 32) | v);
+    }
+}
+
+__global__ void k_rcmpp_start(int32_t nslots, const int32_t* __restrict__ part,
+                              const unsigned long long* __restrict__ best, uint32_t* __restrict__ start) {
+    for (int32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < nslots; j += gridDim.x * blockDim.x)
+        if (part[j] && best[j] != ~0ull) start[j] = (uint32_t)(best[j] & 0xFFFFFFFFull);
 }
 
 // George-Liu step: keep sweeping while the eccentricity grows.
@@ -785,9 +833,9 @@ T read_dev(const T* p, cudaStream_t s) {
 // Reverse Cuthill-McKee for the listed communities (see the kernels above).
 // Returns the number of BFS levels run.
 int64_t rcm_communities(const DeviceCSR& g, const uint32_t* memb, const int32_t* blist, const int32_t* count_p,
-                        int32_t nslots, const uint32_t* order_v, const int64_t* offs, const int64_t* ssize,
-                        int64_t C, int64_t nn, uint32_t largest, uint32_t* local, cudaStream_t s,
-                        int64_t* launches) {
+                        int32_t nslots, const uint32_t* order_v, const uint32_t* ranks, const int64_t* offs,
+                        const int64_t* ssize, int64_t C, int64_t nn, uint32_t largest, bool pp, uint32_t* local,
+                        cudaStream_t s, int64_t* launches) {
     const int64_t n = g.n;
     DevBuf<int32_t> slot_of_comm(C, s);
     GB_CUDA(cudaMemsetAsync(slot_of_comm, 0xFF, C * sizeof(int32_t), s));
@@ -813,14 +861,16 @@ int64_t rcm_communities(const DeviceCSR& g, const uint32_t* memb, const int32_t*
     DevBuf<int32_t> F(nn + 1, s), NF(nn + 1, s);
     DevBuf<int64_t> D(nn + 1, s), parent(nn + 1, s);
     int64_t levels = 0;
-    // One BFS over the participating slots; Cuthill-McKee ordering when cm.
-    auto sweep = [&](bool cm) -> void {
+    DevBuf<uint32_t> depth(pp ? n : 0, s);
+    // One BFS over the participating slots: a George-Liu sweep, the
+    // Cuthill-McKee order (cm), or the RCM++ depths from the seed (dep).
+    auto sweep = [&](bool cm, bool dep = false) -> void {
         exclusive_scan_i32_to_i64(part, pos, nslots, pos.get() + nslots, s);
         const int64_t np = read_dev(pos.get() + nslots, s);
         GB_CUDA(cudaMemsetAsync(visited, 0, n, s));
         GB_CUDA(cudaMemsetAsync(claim, 0xFF, n * sizeof(unsigned long long), s));
-        k_rcm_frontier<<<grid_for(nslots, kT), kT, 0, s>>>(nslots, part, pos, start, cm ? 1 : 0, F, visited, fs, fe,
-                                                           qlen, ecc, cand);
+        k_rcm_frontier<<<grid_for(nslots, kT), kT, 0, s>>>(nslots, part, pos, start, (cm || dep) ? 1 : 0, F,
+                                                           visited, fs, fe, qlen, ecc, cand);
         GB_LAUNCH_CHECK();
         *launches += 4;
         if (cm) {
@@ -835,8 +885,15 @@ int64_t rcm_communities(const DeviceCSR& g, const uint32_t* memb, const int32_t*
             *launches += 1;
         }
         int64_t nf = np;
+        uint32_t level = 0;
         while (nf > 0) {
             ++levels;
+            if (dep) {
+                k_rcm_depth<<<grid_for(nf, kT), kT, 0, s>>>(F, nf, level, depth);
+                GB_LAUNCH_CHECK();
+                ++*launches;
+            }
+            ++level;
             k_frontier_degrees<<<grid_for(nf, kT), kT, 0, s>>>(F, nf, g.row_ptr, D);
             GB_LAUNCH_CHECK();
             exclusive_scan_i64_total(D, D, nf, D.get() + nf, s);
@@ -860,14 +917,14 @@ int64_t rcm_communities(const DeviceCSR& g, const uint32_t* memb, const int32_t*
                 GB_LAUNCH_CHECK();
             }
             const int64_t next = T > 0 ? read_dev(P.get() + T, s) : 0;
-            if (!cm) {
+            if (!cm && !dep) {
                 k_rcm_last_level<<<grid_for(nf, kT), kT, 0, s>>>(F, nf, g.row_ptr, memb, slot_of_comm, bbase, bend,
-                                                                 cand);
+                                                                 pp ? 1 : 0, cand);
                 GB_LAUNCH_CHECK();
-                k_rcm_level_done<<<grid_for(nslots, kT), kT, 0, s>>>(nslots, fs, fe, bbase, bend, F, cand, last_node,
-                                                                     ecc);
+                k_rcm_level_done<<<grid_for(nslots, kT), kT, 0, s>>>(nslots, fs, fe, bbase, bend, F, pp ? 1 : 0, cand,
+                                                                     last_node, ecc);
                 GB_LAUNCH_CHECK();
-            } else if (next > 0) {
+            } else if (cm && next > 0) {
                 // Children of one parent by (degree, id): stable sort by (parent, degree).
                 unsigned long long md = 0;
                 {
@@ -896,6 +953,50 @@ int64_t rcm_communities(const DeviceCSR& g, const uint32_t* memb, const int32_t*
             nf = next;
         }
     };
+    if (pp) {
+        // RCM++ start for the communities above 32 vertices: BFS depths from
+        // the seed, ranks by (degree, id) and (depth descending, id), least sum.
+        int32_t np_host = 0;
+        {
+            DevBuf<int64_t> tot(1, s);
+            exclusive_scan_i32_to_i64(part, pos, nslots, tot, s);
+            np_host = (int32_t)read_dev(tot.get(), s);
+        }
+        if (np_host > 0) {
+            GB_CUDA(cudaMemsetAsync(depth, 0, n * sizeof(uint32_t), s));
+            sweep(false, true);
+            DevBuf<unsigned long long> mx(1, s);
+            GB_CUDA(cudaMemsetAsync(mx, 0, sizeof(unsigned long long), s));
+            k_max_degree_of<<<grid_for(nn, kT), kT, 0, s>>>(reinterpret_cast<const int32_t*>(order_v), nn, g.row_ptr,
+                                                            mx);
+            GB_LAUNCH_CHECK();
+            const int degbits = bits_for(read_dev(mx.get(), s));
+            const uint32_t max_depth = (uint32_t)std::max<int64_t>(0, levels);   // depth < levels run so far
+            const int dbits = bits_for(max_depth);
+            const int rbits = bits_for((uint64_t)(C > 1 ? C - 1 : 1));
+            DevBuf<int64_t> score(nn, s);
+            GB_CUDA(cudaMemsetAsync(score, 0, nn * sizeof(int64_t), s));
+            DevBuf<uint64_t> keys(nn, s);
+            DevBuf<uint32_t> sp(nn, s);
+            for (int by_depth = 0; by_depth < 2; ++by_depth) {
+                const int low = by_depth ? dbits : degbits;
+                k_rcmpp_keys<<<grid_for(nn, kT), kT, 0, s>>>(order_v, ranks, nn, g.row_ptr, depth.get(), low, max_depth,
+                                                            by_depth, keys, sp);
+                GB_LAUNCH_CHECK();
+                radix_sort_pairs_u64(keys, sp, nn, low + rbits, s);
+                k_rcmpp_rank<<<grid_for(nn, kT), kT, 0, s>>>(sp, ranks, offs, nn, score);
+                GB_LAUNCH_CHECK();
+                *launches += 2 + 3 * ((low + rbits + 7) / 8);
+            }
+            DevBuf<unsigned long long> best(nslots, s);
+            GB_CUDA(cudaMemsetAsync(best, 0xFF, nslots * sizeof(unsigned long long), s));
+            k_rcmpp_pick<<<grid_for(nn, kT), kT, 0, s>>>(order_v, nn, memb, slot_of_comm, part, score, best);
+            GB_LAUNCH_CHECK();
+            k_rcmpp_start<<<grid_for(nslots, kT), kT, 0, s>>>(nslots, part, best, start);
+            GB_LAUNCH_CHECK();
+            *launches += 3;
+        }
+    }
     // George-Liu sweeps (communities above 32 vertices), at most three.
     for (int it = 0; it < 3; ++it) {
         int32_t np_host = 0;
@@ -938,7 +1039,8 @@ void compose_device(const DeviceCSR& g, const uint32_t* memb, const ComposeParam
     int intra = p.intra_order;
     if (intra == kIntraDendrogram) intra = kIntraBFS;  // Leiden has no Rabbit dendrogram (:6668-6677)
     const bool sorted_intra = is_sorted_intra_order(intra);
-    GB_REQUIRE(intra == kIntraBFS || intra == kIntraGorder || intra == kIntraRCM || sorted_intra,
+    GB_REQUIRE(intra == kIntraBFS || intra == kIntraGorder || intra == kIntraRCM || intra == kIntraRCMpp ||
+                   sorted_intra,
                GBGPU_E_UNSUPPORTED, "intra-community order not available on the GPU path");
     const int co = p.community_order;
     GB_REQUIRE(co == kSizeDesc || co == kSizeAsc || co == kDegreeDesc || co == kDegreeAsc || co == kIdentity,
@@ -1089,14 +1191,14 @@ void compose_device(const DeviceCSR& g, const uint32_t* memb, const ComposeParam
     // ---- RCM: every community of two or more vertices ----
     const int32_t nbfs = hc.n[4];
     int64_t levels = 0;
-    if (nbfs > 0 && intra == kIntraRCM) {
-        levels = rcm_communities(g, memb, lists.get() + 4 * C, cc.get()->n + 4, nbfs, order_v, offs, ssize, C, nn,
-                                 hc.largest, local, s, &launches);
+    if (nbfs > 0 && (intra == kIntraRCM || intra == kIntraRCMpp)) {
+        levels = rcm_communities(g, memb, lists.get() + 4 * C, cc.get()->n + 4, nbfs, order_v, vkeys, offs, ssize, C,
+                                 nn, hc.largest, intra == kIntraRCMpp, local, s, &launches);
     }
     // ---- sorted orders: every community ----
     if (sorted_intra) sorted_communities(g, memb, intra, order_v, vkeys, offs, ssize, nn, local, s, &launches);
     // ---- BFS communities ----
-    if (nbfs > 0 && intra != kIntraRCM && !sorted_intra) {
+    if (nbfs > 0 && intra != kIntraRCM && intra != kIntraRCMpp && !sorted_intra) {
         const int32_t* blist = lists.get() + 4 * C;
         DevBuf<int32_t> slot_of_comm(C, s);
         GB_CUDA(cudaMemsetAsync(slot_of_comm, 0xFF, C * sizeof(int32_t), s));

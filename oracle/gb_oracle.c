@@ -182,6 +182,42 @@ static int local_move_serial(const orc_graph *g, uint32_t *vcom, double *ctot,
     return iterations;
 }
 
+/* Refinement (RG:7330-7392): bounds = the local-moving membership, every
+ * vertex back to a singleton, then one serial sweep of
+ * localMovingPhase<true> (RG:1588-1734): a vertex whose community already
+ * holds more than itself (ctot > k_u * 1.001) stays; the others scan only
+ * neighbours inside their bound (scanCommunities<true>, RG:1392-1437) and
+ * move greedily; changeCommunity<true> (RG:1538-1573) repeats the singleton
+ * test, which in serial order always passes here. */
+static void refine_serial(const orc_graph *g, uint32_t *vcom, double *ctot, const double *vtot,
+                          const uint32_t *vcob, double M, double R, orc_acc *acc)
+{
+    const int64_t n = g->n;
+    for (int64_t u = 0; u < n; ++u) {
+        const uint32_t d = vcom[u];
+        if (ctot[d] > vtot[u] * 1.001) continue;
+        acc_clear(acc);
+        for (int64_t e = g->row_ptr[u]; e < g->row_ptr[u + 1]; ++e) {
+            const int32_t v = g->col[e];
+            if (v == u) continue;
+            if (vcob[v] != vcob[u]) continue;
+            acc_add(acc, vcom[v], 1.0);
+        }
+        double delta;
+        const uint32_t best_c = choose_community(acc, d, vtot[u], ctot, M, R, &delta);
+        if (best_c != d) {
+            const double old_ctot = ctot[d];
+            ctot[d] -= vtot[u];
+            if (old_ctot > vtot[u] * 1.001) {
+                ctot[d] += vtot[u];
+                continue;
+            }
+            ctot[best_c] += vtot[u];
+            vcom[u] = best_c;
+        }
+    }
+}
+
 #ifdef _OPENMP
 /* localMovingPhase<false> as the reference runs it with several threads:
  * dynamic chunks of 4096 vertices (DEFAULT_TILE_SIZE), racy reads of vcom and
@@ -464,6 +500,7 @@ int orc_leiden(const orc_graph *g, const orc_leiden_cfg *cfg,
     double *ctot = (double *)malloc((size_t)n * sizeof(double));
     char *vaff = (char *)malloc((size_t)n);
     uint32_t *cmap = (uint32_t *)malloc((size_t)n * sizeof(uint32_t));
+    uint32_t *vcob = NULL;
     orc_acc *accs = NULL;
     int nacc = 1;
 #ifdef _OPENMP
@@ -502,6 +539,19 @@ int orc_leiden(const orc_graph *g, const orc_leiden_cfg *cfg,
         stats->local_move_seconds += now_seconds() - t0;
         if (pass < 16) stats->pass_iterations[pass] = iters;
         stats->iterations += iters;
+        if (cfg->refine && (cfg->refine_depth < 0 || pass <= cfg->refine_depth)) {
+            if (cfg->parallel) { rc = ORC_EUNSUPPORTED; goto done; }
+            if (!vcob) {
+                vcob = (uint32_t *)malloc((size_t)n * sizeof(uint32_t));
+                if (!vcob) goto done;
+            }
+            memcpy(vcob, membership, (size_t)n * sizeof(uint32_t));
+            for (int64_t u = 0; u < n; ++u) {
+                membership[u] = (uint32_t)u;
+                ctot[u] = vtot[u];
+            }
+            refine_serial(g, membership, ctot, vtot, vcob, M, R, &accs[0]);
+        }
 
         const int64_t nc = count_communities(membership, n, cmap);
         if (pass == 0) stats->pass0_communities = nc;
@@ -534,6 +584,7 @@ done:
     free(ctot);
     free(vaff);
     free(cmap);
+    free(vcob);
     if (accs) {
         for (int i = 0; i < nacc; ++i) acc_free(&accs[i]);
         free(accs);
@@ -590,21 +641,99 @@ static int pair_cmp(const void *a, const void *b)
     return 0;
 }
 
+typedef struct { uint64_t key; uint32_t v; } orc_rankrec;
+
+static int rankrec_cmp(const void *a, const void *b)
+{
+    const orc_rankrec *x = (const orc_rankrec *)a, *y = (const orc_rankrec *)b;
+    if (x->key != y->key) return x->key < y->key ? -1 : 1;
+    return x->v < y->v ? -1 : (x->v > y->v);
+}
+
+/* RCM++ start (RG:4185-4256): BFS depths from the min-degree seed (seed
+ * marked visited; unreached vertices keep depth 0), then the vertex with
+ * the least degree rank + depth rank, ranks by (degree, id) ascending and
+ * (depth descending, id); ties to the smaller id.  The reference's score
+ * 0.5 * degRank + 0.5 * depthRank is exact in double, so the sum of ranks
+ * orders the same. */
+static int rcmpp_start(const orc_graph *g, const uint32_t *verts, int64_t sz, uint32_t c,
+                       const uint32_t *memb, const uint32_t *deg, const int64_t *v2l, uint32_t seed,
+                       char *visited, uint32_t *level_a, uint32_t *level_b, uint32_t *out)
+{
+    uint32_t *depth = (uint32_t *)calloc((size_t)sz, sizeof(uint32_t));
+    orc_rankrec *byd = (orc_rankrec *)malloc((size_t)sz * sizeof(orc_rankrec));
+    orc_rankrec *byp = (orc_rankrec *)malloc((size_t)sz * sizeof(orc_rankrec));
+    int64_t *rank = (int64_t *)calloc((size_t)sz, sizeof(int64_t));
+    if (!depth || !byd || !byp || !rank) {
+        free(depth); free(byd); free(byp); free(rank);
+        return ORC_ENOMEM;
+    }
+    memset(visited, 0, (size_t)sz);
+    uint32_t *cur = level_a, *nxt = level_b;
+    int64_t ncur = 1, nnxt;
+    cur[0] = seed;
+    visited[v2l[seed]] = 1;
+    uint32_t d = 0;
+    while (ncur > 0) {
+        nnxt = 0;
+        for (int64_t i = 0; i < ncur; ++i) {
+            const uint32_t u = cur[i];
+            depth[v2l[u]] = d;
+            for (int64_t e = g->row_ptr[u]; e < g->row_ptr[u + 1]; ++e) {
+                const int32_t v = g->col[e];
+                if (memb[v] != c) continue;
+                const int64_t li = v2l[v];
+                if (li != -1 && !visited[li]) { visited[li] = 1; nxt[nnxt++] = (uint32_t)v; }
+            }
+        }
+        ++d;
+        uint32_t *t = cur; cur = nxt; nxt = t; ncur = nnxt;
+    }
+    for (int64_t i = 0; i < sz; ++i) {
+        const uint32_t v = verts[i];
+        byd[i].key = deg[v];
+        byd[i].v = v;
+        byp[i].key = ~(uint64_t)depth[i];
+        byp[i].v = v;
+    }
+    qsort(byd, (size_t)sz, sizeof(orc_rankrec), rankrec_cmp);
+    qsort(byp, (size_t)sz, sizeof(orc_rankrec), rankrec_cmp);
+    for (int64_t i = 0; i < sz; ++i) {
+        rank[v2l[byd[i].v]] += i;
+        rank[v2l[byp[i].v]] += i;
+    }
+    uint32_t best = seed;
+    int64_t best_rank = INT64_MAX;
+    for (int64_t i = 0; i < sz; ++i) {
+        const uint32_t v = verts[i];
+        if (rank[i] < best_rank || (rank[i] == best_rank && v < best)) { best_rank = rank[i]; best = v; }
+    }
+    *out = best;
+    free(depth); free(byd); free(byp); free(rank);
+    return ORC_OK;
+}
+
 /* intraRCM (RG:4000-4134): min-degree start (ties -> smaller id), up to 3
  * George-Liu steps for sz > 32, Cuthill-McKee BFS with children sorted by
- * (degree, id), reversal of the reached part, unreached tail in input order. */
-static void intra_rcm(const orc_graph *g, const uint32_t *verts, int64_t sz, uint32_t c,
-                      const uint32_t *memb, const uint32_t *deg, const int64_t *v2l,
-                      uint32_t *local_ids, char *visited, uint32_t *queue,
-                      uint32_t *level_a, uint32_t *level_b, orc_pair *cand)
+ * (degree, id), reversal of the reached part, unreached tail in input order.
+ * pp: intraRCMpp (RG:4154-4342), the same with the RCM++ start for sz > 32
+ * and George-Liu ties to the smaller id instead of the first in level order. */
+static int intra_rcm(const orc_graph *g, const uint32_t *verts, int64_t sz, uint32_t c,
+                     const uint32_t *memb, const uint32_t *deg, const int64_t *v2l,
+                     uint32_t *local_ids, char *visited, uint32_t *queue,
+                     uint32_t *level_a, uint32_t *level_b, orc_pair *cand, int pp)
 {
-    if (sz == 0) return;
-    if (sz == 1) { local_ids[verts[0]] = 0; return; }
+    if (sz == 0) return ORC_OK;
+    if (sz == 1) { local_ids[verts[0]] = 0; return ORC_OK; }
     uint32_t start = verts[0];
     uint32_t min_deg = deg[verts[0]];
     for (int64_t i = 0; i < sz; ++i) {
         const uint32_t v = verts[i];
         if (deg[v] < min_deg || (deg[v] == min_deg && v < start)) { min_deg = deg[v]; start = v; }
+    }
+    if (pp && sz > 32) {
+        const int rc = rcmpp_start(g, verts, sz, c, memb, deg, v2l, start, visited, level_a, level_b, &start);
+        if (rc != ORC_OK) return rc;
     }
     const int max_gl = sz <= 32 ? 0 : 3;
     if (max_gl > 0) {
@@ -637,7 +766,10 @@ static void intra_rcm(const orc_graph *g, const uint32_t *verts, int64_t sz, uin
             uint32_t best_v = cur[0];
             uint32_t best_deg = deg[cur[0]];
             for (int64_t i = 1; i < ncur; ++i)
-                if (deg[cur[i]] < best_deg) { best_deg = deg[cur[i]]; best_v = cur[i]; }
+                if (deg[cur[i]] < best_deg || (pp && deg[cur[i]] == best_deg && cur[i] < best_v)) {
+                    best_deg = deg[cur[i]];
+                    best_v = cur[i];
+                }
             gl_node = best_v;
         }
         start = gl_node;
@@ -670,6 +802,7 @@ static void intra_rcm(const orc_graph *g, const uint32_t *verts, int64_t sz, uin
         if (!visited[i]) order[nord++] = verts[i];
     for (int64_t i = 0; i < main_size; ++i) local_ids[order[i]] = (uint32_t)(main_size - 1 - i);
     for (int64_t i = main_size; i < nord; ++i) local_ids[order[i]] = (uint32_t)i;
+    return ORC_OK;
 }
 
 /* intraGorderGreedy (RG:4420-4587): relaxed Gorder with a UnitHeap.  The
@@ -1225,7 +1358,8 @@ int orc_compose(const orc_graph *g, const uint32_t *membership,
     if (n == 0) return ORC_OK;
     if (cfg->intra_order == ORC_INTRA_GORDER && cfg->gorder_window <= 0) return ORC_EINVAL;
     if (cfg->intra_order != ORC_INTRA_BFS && cfg->intra_order != ORC_INTRA_RCM &&
-        cfg->intra_order != ORC_INTRA_GORDER && !is_sorted_intra(cfg->intra_order))
+        cfg->intra_order != ORC_INTRA_RCMPP && cfg->intra_order != ORC_INTRA_GORDER &&
+        !is_sorted_intra(cfg->intra_order))
         return ORC_EUNSUPPORTED;
 
     int rc = ORC_ENOMEM;
@@ -1346,9 +1480,14 @@ int orc_compose(const orc_graph *g, const uint32_t *membership,
                 const int64_t sz = csize[c];
                 if (skey) {
                     intra_sorted(verts, sz, cfg->intra_order, skey, local_ids, t_la);
-                } else if (cfg->intra_order == ORC_INTRA_RCM) {
-                    intra_rcm(g, verts, sz, c, membership, deg, v2l, local_ids, t_visited,
-                              t_queue, t_la, t_lb, t_cand);
+                } else if (cfg->intra_order == ORC_INTRA_RCM || cfg->intra_order == ORC_INTRA_RCMPP) {
+                    if (intra_rcm(g, verts, sz, c, membership, deg, v2l, local_ids, t_visited,
+                                  t_queue, t_la, t_lb, t_cand, cfg->intra_order == ORC_INTRA_RCMPP) != ORC_OK) {
+#ifdef _OPENMP
+#pragma omp atomic write
+#endif
+                        failed = 1;
+                    }
                 } else if (cfg->intra_order == ORC_INTRA_GORDER &&
                            !(cfg->gorder_fallback > 0 && sz > cfg->gorder_fallback)) {
                     if (intra_gorder(g, verts, sz, c, membership, deg, v2l, cfg->gorder_window,

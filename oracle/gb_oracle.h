@@ -48,6 +48,8 @@ typedef struct {
     int super_move_batch;         /* sgmb<k>; 1 = sequential super-move */
     int parallel;                 /* 0: cd_serial semantics; 1: racy OpenMP (cd_parallel) */
     int threads;                  /* OpenMP threads for parallel=1 (0 = runtime default) */
+    int refine;                   /* useRefinement (refine<k> / norefine) */
+    int refine_depth;             /* refinementDepth: -1 every pass, k: passes 0..k */
 } orc_leiden_cfg;
 
 typedef struct {
@@ -84,6 +86,7 @@ enum {
 enum {
     ORC_INTRA_BFS = 0,
     ORC_INTRA_RCM = 1,
+    ORC_INTRA_RCMPP = 2,
     ORC_INTRA_GORDER = 4,
     ORC_INTRA_HUBSORT = 6,
     ORC_INTRA_DEGREE_ASC = 7,

@@ -31,7 +31,7 @@ DEFAULT_AGGREGATION_TOLERANCE = 0.8
 DEFAULT_TOLERANCE_DROP = 10.0
 
 COMM_ORDERS = {"size-desc": 0, "size-asc": 1, "degree-desc": 2, "degree-asc": 3, "identity": 6}
-INTRA_ORDERS = {"bfs": 0, "rcm": 1, "gorder": 4, "hubsort": 6, "degree-asc": 7, "hub2": 8, "alternate": 9,
+INTRA_ORDERS = {"bfs": 0, "rcm": 1, "rcmpp": 2, "gorder": 4, "hubsort": 6, "degree-asc": 7, "hub2": 8, "alternate": 9,
                 "boundary-last": 11, "core": 12}
 _u64p = np.ctypeslib.ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")
 STDSORT_SO = os.path.join(HERE, "_build", "libstdsort.so")
@@ -46,7 +46,8 @@ class LeidenCfg(C.Structure):
                 ("aggregation_tolerance", C.c_double), ("tolerance_drop", C.c_double),
                 ("max_iterations", C.c_int), ("max_passes", C.c_int),
                 ("total_edges_m", C.c_int), ("super_move_batch", C.c_int),
-                ("parallel", C.c_int), ("threads", C.c_int)]
+                ("parallel", C.c_int), ("threads", C.c_int), ("refine", C.c_int),
+                ("refine_depth", C.c_int)]
 
 
 class LeidenStats(C.Structure):
@@ -190,11 +191,14 @@ def auto_resolution(row_ptr, col) -> float:
 
 
 def leiden(row_ptr, col, resolution, max_iterations=2, max_passes=2, super_move_batch=4096,
-           parallel=False, threads=0, total_edges_m=True):
+           parallel=False, threads=0, total_edges_m=True, refine_depth=None):
+    """refine_depth: None = norefine; k = refine<k> (refinement in passes 0..k,
+    -1 in every pass)."""
     g, keep = _as_graph(row_ptr, col)
     cfg = LeidenCfg(resolution, DEFAULT_TOLERANCE, DEFAULT_AGGREGATION_TOLERANCE,
                     DEFAULT_TOLERANCE_DROP, max_iterations, max_passes, int(total_edges_m),
-                    super_move_batch, int(parallel), threads)
+                    super_move_batch, int(parallel), threads, int(refine_depth is not None),
+                    -1 if refine_depth is None else int(refine_depth))
     memb = np.zeros(g.n, dtype=np.uint32)
     st = LeidenStats()
     rc = load().orc_leiden(C.byref(g), C.byref(cfg), memb, C.byref(st))

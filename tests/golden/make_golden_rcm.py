@@ -1,4 +1,4 @@
-"""Golden outputs of orderCompose with intra-community RCM, from the reference.
+"""Golden outputs of orderCompose with intra-community RCM and RCM++, from the reference.
 
 Run where the reference harness is built (``make -C oracle ref``):
 
@@ -11,7 +11,8 @@ stored), ``rcm_cases.npz`` holds the reference's forward map for
     leiden:compose:sg_none:comm_size_desc:intra_rcm:cd_serial:norefine:2:2
 
 i.e. intraRCM (bench/include/graphbrew/reorder/reorder_graphbrew.h:4000-4134)
-applied to every community.
+applied to every community, and the same with ``intra_rcmpp`` (intraRCMpp,
+:4154-4342) as ``<name>/rcmpp_ids``.
 """
 from __future__ import annotations
 
@@ -29,6 +30,7 @@ import pyoracle as po  # noqa: E402
 from graphbrew_gb300 import graphgen as gg  # noqa: E402
 
 RCM = "leiden:compose:sg_none:comm_size_desc:intra_rcm:cd_serial:norefine:2:2"
+RCMPP = RCM.replace("intra_rcm", "intra_rcmpp")
 
 
 def main():
@@ -41,6 +43,7 @@ def main():
         rp, col = cases[f"{name}/row_ptr"], cases[f"{name}/col"]
         memb = cases[f"{name}/membership_serial"]
         out[f"{name}/rcm_ids"] = po.ref_compose(rp, col, memb, RCM, 1.0)[0]
+        out[f"{name}/rcmpp_ids"] = po.ref_compose(rp, col, memb, RCMPP, 1.0)[0]
     gen = {"rmat12_s3": gg.rmat(12, 16, seed=3), "rmat14_s4": gg.rmat(14, 16, seed=4),
            "grid60x70": gg.grid(60, 70, 0.1, seed=5)}
     for name, (rp, col) in gen.items():
@@ -50,6 +53,7 @@ def main():
         out[f"{name}/col"] = col
         out[f"{name}/membership"] = memb
         out[f"{name}/rcm_ids"] = po.ref_compose(rp, col, memb, RCM, 1.0)[0]
+        out[f"{name}/rcmpp_ids"] = po.ref_compose(rp, col, memb, RCMPP, 1.0)[0]
     np.savez_compressed(os.path.join(HERE, "rcm_cases.npz"), **out)
 
 
