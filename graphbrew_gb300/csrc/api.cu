@@ -151,6 +151,8 @@ gb::LeidenParams leiden_params(const gb::Config& c) {
     p.total_edges_m = c.mComputation == gb::MComputation::TotalEdges;
     p.super_move_batch = c.superGraphMoveBatch;
     p.deterministic = c.deterministicCommunityDetection;
+    p.refine = c.useRefinement;
+    p.refine_depth = c.refinementDepth;
     // Schedule knobs (the autotuner's choices; defaults otherwise).
     if (const char* v = std::getenv("GBGPU_EXACT_MAX_VERTICES")) p.exact_max_vertices = std::atoll(v);
     if (const char* v = std::getenv("GBGPU_EXACT_WINDOW")) p.exact_window = std::max(32LL, std::atoll(v));

@@ -713,7 +713,6 @@ std::string effective_config_json(const Config& c) {
 std::string gpu_unsupported_reason(const Config& c) {
     if (c.algorithm != Algorithm::Leiden) return "community detection 'rabbit' is not on the GPU path";
     if (c.aggregation != Aggregation::GveCSR) return "only gvecsr aggregation is on the GPU path";
-    if (c.useRefinement) return "Leiden refinement is not on the GPU path (use norefine)";
     if (c.ordering != Ordering::Compose) return std::string("ordering '") + ordering_name(c.ordering) +
                                                 "' is not on the GPU path (use compose)";
     if (c.superGraphOrder != SuperGraphOrder::None) return "only super-graph order sg_none is on the GPU path";

@@ -69,6 +69,7 @@ struct LocalMoveContext {
     uint32_t* vcom = nullptr;
     unsigned long long* ctot = nullptr;   // int64 totals (two's complement adds)
     uint8_t* vaff = nullptr;
+    const uint32_t* vcob = nullptr;       // refinement bounds: localMovingPhase<true> when set
     double M = 1.0, R = 1.0;
     std::vector<uint32_t> hubs_h;         // vertices above kWarpMaxDeg, id order
     const uint32_t* hubs = nullptr;

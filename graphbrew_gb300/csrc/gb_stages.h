@@ -46,6 +46,8 @@ struct LeidenParams {
     bool total_edges_m = true;
     int super_move_batch = 1;
     bool deterministic = false;
+    bool refine = false;            // Leiden refinement phase (RG:7330-7392)
+    int refine_depth = -1;          // refinement in passes 0..refine_depth (-1: every pass)
     int chunk_vertices = 2048;      // asynchronous engine: vertices per launch
     int64_t super_single_cta_max_edges = 1 << 24;  // super-move in one thread-block cluster up to this size
     int64_t exact_max_vertices = INT64_MAX; // cd_parallel uses the serial-order engine up to this size

@@ -1064,6 +1064,19 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
     for (; pass < p.max_passes && M > 0; ++pass) {
         GB_CUDA(cudaEventRecord(ea, s));
         const int iters = local_move(tolerance);
+        if (p.refine && (p.refine_depth < 0 || pass <= p.refine_depth)) {
+            // Refinement (RG:7330-7392): bounds = this membership, every vertex
+            // back to a singleton, one sweep of localMovingPhase<true>.
+            GB_REQUIRE(exact, GBGPU_E_UNSUPPORTED, "Leiden refinement needs the serial-order engine");
+            DevBuf<uint32_t> vcob(n, s);
+            GB_CUDA(cudaMemcpyAsync(vcob, vcom, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+            k_init_state<<<grid_for(n, kT), kT, 0, s>>>(g.row_ptr, n, vcom, ctot, vaff);
+            GB_LAUNCH_CHECK();
+            ++launches;
+            lmc.vcob = vcob.get();
+            local_move_exact(lmc, tolerance, 1, p.exact_window, s, &launches, &exact_rounds, &exact_evals);
+            lmc.vcob = nullptr;
+        }
         GB_CUDA(cudaEventRecord(eb, s));
         GB_CUDA(cudaEventSynchronize(eb));
         lm_ms += elapsed(ea, eb);

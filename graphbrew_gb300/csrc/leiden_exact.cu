@@ -108,6 +108,7 @@ struct HubSeg {
 struct ExactState {
     const int64_t* rp;
     const int32_t* col;
+    const uint32_t* vcob;  // refinement bounds (localMovingPhase<true>), null otherwise
     uint32_t* vcom;
     unsigned long long* ctot;
     uint8_t* vaff;
@@ -277,6 +278,18 @@ __device__ __forceinline__ bool prev_mover(const ExactState& a, const Round& r, 
 __device__ __forceinline__ uint32_t comm_at(const ExactState& a, const Round& r, int64_t v, int64_t u) {
     if (v >= r.P && v < u && prev_mover(a, r, v)) return r.pbest[v];
     return a.vcom[v];
+}
+
+// Refinement (scanCommunities<true>, RG:1392-1437): only neighbours inside
+// u's bound count; ub = vcob[u] (0 when not refining).
+__device__ __forceinline__ uint32_t bound_of(const ExactState& a, uint32_t u) { return a.vcob ? a.vcob[u] : 0u; }
+__device__ __forceinline__ bool counts(const ExactState& a, int32_t v, uint32_t u, uint32_t ub) {
+    return v != (int32_t)u && (a.vcob == nullptr || a.vcob[v] == ub);
+}
+// localMovingPhase<true> (RG:1663-1666): a vertex whose community already
+// holds more than itself stays.
+__device__ __forceinline__ bool refine_stays(const ExactState& a, double sigma_d, double ku) {
+    return a.vcob != nullptr && sigma_d > __dmul_rn(ku, 1.001);
 }
 
 __device__ __forceinline__ void record(const ExactState& a, const Round& r, int64_t u, uint8_t act, uint32_t best,
@@ -753,13 +766,29 @@ __device__ __forceinline__ void eval_vertex(const ExactState& a, const Round& r,
         return;
     }
     const double ku = (double)deg;
+    const uint32_t ub = bound_of(a, (uint32_t)u);
     double best_d = 0.0;
     uint32_t best_c = kNone;
     if (!kMid) {
+        if (a.vcob) {
+            long long sg1 = 0;
+            if (lane == 0) {
+                const uint32_t cc[1] = {d};
+                const bool vv[1] = {true};
+                long long o[1];
+                sigma_at_k<1>(a, r.tag, r.P, cc, vv, (uint32_t)u, o);
+                sg1 = o[0];
+            }
+            sg1 = __shfl_sync(0xFFFFFFFFu, sg1, 0);
+            if (refine_stays(a, (double)sg1, ku)) {
+                if (lane == 0) record(a, r, u, 1, d, 0.0);
+                return;
+            }
+        }
         uint32_t c = kNone;
         if (lane < deg) {
             const int32_t v = a.col[rb + lane];
-            if (v != (int32_t)u) c = comm_at(a, r, v, u);
+            if (counts(a, v, (uint32_t)u, ub)) c = comm_at(a, r, v, u);
         }
         const unsigned peers = __match_any_sync(0xFFFFFFFFu, c);
         const double kud = (double)__popc(__ballot_sync(0xFFFFFFFFu, c == d));
@@ -786,7 +815,7 @@ __device__ __forceinline__ void eval_vertex(const ExactState& a, const Round& r,
                 c[k] = kNone;
                 if (e < deg) {
                     const int32_t v = a.col[rb + e];
-                    if (v != (int32_t)u) c[k] = comm_at(a, r, v, u);
+                    if (counts(a, v, (uint32_t)u, ub)) c[k] = comm_at(a, r, v, u);
                 }
             }
 #pragma unroll
@@ -840,6 +869,7 @@ __device__ __forceinline__ void eval_vertex(const ExactState& a, const Round& r,
             if (i0 + 128 >= cnt) break;
         }
         __syncwarp();
+        if (refine_stays(a, sd, ku)) best_c = kNone;   // every lane holds the same sd
     }
     warp_argmax(best_d, best_c);
     if (lane == 0) {
@@ -875,10 +905,12 @@ __global__ void __launch_bounds__(kSmallWarpsPerBlock * 32) k_ex_eval_small(Exac
         int32_t v = -1;
         uint32_t d = kNone;
         bool aff = false;
+        uint32_t ub = 0;
         if (tiny) {
             if (j < deg) v = a.col[rb + j];
             d = a.vcom[u];
             aff = a.vaff[u] != 0;
+            ub = bound_of(a, (uint32_t)u);
         }
         bool pm = false;
         uint32_t cv = kNone;
@@ -889,7 +921,21 @@ __global__ void __launch_bounds__(kSmallWarpsPerBlock * 32) k_ex_eval_small(Exac
                 pm = r.pact[v] == 1 && r.pbest[v] != vc;
                 if (pm) cv = r.pbest[v];
             }
-            if (v == (int32_t)u) cv = kNone;   // self loops never count
+            if (!counts(a, v, (uint32_t)u, ub)) cv = kNone;   // self loops (and, refining, other bounds)
+        }
+        // Refinement: the group's vertex stays when its community already holds more.
+        bool stays = false;
+        if (a.vcob) {
+            long long sg1 = 0;
+            if (tiny && j == 0) {
+                const uint32_t cc[1] = {d};
+                const bool vv[1] = {true};
+                long long o[1];
+                sigma_at_k<1>(a, r.tag, r.P, cc, vv, (uint32_t)u, o);
+                sg1 = o[0];
+            }
+            sg1 = __shfl_sync(0xFFFFFFFFu, sg1, lane & ~7);
+            stays = tiny && refine_stays(a, (double)sg1, (double)deg);
         }
         const unsigned pmb = __ballot_sync(0xFFFFFFFFu, pm);
         const bool act = tiny && (aff || (pmb & gmask) != 0);
@@ -915,7 +961,7 @@ __global__ void __launch_bounds__(kSmallWarpsPerBlock * 32) k_ex_eval_small(Exac
         }
         if (tiny && j == 0) {
             if (!act) record(a, r, u, 0, d, 0.0);
-            else if (best_d > 0.0 && best_c != kNone && best_c != d) record(a, r, u, 1, best_c, best_d);
+            else if (!stays && best_d > 0.0 && best_c != kNone && best_c != d) record(a, r, u, 1, best_c, best_d);
             else record(a, r, u, 1, d, 0.0);
         }
         // Rows of degree 9..32: the whole warp, one row at a time.
@@ -950,6 +996,7 @@ __global__ void __launch_bounds__(kBigThreads, 3) k_ex_eval_big(ExactState a) {
         const int64_t rb = a.rp[u], re = a.rp[u + 1];
         const int deg = (int)(re - rb);
         const uint32_t d = a.vcom[u];
+        const uint32_t ub = bound_of(a, u);
         uint32_t H = 64;
         while (H < 2u * (uint32_t)deg) H <<= 1;
         const uint32_t mask = H - 1;
@@ -969,7 +1016,7 @@ __global__ void __launch_bounds__(kBigThreads, 3) k_ex_eval_big(ExactState a) {
                 if (e < re) {
                     const int32_t v = a.col[e];
                     any = any || (v >= r.P && v < (int64_t)u && prev_mover(a, r, v));
-                    if (v != (int32_t)u) c[k] = comm_at(a, r, v, u);
+                    if (counts(a, v, u, ub)) c[k] = comm_at(a, r, v, u);
                 }
             }
 #pragma unroll
@@ -1039,7 +1086,7 @@ __global__ void __launch_bounds__(kBigThreads, 3) k_ex_eval_big(ExactState a) {
             uint32_t bc = red_c[0];
             for (int k = 1; k < (int)(blockDim.x / 32); ++k)
                 if (better(red_d[k], red_c[k], bd, bc)) { bd = red_d[k]; bc = red_c[k]; }
-            if (bd > 0.0 && bc != kNone && bc != d) record(a, r, u, 1, bc, bd);
+            if (!refine_stays(a, sd, ku) && bd > 0.0 && bc != kNone && bc != d) record(a, r, u, 1, bc, bd);
             else record(a, r, u, 1, d, 0.0);
         }
         __syncthreads();
@@ -1093,6 +1140,7 @@ __global__ void __launch_bounds__(kHubThreads2) k_ex_hub_accum(ExactState a) {
         uint32_t* occ = a.hub_occ + a.hub_toff[sg.hub];
         uint32_t* occn = a.hub_occn + sg.hub;
         const uint32_t d = a.vcom[h];
+        const uint32_t ub = bound_of(a, h);
         if (threadIdx.x == 0) s_any = 0;
         __syncthreads();
         bool any = false;
@@ -1104,7 +1152,7 @@ __global__ void __launch_bounds__(kHubThreads2) k_ex_hub_accum(ExactState a) {
             if (e < e1) {
                 const int32_t v = a.col[e];
                 any = any || (v >= r.P && v < (int64_t)h && prev_mover(a, r, v));
-                if (v != (int32_t)h) c[k] = comm_at(a, r, v, h);
+                if (counts(a, v, h, ub)) c[k] = comm_at(a, r, v, h);
             }
         }
         uint32_t own = 0;
@@ -1219,8 +1267,16 @@ __global__ void __launch_bounds__(kHubThreads2, 3) k_ex_hub_select(ExactState a)
                 for (int k = 1; k < (int)(blockDim.x / 32); ++k)
                     if (better(red_d[k], red_c[k], bd, bc)) { bd = red_d[k]; bc = red_c[k]; }
                 const bool act = a.vaff[h] != 0 || ((volatile int32_t*)a.hub_any)[j] != 0;
+                bool stays = false;
+                if (a.vcob) {
+                    const uint32_t cc[1] = {d};
+                    const bool vv[1] = {true};
+                    long long o[1];
+                    sigma_at_k<1>(a, r.tag, r.P, cc, vv, h, o);
+                    stays = refine_stays(a, (double)o[0], ku);
+                }
                 if (!act) record(a, r, h, 0, d, 0.0);
-                else if (bd > 0.0 && bc != kNone && bc != d) record(a, r, h, 1, bc, bd);
+                else if (!stays && bd > 0.0 && bc != kNone && bc != d) record(a, r, h, 1, bc, bd);
                 else record(a, r, h, 1, d, 0.0);
                 a.hub_done[j] = 0;
                 a.hub_any[j] = 0;
@@ -1604,6 +1660,7 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     a.vcom = ctx.vcom;
     a.ctot = ctx.ctot;
     a.vaff = ctx.vaff;
+    a.vcob = ctx.vcob;
     a.mv = mv.get();
     a.ctl = ctl.get();
     a.best[0] = best0.get();

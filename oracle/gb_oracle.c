@@ -1320,7 +1320,7 @@ static void intra_sorted(const uint32_t *verts, int64_t sz, int order, const uin
     memcpy(tmp, verts, (size_t)sz * sizeof(uint32_t));
     ls_sort(tmp, tmp + sz, key);
     if (order == ORC_INTRA_ALTERNATE) {
-        /* Hubs and leaves interleaved from both ends (RG:6799-6818). */
+        /* Hubs and leaves interleaved from both ends (RG:6806-6824). */
         const int64_t mid = (sz + 1) / 2;
         int64_t lo = 0, hi = sz - 1, p = 0;
         for (int64_t i = 0; i < mid; ++i) {
