@@ -102,13 +102,28 @@ __global__ void k_core_init(const uint32_t* __restrict__ order_v, int64_t nn, co
     }
 }
 
+// The peel's control block: level k, the step's frontier size, the next
+// level when a frontier is empty, vertices left, and done.  Every kernel of a
+// step reads it, so steps are enqueued without the host in between.
+struct CoreCtl {
+    uint32_t k;
+    uint32_t count;
+    uint32_t next;
+    uint32_t pad;
+    long long left;
+    int done;
+    int error;
+};
+
 // Frontier of level k: unpeeled vertices whose remaining degree is <= k,
 // appended with one atomic per CTA.
 __global__ void __launch_bounds__(kT)
-k_core_select(const uint32_t* __restrict__ order_v, int64_t nn, uint32_t k, const uint32_t* __restrict__ cd,
-              const uint32_t* __restrict__ core, uint32_t* __restrict__ frontier, unsigned int* __restrict__ count) {
+k_core_select(const uint32_t* __restrict__ order_v, int64_t nn, const uint32_t* __restrict__ cd,
+              const uint32_t* __restrict__ core, uint32_t* __restrict__ frontier, CoreCtl* __restrict__ ctl) {
     __shared__ unsigned wsum[kT / 32];
     __shared__ unsigned base;
+    if (ctl->done) return;
+    const uint32_t k = ctl->k;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int64_t p0 = (int64_t)blockIdx.x * kT; p0 < nn; p0 += (int64_t)gridDim.x * kT) {
         const int64_t p = p0 + threadIdx.x;
@@ -124,7 +139,7 @@ k_core_select(const uint32_t* __restrict__ order_v, int64_t nn, uint32_t k, cons
         if (threadIdx.x == 0) {
             unsigned t = 0;
             for (int q = 0; q < kT / 32; ++q) t += wsum[q];
-            base = t ? atomicAdd(count, t) : 0u;
+            base = t ? atomicAdd(&ctl->count, t) : 0u;
         }
         __syncthreads();
         unsigned o = base;
@@ -134,12 +149,13 @@ k_core_select(const uint32_t* __restrict__ order_v, int64_t nn, uint32_t k, cons
     }
 }
 
-// Smallest remaining degree of the unpeeled vertices (the next level when a
-// level's frontier is empty), one atomic per CTA.
+// Empty frontier: the smallest remaining degree of the unpeeled vertices is
+// the next level (one atomic per CTA).
 __global__ void __launch_bounds__(kT)
 k_core_min(const uint32_t* __restrict__ order_v, int64_t nn, const uint32_t* __restrict__ cd,
-           const uint32_t* __restrict__ core, unsigned int* __restrict__ out) {
+           const uint32_t* __restrict__ core, CoreCtl* __restrict__ ctl) {
     __shared__ unsigned wmin[kT / 32];
+    if (ctl->done || ctl->count != 0) return;
     unsigned m = 0xFFFFFFFFu;
     for (int64_t p = blockIdx.x * (int64_t)kT + threadIdx.x; p < nn; p += (int64_t)gridDim.x * kT) {
         const uint32_t v = order_v[p];
@@ -149,34 +165,47 @@ k_core_min(const uint32_t* __restrict__ order_v, int64_t nn, const uint32_t* __r
     if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = m;
     __syncthreads();
     if (threadIdx.x == 0) {
-        for (int q = 1; q < kT / 32; ++q) m = min(m, wmin[q]);
-        m = min(m, wmin[0]);
-        if (m != 0xFFFFFFFFu) atomicMin(out, m);
+        for (int q = 0; q < kT / 32; ++q) m = min(m, wmin[q]);
+        if (m != 0xFFFFFFFFu) atomicMin(&ctl->next, m);
     }
 }
 
-__global__ void k_core_assign(const uint32_t* __restrict__ frontier, const unsigned int* __restrict__ ctr, uint32_t k,
-                              uint32_t* __restrict__ core) {
-    const unsigned cnt = ctr[0];
-    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) core[frontier[i]] = k;
-}
-
-// One warp per peeled vertex: its unpeeled neighbours in the community lose one.
-__global__ void k_core_decrement(const uint32_t* __restrict__ frontier, const unsigned int* __restrict__ ctr,
-                                 const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
-                                 const uint32_t* __restrict__ memb, const uint32_t* __restrict__ core,
-                                 uint32_t* __restrict__ cd) {
+// One warp per peeled vertex: its core number is k, and its unpeeled
+// neighbours in the community lose one (a neighbour in the same frontier
+// may lose one too; it is peeled at k all the same).
+__global__ void k_core_apply(const uint32_t* __restrict__ frontier, const int64_t* __restrict__ rp,
+                             const int32_t* __restrict__ col, const uint32_t* __restrict__ memb,
+                             uint32_t* __restrict__ core, uint32_t* __restrict__ cd, const CoreCtl* __restrict__ ctl) {
+    if (ctl->done) return;
+    const uint32_t cnt = ctl->count, k = ctl->k;
     const int lane = threadIdx.x & 31;
-    const unsigned cnt = ctr[0];
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; i < (int64_t)cnt; i += nw) {
         const uint32_t v = frontier[i];
+        if (lane == 0) core[v] = k;
         const uint32_t c = memb[v];
         for (int64_t e = rp[v] + lane; e < rp[v + 1]; e += 32) {
             const uint32_t u = (uint32_t)col[e];
-            if (memb[u] == c && core[u] == kCoreUnset) atomicSub(&cd[u], 1u);
+            if (u != v && memb[u] == c && core[u] == kCoreUnset) atomicSub(&cd[u], 1u);
         }
     }
+}
+
+__global__ void k_core_ctl(CoreCtl* ctl) {
+    if (ctl->done) return;
+    if (ctl->count == 0) {
+        if (ctl->next == 0xFFFFFFFFu || ctl->next <= ctl->k) {
+            ctl->error = 1;   // unpeeled vertices but no level to go to
+            ctl->done = 1;
+        } else {
+            ctl->k = ctl->next;
+        }
+    } else {
+        ctl->left -= ctl->count;
+        if (ctl->left <= 0) ctl->done = 1;
+    }
+    ctl->count = 0;
+    ctl->next = 0xFFFFFFFFu;
 }
 
 // ---- keys and segments ----
@@ -404,7 +433,7 @@ __global__ void k_seg_final(Segs s) {
 }
 
 // Local ids: position inside the community, or Alternate's interleave of
-// both ends (RG:6799-6818).
+// both ends (RG:6806-6824).
 __global__ void k_sorted_local(const uint32_t* __restrict__ E, int64_t nn, const uint32_t* __restrict__ ranks,
                                const int64_t* __restrict__ offs, const int64_t* __restrict__ ssize, bool alternate,
                                uint32_t* __restrict__ local) {
@@ -451,39 +480,32 @@ int64_t sorted_communities(const DeviceCSR& g, const uint32_t* memb, int intra, 
     }
     if (intra == kCore) {
         // aux holds the internal degree; peel it into core numbers, in place.
+        // Steps are enqueued in batches; the host reads the control block once
+        // per batch.  Every step peels at least one vertex or raises the
+        // level, so at most 2 nn steps run.
         DevBuf<uint32_t> cd(n, s), core(n, s), frontier(nn, s);
-        DevBuf<unsigned int> ctr(2, s);
+        DevBuf<CoreCtl> ctl(1, s);
+        const CoreCtl init{0u, 0u, 0xFFFFFFFFu, 0u, (long long)nn, 0, 0};
+        GB_CUDA(cudaMemcpyAsync(ctl, &init, sizeof(init), cudaMemcpyHostToDevice, s));
         k_core_init<<<grid_for(nn, kT), kT, 0, s>>>(order_v, nn, aux, cd, core);
         GB_LAUNCH_CHECK();
-        uint32_t k = 0;
-        int64_t left = nn;
-        while (left > 0) {
-            GB_CUDA(cudaMemsetAsync(ctr, 0, sizeof(unsigned int), s));
-            k_core_select<<<grid_for(nn, kT), kT, 0, s>>>(order_v, nn, k, cd, core, frontier, ctr);
-            GB_LAUNCH_CHECK();
-            unsigned int h[1];
-            GB_CUDA(cudaMemcpyAsync(h, ctr.get(), sizeof(h), cudaMemcpyDeviceToHost, s));
-            GB_CUDA(cudaStreamSynchronize(s));
-            nl += 1;
-            if (h[0] == 0) {
-                GB_CUDA(cudaMemsetAsync(ctr.get() + 1, 0xFF, sizeof(unsigned int), s));
-                k_core_min<<<grid_for(nn, kT), kT, 0, s>>>(order_v, nn, cd, core, ctr.get() + 1);
-                GB_LAUNCH_CHECK();
-                const unsigned int next = read_dev(ctr.get() + 1, s);
-                nl += 1;
-                GB_REQUIRE(next != 0xFFFFFFFFu && next > k, GBGPU_E_CUDA, "core peel made no progress");
-                k = next;
-                continue;
+        constexpr int kStepsPerCheck = 16;
+        const int g_all = grid_for(nn, kT);
+        const int g_apply = kNumSMs * 8;
+        CoreCtl h{};
+        for (int64_t steps = 0; steps <= 2 * nn + kStepsPerCheck; steps += kStepsPerCheck) {
+            for (int q = 0; q < kStepsPerCheck; ++q) {
+                k_core_select<<<g_all, kT, 0, s>>>(order_v, nn, cd, core, frontier, ctl);
+                k_core_min<<<g_all, kT, 0, s>>>(order_v, nn, cd, core, ctl);
+                k_core_apply<<<g_apply, kT, 0, s>>>(frontier, g.row_ptr, g.col, memb, core, cd, ctl);
+                k_core_ctl<<<1, 1, 0, s>>>(ctl);
             }
-            const int g1 = (int)std::min<int64_t>(ceil_div(h[0], kT), (int64_t)kNumSMs * 8);
-            k_core_assign<<<g1, kT, 0, s>>>(frontier, ctr, k, core);
             GB_LAUNCH_CHECK();
-            const int g2 = (int)std::min<int64_t>(ceil_div((int64_t)h[0] * 32, kT), (int64_t)kNumSMs * 8);
-            k_core_decrement<<<g2, kT, 0, s>>>(frontier, ctr, g.row_ptr, g.col, memb, core, cd);
-            GB_LAUNCH_CHECK();
-            nl += 2;
-            left -= h[0];
+            nl += 4 * kStepsPerCheck;
+            h = read_dev(ctl.get(), s);
+            if (h.done) break;
         }
+        GB_REQUIRE(h.done && !h.error, GBGPU_E_CUDA, "core peel made no progress");
         GB_CUDA(cudaMemcpyAsync(aux, core, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
     }
 

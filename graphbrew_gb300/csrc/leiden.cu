@@ -790,7 +790,9 @@ k_super_move_cluster(SmArgs a, int max_iter, int* iters_out, long long* moves_ou
     }
 }
 
-// Multi-CTA variant: one launch pair per batch.
+// Batched launches for super-graphs above one cluster's size: per batch,
+// warps propose the super-nodes up to kBigSuper neighbours (shared tables,
+// then per-warp global tables), CTAs the bigger ones, then the commit.
 __global__ void k_super_propose_batch(SmArgs a, int64_t bt) {
     __shared__ uint32_t tk[8][kSmSmall];
     __shared__ uint32_t tv[8][kSmSmall];
@@ -798,8 +800,24 @@ __global__ void k_super_propose_batch(SmArgs a, int64_t bt) {
     const int64_t lo = a.bstart[bt], hi = a.bstart[bt + 1];
     const int64_t gw = (int64_t)blockIdx.x * 8 + w;
     const int64_t nwt = (int64_t)gridDim.x * 8;
-    for (int64_t i = lo + gw; i < hi; i += nwt)
-        super_propose(a, a.active[i], tk[w], tv[w], a.gkeys + gw * a.gcap, a.gvals + gw * a.gcap);
+    for (int64_t i = lo + gw; i < hi; i += nwt) {
+        const uint32_t c = a.active[i];
+        if (a.soff[c + 1] - a.soff[c] > kBigSuper) continue;
+        super_propose(a, c, tk[w], tv[w], a.gkeys + gw * a.gcap, a.gvals + gw * a.gcap);
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_super_propose_big_batch(SmArgs a, int64_t bt) {
+    __shared__ SmProposal bprop;
+    __shared__ double red_d[32];
+    __shared__ uint32_t red_c[32];
+    for (int64_t j = a.bigstart[bt] + blockIdx.x; j < a.bigstart[bt + 1]; j += gridDim.x) {
+        super_propose_block(a, a.big_active[j], &bprop, red_d, red_c);
+        if (threadIdx.x == 0) {
+            a.proposed[bprop.c] = bprop.best;
+            a.pdelta[bprop.c] = bprop.delta;
+        }
+    }
 }
 
 __global__ void k_super_commit_batch(SmArgs a, int64_t bt, int* moves) {
@@ -1177,7 +1195,7 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
             const bool single = nuniq <= p.super_single_cta_max_edges;
             // The cluster kernel gives super-nodes above kBigSuper neighbours a
             // CTA each; warps then need tables for at most kBigSuper.
-            const int64_t warp_max = single ? std::min<int64_t>(max_sdeg, kBigSuper) : max_sdeg;
+            const int64_t warp_max = std::min<int64_t>(max_sdeg, kBigSuper);
             int64_t gcap = 64;
             while (gcap < 2 * warp_max) gcap <<= 1;
             int64_t bcap = 64;
@@ -1185,7 +1203,7 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
             int64_t nbig = 0;
             DevBuf<uint32_t> big_active;
             DevBuf<int64_t> bigstart(nbatch + 1, s);
-            if (single) {
+            {
                 DevBuf<int32_t> bflag(na, s);
                 DevBuf<int64_t> bpos(na + 1, s);
                 k_big_super_flags<<<grid_for(na, kT), kT, 0, s>>>(active, na, soff, kBigSuper, bflag);
@@ -1202,13 +1220,25 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
                 launches += 6;
             }
             const int cluster = super_cluster_size(sm_smem);
-            DevBuf<uint32_t> bk(single && nbig ? (int64_t)cluster * bcap : 1, s);
-            DevBuf<uint32_t> bv(single && nbig ? (int64_t)cluster * bcap : 1, s);
-            // Per-warp global tables for super-nodes above kSmSmall / 2 neighbours,
-            // capped at 512 MB in total.
-            int64_t nwarps_total = single ? (int64_t)cluster * 32 : (int64_t)kNumSMs * 4 * 8;
-            if (!single && gcap > kSmSmall)
-                nwarps_total = std::max<int64_t>(8, std::min<int64_t>(nwarps_total, ((int64_t)1 << 26) / gcap) / 8 * 8);
+            // Batched launches: the big super-nodes of a batch get one CTA each.
+            std::vector<int64_t> bs, bgs;
+            int64_t max_big_in_batch = 0;
+            if (!single) {
+                bs.resize(nbatch + 1);
+                bgs.resize(nbatch + 1);
+                GB_CUDA(cudaMemcpyAsync(bs.data(), bstart.get(), (nbatch + 1) * sizeof(int64_t),
+                                        cudaMemcpyDeviceToHost, s));
+                GB_CUDA(cudaMemcpyAsync(bgs.data(), bigstart.get(), (nbatch + 1) * sizeof(int64_t),
+                                        cudaMemcpyDeviceToHost, s));
+                GB_CUDA(cudaStreamSynchronize(s));
+                for (int64_t bt = 0; bt < nbatch; ++bt) max_big_in_batch = std::max(max_big_in_batch, bgs[bt + 1] - bgs[bt]);
+            }
+            const int big_grid = (int)std::min<int64_t>(std::max<int64_t>(1, max_big_in_batch), kNumSMs);
+            const int64_t big_tables = nbig ? (single ? (int64_t)cluster : (int64_t)big_grid) * bcap : 1;
+            DevBuf<uint32_t> bk(big_tables, s);
+            DevBuf<uint32_t> bv(big_tables, s);
+            // Per-warp global tables for super-nodes of kSmSmall / 2 .. kBigSuper neighbours.
+            const int64_t nwarps_total = single ? (int64_t)cluster * 32 : (int64_t)kNumSMs * 4 * 8;
             DevBuf<uint32_t> gk(gcap > kSmSmall ? nwarps_total * gcap : 1, s);
             DevBuf<uint32_t> gv(gcap > kSmSmall ? nwarps_total * gcap : 1, s);
             DevBuf<uint8_t> light(nbatch, s);
@@ -1248,22 +1278,27 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
                 super_iters += read_dev(iters_d.get(), s);
                 super_moves += read_dev(moves_d.get(), s);
             } else {
-                std::vector<int64_t> bs(nbatch + 1);
-                GB_CUDA(cudaMemcpyAsync(bs.data(), bstart.get(), (nbatch + 1) * sizeof(int64_t),
-                                        cudaMemcpyDeviceToHost, s));
-                GB_CUDA(cudaStreamSynchronize(s));
                 DevBuf<int> mv(1, s);
                 for (int it = 0; it < super_max_iter; ++it) {
                     GB_CUDA(cudaMemsetAsync(mv, 0, sizeof(int), s));
                     for (int64_t bt = 0; bt < nbatch; ++bt) {
                         const int64_t cnt = bs[bt + 1] - bs[bt];
                         if (cnt == 0) continue;
-                        const int grid = (int)std::min<int64_t>(ceil_div(cnt, 8), nwarps_total / 8);
-                        k_super_propose_batch<<<grid, 256, 0, s>>>(sa, bt);
-                        GB_LAUNCH_CHECK();
+                        const int64_t nb = bgs[bt + 1] - bgs[bt];
+                        if (cnt > nb) {
+                            const int grid = (int)std::min<int64_t>(ceil_div(cnt - nb, 8), nwarps_total / 8);
+                            k_super_propose_batch<<<grid, 256, 0, s>>>(sa, bt);
+                            GB_LAUNCH_CHECK();
+                            ++launches;
+                        }
+                        if (nb > 0) {
+                            k_super_propose_big_batch<<<(int)std::min<int64_t>(nb, big_grid), 1024, 0, s>>>(sa, bt);
+                            GB_LAUNCH_CHECK();
+                            ++launches;
+                        }
                         k_super_commit_batch<<<(int)std::min<int64_t>(ceil_div(cnt, 256), 1024), 256, 0, s>>>(sa, bt, mv);
                         GB_LAUNCH_CHECK();
-                        launches += 2;
+                        ++launches;
                     }
                     ++super_iters;
                     const int moved = read_dev(mv.get(), s);

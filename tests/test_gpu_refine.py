@@ -59,3 +59,19 @@ def test_refine_rmat_against_oracle(ctx, scale):
     memb, _ = po.leiden(rp, col, ar, refine_depth=0)
     ids_orc, _ = po.compose(rp, col, memb)
     np.testing.assert_array_equal(ids.cpu().numpy(), ids_orc)
+
+
+@pytest.mark.parametrize("refine", [False, True])
+def test_batched_super_move_against_oracle(ctx, monkeypatch, refine):
+    """The super-move's batched launches (used above one cluster's size;
+    forced here) give the cluster kernel's memberships: warps for super-nodes
+    up to 1,024 neighbours, a CTA each above."""
+    monkeypatch.setenv("GBGPU_SUPER_CLUSTER_MAX_EDGES", "0")
+    rp_t, col_t = gg.rmat(17, 16, seed=400, device="cuda")
+    rp, col = rp_t.cpu().numpy(), col_t.cpu().numpy()
+    ar = po.auto_resolution(rp, col)
+    recipe = REFINE if refine else REFINE.replace("refine0", "norefine")
+    memb, st = ctx.run_graphbrew(rp_t, col_t, recipe, ar)
+    assert st["super_move_ctas"] == 0
+    want, _ = po.leiden(rp, col, ar, refine_depth=0 if refine else None)
+    np.testing.assert_array_equal(memb.cpu().numpy().view(np.uint32), want)
