@@ -407,63 +407,6 @@ struct SmArgs {
 
 constexpr int kSmSmall = 256;     // per-warp shared table slots
 
-// Proposal for super-node c by one warp (proposals of :2264-2302).
-__device__ void super_propose(const SmArgs& a, uint32_t c, uint32_t* tk, uint32_t* tv, uint32_t* gk, uint32_t* gv) {
-    const int lane = threadIdx.x & 31;
-    const int64_t b = a.soff[c], e = a.soff[c + 1];
-    const int64_t deg = e - b;
-    uint32_t H = 64;
-    while ((int64_t)H < 2 * deg) H <<= 1;
-    uint32_t *k = tk, *v = tv;
-    if (H > (uint32_t)kSmSmall) { k = gk; v = gv; }
-    const uint32_t mask = H - 1;
-    for (uint32_t i = lane; i < H; i += 32) { k[i] = kNone; v[i] = 0; }
-    __syncwarp();
-    for (int64_t i0 = b; i0 < e; i0 += 32) {
-        uint32_t key = kNone, wgt = 0;
-        if (i0 + lane < e) {
-            key = a.scomm[a.snbr[i0 + lane]];
-            wgt = a.sw[i0 + lane];
-        }
-        const unsigned peers = __match_any_sync(0xFFFFFFFFu, key);
-        uint32_t sum = wgt;
-        // sum weights of peers (small groups): leader gathers by shuffles
-        for (int l = 0; l < 32; ++l) {
-            const uint32_t ow = __shfl_sync(0xFFFFFFFFu, wgt, l);
-            if (l != lane && ((peers >> l) & 1u)) sum += ow;
-        }
-        if (key != kNone && lane == __ffs(peers) - 1) table_add(k, v, mask, key, sum);
-    }
-    __syncwarp();
-    const uint32_t d = a.scomm[c];
-    const double kc = (double)a.sweight[c];
-    const double sigma_d = (double)(long long)a.sctot[d];
-    const double removal = __ddiv_rn(__dmul_rn(__dmul_rn(a.R, kc), __dsub_rn(sigma_d, kc)), a.M);
-    const double kc_to_d = (double)table_get(k, v, mask, d);
-    double best_d = 0.0;
-    uint32_t best_c = d;
-    for (uint32_t i = lane; i < H; i += 32) {
-        const uint32_t ek = k[i];
-        if (ek == kNone) continue;
-        const double kce = (double)v[i];
-        double add;
-        if (ek == d) {
-            add = __dsub_rn(kc_to_d, removal);
-        } else {
-            const double se = (double)(long long)a.sctot[ek];
-            add = __dsub_rn(kce, __ddiv_rn(__dmul_rn(__dmul_rn(a.R, kc), se), a.M));
-        }
-        const double dl = __dadd_rn(__dsub_rn(add, removal), kc_to_d);
-        if (better(dl, ek, best_d, best_c)) { best_d = dl; best_c = ek; }
-    }
-    warp_argmax(best_d, best_c);
-    if (lane == 0) {
-        a.proposed[c] = best_c;
-        a.pdelta[c] = best_d;
-    }
-    __syncwarp();
-}
-
 __device__ __forceinline__ void super_commit(const SmArgs& a, uint32_t c, int* moves) {
     const uint32_t d = a.scomm[c];
     const uint32_t best = a.proposed[c];
@@ -498,8 +441,11 @@ struct SmProposal {
     double delta;
 };
 
-// Proposal for super-node c (as super_propose) with a shared table whose
-// third array holds the candidates' totals, loaded by the inserting lane.
+// Proposal for super-node c by one warp (the GVE super-move proposals of
+// RG:2264-2302): neighbour communities into a shared table (a per-warp
+// global one above kSmSmall / 2 neighbours) whose third array caches each
+// candidate's total, loaded by the inserting lane; best Delta-modularity,
+// ties to the smaller community.
 __device__ void super_propose_cached(const SmArgs& a, uint32_t c, uint32_t* tk, uint32_t* tv,
                                      unsigned long long* tt, uint32_t* gk, uint32_t* gv, SmProposal& out) {
     const int lane = threadIdx.x & 31;
@@ -796,14 +742,20 @@ k_super_move_cluster(SmArgs a, int max_iter, int* iters_out, long long* moves_ou
 __global__ void k_super_propose_batch(SmArgs a, int64_t bt) {
     __shared__ uint32_t tk[8][kSmSmall];
     __shared__ uint32_t tv[8][kSmSmall];
-    const int w = threadIdx.x >> 5;
+    __shared__ unsigned long long tt[8][kSmSmall];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t lo = a.bstart[bt], hi = a.bstart[bt + 1];
     const int64_t gw = (int64_t)blockIdx.x * 8 + w;
     const int64_t nwt = (int64_t)gridDim.x * 8;
     for (int64_t i = lo + gw; i < hi; i += nwt) {
         const uint32_t c = a.active[i];
         if (a.soff[c + 1] - a.soff[c] > kBigSuper) continue;
-        super_propose(a, c, tk[w], tv[w], a.gkeys + gw * a.gcap, a.gvals + gw * a.gcap);
+        SmProposal pr;
+        super_propose_cached(a, c, tk[w], tv[w], tt[w], a.gkeys + gw * a.gcap, a.gvals + gw * a.gcap, pr);
+        if (lane == 0) {
+            a.proposed[pr.c] = pr.best;
+            a.pdelta[pr.c] = pr.delta;
+        }
     }
 }
 
