@@ -403,6 +403,7 @@ struct SmArgs {
     // Batches of at most kLightNodes super-nodes of degree <= kLightDeg: one
     // thread per super-node on the cluster's first CTA.
     const uint8_t* light;
+    int64_t warp_max;             // batched launches: warps take super-nodes up to this degree
 };
 
 constexpr int kSmSmall = 256;     // per-warp shared table slots
@@ -429,6 +430,7 @@ constexpr int kSmCluster = 8;     // portable cluster size
 constexpr int kSmClusterMax = 16; // non-portable size, used where the GPU can place it
 constexpr int kSmPerWarp = 16;    // proposals a warp keeps per batch (4096 / (8 x 32))
 constexpr int kBigSuper = 1024;   // super-nodes with more neighbours: one CTA each
+constexpr int kBigSuperBatched = kSmSmall / 2;   // batched launches: warps only with shared tables
 
 __device__ __forceinline__ void cluster_sync_all() {
     asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
@@ -737,8 +739,8 @@ k_super_move_cluster(SmArgs a, int max_iter, int* iters_out, long long* moves_ou
 }
 
 // Batched launches for super-graphs above one cluster's size: per batch,
-// warps propose the super-nodes up to kBigSuper neighbours (shared tables,
-// then per-warp global tables), CTAs the bigger ones, then the commit.
+// warps propose the super-nodes up to kBigSuperBatched neighbours (shared
+// tables), CTAs the bigger ones, then the commit.
 __global__ void k_super_propose_batch(SmArgs a, int64_t bt) {
     __shared__ uint32_t tk[8][kSmSmall];
     __shared__ uint32_t tv[8][kSmSmall];
@@ -749,7 +751,7 @@ __global__ void k_super_propose_batch(SmArgs a, int64_t bt) {
     const int64_t nwt = (int64_t)gridDim.x * 8;
     for (int64_t i = lo + gw; i < hi; i += nwt) {
         const uint32_t c = a.active[i];
-        if (a.soff[c + 1] - a.soff[c] > kBigSuper) continue;
+        if (a.soff[c + 1] - a.soff[c] > a.warp_max) continue;
         SmProposal pr;
         super_propose_cached(a, c, tk[w], tv[w], tt[w], a.gkeys + gw * a.gcap, a.gvals + gw * a.gcap, pr);
         if (lane == 0) {
@@ -1147,7 +1149,8 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
             const bool single = nuniq <= p.super_single_cta_max_edges;
             // The cluster kernel gives super-nodes above kBigSuper neighbours a
             // CTA each; warps then need tables for at most kBigSuper.
-            const int64_t warp_max = std::min<int64_t>(max_sdeg, kBigSuper);
+            const int64_t big_min = single ? kBigSuper : kBigSuperBatched;   // degree above: a CTA each
+            const int64_t warp_max = std::min<int64_t>(max_sdeg, big_min);
             int64_t gcap = 64;
             while (gcap < 2 * warp_max) gcap <<= 1;
             int64_t bcap = 64;
@@ -1158,7 +1161,7 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
             {
                 DevBuf<int32_t> bflag(na, s);
                 DevBuf<int64_t> bpos(na + 1, s);
-                k_big_super_flags<<<grid_for(na, kT), kT, 0, s>>>(active, na, soff, kBigSuper, bflag);
+                k_big_super_flags<<<grid_for(na, kT), kT, 0, s>>>(active, na, soff, big_min, bflag);
                 GB_LAUNCH_CHECK();
                 exclusive_scan_i32_to_i64(bflag, bpos, na, bpos.get() + na, s);
                 nbig = read_dev(bpos.get() + na, s);
@@ -1202,7 +1205,7 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
             }
             SmArgs sa{soff, snbr, sw, sweight, scomm, sctot, active, bstart, nbatch, proposed, pdelta, M, R,
                       gk, gv, gcap > kSmSmall ? gcap : 0, big_active.get(), bigstart.get(), bk.get(), bv.get(),
-                      bcap, light.get()};
+                      bcap, light.get(), big_min};
             DevBuf<int> iters_d(1, s), gmoves(super_max_iter, s);
             DevBuf<long long> moves_d(1, s);
             launches += 2;

@@ -65,7 +65,7 @@ def test_refine_rmat_against_oracle(ctx, scale):
 def test_batched_super_move_against_oracle(ctx, monkeypatch, refine):
     """The super-move's batched launches (used above one cluster's size;
     forced here) give the cluster kernel's memberships: warps for super-nodes
-    up to 1,024 neighbours, a CTA each above."""
+    up to 128 neighbours, a CTA each above."""
     monkeypatch.setenv("GBGPU_SUPER_CLUSTER_MAX_EDGES", "0")
     rp_t, col_t = gg.rmat(17, 16, seed=400, device="cuda")
     rp, col = rp_t.cpu().numpy(), col_t.cpu().numpy()
