@@ -404,6 +404,22 @@ struct SmArgs {
     // thread per super-node on the cluster's first CTA.
     const uint8_t* light;
     int64_t warp_max;             // batched launches: warps take super-nodes up to this degree
+    // Batched launches: super-nodes above huge_min neighbours are split over
+    // several CTAs (edge segments accumulate into one table per node, table
+    // segments select, the last CTA of a node reduces).  huge_min 0: none.
+    int64_t huge_min;
+    const uint32_t* huge_c;       // huge super-nodes, id order
+    const int64_t* huge_toff;     // table offset in the pool
+    const uint32_t* huge_tcap;    // table capacity (pow2 >= 2 x degree)
+    const int32_t* huge_tfirst;   // first table segment of each node
+    const int32_t* huge_tcount;   // table segments of each node
+    int32_t* huge_done;           // table segments finished, per node
+    const int2* huge_eseg;        // (node, part) of every edge segment
+    const int2* huge_tseg;        // (node, part) of every table segment
+    uint32_t* hkeys;              // table pool
+    uint32_t* hvals;
+    double* part_d;               // best of each table segment
+    uint32_t* part_c;
 };
 
 constexpr int kSmSmall = 256;     // per-warp shared table slots
@@ -766,10 +782,107 @@ __global__ void __launch_bounds__(1024) k_super_propose_big_batch(SmArgs a, int6
     __shared__ double red_d[32];
     __shared__ uint32_t red_c[32];
     for (int64_t j = a.bigstart[bt] + blockIdx.x; j < a.bigstart[bt + 1]; j += gridDim.x) {
-        super_propose_block(a, a.big_active[j], &bprop, red_d, red_c);
+        const uint32_t c = a.big_active[j];
+        if (a.huge_min > 0 && a.soff[c + 1] - a.soff[c] > a.huge_min) continue;   // split over CTAs
+        super_propose_block(a, c, &bprop, red_d, red_c);
         if (threadIdx.x == 0) {
             a.proposed[bprop.c] = bprop.best;
             a.pdelta[bprop.c] = bprop.delta;
+        }
+    }
+}
+
+// Huge super-nodes, first half: each CTA inserts one segment of kHugeSeg
+// neighbour entries into the node's table (the pool is cleared before every
+// iteration of the super-move).
+constexpr int kHugeSeg = 4096;    // entries (edges or table slots) per CTA: 4 per thread
+
+__global__ void __launch_bounds__(1024) k_super_huge_accum(SmArgs a, int64_t seg0) {
+    const int2 sg = a.huge_eseg[seg0 + blockIdx.x];
+    const uint32_t c = a.huge_c[sg.x];
+    const int64_t e = a.soff[c + 1];
+    const int64_t e0 = a.soff[c] + (int64_t)sg.y * kHugeSeg, e1 = min(e, e0 + kHugeSeg);
+    uint32_t* k = a.hkeys + a.huge_toff[sg.x];
+    uint32_t* v = a.hvals + a.huge_toff[sg.x];
+    const uint32_t mask = a.huge_tcap[sg.x] - 1;
+    uint32_t key[4], w[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int64_t i = e0 + q * (int64_t)blockDim.x + threadIdx.x;
+        key[q] = i < e1 ? a.scomm[a.snbr[i]] : kNone;
+        w[q] = i < e1 ? a.sw[i] : 0u;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+        if (key[q] != kNone) table_add(k, v, mask, key[q], w[q]);
+}
+
+// Second half: each CTA scores one segment of the node's table slots with
+// super_propose_block's arithmetic; the last CTA of the node takes the best
+// of the segments' bests (the selection is a total order, so the split does
+// not change it) and records the proposal.
+__global__ void __launch_bounds__(1024) k_super_huge_select(SmArgs a, int64_t seg0) {
+    __shared__ double red_d[32];
+    __shared__ uint32_t red_c[32];
+    __shared__ int s_last;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int64_t q = seg0 + blockIdx.x;
+    const int2 sg = a.huge_tseg[q];
+    const int j = sg.x;
+    const uint32_t c = a.huge_c[j];
+    const uint32_t* k = a.hkeys + a.huge_toff[j];
+    const uint32_t* v = a.hvals + a.huge_toff[j];
+    const uint32_t H = a.huge_tcap[j], mask = H - 1;
+    const uint32_t d = a.scomm[c];
+    const long long kcl = a.sweight[c];
+    const double kc = (double)kcl;
+    const double sigma_d = (double)(long long)a.sctot[d];
+    const double removal = __ddiv_rn(__dmul_rn(__dmul_rn(a.R, kc), __dsub_rn(sigma_d, kc)), a.M);
+    const double kc_to_d = (double)table_get(k, v, mask, d);
+    double best_d = 0.0;
+    uint32_t best_c = d;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const uint32_t i = (uint32_t)sg.y * kHugeSeg + r * blockDim.x + tid;
+        if (i >= H) continue;
+        const uint32_t ek = k[i];
+        if (ek == kNone) continue;
+        const double kce = (double)v[i];
+        double add;
+        if (ek == d) {
+            add = __dsub_rn(kc_to_d, removal);
+        } else {
+            const double se = (double)(long long)a.sctot[ek];
+            add = __dsub_rn(kce, __ddiv_rn(__dmul_rn(__dmul_rn(a.R, kc), se), a.M));
+        }
+        const double dl = __dadd_rn(__dsub_rn(add, removal), kc_to_d);
+        if (better(dl, ek, best_d, best_c)) { best_d = dl; best_c = ek; }
+    }
+    warp_argmax(best_d, best_c);
+    if (lane == 0) { red_d[w] = best_d; red_c[w] = best_c; }
+    __syncthreads();
+    if (tid == 0) {
+        double bd = red_d[0];
+        uint32_t bc = red_c[0];
+        for (int r = 1; r < (int)(blockDim.x >> 5); ++r)
+            if (better(red_d[r], red_c[r], bd, bc)) { bd = red_d[r]; bc = red_c[r]; }
+        a.part_d[q] = bd;
+        a.part_c[q] = bc;
+        __threadfence();
+        s_last = atomicAdd(&a.huge_done[j], 1) == a.huge_tcount[j] - 1;
+        if (s_last) {
+            __threadfence();
+            const int f = a.huge_tfirst[j], nt = a.huge_tcount[j];
+            bd = ((volatile double*)a.part_d)[f];
+            bc = ((volatile uint32_t*)a.part_c)[f];
+            for (int r = 1; r < nt; ++r) {
+                const double pd = ((volatile double*)a.part_d)[f + r];
+                const uint32_t pc = ((volatile uint32_t*)a.part_c)[f + r];
+                if (better(pd, pc, bd, bc)) { bd = pd; bc = pc; }
+            }
+            a.proposed[c] = bc;
+            a.pdelta[c] = bd;
+            a.huge_done[j] = 0;
         }
     }
 }
@@ -1153,8 +1266,12 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
             const int64_t warp_max = std::min<int64_t>(max_sdeg, big_min);
             int64_t gcap = 64;
             while (gcap < 2 * warp_max) gcap <<= 1;
+            // Batched launches split super-nodes above kHugeSeg over CTAs; the
+            // per-CTA tables then only hold the ones below.
+            const int64_t split_min = std::max<int64_t>(big_min, p.super_split_min);
+            const bool split_huge = !single && max_sdeg > split_min;
             int64_t bcap = 64;
-            while (bcap < 2 * max_sdeg) bcap <<= 1;
+            while (bcap < 2 * (split_huge ? split_min : max_sdeg)) bcap <<= 1;
             int64_t nbig = 0;
             DevBuf<uint32_t> big_active;
             DevBuf<int64_t> bigstart(nbatch + 1, s);
@@ -1206,6 +1323,86 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
             SmArgs sa{soff, snbr, sw, sweight, scomm, sctot, active, bstart, nbatch, proposed, pdelta, M, R,
                       gk, gv, gcap > kSmSmall ? gcap : 0, big_active.get(), bigstart.get(), bk.get(), bv.get(),
                       bcap, light.get(), big_min};
+            // Batched launches: super-nodes above kHugeSeg neighbours, split over CTAs.
+            struct HugeBatch { int64_t e0 = 0, ne = 0, t0 = 0, nt = 0; };
+            std::vector<HugeBatch> hb;
+            DevBuf<uint32_t> huge_c, hkeys, hvals, part_c;
+            DevBuf<int64_t> huge_toff;
+            DevBuf<uint32_t> huge_tcap;
+            DevBuf<int32_t> huge_tfirst, huge_tcount, huge_done;
+            DevBuf<int2> huge_eseg, huge_tseg;
+            DevBuf<double> part_d;
+            int64_t hpool = 0;
+            if (split_huge && nbig > 0) {
+                std::vector<uint32_t> big_h(nbig);
+                std::vector<int64_t> soff_h(C + 1);
+                GB_CUDA(cudaMemcpyAsync(big_h.data(), big_active.get(), nbig * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                        s));
+                GB_CUDA(cudaMemcpyAsync(soff_h.data(), soff, (C + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+                GB_CUDA(cudaStreamSynchronize(s));
+                std::vector<uint32_t> hc, htcap;
+                std::vector<int64_t> htoff;
+                std::vector<int32_t> htfirst, htcount;
+                std::vector<int2> he, ht;
+                hb.assign(nbatch, HugeBatch{});
+                for (const uint32_t c : big_h) {   // ascending ids: batches in order
+                    const int64_t deg = soff_h[c + 1] - soff_h[c];
+                    if (deg <= split_min) continue;
+                    const int j = (int)hc.size();
+                    const int64_t bt = (int64_t)c / batch;
+                    int64_t H = 64;
+                    while (H < 2 * deg) H <<= 1;
+                    hc.push_back(c);
+                    htoff.push_back(hpool);
+                    htcap.push_back((uint32_t)H);
+                    hpool += H;
+                    HugeBatch& b = hb[bt];
+                    if (b.ne == 0 && b.nt == 0) { b.e0 = (int64_t)he.size(); b.t0 = (int64_t)ht.size(); }
+                    for (int64_t q = 0; q < ceil_div(deg, kHugeSeg); ++q) he.push_back(make_int2(j, (int)q));
+                    htfirst.push_back((int32_t)ht.size());
+                    const int64_t ntseg = ceil_div(H, kHugeSeg);
+                    htcount.push_back((int32_t)ntseg);
+                    for (int64_t q = 0; q < ntseg; ++q) ht.push_back(make_int2(j, (int)q));
+                    b.ne = (int64_t)he.size() - b.e0;
+                    b.nt = (int64_t)ht.size() - b.t0;
+                }
+                const int64_t nh = (int64_t)hc.size();
+                if (nh > 0) {
+                    auto up = [&](auto& buf, const auto& vec) {
+                        buf.alloc(vec.size(), s);
+                        GB_CUDA(cudaMemcpyAsync(buf.get(), vec.data(), vec.size() * sizeof(vec[0]),
+                                                cudaMemcpyHostToDevice, s));
+                    };
+                    up(huge_c, hc);
+                    up(huge_toff, htoff);
+                    up(huge_tcap, htcap);
+                    up(huge_tfirst, htfirst);
+                    up(huge_tcount, htcount);
+                    up(huge_eseg, he);
+                    up(huge_tseg, ht);
+                    huge_done.alloc(nh, s);
+                    GB_CUDA(cudaMemsetAsync(huge_done, 0, nh * sizeof(int32_t), s));
+                    hkeys.alloc(hpool, s);
+                    hvals.alloc(hpool, s);
+                    part_d.alloc(ht.size(), s);
+                    part_c.alloc(ht.size(), s);
+                    sa.huge_min = split_min;
+                    sa.huge_c = huge_c.get();
+                    sa.huge_toff = huge_toff.get();
+                    sa.huge_tcap = huge_tcap.get();
+                    sa.huge_tfirst = huge_tfirst.get();
+                    sa.huge_tcount = huge_tcount.get();
+                    sa.huge_done = huge_done.get();
+                    sa.huge_eseg = huge_eseg.get();
+                    sa.huge_tseg = huge_tseg.get();
+                    sa.hkeys = hkeys.get();
+                    sa.hvals = hvals.get();
+                    sa.part_d = part_d.get();
+                    sa.part_c = part_c.get();
+                    launches += 1;
+                }
+            }
+            GB_REQUIRE(!split_huge || hpool > 0, GBGPU_E_CUDA, "super-move: no huge super-node to split");
             DevBuf<int> iters_d(1, s), gmoves(super_max_iter, s);
             DevBuf<long long> moves_d(1, s);
             launches += 2;
@@ -1236,10 +1433,21 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
                 DevBuf<int> mv(1, s);
                 for (int it = 0; it < super_max_iter; ++it) {
                     GB_CUDA(cudaMemsetAsync(mv, 0, sizeof(int), s));
+                    if (hpool > 0) {
+                        GB_CUDA(cudaMemsetAsync(hkeys, 0xFF, hpool * sizeof(uint32_t), s));
+                        GB_CUDA(cudaMemsetAsync(hvals, 0, hpool * sizeof(uint32_t), s));
+                    }
                     for (int64_t bt = 0; bt < nbatch; ++bt) {
                         const int64_t cnt = bs[bt + 1] - bs[bt];
                         if (cnt == 0) continue;
                         const int64_t nb = bgs[bt + 1] - bgs[bt];
+                        if (hpool > 0 && hb[bt].ne > 0) {
+                            k_super_huge_accum<<<(int)hb[bt].ne, 1024, 0, s>>>(sa, hb[bt].e0);
+                            GB_LAUNCH_CHECK();
+                            k_super_huge_select<<<(int)hb[bt].nt, 1024, 0, s>>>(sa, hb[bt].t0);
+                            GB_LAUNCH_CHECK();
+                            launches += 2;
+                        }
                         if (cnt > nb) {
                             const int grid = (int)std::min<int64_t>(ceil_div(cnt - nb, 8), nwarps_total / 8);
                             k_super_propose_batch<<<grid, 256, 0, s>>>(sa, bt);
