@@ -394,7 +394,8 @@ struct SmArgs {
     uint32_t* gkeys;              // per-warp global tables for big super-nodes
     uint32_t* gvals;
     int64_t gcap;
-    // Super-nodes above kBigSuper neighbours: one CTA each (cluster kernel).
+    // Super-nodes above kBigSuper (cluster kernel) or kBigSuperBatched
+    // (batched launches) neighbours: one CTA each.
     const uint32_t* big_active;   // ascending
     const int64_t* bigstart;      // per batch
     uint32_t* bkeys;              // per-CTA global tables
@@ -1260,8 +1261,9 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
                 ++launches;
             }
             const bool single = nuniq <= p.super_single_cta_max_edges;
-            // The cluster kernel gives super-nodes above kBigSuper neighbours a
-            // CTA each; warps then need tables for at most kBigSuper.
+            // Super-nodes above big_min neighbours get a CTA each (the cluster
+            // kernel: kBigSuper; batched launches: kBigSuperBatched); warps then
+            // need tables for at most big_min.
             const int64_t big_min = single ? kBigSuper : kBigSuperBatched;   // degree above: a CTA each
             const int64_t warp_max = std::min<int64_t>(max_sdeg, big_min);
             int64_t gcap = 64;
@@ -1309,7 +1311,7 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
             const int64_t big_tables = nbig ? (single ? (int64_t)cluster : (int64_t)big_grid) * bcap : 1;
             DevBuf<uint32_t> bk(big_tables, s);
             DevBuf<uint32_t> bv(big_tables, s);
-            // Per-warp global tables for super-nodes of kSmSmall / 2 .. kBigSuper neighbours.
+            // Per-warp global tables for super-nodes of kSmSmall / 2 .. big_min neighbours.
             const int64_t nwarps_total = single ? (int64_t)cluster * 32 : (int64_t)kNumSMs * 4 * 8;
             DevBuf<uint32_t> gk(gcap > kSmSmall ? nwarps_total * gcap : 1, s);
             DevBuf<uint32_t> gv(gcap > kSmSmall ? nwarps_total * gcap : 1, s);

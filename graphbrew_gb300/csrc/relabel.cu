@@ -10,8 +10,9 @@
 // new row x = sorted { new_ids[v] : v in N(old(x)) }.  Remap and sort are
 // fused per row; rows are bucketed by length: one thread (<= 16 entries),
 // one warp with a shared-memory bitonic sort (<= 256), one 256-thread CTA
-// (<= 2048) or one 1024-thread CTA (<= 16384) with a shared-memory bitonic
-// sort, and a global segmented radix sort for the few longer rows.
+// (<= 2048) or one 1024-thread CTA (<= 16384) with a shared-memory LSD radix
+// sort, and a global radix sort of (row, new id) keys for the few longer
+// rows.  The three middle classes run concurrently on forked streams.
 #include "gb_common.cuh"
 #include "gb_stages.h"
 
