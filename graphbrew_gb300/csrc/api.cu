@@ -158,6 +158,7 @@ gb::LeidenParams leiden_params(const gb::Config& c) {
     if (const char* v = std::getenv("GBGPU_EXACT_WINDOW")) p.exact_window = std::max(32LL, std::atoll(v));
     if (tl_exact_window > 0) p.exact_window = std::max<int64_t>(32, tl_exact_window);
     if (const char* v = std::getenv("GBGPU_ASYNC_CHUNK")) p.chunk_vertices = std::max(32, std::atoi(v));
+    if (const char* v = std::getenv("GBGPU_ASYNC_STREAMS")) p.async_streams = std::max(0LL, std::atoll(v));
     if (const char* v = std::getenv("GBGPU_SUPER_CLUSTER_MAX_EDGES")) p.super_single_cta_max_edges = std::atoll(v);
     if (const char* v = std::getenv("GBGPU_SUPER_SPLIT_MIN")) p.super_split_min = std::atoll(v);
     return p;

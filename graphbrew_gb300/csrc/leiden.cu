@@ -51,9 +51,21 @@ struct LmArgs {
     unsigned long long* moves;
 };
 
-// Warp per vertex, degree <= kWarpMaxDeg.
+// Vertex state read by the asynchronous engine: through L2 in stream mode,
+// where a warp reads right after its own (atomic) updates.
+template <bool kStream, typename T>
+__device__ __forceinline__ T lm_load(const T* p) {
+    if constexpr (kStream) return __ldcg(p);
+    else return *p;
+}
+
+// Warp per vertex, degree <= kWarpMaxDeg.  Chunk mode: the warps of a launch
+// take the vertices of [begin, end) round-robin.  Stream mode: warp w sweeps
+// its own contiguous block of stream_len vertices in order, as one thread of
+// the reference's parallel mode sweeps its block (racy across warps).
+template <bool kStream>
 __global__ void __launch_bounds__(kLmWarpsPerBlock * 32)
-k_local_move_warp(LmArgs a, int64_t begin, int64_t end) {
+k_local_move_warp(LmArgs a, int64_t begin, int64_t end, int64_t stream_len) {
     extern __shared__ uint32_t lm_smem[];  // kLmWarpsPerBlock x (keys, vals) x kWarpHash
     __shared__ double sdelta[kLmWarpsPerBlock];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -62,12 +74,16 @@ k_local_move_warp(LmArgs a, int64_t begin, int64_t end) {
     double acc_delta = 0.0;
     unsigned long long acc_moves = 0;
     const int64_t warps_total = (int64_t)gridDim.x * kLmWarpsPerBlock;
-    for (int64_t u = begin + (int64_t)blockIdx.x * kLmWarpsPerBlock + w; u < end; u += warps_total) {
+    const int64_t gw = (int64_t)blockIdx.x * kLmWarpsPerBlock + w;
+    const int64_t u0 = kStream ? begin + gw * stream_len : begin + gw;
+    const int64_t u1 = kStream ? min(end, u0 + stream_len) : end;
+    const int64_t step = kStream ? 1 : warps_total;
+    for (int64_t u = u0; u < u1; u += step) {
         const int64_t rb = a.rp[u];
         const int deg = (int)(a.rp[u + 1] - rb);
         if (deg > kWarpMaxDeg) continue;  // hub kernel
-        if (!a.vaff[u]) continue;
-        const uint32_t d = a.vcom[u];
+        if (!lm_load<kStream>(&a.vaff[u])) continue;
+        const uint32_t d = lm_load<kStream>(&a.vcom[u]);
         const double ku = (double)deg;
         double best_d = 0.0;
         uint32_t best_c = kNone;
@@ -75,15 +91,15 @@ k_local_move_warp(LmArgs a, int64_t begin, int64_t end) {
             uint32_t c = kNone;
             if (lane < deg) {
                 const int32_t v = a.col[rb + lane];
-                if (v != (int32_t)u) c = a.vcom[v];
+                if (v != (int32_t)u) c = lm_load<kStream>(&a.vcom[v]);
             }
             const unsigned peers = __match_any_sync(0xFFFFFFFFu, c);
             const unsigned dmask = __ballot_sync(0xFFFFFFFFu, c == d);
             const double kud = (double)__popc(dmask);
             const bool leader = (c != kNone) && (lane == __ffs(peers) - 1) && c != d;
             if (leader) {
-                const double sd = (double)(long long)a.ctot[d];
-                const double sc = (double)(long long)a.ctot[c];
+                const double sd = (double)(long long)lm_load<kStream>(&a.ctot[d]);
+                const double sc = (double)(long long)lm_load<kStream>(&a.ctot[c]);
                 const double dl = delta_q((double)__popc(peers), kud, ku, sc, sd, a.M, a.R);
                 if (dl > 0.0) { best_d = dl; best_c = c; }
             }
@@ -97,18 +113,18 @@ k_local_move_warp(LmArgs a, int64_t begin, int64_t end) {
                 uint32_t c = kNone;
                 if (base + lane < deg) {
                     const int32_t v = a.col[rb + base + lane];
-                    if (v != (int32_t)u) c = a.vcom[v];
+                    if (v != (int32_t)u) c = lm_load<kStream>(&a.vcom[v]);
                 }
                 const unsigned peers = __match_any_sync(0xFFFFFFFFu, c);
                 if (c != kNone && lane == __ffs(peers) - 1) table_add(tk, tv, mask, c, (uint32_t)__popc(peers));
             }
             __syncwarp();
             const double kud = (double)table_get(tk, tv, mask, d);
-            const double sd = (double)(long long)a.ctot[d];
+            const double sd = (double)(long long)lm_load<kStream>(&a.ctot[d]);
             for (uint32_t i = lane; i < H; i += 32) {
                 const uint32_t c = tk[i];
                 if (c == kNone || c == d) continue;
-                const double sc = (double)(long long)a.ctot[c];
+                const double sc = (double)(long long)lm_load<kStream>(&a.ctot[c]);
                 const double dl = delta_q((double)tv[i], kud, ku, sc, sd, a.M, a.R);
                 if (dl > 0.0 && better(dl, c, best_d, best_c)) { best_d = dl; best_c = c; }
             }
@@ -1078,7 +1094,8 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
     const int hub_smem = 2 * kHubSmemSlots * (int)sizeof(uint32_t);
     GB_CUDA(cudaFuncSetAttribute(k_local_move_hub, cudaFuncAttributeMaxDynamicSharedMemorySize, hub_smem));
     const int lm_smem = kLmWarpsPerBlock * 2 * kWarpHash * (int)sizeof(uint32_t);
-    GB_CUDA(cudaFuncSetAttribute(k_local_move_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, lm_smem));
+    GB_CUDA(cudaFuncSetAttribute(k_local_move_warp<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lm_smem));
+    GB_CUDA(cudaFuncSetAttribute(k_local_move_warp<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lm_smem));
     const int sm_smem = 32 * 4 * kSmSmall * (int)sizeof(uint32_t);
     GB_CUDA(cudaFuncSetAttribute(k_super_move_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_smem));
 
@@ -1111,13 +1128,24 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
         for (int it = 0; it < p.max_iterations; ++it) {
             GB_CUDA(cudaMemsetAsync(dacc, 0, sizeof(double), s));
             GB_CUDA(cudaMemsetAsync(macc, 0, sizeof(unsigned long long), s));
-            for (int64_t b = 0; b < n; b += chunk) {
-                const int64_t e = std::min(n, b + chunk);
-                const int64_t warps = e - b;
-                const int grid = (int)std::min<int64_t>(ceil_div(warps, kLmWarpsPerBlock), (int64_t)kNumSMs * 16);
-                k_local_move_warp<<<grid, kLmWarpsPerBlock * 32, lm_smem, s>>>(la, b, e);
+            if (p.async_streams > 0) {
+                // Stream mode: every warp sweeps one contiguous block in order.
+                const int64_t warps = std::min<int64_t>(p.async_streams, std::max<int64_t>(1, n));
+                const int grid = (int)ceil_div(warps, kLmWarpsPerBlock);
+                // Warps past the last block (gw >= warps) start at or past n.
+                const int64_t len = ceil_div(n, warps);
+                k_local_move_warp<true><<<grid, kLmWarpsPerBlock * 32, lm_smem, s>>>(la, 0, n, len);
                 GB_LAUNCH_CHECK();
                 ++launches;
+            } else {
+                for (int64_t b = 0; b < n; b += chunk) {
+                    const int64_t e = std::min(n, b + chunk);
+                    const int64_t warps = e - b;
+                    const int grid = (int)std::min<int64_t>(ceil_div(warps, kLmWarpsPerBlock), (int64_t)kNumSMs * 16);
+                    k_local_move_warp<false><<<grid, kLmWarpsPerBlock * 32, lm_smem, s>>>(la, b, e, 0);
+                    GB_LAUNCH_CHECK();
+                    ++launches;
+                }
             }
             // Hubs in one launch per iteration, one CTA each: they see the
             // moves of every lower-degree vertex of this iteration.
