@@ -102,67 +102,117 @@ __global__ void k_core_init(const uint32_t* __restrict__ order_v, int64_t nn, co
     }
 }
 
-// The peel's control block: level k, the step's frontier size, the next
-// level when a frontier is empty, vertices left, and done.  Every kernel of a
-// step reads it, so steps are enqueued without the host in between.
+// The peel's control block.  A level k starts with a scan for the unpeeled
+// vertices whose remaining degree is <= k (the first frontier); peeling a
+// frontier appends every neighbour whose remaining degree falls from k + 1 to
+// k to the next frontier, so a level scans the vertices once and then touches
+// only its frontiers.  When a level's frontiers run out, level k + 1 starts
+// with a scan; a scan that finds nothing moves to the smallest remaining
+// degree, which the same scan found.  A scan reads only the vertices that
+// were unpeeled at the previous scan and writes out those it leaves.  A step
+// is two kernels (scan, apply); the apply's last CTA ends the step.
+//
+// A frontier is three lists by row length, so that no row holds one warp for
+// long: rows up to kCoreWarpMax entries get a warp, rows up to kCoreCtaMax a
+// CTA, longer rows every warp of the grid.
+constexpr int64_t kCoreWarpMax = 512;
+constexpr int64_t kCoreCtaMax = 8192;
+
 struct CoreCtl {
-    uint32_t k;
-    uint32_t count;
-    uint32_t next;
-    uint32_t pad;
-    long long left;
+    uint32_t k;        // level
+    uint32_t next;     // smallest remaining degree above k (an empty scan's next level)
+    uint32_t cnt[3];   // vertices in the current frontier, per tier
+    uint32_t ncnt[3];  // vertices appended to the next frontier, per tier
+    long long left;    // vertices not yet peeled
+    long long steps;   // steps run
+    long long max_steps;  // bound on steps (each one peels a vertex or raises the level)
+    int scan;          // this step starts level k with a scan
+    int par;           // the current frontier's buffers
     int done;
     int error;
+    unsigned arrive;   // apply CTAs finished in this step
+    unsigned rcount;   // vertices in the current remaining list
+    unsigned rnext;    // vertices the scan wrote to the next remaining list
+    int rpar;          // the current remaining list's buffer
 };
 
-// Frontier of level k: unpeeled vertices whose remaining degree is <= k,
-// appended with one atomic per CTA.
-__global__ void __launch_bounds__(kT)
-k_core_select(const uint32_t* __restrict__ order_v, int64_t nn, const uint32_t* __restrict__ cd,
-              const uint32_t* __restrict__ core, uint32_t* __restrict__ frontier, CoreCtl* __restrict__ ctl) {
-    __shared__ unsigned wsum[kT / 32];
-    __shared__ unsigned base;
-    if (ctl->done) return;
-    const uint32_t k = ctl->k;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int64_t p0 = (int64_t)blockIdx.x * kT; p0 < nn; p0 += (int64_t)gridDim.x * kT) {
-        const int64_t p = p0 + threadIdx.x;
-        uint32_t v = 0;
-        bool take = false;
-        if (p < nn) {
-            v = order_v[p];
-            take = core[v] == kCoreUnset && cd[v] <= k;
-        }
-        const unsigned b = __ballot_sync(0xFFFFFFFFu, take);
-        if (lane == 0) wsum[w] = (unsigned)__popc(b);
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            unsigned t = 0;
-            for (int q = 0; q < kT / 32; ++q) t += wsum[q];
-            base = t ? atomicAdd(&ctl->count, t) : 0u;
-        }
-        __syncthreads();
-        unsigned o = base;
-        for (int q = 0; q < w; ++q) o += wsum[q];
-        if (take) frontier[o + __popc(b & ((1u << lane) - 1u))] = v;
-        __syncthreads();
-    }
+// Frontier buffers: f[buffer][tier], each n entries.
+struct CoreFronts {
+    uint32_t* f[2][3];
+};
+
+__device__ __forceinline__ int core_tier(const int64_t* __restrict__ rp, uint32_t v) {
+    const int64_t d = rp[v + 1] - rp[v];
+    return d <= kCoreWarpMax ? 0 : (d <= kCoreCtaMax ? 1 : 2);
 }
 
-// Empty frontier: the smallest remaining degree of the unpeeled vertices is
-// the next level (one atomic per CTA).
+// Scan of level k: unpeeled vertices whose remaining degree is <= k form the
+// first frontier; the others go to the next remaining list (one atomic per
+// CTA for warp-tier rows and survivors, one per vertex for longer rows), and
+// their smallest remaining degree is the next level if no vertex is taken
+// (one atomicMin per CTA).
 __global__ void __launch_bounds__(kT)
-k_core_min(const uint32_t* __restrict__ order_v, int64_t nn, const uint32_t* __restrict__ cd,
-           const uint32_t* __restrict__ core, CoreCtl* __restrict__ ctl) {
+k_core_scan(uint32_t* rem0, uint32_t* rem1, const int64_t* __restrict__ rp, const uint32_t* __restrict__ cd,
+            const uint32_t* __restrict__ core, CoreFronts fr, CoreCtl* __restrict__ ctl) {
+    __shared__ unsigned wsum[kT / 32], wkeep[kT / 32];
     __shared__ unsigned wmin[kT / 32];
-    if (ctl->done || ctl->count != 0) return;
+    __shared__ unsigned base, kbase;
+    if (ctl->done || !ctl->scan) return;
+    const uint32_t k = ctl->k;
+    const int64_t nr = ctl->rcount;
+    const int par = ctl->par;
+    const uint32_t* rem = ctl->rpar ? rem1 : rem0;
+    uint32_t* rnext = ctl->rpar ? rem0 : rem1;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     unsigned m = 0xFFFFFFFFu;
-    for (int64_t p = blockIdx.x * (int64_t)kT + threadIdx.x; p < nn; p += (int64_t)gridDim.x * kT) {
-        const uint32_t v = order_v[p];
-        if (core[v] == kCoreUnset) m = min(m, cd[v]);
+    for (int64_t p0 = (int64_t)blockIdx.x * kT; p0 < nr; p0 += (int64_t)gridDim.x * kT) {
+        const int64_t p = p0 + threadIdx.x;
+        uint32_t v = 0;
+        bool take = false, keep = false;
+        if (p < nr) {
+            v = rem[p];
+            if (core[v] == kCoreUnset) {
+                const uint32_t d = cd[v];
+                take = d <= k;
+                keep = !take;
+                if (keep) m = min(m, d);
+            }
+        }
+        if (take) {
+            const int t = core_tier(rp, v);
+            if (t > 0) {
+                fr.f[par][t][atomicAdd(&ctl->cnt[t], 1u)] = v;   // long rows: few, one atomic each
+                take = false;
+            }
+        }
+        const unsigned b = __ballot_sync(0xFFFFFFFFu, take);
+        const unsigned kb = __ballot_sync(0xFFFFFFFFu, keep);
+        if (lane == 0) {
+            wsum[w] = (unsigned)__popc(b);
+            wkeep[w] = (unsigned)__popc(kb);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned t = 0, tk = 0;
+            for (int q = 0; q < kT / 32; ++q) {
+                t += wsum[q];
+                tk += wkeep[q];
+            }
+            base = t ? atomicAdd(&ctl->cnt[0], t) : 0u;
+            kbase = tk ? atomicAdd(&ctl->rnext, tk) : 0u;
+        }
+        __syncthreads();
+        unsigned o = base, ok = kbase;
+        for (int q = 0; q < w; ++q) {
+            o += wsum[q];
+            ok += wkeep[q];
+        }
+        if (take) fr.f[par][0][o + __popc(b & ((1u << lane) - 1u))] = v;
+        if (keep) rnext[ok + __popc(kb & ((1u << lane) - 1u))] = v;
+        __syncthreads();
     }
     m = __reduce_min_sync(0xFFFFFFFFu, m);
-    if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = m;
+    if (lane == 0) wmin[w] = m;
     __syncthreads();
     if (threadIdx.x == 0) {
         for (int q = 0; q < kT / 32; ++q) m = min(m, wmin[q]);
@@ -170,43 +220,135 @@ k_core_min(const uint32_t* __restrict__ order_v, int64_t nn, const uint32_t* __r
     }
 }
 
-// One warp per peeled vertex: its core number is k, and its unpeeled
-// neighbours in the community lose one (a neighbour in the same frontier
-// may lose one too; it is peeled at k all the same).
-__global__ void k_core_apply(const uint32_t* __restrict__ frontier, const int64_t* __restrict__ rp,
-                             const int32_t* __restrict__ col, const uint32_t* __restrict__ memb,
-                             uint32_t* __restrict__ core, uint32_t* __restrict__ cd, const CoreCtl* __restrict__ ctl) {
-    if (ctl->done) return;
-    const uint32_t cnt = ctl->count, k = ctl->k;
+// End of a step (the last apply CTA, after every other CTA's updates).
+__device__ void core_step_end(volatile CoreCtl* c) {
+    const unsigned peeled = c->cnt[0] + c->cnt[1] + c->cnt[2];
+    const unsigned appended = c->ncnt[0] + c->ncnt[1] + c->ncnt[2];
+    if (c->scan) {
+        c->rcount = c->rnext;   // the scan's survivors are the remaining list
+        c->rnext = 0;
+        c->rpar = c->rpar ^ 1;
+    }
+    bool clear = true;
+    if (c->scan && peeled == 0) {
+        // Nothing at level k: go to the smallest remaining degree.
+        if (c->next == 0xFFFFFFFFu || c->next <= c->k) {
+            c->error = 1;   // unpeeled vertices but no level to go to
+            c->done = 1;
+        } else {
+            c->k = c->next;
+        }
+    } else {
+        c->left = c->left - peeled;
+        if (c->left <= 0) {
+            c->done = 1;
+        } else if (appended > 0) {
+            c->par = c->par ^ 1;    // the appended vertices are the next frontier
+            for (int t = 0; t < 3; ++t) c->cnt[t] = c->ncnt[t];
+            c->scan = 0;
+            clear = false;
+        } else {
+            c->k = c->k + 1;        // level k is peeled: scan level k + 1
+            c->scan = 1;
+        }
+    }
+    for (int t = 0; t < 3; ++t) {
+        if (clear) c->cnt[t] = 0;
+        c->ncnt[t] = 0;
+    }
+    c->next = 0xFFFFFFFFu;
+    c->steps = c->steps + 1;
+    if (c->steps >= c->max_steps && !c->done) {
+        c->error = 1;   // the bound only guards against a broken invariant
+        c->done = 1;
+    }
+}
+
+// Removing peeled vertex v at level k: its unpeeled neighbours in the
+// community lose one (a neighbour in the same frontier may lose one too; it
+// is peeled at k all the same).  The one decrement that takes a neighbour
+// from k + 1 to k appends it to the next frontier.  Edges [e_begin, e_end)
+// of v's row, e_begin warp-uniform, in steps of `stride` per warp.
+__device__ __forceinline__ void core_remove(uint32_t v, int64_t e_begin, int64_t e_end, int64_t stride, uint32_t k,
+                                            const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
+                                            const uint32_t* __restrict__ memb, const uint32_t* core,
+                                            uint32_t* __restrict__ cd, const CoreFronts& fr, int npar,
+                                            CoreCtl* __restrict__ ctl) {
     const int lane = threadIdx.x & 31;
-    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; i < (int64_t)cnt; i += nw) {
-        const uint32_t v = frontier[i];
-        if (lane == 0) core[v] = k;
-        const uint32_t c = memb[v];
-        for (int64_t e = rp[v] + lane; e < rp[v + 1]; e += 32) {
-            const uint32_t u = (uint32_t)col[e];
-            if (u != v && memb[u] == c && core[u] == kCoreUnset) atomicSub(&cd[u], 1u);
+    const uint32_t c = memb[v];
+    for (int64_t e0 = e_begin; e0 < e_end; e0 += stride) {
+        const int64_t e = e0 + lane;
+        uint32_t u = 0;
+        bool push = false;
+        if (e < e_end) {
+            u = (uint32_t)col[e];
+            if (u != v && memb[u] == c && core[u] == kCoreUnset) push = atomicSub(&cd[u], 1u) == k + 1u;
+        }
+        if (push) {
+            const int t = core_tier(rp, u);
+            if (t > 0) {
+                fr.f[npar][t][atomicAdd(&ctl->ncnt[t], 1u)] = u;   // long rows: few, one atomic each
+                push = false;
+            }
+        }
+        const unsigned b = __ballot_sync(0xFFFFFFFFu, push);
+        if (b) {
+            unsigned base = 0;
+            if (lane == 0) base = atomicAdd(&ctl->ncnt[0], (unsigned)__popc(b));
+            base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            if (push) fr.f[npar][0][base + __popc(b & ((1u << lane) - 1u))] = u;
         }
     }
 }
 
-__global__ void k_core_ctl(CoreCtl* ctl) {
-    if (ctl->done) return;
-    if (ctl->count == 0) {
-        if (ctl->next == 0xFFFFFFFFu || ctl->next <= ctl->k) {
-            ctl->error = 1;   // unpeeled vertices but no level to go to
-            ctl->done = 1;
-        } else {
-            ctl->k = ctl->next;
+// Peels the frontier: a warp per warp-tier vertex, a CTA per CTA-tier
+// vertex, every warp of the grid on each longer row.  The last CTA to
+// finish ends the step and sets the peel loop's condition (the graph's while
+// node); no CTA waits for another.
+__global__ void __launch_bounds__(kT)
+k_core_apply(CoreFronts fr, const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
+             const uint32_t* __restrict__ memb, uint32_t* __restrict__ core, uint32_t* __restrict__ cd,
+             CoreCtl* __restrict__ ctl, cudaGraphConditionalHandle cond) {
+    __shared__ bool s_last;
+    const uint32_t c0 = ctl->cnt[0], c1 = ctl->cnt[1], c2 = ctl->cnt[2];
+    const bool active = !ctl->done && !(ctl->scan && c0 + c1 + c2 == 0);
+    if (active) {
+        const uint32_t k = ctl->k;
+        const int par = ctl->par, npar = par ^ 1;
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+        const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+        for (int64_t i = gw; i < (int64_t)c0; i += nw) {
+            const uint32_t v = fr.f[par][0][i];
+            if (lane == 0) core[v] = k;
+            core_remove(v, rp[v], rp[v + 1], 32, k, rp, col, memb, core, cd, fr, npar, ctl);
         }
-    } else {
-        ctl->left -= ctl->count;
-        if (ctl->left <= 0) ctl->done = 1;
+        for (int64_t i = blockIdx.x; i < (int64_t)c1; i += gridDim.x) {
+            const uint32_t v = fr.f[par][1][i];
+            if (threadIdx.x == 0) core[v] = k;
+            core_remove(v, rp[v] + w * 32, rp[v + 1], kT, k, rp, col, memb, core, cd, fr, npar, ctl);
+        }
+        for (uint32_t j = 0; j < c2; ++j) {
+            const uint32_t v = fr.f[par][2][j];
+            if (gw == 0 && lane == 0) core[v] = k;
+            core_remove(v, rp[v] + gw * 32, rp[v + 1], nw * 32, k, rp, col, memb, core, cd, fr, npar, ctl);
+        }
     }
-    ctl->count = 0;
-    ctl->next = 0xFFFFFFFFu;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        s_last = atomicAdd(&ctl->arrive, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (s_last && threadIdx.x == 0) {
+        __threadfence();
+        volatile CoreCtl* c = ctl;
+        if (!c->done) core_step_end(c);
+        c->arrive = 0;
+        cudaGraphSetConditional(cond, c->done ? 0u : 1u);
+    }
 }
+
 
 // ---- keys and segments ----
 __global__ void k_sorted_keys(const uint32_t* __restrict__ order_v, int64_t nn, const int64_t* __restrict__ rp,
@@ -480,31 +622,63 @@ int64_t sorted_communities(const DeviceCSR& g, const uint32_t* memb, int intra, 
     }
     if (intra == kCore) {
         // aux holds the internal degree; peel it into core numbers, in place.
-        // Steps are enqueued in batches; the host reads the control block once
-        // per batch.  Every step peels at least one vertex or raises the
-        // level, so at most 2 nn steps run.
-        DevBuf<uint32_t> cd(n, s), core(n, s), frontier(nn, s);
+        // The whole peel is one graph launch: a while node over steps
+        // (scan, apply) whose condition the apply's last CTA sets.
+        // Every step peels at least one vertex or raises the level, so at
+        // most 2 nn steps run.
+        DevBuf<uint32_t> cd(n, s), core(n, s), rem0(nn, s), rem1(nn, s);
+        DevBuf<uint32_t> fbuf[2][3];
+        CoreFronts fr{};
+        for (int b = 0; b < 2; ++b)
+            for (int t = 0; t < 3; ++t) {
+                fbuf[b][t].alloc(nn, s);
+                fr.f[b][t] = fbuf[b][t].get();
+            }
         DevBuf<CoreCtl> ctl(1, s);
-        const CoreCtl init{0u, 0u, 0xFFFFFFFFu, 0u, (long long)nn, 0, 0};
+        CoreCtl init{};
+        init.next = 0xFFFFFFFFu;
+        init.left = (long long)nn;
+        init.max_steps = 2 * (long long)nn + 2;
+        init.scan = 1;
+        init.rcount = (unsigned)nn;
         GB_CUDA(cudaMemcpyAsync(ctl, &init, sizeof(init), cudaMemcpyHostToDevice, s));
+        GB_CUDA(cudaMemcpyAsync(rem0, order_v, nn * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
         k_core_init<<<grid_for(nn, kT), kT, 0, s>>>(order_v, nn, aux, cd, core);
         GB_LAUNCH_CHECK();
-        constexpr int kStepsPerCheck = 16;
-        const int g_all = grid_for(nn, kT);
+        // Grid-stride scans with one resident wave: most steps skip them.
+        const int g_all = std::min(grid_for(nn, kT), kNumSMs * 8);
         const int g_apply = kNumSMs * 8;
-        CoreCtl h{};
-        for (int64_t steps = 0; steps <= 2 * nn + kStepsPerCheck; steps += kStepsPerCheck) {
-            for (int q = 0; q < kStepsPerCheck; ++q) {
-                k_core_select<<<g_all, kT, 0, s>>>(order_v, nn, cd, core, frontier, ctl);
-                k_core_min<<<g_all, kT, 0, s>>>(order_v, nn, cd, core, ctl);
-                k_core_apply<<<g_apply, kT, 0, s>>>(frontier, g.row_ptr, g.col, memb, core, cd, ctl);
-                k_core_ctl<<<1, 1, 0, s>>>(ctl);
+        struct PeelGraph {
+            cudaGraph_t g = nullptr;
+            cudaGraphExec_t e = nullptr;
+            cudaStream_t cs = nullptr;
+            ~PeelGraph() {
+                if (e) cudaGraphExecDestroy(e);
+                if (g) cudaGraphDestroy(g);
+                if (cs) cudaStreamDestroy(cs);
             }
-            GB_LAUNCH_CHECK();
-            nl += 4 * kStepsPerCheck;
-            h = read_dev(ctl.get(), s);
-            if (h.done) break;
-        }
+        } pg;
+        GB_CUDA(cudaStreamCreateWithFlags(&pg.cs, cudaStreamNonBlocking));
+        GB_CUDA(cudaGraphCreate(&pg.g, 0));
+        cudaGraphConditionalHandle cond;
+        GB_CUDA(cudaGraphConditionalHandleCreate(&cond, pg.g, 1, cudaGraphCondAssignDefault));
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = cond;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t loop_node;
+        GB_CUDA(cudaGraphAddNode(&loop_node, pg.g, nullptr, nullptr, 0, &cp));
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        GB_CUDA(cudaStreamBeginCaptureToGraph(pg.cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        k_core_scan<<<g_all, kT, 0, pg.cs>>>(rem0, rem1, g.row_ptr, cd, core, fr, ctl);
+        k_core_apply<<<g_apply, kT, 0, pg.cs>>>(fr, g.row_ptr, g.col, memb, core, cd, ctl, cond);
+        GB_LAUNCH_CHECK();
+        GB_CUDA(cudaStreamEndCapture(pg.cs, &body));
+        GB_CUDA(cudaGraphInstantiate(&pg.e, pg.g, 0));
+        GB_CUDA(cudaGraphLaunch(pg.e, s));
+        const CoreCtl h = read_dev(ctl.get(), s);
+        nl += 2 * h.steps;
         GB_REQUIRE(h.done && !h.error, GBGPU_E_CUDA, "core peel made no progress");
         GB_CUDA(cudaMemcpyAsync(aux, core, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
     }

@@ -202,7 +202,7 @@ def test_serial_mapping_bit_exact(ctx, name, manifest, golden_arrays):
 
 
 @pytest.mark.parametrize("scale,window", [(14, 8192), (16, 32768), (16, 1024), (18, 4096), (20, 8192),
-                                          (20, 32768)])
+                                          (20, 32768), (18, 65536)])
 def test_serial_engine_against_oracle(ctx, scale, window, monkeypatch):
     """Serial-order engine at larger sizes and window settings: bit-exact."""
     monkeypatch.setenv("GBGPU_EXACT_WINDOW", str(window))

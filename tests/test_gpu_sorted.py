@@ -105,3 +105,46 @@ def test_sorted_heap_fallback_against_oracle(ctx, order):
     if order == "hubsort":
         base = ids[:700].min()
         np.testing.assert_array_equal(np.argsort(ids[:700] - base), want)
+
+
+def _hub_core_graph(seed):
+    """Two communities over 30,000 vertices; about ten hubs of 4,500-12,000
+    neighbours in each (rows of the peel's CTA tier, 513-8,192 entries, and of
+    its whole-grid tier above), a dense core of 60 vertices, and random
+    background edges, so that long rows enter the peel's frontiers both from
+    the level scans and from decrements."""
+    rng = np.random.default_rng(seed)
+    n = 30000
+    memb = (rng.random(n) < 0.5).astype(np.uint32)
+    src, dst = [], []
+    hubs = rng.choice(n, 20, replace=False)
+    for h in hubs:
+        d = int(rng.integers(4500, 12000))
+        nb = rng.choice(n, d, replace=False)
+        src.append(np.full(d, h))
+        dst.append(nb)
+    core = rng.choice(n, 60, replace=False)
+    cs, cd = np.meshgrid(core, core)
+    src.append(cs.ravel())
+    dst.append(cd.ravel())
+    e = rng.integers(0, n, size=(150000, 2))
+    src.append(e[:, 0])
+    dst.append(e[:, 1])
+    s_ = np.concatenate(src + dst)
+    d_ = np.concatenate(dst + src)
+    keep = s_ != d_
+    key = np.unique(s_[keep].astype(np.int64) * n + d_[keep])
+    rows, cols = key // n, (key % n).astype(np.int32)
+    rp = np.zeros(n + 1, dtype=np.int64)
+    np.add.at(rp, rows + 1, 1)
+    return np.cumsum(rp), cols, memb
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_core_order_heavy_rows_against_oracle(ctx, seed):
+    rp, col, memb = _hub_core_graph(seed)
+    deg = np.diff(rp)
+    assert ((deg > 512) & (deg <= 8192)).sum() >= 5 and (deg > 8192).sum() >= 5
+    ids, _ = ctx.order_compose(rp, col, memb, recipe("core"))
+    ids_orc, _ = po.compose(rp, col, memb, "size-desc", "core")
+    np.testing.assert_array_equal(ids, ids_orc)
