@@ -79,7 +79,8 @@ class GbgpuStats(C.Structure):
                 ("gorder_max_community", C.c_int64), ("fallback_communities", C.c_int64),
                 ("fallback_vertices", C.c_int64), ("largest_community", C.c_int64),
                 ("bfs_levels", C.c_int64), ("kernel_launches", C.c_int64), ("resolution", C.c_double),
-                ("local_move_rounds", C.c_int64), ("local_move_evaluations", C.c_int64)]
+                ("local_move_rounds", C.c_int64), ("local_move_evaluations", C.c_int64),
+                ("local_move_streams", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -159,6 +159,7 @@ gb::LeidenParams leiden_params(const gb::Config& c) {
     if (tl_exact_window > 0) p.exact_window = std::max<int64_t>(32, tl_exact_window);
     if (const char* v = std::getenv("GBGPU_ASYNC_CHUNK")) p.chunk_vertices = std::max(32, std::atoi(v));
     if (const char* v = std::getenv("GBGPU_ASYNC_STREAMS")) p.async_streams = std::max(0LL, std::atoll(v));
+    if (const char* v = std::getenv("GBGPU_ASYNC_AUTO")) p.auto_streams = v[0] != '0';
     if (const char* v = std::getenv("GBGPU_SUPER_CLUSTER_MAX_EDGES")) p.super_single_cta_max_edges = std::atoll(v);
     if (const char* v = std::getenv("GBGPU_SUPER_SPLIT_MIN")) p.super_split_min = std::atoll(v);
     return p;

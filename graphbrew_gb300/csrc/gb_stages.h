@@ -50,6 +50,8 @@ struct LeidenParams {
     int refine_depth = -1;          // refinement in passes 0..refine_depth (-1: every pass)
     int chunk_vertices = 2048;      // asynchronous engine: vertices per launch
     int64_t async_streams = 0;      // asynchronous engine: > 0 = this many in-order streams (one warp each)
+    bool auto_streams = true;       // cd_parallel: stream mode on large graphs whose neighbours sit at nearby ids
+    int64_t auto_streams_min_vertices = 1 << 20;
     int64_t super_single_cta_max_edges = 1 << 24;  // super-move in one thread-block cluster up to this size
     int64_t super_split_min = 4096;         // batched super-move: split super-nodes above this degree over CTAs
     int64_t exact_max_vertices = INT64_MAX; // cd_parallel uses the serial-order engine up to this size

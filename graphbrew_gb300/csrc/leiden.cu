@@ -158,6 +158,40 @@ k_local_move_warp(LmArgs a, int64_t begin, int64_t end, int64_t stream_len) {
     if (lane == 0 && acc_moves) atomicAdd(a.moves, acc_moves);
 }
 
+// Id locality of a graph, sampled: for every eighth vertex u, the first 32
+// entries of its row; counts entries v with |u - v| <= 64 (near) and all
+// sampled entries.  A warp takes 32 sampled vertices, one coalesced row
+// prefix at a time.
+__global__ void __launch_bounds__(256)
+k_near_sample(const int64_t* __restrict__ rp, const int32_t* __restrict__ col, int64_t n,
+              unsigned long long* __restrict__ near_total) {
+    const int lane = threadIdx.x & 31;
+    const int64_t samples = (n + 7) / 8;
+    const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    unsigned long long near = 0, total = 0;
+    for (int64_t s0 = gw * 32; s0 < samples; s0 += nw * 32) {
+        const int64_t s1 = min(samples, s0 + 32);
+        for (int64_t si = s0; si < s1; ++si) {
+            const int64_t u = si * 8;
+            const int64_t rb = rp[u];
+            const int64_t len = rp[u + 1] - rb;
+            const int64_t d = len < 32 ? len : 32;
+            if (lane < d) {
+                const int64_t v = col[rb + lane];
+                near += (v - u <= 64 && u - v <= 64);
+                ++total;
+            }
+        }
+    }
+    near = __reduce_add_sync(0xFFFFFFFFu, (unsigned)near);
+    total = __reduce_add_sync(0xFFFFFFFFu, (unsigned)total);
+    if (lane == 0 && total) {
+        atomicAdd(&near_total[0], near);
+        atomicAdd(&near_total[1], total);
+    }
+}
+
 // CTA per hub vertex (degree > kWarpMaxDeg).  Table in shared memory when it
 // fits, otherwise in this CTA's slice of a global workspace.
 __global__ void __launch_bounds__(kHubThreads)
@@ -1102,9 +1136,33 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
     LmArgs la{g.row_ptr, g.col, vcom, ctot, vaff, M, R, dacc, macc};
     const int64_t chunk = p.chunk_vertices > 0 ? p.chunk_vertices : n;
 
-    // Serial-order engine: cd_serial always; cd_parallel below the size where
-    // the asynchronous engine is both faster and statistically equivalent.
-    const bool exact = p.deterministic || n <= p.exact_max_vertices;
+    // Serial-order engine: cd_serial always; cd_parallel too, except on large
+    // graphs whose neighbours sit at nearby ids (meshes, grids, road networks
+    // in traversal order): there a decision changes every few thousand
+    // vertices, the serial order's rounds commit little, and the stream mode
+    // (each warp sweeping its own block in order, as one thread of the
+    // reference's parallel mode does) keeps the serial order's modularity at
+    // a fraction of its time.
+    // 4,864 streams (32 warps on each of the 152 SMs): on a 4096 x 4096 grid
+    // this keeps modularity 0.509 (serial order 0.536, the reference's
+    // parallel mode ~0.50); 152 streams keep 0.530 at four times the time.
+    constexpr int64_t kAutoStreams = 4864;
+    bool exact = p.deterministic || n <= p.exact_max_vertices;
+    int64_t streams = p.async_streams;
+    if (exact && !p.deterministic && p.auto_streams && streams == 0 && n >= p.auto_streams_min_vertices) {
+        DevBuf<unsigned long long> nt(2, s);
+        GB_CUDA(cudaMemsetAsync(nt, 0, 2 * sizeof(unsigned long long), s));
+        k_near_sample<<<kNumSMs * 8, 256, 0, s>>>(g.row_ptr, g.col, n, nt);
+        GB_LAUNCH_CHECK();
+        ++launches;
+        unsigned long long h[2] = {0, 0};
+        GB_CUDA(cudaMemcpyAsync(h, nt.get(), sizeof(h), cudaMemcpyDeviceToHost, s));
+        GB_CUDA(cudaStreamSynchronize(s));
+        if (h[1] > 0 && 4 * h[0] >= h[1]) {   // a quarter of the sampled entries near
+            exact = false;
+            streams = kAutoStreams;
+        }
+    }
     LocalMoveContext lmc;
     lmc.g = g;
     lmc.vcom = vcom;
@@ -1128,9 +1186,9 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
         for (int it = 0; it < p.max_iterations; ++it) {
             GB_CUDA(cudaMemsetAsync(dacc, 0, sizeof(double), s));
             GB_CUDA(cudaMemsetAsync(macc, 0, sizeof(unsigned long long), s));
-            if (p.async_streams > 0) {
+            if (streams > 0) {
                 // Stream mode: every warp sweeps one contiguous block in order.
-                const int64_t warps = std::min<int64_t>(p.async_streams, std::max<int64_t>(1, n));
+                const int64_t warps = std::min<int64_t>(streams, std::max<int64_t>(1, n));
                 const int grid = (int)ceil_div(warps, kLmWarpsPerBlock);
                 // Warps past the last block (gw >= warps) start at or past n.
                 const int64_t len = ceil_div(n, warps);
@@ -1553,6 +1611,7 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
         st->kernel_launches += launches;
         st->local_move_rounds = exact_rounds;
         st->local_move_evaluations = exact_evals;
+        st->local_move_streams = exact ? 0 : streams;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

@@ -113,6 +113,7 @@ typedef struct {
     double resolution;              /* resolution used */
     int64_t local_move_rounds;      /* speculative rounds of the serial-order engine */
     int64_t local_move_evaluations; /* vertex evaluations in those rounds */
+    int64_t local_move_streams;     /* > 0: cd_parallel ran the stream-mode engine with this many streams */
 } gbgpu_stats;
 
 /* Context lifetime.  device < 0 selects the current device. */

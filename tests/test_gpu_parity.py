@@ -327,6 +327,34 @@ def test_async_streams_quality_on_grid(ctx, monkeypatch, streams):
     assert ctx.validate_permutation(ids) == 0
 
 
+def test_auto_stream_mode_on_high_locality_graphs(ctx, monkeypatch):
+    """cd_parallel picks the stream mode on large graphs whose neighbours sit
+    at nearby ids (a 1024 x 1024 grid) and keeps the serial order's
+    modularity; GBGPU_ASYNC_AUTO=0 keeps the serial-order engine, bit for
+    bit; RMAT (no id locality) keeps it by itself."""
+    rp_t, col_t = gg.grid(1024, 1024, 0.05, seed=13, device="cuda")
+    rp, col = rp_t.cpu().numpy(), col_t.cpu().numpy()
+    ar = po.auto_resolution(rp, col)
+    m_ser, _ = po.leiden(rp, col, ar)
+    q_ser = po.modularity(rp, col, m_ser, 1.0)
+    memb, st = ctx.run_graphbrew(rp_t, col_t, PARALLEL, ar)
+    assert st["local_move_streams"] >= 1216
+    m = memb.cpu().numpy().view(np.uint32)
+    _check_membership(rp, col, m)
+    q = po.modularity(rp, col, m, 1.0)
+    assert q >= q_ser - 0.01, (q, q_ser)
+    ids, st = ctx.generate_mapping(rp_t, col_t, PARALLEL, ar)
+    assert ctx.validate_permutation(ids) == 0
+    monkeypatch.setenv("GBGPU_ASYNC_AUTO", "0")
+    memb, st = ctx.run_graphbrew(rp_t, col_t, PARALLEL, ar)
+    assert st["local_move_streams"] == 0
+    np.testing.assert_array_equal(memb.cpu().numpy().view(np.uint32), m_ser)
+    monkeypatch.delenv("GBGPU_ASYNC_AUTO")
+    rp_t, col_t = gg.rmat(20, 16, seed=14, device="cuda")
+    _, st = ctx.run_graphbrew(rp_t, col_t, PARALLEL)
+    assert st["local_move_streams"] == 0
+
+
 def _check_membership(rp, col, memb):
     n = len(rp) - 1
     assert memb.shape == (n,)
