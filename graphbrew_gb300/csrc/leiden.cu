@@ -1519,6 +1519,26 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
                 super_moves += read_dev(moves_d.get(), s);
             } else {
                 DevBuf<int> mv(1, s);
+                // A batch's three proposal paths read the state before the
+                // batch and write disjoint super-nodes' proposals: the
+                // CTA-per-super-node and split paths run on side streams
+                // beside the warp path, joined before the commit.
+                struct BatchFork {
+                    cudaStream_t sb = nullptr, sh = nullptr;
+                    cudaEvent_t fork = nullptr, jb = nullptr, jh = nullptr;
+                    ~BatchFork() {
+                        if (fork) cudaEventDestroy(fork);
+                        if (jb) cudaEventDestroy(jb);
+                        if (jh) cudaEventDestroy(jh);
+                        if (sb) cudaStreamDestroy(sb);
+                        if (sh) cudaStreamDestroy(sh);
+                    }
+                } bf;
+                GB_CUDA(cudaStreamCreateWithFlags(&bf.sb, cudaStreamNonBlocking));
+                GB_CUDA(cudaStreamCreateWithFlags(&bf.sh, cudaStreamNonBlocking));
+                GB_CUDA(cudaEventCreateWithFlags(&bf.fork, cudaEventDisableTiming));
+                GB_CUDA(cudaEventCreateWithFlags(&bf.jb, cudaEventDisableTiming));
+                GB_CUDA(cudaEventCreateWithFlags(&bf.jh, cudaEventDisableTiming));
                 for (int it = 0; it < super_max_iter; ++it) {
                     GB_CUDA(cudaMemsetAsync(mv, 0, sizeof(int), s));
                     if (hpool > 0) {
@@ -1529,12 +1549,23 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
                         const int64_t cnt = bs[bt + 1] - bs[bt];
                         if (cnt == 0) continue;
                         const int64_t nb = bgs[bt + 1] - bgs[bt];
-                        if (hpool > 0 && hb[bt].ne > 0) {
-                            k_super_huge_accum<<<(int)hb[bt].ne, 1024, 0, s>>>(sa, hb[bt].e0);
+                        const bool huge = hpool > 0 && hb[bt].ne > 0;
+                        if (huge || nb > 0) GB_CUDA(cudaEventRecord(bf.fork, s));
+                        if (huge) {
+                            GB_CUDA(cudaStreamWaitEvent(bf.sh, bf.fork, 0));
+                            k_super_huge_accum<<<(int)hb[bt].ne, 1024, 0, bf.sh>>>(sa, hb[bt].e0);
                             GB_LAUNCH_CHECK();
-                            k_super_huge_select<<<(int)hb[bt].nt, 1024, 0, s>>>(sa, hb[bt].t0);
+                            k_super_huge_select<<<(int)hb[bt].nt, 1024, 0, bf.sh>>>(sa, hb[bt].t0);
                             GB_LAUNCH_CHECK();
+                            GB_CUDA(cudaEventRecord(bf.jh, bf.sh));
                             launches += 2;
+                        }
+                        if (nb > 0) {
+                            GB_CUDA(cudaStreamWaitEvent(bf.sb, bf.fork, 0));
+                            k_super_propose_big_batch<<<(int)std::min<int64_t>(nb, big_grid), 1024, 0, bf.sb>>>(sa, bt);
+                            GB_LAUNCH_CHECK();
+                            GB_CUDA(cudaEventRecord(bf.jb, bf.sb));
+                            ++launches;
                         }
                         if (cnt > nb) {
                             const int grid = (int)std::min<int64_t>(ceil_div(cnt - nb, 8), nwarps_total / 8);
@@ -1542,11 +1573,8 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
                             GB_LAUNCH_CHECK();
                             ++launches;
                         }
-                        if (nb > 0) {
-                            k_super_propose_big_batch<<<(int)std::min<int64_t>(nb, big_grid), 1024, 0, s>>>(sa, bt);
-                            GB_LAUNCH_CHECK();
-                            ++launches;
-                        }
+                        if (huge) GB_CUDA(cudaStreamWaitEvent(s, bf.jh, 0));
+                        if (nb > 0) GB_CUDA(cudaStreamWaitEvent(s, bf.jb, 0));
                         k_super_commit_batch<<<(int)std::min<int64_t>(ceil_div(cnt, 256), 1024), 256, 0, s>>>(sa, bt, mv);
                         GB_LAUNCH_CHECK();
                         ++launches;
