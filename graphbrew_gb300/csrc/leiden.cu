@@ -828,7 +828,11 @@ __global__ void k_super_propose_batch(SmArgs a, int64_t bt) {
     }
 }
 
-__global__ void __launch_bounds__(1024) k_super_propose_big_batch(SmArgs a, int64_t bt) {
+// CTA per super-node of the batch's big list (a quarter of an SM each, so
+// four run per SM); the table is the CTA's global slice.
+constexpr int kBigBatchThreads = 256;
+
+__global__ void __launch_bounds__(kBigBatchThreads) k_super_propose_big_batch(SmArgs a, int64_t bt) {
     __shared__ SmProposal bprop;
     __shared__ double red_d[32];
     __shared__ uint32_t red_c[32];
@@ -1393,7 +1397,7 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
                 GB_CUDA(cudaStreamSynchronize(s));
                 for (int64_t bt = 0; bt < nbatch; ++bt) max_big_in_batch = std::max(max_big_in_batch, bgs[bt + 1] - bgs[bt]);
             }
-            const int big_grid = (int)std::min<int64_t>(std::max<int64_t>(1, max_big_in_batch), kNumSMs);
+            const int big_grid = (int)std::min<int64_t>(std::max<int64_t>(1, max_big_in_batch), 4 * kNumSMs);
             const int64_t big_tables = nbig ? (single ? (int64_t)cluster : (int64_t)big_grid) * bcap : 1;
             DevBuf<uint32_t> bk(big_tables, s);
             DevBuf<uint32_t> bv(big_tables, s);
@@ -1562,7 +1566,8 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
                         }
                         if (nb > 0) {
                             GB_CUDA(cudaStreamWaitEvent(bf.sb, bf.fork, 0));
-                            k_super_propose_big_batch<<<(int)std::min<int64_t>(nb, big_grid), 1024, 0, bf.sb>>>(sa, bt);
+                            const int bgrid = (int)std::min<int64_t>(nb, big_grid);
+                            k_super_propose_big_batch<<<bgrid, kBigBatchThreads, 0, bf.sb>>>(sa, bt);
                             GB_LAUNCH_CHECK();
                             GB_CUDA(cudaEventRecord(bf.jb, bf.sb));
                             ++launches;
