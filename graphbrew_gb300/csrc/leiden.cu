@@ -158,7 +158,7 @@ k_local_move_warp(LmArgs a, int64_t begin, int64_t end, int64_t stream_len) {
     if (lane == 0 && acc_moves) atomicAdd(a.moves, acc_moves);
 }
 
-// Id locality of a graph, sampled: for every eighth vertex u, the first 32
+// Id locality of a graph, sampled: for every 64th vertex u, the first 32
 // entries of its row; counts entries v with |u - v| <= 64 (near) and all
 // sampled entries.  A warp takes 32 sampled vertices, one coalesced row
 // prefix at a time.
@@ -166,14 +166,14 @@ __global__ void __launch_bounds__(256)
 k_near_sample(const int64_t* __restrict__ rp, const int32_t* __restrict__ col, int64_t n,
               unsigned long long* __restrict__ near_total) {
     const int lane = threadIdx.x & 31;
-    const int64_t samples = (n + 7) / 8;
+    const int64_t samples = (n + 63) / 64;
     const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     unsigned long long near = 0, total = 0;
     for (int64_t s0 = gw * 32; s0 < samples; s0 += nw * 32) {
         const int64_t s1 = min(samples, s0 + 32);
         for (int64_t si = s0; si < s1; ++si) {
-            const int64_t u = si * 8;
+            const int64_t u = si * 64;
             const int64_t rb = rp[u];
             const int64_t len = rp[u + 1] - rb;
             const int64_t d = len < 32 ? len : 32;
