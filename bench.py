@@ -1,7 +1,9 @@
 """Benchmark: algorithm-12 mapping construction (FastLeiden-Gorder8) on one GB300.
 
-Workload: RMAT scale 22, edge factor 16 (a/b/c = 0.57/0.19/0.19), seeded,
-symmetrized int32 CSR (4.19M vertices, ~128M directed entries) and the recipe
+Workload: GAPBS's own RMAT graph for ``converter -g 22 -s`` (scale 22, degree
+16, a/b/c = 0.57/0.19/0.19, seed kRandSeed; generator.h:101-164 and the
+builder's squish), rebuilt here by the library's GAPBS generator: 4,194,302
+vertices, 128,311,450 directed int32 entries.  Recipe
 ``-o 12:leiden:compose:sg_none:comm_size_desc:intra_gorder:gw8:cd_parallel:
 sgmb4096:gordf5000:norefine:2:2``.  One step = the builder's mapping
 lifecycle: GraphBrew core (Leiden + COMPOSE) + permutation validation + CSR
@@ -11,10 +13,14 @@ metric  Medges/s = directed CSR entries / end-to-end mapping seconds.
 value   device-resident graph, CUDA events on the library's stream.
 e2e     same metric through the public C ABI with host (pinned) buffers:
         the CSR copied in and the permutation plus relabelled CSR copied out
-        inside every step.
+        inside every step.  ``e2e_pageable`` is the same with pageable buffers
+        (what a GAPBS caller's pvector memory is).
+parity  outside the timed region: the timed permutation's "Mapping
+        Fingerprint" and the relabelled CSR's checksums against the
+        reference's values on the same graph (tests/golden/gapbs_pins.json).
 
 ``--impl reference`` times the CPU restatement of the reference's path (the
-oracle, OpenMP on every host core) on the same workload; the reference's own
+oracle, OpenMP on every host core) on the same graph; the reference's own
 sources are not present on the GPU host, so it cannot be compiled there.
 """
 from __future__ import annotations
@@ -36,7 +42,21 @@ RECIPE = ("leiden:compose:sg_none:comm_size_desc:intra_gorder:gw8:cd_parallel:"
 METRIC = "GPU reorder Medges/s vs host CPU; map+kernel time, learned vs frozen rule"
 SCALE = 22
 EDGE_FACTOR = 16
-SEED = 27491095
+CPU_BASELINE_RUNS = 5
+PINS_PATH = os.path.join(ROOT, "tests", "golden", "gapbs_pins.json")
+
+
+def load_pins(scale):
+    """The reference's answers on GAPBS -g <scale> (None if not pinned)."""
+    try:
+        with open(PINS_PATH) as f:
+            return json.load(f)["rmat"].get(str(scale))
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def workload_name(scale):
+    return f"gapbs_rmat{scale}_ef{EDGE_FACTOR}_fastleiden_gorder8"
 
 
 def parse_args():
@@ -160,28 +180,28 @@ def run_reference_arm(args):
         return 0
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as po
-    from graphbrew_gb300 import graphgen as gg
     po.build()
     threads = host_cores()
     os.environ.setdefault("OMP_NUM_THREADS", str(threads))
-    # Bound the run: full scale while the step count is small, else a scale-20 sample.
-    scale = args.scale if (args.steps + args.warmup) <= 12 else min(args.scale, 20)
-    rp_t, col_t = gg.rmat(scale, EDGE_FACTOR, seed=SEED)
-    rp, col = rp_t.numpy(), col_t.numpy()
+    # The same graph as the GPU arm, at the requested scale: every step is one
+    # full mapping + validation + relabel of it.
+    rp, col = po.gapbs_graph(args.scale, EDGE_FACTOR)
     nnz = len(col)
     for _ in range(args.warmup):
         cpu_mapping_seconds(rp, col, threads)
     times = [cpu_mapping_seconds(rp, col, threads)[0] for _ in range(args.steps)]
     total = sum(times)
     value = nnz * len(times) / total / 1e6
-    sample = f"RMAT scale {scale} ef {EDGE_FACTOR}, {nnz} directed entries, full mapping+validation+relabel per step"
+    sample = (f"GAPBS -g {args.scale} graph ({nnz} directed entries), one full mapping+validation+relabel per "
+              f"step, {len(times)} steps, median {statistics.median(times):.2f} s")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Medges/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total / len(times) * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded RMAT)",
-        "config": {"workload": f"rmat{scale}_ef{EDGE_FACTOR}_fastleiden_gorder8", "recipe": "12:" + RECIPE,
-                   "scale": scale, "edge_factor": EDGE_FACTOR, "directed_entries": nnz},
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic (GAPBS RMAT generator, kRandSeed)",
+        "config": {"workload": workload_name(args.scale), "recipe": "12:" + RECIPE,
+                   "scale": args.scale, "edge_factor": EDGE_FACTOR, "vertices": len(rp) - 1,
+                   "directed_entries": nnz},
         "cpu_baseline": {"value": value, "unit": "Medges/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "Medges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -233,7 +253,7 @@ def main():
     from graphbrew_gb300 import graphgen as gg
 
     # Every rank maps its own replica (the path does not shard; no collective).
-    rp, col = gg.rmat(args.scale, EDGE_FACTOR, seed=SEED, device="cuda")
+    rp, col = gg.gapbs(args.scale, EDGE_FACTOR, device="cuda")
     n, nnz = rp.numel() - 1, col.numel()
     ctx = gb.Context(local)
     stream = torch.cuda.current_stream()
@@ -271,17 +291,35 @@ def main():
     ms_step = ms_total / args.steps
     value = nnz * world * args.steps / (ms_total / 1e3) / 1e6
 
-    # Correctness of what was timed: a valid permutation.
+    # Correctness of what was timed (outside the timed region): a valid
+    # permutation, and -- where the reference's answer on this graph is
+    # pinned -- the same permutation and relabelled CSR as the reference's.
     assert ctx.validate_permutation(ids) == 0
+    pin = load_pins(args.scale)
+    fp = gb.mapping_fingerprint(ids)
+    parity = {"fingerprint": fp, "relabel_row_ptr": gg.checksum(orp), "relabel_col": gg.checksum(ocol)}
+    if pin is not None:
+        same = (fp == pin["fingerprint_cd_serial"] and parity["relabel_row_ptr"] == pin["relabel_row_ptr"]
+                and parity["relabel_col"] == pin["relabel_col"])
+        parity.update({"reference_fingerprint": pin["fingerprint_cd_serial"],
+                       "graph_matches_reference": gg.checksum(rp) == pin["row_ptr"] and gg.checksum(col) == pin["col"],
+                       "result": "bit-exact" if same else "mismatch",
+                       "against": "reference cd_serial mapping + RelabelByMapping on the same graph"})
+    else:
+        parity["result"] = "unpinned at this scale"
 
-    # End to end through the C ABI with pinned host buffers.
-    e2e = None
-    if not args.no_e2e:
-        h_rp = rp.cpu().pin_memory()
-        h_col = col.cpu().pin_memory()
-        h_ids = torch.empty(n, dtype=torch.int32).pin_memory()
-        h_orp = torch.empty(n + 1, dtype=torch.int64).pin_memory()
-        h_ocol = torch.empty(nnz, dtype=torch.int32).pin_memory()
+    def host_e2e(pinned):
+        """Median-free whole-step timing through the C ABI with host buffers."""
+        if pinned:
+            h_rp, h_col = rp.cpu().pin_memory(), col.cpu().pin_memory()
+            h_ids = torch.empty(n, dtype=torch.int32).pin_memory()
+            h_orp = torch.empty(n + 1, dtype=torch.int64).pin_memory()
+            h_ocol = torch.empty(nnz, dtype=torch.int32).pin_memory()
+        else:
+            h_rp, h_col = rp.cpu(), col.cpu()
+            h_ids = torch.empty(n, dtype=torch.int32)
+            h_orp = torch.empty(n + 1, dtype=torch.int64)
+            h_ocol = torch.empty(nnz, dtype=torch.int32)
         lib = gb.library()
         opts = RECIPE.encode()
 
@@ -298,16 +336,23 @@ def main():
         t0 = time.perf_counter()
         host_stats = [host_step() for _ in range(args.steps)]
         t1 = time.perf_counter()
+        assert gb.mapping_fingerprint(h_ids.numpy()) == fp
         e2e_s = (t1 - t0) / args.steps
-        e2e = {"value": nnz * world / e2e_s / 1e6, "unit": "Medges/s",
-               "h2d_bytes_per_step": 8 * (n + 1) + 4 * nnz,
-               "d2h_bytes_per_step": 4 * n + 8 * (n + 1) + 4 * nnz,
-               "ms_per_step": e2e_s * 1e3,
-               "h2d_ms": float(np.median([x.h2d_ms for x in host_stats])),
-               "d2h_ms": float(np.median([x.d2h_ms for x in host_stats])),
-               "call_device_ms": float(np.median([x.total_ms for x in host_stats])),
-               "call_stages_ms": {k: float(np.median([getattr(x, k) for x in host_stats]))
-                                  for k in ("local_move_ms", "aggregate_ms", "compose_ms", "relabel_ms")}}
+        return {"value": nnz * world / e2e_s / 1e6, "unit": "Medges/s",
+                "h2d_bytes_per_step": 8 * (n + 1) + 4 * nnz,
+                "d2h_bytes_per_step": 4 * n + 8 * (n + 1) + 4 * nnz,
+                "ms_per_step": e2e_s * 1e3, "host_buffers": "pinned" if pinned else "pageable",
+                "h2d_ms": float(np.median([x.h2d_ms for x in host_stats])),
+                "d2h_ms": float(np.median([x.d2h_ms for x in host_stats])),
+                "call_device_ms": float(np.median([x.total_ms for x in host_stats])),
+                "call_stages_ms": {k: float(np.median([getattr(x, k) for x in host_stats]))
+                                   for k in ("local_move_ms", "aggregate_ms", "compose_ms", "relabel_ms")}}
+
+    # End to end through the C ABI with host buffers (pinned, then pageable).
+    e2e = e2e_pageable = None
+    if not args.no_e2e:
+        e2e = host_e2e(True)
+        e2e_pageable = host_e2e(False)
 
     # Stage split and the roofline of the dominant stage.  The serial-order
     # local moving is a chain of short dependent rounds (latency-bound by
@@ -339,22 +384,27 @@ def main():
         import pyoracle as po
         po.build()
         threads = host_cores()
-        secs, cpu_ids = cpu_mapping_seconds(rp.cpu().numpy(), col.cpu().numpy(), threads)
-        cpu = {"value": nnz / secs / 1e6, "unit": "Medges/s", "cores": threads, "kind": "port",
-               "sample": f"one full mapping+validation+relabel of the same RMAT scale {args.scale} graph "
-                         f"({secs:.1f} s, OpenMP cd_parallel restatement)"}
+        h_rp, h_col = rp.cpu().numpy(), col.cpu().numpy()
+        secs = sorted(cpu_mapping_seconds(h_rp, h_col, threads)[0] for _ in range(CPU_BASELINE_RUNS))
+        med = statistics.median(secs)
+        cpu = {"value": nnz / med / 1e6, "unit": "Medges/s", "cores": threads, "kind": "port",
+               "sample": f"median of {CPU_BASELINE_RUNS} full mappings+validation+relabel of the same GAPBS "
+                         f"-g {args.scale} graph (OpenMP cd_parallel restatement; runs "
+                         + ", ".join(f"{x:.2f}" for x in secs) + " s)"}
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "Medges/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded RMAT, generated on device)",
-            "config": {"workload": f"rmat{args.scale}_ef{EDGE_FACTOR}_fastleiden_gorder8",
+            "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic (GAPBS RMAT generator, kRandSeed; edge list on the host, squished on the device)",
+            "config": {"workload": workload_name(args.scale),
                        "recipe": "12:" + RECIPE, "scale": args.scale, "edge_factor": EDGE_FACTOR,
                        "vertices": n, "directed_entries": nnz, "parallelism": f"replicas{world}",
                        "local_move_engine": args.engine,
                        "l2": "inputs larger than L2 (CSR 0.55 GB vs 129 MB L2)"},
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "e2e_pageable": e2e_pageable,
+            "parity": parity,
             "clocks": clocks,
             "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
             "stages_ms": stage_ms,

@@ -108,6 +108,8 @@ SIGNATURES = {
                                         C.POINTER(GbgpuStats), C.c_uint32]),
     "gbgpu_validate_permutation_noalloc": (C.c_int, [_P, _P, C.c_int64, C.POINTER(C.c_int32)]),
     "gbgpu_fingerprint": (C.c_uint64, [_P, C.c_int64]),
+    "gbgpu_gapbs_edge_count": (C.c_int64, [C.c_int32, C.c_int32]),
+    "gbgpu_gapbs_edge_list": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _P, _P, C.c_int32]),
     "gbgpu_version": (C.c_char_p, []),
     "gbgpu_generate_mappings_batched": (C.c_int, [_P, C.POINTER(GbgpuGraph), C.c_int32, C.c_char_p,
                                                   C.POINTER(GbgpuSchedule), _P, C.POINTER(C.c_double), C.c_uint32]),

@@ -13,6 +13,12 @@
 // Flags: -f <file.el|.sg>  -g <scale>  -u <scale>  -k <degree>  -s
 //        -o 12:<tokens> (repeatable)  -q <out.lo>  -x <out.so>  -b <out.sg>
 //        -e <out.el>  -d <cuda device>  -r <seed>
+//
+// -g / -u build GAPBS's own synthetic graph (generator.h:101-164 through
+// gbgpu_gapbs_edge_list, then the builder's squish), so `gbconvert -g 22`
+// maps the same graph as `converter -g 22` and prints the same "Mapping
+// Fingerprint".  With -r <seed> they build the project's seeded SplitMix64
+// family instead (graphgen.py), which GAPBS has no counterpart for.
 #include <cuda_runtime.h>
 #include <getopt.h>
 
@@ -150,6 +156,24 @@ HostGraph gen_rmat(int scale, int degree, uint64_t seed) {
     return squish(n, src, dst, true);
 }
 
+// GAPBS's graph: the generator's edge list, vertex count = largest id + 1
+// (builder.h:469-470), squished.
+HostGraph gen_gapbs(int scale, int degree, bool uniform) {
+    const int64_t m = gbgpu_gapbs_edge_count(scale, degree);
+    if (m < 0) throw std::invalid_argument("bad generator scale or degree");
+    std::vector<int32_t> s32((size_t)std::max<int64_t>(m, 1)), d32((size_t)std::max<int64_t>(m, 1));
+    if (gbgpu_gapbs_edge_list(scale, degree, uniform ? 1 : 0, s32.data(), d32.data(), 0) != GBGPU_OK)
+        throw std::runtime_error("gbgpu_gapbs_edge_list failed");
+    int64_t n = 0;
+    for (int64_t e = 0; e < m; ++e) n = std::max<int64_t>(n, std::max(s32[e], d32[e]) + 1);
+    std::vector<uint64_t> src((size_t)m), dst((size_t)m);
+    for (int64_t e = 0; e < m; ++e) {
+        src[e] = (uint64_t)s32[e];
+        dst[e] = (uint64_t)d32[e];
+    }
+    return squish(n, src, dst, true);
+}
+
 HostGraph gen_uniform(int scale, int degree, uint64_t seed) {
     const int64_t n = int64_t(1) << scale, m = n * degree;
     Draw draw(seed, 3);
@@ -230,6 +254,7 @@ int run(int argc, char** argv) {
     std::string file, lo, so, sgout, elout;
     int gscale = -1, uscale = -1, degree = 16, device = 0;
     uint64_t seed = 27491095;
+    bool seeded = false;
     bool symmetrize = false;
     std::vector<std::string> orders;
     int c;
@@ -246,10 +271,15 @@ int run(int argc, char** argv) {
             case 'b': sgout = optarg; break;
             case 'e': elout = optarg; break;
             case 'd': device = std::atoi(optarg); break;
-            case 'r': seed = std::strtoull(optarg, nullptr, 10); break;
+            case 'r':
+                seed = std::strtoull(optarg, nullptr, 10);
+                seeded = true;
+                break;
             default:
-                std::printf("gbconvert -f <file.el|.sg> | -g <scale> | -u <scale> [-k deg] [-s]\n"
-                            "          -o 12:<tokens> [-q out.lo] [-x out.so] [-b out.sg] [-e out.el] [-d dev]\n");
+                std::printf("gbconvert -f <file.el|.sg> | -g <scale> | -u <scale> [-k deg] [-r seed] [-s]\n"
+                            "          -o 12:<tokens> [-q out.lo] [-x out.so] [-b out.sg] [-e out.el] [-d dev]\n"
+                            "  -g/-u: GAPBS's generator (same graph as converter); with -r <seed>: the\n"
+                            "         project's seeded generator\n");
                 return c == 'h' ? 0 : 1;
         }
     }
@@ -259,8 +289,8 @@ int run(int argc, char** argv) {
     }
     double t0 = now();
     HostGraph g;
-    if (gscale >= 0) g = gen_rmat(gscale, degree, seed);
-    else if (uscale >= 0) g = gen_uniform(uscale, degree, seed);
+    if (gscale >= 0) g = seeded ? gen_rmat(gscale, degree, seed) : gen_gapbs(gscale, degree, false);
+    else if (uscale >= 0) g = seeded ? gen_uniform(uscale, degree, seed) : gen_gapbs(uscale, degree, true);
     else if (file.size() > 3 && file.substr(file.size() - 3) == ".sg") g = read_sg(file);
     else g = read_el(file, symmetrize);
     print_time("Build Time", now() - t0);

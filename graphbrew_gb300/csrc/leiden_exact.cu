@@ -200,6 +200,10 @@ __device__ __forceinline__ void sigma_at_k(const ExactState& a, unsigned long lo
                 lo[k] = l[k] = sm[k].start;
                 r[k] = (int)(sm[k].endh & ((1u << kEndBits) - 1u));
                 hot[k] = sm[k].endh >> kEndBits;
+                if (hot[k] > (uint32_t)kHotMax) {   // never written by a finished table
+                    a.ctl->error = 2;
+                    hot[k] = 0;
+                }
                 pending[k] = false;
             } else if ((sm[k].tkey >> 32) != tag) {   // a slot of an older table: empty
                 pending[k] = false;
@@ -727,6 +731,10 @@ __global__ void __launch_bounds__(kTbFinishThreads) k_tb_finish(ExactState a) {
             const int k = k0 + j;
             const uint32_t hid = eh[j] >> kEndBits;
             if (k >= b1 || !hid) continue;
+            if (hid > (uint32_t)kHotMax) {   // never written by a finished table
+                a.ctl->error = 2;
+                continue;
+            }
             const uint32_t sl = (uint32_t)(key[j] >> 32), e = (uint32_t)key[j];
             const int end = (int)(eh[j] & ((1u << kEndBits) - 1u));
             int32_t* bx = a.hot_bidx + (size_t)(hid - 1) * kHotStride;
@@ -1891,6 +1899,8 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
                 if (hctl->P >= n) break;
             }
         }
+        if (hctl->error == 2)
+            throw Error(GBGPU_E_CUDA, "serial-order local moving: event table slot with an invalid hot index");
         if (hctl->error)
             throw Error(GBGPU_E_CUDA, "serial-order local moving: round loop stopped without progress");
         nl += 4 + (nh ? 1 : 0) + hctl->round * per_round;

@@ -1,8 +1,8 @@
 // noalloc.cu -- permutation check that allocates no device memory.
 //
 // Some callers of this library cannot allocate: a serving process whose GPU
-// memory is reserved up front by another framework's allocator, code running
-// inside a CUDA stream capture (where cudaMalloc is not permitted), or a
+// memory is reserved up front by another framework's allocator (a cudaMalloc
+// there fails or steals memory the framework has promised elsewhere), or a
 // latency-critical loop that cannot afford the implicit device
 // synchronisation of cudaMalloc/cudaFree.  gbgpu_validate_permutation_noalloc
 // gives them the builder's permutation check (same results as
@@ -13,12 +13,13 @@
 // library holds it (4 MiB) until the process exits.  Host code must not use the
 // array's name as a device address; the address is obtained once per device
 // with cudaGetSymbolAddress while that device is current, and passed to the
-// kernels.  That lookup happens on the first call on each device, so the
-// first call should come before any stream capture.  Every call shares the
+// kernels.  That lookup happens on the first call on each device (a
+// one-time set-up step, not an allocation).  Every call shares the
 // array and the array keeps the last call's contents: each call re-initialises
 // the part it reads.  Calls whose GPU work overlaps (different streams or
 // contexts on one device) race on the array and must be serialised by the
-// caller.
+// caller.  The call reads its two-word result back and waits for its stream,
+// and it leaves the caller's current device as it found it.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -86,7 +87,11 @@ __global__ void k_na_dup(const int32_t* __restrict__ ids, int64_t n, int32_t* __
 
 extern "C" int gbgpu_validate_permutation_noalloc(gbgpu_ctx* ctx, const int32_t* new_ids_dev, int64_t n,
                                                   int32_t* result) {
-    if (!ctx || !result || n < 0 || (n > 0 && !new_ids_dev)) return GBGPU_E_INVALID;
+    if (!ctx) return GBGPU_E_INVALID;
+    if (!result || n < 0 || (n > 0 && !new_ids_dev)) {
+        gb_ctx_set_error(ctx, "gbgpu_validate_permutation_noalloc: null result, negative n, or null new_ids_dev");
+        return GBGPU_E_INVALID;
+    }
     if (n > kMax) {
         gb_ctx_set_error(ctx, ("gbgpu_validate_permutation_noalloc: n = " + std::to_string(n) +
                                " exceeds GBGPU_NOALLOC_MAX_VERTICES = " + std::to_string(kMax))
@@ -95,10 +100,33 @@ extern "C" int gbgpu_validate_permutation_noalloc(gbgpu_ctx* ctx, const int32_t*
     }
     if (n == 0) {
         *result = 0;
+        gb_ctx_set_error(ctx, "");
         return GBGPU_OK;
     }
     const int device = gb_ctx_device(ctx);
-    if (cudaSetDevice(device) != cudaSuccess) return GBGPU_E_CUDA;
+    if (device < 0 || device >= kMaxDevices) {
+        gb_ctx_set_error(ctx, ("gbgpu_validate_permutation_noalloc: device index " + std::to_string(device) +
+                               " is beyond the " + std::to_string(kMaxDevices) + " devices it supports")
+                                  .c_str());
+        return GBGPU_E_INVALID;
+    }
+    // The context's device becomes current for the launches; the caller's
+    // current device is put back before returning, on every path.
+    int caller_device = -1;
+    cudaError_t e = cudaGetDevice(&caller_device);
+    if (e == cudaSuccess && caller_device != device) e = cudaSetDevice(device);
+    if (e != cudaSuccess) {
+        gb_ctx_set_error(ctx, (std::string("gbgpu_validate_permutation_noalloc: cannot make device ") +
+                               std::to_string(device) + " current: " + cudaGetErrorString(e))
+                                  .c_str());
+        return GBGPU_E_CUDA;
+    }
+    struct RestoreDevice {
+        int caller, own;
+        ~RestoreDevice() {
+            if (caller >= 0 && caller != own) cudaSetDevice(caller);
+        }
+    } restore{caller_device, device};
     int32_t* scratch = nullptr;
     const int rc = scratch_for_current_device(device, &scratch);
     if (rc != GBGPU_OK) {
@@ -111,7 +139,7 @@ extern "C" int gbgpu_validate_permutation_noalloc(gbgpu_ctx* ctx, const int32_t*
     k_na_first<<<grid, 256, 0, s>>>(new_ids_dev, n, scratch);
     k_na_dup<<<grid, 256, 0, s>>>(new_ids_dev, n, scratch);
     int32_t mins[2] = {kIntMax, kIntMax};
-    cudaError_t e = cudaGetLastError();
+    e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(mins, scratch + kMax, sizeof(mins), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {

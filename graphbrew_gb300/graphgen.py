@@ -3,11 +3,17 @@
 These build the inputs of the mapping path (the GAPBS builder's job in the
 reference: ``bench/include/external/gapbs/generator.h:101-164`` generates the
 edge list and ``builder.h:254-312`` symmetrizes, sorts, de-duplicates and drops
-self-loops).  The reference seeds ``std::mt19937`` per 2^18-edge block and
-shuffles ids with ``std::shuffle``; here every random draw is a counter-based
-SplitMix64 hash of ``(seed, stream, index)`` so the same graph comes out of
-any device and any block partition.  The RMAT quadrant rule (A/B/C =
-0.57/0.19/0.19 compared on 32-bit draws) follows ``generator.h:124-146``.
+self-loops).
+
+``gapbs`` is the reference's own graph: the edge list of ``converter -g/-u``
+drawn by the library's host generator (``gbgpu_gapbs_edge_list``: per-block
+``std::mt19937`` seeded with kRandSeed + block, ``std::shuffle`` id
+permutation), then squished here with the builder's vertex count (largest id
++ 1).  The other generators are the project's seeded families: every random
+draw is a counter-based SplitMix64 hash of ``(seed, stream, index)`` so the
+same graph comes out of any device and any block partition.  Their RMAT
+quadrant rule (A/B/C = 0.57/0.19/0.19 compared on 32-bit draws) follows
+``generator.h:124-146``.
 
 All functions take a ``device`` so bench-sized graphs are built in HBM; the
 arithmetic is plain 64-bit integer work and gives identical graphs on CPU and
@@ -54,6 +60,17 @@ def draw64(seed: int, stream: int, index: torch.Tensor) -> torch.Tensor:
     return mix64(index ^ base)
 
 
+def checksum(t: torch.Tensor) -> str:
+    """Position-dependent 64-bit checksum of an integer array (on its own
+    device): the wrapping sum over i of mix64(i * golden + t[i]), as 16 hex
+    digits.  Equal arrays give equal sums; used to pin large CSR arrays against
+    committed values without storing them."""
+    x = t.reshape(-1).to(torch.int64)
+    idx = torch.arange(x.numel(), dtype=torch.int64, device=x.device)
+    total = int(mix64(idx * _G + x).sum().item())
+    return "%016x" % (total & _MASK64)
+
+
 def _permutation(n: int, seed: int, device) -> torch.Tensor:
     """A seeded permutation of 0..n-1 (rank of each id under a hash key)."""
     ids = torch.arange(n, dtype=torch.int64, device=device)
@@ -81,6 +98,30 @@ def squish(src: torch.Tensor, dst: torch.Tensor, n: int):
     row_ptr = torch.zeros(n + 1, dtype=torch.int64, device=u.device)
     row_ptr[1:] = torch.cumsum(counts, 0)
     return row_ptr, v.to(torch.int32)
+
+
+def gapbs(scale: int, degree: int = 16, uniform: bool = False, device="cpu", threads: int = 0):
+    """The graph GAPBS builds for ``-g <scale> -k <degree> -s`` (RMAT) or
+    ``-u <scale> -k <degree> -s`` (uniform): same edge list, vertex count =
+    largest id + 1 (builder.h:469-470), symmetrized and squished."""
+    import numpy as np
+
+    from graphbrew_gb300 import library
+    lib = library()
+    m = lib.gbgpu_gapbs_edge_count(scale, degree)
+    if m < 0:
+        raise ValueError(f"GAPBS generator: bad scale {scale} or degree {degree}")
+    src = np.empty(max(m, 1), dtype=np.int32)
+    dst = np.empty(max(m, 1), dtype=np.int32)
+    rc = lib.gbgpu_gapbs_edge_list(scale, degree, int(bool(uniform)), src.ctypes.data, dst.ctypes.data, threads)
+    if rc != 0:
+        raise RuntimeError(f"gbgpu_gapbs_edge_list failed with status {rc}")
+    src, dst = src[:m], dst[:m]
+    n = int(max(int(src.max()), int(dst.max())) + 1) if m > 0 else 0
+    s = torch.from_numpy(src).to(device=device, dtype=torch.int64)
+    d = torch.from_numpy(dst).to(device=device, dtype=torch.int64)
+    del src, dst
+    return squish(s, d, n)
 
 
 def rmat(scale: int, edge_factor: int = 16, seed: int = 27491095, device="cpu",

@@ -215,21 +215,36 @@ int gbgpu_generate_mappings_batched(gbgpu_ctx* ctx, const gbgpu_graph* graphs, i
 
 /* Permutation check that allocates no device memory.  No counterpart in the
  * reference: it serves callers that cannot allocate device memory -- a process
- * whose GPU memory is reserved by another framework's allocator, work issued
- * inside a CUDA stream capture, or a latency-critical loop that cannot take
- * cudaMalloc's implicit synchronisation.  Same *result codes as
- * gbgpu_validate_permutation; new_ids_dev must be device memory; n at most
- * GBGPU_NOALLOC_MAX_VERTICES (larger n returns GBGPU_E_OVERFLOW).  Scratch is a
- * fixed 4 MiB array in the library's device image, held by every GPU that loads
- * the library until exit and shared by all calls: calls whose GPU work
- * overlaps race and must be serialised by the caller.  The first call on each
- * device looks up that array's address, so make it before any stream capture. */
+ * whose GPU memory is reserved by another framework's allocator, or a
+ * latency-critical loop that cannot take cudaMalloc's implicit
+ * synchronisation.  Same *result codes as gbgpu_validate_permutation;
+ * new_ids_dev must be device memory; n at most GBGPU_NOALLOC_MAX_VERTICES
+ * (larger n returns GBGPU_E_OVERFLOW).  Scratch is a fixed 4 MiB array in the
+ * library's device image, held by every GPU that loads the library until exit
+ * and shared by all calls: calls whose GPU work overlaps race and must be
+ * serialised by the caller.  The first call on each device looks up that
+ * array's address (a one-time set-up step).  The call waits for its result on
+ * the context's stream and leaves the caller's current device unchanged. */
 int gbgpu_validate_permutation_noalloc(gbgpu_ctx* ctx, const int32_t* new_ids_dev, int64_t n,
                                        int32_t* result);
 
 /* FNV-1a-64 fingerprint of a forward map, on the host, as the builder prints
  * it ("Mapping Fingerprint"). */
 uint64_t gbgpu_fingerprint(const int32_t* new_ids, int64_t n);
+
+/* ---- Synthetic inputs of the builder lifecycle ----
+ * gbgpu_gapbs_edge_list -> Generator::GenerateEL (bench/include/external/gapbs/
+ *   generator.h:101-164): the edge list `converter -g <scale> -k <degree>`
+ *   (uniform = 0, RMAT with permuted ids) or `-u <scale> -k <degree>`
+ *   (uniform = 1) draws, seed kRandSeed (util.h:47), on the HOST with
+ *   `threads` threads (0 = all).  src/dst are host arrays of
+ *   gbgpu_gapbs_edge_count(scale, degree) entries.  The builder's squish
+ *   (vertex count = largest id + 1, symmetrize, sort, de-duplicate, drop
+ *   self-loops; builder.h:254-312) is left to the caller.  gbgpu_gapbs_edge_count
+ *   returns -1 for a scale outside 0..30 or a negative degree. */
+int64_t gbgpu_gapbs_edge_count(int32_t scale, int32_t degree);
+int gbgpu_gapbs_edge_list(int32_t scale, int32_t degree, int32_t uniform, int32_t* src, int32_t* dst,
+                          int32_t threads);
 
 /* ---- Consumers timed after a mapping, and the selector's other arm ----
  * The reference's "map + kernel" end-to-end time is the mapping plus runs of

@@ -72,9 +72,29 @@ class ComposeStats(C.Structure):
 
 
 def build() -> str:
-    """Compile the plain-C oracle (seconds)."""
-    subprocess.run(["make", "-s", "-C", HERE, "_build/libgborc.so"], check=True)
+    """Compile the plain-C oracle and the CPU-side GAPBS graph builder (seconds)."""
+    subprocess.run(["make", "-s", "-C", HERE, "_build/libgborc.so", "_build/libgbgapbs.so"], check=True)
     return ORACLE_SO
+
+
+GAPBS_SO = os.path.join(HERE, "_build", "libgbgapbs.so")
+
+
+def gapbs_graph(scale, degree=16, uniform=False):
+    """GAPBS's graph for ``-g/-u <scale> -k <degree> -s`` built on the host
+    (oracle/gapbs_graph.cc): (row_ptr int64, col int32) numpy arrays."""
+    if not os.path.exists(GAPBS_SO):
+        build()
+    lib = C.CDLL(GAPBS_SO)
+    lib.orc_gapbs_build.restype = C.c_int64
+    lib.orc_gapbs_build.argtypes = [C.c_int, C.c_int, C.c_int]
+    lib.orc_gapbs_nnz.restype = C.c_int64
+    lib.orc_gapbs_copy.argtypes = [_i64p, _i32p]
+    n = lib.orc_gapbs_build(scale, degree, int(bool(uniform)))
+    rp = np.zeros(n + 1, dtype=np.int64)
+    cl = np.zeros(lib.orc_gapbs_nnz(), dtype=np.int32)
+    lib.orc_gapbs_copy(rp, cl)
+    return rp, cl
 
 
 _lib = None

@@ -87,3 +87,22 @@ def test_cli_serial_mapping_lifecycle(cli, tmp_path):
     assert f"Mapping Fingerprint: {po.fingerprint(ids)}" in r.stdout
     for label in ("Reorder Core Time", "Reorder Validation Time", "Reorder Apply Time", "Reorder End-to-End Time"):
         assert label + ":" in r.stdout
+
+
+@pytest.mark.parametrize("flag,scale", [("-g", 12), ("-u", 11)])
+def test_gapbs_generator_without_seed(cli, tmp_path, flag, scale):
+    """Without -r, -g/-u build GAPBS's own graph (the converter's)."""
+    out = tmp_path / "g.sg"
+    subprocess.run([cli, flag, str(scale), "-b", str(out)], check=True, capture_output=True)
+    rp, col, _ = read_sg(out)
+    erp, ecol = po.gapbs_graph(scale, 16, uniform=(flag == "-u"))
+    np.testing.assert_array_equal(rp, erp)
+    np.testing.assert_array_equal(col, ecol)
+
+
+@pytest.mark.gpu
+def test_cli_gapbs_g16_prints_the_converters_fingerprint(cli):
+    """`gbconvert -g 16 -s -o 12:<cd_serial recipe>` prints the fingerprint the
+    reference's `converter` printed for the same command (9b52c0603aacbbdb)."""
+    r = subprocess.run([cli, "-g", "16", "-s", "-o", "12:" + SERIAL], check=True, capture_output=True, text=True)
+    assert "Mapping Fingerprint: 9b52c0603aacbbdb" in r.stdout

@@ -2,8 +2,8 @@
 
 gbgpu_validate_permutation_noalloc exists for callers that cannot allocate
 device memory (a process whose GPU memory belongs to another framework's
-allocator, work issued during stream capture, latency-critical loops that
-cannot take cudaMalloc's implicit synchronisation).  It must give the same
+allocator, latency-critical loops that cannot take cudaMalloc's implicit
+synchronisation).  It must give the same
 answers as gbgpu_validate_permutation, call after call, although every call
 reuses one fixed scratch array that still holds the previous call's data.
 
