@@ -86,6 +86,32 @@ class GbgpuStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class GbgpuSelectionPolicy(C.Structure):
+    _fields_ = [("model", C.c_int32), ("criterion", C.c_int32), ("reuse", C.c_double),
+                ("reuse_explicit", C.c_int32)]
+
+
+class GbgpuSelectorModel(C.Structure):
+    _fields_ = [("in_dim", C.c_int32), ("params", C.c_void_p), ("mean", C.c_void_p), ("std", C.c_void_p),
+                ("lo", C.c_void_p), ("hi", C.c_void_p), ("cache_bytes", C.c_int64)]
+
+
+class GbgpuSelection(C.Structure):
+    _fields_ = [("policy", GbgpuSelectionPolicy), ("arm", C.c_int32), ("applied", C.c_char * 160),
+                ("reason", C.c_char * 48), ("features", C.c_double * 9), ("property_bytes", C.c_int64),
+                ("cache_bytes", C.c_int64), ("property_wsr", C.c_double), ("predicted_log10_ms", C.c_float * 3)]
+
+    def as_dict(self):
+        return {"model": self.policy.model, "criterion": self.policy.criterion, "reuse": self.policy.reuse,
+                "arm": self.arm, "applied": self.applied.decode(), "reason": self.reason.decode(),
+                "features": list(self.features), "property_bytes": self.property_bytes,
+                "cache_bytes": self.cache_bytes, "property_wsr": self.property_wsr,
+                "predicted_log10_ms": list(self.predicted_log10_ms)}
+
+
+KERNELS = {"generic": 0, "pr": 1, "bfs": 2, "cc": 3, "sssp": 4, "bc": 5, "tc": 6, "pr_spmv": 7, "cc_sv": 8}
+SELECTOR_MODEL_PATH = os.path.join(_HERE, "data", "selector_mlp.gbsel")
+
 # Every entry point declared in include/gbgpu.h, with its ctypes signature.
 _P = C.c_void_p
 SIGNATURES = {
@@ -111,6 +137,17 @@ SIGNATURES = {
     "gbgpu_gapbs_edge_count": (C.c_int64, [C.c_int32, C.c_int32]),
     "gbgpu_gapbs_edge_list": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _P, _P, C.c_int32]),
     "gbgpu_version": (C.c_char_p, []),
+    "gbgpu_parse_selection_policy": (C.c_int, [C.c_char_p, C.POINTER(GbgpuSelectionPolicy), C.c_char_p,
+                                               C.c_size_t]),
+    "gbgpu_selection_model_name": (C.c_char_p, [C.c_int32]),
+    "gbgpu_selection_criterion_name": (C.c_char_p, [C.c_int32]),
+    "gbgpu_apply_selection_rule": (C.c_int, [C.c_int32, _P, C.c_double, C.c_int32, C.c_double,
+                                             C.POINTER(GbgpuSelection)]),
+    "gbgpu_modeled_property_bytes": (C.c_int64, [C.c_int32, C.c_int64, C.c_int64]),
+    "gbgpu_selector_model_load": (C.c_int, [C.c_char_p, C.POINTER(C.POINTER(GbgpuSelectorModel))]),
+    "gbgpu_selector_model_free": (None, [C.POINTER(GbgpuSelectorModel)]),
+    "gbgpu_select_arm": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int64, C.c_char_p, C.c_int32,
+                                   C.POINTER(GbgpuSelectorModel), C.POINTER(GbgpuSelection), C.c_uint32]),
     "gbgpu_generate_mappings_batched": (C.c_int, [_P, C.POINTER(GbgpuGraph), C.c_int32, C.c_char_p,
                                                   C.POINTER(GbgpuSchedule), _P, C.POINTER(C.c_double), C.c_uint32]),
     "gbgpu_pagerank": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int64, C.c_int32, C.c_double, _P,
@@ -456,6 +493,18 @@ class Context:
                                                   y.ctypes.data, 0))
         return y
 
+    def select_arm(self, row_ptr, col, options, kernel="pr", model=None):
+        """Algorithm 14 on one graph: ``options`` are the fields after "14:"
+        (e.g. "_:_:_:learned-mlp:best-endtoend:1"), ``kernel`` the benchmark
+        kind, ``model`` a SelectorModel (needed by learned-mlp).  Returns the
+        selection as a dict (arm 12 / 5 / 0, recipe, reason, features)."""
+        rp, cl, prp, pcl, n, nnz, dev = self._graph_args(row_ptr, col)
+        out = GbgpuSelection()
+        mp = model.ptr if model is not None else None
+        self._check(library().gbgpu_select_arm(self._h, prp, pcl, n, nnz, options.encode(), KERNELS[kernel], mp,
+                                                 C.byref(out), DEVICE_POINTERS if dev else 0))
+        return out.as_dict()
+
     def mlp_gradient(self, params, X, T):
         """(gradient packed like params, mean squared error)."""
         p, x, t = self._f32(params), self._f32(X), self._f32(T)
@@ -484,6 +533,38 @@ def default_context() -> Context:
     if _default_ctx is None:
         _default_ctx = Context()
     return _default_ctx
+
+
+class SelectorModel:
+    """A learned selector loaded by the C ABI (gbgpu_selector_model_load)."""
+
+    def __init__(self, path=SELECTOR_MODEL_PATH):
+        self.ptr = C.POINTER(GbgpuSelectorModel)()
+        rc = library().gbgpu_selector_model_load(path.encode(), C.byref(self.ptr))
+        if rc != OK:
+            _raise(rc, f"cannot load selector model {path}")
+
+    def close(self):
+        if self.ptr:
+            library().gbgpu_selector_model_free(self.ptr)
+            self.ptr = C.POINTER(GbgpuSelectorModel)()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def parse_selection_policy(options: str) -> dict:
+    """ParseDeployableSelectionPolicy on the fields after "14:"; raises
+    ValueError with the reference's exception text."""
+    pol = GbgpuSelectionPolicy()
+    err = C.create_string_buffer(512)
+    rc = library().gbgpu_parse_selection_policy(options.encode(), C.byref(pol), err, 512)
+    if rc != OK:
+        _raise(rc, err.value.decode())
+    return {"model": pol.model, "criterion": pol.criterion, "reuse": pol.reuse, "explicit": pol.reuse_explicit}
 
 
 def generate_mapping(row_ptr, col, options=DEFAULT_RECIPE, auto_resolution=None):

@@ -11,8 +11,18 @@
 // in GAPBS's formats (writer.h:336-398).
 //
 // Flags: -f <file.el|.sg>  -g <scale>  -u <scale>  -k <degree>  -s
-//        -o 12:<tokens> (repeatable)  -q <out.lo>  -x <out.so>  -b <out.sg>
-//        -e <out.el>  -d <cuda device>  -r <seed>
+//        -o 12:<tokens> | -o 14:<fields> (repeatable)  -q <out.lo>  -x <out.so>
+//        -b <out.sg>  -e <out.el>  -d <cuda device>  -r <seed>
+//        -K <kernel: pr|bfs|cc|sssp|bc|tc|pr_spmv|cc_sv>  -M <selector model file>
+//
+// -o 14:_:_:_:<model>:<criterion>:<reuse> is the deployable selector
+// (reorder_adaptive.h:517-715): gbgpu_select_arm picks algorithm 12, DBG "5"
+// or the original order "0" for the graph and the kernel named by -K (the
+// benchmark binaries' type hint; without it the selection fails as the
+// reference's converter does), and that arm's mapping then goes through the
+// same lifecycle.  Models: allkernel-lowreuse-rule, budgeted-rule, or
+// learned-mlp (weights from -M, default data/selector_mlp.gbsel beside this
+// binary).
 //
 // -g / -u build GAPBS's own synthetic graph (generator.h:101-164 through
 // gbgpu_gapbs_edge_list, then the builder's squish), so `gbconvert -g 22`
@@ -21,6 +31,7 @@
 // family instead (graphgen.py), which GAPBS has no counterpart for.
 #include <cuda_runtime.h>
 #include <getopt.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <chrono>
@@ -250,15 +261,34 @@ void write_outputs(const HostGraph& g, const std::string& lo, const std::string&
     }
 }
 
+// Directory of this executable (for the default selector model).
+std::string exe_dir() {
+    char buf[4096];
+    const ssize_t k = readlink("/proc/self/exe", buf, sizeof(buf) - 1);
+    if (k <= 0) return ".";
+    buf[k] = '\0';
+    std::string p(buf);
+    const size_t slash = p.rfind('/');
+    return slash == std::string::npos ? "." : p.substr(0, slash);
+}
+
+int kernel_of(const std::string& k) {
+    static const char* names[] = {"generic", "pr", "bfs", "cc", "sssp", "bc", "tc", "pr_spmv", "cc_sv"};
+    for (int i = 0; i < 9; ++i)
+        if (k == names[i]) return i;
+    throw std::invalid_argument("unknown kernel for -K: " + k);
+}
+
 int run(int argc, char** argv) {
-    std::string file, lo, so, sgout, elout;
+    std::string file, lo, so, sgout, elout, model_path;
+    int kernel = GBGPU_KERNEL_GENERIC;
     int gscale = -1, uscale = -1, degree = 16, device = 0;
     uint64_t seed = 27491095;
     bool seeded = false;
     bool symmetrize = false;
     std::vector<std::string> orders;
     int c;
-    while ((c = getopt(argc, argv, "f:g:u:k:so:q:x:b:e:d:r:h")) != -1) {
+    while ((c = getopt(argc, argv, "f:g:u:k:so:q:x:b:e:d:r:K:M:h")) != -1) {
         switch (c) {
             case 'f': file = optarg; break;
             case 'g': gscale = std::atoi(optarg); break;
@@ -275,9 +305,12 @@ int run(int argc, char** argv) {
                 seed = std::strtoull(optarg, nullptr, 10);
                 seeded = true;
                 break;
+            case 'K': kernel = kernel_of(optarg); break;
+            case 'M': model_path = optarg; break;
             default:
                 std::printf("gbconvert -f <file.el|.sg> | -g <scale> | -u <scale> [-k deg] [-r seed] [-s]\n"
                             "          -o 12:<tokens> [-q out.lo] [-x out.so] [-b out.sg] [-e out.el] [-d dev]\n"
+                            "          -o 14:_:_:_:<model>:<criterion>:<reuse> -K <pr|bfs|cc|...> [-M model.gbsel]\n"
                             "  -g/-u: GAPBS's generator (same graph as converter); with -r <seed>: the\n"
                             "         project's seeded generator\n");
                 return c == 'h' ? 0 : 1;
@@ -318,11 +351,9 @@ int run(int argc, char** argv) {
     gbgpu_auto_resolution(ctx, d_rp, g.n, nnz, GBGPU_DEVICE_POINTERS, &auto_res);
 
     std::vector<int32_t> ids(g.n);
-    for (const std::string& o : orders) {
-        const size_t colon = o.find(':');
-        const std::string algo = o.substr(0, colon);
-        const std::string opts = colon == std::string::npos ? "" : o.substr(colon + 1);
-        if (algo != "12") throw std::invalid_argument("gbconvert runs reordering algorithm 12 only, got " + algo);
+    // Algorithm 12 on the resident graph: prints the GraphBrew lines, returns
+    // the core seconds.
+    auto map12 = [&](const std::string& opts) {
         char json[16384];
         gbgpu_config cfg;
         int rc = gbgpu_parse_config(opts.c_str(), auto_res, &cfg, json, sizeof(json));
@@ -332,7 +363,7 @@ int run(int argc, char** argv) {
                     cfg.max_iterations, cfg.max_passes);
         std::printf("GraphBrew: community-detection=%s\n", cfg.deterministic ? "serial" : "parallel");
         gbgpu_stats st;
-        double t = now();
+        const double t = now();
         rc = gbgpu_generate_mapping(ctx, d_rp, d_col, g.n, nnz, opts.c_str(), auto_res, d_ids, &st,
                                     GBGPU_DEVICE_POINTERS);
         const double core = now() - t;
@@ -347,11 +378,69 @@ int run(int argc, char** argv) {
                     "fallback-communities=%ld, fallback-vertices=%ld\n",
                     (long)st.gorder_communities, (long)st.gorder_vertices, (long)st.gorder_max_community,
                     (long)st.fallback_communities, (long)st.fallback_vertices);
+        return core;
+    };
+    gbgpu_selector_model* model = nullptr;
+    for (const std::string& o : orders) {
+        const size_t colon = o.find(':');
+        const std::string algo = o.substr(0, colon);
+        const std::string opts = colon == std::string::npos ? "" : o.substr(colon + 1);
+        if (algo != "12" && algo != "14")
+            throw std::invalid_argument("gbconvert runs reordering algorithms 12 and 14 only, got " + algo);
+        double core = 0.0;
+        if (algo == "12") {
+            core = map12(opts);
+        } else {
+            // Full-graph AdaptiveOrder (reorder_adaptive.h:517-715) with the
+            // deployable models.
+            std::cout << "=== Full-Graph Adaptive Mode (Standalone) ===" << std::endl;
+            std::cout << "Nodes: " << g.n << ", Edges: " << nnz << std::endl;
+            gbgpu_selection_policy pol;
+            char err[512];
+            if (gbgpu_parse_selection_policy(opts.c_str(), &pol, err, sizeof(err)) != GBGPU_OK)
+                throw std::invalid_argument(err);
+            if (pol.model == 9 && !model) {
+                const std::string path = model_path.empty() ? exe_dir() + "/data/selector_mlp.gbsel" : model_path;
+                if (gbgpu_selector_model_load(path.c_str(), &model) != GBGPU_OK)
+                    throw std::invalid_argument("cannot load selector model " + path);
+            }
+            const double t0 = now();
+            gbgpu_selection sel;
+            int rc = gbgpu_select_arm(ctx, d_rp, d_col, g.n, nnz, opts.c_str(), kernel, model, &sel,
+                                      GBGPU_DEVICE_POINTERS);
+            if (rc == GBGPU_E_PARSE || rc == GBGPU_E_INVALID) throw std::invalid_argument(gbgpu_last_error(ctx));
+            if (rc != GBGPU_OK) throw std::runtime_error(gbgpu_last_error(ctx));
+            const double tsel = now() - t0;
+            print_time("Property WSR LLC", sel.property_wsr);
+            std::printf("Selection: model=%s criterion=%s\n", gbgpu_selection_model_name(sel.policy.model),
+                        gbgpu_selection_criterion_name(sel.policy.criterion));
+            print_time("Adaptive Selection Time", tsel);
+            print_label("Adaptive Applied", sel.applied);
+            print_label("Adaptive Override Reason", sel.reason);
+            std::printf("\n=== Selected Algorithm: %s ===\n", sel.applied);
+            const double ta = now();
+            if (sel.arm == 12) {
+                const std::string applied(sel.applied);
+                map12(applied.substr(applied.find(':') + 1));
+            } else if (sel.arm == 5) {
+                rc = gbgpu_dbg_mapping(ctx, d_rp, d_col, g.n, nnz, d_ids, nullptr, GBGPU_DEVICE_POINTERS);
+                if (rc != GBGPU_OK) throw std::runtime_error(gbgpu_last_error(ctx));
+            } else {
+                std::vector<int32_t> iota(g.n);
+                for (int64_t v = 0; v < g.n; ++v) iota[v] = (int32_t)v;
+                CU(cudaMemcpy(d_ids, iota.data(), g.n * sizeof(int32_t), cudaMemcpyHostToDevice));
+            }
+            CU(cudaDeviceSynchronize());
+            print_time("Adaptive Arm Map Time", now() - ta);
+            core = now() - t0;
+            print_time("Full-Graph Adaptive Time", core);
+        }
         std::cout << "=== Reorder Summary ===" << std::endl;
-        print_label("Algorithm", "GraphBrewOrder");
+        print_label("Algorithm", algo == "12" ? "GraphBrewOrder" : "AdaptiveOrder");
         print_time("Reorder Core Time", core);
         print_time("Reorder Time", core);
-        t = now();
+        double t = now();
+        int rc = GBGPU_OK;
         int32_t valid = 0;
         rc = gbgpu_validate_permutation(ctx, d_ids, g.n, GBGPU_DEVICE_POINTERS, &valid);
         const double vtime = now() - t;
@@ -387,6 +476,7 @@ int run(int argc, char** argv) {
     cudaFree(d_orp);
     cudaFree(d_ocol);
     cudaFree(d_ids);
+    if (model) gbgpu_selector_model_free(model);
     gbgpu_ctx_destroy(ctx);
     return 0;
 }

@@ -52,11 +52,12 @@ constexpr int kCoarseBits = 9;                // event grouping: 512 coarse buck
 constexpr int kCoarse = 1 << kCoarseBits;
 constexpr int kFineBits = kSlotBits - kCoarseBits;
 constexpr int kTbThreads = 1024;              // table insert / group: one window vertex per thread
-constexpr int kTbChunks = kWindowMax / kTbThreads;
+constexpr int kTbMinChunk = 512;            // smallest insert chunk (persistent CTAs)
+constexpr int kTbChunks = kWindowMax / kTbMinChunk;   // stride of the per-chunk histograms
 constexpr int kTbFinishThreads = 1024;        // table finish: one CTA per coarse bucket
 constexpr uint32_t kPadSlot = 0xFFFFFFFFu;
 static_assert(kTableSlots >= 2 * kEventsMax, "hash load factor <= 1/2");
-static_assert(kCoarse <= kTbThreads, "one coarse bucket per grouping thread");
+static_assert(kCoarse <= kTbMinChunk, "one coarse bucket per grouping thread");
 // Slots with many events ("hot": a community that many window vertices join
 // or leave) get a time-bucket index: bidx[b] = first event at time >= P + 16 b,
 // so a lookup searches at most 16 events instead of the whole slot.
@@ -261,12 +262,12 @@ struct Round {
     double* ndelta;
 };
 
-__device__ __forceinline__ Round round_view(const ExactState& a) {
+__device__ __forceinline__ Round round_view(const ExactState& a, const Ctl* c) {
     Round r;
-    r.P = a.ctl->P;
-    r.E = a.ctl->E;
-    r.tag = a.ctl->tag;
-    const int par = (int)(a.ctl->round & 1);
+    r.P = c->P;
+    r.E = c->E;
+    r.tag = c->tag;
+    const int par = (int)(c->round & 1);
     r.pbest = a.best[par];
     r.pact = a.act[par];
     r.nbest = a.best[par ^ 1];
@@ -348,7 +349,7 @@ __device__ __forceinline__ long long warp_lower_bound_u32(const uint32_t* a, lon
 
 // Window ranges of the hub segment lists, the mid-degree list and the
 // big-row list for the window [P, E): eight searches on warps 0-7.
-__device__ __forceinline__ void window_ranges(const ExactState& a, long long P, long long E) {
+__device__ __forceinline__ void window_ranges(const ExactState& a, Ctl* c, long long P, long long E) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (w >= 8) return;
     const uint32_t* arr = w < 2 ? a.eseg_v : (w < 4 ? a.tseg_v : (w < 6 ? a.mid_v : a.big_v));
@@ -356,14 +357,14 @@ __device__ __forceinline__ void window_ranges(const ExactState& a, long long P, 
     const long long pos = warp_lower_bound_u32(arr, len, (uint32_t)((w & 1) ? E : P), lane);
     if (lane == 0) {
         switch (w) {
-            case 0: a.ctl->es0 = pos; break;
-            case 1: a.ctl->es1 = pos; break;
-            case 2: a.ctl->ts0 = pos; break;
-            case 3: a.ctl->ts1 = pos; break;
-            case 4: a.ctl->ms0 = pos; break;
-            case 5: a.ctl->ms1 = pos; break;
-            case 6: a.ctl->bs0 = pos; break;
-            default: a.ctl->bs1 = pos; break;
+            case 0: c->es0 = pos; break;
+            case 1: c->es1 = pos; break;
+            case 2: c->ts0 = pos; break;
+            case 3: c->ts1 = pos; break;
+            case 4: c->ms0 = pos; break;
+            case 5: c->ms1 = pos; break;
+            case 6: c->bs0 = pos; break;
+            default: c->bs1 = pos; break;
         }
     }
 }
@@ -413,23 +414,16 @@ __device__ __forceinline__ uint32_t table_insert(SlotMeta* slots, unsigned long 
     }
 }
 
-__global__ void __launch_bounds__(kTbThreads) k_tb_insert(ExactState a) {
+// Window chunk `chunk` (blockDim.x consecutive window vertices).
+__device__ __forceinline__ void tb_insert_chunk(const ExactState& a, const Ctl* c, int chunk) {
     __shared__ int32_t hist[kCoarse];
-    const long long P = a.ctl->P, E = a.ctl->E;
-    if (P >= a.ctl->n) return;
-    const Round r = round_view(a);
-    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const long long P = c->P, E = c->E;
+    const Round r = round_view(a, c);
+    const int tid = threadIdx.x;
     for (int b = tid; b < kCoarse; b += blockDim.x) hist[b] = 0;
-    if (blockIdx.x == 0 && tid == 0) {
-        a.ctl->first_change = kNoChange;
-        a.ctl->nhot = 0;
-        a.ctl->tb_big = 0;
-    }
-    (void)lane;
-    (void)w;
     __syncthreads();
     const int W = (int)(E - P);
-    const int i = blockIdx.x * blockDim.x + tid;
+    const int i = chunk * blockDim.x + tid;
     if (i < W) {
         const int64_t wv = P + i;
         const uint8_t pa = r.pact[wv];
@@ -449,25 +443,35 @@ __global__ void __launch_bounds__(kTbThreads) k_tb_insert(ExactState a) {
         a.wdeg[i] = dg;
     }
     __syncthreads();
-    for (int b = tid; b < kCoarse; b += blockDim.x) a.tb_hist[b * kTbChunks + blockIdx.x] = hist[b];
+    for (int b = tid; b < kCoarse; b += blockDim.x) a.tb_hist[b * kTbChunks + chunk] = hist[b];
+    __syncthreads();   // hist is reused by the CTA's next chunk
+}
+
+__global__ void __launch_bounds__(kTbThreads) k_tb_insert(ExactState a) {
+    if (a.ctl->P >= a.ctl->n) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.ctl->first_change = kNoChange;
+        a.ctl->nhot = 0;
+        a.ctl->tb_big = 0;
+    }
+    tb_insert_chunk(a, a.ctl, blockIdx.x);
 }
 
 // Stable scatter of each chunk's events to their coarse buckets.  Warp w of a
 // chunk owns its 32 consecutive vertices, i.e. 64 consecutive events.
-__global__ void __launch_bounds__(kTbThreads) k_tb_group(ExactState a) {
+__device__ __forceinline__ void tb_group_chunk(const ExactState& a, const Ctl* c, int chunk, int chunks) {
     __shared__ int32_t base[kCoarse];
     __shared__ int32_t warp_sum[32];
-    extern __shared__ int32_t wcnt[];   // 32 warps x kCoarse
-    const long long P = a.ctl->P, E = a.ctl->E;
-    if (P >= a.ctl->n) return;
+    extern __shared__ int32_t wcnt[];   // warps x kCoarse
+    const long long P = c->P, E = c->E;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int nwarps = blockDim.x >> 5;
     const int W = (int)(E - P);
-    const int chunks = gridDim.x;
     // Bucket totals over all chunks and this chunk's offset inside each bucket.
     int tot = 0, pre = 0;
     if (tid < kCoarse) {
         // Eight chunk counts in flight per step.
-        const int32_t* h = a.tb_hist + tid * kTbChunks;
+        const int32_t* h = a.tb_hist + tid * kTbChunks;   // bucket tid's counts, one per chunk
         for (int c0 = 0; c0 < chunks; c0 += 8) {
             int v[8];
 #pragma unroll
@@ -475,7 +479,7 @@ __global__ void __launch_bounds__(kTbThreads) k_tb_group(ExactState a) {
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
                 tot += v[k];
-                if (c0 + k < (int)blockIdx.x) pre += v[k];
+                if (c0 + k < chunk) pre += v[k];
             }
         }
     }
@@ -488,7 +492,7 @@ __global__ void __launch_bounds__(kTbThreads) k_tb_group(ExactState a) {
     if (lane == 31) warp_sum[w] = incl;
     __syncthreads();
     if (w == 0) {
-        const int v = warp_sum[lane];
+        const int v = lane < nwarps ? warp_sum[lane] : 0;
         int vi = v;
         for (int o = 1; o < 32; o <<= 1) {
             const int y = __shfl_up_sync(0xFFFFFFFFu, vi, o);
@@ -500,16 +504,16 @@ __global__ void __launch_bounds__(kTbThreads) k_tb_group(ExactState a) {
     const int excl = warp_sum[w] + incl - tot;
     if (tid < kCoarse) {
         base[tid] = excl + pre;
-        if (blockIdx.x == 0) {
+        if (chunk == 0) {
             a.tb_bstart[tid] = excl;
             if (tid == kCoarse - 1) a.tb_bstart[kCoarse] = excl + tot;
             if (tot) atomicMax(&a.ctl->tb_big, ((unsigned long long)tot << 32) | (unsigned long long)tid);
         }
     }
-    for (int k = tid; k < 32 * kCoarse; k += blockDim.x) wcnt[k] = 0;
+    for (int k = tid; k < nwarps * kCoarse; k += blockDim.x) wcnt[k] = 0;
     __syncthreads();
     // Count per warp, then turn counts into per-warp offsets (exclusive over warps).
-    const int v0 = blockIdx.x * kTbThreads + w * 32;   // first window offset of this warp
+    const int v0 = chunk * (int)blockDim.x + w * 32;   // first window offset of this warp
     uint32_t sl[2];
 #pragma unroll
     for (int st = 0; st < 2; ++st) {
@@ -524,7 +528,7 @@ __global__ void __launch_bounds__(kTbThreads) k_tb_group(ExactState a) {
     __syncthreads();
     for (int b = tid; b < kCoarse; b += blockDim.x) {
         int acc = base[b];
-        for (int ww = 0; ww < 32; ++ww) {
+        for (int ww = 0; ww < nwarps; ++ww) {
             const int t = wcnt[ww * kCoarse + b];
             wcnt[ww * kCoarse + b] = acc;
             acc += t;
@@ -545,31 +549,37 @@ __global__ void __launch_bounds__(kTbThreads) k_tb_group(ExactState a) {
         }
         __syncwarp();
     }
+    __syncthreads();   // shared arrays are reused by the CTA's next chunk
+}
+
+__global__ void __launch_bounds__(kTbThreads) k_tb_group(ExactState a) {
+    if (a.ctl->P >= a.ctl->n) return;
+    tb_group_chunk(a, a.ctl, blockIdx.x, gridDim.x);
 }
 
 // One CTA per coarse bucket: stable pass on the fine slot bits, then the
 // segmented inclusive scan of signed degrees; writes times, prefixes and the
 // slots' event ranges.
-__global__ void __launch_bounds__(kTbFinishThreads) k_tb_finish(ExactState a) {
+// Coarse bucket number `vb` (after swapping the largest bucket to 0); the
+// CTA has at least kFine threads.
+__device__ __forceinline__ void tb_finish_bucket(const ExactState& a, const Ctl* c, int vb) {
     constexpr int kFine = 1 << kFineBits;
-    constexpr int kW = kTbFinishThreads / 32;
     constexpr int kRow = kFine + 1;          // padded row of per-warp digit counts
-    extern __shared__ int32_t wcnt[];   // kW x kRow per-warp digit counts (dynamic: > 48 KB)
+    extern __shared__ int32_t wcnt[];   // warps x kRow per-warp digit counts (dynamic: > 48 KB)
     __shared__ int32_t digit[kFine];
     __shared__ long long warp_v[32];
     __shared__ int warp_h[32];
-    const long long P = a.ctl->P;
-    if (P >= a.ctl->n) return;
+    const long long P = c->P;
     // The largest bucket (the one holding a community many window vertices
-    // join) goes to CTA 0, which the scheduler starts first.
+    // join) goes first (CTA 0 / virtual bucket 0).
     const int big = (int)(a.ctl->tb_big & 0xFFFFFFFFull);
-    const int bucket = blockIdx.x == 0 ? big : ((int)blockIdx.x == big ? 0 : (int)blockIdx.x);
+    const int bucket = vb == 0 ? big : (vb == big ? 0 : vb);
     const int bs = a.tb_bstart[bucket], be = a.tb_bstart[bucket + 1];
     const int cnt = be - bs;
     if (cnt == 0) return;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int nwarps = blockDim.x >> 5;
-    static_assert(kFine % 32 == 0 && kFine <= kTbFinishThreads, "digit scan layout");
+    static_assert(kFine % 32 == 0 && kFine <= kTbMinChunk, "digit scan layout: one thread per fine digit");
     for (int k = tid; k < nwarps * kRow; k += blockDim.x) wcnt[k] = 0;
     __syncthreads();
     // Stable pass on the fine slot bits: warp w owns a contiguous range; the
@@ -718,7 +728,7 @@ __global__ void __launch_bounds__(kTbFinishThreads) k_tb_finish(ExactState a) {
     __syncthreads();
     // Hot slots: their time-bucket starts (bidx[b] = first event at a time
     // >= P + kBucketV * b).
-    const int nb = (int)((a.ctl->E - P + kBucketV - 1) / kBucketV);
+    const int nb = (int)((c->E - P + kBucketV - 1) / kBucketV);
     for (int k0 = b0; k0 < b1; k0 += 8) {
         unsigned long long key[8];
         uint32_t eh[8];
@@ -745,6 +755,12 @@ __global__ void __launch_bounds__(kTbFinishThreads) k_tb_finish(ExactState a) {
                 for (int b = bk + 1; b <= nb; ++b) bx[b] = end;
         }
     }
+    __syncthreads();   // shared arrays are reused by the CTA's next bucket
+}
+
+__global__ void __launch_bounds__(kTbFinishThreads) k_tb_finish(ExactState a) {
+    if (a.ctl->P >= a.ctl->n) return;
+    tb_finish_bucket(a, a.ctl, blockIdx.x);
 }
 
 constexpr int kMidWarpsPerBlock = 4;
@@ -892,14 +908,14 @@ __device__ __forceinline__ void eval_vertex(const ExactState& a, const Round& r,
 // whole warp.
 constexpr int kTinyDeg = 8;
 
-__global__ void __launch_bounds__(kSmallWarpsPerBlock * 32) k_ex_eval_small(ExactState a) {
-    if (a.ctl->P >= a.ctl->n) return;
-    const Round r = round_view(a);
+__device__ __forceinline__ void eval_small_body(const ExactState& a, const Ctl* c) {
+    const Round r = round_view(a, c);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int g = lane >> 3, j = lane & 7;
     const unsigned gmask = 0xFFu << (g * 8);
-    const int64_t nw = (int64_t)gridDim.x * kSmallWarpsPerBlock;
-    for (int64_t u0 = r.P + 4 * ((int64_t)blockIdx.x * kSmallWarpsPerBlock + w); u0 < r.E; u0 += 4 * nw) {
+    const int wpb = (int)(blockDim.x >> 5);
+    const int64_t nw = (int64_t)gridDim.x * wpb;
+    for (int64_t u0 = r.P + 4 * ((int64_t)blockIdx.x * wpb + w); u0 < r.E; u0 += 4 * nw) {
         const int64_t u = u0 + g;
         const bool inwin = u < r.E;
         int64_t rb = 0;
@@ -982,10 +998,15 @@ __global__ void __launch_bounds__(kSmallWarpsPerBlock * 32) k_ex_eval_small(Exac
     }
 }
 
+__global__ void __launch_bounds__(kSmallWarpsPerBlock * 32) k_ex_eval_small(ExactState a) {
+    if (a.ctl->P >= a.ctl->n) return;
+    eval_small_body(a, a.ctl);
+}
+
 // Big rows (kWarpMaxDeg < degree <= kBigMaxDeg): one CTA per row, table in
 // shared memory, candidates compacted, lookups of four per thread interleaved.
 // Three CTAs per SM (registers capped near 80): more lookups in flight.
-__global__ void __launch_bounds__(kBigThreads, 3) k_ex_eval_big(ExactState a) {
+__device__ __forceinline__ void eval_big_body(const ExactState& a, const Ctl* c) {
     extern __shared__ uint32_t big_smem[];
     uint32_t* tk = big_smem;                      // kBigSlots keys
     uint32_t* tv = tk + kBigSlots;                // kBigSlots counts
@@ -993,11 +1014,10 @@ __global__ void __launch_bounds__(kBigThreads, 3) k_ex_eval_big(ExactState a) {
     uint32_t* cand_w = cand_c + kBigMaxDeg;
     __shared__ int s_any;
     __shared__ uint32_t s_cnt;
-    __shared__ double red_d[kBigThreads / 32];
-    __shared__ uint32_t red_c[kBigThreads / 32];
-    if (a.ctl->P >= a.ctl->n) return;
-    const Round r = round_view(a);
-    const long long b0 = a.ctl->bs0, b1 = a.ctl->bs1;
+    __shared__ double red_d[32];
+    __shared__ uint32_t red_c[32];
+    const Round r = round_view(a, c);
+    const long long b0 = c->bs0, b1 = c->bs1;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     for (long long bi = b0 + blockIdx.x; bi < b1; bi += gridDim.x) {
         const uint32_t u = a.big_v[bi];
@@ -1101,18 +1121,28 @@ __global__ void __launch_bounds__(kBigThreads, 3) k_ex_eval_big(ExactState a) {
     }
 }
 
-// Mid rows of the window (from the ascending list of mid-degree vertices).
-__global__ void __launch_bounds__(kMidWarpsPerBlock * 32) k_ex_eval_mid(ExactState a) {
-    extern __shared__ uint32_t ex_smem[];
+__global__ void __launch_bounds__(kBigThreads, 3) k_ex_eval_big(ExactState a) {
     if (a.ctl->P >= a.ctl->n) return;
-    const Round r = round_view(a);
-    const long long m0 = a.ctl->ms0, m1 = a.ctl->ms1;
+    eval_big_body(a, a.ctl);
+}
+
+// Mid rows of the window (from the ascending list of mid-degree vertices).
+__device__ __forceinline__ void eval_mid_body(const ExactState& a, const Ctl* c) {
+    extern __shared__ uint32_t ex_smem[];
+    const Round r = round_view(a, c);
+    const long long m0 = c->ms0, m1 = c->ms1;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int wpb = (int)(blockDim.x >> 5);
     uint32_t* tk = ex_smem + (size_t)w * 2 * kWarpHash;
     uint32_t* tv = tk + kWarpHash;
-    const long long nw = (long long)gridDim.x * kMidWarpsPerBlock;
-    for (long long i = m0 + (long long)blockIdx.x * kMidWarpsPerBlock + w; i < m1; i += nw)
+    const long long nw = (long long)gridDim.x * wpb;
+    for (long long i = m0 + (long long)blockIdx.x * wpb + w; i < m1; i += nw)
         eval_vertex<true>(a, r, a.mid_v[i], lane, tk, tv);
+}
+
+__global__ void __launch_bounds__(kMidWarpsPerBlock * 32) k_ex_eval_mid(ExactState a) {
+    if (a.ctl->P >= a.ctl->n) return;
+    eval_mid_body(a, a.ctl);
 }
 
 __global__ void k_mid_flags(const int64_t* __restrict__ rp, int64_t n, int32_t* __restrict__ flag) {
@@ -1131,10 +1161,9 @@ __global__ void k_mid_scatter(const int32_t* __restrict__ flag, const int64_t* _
 // Hub accumulation: one CTA per kHubSeg-edge segment of a window hub, four
 // edges per thread in flight.  Needs no event table: it runs while the
 // previous window commits its affected flags and the event table is built.
-__global__ void __launch_bounds__(kHubThreads2) k_ex_hub_accum(ExactState a) {
-    if (a.ctl->P >= a.ctl->n) return;
-    const Round r = round_view(a);
-    const long long q0 = a.ctl->es0, q1 = a.ctl->es1;
+__device__ __forceinline__ void hub_accum_body(const ExactState& a, const Ctl* c) {
+    const Round r = round_view(a, c);
+    const long long q0 = c->es0, q1 = c->es1;
     const int lane = threadIdx.x & 31;
     __shared__ int s_any;
     for (long long q = q0 + blockIdx.x; q < q1; q += gridDim.x) {
@@ -1155,7 +1184,7 @@ __global__ void __launch_bounds__(kHubThreads2) k_ex_hub_accum(ExactState a) {
         uint32_t c[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            const int64_t e = e0 + k * kHubThreads2 + threadIdx.x;
+            const int64_t e = e0 + k * (int64_t)blockDim.x + threadIdx.x;
             c[k] = kNone;
             if (e < e1) {
                 const int32_t v = a.col[e];
@@ -1190,16 +1219,20 @@ __global__ void __launch_bounds__(kHubThreads2) k_ex_hub_accum(ExactState a) {
     }
 }
 
+__global__ void __launch_bounds__(kHubThreads2) k_ex_hub_accum(ExactState a) {
+    if (a.ctl->P >= a.ctl->n) return;
+    hub_accum_body(a, a.ctl);
+}
+
 // Hub selection: one CTA per kTabSeg-slot segment of a window hub's table,
 // one slot per thread; the last CTA of a hub reduces the partial maxima and
 // records the decision.  Three CTAs per SM, as for the big rows.
-__global__ void __launch_bounds__(kHubThreads2, 3) k_ex_hub_select(ExactState a) {
-    if (a.ctl->P >= a.ctl->n) return;
-    const Round r = round_view(a);
-    const long long q0 = a.ctl->ts0, q1 = a.ctl->ts1;
+__device__ __forceinline__ void hub_select_body(const ExactState& a, const Ctl* c) {
+    const Round r = round_view(a, c);
+    const long long q0 = c->ts0, q1 = c->ts1;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    __shared__ double red_d[8];
-    __shared__ uint32_t red_c[8];
+    __shared__ double red_d[32];
+    __shared__ uint32_t red_c[32];
     __shared__ int s_last;
     for (long long q = q0 + blockIdx.x; q < q1; q += gridDim.x) {
         const HubSeg sg = a.tseg[q];
@@ -1295,9 +1328,19 @@ __global__ void __launch_bounds__(kHubThreads2, 3) k_ex_hub_select(ExactState a)
     }
 }
 
-__device__ __forceinline__ long long commit_end(const ExactState& a) {
-    const unsigned long long f = a.ctl->first_change;
-    const long long E = a.ctl->E;
+__global__ void __launch_bounds__(kHubThreads2, 3) k_ex_hub_select(ExactState a) {
+    if (a.ctl->P >= a.ctl->n) return;
+    hub_select_body(a, a.ctl);
+}
+
+// First change of the decided window (global, written by record()).
+__device__ __forceinline__ unsigned long long first_change_of(const ExactState& a) {
+    return *(volatile unsigned long long*)&a.ctl->first_change;
+}
+
+__device__ __forceinline__ long long commit_end(const ExactState& a, const Ctl* c) {
+    const unsigned long long f = first_change_of(a);
+    const long long E = c->E;
     return f == kNoChange ? E - 1 : min((long long)f, E - 1);
 }
 
@@ -1311,11 +1354,11 @@ struct CommitView {
     const double* delta;
 };
 
-__device__ __forceinline__ CommitView commit_view(const ExactState& a) {
+__device__ __forceinline__ CommitView commit_view(const ExactState& a, const Ctl* ct) {
     CommitView c;
-    c.P = a.ctl->cP;
-    c.x = a.ctl->cX;
-    const int par = (int)(a.ctl->round & 1);
+    c.P = ct->cP;
+    c.x = ct->cX;
+    const int par = (int)(ct->round & 1);
     c.act = a.act[par];
     c.best = a.best[par];
     c.delta = a.delta[par];
@@ -1325,8 +1368,8 @@ __device__ __forceinline__ CommitView commit_view(const ExactState& a) {
 // Commit [cP, cX]: totals and memberships of movers, final deltas, processed
 // flags cleared, move flags for the affected-flag kernels; and the decided
 // window's hub tables cleared for the next round.
-__global__ void k_ex_commit_a(ExactState a) {
-    const CommitView c = commit_view(a);
+__device__ __forceinline__ void commit_a_body(const ExactState& a, const Ctl* ct) {
+    const CommitView c = commit_view(a, ct);
     if (c.x < c.P) return;
     for (long long u = c.P + blockIdx.x * (long long)blockDim.x + threadIdx.x; u <= c.x;
          u += (long long)gridDim.x * blockDim.x) {
@@ -1344,7 +1387,7 @@ __global__ void k_ex_commit_a(ExactState a) {
         a.final_delta[u] = dl;
         a.vaff[u] = 0;
     }
-    const long long q0 = a.ctl->c_ts0, q1 = a.ctl->c_ts1;
+    const long long q0 = ct->c_ts0, q1 = ct->c_ts1;
     __shared__ int s_last;
     for (long long q = q0 + blockIdx.x; q < q1; q += gridDim.x) {
         const HubSeg sg = a.tseg[q];
@@ -1370,11 +1413,13 @@ __global__ void k_ex_commit_a(ExactState a) {
     }
 }
 
+__global__ void k_ex_commit_a(ExactState a) { commit_a_body(a, a.ctl); }
+
 // Affected flags from committed movers: every neighbour outside [cP, cX] and
 // every neighbour in [cP, cX] processed before the mover.  Non-hub movers
 // here, hub movers in k_ex_commit_hub.
-__global__ void k_ex_commit_b(ExactState a) {
-    const CommitView c = commit_view(a);
+__device__ __forceinline__ void commit_b_body(const ExactState& a, const Ctl* ct) {
+    const CommitView c = commit_view(a, ct);
     if (c.x < c.P) return;
     const int lane = threadIdx.x & 31;
     const long long wid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
@@ -1390,12 +1435,14 @@ __global__ void k_ex_commit_b(ExactState a) {
     }
 }
 
-__global__ void __launch_bounds__(kHubThreads2) k_ex_commit_hub(ExactState a) {
-    const CommitView c = commit_view(a);
+__global__ void k_ex_commit_b(ExactState a) { commit_b_body(a, a.ctl); }
+
+__device__ __forceinline__ void commit_hub_body(const ExactState& a, const Ctl* ct) {
+    const CommitView c = commit_view(a, ct);
     if (c.x < c.P) return;
     // Work items: the decided window's hub edge segments, then its big rows.
-    const long long q0 = a.ctl->c_es0, q1 = a.ctl->c_es1;
-    const long long g0 = a.ctl->c_bs0, g1 = a.ctl->c_bs1;
+    const long long q0 = ct->c_es0, q1 = ct->c_es1;
+    const long long g0 = ct->c_bs0, g1 = ct->c_bs1;
     const long long nseg = q1 - q0, items = nseg + (g1 - g0);
     for (long long q = blockIdx.x; q < items; q += gridDim.x) {
         uint32_t h;
@@ -1418,72 +1465,232 @@ __global__ void __launch_bounds__(kHubThreads2) k_ex_commit_hub(ExactState a) {
     }
 }
 
+__global__ void __launch_bounds__(kHubThreads2) k_ex_commit_hub(ExactState a) { commit_hub_body(a, a.ctl); }
+
 // After the window's decisions: fix the committed prefix [P, x] for the commit
 // kernels, slide the window (the new decisions become D_prev; entering
 // vertices are unknown) and tell the graph's loop whether to go on.  The next
 // window's event table and this window's commits then run concurrently: they
-// touch disjoint vertices.
-__global__ void __launch_bounds__(1024) k_ex_advance(ExactState a) {
-    const long long P = a.ctl->P, E = a.ctl->E, n = a.ctl->n, B = a.ctl->B;
+// touch disjoint vertices.  `c` is the control block this CTA works on; the
+// entering vertices' marks are written by threads (tid0, tid0 + tstride, ...),
+// one CTA in the graph, every CTA in the persistent kernel.  Ends with a CTA
+// barrier, so every thread sees the updated block.
+__device__ __forceinline__ void advance_ctl(const ExactState& a, Ctl* c, long long tid0, long long tstride,
+                                            bool set_cond) {
+    const long long P = c->P, E = c->E, n = c->n, B = c->B;
     if (P >= n) {
         __syncthreads();
         if (threadIdx.x == 0) {
-            a.ctl->cP = 1;   // nothing to commit
-            a.ctl->cX = 0;
-            if (a.use_cond) cudaGraphSetConditional(a.cond, 0u);
+            c->cP = 1;   // nothing to commit
+            c->cX = 0;
+            if (set_cond) cudaGraphSetConditional(a.cond, 0u);
         }
+        __syncthreads();
         return;
     }
-    const long long x = commit_end(a);
+    const long long x = commit_end(a, c);
     const long long nP = x + 1, nE = min(n, nP + B);
-    const int par = (int)(a.ctl->round & 1);
+    const int par = (int)(c->round & 1);
     uint8_t* next_prev_act = a.act[par ^ 1];
-    for (long long u = E + threadIdx.x; u < nE; u += blockDim.x) next_prev_act[u] = kUnknown;
+    for (long long u = E + tid0; u < nE; u += tstride) next_prev_act[u] = kUnknown;
     if (threadIdx.x == 0) {
-        a.ctl->c_es0 = a.ctl->es0;
-        a.ctl->c_es1 = a.ctl->es1;
-        a.ctl->c_ts0 = a.ctl->ts0;
-        a.ctl->c_ts1 = a.ctl->ts1;
-        a.ctl->c_bs0 = a.ctl->bs0;
-        a.ctl->c_bs1 = a.ctl->bs1;
+        c->c_es0 = c->es0;
+        c->c_es1 = c->es1;
+        c->c_ts0 = c->ts0;
+        c->c_ts1 = c->ts1;
+        c->c_bs0 = c->bs0;
+        c->c_bs1 = c->bs1;
     }
     __syncthreads();
-    window_ranges(a, nP, nE);
+    window_ranges(a, c, nP, nE);
     if (threadIdx.x == 0) {
-        const long long rnd = a.ctl->round + 1;
-        a.ctl->cP = P;
-        a.ctl->cX = x;
-        a.ctl->evals = a.ctl->evals + (E - P);
-        a.ctl->P = nP;
-        a.ctl->E = nE;
-        a.ctl->round = rnd;
-        a.ctl->tag = a.ctl->tag + 1;
+        const long long rnd = c->round + 1;
+        c->cP = P;
+        c->cX = x;
+        c->evals = c->evals + (E - P);
+        c->P = nP;
+        c->E = nE;
+        c->round = rnd;
+        c->tag = c->tag + 1;
         // Every round commits at least vertex P, so the loop ends within n
         // rounds; the bound only guards against a broken invariant.
         bool more = nP < n;
-        if (nP <= P || (more && rnd >= a.ctl->max_rounds)) {
-            a.ctl->error = 1;
-            a.ctl->P = n;
+        if (nP <= P || (more && rnd >= c->max_rounds)) {
+            c->error = 1;
+            c->P = n;
             more = false;
         }
-        if (a.use_cond) cudaGraphSetConditional(a.cond, more ? 1u : 0u);
+        if (set_cond) cudaGraphSetConditional(a.cond, more ? 1u : 0u);
     }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(1024) k_ex_advance(ExactState a) {
+    advance_ctl(a, a.ctl, threadIdx.x, blockDim.x, a.use_cond != 0);
+}
+
+// The first window of an iteration; same split of the marks as advance_ctl.
+__device__ __forceinline__ void init_ctl(const ExactState& a, Ctl* c, long long tid0, long long tstride) {
+    const long long n = c->n, B = c->B;
+    const long long E = min(n, B);
+    for (long long u = tid0; u < E; u += tstride) a.act[0][u] = kUnknown;
+    window_ranges(a, c, 0, E);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        c->P = 0;
+        c->E = E;
+        c->round = 0;
+        c->evals = 0;
+        c->cP = 1;
+        c->cX = 0;
+        c->tag = c->tag + 1;
+    }
+    __syncthreads();
 }
 
 __global__ void __launch_bounds__(1024) k_ex_init_iter(ExactState a) {
-    const long long n = a.ctl->n, B = a.ctl->B;
-    const long long E = min(n, B);
-    for (long long u = threadIdx.x; u < E; u += blockDim.x) a.act[0][u] = kUnknown;
-    window_ranges(a, 0, E);
+    init_ctl(a, a.ctl, threadIdx.x, blockDim.x);
+}
+
+// ---------------------------------------------------------------------------
+// Persistent engine: one iteration of local moving in one cooperative launch,
+// one CTA per SM.  Every CTA keeps an identical copy of the control block in
+// shared memory and runs the advance itself, so rounds need no host or graph
+// step; the phases of a round are separated by grid barriers:
+//   decide (hub selection, big / mid / small rows)
+//   | advance + next window's table insert + commit of [cP, cX]
+//   | table grouping + affected flags + next window's hub accumulation
+//   | table finish |
+// which is the dependency order of the graph round above, linearised.
+// ---------------------------------------------------------------------------
+constexpr int kPT = 512;                          // threads per persistent CTA
+constexpr long long kBarrierSpins = 1ll << 22;    // polls before a grid barrier gives up (seconds)
+
+struct GridBarrier {
+    unsigned int count;   // CTAs arrived in the current generation
+    unsigned int gen;     // generation, bumped by the last arrival
+};
+
+// All CTAs of the grid meet here (release / acquire at GPU scope, as a
+// cooperative grid sync does).  The wait is bounded: false means the barrier
+// gave up, after which the caller stops.
+__device__ __forceinline__ bool grid_barrier(GridBarrier* gbar, unsigned int nblocks) {
+    __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
-        a.ctl->P = 0;
-        a.ctl->E = E;
-        a.ctl->round = 0;
-        a.ctl->evals = 0;
-        a.ctl->cP = 1;
-        a.ctl->cX = 0;
-        a.ctl->tag = a.ctl->tag + 1;
+        unsigned int g, old, cur;
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(g) : "l"(&gbar->gen) : "memory");
+        asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(&gbar->count) : "memory");
+        int ok = 1;
+        if (old == nblocks - 1) {
+            asm volatile("st.relaxed.gpu.global.u32 [%0], 0;" ::"l"(&gbar->count) : "memory");
+            asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(&gbar->gen) : "memory");
+        } else {
+            long long spins = 0;
+            while (true) {
+                asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(&gbar->gen) : "memory");
+                if (cur != g) break;
+                if (++spins > kBarrierSpins) {
+                    ok = 0;
+                    break;
+                }
+            }
+        }
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// The persistent kernel calls each phase through its own (not inlined)
+// function, so that registers are allocated per phase rather than across the
+// whole round.
+__device__ __noinline__ void p_tb_insert(const ExactState& a, const Ctl* c, int ch) { tb_insert_chunk(a, c, ch); }
+__device__ __noinline__ void p_tb_group(const ExactState& a, const Ctl* c, int ch, int chunks) {
+    tb_group_chunk(a, c, ch, chunks);
+}
+__device__ __noinline__ void p_tb_finish(const ExactState& a, const Ctl* c, int vb) { tb_finish_bucket(a, c, vb); }
+__device__ __noinline__ void p_eval_small(const ExactState& a, const Ctl* c) { eval_small_body(a, c); }
+__device__ __noinline__ void p_eval_mid(const ExactState& a, const Ctl* c) { eval_mid_body(a, c); }
+__device__ __noinline__ void p_eval_big(const ExactState& a, const Ctl* c) { eval_big_body(a, c); }
+__device__ __noinline__ void p_hub_select(const ExactState& a, const Ctl* c) { hub_select_body(a, c); }
+__device__ __noinline__ void p_hub_accum(const ExactState& a, const Ctl* c) { hub_accum_body(a, c); }
+__device__ __noinline__ void p_commit_a(const ExactState& a, const Ctl* c) { commit_a_body(a, c); }
+__device__ __noinline__ void p_commit_b(const ExactState& a, const Ctl* c) { commit_b_body(a, c); }
+__device__ __noinline__ void p_commit_hub(const ExactState& a, const Ctl* c) { commit_hub_body(a, c); }
+
+__global__ void __launch_bounds__(kPT, 1) k_ex_persistent(ExactState a, GridBarrier* gbar) {
+    __shared__ Ctl sc;
+    const unsigned int nb = gridDim.x;
+    const long long gtid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long gstride = (long long)gridDim.x * blockDim.x;
+    const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
+    if (threadIdx.x == 0) sc = *a.ctl;   // n, B, max_rounds and the table generation
+    __syncthreads();
+    init_ctl(a, &sc, gtid, gstride);
+    int chunks = (int)((sc.E - sc.P + blockDim.x - 1) / blockDim.x);
+    // The first window's table and hub accumulation.
+    bool ok = grid_barrier(gbar, nb);
+    if (ok) {
+        if (lead) {
+            a.ctl->first_change = kNoChange;
+            a.ctl->nhot = 0;
+            a.ctl->tb_big = 0;
+        }
+        for (int ch = blockIdx.x; ch < chunks; ch += nb) p_tb_insert(a, &sc, ch);
+        p_hub_accum(a, &sc);
+        ok = grid_barrier(gbar, nb);
+    }
+    if (ok) {
+        for (int ch = blockIdx.x; ch < chunks; ch += nb) p_tb_group(a, &sc, ch, chunks);
+        ok = grid_barrier(gbar, nb);
+    }
+    if (ok) {
+        for (int vb = blockIdx.x; vb < kCoarse; vb += nb) p_tb_finish(a, &sc, vb);
+        ok = grid_barrier(gbar, nb);
+    }
+    while (ok && sc.P < sc.n) {
+        // Decide the window.
+        p_hub_select(a, &sc);
+        p_eval_big(a, &sc);
+        __syncthreads();   // the big rows' shared tables are the mid rows' next
+        p_eval_mid(a, &sc);
+        p_eval_small(a, &sc);
+        if (!(ok = grid_barrier(gbar, nb))) break;
+        // Advance (each CTA on its copy), next window's table insert, commit.
+        advance_ctl(a, &sc, gtid, gstride, false);
+        const bool more = sc.P < sc.n;
+        chunks = (int)((sc.E - sc.P + blockDim.x - 1) / blockDim.x);
+        if (lead) {
+            a.ctl->nhot = 0;
+            a.ctl->tb_big = 0;
+        }
+        if (more)
+            for (int ch = blockIdx.x; ch < chunks; ch += nb) p_tb_insert(a, &sc, ch);
+        p_commit_a(a, &sc);
+        if (!(ok = grid_barrier(gbar, nb))) break;
+        // Every CTA has read first_change (advance): reset it for the next decisions.
+        if (lead) a.ctl->first_change = kNoChange;
+        if (more)
+            for (int ch = blockIdx.x; ch < chunks; ch += nb) p_tb_group(a, &sc, ch, chunks);
+        p_commit_b(a, &sc);
+        p_commit_hub(a, &sc);
+        if (more) p_hub_accum(a, &sc);
+        if (!(ok = grid_barrier(gbar, nb))) break;
+        if (!more) break;
+        for (int vb = blockIdx.x; vb < kCoarse; vb += nb) p_tb_finish(a, &sc, vb);
+        if (!(ok = grid_barrier(gbar, nb))) break;
+    }
+    if (!ok && threadIdx.x == 0) atomicExch(reinterpret_cast<unsigned long long*>(&a.ctl->error), 3ull);
+    if (lead && ok) {
+        a.ctl->P = sc.P;
+        a.ctl->E = sc.E;
+        a.ctl->round = sc.round;
+        a.ctl->evals = sc.evals;
+        a.ctl->cP = sc.cP;
+        a.ctl->cX = sc.cX;
+        a.ctl->tag = sc.tag;
+        if (sc.error && a.ctl->error == 0) a.ctl->error = sc.error;
     }
 }
 
@@ -1825,8 +2032,33 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     // One local-moving iteration as one graph: the init kernel, then a
     // device-side while loop over rounds whose condition the advance kernel
     // sets.  GBGPU_EXACT_GRAPH=0 enqueues rounds from the host instead.
+    // Default: the persistent cooperative kernel (one launch per iteration).
+    // GBGPU_EXACT_PERSISTENT=0 runs the rounds as a CUDA graph per iteration
+    // (GBGPU_EXACT_GRAPH=0: enqueued from the host) with the same kernels'
+    // bodies; all three give the same result.
+    const char* penv = std::getenv("GBGPU_EXACT_PERSISTENT");
+    bool persistent = !(penv && penv[0] == '0');
+    int p_grid = 0;
+    const int p_smem = std::max(std::max((kPT / 32) * 2 * kWarpHash, 2 * kBigSlots + 2 * kBigMaxDeg),
+                                std::max((kPT / 32) * kCoarse, (kPT / 32) * ((1 << kFineBits) + 1))) *
+                       (int)sizeof(uint32_t);
+    if (persistent) {
+        int dev = 0, coop = 0, sms = kNumSMs, per_sm = 0;
+        GB_CUDA(cudaGetDevice(&dev));
+        GB_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+        GB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        GB_CUDA(cudaFuncSetAttribute(k_ex_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, p_smem));
+        GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ex_persistent, kPT, p_smem));
+        // One CTA per SM: the grid is co-resident by construction (checked by
+        // the cooperative launch), so the grid barriers cannot wait on a CTA
+        // that never starts.
+        if (coop && per_sm >= 1) p_grid = sms;
+        else persistent = false;
+    }
+    DevBuf<GridBarrier> gbar(1, s);
+    GB_CUDA(cudaMemsetAsync(gbar, 0, sizeof(GridBarrier), s));
     const char* genv = std::getenv("GBGPU_EXACT_GRAPH");
-    const bool use_graph = !(genv && genv[0] == '0');
+    const bool use_graph = !persistent && !(genv && genv[0] == '0');
     struct GraphGuard {
         cudaGraph_t g = nullptr;
         cudaGraphExec_t e = nullptr;
@@ -1885,7 +2117,15 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     int iterations = 0;
     int64_t rounds = 0, nl = 0, evals = 0;
     for (int it = 0; it < max_iterations; ++it) {
-        if (use_graph) {
+        if (persistent) {
+            a.use_cond = 0;
+            GridBarrier* bar = gbar.get();
+            void* args[] = {(void*)&a, (void*)&bar};
+            GB_CUDA(cudaLaunchCooperativeKernel((const void*)k_ex_persistent, dim3(p_grid), dim3(kPT), args,
+                                                (size_t)p_smem, s));
+            GB_CUDA(cudaMemcpyAsync(hctl, ctl.get(), sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+            GB_CUDA(cudaStreamSynchronize(s));
+        } else if (use_graph) {
             GB_CUDA(cudaGraphLaunch(gg.e, s));
             GB_CUDA(cudaMemcpyAsync(hctl, ctl.get(), sizeof(Ctl), cudaMemcpyDeviceToHost, s));
             GB_CUDA(cudaStreamSynchronize(s));
@@ -1899,11 +2139,13 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
                 if (hctl->P >= n) break;
             }
         }
+        if (hctl->error == 3)
+            throw Error(GBGPU_E_TIMEOUT, "serial-order local moving: a grid barrier of the persistent kernel timed out");
         if (hctl->error == 2)
             throw Error(GBGPU_E_CUDA, "serial-order local moving: event table slot with an invalid hot index");
         if (hctl->error)
             throw Error(GBGPU_E_CUDA, "serial-order local moving: round loop stopped without progress");
-        nl += 4 + (nh ? 1 : 0) + hctl->round * per_round;
+        nl += persistent ? 1 : 4 + (nh ? 1 : 0) + hctl->round * per_round;
         rounds += hctl->round;
         evals += hctl->evals;
         ++iterations;

@@ -23,6 +23,10 @@ Command line (GPU):
     python -m graphbrew_gb300.selector collect --first 0 --count 2200 --out records.npz
     python -m graphbrew_gb300.selector train --data records.npz --out model.npz
     python -m graphbrew_gb300.selector evaluate --data records.npz --model model.npz
+    python -m graphbrew_gb300.selector export --model model.npz --out model.gbsel
+
+The exported file drives ``-o 14:_:_:_:learned-mlp:best-endtoend:<reuse>``
+through the C ABI (``gbgpu_select_arm``) and ``gbconvert -M model.gbsel``.
 """
 from __future__ import annotations
 
@@ -231,6 +235,19 @@ class LearnedSelector:
             return frozen_rule(tier0, kernel, reuse, self.cache_bytes), "frozen-rule-fallback"
         return ARMS[int(np.argmin(self.predict(ctx, x)[0]))], "learned-mlp"
 
+    def save_binary(self, path):
+        """The model file gbgpu_selector_model_load reads (include/gbgpu.h):
+        magic, sizes, cache bytes, float32 parameters, float64 mean / std / lo / hi."""
+        import struct
+        in_dim = int(len(self.mean))
+        with open(path, "wb") as f:
+            f.write(b"GBSEL01\0")
+            f.write(struct.pack("<4i", in_dim, 64, 3, 0))
+            f.write(struct.pack("<q", int(self.cache_bytes)))
+            f.write(np.ascontiguousarray(self.params, dtype="<f4").tobytes())
+            for v in (self.mean, self.std, self.lo, self.hi):
+                f.write(np.ascontiguousarray(v, dtype="<f8").tobytes())
+
     def save(self, path):
         np.savez(path, params=self.params, mean=self.mean, std=self.std, lo=self.lo, hi=self.hi,
                  cache_bytes=self.cache_bytes)
@@ -286,7 +303,13 @@ def main(argv=None):
     e = sub.add_parser("evaluate")
     e.add_argument("--data", required=True)
     e.add_argument("--model", required=True)
+    x = sub.add_parser("export")
+    x.add_argument("--model", required=True)
+    x.add_argument("--out", required=True)
     a = ap.parse_args(argv)
+    if a.cmd == "export":
+        LearnedSelector.load(a.model).save_binary(a.out)
+        return
     ctx = Context(0)
     if a.cmd == "collect":
         data = collect(ctx, range(a.first, a.first + a.count), log=lambda m: print(m, file=sys.stderr),

@@ -290,6 +290,96 @@ int gbgpu_mlp_train(gbgpu_ctx* ctx, float* params_inout, const float* X, const f
                     int32_t in_dim, int32_t epochs, int32_t batch, float lr, uint64_t seed, float* loss_out,
                     uint32_t flags);
 
+/* ---- Algorithm 14: deployable selector ("-o 14:_:_:_:<model>:<criterion>:<reuse>") ----
+ * Replaces the full-graph AdaptiveOrder entry
+ * (GenerateAdaptiveMappingFullGraphStandalone,
+ * bench/include/graphbrew/reorder/reorder_adaptive.h:517-715) for the
+ * deployable models:
+ *   gbgpu_parse_selection_policy -> ParseDeployableSelectionPolicy
+ *       (reorder_adaptive.h:166-228; model names from GetSelectionModel /
+ *       GetSelectionCriterion, reorder_types.h:1927-2066), same exception texts
+ *       in err (status GBGPU_E_PARSE); opts are the fields after "14:".
+ *       Models: 0 perceptron (parses; selecting with it returns
+ *       GBGPU_E_UNSUPPORTED: it needs the reference's weight database),
+ *       7 budgeted-rule, 8 allkernel-lowreuse-rule (the frozen rule), and
+ *       9 learned-mlp (aliases mlp, learned): this library's MLP, which like
+ *       the rules needs an explicit reuse count.
+ *   gbgpu_select_arm -> the selection itself: Tier-0 features on the GPU,
+ *       ModeledPropertyBytes (reorder_types.h:1226-1258) of `kernel` against a
+ *       cache (the device's L2 for the rules, the model's cache_bytes for
+ *       learned-mlp), then SelectAllKernelLowReuseRule /
+ *       SelectBudgetedOneUseRule (reorder_adaptive.h:240-385) or the MLP's
+ *       smallest predicted end-to-end time.  The learned model falls back to
+ *       the frozen rule (reason "frozen-rule-fallback") where the features lie
+ *       more than a quarter of their training range outside it, or for a
+ *       kernel it was not trained on.  The chosen arm is out->arm: 12 (the
+ *       recipe in out->applied, run with gbgpu_generate_mapping), 5 (DBG,
+ *       gbgpu_dbg_mapping) or 0 (original order).  kernel GBGPU_KERNEL_GENERIC
+ *       fails like the reference ("Kernel-specific modeled property bytes are
+ *       unavailable").
+ *   gbgpu_selector_model_load reads a model file written by
+ *       graphbrew_gb300.selector (LearnedSelector.save_binary): magic
+ *       "GBSEL01\0", int32 in_dim, hidden (64), outputs (3), reserved, int64
+ *       cache_bytes, float32 params[gbgpu_mlp_param_count(in_dim)], then
+ *       float64 mean, std, lo, hi [in_dim] each. */
+enum {
+    GBGPU_KERNEL_GENERIC = 0,
+    GBGPU_KERNEL_PR = 1,
+    GBGPU_KERNEL_BFS = 2,
+    GBGPU_KERNEL_CC = 3,
+    GBGPU_KERNEL_SSSP = 4,
+    GBGPU_KERNEL_BC = 5,
+    GBGPU_KERNEL_TC = 6,
+    GBGPU_KERNEL_PR_SPMV = 7,
+    GBGPU_KERNEL_CC_SV = 8
+};
+
+typedef struct {
+    int32_t model;          /* 0 perceptron, 7 budgeted-rule, 8 allkernel-lowreuse-rule, 9 learned-mlp */
+    int32_t criterion;      /* 0 fastest-reorder, 1 fastest-execution, 2 best-endtoend, 3 best-amortization */
+    double reuse;           /* reuse count (1.0 unless given) */
+    int32_t reuse_explicit; /* the reuse field was given */
+} gbgpu_selection_policy;
+
+typedef struct {
+    int32_t in_dim;         /* features per row (12) */
+    const float* params;    /* gbgpu_mlp_param_count(in_dim) floats, packed as for gbgpu_mlp_forward */
+    const double* mean;     /* standardisation and training range, in_dim each */
+    const double* std;
+    const double* lo;
+    const double* hi;
+    int64_t cache_bytes;    /* cache the model's working-set ratio feature is taken against */
+} gbgpu_selector_model;
+
+typedef struct {
+    gbgpu_selection_policy policy;
+    int32_t arm;                  /* 12, 5 or 0 */
+    char applied[160];            /* "12:<recipe>", "5" or "0" */
+    char reason[48];              /* allkernel-lowreuse-match / -fallback, budgeted-one-use-match /
+                                     -fallback, learned-mlp, frozen-rule-fallback, empty-graph */
+    double features[9];           /* Tier-0 features (as gbgpu_tier0_features) */
+    int64_t property_bytes;       /* ModeledPropertyBytes of the kernel */
+    int64_t cache_bytes;          /* cache the working-set ratio is taken against */
+    double property_wsr;          /* property_bytes / cache_bytes */
+    float predicted_log10_ms[3];  /* learned-mlp: predicted log10 ms of arms 12, 5, 0 */
+} gbgpu_selection;
+
+int gbgpu_parse_selection_policy(const char* opts, gbgpu_selection_policy* out, char* err, size_t err_len);
+const char* gbgpu_selection_model_name(int32_t model);
+const char* gbgpu_selection_criterion_name(int32_t criterion);
+/* The rule step alone on features the caller already has (model 7 or 8;
+ * features as gbgpu_tier0_features, property_wsr = property bytes / cache
+ * bytes): fills out->arm, applied and reason. */
+int gbgpu_apply_selection_rule(int32_t model, const double* features, double property_wsr, int32_t kernel,
+                               double reuse, gbgpu_selection* out);
+/* ModeledPropertyBytes; -1 for GBGPU_KERNEL_GENERIC (the reference throws). */
+int64_t gbgpu_modeled_property_bytes(int32_t kernel, int64_t nodes, int64_t directed_edges);
+int gbgpu_selector_model_load(const char* path, gbgpu_selector_model** out);
+void gbgpu_selector_model_free(gbgpu_selector_model* model);
+int gbgpu_select_arm(gbgpu_ctx* ctx, const int64_t* row_ptr, const int32_t* col, int64_t n, int64_t nnz,
+                     const char* opts, int32_t kernel, const gbgpu_selector_model* model, gbgpu_selection* out,
+                     uint32_t flags);
+
 /* Library version string. */
 const char* gbgpu_version(void);
 

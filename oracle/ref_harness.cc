@@ -295,4 +295,53 @@ void ref_tier0_features(int64_t n, const int64_t* row_ptr, const int32_t* col, d
     for (int i = 0; i < 9; ++i) out[i] = v[i];
 }
 
+// ParseDeployableSelectionPolicy on the fields after "14:" (split on ':'):
+// model and criterion ordinals, reuse and whether it was given; or the
+// exception text (return 1).
+int ref_parse_selection_policy(const char* opts, int* model, int* criterion, double* reuse, int* explicit_reuse,
+                               char* err, size_t cap) {
+    try {
+        auto p = adaptive::ParseDeployableSelectionPolicy(SplitTokens(opts));
+        *model = (int)p.model;
+        *criterion = (int)p.criterion;
+        *reuse = p.reuse_count;
+        *explicit_reuse = p.reuse_count_explicit ? 1 : 0;
+        return 0;
+    } catch (const std::exception& e) {
+        std::snprintf(err, cap, "%s", e.what());
+        return 1;
+    }
+}
+
+// The two frozen rules on given features (kernel = BenchmarkType ordinal).
+int ref_allkernel_rule(double num_nodes, double avg_degree, double degree_variance, double hub_concentration,
+                       double wsr, int kernel, double reuse) {
+    CommunityFeatures f;
+    f.num_nodes = (size_t)num_nodes;
+    f.avg_degree = avg_degree;
+    f.degree_variance = degree_variance;
+    f.hub_concentration = hub_concentration;
+    f.working_set_ratio = wsr;
+    return adaptive::ShouldUseAllKernelLowReuseRule(f, (BenchmarkType)kernel, reuse) ? 1 : 0;
+}
+
+int ref_budgeted_rule(double num_nodes, double avg_degree, double degree_variance, double hub_concentration,
+                      int kernel, double reuse) {
+    CommunityFeatures f;
+    f.num_nodes = (size_t)num_nodes;
+    f.avg_degree = avg_degree;
+    f.degree_variance = degree_variance;
+    f.hub_concentration = hub_concentration;
+    return adaptive::ShouldUseBudgetedLeidenGorder(f, (BenchmarkType)kernel, reuse) ? 1 : 0;
+}
+
+// ModeledPropertyBytes; -1 when the reference throws (generic kernel).
+long long ref_property_bytes(int kernel, unsigned long long nodes, unsigned long long edges) {
+    try {
+        return (long long)ModeledPropertyBytes((BenchmarkType)kernel, nodes, edges);
+    } catch (const std::exception&) {
+        return -1;
+    }
+}
+
 }  // extern "C"
