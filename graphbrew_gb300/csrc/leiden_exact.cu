@@ -52,7 +52,7 @@ constexpr int kCoarseBits = 9;                // event grouping: 512 coarse buck
 constexpr int kCoarse = 1 << kCoarseBits;
 constexpr int kFineBits = kSlotBits - kCoarseBits;
 constexpr int kTbThreads = 1024;              // table insert / group: one window vertex per thread
-constexpr int kTbMinChunk = 512;            // smallest insert chunk (persistent CTAs)
+constexpr int kTbMinChunk = 512;            // smallest insert chunk (CTA size) the table kernels accept
 constexpr int kTbChunks = kWindowMax / kTbMinChunk;   // stride of the per-chunk histograms
 constexpr int kTbFinishThreads = 1024;        // table finish: one CTA per coarse bucket
 constexpr uint32_t kPadSlot = 0xFFFFFFFFu;
@@ -66,6 +66,15 @@ constexpr int kBucketV = 16;                  // window vertices per time bucket
 constexpr int kHotStride = kWindowMax / kBucketV + 1;
 constexpr int kHotMax = 2 * kEventsMax / kHotMin;
 constexpr int kEndBits = 18;                  // SlotMeta.endh: end | (hot id + 1) << kEndBits
+// Designated communities: the few communities with the most events (on RMAT
+// the one most vertices join) leave the sorted table.  Each gets a dense row
+// over the window (the signed degree of every window offset's move into or
+// out of it) and the prefix of its 16-offset bucket sums, so a lookup is one
+// prefix load plus one 64-byte read, and no bucket of the sorted table holds
+// a giant community.  Chosen each round from the previous table's counts.
+constexpr int kZMax = 8;                      // designated communities at most
+constexpr int kZKeep = 64;                    // events a designated community needs to stay / be chosen
+constexpr int kZCand = 128;                   // hot slots of the sorted table considered
 static_assert(kEventsMax < (1 << kEndBits), "event positions fit the end field");
 constexpr int kHubThreads2 = 256;             // threads of the hub kernels
 constexpr int kBigMaxDeg = 2048;              // rows above kWarpMaxDeg up to this: one CTA each
@@ -93,6 +102,9 @@ struct Ctl {
     unsigned long long tag;   // generation of the event table (slots of older tags are empty)
     unsigned int nhot;        // hot slots of the current table
     unsigned long long tb_big; // largest coarse bucket: size << 32 | bucket (its CTA starts first)
+    unsigned int nz;                 // designated communities of the current table
+    unsigned int zc[kZMax];          // their ids
+    unsigned int zcount[kZMax];      // events each received in the current table
 };
 
 struct __align__(16) SlotMeta {
@@ -132,6 +144,11 @@ struct ExactState {
     unsigned long long* ev1;  // events grouped by coarse bucket: slot << 32 | event index
     unsigned long long* ev2;  // events sorted by slot
     int32_t* hot_bidx;        // kHotMax x kHotStride time-bucket starts of hot slots
+    uint8_t* zof;             // per community: designated index + 1, 0 = in the sorted table
+    int32_t* zcontrib;        // [2 parities][kZMax][kWindowMax] signed degree per window offset
+    long long* zbsum;         // [2][kZMax][kHotStride] 16-offset bucket sums
+    long long* zpre;          // [2][kZMax][kHotStride] exclusive prefix of the bucket sums
+    unsigned long long* zcand;  // hot slots of the sorted table: events << 32 | community
     // hubs
     const uint32_t* hub_v;        // hub vertex ids (ascending)
     const int64_t* hub_toff;      // table offset
@@ -171,17 +188,21 @@ __device__ __forceinline__ uint32_t slot_hash(uint32_t c) {
 // speculative events of c before u -- a 16-byte probe per hash step, then a
 // binary search over the slot's time-sorted events.  The K probe chains and
 // searches advance in lockstep so their loads are in flight together.
+// Designated communities read their dense row instead (their probe, issued
+// alongside, finds no slot: they are not in the table).
 // valid[k] = false entries return 0.
 template <int K>
-__device__ __forceinline__ void sigma_at_k(const ExactState& a, unsigned long long tag, long long P,
+__device__ __forceinline__ void sigma_at_k(const ExactState& a, unsigned long long tag, long long P, int par,
                                            const uint32_t (&c)[K], const bool (&valid)[K], uint32_t u,
                                            long long (&out)[K]) {
     uint32_t h[K], hot[K];
     int lo[K], l[K], r[K];
     bool pending[K];
+    uint32_t zd[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         out[k] = valid[k] ? (long long)a.ctot[c[k]] : 0;
+        zd[k] = valid[k] ? a.zof[c[k]] : 0u;
         h[k] = slot_hash(c[k]) & (kTableSlots - 1);
         pending[k] = valid[k];
         lo[k] = l[k] = r[k] = 0;
@@ -250,11 +271,30 @@ __device__ __forceinline__ void sigma_at_k(const ExactState& a, unsigned long lo
 #pragma unroll
     for (int k = 0; k < K; ++k)
         if (l[k] > lo[k]) out[k] += a.epre[l[k] - 1];
+    // Designated communities: bucket prefix + the bucket's offsets before u.
+    const int off = (int)((long long)u - P), bk = off >> 4, rem = off & 15;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        if (!zd[k]) continue;
+        const size_t row = (size_t)(par * kZMax + (int)zd[k] - 1);
+        const int4* q = reinterpret_cast<const int4*>(a.zcontrib + row * kWindowMax + ((size_t)bk << 4));
+        long long sum = a.zpre[row * kHotStride + bk];
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            const int4 v = q[m];
+            if (4 * m + 0 < rem) sum += v.x;
+            if (4 * m + 1 < rem) sum += v.y;
+            if (4 * m + 2 < rem) sum += v.z;
+            if (4 * m + 3 < rem) sum += v.w;
+        }
+        out[k] += sum;
+    }
 }
 
 struct Round {
     long long P, E;
     unsigned long long tag;
+    int par;              // parity of the round (decision buffers and dense rows)
     const uint32_t* pbest;
     const uint8_t* pact;
     uint32_t* nbest;
@@ -268,6 +308,7 @@ __device__ __forceinline__ Round round_view(const ExactState& a, const Ctl* c) {
     r.E = c->E;
     r.tag = c->tag;
     const int par = (int)(c->round & 1);
+    r.par = par;
     r.pbest = a.best[par];
     r.pact = a.act[par];
     r.nbest = a.best[par ^ 1];
@@ -424,23 +465,48 @@ __device__ __forceinline__ void tb_insert_chunk(const ExactState& a, const Ctl* 
     __syncthreads();
     const int W = (int)(E - P);
     const int i = chunk * blockDim.x + tid;
+    const int nz = (int)c->nz;
+    uint32_t z0 = 0, z1 = 0;   // designated index + 1 of the departure / arrival community
+    int dg = 0;
     if (i < W) {
         const int64_t wv = P + i;
         const uint8_t pa = r.pact[wv];
         const uint32_t pb = r.pbest[wv], vc = a.vcom[wv];
         const int64_t r0 = a.rp[wv], r1 = a.rp[wv + 1];
         uint32_t s0 = kPadSlot, s1 = kPadSlot;
-        int dg = 0;
         if (pa == 1 && pb != vc) {
             dg = (int)(r1 - r0);
-            s0 = table_insert(a.slots, r.tag, vc);
-            s1 = table_insert(a.slots, r.tag, pb);
-            atomicAdd(&hist[s0 >> kFineBits], 1);
-            atomicAdd(&hist[s1 >> kFineBits], 1);
+            if (nz) {
+                z0 = a.zof[vc];
+                z1 = a.zof[pb];
+            }
+            if (!z0) {
+                s0 = table_insert(a.slots, r.tag, vc);
+                atomicAdd(&hist[s0 >> kFineBits], 1);
+            }
+            if (!z1) {
+                s1 = table_insert(a.slots, r.tag, pb);
+                atomicAdd(&hist[s1 >> kFineBits], 1);
+            }
         }
         a.tb_s0[i] = s0;
         a.tb_s1[i] = s1;
         a.wdeg[i] = dg;
+    }
+    // Dense rows: every window offset writes its signed degree for each
+    // designated community (zero when it does not move into or out of it), and
+    // each 16-offset bucket (a half-warp) its sum; warp-aggregated event counts.
+    for (int j = 0; j < nz; ++j) {
+        const int v = (z1 == (uint32_t)j + 1 ? dg : 0) - (z0 == (uint32_t)j + 1 ? dg : 0);
+        const size_t row = (size_t)(r.par * kZMax + j);
+        if (i < W) a.zcontrib[row * kWindowMax + i] = v;
+        long long sum = v;
+#pragma unroll
+        for (int o = 8; o > 0; o >>= 1) sum += __shfl_xor_sync(0xFFFFFFFFu, sum, o);
+        if ((i & 15) == 0 && i < W) a.zbsum[row * kHotStride + (i >> 4)] = sum;
+        const int evs = __popc(__ballot_sync(0xFFFFFFFFu, z0 == (uint32_t)j + 1)) +
+                        __popc(__ballot_sync(0xFFFFFFFFu, z1 == (uint32_t)j + 1));
+        if ((tid & 31) == 0 && evs) atomicAdd(&a.ctl->zcount[j], (unsigned)evs);
     }
     __syncthreads();
     for (int b = tid; b < kCoarse; b += blockDim.x) a.tb_hist[b * kTbChunks + chunk] = hist[b];
@@ -570,6 +636,44 @@ __device__ __forceinline__ void tb_finish_bucket(const ExactState& a, const Ctl*
     __shared__ long long warp_v[32];
     __shared__ int warp_h[32];
     const long long P = c->P;
+    if (vb >= kCoarse) {
+        // Designated community j = vb - kCoarse: exclusive prefix of its
+        // bucket sums (one extra entry holds the total).
+        const int j = vb - kCoarse;
+        if (j >= (int)c->nz) return;
+        const int nbk = (int)((c->E - P + kBucketV - 1) / kBucketV);
+        const size_t row = ((size_t)(c->round & 1) * kZMax + j) * kHotStride;
+        const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, nwarps = blockDim.x >> 5;
+        const int per = (nbk + blockDim.x - 1) / blockDim.x;
+        const int b0 = min(nbk, tid * per), b1 = min(nbk, b0 + per);
+        long long own = 0;
+        for (int b = b0; b < b1; ++b) own += a.zbsum[row + b];
+        long long inc = own;
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long y = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        if (lane == 31) warp_v[w] = inc;
+        __syncthreads();
+        if (w == 0) {
+            const long long x = lane < nwarps ? warp_v[lane] : 0;
+            long long xi = x;
+            for (int o = 1; o < 32; o <<= 1) {
+                const long long y = __shfl_up_sync(0xFFFFFFFFu, xi, o);
+                if (lane >= o) xi += y;
+            }
+            if (lane < nwarps) warp_v[lane] = xi - x;
+        }
+        __syncthreads();
+        long long run = warp_v[w] + inc - own;
+        for (int b = b0; b < b1; ++b) {
+            a.zpre[row + b] = run;
+            run += a.zbsum[row + b];
+        }
+        if (tid == (int)blockDim.x - 1) a.zpre[row + nbk] = run;
+        __syncthreads();
+        return;
+    }
     // The largest bucket (the one holding a community many window vertices
     // join) goes first (CTA 0 / virtual bucket 0).
     const int big = (int)(a.ctl->tb_big & 0xFFFFFFFFull);
@@ -719,6 +823,8 @@ __device__ __forceinline__ void tb_finish_bucket(const ExactState& a, const Ctl*
                     if (runc >= kHotMin) {
                         const unsigned id = atomicAdd(&a.ctl->nhot, 1u);
                         if (id < (unsigned)kHotMax) endh |= (id + 1) << kEndBits;
+                        if (id < (unsigned)kZCand)
+                            a.zcand[id] = (unsigned long long)runc << 32 | (uint32_t)a.slots[sl].tkey;
                     }
                     a.slots[sl].endh = endh;
                 }
@@ -758,6 +864,7 @@ __device__ __forceinline__ void tb_finish_bucket(const ExactState& a, const Ctl*
     __syncthreads();   // shared arrays are reused by the CTA's next bucket
 }
 
+// Grid: kCoarse buckets + kZMax designated-community prefixes.
 __global__ void __launch_bounds__(kTbFinishThreads) k_tb_finish(ExactState a) {
     if (a.ctl->P >= a.ctl->n) return;
     tb_finish_bucket(a, a.ctl, blockIdx.x);
@@ -800,7 +907,7 @@ __device__ __forceinline__ void eval_vertex(const ExactState& a, const Round& r,
                 const uint32_t cc[1] = {d};
                 const bool vv[1] = {true};
                 long long o[1];
-                sigma_at_k<1>(a, r.tag, r.P, cc, vv, (uint32_t)u, o);
+                sigma_at_k<1>(a, r.tag, r.P, r.par, cc, vv, (uint32_t)u, o);
                 sg1 = o[0];
             }
             sg1 = __shfl_sync(0xFFFFFFFFu, sg1, 0);
@@ -820,7 +927,7 @@ __device__ __forceinline__ void eval_vertex(const ExactState& a, const Round& r,
             const uint32_t cc[2] = {c, d};
             const bool vv[2] = {true, true};
             long long sg[2];
-            sigma_at_k<2>(a, r.tag, r.P, cc, vv, (uint32_t)u, sg);
+            sigma_at_k<2>(a, r.tag, r.P, r.par, cc, vv, (uint32_t)u, sg);
             const double dl = delta_q((double)__popc(peers), kud, ku, (double)sg[0], (double)sg[1], a.M, a.R);
             if (dl > 0.0) { best_d = dl; best_c = c; }
         }
@@ -882,7 +989,7 @@ __device__ __forceinline__ void eval_vertex(const ExactState& a, const Round& r,
             }
             cc[4] = d;
             vv[4] = i0 == 0;
-            sigma_at_k<5>(a, r.tag, r.P, cc, vv, (uint32_t)u, sg);
+            sigma_at_k<5>(a, r.tag, r.P, r.par, cc, vv, (uint32_t)u, sg);
             if (i0 == 0) sd = (double)sg[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
@@ -955,7 +1062,7 @@ __device__ __forceinline__ void eval_small_body(const ExactState& a, const Ctl* 
                 const uint32_t cc[1] = {d};
                 const bool vv[1] = {true};
                 long long o[1];
-                sigma_at_k<1>(a, r.tag, r.P, cc, vv, (uint32_t)u, o);
+                sigma_at_k<1>(a, r.tag, r.P, r.par, cc, vv, (uint32_t)u, o);
                 sg1 = o[0];
             }
             sg1 = __shfl_sync(0xFFFFFFFFu, sg1, lane & ~7);
@@ -972,7 +1079,7 @@ __device__ __forceinline__ void eval_small_body(const ExactState& a, const Ctl* 
             const uint32_t cc[2] = {c, d};
             const bool vv[2] = {true, true};
             long long sg[2];
-            sigma_at_k<2>(a, r.tag, r.P, cc, vv, (uint32_t)u, sg);
+            sigma_at_k<2>(a, r.tag, r.P, r.par, cc, vv, (uint32_t)u, sg);
             const double dl = delta_q((double)__popc(peers), (double)__popc(eqd), (double)deg, (double)sg[0],
                                       (double)sg[1], a.M, a.R);
             if (dl > 0.0) { best_d = dl; best_c = c; }
@@ -1095,7 +1202,7 @@ __device__ __forceinline__ void eval_big_body(const ExactState& a, const Ctl* c)
             }
             cc[4] = d;
             vv[4] = i0 == 0;
-            sigma_at_k<5>(a, r.tag, r.P, cc, vv, u, sg);
+            sigma_at_k<5>(a, r.tag, r.P, r.par, cc, vv, u, sg);
             if (i0 == 0) sd = (double)sg[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
@@ -1264,7 +1371,7 @@ __device__ __forceinline__ void hub_select_body(const ExactState& a, const Ctl* 
             }
             cc[4] = d;
             vv[4] = true;
-            sigma_at_k<5>(a, r.tag, r.P, cc, vv, h, sgm);
+            sigma_at_k<5>(a, r.tag, r.P, r.par, cc, vv, h, sgm);
             const double sd = (double)sgm[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
@@ -1313,7 +1420,7 @@ __device__ __forceinline__ void hub_select_body(const ExactState& a, const Ctl* 
                     const uint32_t cc[1] = {d};
                     const bool vv[1] = {true};
                     long long o[1];
-                    sigma_at_k<1>(a, r.tag, r.P, cc, vv, h, o);
+                    sigma_at_k<1>(a, r.tag, r.P, r.par, cc, vv, h, o);
                     stays = refine_stays(a, (double)o[0], ku);
                 }
                 if (!act) record(a, r, h, 0, d, 0.0);
@@ -1467,14 +1574,83 @@ __device__ __forceinline__ void commit_hub_body(const ExactState& a, const Ctl* 
 
 __global__ void __launch_bounds__(kHubThreads2) k_ex_commit_hub(ExactState a) { commit_hub_body(a, a.ctl); }
 
+// Re-choose the designated communities of the next table from the counts of
+// the table just used: the designated ones' event counts and the sorted
+// table's hot slots, largest first, at least kZKeep events each.  Keeps the
+// set when nothing in the sorted table was hot and every member kept its
+// events.  Called by every thread of one CTA.
+__device__ __forceinline__ void designate(const ExactState& a, Ctl* c) {
+    __shared__ unsigned long long cand[kZMax + kZCand];
+    __shared__ int s_change;
+    const int tid = threadIdx.x;
+    const int nz = (int)c->nz;
+    const int nh = min((int)a.ctl->nhot, kZCand);
+    if (tid == 0) {
+        int change = nh > 0;
+        for (int j = 0; j < nz; ++j) change |= c->zcount[j] < (unsigned)kZKeep;
+        s_change = change;
+    }
+    __syncthreads();
+    if (!s_change) {
+        if (tid < kZMax) c->zcount[tid] = 0;
+        __syncthreads();
+        return;
+    }
+    if (tid < nz) cand[tid] = (unsigned long long)c->zcount[tid] << 32 | c->zc[tid];
+    if (tid < nh) cand[nz + tid] = a.zcand[tid];
+    __syncthreads();
+    if (tid < 32) {
+        const int total = nz + nh;
+        uint32_t chosen[kZMax];
+        int nc = 0;
+#pragma unroll 1
+        for (int pick = 0; pick < kZMax; ++pick) {
+            unsigned long long best = 0;
+            int bi = -1;
+            for (int t = tid; t < total; t += 32) {
+                const unsigned long long v = cand[t];
+                if ((v >> 32) >= (unsigned long long)kZKeep && v > best) {
+                    best = v;
+                    bi = t;
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const unsigned long long ob = __shfl_xor_sync(0xFFFFFFFFu, best, o);
+                const int oi = __shfl_xor_sync(0xFFFFFFFFu, bi, o);
+                if (ob > best) {
+                    best = ob;
+                    bi = oi;
+                }
+            }
+            if (best == 0) break;
+            if (tid == 0) {
+                chosen[nc] = (uint32_t)best;
+                cand[bi] = 0;
+            }
+            ++nc;
+            __syncwarp();
+        }
+        if (tid == 0) {
+            for (int j = 0; j < nz; ++j) a.zof[c->zc[j]] = 0;
+            for (int j = 0; j < nc; ++j) {
+                a.zof[chosen[j]] = (uint8_t)(j + 1);
+                c->zc[j] = chosen[j];
+            }
+            c->nz = (unsigned)nc;
+            for (int j = 0; j < kZMax; ++j) c->zcount[j] = 0;
+        }
+    }
+    __syncthreads();
+}
+
 // After the window's decisions: fix the committed prefix [P, x] for the commit
 // kernels, slide the window (the new decisions become D_prev; entering
 // vertices are unknown) and tell the graph's loop whether to go on.  The next
 // window's event table and this window's commits then run concurrently: they
 // touch disjoint vertices.  `c` is the control block this CTA works on; the
-// entering vertices' marks are written by threads (tid0, tid0 + tstride, ...),
-// one CTA in the graph, every CTA in the persistent kernel.  Ends with a CTA
-// barrier, so every thread sees the updated block.
+// entering vertices' marks are written by threads (tid0, tid0 + tstride, ...).
+// Ends with a CTA barrier, so every thread sees the updated block.
 __device__ __forceinline__ void advance_ctl(const ExactState& a, Ctl* c, long long tid0, long long tstride,
                                             bool set_cond) {
     const long long P = c->P, E = c->E, n = c->n, B = c->B;
@@ -1503,6 +1679,7 @@ __device__ __forceinline__ void advance_ctl(const ExactState& a, Ctl* c, long lo
     }
     __syncthreads();
     window_ranges(a, c, nP, nE);
+    designate(a, c);
     if (threadIdx.x == 0) {
         const long long rnd = c->round + 1;
         c->cP = P;
@@ -1544,154 +1721,13 @@ __device__ __forceinline__ void init_ctl(const ExactState& a, Ctl* c, long long 
         c->cP = 1;
         c->cX = 0;
         c->tag = c->tag + 1;
+        for (int j = 0; j < kZMax; ++j) c->zcount[j] = 0;
     }
     __syncthreads();
 }
 
 __global__ void __launch_bounds__(1024) k_ex_init_iter(ExactState a) {
     init_ctl(a, a.ctl, threadIdx.x, blockDim.x);
-}
-
-// ---------------------------------------------------------------------------
-// Persistent engine: one iteration of local moving in one cooperative launch,
-// one CTA per SM.  Every CTA keeps an identical copy of the control block in
-// shared memory and runs the advance itself, so rounds need no host or graph
-// step; the phases of a round are separated by grid barriers:
-//   decide (hub selection, big / mid / small rows)
-//   | advance + next window's table insert + commit of [cP, cX]
-//   | table grouping + affected flags + next window's hub accumulation
-//   | table finish |
-// which is the dependency order of the graph round above, linearised.
-// ---------------------------------------------------------------------------
-constexpr int kPT = 512;                          // threads per persistent CTA
-constexpr long long kBarrierSpins = 1ll << 22;    // polls before a grid barrier gives up (seconds)
-
-struct GridBarrier {
-    unsigned int count;   // CTAs arrived in the current generation
-    unsigned int gen;     // generation, bumped by the last arrival
-};
-
-// All CTAs of the grid meet here (release / acquire at GPU scope, as a
-// cooperative grid sync does).  The wait is bounded: false means the barrier
-// gave up, after which the caller stops.
-__device__ __forceinline__ bool grid_barrier(GridBarrier* gbar, unsigned int nblocks) {
-    __shared__ int s_ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned int g, old, cur;
-        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(g) : "l"(&gbar->gen) : "memory");
-        asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(&gbar->count) : "memory");
-        int ok = 1;
-        if (old == nblocks - 1) {
-            asm volatile("st.relaxed.gpu.global.u32 [%0], 0;" ::"l"(&gbar->count) : "memory");
-            asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(&gbar->gen) : "memory");
-        } else {
-            long long spins = 0;
-            while (true) {
-                asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(&gbar->gen) : "memory");
-                if (cur != g) break;
-                if (++spins > kBarrierSpins) {
-                    ok = 0;
-                    break;
-                }
-            }
-        }
-        s_ok = ok;
-    }
-    __syncthreads();
-    return s_ok != 0;
-}
-
-// The persistent kernel calls each phase through its own (not inlined)
-// function, so that registers are allocated per phase rather than across the
-// whole round.
-__device__ __noinline__ void p_tb_insert(const ExactState& a, const Ctl* c, int ch) { tb_insert_chunk(a, c, ch); }
-__device__ __noinline__ void p_tb_group(const ExactState& a, const Ctl* c, int ch, int chunks) {
-    tb_group_chunk(a, c, ch, chunks);
-}
-__device__ __noinline__ void p_tb_finish(const ExactState& a, const Ctl* c, int vb) { tb_finish_bucket(a, c, vb); }
-__device__ __noinline__ void p_eval_small(const ExactState& a, const Ctl* c) { eval_small_body(a, c); }
-__device__ __noinline__ void p_eval_mid(const ExactState& a, const Ctl* c) { eval_mid_body(a, c); }
-__device__ __noinline__ void p_eval_big(const ExactState& a, const Ctl* c) { eval_big_body(a, c); }
-__device__ __noinline__ void p_hub_select(const ExactState& a, const Ctl* c) { hub_select_body(a, c); }
-__device__ __noinline__ void p_hub_accum(const ExactState& a, const Ctl* c) { hub_accum_body(a, c); }
-__device__ __noinline__ void p_commit_a(const ExactState& a, const Ctl* c) { commit_a_body(a, c); }
-__device__ __noinline__ void p_commit_b(const ExactState& a, const Ctl* c) { commit_b_body(a, c); }
-__device__ __noinline__ void p_commit_hub(const ExactState& a, const Ctl* c) { commit_hub_body(a, c); }
-
-__global__ void __launch_bounds__(kPT, 1) k_ex_persistent(ExactState a, GridBarrier* gbar) {
-    __shared__ Ctl sc;
-    const unsigned int nb = gridDim.x;
-    const long long gtid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    const long long gstride = (long long)gridDim.x * blockDim.x;
-    const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
-    if (threadIdx.x == 0) sc = *a.ctl;   // n, B, max_rounds and the table generation
-    __syncthreads();
-    init_ctl(a, &sc, gtid, gstride);
-    int chunks = (int)((sc.E - sc.P + blockDim.x - 1) / blockDim.x);
-    // The first window's table and hub accumulation.
-    bool ok = grid_barrier(gbar, nb);
-    if (ok) {
-        if (lead) {
-            a.ctl->first_change = kNoChange;
-            a.ctl->nhot = 0;
-            a.ctl->tb_big = 0;
-        }
-        for (int ch = blockIdx.x; ch < chunks; ch += nb) p_tb_insert(a, &sc, ch);
-        p_hub_accum(a, &sc);
-        ok = grid_barrier(gbar, nb);
-    }
-    if (ok) {
-        for (int ch = blockIdx.x; ch < chunks; ch += nb) p_tb_group(a, &sc, ch, chunks);
-        ok = grid_barrier(gbar, nb);
-    }
-    if (ok) {
-        for (int vb = blockIdx.x; vb < kCoarse; vb += nb) p_tb_finish(a, &sc, vb);
-        ok = grid_barrier(gbar, nb);
-    }
-    while (ok && sc.P < sc.n) {
-        // Decide the window.
-        p_hub_select(a, &sc);
-        p_eval_big(a, &sc);
-        __syncthreads();   // the big rows' shared tables are the mid rows' next
-        p_eval_mid(a, &sc);
-        p_eval_small(a, &sc);
-        if (!(ok = grid_barrier(gbar, nb))) break;
-        // Advance (each CTA on its copy), next window's table insert, commit.
-        advance_ctl(a, &sc, gtid, gstride, false);
-        const bool more = sc.P < sc.n;
-        chunks = (int)((sc.E - sc.P + blockDim.x - 1) / blockDim.x);
-        if (lead) {
-            a.ctl->nhot = 0;
-            a.ctl->tb_big = 0;
-        }
-        if (more)
-            for (int ch = blockIdx.x; ch < chunks; ch += nb) p_tb_insert(a, &sc, ch);
-        p_commit_a(a, &sc);
-        if (!(ok = grid_barrier(gbar, nb))) break;
-        // Every CTA has read first_change (advance): reset it for the next decisions.
-        if (lead) a.ctl->first_change = kNoChange;
-        if (more)
-            for (int ch = blockIdx.x; ch < chunks; ch += nb) p_tb_group(a, &sc, ch, chunks);
-        p_commit_b(a, &sc);
-        p_commit_hub(a, &sc);
-        if (more) p_hub_accum(a, &sc);
-        if (!(ok = grid_barrier(gbar, nb))) break;
-        if (!more) break;
-        for (int vb = blockIdx.x; vb < kCoarse; vb += nb) p_tb_finish(a, &sc, vb);
-        if (!(ok = grid_barrier(gbar, nb))) break;
-    }
-    if (!ok && threadIdx.x == 0) atomicExch(reinterpret_cast<unsigned long long*>(&a.ctl->error), 3ull);
-    if (lead && ok) {
-        a.ctl->P = sc.P;
-        a.ctl->E = sc.E;
-        a.ctl->round = sc.round;
-        a.ctl->evals = sc.evals;
-        a.ctl->cP = sc.cP;
-        a.ctl->cX = sc.cX;
-        a.ctl->tag = sc.tag;
-        if (sc.error && a.ctl->error == 0) a.ctl->error = sc.error;
-    }
 }
 
 // Deterministic tree sum of the iteration's committed deltas (and count).
@@ -1858,6 +1894,11 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     DevBuf<int32_t> wdeg(kWindowMax, s), tb_hist(kCoarse * kTbChunks, s), tb_bstart(kCoarse + 1, s);
     DevBuf<unsigned long long> ev1(kEventsMax, s), ev2(kEventsMax, s);
     DevBuf<int32_t> hot_bidx((size_t)kHotMax * kHotStride, s);
+    DevBuf<uint8_t> zof(n > 0 ? n : 1, s);
+    GB_CUDA(cudaMemsetAsync(zof, 0, (n > 0 ? n : 1), s));
+    DevBuf<int32_t> zcontrib((size_t)2 * kZMax * kWindowMax, s);
+    DevBuf<long long> zbsum((size_t)2 * kZMax * kHotStride, s), zpre((size_t)2 * kZMax * kHotStride, s);
+    DevBuf<unsigned long long> zcand(kZCand, s);
     DevBuf<Ctl> ctl(1, s);
     Ctl* hctl = nullptr;
     GB_CUDA(cudaMallocHost(&hctl, sizeof(Ctl)));
@@ -1894,6 +1935,11 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     a.ev1 = ev1.get();
     a.ev2 = ev2.get();
     a.hot_bidx = hot_bidx.get();
+    a.zof = zof.get();
+    a.zcontrib = zcontrib.get();
+    a.zbsum = zbsum.get();
+    a.zpre = zpre.get();
+    a.zcand = zcand.get();
     a.stime = stime.get();
     a.epre = epre.get();
     a.hub_v = d_hub_v.get();
@@ -1933,7 +1979,7 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     auto enqueue_table = [&](cudaStream_t st) {
         k_tb_insert<<<tb_grid, kTbThreads, 0, st>>>(a);
         k_tb_group<<<tb_grid, kTbThreads, group_smem, st>>>(a);
-        k_tb_finish<<<kCoarse, kTbFinishThreads, finish_smem, st>>>(a);
+        k_tb_finish<<<kCoarse + kZMax, kTbFinishThreads, finish_smem, st>>>(a);
     };
     const int mid_smem = kMidWarpsPerBlock * 2 * kWarpHash * (int)sizeof(uint32_t);
     GB_CUDA(cudaFuncSetAttribute(k_ex_eval_mid, cudaFuncAttributeMaxDynamicSharedMemorySize, mid_smem));
@@ -2032,33 +2078,8 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     // One local-moving iteration as one graph: the init kernel, then a
     // device-side while loop over rounds whose condition the advance kernel
     // sets.  GBGPU_EXACT_GRAPH=0 enqueues rounds from the host instead.
-    // Default: the persistent cooperative kernel (one launch per iteration).
-    // GBGPU_EXACT_PERSISTENT=0 runs the rounds as a CUDA graph per iteration
-    // (GBGPU_EXACT_GRAPH=0: enqueued from the host) with the same kernels'
-    // bodies; all three give the same result.
-    const char* penv = std::getenv("GBGPU_EXACT_PERSISTENT");
-    bool persistent = !(penv && penv[0] == '0');
-    int p_grid = 0;
-    const int p_smem = std::max(std::max((kPT / 32) * 2 * kWarpHash, 2 * kBigSlots + 2 * kBigMaxDeg),
-                                std::max((kPT / 32) * kCoarse, (kPT / 32) * ((1 << kFineBits) + 1))) *
-                       (int)sizeof(uint32_t);
-    if (persistent) {
-        int dev = 0, coop = 0, sms = kNumSMs, per_sm = 0;
-        GB_CUDA(cudaGetDevice(&dev));
-        GB_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
-        GB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        GB_CUDA(cudaFuncSetAttribute(k_ex_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, p_smem));
-        GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ex_persistent, kPT, p_smem));
-        // One CTA per SM: the grid is co-resident by construction (checked by
-        // the cooperative launch), so the grid barriers cannot wait on a CTA
-        // that never starts.
-        if (coop && per_sm >= 1) p_grid = sms;
-        else persistent = false;
-    }
-    DevBuf<GridBarrier> gbar(1, s);
-    GB_CUDA(cudaMemsetAsync(gbar, 0, sizeof(GridBarrier), s));
     const char* genv = std::getenv("GBGPU_EXACT_GRAPH");
-    const bool use_graph = !persistent && !(genv && genv[0] == '0');
+    const bool use_graph = !(genv && genv[0] == '0');
     struct GraphGuard {
         cudaGraph_t g = nullptr;
         cudaGraphExec_t e = nullptr;
@@ -2117,15 +2138,7 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     int iterations = 0;
     int64_t rounds = 0, nl = 0, evals = 0;
     for (int it = 0; it < max_iterations; ++it) {
-        if (persistent) {
-            a.use_cond = 0;
-            GridBarrier* bar = gbar.get();
-            void* args[] = {(void*)&a, (void*)&bar};
-            GB_CUDA(cudaLaunchCooperativeKernel((const void*)k_ex_persistent, dim3(p_grid), dim3(kPT), args,
-                                                (size_t)p_smem, s));
-            GB_CUDA(cudaMemcpyAsync(hctl, ctl.get(), sizeof(Ctl), cudaMemcpyDeviceToHost, s));
-            GB_CUDA(cudaStreamSynchronize(s));
-        } else if (use_graph) {
+        if (use_graph) {
             GB_CUDA(cudaGraphLaunch(gg.e, s));
             GB_CUDA(cudaMemcpyAsync(hctl, ctl.get(), sizeof(Ctl), cudaMemcpyDeviceToHost, s));
             GB_CUDA(cudaStreamSynchronize(s));
@@ -2139,13 +2152,11 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
                 if (hctl->P >= n) break;
             }
         }
-        if (hctl->error == 3)
-            throw Error(GBGPU_E_TIMEOUT, "serial-order local moving: a grid barrier of the persistent kernel timed out");
         if (hctl->error == 2)
             throw Error(GBGPU_E_CUDA, "serial-order local moving: event table slot with an invalid hot index");
         if (hctl->error)
             throw Error(GBGPU_E_CUDA, "serial-order local moving: round loop stopped without progress");
-        nl += persistent ? 1 : 4 + (nh ? 1 : 0) + hctl->round * per_round;
+        nl += 4 + (nh ? 1 : 0) + hctl->round * per_round;
         rounds += hctl->round;
         evals += hctl->evals;
         ++iterations;
