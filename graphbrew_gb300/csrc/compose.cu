@@ -130,6 +130,7 @@ struct ClassCounts {
 
 constexpr int kThreadGorderMax = 32;
 constexpr int kSmemGorderMax = 4096;
+constexpr int kMaxGorderWindow = 100;   // the thread variant's bound (kMaxB) too
 
 __global__ void k_classify(const int64_t* __restrict__ ssize, int64_t C, int intra, int fallback,
                            int32_t* __restrict__ lists, ClassCounts* __restrict__ cc) {
@@ -353,42 +354,242 @@ __global__ void k_gorder_thread(const int32_t* __restrict__ list, const int32_t*
     }
 }
 
-// One warp per community; heap in shared memory (lane 0 runs it, the warp
-// stages degrees).  Global variant for communities too large for shared memory.
+// ---------------------------------------------------------------------------
+// The same UnitHeap, held so that a warp can apply a placed vertex's bumps
+// together.  Each bucket is a stack in a push log: a bump pushes the vertex
+// onto its new bucket's stack; an entry is live while it is its vertex's
+// latest push and the vertex is unplaced; a bucket's front (extract-max,
+// bucket-front insertion) is its newest live entry.  That is the linked
+// list's order exactly: a bucket lists the vertices moved into it, newest
+// first, then -- bucket 0 only -- the untouched vertices in local order (the
+// initial pushes, vertex 0 last).  A batch of bumps by one placed vertex
+// touches distinct vertices, so it is applied a warp at a time, pushes
+// ordered as the reference processes the adjacency: entries are allocated in
+// that order and each links to the previous push onto the same bucket (a
+// __match_any_sync group).  Stale entries are skipped when a front is taken;
+// when the log is full, a compaction keeps each live vertex's latest entry in
+// push order and relinks the stacks.
+// ---------------------------------------------------------------------------
+struct LazyHeap {
+    int* key;        // [S] bucket of each local vertex, -1 once placed
+    int* lastpush;   // [S] log entry of its latest push
+    int* log_v;      // [L] pushed vertex
+    int* log_next;   // [L] entry below it in the same bucket (-1: bottom)
+    int* top;        // [nb] newest entry of each bucket (-1: empty)
+    int* last;       // [nb] compaction scratch
+    int* ring;       // [window + 1] the last placed vertices
+    uint32_t* degs;  // [S] degrees (seed choice)
+    int L;
+};
+
+__host__ __device__ constexpr int lazy_log_cap(int S) { return 2 * S + 64; }
+__host__ __device__ constexpr int64_t lazy_ws_ints(int64_t S, int nb, int window) {
+    return 3 * S + 2 * (int64_t)lazy_log_cap((int)S) + 2 * nb + window + 1;
+}
+
+__device__ __forceinline__ LazyHeap lazy_view(int* ws, int64_t S, int nb, int window) {
+    LazyHeap h;
+    h.L = lazy_log_cap((int)S);
+    h.key = ws;
+    h.lastpush = h.key + S;
+    h.log_v = h.lastpush + S;
+    h.log_next = h.log_v + h.L;
+    h.top = h.log_next + h.L;
+    h.last = h.top + nb;
+    h.ring = h.last + nb;
+    h.degs = reinterpret_cast<uint32_t*>(h.ring + window + 1);
+    return h;
+}
+
+template <typename LAdj>
+__device__ void gorder_lazy_warp(const LazyHeap& h, int sz, int nb, int window, const LAdj* __restrict__ ladj,
+                                 const int64_t* __restrict__ loff, uint32_t* __restrict__ out_local) {
+    const int lane = threadIdx.x & 31;
+    constexpr unsigned kFull = 0xFFFFFFFFu;
+    const unsigned lower_lanes = (1u << lane) - 1u;
+    // Bucket 0 lists 0..sz-1 with 0 in front: pushed sz-1 first, 0 last.
+    for (int e = lane; e < sz; e += 32) {
+        const int v = sz - 1 - e;
+        h.log_v[e] = v;
+        h.log_next[e] = e - 1;
+        h.key[v] = 0;
+        h.lastpush[v] = e;
+    }
+    for (int b = lane; b < nb; b += 32) h.top[b] = b == 0 ? sz - 1 : -1;
+    // Seed: largest degree, first in local order.
+    uint32_t bd = 0;
+    int bi = -1;
+    for (int i = lane; i < sz; i += 32)
+        if (bi < 0 || h.degs[i] > bd) {
+            bd = h.degs[i];
+            bi = i;
+        }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const uint32_t od = __shfl_xor_sync(kFull, bd, o);
+        const int oi = __shfl_xor_sync(kFull, bi, o);
+        if (oi >= 0 && (bi < 0 || od > bd || (od == bd && oi < bi))) {
+            bd = od;
+            bi = oi;
+        }
+    }
+    const int seed = bi;
+    int len = sz, max_key = 0;
+    __syncwarp();
+    if (lane == 0) {
+        h.key[seed] = -1;
+        out_local[seed] = 0;
+        h.ring[0] = seed;
+    }
+    __syncwarp();
+
+    auto compact = [&]() {
+        for (int b = lane; b < nb; b += 32) h.last[b] = -1;
+        __syncwarp();
+        int nl = 0;
+        for (int c0 = 0; c0 < len; c0 += 32) {
+            const int e = c0 + lane;
+            int v = -1, b = -1;
+            bool keep = false;
+            if (e < len) {
+                v = h.log_v[e];
+                b = h.key[v];
+                keep = b >= 0 && h.lastpush[v] == e;
+            }
+            const unsigned kb = __ballot_sync(kFull, keep);
+            const int ne = nl + __popc(kb & lower_lanes);
+            const unsigned peers = __match_any_sync(kFull, keep ? b : -1 - lane);
+            const unsigned below = peers & lower_lanes;
+            const int ne_below = __shfl_sync(kFull, ne, below ? 31 - __clz(below) : lane);
+            const int prev = keep ? (below ? ne_below : h.last[b]) : -1;
+            __syncwarp();
+            if (keep) {
+                h.log_v[ne] = v;
+                h.log_next[ne] = prev;
+                h.lastpush[v] = ne;
+                if ((peers >> lane) == 1u) h.last[b] = ne;
+            }
+            nl += __popc(kb);
+            __syncwarp();
+        }
+        for (int b = lane; b < nb; b += 32) h.top[b] = h.last[b];
+        len = nl;
+        __syncwarp();
+    };
+
+    // bump(n, delta) for every neighbour n of v, in adjacency order.
+    auto bump_all = [&](int v, int delta) {
+        const int64_t e0 = loff[v], e1 = loff[v + 1];
+        if (len + (e1 - e0) > h.L) compact();
+        for (int64_t base = e0; base < e1; base += 32) {
+            const int64_t idx = base + lane;
+            int n = -1, k = -1;
+            if (idx < e1) {
+                n = (int)ladj[idx];
+                k = h.key[n];
+            }
+            const bool app = k >= 0 && !(delta < 0 && k <= 0);
+            const int t = k + delta;
+            const unsigned ab = __ballot_sync(kFull, app);
+            const int e = len + __popc(ab & lower_lanes);
+            const unsigned peers = __match_any_sync(kFull, app ? t : -1 - lane);
+            const unsigned below = peers & lower_lanes;
+            const int e_below = __shfl_sync(kFull, e, below ? 31 - __clz(below) : lane);
+            const int prev = app ? (below ? e_below : h.top[t]) : -1;
+            __syncwarp();
+            if (app) {
+                h.log_v[e] = n;
+                h.log_next[e] = prev;
+                h.key[n] = t;
+                h.lastpush[n] = e;
+                if ((peers >> lane) == 1u) h.top[t] = e;
+            }
+            len += __popc(ab);
+            int tm = app ? t : 0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) tm = max(tm, __shfl_xor_sync(kFull, tm, o));
+            max_key = max(max_key, tm);
+            __syncwarp();
+        }
+    };
+
+    bump_all(seed, +1);
+    int nplaced = 1;
+    for (int lid = 1; lid < sz; ++lid) {
+        // extract-max: newest live entry of the highest non-empty bucket.
+        int best = -1, b = max_key;
+        if (lane == 0) {
+            while (true) {
+                int e = h.top[b];
+                while (e >= 0) {
+                    const int v = h.log_v[e];
+                    if (h.key[v] == b && h.lastpush[v] == e) break;
+                    e = h.log_next[e];
+                }
+                if (e >= 0) {
+                    best = h.log_v[e];
+                    h.top[b] = h.log_next[e];
+                    h.key[best] = -1;
+                    break;
+                }
+                h.top[b] = -1;
+                if (b == 0) break;
+                --b;
+            }
+        }
+        best = __shfl_sync(kFull, best, 0);
+        max_key = __shfl_sync(kFull, b, 0);
+        if (best < 0) {   // no live vertex left: the rest in local order
+            if (lane == 0)
+                for (int i = 0; i < sz && lid < sz; ++i)
+                    if (h.key[i] >= 0) {
+                        h.key[i] = -1;
+                        out_local[i] = (uint32_t)lid++;
+                    }
+            break;
+        }
+        if (lane == 0) {
+            out_local[best] = (uint32_t)lid;
+            h.ring[nplaced % (window + 1)] = best;
+        }
+        ++nplaced;
+        __syncwarp();
+        bump_all(best, +1);
+        if (nplaced > window) {
+            int old_v = 0;
+            if (lane == 0) old_v = h.ring[(nplaced - 1 - window) % (window + 1)];
+            old_v = __shfl_sync(kFull, old_v, 0);
+            bump_all(old_v, -1);
+        }
+    }
+    __syncwarp();
+}
+
+// One warp per community of 33..gordf vertices; its workspace in shared
+// memory (capacity S of the launch) or, for the largest class, in global
+// memory (one slice per CTA).
 template <typename LAdj, bool kShared>
 __global__ void k_gorder_warp(const int32_t* __restrict__ list, const int32_t* __restrict__ count_p,
                               const int64_t* __restrict__ offs, const int64_t* __restrict__ ssize,
                               const uint32_t* __restrict__ order_v, const int64_t* __restrict__ rp,
                               const LAdj* __restrict__ ladj, const int64_t* __restrict__ loff, int window,
-                              uint32_t* __restrict__ local_by_pos, int* __restrict__ gws, int64_t gcap,
-                              uint32_t* __restrict__ gdeg) {
+                              uint32_t* __restrict__ local_by_pos, int* __restrict__ gws, int64_t cap) {
     extern __shared__ int smem[];
     const int32_t count = *count_p;
     const int lane = threadIdx.x & 31;
     const int nb = window + 2;
+    int* ws = kShared ? smem : gws + (int64_t)blockIdx.x * lazy_ws_ints(cap, nb, window);
+    const LazyHeap h = lazy_view(ws, cap, nb, window);
     for (int32_t j = blockIdx.x; j < count; j += gridDim.x) {
         const int32_t r = list[j];
         const int64_t base = offs[r];
         const int sz = (int)ssize[r];
-        int* ws;
-        uint32_t* degs;
-        if (kShared) {
-            ws = smem;
-            degs = reinterpret_cast<uint32_t*>(smem + 4 * kSmemGorderMax + 2 * nb);
-        } else {
-            ws = gws + (int64_t)blockIdx.x * (4 * gcap + 2 * nb);
-            degs = gdeg + (int64_t)blockIdx.x * gcap;
-        }
-        const int cap = kShared ? kSmemGorderMax : (int)gcap;
         for (int i = lane; i < sz; i += 32) {
             const uint32_t u = order_v[base + i];
-            degs[i] = (uint32_t)(rp[u + 1] - rp[u]);
+            h.degs[i] = (uint32_t)(rp[u + 1] - rp[u]);
         }
         __syncwarp();
-        if (lane == 0) {
-            HeapView h{ws, ws + cap, ws + 2 * cap, ws + 4 * cap, ws + 4 * cap + nb, 0};
-            gorder_run<LAdj>(h, sz, nb, window, ladj, loff + base, degs, ws + 3 * cap, local_by_pos + base);
-        }
+        gorder_lazy_warp<LAdj>(h, sz, nb, window, ladj, loff + base, local_by_pos + base);
         __syncwarp();
     }
 }
@@ -1159,13 +1360,21 @@ void compose_device(const DeviceCSR& g, const uint32_t* memb, const ComposeParam
                 ++launches;
             }
             if (hc.n[2] > 0) {
+                // Workspace sized by this call's largest community of the class
+                // (occupancy follows it); the attribute is the one constant
+                // maximum, so concurrent callers never race on it.
                 const int nb = p.gorder_window + 2;
-                const int smem = (int)sizeof(int) * (5 * kSmemGorderMax + 2 * nb);
-                GB_CUDA(cudaFuncSetAttribute(k_gorder_warp<LT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-                const int grid = std::min<int>(hc.n[2], kNumSMs * 16);
+                const int64_t cap = std::min<int64_t>(kSmemGorderMax, std::max<int64_t>(hc.gorder_max, 33));
+                const int smem = (int)(sizeof(int) * lazy_ws_ints(cap, nb, p.gorder_window));
+                GB_CUDA(cudaFuncSetAttribute(k_gorder_warp<LT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)(sizeof(int) * lazy_ws_ints(kSmemGorderMax, kMaxGorderWindow + 2,
+                                                                              kMaxGorderWindow))));
+                int per_sm = 1;
+                GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gorder_warp<LT, true>, 32, smem));
+                const int grid = std::min<int>(hc.n[2], kNumSMs * std::max(1, per_sm));
                 k_gorder_warp<LT, true><<<grid, 32, smem, s>>>(lists.get() + 2 * C, cc.get()->n + 2, offs, ssize,
                                                                order_v, g.row_ptr, ladj, loff, p.gorder_window,
-                                                               local_by_pos, nullptr, 0, nullptr);
+                                                               local_by_pos, nullptr, cap);
                 GB_LAUNCH_CHECK();
                 ++launches;
             }
@@ -1173,11 +1382,10 @@ void compose_device(const DeviceCSR& g, const uint32_t* memb, const ComposeParam
                 const int grid = std::min<int>(hc.n[3], kNumSMs * 4);
                 const int64_t cap = hc.gorder_max;
                 const int nb = p.gorder_window + 2;
-                DevBuf<int> gws((int64_t)grid * (4 * cap + 2 * nb), s);
-                DevBuf<uint32_t> gdeg((int64_t)grid * cap, s);
+                DevBuf<int> gws((int64_t)grid * lazy_ws_ints(cap, nb, p.gorder_window), s);
                 k_gorder_warp<LT, false><<<grid, 32, 0, s>>>(lists.get() + 3 * C, cc.get()->n + 3, offs, ssize,
                                                              order_v, g.row_ptr, ladj, loff, p.gorder_window,
-                                                             local_by_pos, gws, cap, gdeg);
+                                                             local_by_pos, gws, cap);
                 GB_LAUNCH_CHECK();
                 ++launches;
             }
