@@ -52,3 +52,31 @@ def test_headline_graph_maps_to_reference_fingerprint(ctx, scale):
             assert st["local_move_streams"] == 0  # the serial-order engine ran
         del ids, orp, ocol
     torch.cuda.synchronize()
+
+
+C3 = json.load(open(os.path.join(HERE, "golden", "c3_pins.json")))
+
+
+@pytest.mark.parametrize("family", ["urand23", "grid4096"])
+def test_full_size_weak_structure_bit_exact(ctx, family):
+    """The full-size weak-structure graphs (uniform 2^23 vertices of degree 16;
+    4096 x 4096 grid with 5 % of edges deleted): the serial-order engine's
+    permutation and relabelled CSR equal the oracle's cd_serial result
+    (tests/golden/make_golden_c3.py).  cd_parallel runs that order on the
+    uniform graph; on the grid it would run the racy stream mode, so the grid
+    is mapped with cd_serial."""
+    pin = C3[family]
+    if family == "urand23":
+        rp, col = gg.uniform(23, 16, seed=27491095, device="cuda")
+        recipe = PARALLEL
+    else:
+        rp, col = gg.grid(4096, 4096, 0.05, seed=27491095, device="cuda")
+        recipe = SERIAL
+    assert rp.numel() - 1 == pin["n"] and col.numel() == pin["nnz"]
+    assert gg.checksum(rp) == pin["row_ptr"] and gg.checksum(col) == pin["col"]
+    ids, orp, ocol, st = ctx.map_and_relabel(rp, col, recipe, pin["auto_resolution"])
+    assert st["local_move_streams"] == 0
+    assert gb.mapping_fingerprint(ids) == pin["fingerprint_cd_serial"]
+    assert gg.checksum(orp) == pin["relabel_row_ptr"] and gg.checksum(ocol) == pin["relabel_col"]
+    del ids, orp, ocol, rp, col
+    torch.cuda.synchronize()
