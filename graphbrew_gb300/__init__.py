@@ -134,6 +134,8 @@ SIGNATURES = {
                                         C.POINTER(GbgpuStats), C.c_uint32]),
     "gbgpu_validate_permutation_noalloc": (C.c_int, [_P, _P, C.c_int64, C.POINTER(C.c_int32)]),
     "gbgpu_fingerprint": (C.c_uint64, [_P, C.c_int64]),
+    "gbgpu_selfcheck_delta": (C.c_int, [_P, C.c_double, C.c_double, C.c_int64, C.c_uint64,
+                                        C.POINTER(C.c_int64)]),
     "gbgpu_gapbs_edge_count": (C.c_int64, [C.c_int32, C.c_int32]),
     "gbgpu_gapbs_edge_list": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _P, _P, C.c_int32]),
     "gbgpu_version": (C.c_char_p, []),
@@ -442,6 +444,14 @@ class Context:
         ms = C.c_double()
         self._check(fn(self._h, prp, pcl, n, nnz, *extra, pout, C.byref(ms), DEVICE_POINTERS if dev else 0))
         return out, ms.value
+
+    def selfcheck_delta(self, M, R, count=1 << 22, seed=1):
+        """Results of the reciprocal-based deltaModularity that differ from
+        full double divisions, over `count` seeded inputs (0 expected)."""
+        bad = C.c_int64()
+        self._check(library().gbgpu_selfcheck_delta(self._h, float(M), float(R), int(count), int(seed),
+                                                    C.byref(bad)))
+        return bad.value
 
     def pagerank(self, row_ptr, col, max_iters=20, epsilon=1e-4):
         """PageRank scores (float32), sweeps run, kernel ms."""

@@ -92,6 +92,11 @@ const T* in_dev(const T* p, int64_t count, uint32_t flags, DevBuf<T>& tmp, cudaS
 
 extern "C" {
 
+int gbgpu_selfcheck_delta(gbgpu_ctx* ctx, double M, double R, int64_t count, uint64_t seed, int64_t* mismatches) {
+    if (!ctx || !mismatches) return GBGPU_E_INVALID;
+    return guarded_ext(ctx, [&](cudaStream_t s) { *mismatches = gb::selfcheck_delta_device(M, R, count, seed, s); });
+}
+
 int gbgpu_pagerank(gbgpu_ctx* ctx, const int64_t* row_ptr, const int32_t* col, int64_t n, int64_t nnz,
                    int32_t max_iters, double epsilon, float* scores_out, int32_t* iters_out, double* ms_out,
                    uint32_t flags) {

@@ -64,6 +64,10 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* membersh
 double auto_resolution_device(const int64_t* row_ptr, int64_t n, int64_t nnz, cudaStream_t s);
 
 // ---- kernels.cu: timed consumers and the DBG arm; each returns device ms ----
+// deltaModularity with reciprocal-based exact quotients against full double
+// divisions on `count` seeded inputs; returns the number of differing results.
+int64_t selfcheck_delta_device(double M, double R, int64_t count, uint64_t seed, cudaStream_t s);
+
 double pagerank_device(const DeviceCSR& g, int max_iters, double epsilon, float* score, int* iters_out,
                        cudaStream_t s);
 double bfs_device(const DeviceCSR& g, int64_t source, int32_t* depth, cudaStream_t s);

@@ -47,6 +47,7 @@ struct LmArgs {
     unsigned long long* ctot;   // int64 totals, two's complement adds
     uint8_t* vaff;
     double M, R;
+    DqConst dq;
     double* total_delta;
     unsigned long long* moves;
 };
@@ -84,7 +85,6 @@ k_local_move_warp(LmArgs a, int64_t begin, int64_t end, int64_t stream_len) {
         if (deg > kWarpMaxDeg) continue;  // hub kernel
         if (!lm_load<kStream>(&a.vaff[u])) continue;
         const uint32_t d = lm_load<kStream>(&a.vcom[u]);
-        const double ku = (double)deg;
         double best_d = 0.0;
         uint32_t best_c = kNone;
         if (deg <= 32) {
@@ -95,12 +95,12 @@ k_local_move_warp(LmArgs a, int64_t begin, int64_t end, int64_t stream_len) {
             }
             const unsigned peers = __match_any_sync(0xFFFFFFFFu, c);
             const unsigned dmask = __ballot_sync(0xFFFFFFFFu, c == d);
-            const double kud = (double)__popc(dmask);
+            const int kud = __popc(dmask);
             const bool leader = (c != kNone) && (lane == __ffs(peers) - 1) && c != d;
             if (leader) {
-                const double sd = (double)(long long)lm_load<kStream>(&a.ctot[d]);
-                const double sc = (double)(long long)lm_load<kStream>(&a.ctot[c]);
-                const double dl = delta_q((double)__popc(peers), kud, ku, sc, sd, a.M, a.R);
+                const long long sd = (long long)lm_load<kStream>(&a.ctot[d]);
+                const long long sc = (long long)lm_load<kStream>(&a.ctot[c]);
+                const double dl = delta_qi(a.dq, __popc(peers), kud, deg, sc, sd);
                 if (dl > 0.0) { best_d = dl; best_c = c; }
             }
         } else {
@@ -119,18 +119,18 @@ k_local_move_warp(LmArgs a, int64_t begin, int64_t end, int64_t stream_len) {
                 if (c != kNone && lane == __ffs(peers) - 1) table_add(tk, tv, mask, c, (uint32_t)__popc(peers));
             }
             __syncwarp();
-            const double kud = (double)table_get(tk, tv, mask, d);
-            const double sd = (double)(long long)lm_load<kStream>(&a.ctot[d]);
+            const uint32_t kud = table_get(tk, tv, mask, d);
+            const long long sd = (long long)lm_load<kStream>(&a.ctot[d]);
             for (uint32_t i = lane; i < H; i += 32) {
                 const uint32_t c = tk[i];
                 if (c == kNone || c == d) continue;
-                const double sc = (double)(long long)lm_load<kStream>(&a.ctot[c]);
-                const double dl = delta_q((double)tv[i], kud, ku, sc, sd, a.M, a.R);
-                if (dl > 0.0 && better(dl, c, best_d, best_c)) { best_d = dl; best_c = c; }
+                const long long sc = (long long)lm_load<kStream>(&a.ctot[c]);
+                const double dl = delta_qi(a.dq, tv[i], kud, deg, sc, sd);
+                if (dl > 0.0 && better_pos(dl, c, best_d, best_c)) { best_d = dl; best_c = c; }
             }
             __syncwarp();
         }
-        warp_argmax(best_d, best_c);
+        warp_argmax_pos(best_d, best_c);
         if (best_d > 0.0 && best_c != d && best_c != kNone) {
             if (lane == 0) {
                 atomicAdd(&a.ctot[d], (unsigned long long)(-(long long)deg));
@@ -228,25 +228,24 @@ k_local_move_hub(LmArgs a, const uint32_t* __restrict__ hubs, int64_t hub_begin,
         __syncthreads();
         if (threadIdx.x == 0) s_kud = table_get(tk, tv, mask, d);
         __syncthreads();
-        const double kud = (double)s_kud;
-        const double ku = (double)deg;
-        const double sd = (double)(long long)a.ctot[d];
+        const uint32_t kud = s_kud;
+        const long long sd = (long long)a.ctot[d];
         double best_d = 0.0;
         uint32_t best_c = kNone;
         for (uint32_t i = threadIdx.x; i < H; i += blockDim.x) {
             const uint32_t c = tk[i];
             if (c == kNone || c == d) continue;
-            const double sc = (double)(long long)a.ctot[c];
-            const double dl = delta_q((double)tv[i], kud, ku, sc, sd, a.M, a.R);
-            if (dl > 0.0 && better(dl, c, best_d, best_c)) { best_d = dl; best_c = c; }
+            const long long sc = (long long)a.ctot[c];
+            const double dl = delta_qi(a.dq, tv[i], kud, deg, sc, sd);
+            if (dl > 0.0 && better_pos(dl, c, best_d, best_c)) { best_d = dl; best_c = c; }
         }
-        warp_argmax(best_d, best_c);
+        warp_argmax_pos(best_d, best_c);
         if (lane == 0) { red_d[w] = best_d; red_c[w] = best_c; }
         __syncthreads();
         if (w == 0) {
             best_d = lane < (int)(blockDim.x / 32) ? red_d[lane] : 0.0;
             best_c = lane < (int)(blockDim.x / 32) ? red_c[lane] : kNone;
-            warp_argmax(best_d, best_c);
+            warp_argmax_pos(best_d, best_c);
             if (lane == 0) { red_d[0] = best_d; red_c[0] = best_c; }
         }
         __syncthreads();
@@ -1137,7 +1136,7 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
     const int sm_smem = 32 * 4 * kSmSmall * (int)sizeof(uint32_t);
     GB_CUDA(cudaFuncSetAttribute(k_super_move_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_smem));
 
-    LmArgs la{g.row_ptr, g.col, vcom, ctot, vaff, M, R, dacc, macc};
+    LmArgs la{g.row_ptr, g.col, vcom, ctot, vaff, M, R, make_dq(M, R), dacc, macc};
     const int64_t chunk = p.chunk_vertices > 0 ? p.chunk_vertices : n;
 
     // Serial-order engine: cd_serial always; cd_parallel too, except on large
@@ -1174,6 +1173,7 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
     lmc.vaff = vaff;
     lmc.M = M;
     lmc.R = R;
+    lmc.dq = la.dq;
     lmc.hubs_h = hubs_h;
     lmc.hubs = hubs.get();
     lmc.hub_grid = hub_grid;
@@ -1694,6 +1694,77 @@ double auto_resolution_device(const int64_t* row_ptr, int64_t n, int64_t nnz, cu
         resolution = std::max(0.5, resolution * factor);
     }
     return resolution;
+}
+
+}  // namespace gb
+
+namespace gb {
+
+namespace {
+
+__device__ __forceinline__ uint64_t sc_mix(uint64_t x) {
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+// Two checks per index i, both against full double divisions:
+//  (a) deltaModularity of a graph with total weight M and resolution R, on
+//      counts and totals drawn from that graph's ranges (ku up to 2^24,
+//      totals up to 2M), delta_qi against delta_q;
+//  (b) a bare quotient x / m over random 53-bit significands with exponents
+//      in [-200, 200], div_rn_by against __ddiv_rn, with the reciprocal
+//      pair formed on the device the way make_dq forms it on the host.
+__global__ void k_selfcheck_delta(DqConst q, int64_t count, uint64_t seed, unsigned long long* bad) {
+    unsigned long long local = 0;
+    const double twoM = 2.0 * q.M;
+    const long long tmax = twoM < 9.0e15 ? (long long)twoM : (1ll << 53);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t h0 = sc_mix(seed ^ (uint64_t)i), h1 = sc_mix(h0), h2 = sc_mix(h1), h3 = sc_mix(h2);
+        // ku log-uniform in [1, 2^24], capped by the graph's total weight
+        const int lg = (int)(h0 & 31) % 25;
+        long long ku = 1 + (long long)((h0 >> 8) & ((1ull << lg) - 1));
+        if (ku > tmax && tmax > 0) ku = tmax;
+        const long long kuc = 1 + (long long)((h1 & 0xFFFFFFFFull) % (uint64_t)ku);
+        const long long kud = (long long)((h1 >> 32) % (uint64_t)(ku + 1));
+        // totals: half uniform over [0, 2M], half small
+        const long long span = (h2 & 1) ? tmax : (long long)(ku * 4 + 16);
+        const long long sc = (long long)((h2 >> 1) % (uint64_t)(span + 1));
+        const long long sd = (long long)((h3 >> 1) % (uint64_t)(span + 1));
+        const double ref = delta_q((double)kuc, (double)kud, (double)ku, (double)sc, (double)sd, q.M, q.R);
+        const double got = delta_qi(q, kuc, kud, ku, sc, sd);
+        local += __double_as_longlong(ref) != __double_as_longlong(got);
+        // bare quotient
+        const uint64_t h4 = sc_mix(h3), h5 = sc_mix(h4);
+        const int ex = (int)((h4 >> 52) % 401) - 200, em = (int)((h5 >> 52) % 401) - 200;
+        const double x = __longlong_as_double((long long)(((uint64_t)(1023 + ex) << 52) | (h4 & 0xFFFFFFFFFFFFFull))) *
+                         (h3 & 1 ? -1.0 : 1.0);
+        const double m = __longlong_as_double((long long)(((uint64_t)(1023 + em) << 52) | (h5 & 0xFFFFFFFFFFFFFull)));
+        const double yh = __drcp_rn(m);
+        const double yl = __dmul_rn(__fma_rn(-yh, m, 1.0), yh);
+        local += __double_as_longlong(__ddiv_rn(x, m)) != __double_as_longlong(div_rn_by(x, m, yh, yl));
+    }
+    if (local) atomicAdd(bad, local);
+}
+
+}  // namespace
+
+int64_t selfcheck_delta_device(double M, double R, int64_t count, uint64_t seed, cudaStream_t s) {
+    GB_REQUIRE(M >= 1.0 && M < 4.0e15 && R > 0.0 && R < 1.0e6 && count >= 0, GBGPU_E_INVALID,
+               "selfcheck_delta: M must be in [1, 4e15), R in (0, 1e6), count >= 0");
+    DevBuf<unsigned long long> bad(1, s);
+    GB_CUDA(cudaMemsetAsync(bad.get(), 0, sizeof(unsigned long long), s));
+    if (count > 0) {
+        const int64_t blocks = std::min<int64_t>((count + 255) / 256, 152 * 16);
+        k_selfcheck_delta<<<(int)blocks, 256, 0, s>>>(make_dq(M, R), count, seed, bad.get());
+        GB_CUDA(cudaGetLastError());
+    }
+    unsigned long long h = 0;
+    GB_CUDA(cudaMemcpyAsync(&h, bad.get(), sizeof(h), cudaMemcpyDeviceToHost, s));
+    GB_CUDA(cudaStreamSynchronize(s));
+    return (int64_t)h;
 }
 
 }  // namespace gb

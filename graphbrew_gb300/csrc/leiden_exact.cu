@@ -178,6 +178,7 @@ struct ExactState {
     cudaGraphConditionalHandle cond;  // while-node condition (graph-driven rounds)
     int use_cond;
     double M, R;
+    DqConst dq;
 };
 
 __device__ __forceinline__ uint32_t slot_hash(uint32_t c) {
@@ -922,13 +923,13 @@ __device__ __forceinline__ void eval_vertex(const ExactState& a, const Round& r,
             if (counts(a, v, (uint32_t)u, ub)) c = comm_at(a, r, v, u);
         }
         const unsigned peers = __match_any_sync(0xFFFFFFFFu, c);
-        const double kud = (double)__popc(__ballot_sync(0xFFFFFFFFu, c == d));
+        const int kud = __popc(__ballot_sync(0xFFFFFFFFu, c == d));
         if (c != kNone && c != d && lane == __ffs(peers) - 1) {
             const uint32_t cc[2] = {c, d};
             const bool vv[2] = {true, true};
             long long sg[2];
             sigma_at_k<2>(a, r.tag, r.P, r.par, cc, vv, (uint32_t)u, sg);
-            const double dl = delta_q((double)__popc(peers), kud, ku, (double)sg[0], (double)sg[1], a.M, a.R);
+            const double dl = delta_qi(a.dq, __popc(peers), kud, deg, sg[0], sg[1]);
             if (dl > 0.0) { best_d = dl; best_c = c; }
         }
     } else {
@@ -957,7 +958,7 @@ __device__ __forceinline__ void eval_vertex(const ExactState& a, const Round& r,
             }
         }
         __syncwarp();
-        const double kud = (double)table_get(tk, tv, mask, d);
+        const uint32_t kud = table_get(tk, tv, mask, d);
         // Compact the candidate communities (c != d) to the front of the
         // table, so the selection runs ceil(candidates / 32) lookup rounds.
         uint32_t cnt = 0;
@@ -976,7 +977,7 @@ __device__ __forceinline__ void eval_vertex(const ExactState& a, const Round& r,
         }
         // Four candidates per lane per step, interleaved; the first step also
         // looks up sigma of d.
-        double sd = 0.0;
+        long long sd = 0;
         for (uint32_t i0 = 0;; i0 += 128) {
             uint32_t cc[5];
             bool vv[5];
@@ -990,19 +991,19 @@ __device__ __forceinline__ void eval_vertex(const ExactState& a, const Round& r,
             cc[4] = d;
             vv[4] = i0 == 0;
             sigma_at_k<5>(a, r.tag, r.P, r.par, cc, vv, (uint32_t)u, sg);
-            if (i0 == 0) sd = (double)sg[4];
+            if (i0 == 0) sd = sg[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 if (!vv[k]) continue;
-                const double dl = delta_q((double)tv[i0 + 32 * k + lane], kud, ku, (double)sg[k], sd, a.M, a.R);
-                if (dl > 0.0 && better(dl, cc[k], best_d, best_c)) { best_d = dl; best_c = cc[k]; }
+                const double dl = delta_qi(a.dq, tv[i0 + 32 * k + lane], kud, deg, sg[k], sd);
+                if (dl > 0.0 && better_pos(dl, cc[k], best_d, best_c)) { best_d = dl; best_c = cc[k]; }
             }
             if (i0 + 128 >= cnt) break;
         }
         __syncwarp();
-        if (refine_stays(a, sd, ku)) best_c = kNone;   // every lane holds the same sd
+        if (refine_stays(a, (double)sd, ku)) best_c = kNone;   // every lane holds the same sd
     }
-    warp_argmax(best_d, best_c);
+    warp_argmax_pos(best_d, best_c);
     if (lane == 0) {
         if (best_d > 0.0 && best_c != kNone && best_c != d) record(a, r, u, 1, best_c, best_d);
         else record(a, r, u, 1, d, 0.0);
@@ -1080,15 +1081,14 @@ __device__ __forceinline__ void eval_small_body(const ExactState& a, const Ctl* 
             const bool vv[2] = {true, true};
             long long sg[2];
             sigma_at_k<2>(a, r.tag, r.P, r.par, cc, vv, (uint32_t)u, sg);
-            const double dl = delta_q((double)__popc(peers), (double)__popc(eqd), (double)deg, (double)sg[0],
-                                      (double)sg[1], a.M, a.R);
+            const double dl = delta_qi(a.dq, __popc(peers), __popc(eqd), deg, sg[0], sg[1]);
             if (dl > 0.0) { best_d = dl; best_c = c; }
         }
 #pragma unroll
         for (int o = 4; o > 0; o >>= 1) {   // argmax inside each 8-lane group
             const double od = __shfl_xor_sync(0xFFFFFFFFu, best_d, o);
             const uint32_t oc = __shfl_xor_sync(0xFFFFFFFFu, best_c, o);
-            if (better(od, oc, best_d, best_c)) { best_d = od; best_c = oc; }
+            if (better_pos(od, oc, best_d, best_c)) { best_d = od; best_c = oc; }
         }
         if (tiny && j == 0) {
             if (!act) record(a, r, u, 0, d, 0.0);
@@ -1168,7 +1168,7 @@ __device__ __forceinline__ void eval_big_body(const ExactState& a, const Ctl* c)
             continue;
         }
         const double ku = (double)deg;
-        const double kud = (double)table_get(tk, tv, mask, d);
+        const uint32_t kud = table_get(tk, tv, mask, d);
         // Compact the candidates (c != d); their order does not matter, the
         // selection is a total order.
         for (uint32_t i0 = 0; i0 < H; i0 += blockDim.x) {
@@ -1189,7 +1189,7 @@ __device__ __forceinline__ void eval_big_body(const ExactState& a, const Ctl* c)
         const uint32_t cnt = s_cnt;
         double best_d = 0.0;
         uint32_t best_c = kNone;
-        double sd = 0.0;
+        long long sd = 0;
         for (uint32_t i0 = 0;; i0 += 4 * blockDim.x) {
             uint32_t cc[5];
             bool vv[5];
@@ -1203,25 +1203,24 @@ __device__ __forceinline__ void eval_big_body(const ExactState& a, const Ctl* c)
             cc[4] = d;
             vv[4] = i0 == 0;
             sigma_at_k<5>(a, r.tag, r.P, r.par, cc, vv, u, sg);
-            if (i0 == 0) sd = (double)sg[4];
+            if (i0 == 0) sd = sg[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 if (!vv[k]) continue;
-                const double dl = delta_q((double)cand_w[i0 + k * blockDim.x + tid], kud, ku, (double)sg[k], sd,
-                                          a.M, a.R);
-                if (dl > 0.0 && better(dl, cc[k], best_d, best_c)) { best_d = dl; best_c = cc[k]; }
+                const double dl = delta_qi(a.dq, cand_w[i0 + k * blockDim.x + tid], kud, deg, sg[k], sd);
+                if (dl > 0.0 && better_pos(dl, cc[k], best_d, best_c)) { best_d = dl; best_c = cc[k]; }
             }
             if (i0 + 4 * blockDim.x >= cnt) break;
         }
-        warp_argmax(best_d, best_c);
+        warp_argmax_pos(best_d, best_c);
         if (lane == 0) { red_d[w] = best_d; red_c[w] = best_c; }
         __syncthreads();
         if (tid == 0) {
             double bd = red_d[0];
             uint32_t bc = red_c[0];
             for (int k = 1; k < (int)(blockDim.x / 32); ++k)
-                if (better(red_d[k], red_c[k], bd, bc)) { bd = red_d[k]; bc = red_c[k]; }
-            if (!refine_stays(a, sd, ku) && bd > 0.0 && bc != kNone && bc != d) record(a, r, u, 1, bc, bd);
+                if (better_pos(red_d[k], red_c[k], bd, bc)) { bd = red_d[k]; bc = red_c[k]; }
+            if (!refine_stays(a, (double)sd, ku) && bd > 0.0 && bc != kNone && bc != d) record(a, r, u, 1, bc, bd);
             else record(a, r, u, 1, d, 0.0);
         }
         __syncthreads();
@@ -1350,8 +1349,8 @@ __device__ __forceinline__ void hub_select_body(const ExactState& a, const Ctl* 
         const uint32_t* occ = a.hub_occ + a.hub_toff[j];
         const uint32_t nocc = a.hub_occn[j];
         const uint32_t d = a.vcom[h];
-        const double ku = (double)(a.rp[h + 1] - a.rp[h]);
-        const double kud = (double)a.hub_kud[j];
+        const long long ku = a.rp[h + 1] - a.rp[h];
+        const uint32_t kud = a.hub_kud[j];
         double best_d = 0.0;
         uint32_t best_c = kNone;
         // Segment `part` covers occupied-list positions [s0, s0 + kTabSeg):
@@ -1372,22 +1371,22 @@ __device__ __forceinline__ void hub_select_body(const ExactState& a, const Ctl* 
             cc[4] = d;
             vv[4] = true;
             sigma_at_k<5>(a, r.tag, r.P, r.par, cc, vv, h, sgm);
-            const double sd = (double)sgm[4];
+            const long long sd = sgm[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 if (!vv[k]) continue;
-                const double dl = delta_q((double)cw[k], kud, ku, (double)sgm[k], sd, a.M, a.R);
-                if (dl > 0.0 && better(dl, cc[k], best_d, best_c)) { best_d = dl; best_c = cc[k]; }
+                const double dl = delta_qi(a.dq, cw[k], kud, ku, sgm[k], sd);
+                if (dl > 0.0 && better_pos(dl, cc[k], best_d, best_c)) { best_d = dl; best_c = cc[k]; }
             }
         }
-        warp_argmax(best_d, best_c);
+        warp_argmax_pos(best_d, best_c);
         if (lane == 0) { red_d[w] = best_d; red_c[w] = best_c; }
         __syncthreads();
         if (threadIdx.x == 0) {
             double bd = red_d[0];
             uint32_t bc = red_c[0];
             for (int k = 1; k < (int)(blockDim.x / 32); ++k)
-                if (better(red_d[k], red_c[k], bd, bc)) { bd = red_d[k]; bc = red_c[k]; }
+                if (better_pos(red_d[k], red_c[k], bd, bc)) { bd = red_d[k]; bc = red_c[k]; }
             a.part_d[q] = bd;
             a.part_c[q] = bc;
             __threadfence();
@@ -1403,9 +1402,9 @@ __device__ __forceinline__ void hub_select_body(const ExactState& a, const Ctl* 
             for (int k = threadIdx.x; k < nt; k += blockDim.x) {
                 const double pd = ((volatile double*)a.part_d)[f + k];
                 const uint32_t pc = ((volatile uint32_t*)a.part_c)[f + k];
-                if (better(pd, pc, bd, bc)) { bd = pd; bc = pc; }
+                if (better_pos(pd, pc, bd, bc)) { bd = pd; bc = pc; }
             }
-            warp_argmax(bd, bc);
+            warp_argmax_pos(bd, bc);
             __syncthreads();
             if (lane == 0) { red_d[w] = bd; red_c[w] = bc; }
             __syncthreads();
@@ -1413,7 +1412,7 @@ __device__ __forceinline__ void hub_select_body(const ExactState& a, const Ctl* 
                 bd = red_d[0];
                 bc = red_c[0];
                 for (int k = 1; k < (int)(blockDim.x / 32); ++k)
-                    if (better(red_d[k], red_c[k], bd, bc)) { bd = red_d[k]; bc = red_c[k]; }
+                    if (better_pos(red_d[k], red_c[k], bd, bc)) { bd = red_d[k]; bc = red_c[k]; }
                 const bool act = a.vaff[h] != 0 || ((volatile int32_t*)a.hub_any)[j] != 0;
                 bool stays = false;
                 if (a.vcob) {
@@ -1969,6 +1968,7 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     a.n_mid = n_mid;
     a.M = ctx.M;
     a.R = ctx.R;
+    a.dq = ctx.dq;
 
     static_assert(kEventsMax + 32 * 257 <= kTableSlots + kEventsMax, "sort scratch fits the hash area");
     const int group_smem = 32 * kCoarse * (int)sizeof(int32_t);

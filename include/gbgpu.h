@@ -228,6 +228,16 @@ int gbgpu_generate_mappings_batched(gbgpu_ctx* ctx, const gbgpu_graph* graphs, i
 int gbgpu_validate_permutation_noalloc(gbgpu_ctx* ctx, const int32_t* new_ids_dev, int64_t n,
                                        int32_t* result);
 
+/* Arithmetic self-check, no counterpart in the reference.  The local-moving
+ * kernels evaluate deltaModularity (reorder_graphbrew.h:1295-1298) with the
+ * two quotients formed from precomputed double-double reciprocals and an
+ * exact FMA remainder instead of full double divisions.  This call runs both
+ * forms on the device over `count` seeded inputs (a graph of total weight M,
+ * 1 <= M < 4e15, resolution 0 < R < 1e6; plus bare quotients over a wide
+ * exponent range) and writes into *mismatches how many results differ in any
+ * bit; 0 is the expected answer. */
+int gbgpu_selfcheck_delta(gbgpu_ctx* ctx, double M, double R, int64_t count, uint64_t seed, int64_t* mismatches);
+
 /* FNV-1a-64 fingerprint of a forward map, on the host, as the builder prints
  * it ("Mapping Fingerprint"). */
 uint64_t gbgpu_fingerprint(const int32_t* new_ids, int64_t n);

@@ -483,3 +483,17 @@ def test_map_and_relabel_lifecycle(ctx, golden_arrays):
     np.testing.assert_array_equal(orp, erp)
     np.testing.assert_array_equal(ocol, ecol)
     assert st["total_ms"] > 0 and st["kernel_launches"] > 0
+
+
+@pytest.mark.parametrize("M,R", [
+    (64155273.0, 1.0),            # RMAT scale 22 (directed entries / 2), resolution 1
+    (64155273.0, 0.6969314931),   # ... and a fractional resolution like the automatic one
+    (1.0, 1.0), (7.0, 3.25), (1234567.0, 0.1),
+    (2.0 ** 40 + 12345.0, 1.5),   # totals near 2^41
+    (3.9e15, 0.75),               # 2 M M far above 2^53
+])
+def test_delta_reciprocal_form_equals_division(ctx, M, R):
+    """The kernels' deltaModularity (double-double reciprocals, exact FMA
+    remainder, midpoint test) equals the two full divisions bit for bit; the
+    same call also checks bare quotients over exponents -200..200."""
+    assert ctx.selfcheck_delta(M, R, count=1 << 22, seed=int(M) % 1000 + 7) == 0
