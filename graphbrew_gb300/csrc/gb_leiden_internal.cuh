@@ -30,12 +30,20 @@ __device__ __forceinline__ double delta_q(double kuc, double kud, double ku, dou
 // reciprocals, so that a candidate's quotients cost a few multiply-adds
 // instead of two full divisions (this GPU's FP64 rate is low, and the
 // evaluation kernels spend most of their issue slots on FP64).
+constexpr int kAtabMax = 1024;   // RN(k / M) tabulated for 0 <= k <= kAtabMax
+
 struct DqConst {
     double M = 1.0, R = 1.0;
     double den = 2.0;            // (2 M) M, formed as the reference forms it
     double yMh = 1.0, yMl = 0.0; // 1/M   ~ yMh + yMl
     double yDh = 0.5, yDl = 0.0; // 1/den ~ yDh + yDl
+    const double* atab = nullptr;  // device: RN(k / M), k = 0..kAtabMax (fill_atab), or null
 };
+
+// Fills the device table tab[k] = RN(k / M), k = 0..kAtabMax, by full double
+// divisions: (kuc - kud) / M of a row with at most kAtabMax neighbours in
+// either community is then one load.
+void fill_atab(double* tab, double M, cudaStream_t s);
 
 // Host side: yh = RN(1/m); the remainder e = 1 - yh m is exact (the
 // remainder of a correctly rounded quotient is representable), and
@@ -97,10 +105,22 @@ __device__ __forceinline__ double div_rn_by(double x, double m, double yh, doubl
 // correctly rounded by div_rn_by, so the value is bit-identical to delta_q.
 __device__ __forceinline__ double delta_qi(const DqConst& q, long long kuc, long long kud, long long ku,
                                            long long sc, long long sd) {
-    const double a = div_rn_by((double)(kuc - kud), q.M, q.yMh, q.yMl);
+    // RN(-k / M) = -RN(k / M): round-to-nearest is symmetric.
+    const long long dk = kuc - kud, adk = dk < 0 ? -dk : dk;
+    double a;
+    if (adk <= kAtabMax && q.atab) {
+        a = __ldg(q.atab + adk);
+        if (dk < 0) a = -a;
+    } else {
+        a = div_rn_by((double)dk, q.M, q.yMh, q.yMl);
+    }
     const double b = __dmul_rn(__dmul_rn(q.R, (double)ku), (double)(sc - sd + ku));
     return __dsub_rn(a, div_rn_by(b, q.den, q.yDh, q.yDl));
 }
+
+// d > 0.0 for a delta that is not NaN, on the integer pipe: a double is
+// above +0.0 exactly when its bit pattern, read as a signed integer, is.
+__device__ __forceinline__ bool dpos(double d) { return __double_as_longlong(d) > 0; }
 
 // (delta, id) ordering: larger delta first, then smaller id.
 __device__ __forceinline__ bool better(double da, uint32_t ia, double db, uint32_t ib) {

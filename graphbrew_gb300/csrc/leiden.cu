@@ -101,7 +101,7 @@ k_local_move_warp(LmArgs a, int64_t begin, int64_t end, int64_t stream_len) {
                 const long long sd = (long long)lm_load<kStream>(&a.ctot[d]);
                 const long long sc = (long long)lm_load<kStream>(&a.ctot[c]);
                 const double dl = delta_qi(a.dq, __popc(peers), kud, deg, sc, sd);
-                if (dl > 0.0) { best_d = dl; best_c = c; }
+                if (dpos(dl)) { best_d = dl; best_c = c; }
             }
         } else {
             uint32_t H = 64;
@@ -126,7 +126,7 @@ k_local_move_warp(LmArgs a, int64_t begin, int64_t end, int64_t stream_len) {
                 if (c == kNone || c == d) continue;
                 const long long sc = (long long)lm_load<kStream>(&a.ctot[c]);
                 const double dl = delta_qi(a.dq, tv[i], kud, deg, sc, sd);
-                if (dl > 0.0 && better_pos(dl, c, best_d, best_c)) { best_d = dl; best_c = c; }
+                if (dpos(dl) && better_pos(dl, c, best_d, best_c)) { best_d = dl; best_c = c; }
             }
             __syncwarp();
         }
@@ -237,7 +237,7 @@ k_local_move_hub(LmArgs a, const uint32_t* __restrict__ hubs, int64_t hub_begin,
             if (c == kNone || c == d) continue;
             const long long sc = (long long)a.ctot[c];
             const double dl = delta_qi(a.dq, tv[i], kud, deg, sc, sd);
-            if (dl > 0.0 && better_pos(dl, c, best_d, best_c)) { best_d = dl; best_c = c; }
+            if (dpos(dl) && better_pos(dl, c, best_d, best_c)) { best_d = dl; best_c = c; }
         }
         warp_argmax_pos(best_d, best_c);
         if (lane == 0) { red_d[w] = best_d; red_c[w] = best_c; }
@@ -1136,7 +1136,10 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
     const int sm_smem = 32 * 4 * kSmSmall * (int)sizeof(uint32_t);
     GB_CUDA(cudaFuncSetAttribute(k_super_move_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_smem));
 
+    DevBuf<double> atab(kAtabMax + 1, s);
+    fill_atab(atab.get(), M, s);
     LmArgs la{g.row_ptr, g.col, vcom, ctot, vaff, M, R, make_dq(M, R), dacc, macc};
+    la.dq.atab = atab.get();
     const int64_t chunk = p.chunk_vertices > 0 ? p.chunk_vertices : n;
 
     // Serial-order engine: cd_serial always; cd_parallel too, except on large
@@ -1751,14 +1754,30 @@ __global__ void k_selfcheck_delta(DqConst q, int64_t count, uint64_t seed, unsig
 
 }  // namespace
 
+namespace {
+__global__ void k_fill_atab(double* tab, double M) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k <= kAtabMax; k += gridDim.x * blockDim.x)
+        tab[k] = __ddiv_rn((double)k, M);
+}
+}  // namespace
+
+void fill_atab(double* tab, double M, cudaStream_t s) {
+    k_fill_atab<<<(kAtabMax + 256) / 256, 256, 0, s>>>(tab, M);
+    GB_CUDA(cudaGetLastError());
+}
+
 int64_t selfcheck_delta_device(double M, double R, int64_t count, uint64_t seed, cudaStream_t s) {
     GB_REQUIRE(M >= 1.0 && M < 4.0e15 && R > 0.0 && R < 1.0e6 && count >= 0, GBGPU_E_INVALID,
                "selfcheck_delta: M must be in [1, 4e15), R in (0, 1e6), count >= 0");
     DevBuf<unsigned long long> bad(1, s);
+    DevBuf<double> atab(kAtabMax + 1, s);
+    fill_atab(atab.get(), M, s);
     GB_CUDA(cudaMemsetAsync(bad.get(), 0, sizeof(unsigned long long), s));
     if (count > 0) {
         const int64_t blocks = std::min<int64_t>((count + 255) / 256, 152 * 16);
-        k_selfcheck_delta<<<(int)blocks, 256, 0, s>>>(make_dq(M, R), count, seed, bad.get());
+        DqConst q = make_dq(M, R);
+        q.atab = atab.get();
+        k_selfcheck_delta<<<(int)blocks, 256, 0, s>>>(q, count, seed, bad.get());
         GB_CUDA(cudaGetLastError());
     }
     unsigned long long h = 0;

@@ -930,7 +930,7 @@ __device__ __forceinline__ void eval_vertex(const ExactState& a, const Round& r,
             long long sg[2];
             sigma_at_k<2>(a, r.tag, r.P, r.par, cc, vv, (uint32_t)u, sg);
             const double dl = delta_qi(a.dq, __popc(peers), kud, deg, sg[0], sg[1]);
-            if (dl > 0.0) { best_d = dl; best_c = c; }
+            if (dpos(dl)) { best_d = dl; best_c = c; }
         }
     } else {
         uint32_t H = 64;
@@ -996,7 +996,7 @@ __device__ __forceinline__ void eval_vertex(const ExactState& a, const Round& r,
             for (int k = 0; k < 4; ++k) {
                 if (!vv[k]) continue;
                 const double dl = delta_qi(a.dq, tv[i0 + 32 * k + lane], kud, deg, sg[k], sd);
-                if (dl > 0.0 && better_pos(dl, cc[k], best_d, best_c)) { best_d = dl; best_c = cc[k]; }
+                if (dpos(dl) && better_pos(dl, cc[k], best_d, best_c)) { best_d = dl; best_c = cc[k]; }
             }
             if (i0 + 128 >= cnt) break;
         }
@@ -1082,7 +1082,7 @@ __device__ __forceinline__ void eval_small_body(const ExactState& a, const Ctl* 
             long long sg[2];
             sigma_at_k<2>(a, r.tag, r.P, r.par, cc, vv, (uint32_t)u, sg);
             const double dl = delta_qi(a.dq, __popc(peers), __popc(eqd), deg, sg[0], sg[1]);
-            if (dl > 0.0) { best_d = dl; best_c = c; }
+            if (dpos(dl)) { best_d = dl; best_c = c; }
         }
 #pragma unroll
         for (int o = 4; o > 0; o >>= 1) {   // argmax inside each 8-lane group
@@ -1208,7 +1208,7 @@ __device__ __forceinline__ void eval_big_body(const ExactState& a, const Ctl* c)
             for (int k = 0; k < 4; ++k) {
                 if (!vv[k]) continue;
                 const double dl = delta_qi(a.dq, cand_w[i0 + k * blockDim.x + tid], kud, deg, sg[k], sd);
-                if (dl > 0.0 && better_pos(dl, cc[k], best_d, best_c)) { best_d = dl; best_c = cc[k]; }
+                if (dpos(dl) && better_pos(dl, cc[k], best_d, best_c)) { best_d = dl; best_c = cc[k]; }
             }
             if (i0 + 4 * blockDim.x >= cnt) break;
         }
@@ -1376,7 +1376,7 @@ __device__ __forceinline__ void hub_select_body(const ExactState& a, const Ctl* 
             for (int k = 0; k < 4; ++k) {
                 if (!vv[k]) continue;
                 const double dl = delta_qi(a.dq, cw[k], kud, ku, sgm[k], sd);
-                if (dl > 0.0 && better_pos(dl, cc[k], best_d, best_c)) { best_d = dl; best_c = cc[k]; }
+                if (dpos(dl) && better_pos(dl, cc[k], best_d, best_c)) { best_d = dl; best_c = cc[k]; }
             }
         }
         warp_argmax_pos(best_d, best_c);

@@ -231,7 +231,8 @@ int gbgpu_validate_permutation_noalloc(gbgpu_ctx* ctx, const int32_t* new_ids_de
 /* Arithmetic self-check, no counterpart in the reference.  The local-moving
  * kernels evaluate deltaModularity (reorder_graphbrew.h:1295-1298) with the
  * two quotients formed from precomputed double-double reciprocals and an
- * exact FMA remainder instead of full double divisions.  This call runs both
+ * exact FMA remainder instead of full double divisions (and the first one,
+ * (kuc - kud) / M, read from a table of RN(k / M) for |k| <= 1024).  This call runs both
  * forms on the device over `count` seeded inputs (a graph of total weight M,
  * 1 <= M < 4e15, resolution 0 < R < 1e6; plus bare quotients over a wide
  * exponent range) and writes into *mismatches how many results differ in any
