@@ -54,7 +54,7 @@ constexpr int kFineBits = kSlotBits - kCoarseBits;
 constexpr int kTbThreads = 1024;              // table insert / group: one window vertex per thread
 constexpr int kTbMinChunk = 512;            // smallest insert chunk (CTA size) the table kernels accept
 constexpr int kTbChunks = kWindowMax / kTbMinChunk;   // stride of the per-chunk histograms
-constexpr int kTbFinishThreads = 1024;        // table finish: one CTA per coarse bucket
+constexpr int kTbFinishThreads = 512;         // table finish: one CTA per coarse bucket, a thread per fine digit
 constexpr uint32_t kPadSlot = 0xFFFFFFFFu;
 static_assert(kTableSlots >= 2 * kEventsMax, "hash load factor <= 1/2");
 static_assert(kCoarse <= kTbMinChunk, "one coarse bucket per grouping thread");
@@ -102,6 +102,7 @@ struct Ctl {
     unsigned long long tag;   // generation of the event table (slots of older tags are empty)
     unsigned int nhot;        // hot slots of the current table
     unsigned long long tb_big; // largest coarse bucket: size << 32 | bucket (its CTA starts first)
+    unsigned int tb_ticket;    // insert CTAs done this round (the last one scans the histogram)
     unsigned int nz;                 // designated communities of the current table
     unsigned int zc[kZMax];          // their ids
     unsigned int zcount[kZMax];      // events each received in the current table
@@ -140,6 +141,7 @@ struct ExactState {
     uint32_t* tb_s1;      // slot of the arrival event
     int32_t* wdeg;        // degree of a window mover, 0 otherwise
     int32_t* tb_hist;     // coarse bucket x insert chunk counts
+    int32_t* tb_base;     // their exclusive prefix in bucket-major order: where a chunk's events of a bucket go
     int32_t* tb_bstart;   // coarse bucket starts (kCoarse + 1)
     unsigned long long* ev1;  // events grouped by coarse bucket: slot << 32 | event index
     unsigned long long* ev2;  // events sorted by slot
@@ -514,69 +516,121 @@ __device__ __forceinline__ void tb_insert_chunk(const ExactState& a, const Ctl* 
     __syncthreads();   // hist is reused by the CTA's next chunk
 }
 
+// Run by the last insert CTA of a round (chunks = the insert grid): exclusive
+// prefix of the (bucket, chunk) counts in bucket-major order -- the offset of
+// each chunk's events inside the grouped array -- plus the bucket starts and
+// the largest bucket.  Once per round instead of once per grouping CTA.  Warp
+// w owns buckets [w * kPerWarp, (w + 1) * kPerWarp); lane l holds chunks l and
+// l + 32 of each; all loads are issued before the scans.
+constexpr int kScanPerWarp = kCoarse / (kTbThreads / 32);
+static_assert(kCoarse % (kTbThreads / 32) == 0, "buckets split evenly over the insert CTA's warps");
+static_assert(kWindowMax / kTbThreads <= 64, "two insert chunks per lane");
+
+__device__ __forceinline__ void tb_scan_hist(const ExactState& a, int chunks) {
+    __shared__ int32_t bstart[kCoarse];
+    __shared__ int32_t wsum[32];
+    __shared__ unsigned long long wbig[32];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    int v0[kScanPerWarp], v1[kScanPerWarp];
+#pragma unroll
+    for (int k = 0; k < kScanPerWarp; ++k) {
+        const int32_t* h = a.tb_hist + (size_t)(w * kScanPerWarp + k) * kTbChunks;
+        v0[k] = lane < chunks ? h[lane] : 0;
+        v1[k] = lane + 32 < chunks ? h[lane + 32] : 0;
+    }
+#pragma unroll
+    for (int k = 0; k < kScanPerWarp; ++k) {
+        int x0 = v0[k], x1 = v1[k];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y0 = __shfl_up_sync(0xFFFFFFFFu, x0, o), y1 = __shfl_up_sync(0xFFFFFFFFu, x1, o);
+            if (lane >= o) { x0 += y0; x1 += y1; }
+        }
+        const int t0 = __shfl_sync(0xFFFFFFFFu, x0, 31), t1 = __shfl_sync(0xFFFFFFFFu, x1, 31);
+        v0[k] = x0 - v0[k];          // exclusive, inside the bucket
+        v1[k] = t0 + x1 - v1[k];
+        if (lane == 0) bstart[w * kScanPerWarp + k] = t0 + t1;   // bucket total for now
+    }
+    __syncthreads();
+    // Exclusive scan of the bucket totals (kCoarse <= threads) and the largest bucket.
+    int tot = tid < kCoarse ? bstart[tid] : 0;
+    int incl = tot;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    unsigned long long big = tot ? ((unsigned long long)tot << 32) | (unsigned long long)tid : 0ull;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) big = max(big, __shfl_xor_sync(0xFFFFFFFFu, big, o));
+    if (lane == 31) wsum[w] = incl;
+    if (lane == 0) wbig[w] = big;
+    __syncthreads();
+    if (w == 0) {
+        const int v = wsum[lane];
+        int vi = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xFFFFFFFFu, vi, o);
+            if (lane >= o) vi += y;
+        }
+        wsum[lane] = vi - v;
+        unsigned long long bb = wbig[lane];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) bb = max(bb, __shfl_xor_sync(0xFFFFFFFFu, bb, o));
+        if (lane == 0) {
+            a.ctl->tb_big = bb;
+            a.ctl->tb_ticket = 0;
+        }
+    }
+    __syncthreads();
+    if (tid < kCoarse) {
+        const int excl = wsum[w] + incl - tot;
+        bstart[tid] = excl;
+        a.tb_bstart[tid] = excl;
+        if (tid == kCoarse - 1) a.tb_bstart[kCoarse] = excl + tot;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kScanPerWarp; ++k) {
+        const int b = w * kScanPerWarp + k;
+        int32_t* o = a.tb_base + (size_t)b * kTbChunks;
+        if (lane < chunks) o[lane] = bstart[b] + v0[k];
+        if (lane + 32 < chunks) o[lane + 32] = bstart[b] + v1[k];
+    }
+}
+
 __global__ void __launch_bounds__(kTbThreads) k_tb_insert(ExactState a) {
     if (a.ctl->P >= a.ctl->n) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         a.ctl->first_change = kNoChange;
         a.ctl->nhot = 0;
-        a.ctl->tb_big = 0;
     }
     tb_insert_chunk(a, a.ctl, blockIdx.x);
+    // The last CTA to finish scans every CTA's histogram.
+    __shared__ bool s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(&a.ctl->tb_ticket, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (s_last) {
+        __threadfence();
+        tb_scan_hist(a, (int)gridDim.x);
+    }
 }
 
 // Stable scatter of each chunk's events to their coarse buckets.  Warp w of a
 // chunk owns its 32 consecutive vertices, i.e. 64 consecutive events.
 __device__ __forceinline__ void tb_group_chunk(const ExactState& a, const Ctl* c, int chunk, int chunks) {
     __shared__ int32_t base[kCoarse];
-    __shared__ int32_t warp_sum[32];
     extern __shared__ int32_t wcnt[];   // warps x kCoarse
     const long long P = c->P, E = c->E;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int nwarps = blockDim.x >> 5;
     const int W = (int)(E - P);
-    // Bucket totals over all chunks and this chunk's offset inside each bucket.
-    int tot = 0, pre = 0;
-    if (tid < kCoarse) {
-        // Eight chunk counts in flight per step.
-        const int32_t* h = a.tb_hist + tid * kTbChunks;   // bucket tid's counts, one per chunk
-        for (int c0 = 0; c0 < chunks; c0 += 8) {
-            int v[8];
-#pragma unroll
-            for (int k = 0; k < 8; ++k) v[k] = c0 + k < chunks ? h[c0 + k] : 0;
-#pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                tot += v[k];
-                if (c0 + k < chunk) pre += v[k];
-            }
-        }
-    }
-    // Exclusive scan of the totals (kCoarse <= threads).
-    int incl = tot;
-    for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-        if (lane >= o) incl += y;
-    }
-    if (lane == 31) warp_sum[w] = incl;
-    __syncthreads();
-    if (w == 0) {
-        const int v = lane < nwarps ? warp_sum[lane] : 0;
-        int vi = v;
-        for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(0xFFFFFFFFu, vi, o);
-            if (lane >= o) vi += y;
-        }
-        warp_sum[lane] = vi - v;
-    }
-    __syncthreads();
-    const int excl = warp_sum[w] + incl - tot;
-    if (tid < kCoarse) {
-        base[tid] = excl + pre;
-        if (chunk == 0) {
-            a.tb_bstart[tid] = excl;
-            if (tid == kCoarse - 1) a.tb_bstart[kCoarse] = excl + tot;
-            if (tot) atomicMax(&a.ctl->tb_big, ((unsigned long long)tot << 32) | (unsigned long long)tid);
-        }
-    }
+    (void)chunks;
+    // This chunk's offset inside each bucket (scanned by the last insert CTA).
+    for (int b = tid; b < kCoarse; b += blockDim.x) base[b] = a.tb_base[b * kTbChunks + chunk];
     for (int k = tid; k < nwarps * kCoarse; k += blockDim.x) wcnt[k] = 0;
     __syncthreads();
     // Count per warp, then turn counts into per-warp offsets (exclusive over warps).
@@ -684,7 +738,8 @@ __device__ __forceinline__ void tb_finish_bucket(const ExactState& a, const Ctl*
     if (cnt == 0) return;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int nwarps = blockDim.x >> 5;
-    static_assert(kFine % 32 == 0 && kFine <= kTbMinChunk, "digit scan layout: one thread per fine digit");
+    static_assert(kFine % 32 == 0 && kFine <= kTbMinChunk && kFine <= kTbFinishThreads,
+                  "digit scan layout: one thread per fine digit");
     for (int k = tid; k < nwarps * kRow; k += blockDim.x) wcnt[k] = 0;
     __syncthreads();
     // Stable pass on the fine slot bits: warp w owns a contiguous range; the
@@ -1474,24 +1529,48 @@ __device__ __forceinline__ CommitView commit_view(const ExactState& a, const Ctl
 // Commit [cP, cX]: totals and memberships of movers, final deltas, processed
 // flags cleared, move flags for the affected-flag kernels; and the decided
 // window's hub tables cleared for the next round.
+// Adds (or, with neg, subtracts) v to total[key] once per distinct key of the
+// warp (kNone = no update); every lane of the warp calls it.  Degrees are
+// below 2^31, so the 16-bit halves of 32 of them sum without overflow.
+__device__ __forceinline__ void warp_add_total(unsigned long long* total, uint32_t key, uint32_t v, bool neg) {
+    const unsigned peers = __match_any_sync(0xFFFFFFFFu, key);
+    const unsigned lo = __reduce_add_sync(peers, v & 0xFFFFu), hi = __reduce_add_sync(peers, v >> 16);
+    if (key != kNone && (threadIdx.x & 31) == __ffs(peers) - 1) {
+        const long long sum = ((long long)hi << 16) + (long long)lo;
+        if (sum) atomicAdd(&total[key], (unsigned long long)(neg ? -sum : sum));
+    }
+}
+
 __device__ __forceinline__ void commit_a_body(const ExactState& a, const Ctl* ct) {
     const CommitView c = commit_view(a, ct);
     if (c.x < c.P) return;
-    for (long long u = c.P + blockIdx.x * (long long)blockDim.x + threadIdx.x; u <= c.x;
-         u += (long long)gridDim.x * blockDim.x) {
-        double dl = 0.0;
-        const uint32_t cur = a.vcom[u], nb = c.best[u];
-        const bool moves = c.act[u] == 1 && nb != cur;
-        if (moves) {
-            const long long deg = (long long)(a.rp[u + 1] - a.rp[u]);
-            atomicAdd(&a.ctot[cur], (unsigned long long)(-deg));
-            atomicAdd(&a.ctot[nb], (unsigned long long)deg);
-            dl = c.delta[u];
-            a.vcom[u] = nb;
+    // Warp-uniform loop: the total updates are summed per community inside
+    // the warp first (many movers of a window join the same few communities,
+    // and their atomics on one total would serialise).
+    const int lane = threadIdx.x & 31;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long base = c.P + ((blockIdx.x * (long long)blockDim.x + threadIdx.x) & ~31ll); base <= c.x;
+         base += stride) {
+        const long long u = base + lane;
+        bool moves = false;
+        uint32_t cur = kNone, nb = kNone;
+        uint32_t deg = 0;
+        if (u <= c.x) {
+            double dl = 0.0;
+            cur = a.vcom[u];
+            nb = c.best[u];
+            moves = c.act[u] == 1 && nb != cur;
+            if (moves) {
+                deg = (uint32_t)(a.rp[u + 1] - a.rp[u]);
+                dl = c.delta[u];
+                a.vcom[u] = nb;
+            }
+            a.mv[u] = moves;
+            a.final_delta[u] = dl;
+            a.vaff[u] = 0;
         }
-        a.mv[u] = moves;
-        a.final_delta[u] = dl;
-        a.vaff[u] = 0;
+        warp_add_total(a.ctot, moves ? cur : kNone, deg, true);
+        warp_add_total(a.ctot, moves ? nb : kNone, deg, false);
     }
     const long long q0 = ct->c_ts0, q1 = ct->c_ts1;
     __shared__ int s_last;
@@ -1527,16 +1606,41 @@ __global__ void k_ex_commit_a(ExactState a) { commit_a_body(a, a.ctl); }
 __device__ __forceinline__ void commit_b_body(const ExactState& a, const Ctl* ct) {
     const CommitView c = commit_view(a, ct);
     if (c.x < c.P) return;
+    // A thread per window vertex: rows of up to kOwnRow entries are flagged
+    // by their own thread (four entries in flight), longer ones by the whole
+    // warp, one row after another.
+    constexpr int kOwnRow = 16;
     const int lane = threadIdx.x & 31;
-    const long long wid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long w = c.P + wid; w <= c.x; w += nw) {
-        if (!a.mv[w]) continue;
-        const int64_t rb = a.rp[w], re = a.rp[w + 1];
-        if (re - rb > kWarpMaxDeg) continue;
-        for (int64_t e = rb + lane; e < re; e += 32) {
-            const int32_t v = a.col[e];
-            if (v < c.P || v > c.x || v < w) a.vaff[v] = 1;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long base = c.P + ((blockIdx.x * (long long)blockDim.x + threadIdx.x) & ~31ll); base <= c.x;
+         base += stride) {
+        const long long w = base + lane;
+        int64_t rb = 0, re = 0;
+        if (w <= c.x && a.mv[w]) {
+            rb = a.rp[w];
+            re = a.rp[w + 1];
+            if (re - rb > kWarpMaxDeg) re = rb;   // hubs and big rows: k_ex_commit_hub
+        }
+        if (re - rb <= kOwnRow) {
+            for (int64_t e0 = rb; e0 < re; e0 += 4) {
+                int32_t v[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) v[k] = e0 + k < re ? a.col[e0 + k] : -1;
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if (v[k] >= 0 && (v[k] < c.P || v[k] > c.x || v[k] < w)) a.vaff[v[k]] = 1;
+            }
+        }
+        unsigned longer = __ballot_sync(0xFFFFFFFFu, re - rb > kOwnRow);
+        while (longer) {
+            const int src = __ffs(longer) - 1;
+            longer &= longer - 1;
+            const long long ws = __shfl_sync(0xFFFFFFFFu, w, src);
+            const int64_t rbs = __shfl_sync(0xFFFFFFFFu, rb, src), res = __shfl_sync(0xFFFFFFFFu, re, src);
+            for (int64_t e = rbs + lane; e < res; e += 32) {
+                const int32_t v = a.col[e];
+                if (v < c.P || v > c.x || v < ws) a.vaff[v] = 1;
+            }
         }
     }
 }
@@ -1890,7 +1994,8 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     GB_CUDA(cudaMemsetAsync(slots, 0xFF, kTableSlots * sizeof(SlotMeta), s));   // no generation yet
     DevBuf<uint32_t> stime(kEventsMax, s), tb_s0(kWindowMax, s), tb_s1(kWindowMax, s);
     DevBuf<long long> epre(kEventsMax, s);
-    DevBuf<int32_t> wdeg(kWindowMax, s), tb_hist(kCoarse * kTbChunks, s), tb_bstart(kCoarse + 1, s);
+    DevBuf<int32_t> wdeg(kWindowMax, s), tb_hist(kCoarse * kTbChunks, s), tb_base(kCoarse * kTbChunks, s),
+        tb_bstart(kCoarse + 1, s);
     DevBuf<unsigned long long> ev1(kEventsMax, s), ev2(kEventsMax, s);
     DevBuf<int32_t> hot_bidx((size_t)kHotMax * kHotStride, s);
     DevBuf<uint8_t> zof(n > 0 ? n : 1, s);
@@ -1930,6 +2035,7 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     a.tb_s1 = tb_s1.get();
     a.wdeg = wdeg.get();
     a.tb_hist = tb_hist.get();
+    a.tb_base = tb_base.get();
     a.tb_bstart = tb_bstart.get();
     a.ev1 = ev1.get();
     a.ev2 = ev2.get();
@@ -2001,7 +2107,7 @@ int local_move_exact(const LocalMoveContext& ctx, double tolerance, int max_iter
     const int big_grid = resident((const void*)k_ex_eval_big, kBigThreads, big_smem);
     const int hub_grid = resident((const void*)k_ex_hub_accum, kHubThreads2, 0);
     const int commit_grid = (int)std::max<int64_t>(1, ceil_div(B, kT));
-    const int commit_b_grid = (int)std::max<int64_t>(1, ceil_div(B * 32, kT));
+    const int commit_b_grid = (int)std::max<int64_t>(1, ceil_div(B, kT));
     // eval_small, advance, 3 table kernels, commit_a, commit_b; eval_mid;
     // eval_big; hub_select + hub_accum; commit_hub (hubs or big rows).
     const int per_round = 7 + (n_mid ? 1 : 0) + (n_big ? 1 : 0) + (nh ? 2 : 0) + ((nh || n_big) ? 1 : 0);
