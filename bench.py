@@ -43,6 +43,9 @@ METRIC = "GPU reorder Medges/s vs host CPU; map+kernel time, learned vs frozen r
 SCALE = 22
 EDGE_FACTOR = 16
 CPU_BASELINE_RUNS = 5
+# Local-moving DRAM traffic per mapping of GAPBS -g 22 (ncu, warm L2):
+# 8.722 GB read + 4.728 GB written by the round kernels.
+LOCAL_MOVE_DRAM_BYTES_G22 = 13.449e9
 PINS_PATH = os.path.join(ROOT, "tests", "golden", "gapbs_pins.json")
 
 
@@ -371,9 +374,18 @@ def main():
         ach = b / (ms / 1e3) / 1e9 if ms > 0 else 0.0
         stages[k] = {"ms": ms, "algorithmic_bytes": b, "achieved_gbs": ach, "frac": ach / peak}
     dom = max(stages, key=lambda k: stages[k]["ms"])
+    # DRAM bytes (read + write) of the stage's kernels per mapping, from one
+    # ncu capture of this workload (profiles/launches_dram_gapbs22.md); only
+    # the GAPBS -g 22 workload was captured.
+    traffic = extra = None
+    if dom == "local_move" and args.scale == 22:
+        traffic = LOCAL_MOVE_DRAM_BYTES_G22
+        extra = {"per": "mapping: the stage's kernel launches summed, like achieved",
+                 "ratio_to_algorithmic": LOCAL_MOVE_DRAM_BYTES_G22 / stage_bytes[dom],
+                 "source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, warm L2, one full-size capture"}
     roofline = {"bound": "hbm", "kernel": dom + " (stage: its kernels' launches per mapping)",
                 "achieved": stages[dom]["achieved_gbs"], "peak": peak, "unit": "GB/s",
-                "frac": stages[dom]["frac"], "peak_source": peak_kind, "traffic": None,
+                "frac": stages[dom]["frac"], "peak_source": peak_kind, "traffic": traffic, "traffic_detail": extra,
                 "algorithmic_bytes_per_launch": stage_bytes[dom], "stages": stages,
                 "local_move_rounds": avg("local_move_rounds"),
                 "note": "serial-order local moving is bound by the latency of its dependent rounds, not by HBM"}
