@@ -143,6 +143,15 @@ double orc_modularity(const orc_graph *g, const uint32_t *membership,
 /* Number of OpenMP threads the library was built to use (1 without OpenMP). */
 int orc_max_threads(void);
 
+/* The reference's CPU benchmark kernels (gb_kernels_cpu.c), for timing the
+ * selector's arms on the host; each returns its wall time in ms.
+ * `threads` <= 0 keeps the OpenMP default. */
+double orc_pagerank_gs(const orc_graph *g, int max_iters, double epsilon, float *scores, int threads,
+                       int *iters_out);
+double orc_bfs_do(const orc_graph *g, int64_t source, int32_t *depth, int threads);
+double orc_cc_afforest(const orc_graph *g, int32_t *comp, int threads);
+double orc_dbg_cpu(const orc_graph *g, int32_t *new_ids, int threads);
+
 #ifdef __cplusplus
 }
 #endif

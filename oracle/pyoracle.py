@@ -24,6 +24,7 @@ REF_SO = os.path.join(HERE, "_ref", "libgbref.so")
 _i64p = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
 _i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 _u32p = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
+_f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
 
 # Algorithm-12 defaults (reorder_types.h:213-226) for the GVE-style path.
 DEFAULT_TOLERANCE = 1e-2
@@ -120,6 +121,15 @@ def load():
         lib.orc_max_threads.restype = C.c_int
         lib.orc_libstdcxx_sort.argtypes = [_u32p, C.c_int64, _u64p]
         lib.orc_libstdcxx_heap_sort.argtypes = [_u32p, C.c_int64, _u64p]
+        lib.orc_pagerank_gs.restype = C.c_double
+        lib.orc_pagerank_gs.argtypes = [C.POINTER(Graph), C.c_int, C.c_double, _f32p, C.c_int,
+                                        C.POINTER(C.c_int)]
+        lib.orc_bfs_do.restype = C.c_double
+        lib.orc_bfs_do.argtypes = [C.POINTER(Graph), C.c_int64, _i32p, C.c_int]
+        lib.orc_cc_afforest.restype = C.c_double
+        lib.orc_cc_afforest.argtypes = [C.POINTER(Graph), _i32p, C.c_int]
+        lib.orc_dbg_cpu.restype = C.c_double
+        lib.orc_dbg_cpu.argtypes = [C.POINTER(Graph), _i32p, C.c_int]
         _lib = lib
     return _lib
 
@@ -397,6 +407,40 @@ def dbg_mapping(row_ptr, col):
     ids = np.empty(n, dtype=np.int32)
     ids[order] = np.arange(n, dtype=np.int32)
     return ids
+
+
+# ---- the reference's CPU benchmark kernels (OpenMP; for timing arms) ----
+def pagerank_cpu(row_ptr, col, max_iters=20, epsilon=1e-4, threads=0):
+    """PageRank pull, Gauss-Seidel (bench/src/pr.cc:40-90): (scores, iterations, ms)."""
+    g, keep = _as_graph(row_ptr, col)
+    out = np.zeros(g.n, dtype=np.float32)
+    it = C.c_int()
+    ms = load().orc_pagerank_gs(C.byref(g), int(max_iters), float(epsilon), out, int(threads), C.byref(it))
+    return out, it.value, ms
+
+
+def bfs_cpu(row_ptr, col, source, threads=0):
+    """Direction-optimizing BFS (bench/src/bfs.cc): (depths, ms)."""
+    g, keep = _as_graph(row_ptr, col)
+    out = np.zeros(g.n, dtype=np.int32)
+    ms = load().orc_bfs_do(C.byref(g), int(source), out, int(threads))
+    return out, ms
+
+
+def cc_cpu(row_ptr, col, threads=0):
+    """Afforest connected components (bench/src/cc.cc): (component ids, ms)."""
+    g, keep = _as_graph(row_ptr, col)
+    out = np.zeros(g.n, dtype=np.int32)
+    ms = load().orc_cc_afforest(C.byref(g), out, int(threads))
+    return out, ms
+
+
+def dbg_cpu(row_ptr, col, threads=0):
+    """GenerateDBGMapping on the host cores: (new ids, ms)."""
+    g, keep = _as_graph(row_ptr, col)
+    out = np.zeros(g.n, dtype=np.int32)
+    ms = load().orc_dbg_cpu(C.byref(g), out, int(threads))
+    return out, ms
 
 
 def bfs_depths(row_ptr, col, source):

@@ -94,3 +94,40 @@ def test_pagerank_fixed_point():
     contrib = np.where(deg > 0, s / np.maximum(deg, 1), 0.0)
     inc = np.bincount(np.repeat(np.arange(n), np.diff(rp)), weights=contrib[col], minlength=n)
     np.testing.assert_allclose(s, 0.15 / n + 0.85 * inc, rtol=1e-10, atol=1e-15)
+
+
+# ---- the OpenMP CPU kernels used to time the selector's arms on the host ----
+@pytest.mark.parametrize("kind", ["planted", "rmat", "grid"])
+def test_cpu_kernels_against_scipy(kind):
+    if kind == "planted":
+        rp, col, _ = gg.planted_partition(20000, 8, degree=4, mixing=0.01, seed=3)
+    elif kind == "rmat":
+        rp, col = gg.rmat(15, 8, seed=4)
+    else:
+        rp, col = gg.grid(150, 160, 0.1, seed=5)
+    rp, col = rp.numpy(), col.numpy()
+    A = _scipy_graph(rp, col)
+    src = int(np.argmax(np.diff(rp)))
+    dist = csg.shortest_path(A, unweighted=True, indices=src)
+    want = np.where(np.isinf(dist), -1, dist).astype(np.int32)
+    for threads in (1, 4):
+        got, ms = po.bfs_cpu(rp, col, src, threads=threads)
+        np.testing.assert_array_equal(got, want)
+        assert ms >= 0
+        comp, _ = po.cc_cpu(rp, col, threads=threads)
+        _, labels = csg.connected_components(A, directed=False)
+        # same partition: component ids map one to one
+        pairs = set(zip(comp.tolist(), labels.tolist()))
+        assert len(pairs) == len(set(comp.tolist())) == len(set(labels.tolist()))
+    ids, _ = po.dbg_cpu(rp, col, threads=4)
+    np.testing.assert_array_equal(ids, po.dbg_mapping(rp, col))
+
+
+def test_cpu_pagerank_matches_fixed_point():
+    rp, col = gg.rmat(14, 8, seed=6)
+    rp, col = rp.numpy(), col.numpy()
+    ref = po.pagerank(rp, col, max_iters=200, epsilon=1e-12)
+    got, iters, ms = po.pagerank_cpu(rp, col, max_iters=200, epsilon=1e-9, threads=4)
+    assert iters < 200 and ms >= 0
+    # float32 scores, Gauss-Seidel sweeps: the same fixed point to float accuracy
+    np.testing.assert_allclose(got, ref, rtol=2e-3, atol=1e-9)
