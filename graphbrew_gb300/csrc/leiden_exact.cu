@@ -1030,30 +1030,22 @@ __device__ __forceinline__ void eval_vertex(const ExactState& a, const Round& r,
             cnt += __popc(bal);
             __syncwarp();
         }
-        // Four candidates per lane per step, interleaved; the first step also
-        // looks up sigma of d.
+        // One candidate per lane per step, its lookup interleaved with d's in
+        // the first step (wider interleaving costs registers, and occupancy
+        // matters more here: 64 registers, 28 warps per SM).
         long long sd = 0;
-        for (uint32_t i0 = 0;; i0 += 128) {
-            uint32_t cc[5];
-            bool vv[5];
-            long long sg[5];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const uint32_t i = i0 + 32 * k + lane;
-                vv[k] = i < cnt;
-                cc[k] = vv[k] ? tk[i] : kNone;
+        for (uint32_t i0 = 0;; i0 += 32) {
+            const uint32_t i = i0 + lane;
+            const uint32_t cc[2] = {i < cnt ? tk[i] : kNone, d};
+            const bool vv[2] = {i < cnt, i0 == 0};
+            long long sg[2];
+            sigma_at_k<2>(a, r.tag, r.P, r.par, cc, vv, (uint32_t)u, sg);
+            if (i0 == 0) sd = sg[1];
+            if (vv[0]) {
+                const double dl = delta_qi(a.dq, tv[i], kud, deg, sg[0], sd);
+                if (dpos(dl) && better_pos(dl, cc[0], best_d, best_c)) { best_d = dl; best_c = cc[0]; }
             }
-            cc[4] = d;
-            vv[4] = i0 == 0;
-            sigma_at_k<5>(a, r.tag, r.P, r.par, cc, vv, (uint32_t)u, sg);
-            if (i0 == 0) sd = sg[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                if (!vv[k]) continue;
-                const double dl = delta_qi(a.dq, tv[i0 + 32 * k + lane], kud, deg, sg[k], sd);
-                if (dpos(dl) && better_pos(dl, cc[k], best_d, best_c)) { best_d = dl; best_c = cc[k]; }
-            }
-            if (i0 + 128 >= cnt) break;
+            if (i0 + 32 >= cnt) break;
         }
         __syncwarp();
         if (refine_stays(a, (double)sd, ku)) best_c = kNone;   // every lane holds the same sd
@@ -1166,8 +1158,9 @@ __global__ void __launch_bounds__(kSmallWarpsPerBlock * 32) k_ex_eval_small(Exac
 }
 
 // Big rows (kWarpMaxDeg < degree <= kBigMaxDeg): one CTA per row, table in
-// shared memory, candidates compacted, lookups of four per thread interleaved.
-// Three CTAs per SM (registers capped near 80): more lookups in flight.
+// shared memory, candidates compacted, one candidate per thread per step (its
+// lookup interleaved with d's in the first step; wider interleaving spilled
+// under the register cap).  Three CTAs per SM (registers capped near 80).
 __device__ __forceinline__ void eval_big_body(const ExactState& a, const Ctl* c) {
     extern __shared__ uint32_t big_smem[];
     uint32_t* tk = big_smem;                      // kBigSlots keys
@@ -1245,27 +1238,18 @@ __device__ __forceinline__ void eval_big_body(const ExactState& a, const Ctl* c)
         double best_d = 0.0;
         uint32_t best_c = kNone;
         long long sd = 0;
-        for (uint32_t i0 = 0;; i0 += 4 * blockDim.x) {
-            uint32_t cc[5];
-            bool vv[5];
-            long long sg[5];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const uint32_t i = i0 + k * blockDim.x + tid;
-                vv[k] = i < cnt;
-                cc[k] = vv[k] ? cand_c[i] : kNone;
+        for (uint32_t i0 = 0;; i0 += blockDim.x) {
+            const uint32_t i = i0 + tid;
+            const uint32_t cc[2] = {i < cnt ? cand_c[i] : kNone, d};
+            const bool vv[2] = {i < cnt, i0 == 0};
+            long long sg[2];
+            sigma_at_k<2>(a, r.tag, r.P, r.par, cc, vv, u, sg);
+            if (i0 == 0) sd = sg[1];
+            if (vv[0]) {
+                const double dl = delta_qi(a.dq, cand_w[i], kud, deg, sg[0], sd);
+                if (dpos(dl) && better_pos(dl, cc[0], best_d, best_c)) { best_d = dl; best_c = cc[0]; }
             }
-            cc[4] = d;
-            vv[4] = i0 == 0;
-            sigma_at_k<5>(a, r.tag, r.P, r.par, cc, vv, u, sg);
-            if (i0 == 0) sd = sg[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                if (!vv[k]) continue;
-                const double dl = delta_qi(a.dq, cand_w[i0 + k * blockDim.x + tid], kud, deg, sg[k], sd);
-                if (dpos(dl) && better_pos(dl, cc[k], best_d, best_c)) { best_d = dl; best_c = cc[k]; }
-            }
-            if (i0 + 4 * blockDim.x >= cnt) break;
+            if (i0 + blockDim.x >= cnt) break;
         }
         warp_argmax_pos(best_d, best_c);
         if (lane == 0) { red_d[w] = best_d; red_c[w] = best_c; }
@@ -1409,29 +1393,24 @@ __device__ __forceinline__ void hub_select_body(const ExactState& a, const Ctl* 
         double best_d = 0.0;
         uint32_t best_c = kNone;
         // Segment `part` covers occupied-list positions [s0, s0 + kTabSeg):
-        // four per thread, lookups interleaved with the one for d.
+        // one per thread per step, the first step's lookup interleaved with
+        // the one for d.
         const uint32_t s0 = (uint32_t)sg.part * kTabSeg, s1 = min(nocc, s0 + kTabSeg);
         if (s0 < s1) {
-            uint32_t cc[5], cw[4];
-            bool vv[5];
-            long long sgm[5];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const uint32_t i = s0 + (uint32_t)k * blockDim.x + threadIdx.x;
+            long long sd = 0;
+            for (uint32_t i0 = s0; i0 < s1; i0 += blockDim.x) {
+                const uint32_t i = i0 + threadIdx.x;
                 const uint32_t slot = i < s1 ? occ[i] : 0u;
-                cc[k] = i < s1 ? tk[slot] : kNone;
-                cw[k] = i < s1 ? tv[slot] : 0;
-                vv[k] = cc[k] != kNone && cc[k] != d;
-            }
-            cc[4] = d;
-            vv[4] = true;
-            sigma_at_k<5>(a, r.tag, r.P, r.par, cc, vv, h, sgm);
-            const long long sd = sgm[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                if (!vv[k]) continue;
-                const double dl = delta_qi(a.dq, cw[k], kud, ku, sgm[k], sd);
-                if (dpos(dl) && better_pos(dl, cc[k], best_d, best_c)) { best_d = dl; best_c = cc[k]; }
+                const uint32_t c0 = i < s1 ? tk[slot] : kNone, w0 = i < s1 ? tv[slot] : 0;
+                const uint32_t cc[2] = {c0, d};
+                const bool vv[2] = {c0 != kNone && c0 != d, i0 == s0};
+                long long sgm[2];
+                sigma_at_k<2>(a, r.tag, r.P, r.par, cc, vv, h, sgm);
+                if (i0 == s0) sd = sgm[1];
+                if (vv[0]) {
+                    const double dl = delta_qi(a.dq, w0, kud, ku, sgm[0], sd);
+                    if (dpos(dl) && better_pos(dl, c0, best_d, best_c)) { best_d = dl; best_c = c0; }
+                }
             }
         }
         warp_argmax_pos(best_d, best_c);
