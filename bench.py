@@ -337,14 +337,18 @@ def main():
         for _ in range(2):
             host_step()
         t0 = time.perf_counter()
-        host_stats = [host_step() for _ in range(args.steps)]
-        t1 = time.perf_counter()
+        host_stats, marks = [], [t0]
+        for _ in range(args.steps):
+            host_stats.append(host_step())
+            marks.append(time.perf_counter())
+        t1 = marks[-1]
         assert gb.mapping_fingerprint(h_ids.numpy()) == fp
         e2e_s = (t1 - t0) / args.steps
         return {"value": nnz * world / e2e_s / 1e6, "unit": "Medges/s",
                 "h2d_bytes_per_step": 8 * (n + 1) + 4 * nnz,
                 "d2h_bytes_per_step": 4 * n + 8 * (n + 1) + 4 * nnz,
                 "ms_per_step": e2e_s * 1e3, "host_buffers": "pinned" if pinned else "pageable",
+                "step_wall_ms": [round((b - a) * 1e3, 2) for a, b in zip(marks, marks[1:])],
                 "h2d_ms": float(np.median([x.h2d_ms for x in host_stats])),
                 "d2h_ms": float(np.median([x.d2h_ms for x in host_stats])),
                 "call_device_ms": float(np.median([x.total_ms for x in host_stats])),
