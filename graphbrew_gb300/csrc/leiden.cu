@@ -1019,6 +1019,83 @@ __global__ void k_hub_emit(const int32_t* __restrict__ flag, const int64_t* __re
         if (flag[v]) hubs[pos[v]] = (uint32_t)v;
 }
 
+// ---- Local moving over the vertices that have neighbours ----
+// A vertex without neighbours never moves and is never a candidate, so its
+// community is a singleton that no other vertex can reach.  Local moving
+// runs on the graph without those vertices, renumbered in id order (the
+// rows keep their offsets: removed rows are empty), and on the communities
+// of the remaining vertices renumbered in id order: both maps are monotone,
+// so the serial order and every id tie-break are the same.
+__global__ void k_nonisolated_flags(const int64_t* __restrict__ rp, int64_t n, int32_t* __restrict__ flag) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
+        flag[v] = rp[v + 1] > rp[v] ? 1 : 0;
+}
+
+__global__ void k_compact_rows(const int64_t* __restrict__ rp, const int32_t* __restrict__ flag,
+                               const int64_t* __restrict__ pos, int64_t n, int64_t* __restrict__ rp_c,
+                               uint32_t* __restrict__ orig) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
+        if (flag[v]) {
+            rp_c[pos[v]] = rp[v];
+            orig[pos[v]] = (uint32_t)v;
+        }
+}
+
+__global__ void k_compact_cols(const int32_t* __restrict__ col, int64_t nnz, const int64_t* __restrict__ pos,
+                               int32_t* __restrict__ col_c) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nnz; e += (int64_t)gridDim.x * blockDim.x)
+        col_c[e] = (int32_t)pos[col[e]];
+}
+
+__global__ void k_map_u32(const uint32_t* __restrict__ in, int64_t m, const int64_t* __restrict__ pos,
+                          uint32_t* __restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (uint32_t)pos[in[i]];
+}
+
+// cflag[c] = 1 for every community of a kept vertex.
+__global__ void k_comm_flags(const uint32_t* __restrict__ vcom, const uint32_t* __restrict__ orig, int64_t nc,
+                             int32_t* __restrict__ cflag) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nc; i += (int64_t)gridDim.x * blockDim.x)
+        cflag[vcom[orig[i]]] = 1;
+}
+
+__global__ void k_comm_inverse(const int32_t* __restrict__ cflag, const int64_t* __restrict__ cpos, int64_t n,
+                               uint32_t* __restrict__ cinv) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x)
+        if (cflag[c]) cinv[cpos[c]] = (uint32_t)c;
+}
+
+__global__ void k_gather_state(const uint32_t* __restrict__ orig, int64_t nc, const uint32_t* __restrict__ vcom,
+                               const uint8_t* __restrict__ vaff, const uint32_t* __restrict__ vcob,
+                               const int64_t* __restrict__ cpos, uint32_t* __restrict__ vcom_c,
+                               uint8_t* __restrict__ vaff_c, uint32_t* __restrict__ vcob_c) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nc; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t v = orig[i];
+        vcom_c[i] = (uint32_t)cpos[vcom[v]];
+        vaff_c[i] = vaff[v];
+        if (vcob) vcob_c[i] = vcob[v];
+    }
+}
+
+__global__ void k_gather_totals(const uint32_t* __restrict__ cinv, int64_t cc, const unsigned long long* __restrict__ ctot,
+                                unsigned long long* __restrict__ ctot_c) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < cc; i += (int64_t)gridDim.x * blockDim.x)
+        ctot_c[i] = ctot[cinv[i]];
+}
+
+__global__ void k_scatter_state(const uint32_t* __restrict__ orig, int64_t nc, const uint32_t* __restrict__ vcom_c,
+                                const uint32_t* __restrict__ cinv, uint32_t* __restrict__ vcom) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nc; i += (int64_t)gridDim.x * blockDim.x)
+        vcom[orig[i]] = cinv[vcom_c[i]];
+}
+
+__global__ void k_scatter_totals(const uint32_t* __restrict__ cinv, int64_t cc,
+                                 const unsigned long long* __restrict__ ctot_c, unsigned long long* __restrict__ ctot) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < cc; i += (int64_t)gridDim.x * blockDim.x)
+        ctot[cinv[i]] = ctot_c[i];
+}
+
 template <typename T>
 T read_dev(const T* p, cudaStream_t s) {
     T h;
@@ -1185,10 +1262,104 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
     lmc.hub_gcap = hub_gcap;
     int64_t exact_rounds = 0, exact_evals = 0;
 
+    // The serial-order engine runs without the vertices that have no
+    // neighbours when they are at least a sixteenth of the graph (RMAT
+    // graphs: ~40 %): they would take window slots and rounds while never
+    // moving (see k_nonisolated_flags).
+    struct Compacted {
+        int64_t nc = 0;
+        DevBuf<int64_t> pos, rp, cpos;
+        DevBuf<int32_t> col, cflag;
+        DevBuf<uint32_t> orig, hubs, vcom, vcob, cinv;
+        DevBuf<unsigned long long> ctot;
+        DevBuf<uint8_t> vaff;
+        LocalMoveContext lmc;
+    } cp;
+    bool compact = false;
+    if (exact && n > 0) {
+        DevBuf<int32_t> flag(n, s);
+        cp.pos.alloc(n + 1, s);
+        k_nonisolated_flags<<<grid_for(n, kT), kT, 0, s>>>(g.row_ptr, n, flag);
+        GB_LAUNCH_CHECK();
+        exclusive_scan_i32_to_i64(flag, cp.pos, n, cp.pos.get() + n, s);
+        cp.nc = read_dev(cp.pos.get() + n, s);
+        launches += 3;
+        if (cp.nc > 0 && (n - cp.nc) * 16 >= n) {
+            compact = true;
+            const int64_t nc = cp.nc;
+            cp.rp.alloc(nc + 1, s);
+            cp.orig.alloc(nc, s);
+            k_compact_rows<<<grid_for(n, kT), kT, 0, s>>>(g.row_ptr, flag, cp.pos, n, cp.rp, cp.orig);
+            GB_LAUNCH_CHECK();
+            GB_CUDA(cudaMemcpyAsync(cp.rp.get() + nc, g.row_ptr + n, sizeof(int64_t), cudaMemcpyDeviceToDevice, s));
+            cp.col.alloc(g.nnz > 0 ? g.nnz : 1, s);
+            if (g.nnz > 0) {
+                k_compact_cols<<<grid_for(g.nnz, kT), kT, 0, s>>>(g.col, g.nnz, cp.pos, cp.col);
+                GB_LAUNCH_CHECK();
+            }
+            cp.lmc = lmc;
+            cp.lmc.g = DeviceCSR{nc, g.nnz, cp.rp.get(), cp.col.get()};
+            if (!hubs_h.empty()) {
+                const int64_t nh = (int64_t)hubs_h.size();
+                cp.hubs.alloc(nh, s);
+                k_map_u32<<<grid_for(nh, kT), kT, 0, s>>>(hubs, nh, cp.pos, cp.hubs);
+                GB_LAUNCH_CHECK();
+                GB_CUDA(cudaMemcpyAsync(cp.lmc.hubs_h.data(), cp.hubs.get(), nh * sizeof(uint32_t),
+                                        cudaMemcpyDeviceToHost, s));
+                GB_CUDA(cudaStreamSynchronize(s));
+                cp.lmc.hubs = cp.hubs.get();
+            }
+            cp.vcom.alloc(nc, s);
+            cp.vaff.alloc(nc, s);
+            cp.ctot.alloc(nc, s);
+            cp.cinv.alloc(nc, s);
+            cp.cflag.alloc(n, s);
+            cp.cpos.alloc(n + 1, s);
+            cp.lmc.vcom = cp.vcom.get();
+            cp.lmc.vaff = cp.vaff.get();
+            cp.lmc.ctot = cp.ctot.get();
+            launches += 3 + (hubs_h.empty() ? 0 : 1);
+        }
+    }
+    // One call of the serial-order engine on the current membership (vcob:
+    // refinement bounds or null), through the compacted graph when there is one.
+    auto run_exact = [&](double tolerance, int max_iterations, const uint32_t* vcob) -> int {
+        if (!compact) {
+            lmc.vcob = vcob;
+            const int it = local_move_exact(lmc, tolerance, max_iterations, p.exact_window, s, &launches,
+                                            &exact_rounds, &exact_evals);
+            lmc.vcob = nullptr;
+            return it;
+        }
+        const int64_t nc = cp.nc;
+        GB_CUDA(cudaMemsetAsync(cp.cflag, 0, n * sizeof(int32_t), s));
+        k_comm_flags<<<grid_for(nc, kT), kT, 0, s>>>(vcom, cp.orig, nc, cp.cflag);
+        GB_LAUNCH_CHECK();
+        exclusive_scan_i32_to_i64(cp.cflag, cp.cpos, n, cp.cpos.get() + n, s);
+        const int64_t cc = read_dev(cp.cpos.get() + n, s);
+        k_comm_inverse<<<grid_for(n, kT), kT, 0, s>>>(cp.cflag, cp.cpos, n, cp.cinv);
+        GB_LAUNCH_CHECK();
+        if (vcob && !cp.vcob) cp.vcob.alloc(nc, s);
+        k_gather_state<<<grid_for(nc, kT), kT, 0, s>>>(cp.orig, nc, vcom, vaff, vcob, cp.cpos, cp.vcom, cp.vaff,
+                                                       vcob ? cp.vcob.get() : nullptr);
+        GB_LAUNCH_CHECK();
+        GB_CUDA(cudaMemsetAsync(cp.ctot, 0, nc * sizeof(unsigned long long), s));
+        k_gather_totals<<<grid_for(cc, kT), kT, 0, s>>>(cp.cinv, cc, ctot, cp.ctot);
+        GB_LAUNCH_CHECK();
+        cp.lmc.vcob = vcob ? cp.vcob.get() : nullptr;
+        const int it = local_move_exact(cp.lmc, tolerance, max_iterations, p.exact_window, s, &launches,
+                                        &exact_rounds, &exact_evals);
+        cp.lmc.vcob = nullptr;
+        k_scatter_state<<<grid_for(nc, kT), kT, 0, s>>>(cp.orig, nc, cp.vcom, cp.cinv, vcom);
+        GB_LAUNCH_CHECK();
+        k_scatter_totals<<<grid_for(cc, kT), kT, 0, s>>>(cp.cinv, cc, cp.ctot, ctot);
+        GB_LAUNCH_CHECK();
+        launches += 9;
+        return it;
+    };
+
     auto local_move = [&](double tolerance) -> int {
-        if (exact)
-            return local_move_exact(lmc, tolerance, p.max_iterations, p.exact_window, s, &launches, &exact_rounds,
-                                    &exact_evals);
+        if (exact) return run_exact(tolerance, p.max_iterations, nullptr);
         int iters = 0;
         for (int it = 0; it < p.max_iterations; ++it) {
             GB_CUDA(cudaMemsetAsync(dacc, 0, sizeof(double), s));
@@ -1252,9 +1423,7 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
             k_init_state<<<grid_for(n, kT), kT, 0, s>>>(g.row_ptr, n, vcom, ctot, vaff);
             GB_LAUNCH_CHECK();
             ++launches;
-            lmc.vcob = vcob.get();
-            local_move_exact(lmc, tolerance, 1, p.exact_window, s, &launches, &exact_rounds, &exact_evals);
-            lmc.vcob = nullptr;
+            run_exact(tolerance, 1, vcob.get());
         }
         GB_CUDA(cudaEventRecord(eb, s));
         GB_CUDA(cudaEventSynchronize(eb));
