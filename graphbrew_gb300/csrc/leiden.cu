@@ -470,6 +470,9 @@ struct SmArgs {
     uint32_t* hvals;
     double* part_d;               // best of each table segment
     uint32_t* part_c;
+    // 1/M as a double-double (make_dq): quotients by M are formed by
+    // div_rn_by, bit-identical to full divisions at a fraction of the FP64 work.
+    double yMh = 0.0, yMl = 0.0;
 };
 
 constexpr int kSmSmall = 256;     // per-warp shared table slots
@@ -551,7 +554,7 @@ __device__ void super_propose_cached(const SmArgs& a, uint32_t c, uint32_t* tk, 
     __syncwarp();
     const double kc = (double)kcl;
     const double sigma_d = (double)(long long)sd_raw;
-    const double removal = __ddiv_rn(__dmul_rn(__dmul_rn(a.R, kc), __dsub_rn(sigma_d, kc)), a.M);
+    const double removal = div_rn_by(__dmul_rn(__dmul_rn(a.R, kc), __dsub_rn(sigma_d, kc)), a.M, a.yMh, a.yMl);
     const double kc_to_d = (double)table_get(k, v, mask, d);
     double best_d = 0.0;
     uint32_t best_c = d;
@@ -564,7 +567,7 @@ __device__ void super_propose_cached(const SmArgs& a, uint32_t c, uint32_t* tk, 
             add = __dsub_rn(kc_to_d, removal);
         } else {
             const double se = (double)(long long)(shared ? tt[i] : a.sctot[ek]);
-            add = __dsub_rn(kce, __ddiv_rn(__dmul_rn(__dmul_rn(a.R, kc), se), a.M));
+            add = __dsub_rn(kce, div_rn_by(__dmul_rn(__dmul_rn(a.R, kc), se), a.M, a.yMh, a.yMl));
         }
         const double dl = __dadd_rn(__dsub_rn(add, removal), kc_to_d);
         if (better(dl, ek, best_d, best_c)) { best_d = dl; best_c = ek; }
@@ -597,7 +600,7 @@ __device__ void super_propose_block(const SmArgs& a, uint32_t c, SmProposal* out
 #pragma unroll 4
     for (int64_t idx = b + tid; idx < e; idx += blockDim.x) table_add(k, v, mask, a.scomm[a.snbr[idx]], a.sw[idx]);
     __syncthreads();
-    const double removal = __ddiv_rn(__dmul_rn(__dmul_rn(a.R, kc), __dsub_rn(sigma_d, kc)), a.M);
+    const double removal = div_rn_by(__dmul_rn(__dmul_rn(a.R, kc), __dsub_rn(sigma_d, kc)), a.M, a.yMh, a.yMl);
     const double kc_to_d = (double)table_get(k, v, mask, d);
     double best_d = 0.0;
     uint32_t best_c = d;
@@ -611,7 +614,7 @@ __device__ void super_propose_block(const SmArgs& a, uint32_t c, SmProposal* out
             add = __dsub_rn(kc_to_d, removal);
         } else {
             const double se = (double)(long long)a.sctot[ek];
-            add = __dsub_rn(kce, __ddiv_rn(__dmul_rn(__dmul_rn(a.R, kc), se), a.M));
+            add = __dsub_rn(kce, div_rn_by(__dmul_rn(__dmul_rn(a.R, kc), se), a.M, a.yMh, a.yMl));
         }
         const double dl = __dadd_rn(__dsub_rn(add, removal), kc_to_d);
         if (better(dl, ek, best_d, best_c)) { best_d = dl; best_c = ek; }
@@ -676,7 +679,7 @@ __device__ void super_propose_light(const SmArgs& a, uint32_t c, SmProposal& out
         if (key[k] == d) kc_to_d_w = wsum[k];
     const double kc = (double)kcl;
     const double sigma_d = (double)(long long)sd_raw;
-    const double removal = __ddiv_rn(__dmul_rn(__dmul_rn(a.R, kc), __dsub_rn(sigma_d, kc)), a.M);
+    const double removal = div_rn_by(__dmul_rn(__dmul_rn(a.R, kc), __dsub_rn(sigma_d, kc)), a.M, a.yMh, a.yMl);
     const double kc_to_d = (double)kc_to_d_w;
     double best_d = 0.0;
     uint32_t best_c = d;
@@ -689,7 +692,7 @@ __device__ void super_propose_light(const SmArgs& a, uint32_t c, SmProposal& out
             add = __dsub_rn(kc_to_d, removal);
         } else {
             const double se = (double)(long long)se_raw[k];
-            add = __dsub_rn((double)wsum[k], __ddiv_rn(__dmul_rn(__dmul_rn(a.R, kc), se), a.M));
+            add = __dsub_rn((double)wsum[k], div_rn_by(__dmul_rn(__dmul_rn(a.R, kc), se), a.M, a.yMh, a.yMl));
         }
         const double dl = __dadd_rn(__dsub_rn(add, removal), kc_to_d);
         if (better(dl, ek, best_d, best_c)) { best_d = dl; best_c = ek; }
@@ -891,7 +894,7 @@ __global__ void __launch_bounds__(1024) k_super_huge_select(SmArgs a, int64_t se
     const long long kcl = a.sweight[c];
     const double kc = (double)kcl;
     const double sigma_d = (double)(long long)a.sctot[d];
-    const double removal = __ddiv_rn(__dmul_rn(__dmul_rn(a.R, kc), __dsub_rn(sigma_d, kc)), a.M);
+    const double removal = div_rn_by(__dmul_rn(__dmul_rn(a.R, kc), __dsub_rn(sigma_d, kc)), a.M, a.yMh, a.yMl);
     const double kc_to_d = (double)table_get(k, v, mask, d);
     double best_d = 0.0;
     uint32_t best_c = d;
@@ -907,7 +910,7 @@ __global__ void __launch_bounds__(1024) k_super_huge_select(SmArgs a, int64_t se
             add = __dsub_rn(kc_to_d, removal);
         } else {
             const double se = (double)(long long)a.sctot[ek];
-            add = __dsub_rn(kce, __ddiv_rn(__dmul_rn(__dmul_rn(a.R, kc), se), a.M));
+            add = __dsub_rn(kce, div_rn_by(__dmul_rn(__dmul_rn(a.R, kc), se), a.M, a.yMh, a.yMl));
         }
         const double dl = __dadd_rn(__dsub_rn(add, removal), kc_to_d);
         if (better(dl, ek, best_d, best_c)) { best_d = dl; best_c = ek; }
@@ -1587,6 +1590,8 @@ void leiden_device(const DeviceCSR& g, const LeidenParams& p, uint32_t* vcom, gb
             SmArgs sa{soff, snbr, sw, sweight, scomm, sctot, active, bstart, nbatch, proposed, pdelta, M, R,
                       gk, gv, gcap > kSmSmall ? gcap : 0, big_active.get(), bigstart.get(), bk.get(), bv.get(),
                       bcap, light.get(), big_min};
+            sa.yMh = la.dq.yMh;
+            sa.yMl = la.dq.yMl;
             // Batched launches: super-nodes above kHugeSeg neighbours, split over CTAs.
             struct HugeBatch { int64_t e0 = 0, ne = 0, t0 = 0, nt = 0; };
             std::vector<HugeBatch> hb;
