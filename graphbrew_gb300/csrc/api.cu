@@ -560,18 +560,31 @@ int gbgpu_map_and_relabel(gbgpu_ctx* ctx, const int64_t* row_ptr, const int32_t*
                 DevBuf<int32_t> ocol;
                 int64_t* rpd = out_row_ptr;
                 int32_t* cold = out_col;
+                bool direct = false;
                 if (!on_device(flags)) {
                     orp.alloc(n + 1, s);
-                    ocol.alloc(nnz > 0 ? nnz : 1, s);
                     rpd = orp.get();
-                    cold = ocol.get();
+                    // A pinned (page-locked, device-mapped) host array takes the
+                    // relabelled columns straight from the kernels over the
+                    // C2C link, overlapping what would be a separate copy;
+                    // pageable memory goes through a device buffer and a copy.
+                    cudaPointerAttributes pa{};
+                    if (nnz > 0 && cudaPointerGetAttributes(&pa, out_col) == cudaSuccess &&
+                        pa.type == cudaMemoryTypeHost && pa.devicePointer) {
+                        cold = static_cast<int32_t*>(pa.devicePointer);
+                        direct = true;
+                    } else {
+                        cudaGetLastError();
+                        ocol.alloc(nnz > 0 ? nnz : 1, s);
+                        cold = ocol.get();
+                    }
                 }
                 gb::relabel_csr_device(rg.csr, ids_dev, inv, rpd, cold, s, &st->kernel_launches);
                 GB_CUDA(cudaEventRecord(tb, s));
                 GB_CUDA(cudaEventSynchronize(tb));
                 st->relabel_ms = ev_ms(ta, tb);
                 copy_out(out_row_ptr, rpd, n + 1, flags, s, st);
-                copy_out(out_col, cold, nnz, flags, s, st);
+                if (!direct) copy_out(out_col, cold, nnz, flags, s, st);
             }
             if (new_ids_out) copy_out(new_ids_out, ids_dev, n, flags, s, st);
         }

@@ -174,7 +174,9 @@ int gbgpu_relabel_csr(gbgpu_ctx* ctx, const int64_t* row_ptr, const int32_t* col
 /* The builder's mapping lifecycle after GenerateMapping (builder.h:829-940):
  * mapping, device-side validation, relabel.  Equivalent to the three calls
  * above on one resident copy of the graph.  out_row_ptr / out_col may be NULL
- * to skip the relabel. */
+ * to skip the relabel.  With host buffers, a page-locked out_col (cudaHostAlloc
+ * / cudaHostRegister, e.g. torch pin_memory) is written by the relabel kernels
+ * directly; pageable memory is filled by a copy afterwards. */
 int gbgpu_map_and_relabel(gbgpu_ctx* ctx, const int64_t* row_ptr, const int32_t* col,
                           int64_t n, int64_t nnz, const char* opts, double auto_resolution,
                           int32_t* new_ids_out, int64_t* out_row_ptr, int32_t* out_col,

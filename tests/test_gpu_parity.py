@@ -497,3 +497,27 @@ def test_delta_reciprocal_form_equals_division(ctx, M, R):
     remainder, midpoint test) equals the two full divisions bit for bit; the
     same call also checks bare quotients over exponents -200..200."""
     assert ctx.selfcheck_delta(M, R, count=1 << 22, seed=int(M) % 1000 + 7) == 0
+
+
+def test_map_and_relabel_into_pinned_host_buffers(ctx):
+    """Host buffers through the C ABI: a page-locked out_col is written by the
+    relabel kernels directly, a pageable one through a copy; both give the
+    device-resident call's permutation and relabelled CSR."""
+    rp, col = gg.rmat(16, 12, seed=21)
+    want_ids, want_rp, want_col, _ = ctx.map_and_relabel(rp.cuda(), col.cuda(), SERIAL)
+    want = (want_ids.cpu().numpy(), want_rp.cpu().numpy(), want_col.cpu().numpy())
+    n, nnz = rp.numel() - 1, col.numel()
+    h_rp, h_col = rp.pin_memory(), col.pin_memory()
+    for pinned in (True, False):
+        ids = torch.empty(n, dtype=torch.int32)
+        orp = torch.empty(n + 1, dtype=torch.int64)
+        ocol = torch.empty(nnz, dtype=torch.int32)
+        if pinned:
+            ids, orp, ocol = ids.pin_memory(), orp.pin_memory(), ocol.pin_memory()
+        st = gb.GbgpuStats()
+        rc = gb.library().gbgpu_map_and_relabel(ctx.handle, h_rp.data_ptr(), h_col.data_ptr(), n, nnz,
+                                                SERIAL.encode(), -1.0, ids.data_ptr(), orp.data_ptr(),
+                                                ocol.data_ptr(), gb.C.byref(st), 0)
+        assert rc == 0
+        for got, exp in zip((ids.numpy(), orp.numpy(), ocol.numpy()), want):
+            np.testing.assert_array_equal(got, exp)
