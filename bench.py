@@ -44,8 +44,8 @@ SCALE = 22
 EDGE_FACTOR = 16
 CPU_BASELINE_RUNS = 5
 # Local-moving DRAM traffic per mapping of GAPBS -g 22 (ncu, warm L2):
-# 8.722 GB read + 4.728 GB written by the round kernels.
-LOCAL_MOVE_DRAM_BYTES_G22 = 13.449e9
+# 6.445 GB read + 3.341 GB written by the round kernels.
+LOCAL_MOVE_DRAM_BYTES_G22 = 9.787e9
 PINS_PATH = os.path.join(ROOT, "tests", "golden", "gapbs_pins.json")
 
 
