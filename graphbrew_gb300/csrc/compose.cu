@@ -713,7 +713,7 @@ __global__ void k_bfs_claim(const int32_t* __restrict__ F, int64_t nf, const int
 __global__ void k_bfs_flag(const int32_t* __restrict__ F, int64_t nf, const int64_t* __restrict__ D, int64_t T,
                            const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
                            const uint32_t* __restrict__ memb, const uint8_t* __restrict__ visited,
-                           const unsigned long long* __restrict__ claim, int32_t* __restrict__ flag) {
+                           const unsigned long long* __restrict__ claim, uint8_t* __restrict__ flag) {
     for_frontier_edges(D, nf, T, [&](int64_t i, int64_t k, int64_t e) {
         const int32_t u = F[i];
         const int32_t w = col[rp[u] + k];
@@ -734,7 +734,7 @@ __global__ void k_bfs_bases(int32_t nslots, const int64_t* __restrict__ fs, cons
 
 __global__ void k_bfs_write(const int32_t* __restrict__ F, int64_t nf, const int64_t* __restrict__ D, int64_t T,
                             const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
-                            const uint32_t* __restrict__ memb, const int32_t* __restrict__ flag,
+                            const uint32_t* __restrict__ memb, const uint8_t* __restrict__ flag,
                             const int64_t* __restrict__ P, const int32_t* __restrict__ slot_of_comm,
                             const int64_t* __restrict__ qlen, const int64_t* __restrict__ base,
                             int32_t* __restrict__ nextF, uint8_t* __restrict__ visited, uint32_t* __restrict__ local) {
@@ -837,7 +837,7 @@ __global__ void k_rcm_frontier(int32_t nslots, const int32_t* __restrict__ part,
 // Children in (parent, row offset) order with their parent's frontier index.
 __global__ void k_rcm_write(const int32_t* __restrict__ F, int64_t nf, const int64_t* __restrict__ D, int64_t T,
                             const int64_t* __restrict__ rp, const int32_t* __restrict__ col,
-                            const int32_t* __restrict__ flag, const int64_t* __restrict__ P,
+                            const uint8_t* __restrict__ flag, const int64_t* __restrict__ P,
                             int32_t* __restrict__ nextF, int64_t* __restrict__ parent, uint8_t* __restrict__ visited) {
     for_frontier_edges(D, nf, T, [&](int64_t i, int64_t k, int64_t e) {
         if (!flag[e]) return;
@@ -1099,14 +1099,14 @@ int64_t rcm_communities(const DeviceCSR& g, const uint32_t* memb, const int32_t*
             GB_LAUNCH_CHECK();
             exclusive_scan_i64_total(D, D, nf, D.get() + nf, s);
             const int64_t T = read_dev(D.get() + nf, s);
-            DevBuf<int32_t> flag(T > 0 ? T : 1, s);
+            DevBuf<uint8_t> flag(T > 0 ? T : 1, s);
             DevBuf<int64_t> P(T + 1, s);
             if (T > 0) {
                 k_bfs_claim<<<edge_grid(T), 256, 0, s>>>(F, nf, D, T, g.row_ptr, g.col, memb, visited, claim);
                 GB_LAUNCH_CHECK();
                 k_bfs_flag<<<edge_grid(T), 256, 0, s>>>(F, nf, D, T, g.row_ptr, g.col, memb, visited, claim, flag);
                 GB_LAUNCH_CHECK();
-                exclusive_scan_i32_to_i64(flag, P, T, P.get() + T, s);
+                exclusive_scan_u8_to_i64(flag, P, T, P.get() + T, s);
             } else {
                 GB_CUDA(cudaMemsetAsync(P, 0, sizeof(int64_t), s));
             }
@@ -1439,13 +1439,13 @@ void compose_device(const DeviceCSR& g, const uint32_t* memb, const ComposeParam
             exclusive_scan_i64_total(D, D, nf, D.get() + nf, s);
             const int64_t T = read_dev(D.get() + nf, s);
             if (T == 0) break;
-            DevBuf<int32_t> flag(T, s);
+            DevBuf<uint8_t> flag(T, s);
             DevBuf<int64_t> P(T + 1, s);
             k_bfs_claim<<<edge_grid(T), 256, 0, s>>>(F, nf, D, T, g.row_ptr, g.col, memb, visited, claim);
             GB_LAUNCH_CHECK();
             k_bfs_flag<<<edge_grid(T), 256, 0, s>>>(F, nf, D, T, g.row_ptr, g.col, memb, visited, claim, flag);
             GB_LAUNCH_CHECK();
-            exclusive_scan_i32_to_i64(flag, P, T, P.get() + T, s);
+            exclusive_scan_u8_to_i64(flag, P, T, P.get() + T, s);
             k_bfs_bases<<<grid_for(nbfs, kT), kT, 0, s>>>(nbfs, fs, fe, D, P, bbase, bend);
             GB_LAUNCH_CHECK();
             k_bfs_write<<<edge_grid(T), 256, 0, s>>>(F, nf, D, T, g.row_ptr, g.col, memb, flag, P, slot_of_comm,

@@ -143,6 +143,7 @@ void exclusive_scan_i64_total(const int64_t* in, int64_t* out, int64_t n, int64_
 // total into *total_dev (device pointer, may be null).
 void exclusive_scan_i32_to_i64(const int32_t* in, int64_t* out, int64_t n, int64_t* total_dev,
                                cudaStream_t s);
+void exclusive_scan_u8_to_i64(const uint8_t* in, int64_t* out, int64_t n, int64_t* total_dev, cudaStream_t s);
 
 // Stable LSD radix sort of (key, value) pairs by the low `key_bits` bits of
 // the key.  keys/values are sorted in place (double-buffered through scratch).

@@ -277,6 +277,10 @@ void exclusive_scan_i32_to_i64(const int32_t* in, int64_t* out, int64_t n, int64
     exclusive_scan_impl<int32_t>(in, out, n, total_dev, s);
 }
 
+void exclusive_scan_u8_to_i64(const uint8_t* in, int64_t* out, int64_t n, int64_t* total_dev, cudaStream_t s) {
+    exclusive_scan_impl<uint8_t>(in, out, n, total_dev, s);
+}
+
 void radix_sort_pairs_u32(uint32_t* keys, uint32_t* values, int64_t n, int key_bits, cudaStream_t s) {
     radix_sort_impl<uint32_t, true>(keys, values, n, key_bits, s);
 }
