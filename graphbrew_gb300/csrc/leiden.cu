@@ -512,6 +512,17 @@ struct SmProposal {
     double delta;
 };
 
+// Candidate (dl, ek) into a running best that starts at (+0.0, own
+// community): a proposal commits only when its delta is > 0, so candidates at
+// or below +0.0 change no outcome and are skipped; among the others the order
+// is better()'s, compared on the integer pipe.
+__device__ __forceinline__ void take_pos(double dl, uint32_t ek, double& best_d, uint32_t& best_c) {
+    if (dpos(dl) && better_pos(dl, ek, best_d, best_c)) {
+        best_d = dl;
+        best_c = ek;
+    }
+}
+
 // Proposal for super-node c by one warp (the GVE super-move proposals of
 // RG:2264-2302): neighbour communities into a shared table (a per-warp
 // global one above kSmSmall / 2 neighbours) whose third array caches each
@@ -552,15 +563,33 @@ __device__ void super_propose_cached(const SmArgs& a, uint32_t c, uint32_t* tk, 
         }
     }
     __syncwarp();
+    const double kc_to_d = (double)table_get(k, v, mask, d);
+    // Occupied slots to the front, in slot order: the scoring loop then takes
+    // ceil(occupied / 32) full-warp steps instead of H / 32 mostly idle ones
+    // (an FP64 instruction costs the same with one lane active or 32).
+    uint32_t occ = 0;
+    for (uint32_t i0 = 0; i0 < H; i0 += 32) {
+        const uint32_t i = i0 + lane;
+        const uint32_t ek = k[i], ev = v[i];
+        const unsigned long long et = shared ? tt[i] : 0ull;
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, ek != kNone);
+        __syncwarp();
+        if (ek != kNone) {
+            const uint32_t j = occ + (uint32_t)__popc(m & ((1u << lane) - 1u));
+            k[j] = ek;
+            v[j] = ev;
+            if (shared) tt[j] = et;
+        }
+        __syncwarp();
+        occ += (uint32_t)__popc(m);
+    }
     const double kc = (double)kcl;
     const double sigma_d = (double)(long long)sd_raw;
     const double removal = div_rn_by(__dmul_rn(__dmul_rn(a.R, kc), __dsub_rn(sigma_d, kc)), a.M, a.yMh, a.yMl);
-    const double kc_to_d = (double)table_get(k, v, mask, d);
     double best_d = 0.0;
     uint32_t best_c = d;
-    for (uint32_t i = lane; i < H; i += 32) {
+    for (uint32_t i = lane; i < occ; i += 32) {
         const uint32_t ek = k[i];
-        if (ek == kNone) continue;
         const double kce = (double)v[i];
         double add;
         if (ek == d) {
@@ -570,9 +599,9 @@ __device__ void super_propose_cached(const SmArgs& a, uint32_t c, uint32_t* tk, 
             add = __dsub_rn(kce, div_rn_by(__dmul_rn(__dmul_rn(a.R, kc), se), a.M, a.yMh, a.yMl));
         }
         const double dl = __dadd_rn(__dsub_rn(add, removal), kc_to_d);
-        if (better(dl, ek, best_d, best_c)) { best_d = dl; best_c = ek; }
+        take_pos(dl, ek, best_d, best_c);
     }
-    warp_argmax(best_d, best_c);
+    warp_argmax_pos(best_d, best_c);
     out.c = c;
     out.d = d;
     out.best = best_c;
@@ -617,16 +646,16 @@ __device__ void super_propose_block(const SmArgs& a, uint32_t c, SmProposal* out
             add = __dsub_rn(kce, div_rn_by(__dmul_rn(__dmul_rn(a.R, kc), se), a.M, a.yMh, a.yMl));
         }
         const double dl = __dadd_rn(__dsub_rn(add, removal), kc_to_d);
-        if (better(dl, ek, best_d, best_c)) { best_d = dl; best_c = ek; }
+        take_pos(dl, ek, best_d, best_c);
     }
-    warp_argmax(best_d, best_c);
+    warp_argmax_pos(best_d, best_c);
     if (lane == 0) { red_d[w] = best_d; red_c[w] = best_c; }
     __syncthreads();
     if (tid == 0) {
         double bd = red_d[0];
         uint32_t bc = red_c[0];
         for (int q = 1; q < (int)(blockDim.x >> 5); ++q)
-            if (better(red_d[q], red_c[q], bd, bc)) { bd = red_d[q]; bc = red_c[q]; }
+            if (better_pos(red_d[q], red_c[q], bd, bc)) { bd = red_d[q]; bc = red_c[q]; }
         out->c = c;
         out->d = d;
         out->best = bc;
@@ -695,7 +724,7 @@ __device__ void super_propose_light(const SmArgs& a, uint32_t c, SmProposal& out
             add = __dsub_rn((double)wsum[k], div_rn_by(__dmul_rn(__dmul_rn(a.R, kc), se), a.M, a.yMh, a.yMl));
         }
         const double dl = __dadd_rn(__dsub_rn(add, removal), kc_to_d);
-        if (better(dl, ek, best_d, best_c)) { best_d = dl; best_c = ek; }
+        take_pos(dl, ek, best_d, best_c);
     }
     out.c = c;
     out.d = d;
@@ -808,9 +837,9 @@ k_super_move_cluster(SmArgs a, int max_iter, int* iters_out, long long* moves_ou
 }
 
 // Batched launches for super-graphs above one cluster's size: per batch,
-// warps propose the super-nodes up to kBigSuperBatched neighbours (shared
-// tables), CTAs the bigger ones, then the commit.
-__global__ void k_super_propose_batch(SmArgs a, int64_t bt) {
+// lanes propose the super-nodes up to kLightDeg neighbours, warps those up to
+// kBigSuperBatched (shared tables), CTAs the bigger ones, then the commit.
+__global__ void __launch_bounds__(256, 4) k_super_propose_batch(SmArgs a, int64_t bt) {
     __shared__ uint32_t tk[8][kSmSmall];
     __shared__ uint32_t tv[8][kSmSmall];
     __shared__ unsigned long long tt[8][kSmSmall];
@@ -818,9 +847,21 @@ __global__ void k_super_propose_batch(SmArgs a, int64_t bt) {
     const int64_t lo = a.bstart[bt], hi = a.bstart[bt + 1];
     const int64_t gw = (int64_t)blockIdx.x * 8 + w;
     const int64_t nwt = (int64_t)gridDim.x * 8;
+    // Light super-nodes, a lane each: warp w of every CTA takes 32 of them
+    // before warp w + 1 of any, so a batch's FP64 work spreads over the SMs.
+    const int64_t lw = (int64_t)w * gridDim.x + blockIdx.x;
+    for (int64_t i = lo + lw * 32 + lane; i < hi; i += nwt * 32) {
+        const uint32_t c = a.active[i];
+        if (a.soff[c + 1] - a.soff[c] > kLightDeg) continue;
+        SmProposal pr;
+        super_propose_light(a, c, pr);
+        a.proposed[c] = pr.best;
+        a.pdelta[c] = pr.delta;
+    }
     for (int64_t i = lo + gw; i < hi; i += nwt) {
         const uint32_t c = a.active[i];
-        if (a.soff[c + 1] - a.soff[c] > a.warp_max) continue;
+        const int64_t deg = a.soff[c + 1] - a.soff[c];
+        if (deg <= kLightDeg || deg > a.warp_max) continue;
         SmProposal pr;
         super_propose_cached(a, c, tk[w], tv[w], tt[w], a.gkeys + gw * a.gcap, a.gvals + gw * a.gcap, pr);
         if (lane == 0) {
@@ -913,16 +954,16 @@ __global__ void __launch_bounds__(1024) k_super_huge_select(SmArgs a, int64_t se
             add = __dsub_rn(kce, div_rn_by(__dmul_rn(__dmul_rn(a.R, kc), se), a.M, a.yMh, a.yMl));
         }
         const double dl = __dadd_rn(__dsub_rn(add, removal), kc_to_d);
-        if (better(dl, ek, best_d, best_c)) { best_d = dl; best_c = ek; }
+        take_pos(dl, ek, best_d, best_c);
     }
-    warp_argmax(best_d, best_c);
+    warp_argmax_pos(best_d, best_c);
     if (lane == 0) { red_d[w] = best_d; red_c[w] = best_c; }
     __syncthreads();
     if (tid == 0) {
         double bd = red_d[0];
         uint32_t bc = red_c[0];
         for (int r = 1; r < (int)(blockDim.x >> 5); ++r)
-            if (better(red_d[r], red_c[r], bd, bc)) { bd = red_d[r]; bc = red_c[r]; }
+            if (better_pos(red_d[r], red_c[r], bd, bc)) { bd = red_d[r]; bc = red_c[r]; }
         a.part_d[q] = bd;
         a.part_c[q] = bc;
         __threadfence();
@@ -935,7 +976,7 @@ __global__ void __launch_bounds__(1024) k_super_huge_select(SmArgs a, int64_t se
             for (int r = 1; r < nt; ++r) {
                 const double pd = ((volatile double*)a.part_d)[f + r];
                 const uint32_t pc = ((volatile uint32_t*)a.part_c)[f + r];
-                if (better(pd, pc, bd, bc)) { bd = pd; bc = pc; }
+                if (better_pos(pd, pc, bd, bc)) { bd = pd; bc = pc; }
             }
             a.proposed[c] = bc;
             a.pdelta[c] = bd;

@@ -61,17 +61,22 @@ def test_refine_rmat_against_oracle(ctx, scale):
     np.testing.assert_array_equal(ids.cpu().numpy(), ids_orc)
 
 
+@pytest.mark.parametrize("graph", ["rmat17", "grid512"])
 @pytest.mark.parametrize("split_min", ["4096", "200"])
 @pytest.mark.parametrize("refine", [False, True])
-def test_batched_super_move_against_oracle(ctx, monkeypatch, refine, split_min):
+def test_batched_super_move_against_oracle(ctx, monkeypatch, refine, split_min, graph):
     """The super-move's batched launches (used above one cluster's size;
-    forced here) give the cluster kernel's memberships: warps for super-nodes
-    up to 128 neighbours, a CTA each above, and above split_min neighbours
-    several CTAs per super-node (edge segments into one table, table
-    segments selecting, the last one reducing)."""
+    forced here) give the cluster kernel's memberships: lanes for super-nodes
+    up to 8 neighbours, warps up to 128, a CTA each above, and above
+    split_min neighbours several CTAs per super-node (edge segments into one
+    table, table segments selecting, the last one reducing).  The grid's
+    super-nodes are mostly of the lane kind, RMAT's of all kinds."""
     monkeypatch.setenv("GBGPU_SUPER_CLUSTER_MAX_EDGES", "0")
     monkeypatch.setenv("GBGPU_SUPER_SPLIT_MIN", split_min)
-    rp_t, col_t = gg.rmat(17, 16, seed=400, device="cuda")
+    if graph == "rmat17":
+        rp_t, col_t = gg.rmat(17, 16, seed=400, device="cuda")
+    else:
+        rp_t, col_t = gg.grid(512, 512, 0.05, seed=401, device="cuda")
     rp, col = rp_t.cpu().numpy(), col_t.cpu().numpy()
     ar = po.auto_resolution(rp, col)
     recipe = REFINE if refine else REFINE.replace("refine0", "norefine")
