@@ -26,7 +26,7 @@ namespace gb {
 namespace {
 
 enum CommunityOrderOrd { kSizeDesc = 0, kSizeAsc = 1, kDegreeDesc = 2, kDegreeAsc = 3, kIdentity = 6 };
-enum IntraOrd { kIntraBFS = 0, kIntraRCM = 1, kIntraRCMpp = 2, kIntraDendrogram = 3, kIntraGorder = 4 };
+enum IntraOrd { kIntraBFS = 0, kIntraRCM = 1, kIntraRCMpp = 2, kIntraDendrogram = 3, kIntraGorder = 4, kIntraRandom = 10 };
 
 constexpr int kT = 256;
 
@@ -1240,8 +1240,9 @@ void compose_device(const DeviceCSR& g, const uint32_t* memb, const ComposeParam
     int intra = p.intra_order;
     if (intra == kIntraDendrogram) intra = kIntraBFS;  // Leiden has no Rabbit dendrogram (:6668-6677)
     const bool sorted_intra = is_sorted_intra_order(intra);
+    const bool random_intra = intra == kIntraRandom;
     GB_REQUIRE(intra == kIntraBFS || intra == kIntraGorder || intra == kIntraRCM || intra == kIntraRCMpp ||
-                   sorted_intra,
+                   sorted_intra || random_intra,
                GBGPU_E_UNSUPPORTED, "intra-community order not available on the GPU path");
     const int co = p.community_order;
     GB_REQUIRE(co == kSizeDesc || co == kSizeAsc || co == kDegreeDesc || co == kDegreeAsc || co == kIdentity,
@@ -1405,8 +1406,12 @@ void compose_device(const DeviceCSR& g, const uint32_t* memb, const ComposeParam
     }
     // ---- sorted orders: every community ----
     if (sorted_intra) sorted_communities(g, memb, intra, order_v, vkeys, offs, ssize, nn, local, s, &launches);
+    // ---- intra_random: every community of two or more vertices ----
+    if (random_intra)
+        random_communities(memb, order_v, vkeys, offs, ssize, lists.get() + 4 * C, cc.get()->n + 4, nbfs, nn, local, s,
+                           &launches);
     // ---- BFS communities ----
-    if (nbfs > 0 && intra != kIntraRCM && intra != kIntraRCMpp && !sorted_intra) {
+    if (nbfs > 0 && intra != kIntraRCM && intra != kIntraRCMpp && !sorted_intra && !random_intra) {
         const int32_t* blist = lists.get() + 4 * C;
         DevBuf<int32_t> slot_of_comm(C, s);
         GB_CUDA(cudaMemsetAsync(slot_of_comm, 0xFF, C * sizeof(int32_t), s));

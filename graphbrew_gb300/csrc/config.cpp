@@ -725,7 +725,7 @@ std::string gpu_unsupported_reason(const Config& c) {
     switch (c.intraCommunityOrder) {
         case IntraOrder::BFSFromHub: case IntraOrder::Gorder: case IntraOrder::Dendrogram: case IntraOrder::RCM:
         case IntraOrder::RCMpp: case IntraOrder::HubSort: case IntraOrder::DegreeAsc: case IntraOrder::Hub2: case IntraOrder::Alternate:
-        case IntraOrder::BoundaryLast: case IntraOrder::CoreOrder: break;
+        case IntraOrder::Random: case IntraOrder::BoundaryLast: case IntraOrder::CoreOrder: break;
         default: return std::string("intra-community order '") + intra_name(c.intraCommunityOrder) +
                         "' is not on the GPU path";
     }

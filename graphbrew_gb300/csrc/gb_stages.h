@@ -35,6 +35,14 @@ int64_t sorted_communities(const DeviceCSR& g, const uint32_t* memb, int intra, 
                            const uint32_t* ranks, const int64_t* offs, const int64_t* ssize, int64_t nn,
                            uint32_t* local, cudaStream_t s, int64_t* launches);
 
+// ---- compose_random.cu: intra_random ----
+// Local ids of every non-isolated vertex for intra_random: list / count_dev
+// (count on the host too) are the ranks of the communities of two or more
+// vertices.  Returns the number of swap rounds.
+int64_t random_communities(const uint32_t* memb, const uint32_t* order_v, const uint32_t* ranks, const int64_t* offs,
+                           const int64_t* ssize, const int32_t* list, const int32_t* count_dev, int32_t count,
+                           int64_t nn, uint32_t* local, cudaStream_t s, int64_t* launches);
+
 // ---- leiden.cu ----
 struct LeidenParams {
     double resolution = 1.0;

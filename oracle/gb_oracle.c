@@ -1332,6 +1332,91 @@ static void intra_sorted(const uint32_t *verts, int64_t sz, int order, const uin
     for (int64_t j = 0; j < sz; ++j) local_ids[tmp[j]] = (uint32_t)j;
 }
 
+/* intra_random (RG:6825-6845): std::mt19937 seeded with 0xDEADBEEF ^ c,
+ * Fisher-Yates from the back, each swap index drawn by
+ * std::uniform_int_distribution<size_t>(0, j).
+ *
+ * The engine is MT19937 (Matsumoto and Nishimura 1998) with the parameters
+ * and seeding recurrence of the C++ standard's mersenne_twister_engine; the
+ * state is twisted all at once when its 624 words are used up, as libstdc++
+ * does (the output sequence does not depend on that).  libstdc++ maps a
+ * 32-bit engine onto [0, j] by Lemire's nearly divisionless method
+ * ("Fast Random Integer Generation in an Interval", 2019): the high half of
+ * draw * (j + 1), redrawing while the low half is below 2^32 mod (j + 1). */
+typedef struct {
+    uint32_t mt[624];
+    int idx;
+} orc_mt19937;
+
+static void mt_seed(orc_mt19937 *r, uint32_t seed)
+{
+    r->mt[0] = seed;
+    for (int i = 1; i < 624; ++i) r->mt[i] = 1812433253u * (r->mt[i - 1] ^ (r->mt[i - 1] >> 30)) + (uint32_t)i;
+    r->idx = 624;
+}
+
+static uint32_t mt_next(orc_mt19937 *r)
+{
+    if (r->idx >= 624) {
+        for (int i = 0; i < 624; ++i) {
+            const uint32_t y = (r->mt[i] & 0x80000000u) | (r->mt[(i + 1) % 624] & 0x7FFFFFFFu);
+            r->mt[i] = r->mt[(i + 397) % 624] ^ (y >> 1) ^ ((y & 1u) ? 0x9908B0DFu : 0u);
+        }
+        r->idx = 0;
+    }
+    uint32_t y = r->mt[r->idx++];
+    y ^= y >> 11;
+    y ^= (y << 7) & 0x9D2C5680u;
+    y ^= (y << 15) & 0xEFC60000u;
+    y ^= y >> 18;
+    return y;
+}
+
+static uint32_t uniform_below(orc_mt19937 *r, uint32_t range)
+{
+    uint64_t prod = (uint64_t)mt_next(r) * range;
+    uint32_t low = (uint32_t)prod;
+    if (low < range) {
+        const uint32_t thr = (0u - range) % range;
+        while (low < thr) {
+            prod = (uint64_t)mt_next(r) * range;
+            low = (uint32_t)prod;
+        }
+    }
+    return (uint32_t)(prod >> 32);
+}
+
+int orc_random_draws(uint32_t seed, int64_t count, uint32_t *out)
+{
+    if (count < 0 || count > 0xFFFFFFFFll || (count > 0 && !out)) return ORC_EINVAL;
+    orc_mt19937 *rng = (orc_mt19937 *)malloc(sizeof(orc_mt19937));
+    if (!rng) return ORC_ENOMEM;
+    mt_seed(rng, seed);
+    if (count > 0) out[0] = 0;
+    for (int64_t j = count - 1; j > 0; --j) out[j] = uniform_below(rng, (uint32_t)j + 1u);
+    free(rng);
+    return ORC_OK;
+}
+
+static void intra_random(const uint32_t *verts, int64_t sz, uint32_t c, uint32_t *local_ids, uint32_t *tmp,
+                         orc_mt19937 *rng)
+{
+    if (sz == 0) return;
+    if (sz == 1) {
+        local_ids[verts[0]] = 0;
+        return;
+    }
+    memcpy(tmp, verts, (size_t)sz * sizeof(uint32_t));
+    mt_seed(rng, 0xDEADBEEFu ^ c);
+    for (int64_t j = sz - 1; j > 0; --j) {
+        const uint32_t k = uniform_below(rng, (uint32_t)j + 1u);
+        const uint32_t t = tmp[j];
+        tmp[j] = tmp[k];
+        tmp[k] = t;
+    }
+    for (int64_t j = 0; j < sz; ++j) local_ids[tmp[j]] = (uint32_t)j;
+}
+
 /* ------------------------------------------------------------------------ */
 /* orderCompose (RG:6286-7087), super-graph order "none".                    */
 /* ------------------------------------------------------------------------ */
@@ -1359,7 +1444,7 @@ int orc_compose(const orc_graph *g, const uint32_t *membership,
     if (cfg->intra_order == ORC_INTRA_GORDER && cfg->gorder_window <= 0) return ORC_EINVAL;
     if (cfg->intra_order != ORC_INTRA_BFS && cfg->intra_order != ORC_INTRA_RCM &&
         cfg->intra_order != ORC_INTRA_RCMPP && cfg->intra_order != ORC_INTRA_GORDER &&
-        !is_sorted_intra(cfg->intra_order))
+        cfg->intra_order != ORC_INTRA_RANDOM && !is_sorted_intra(cfg->intra_order))
         return ORC_EUNSUPPORTED;
 
     int rc = ORC_ENOMEM;
@@ -1463,7 +1548,8 @@ int orc_compose(const orc_graph *g, const uint32_t *membership,
             orc_pair *t_cand = (orc_pair *)malloc((size_t)max_sz * sizeof(orc_pair));
             orc_gorder_ws t_ws;
             memset(&t_ws, 0, sizeof(t_ws));
-            const int ok = t_visited && t_queue && t_la && t_lb && t_cand;
+            orc_mt19937 *t_rng = (orc_mt19937 *)malloc(sizeof(orc_mt19937));
+            const int ok = t_visited && t_queue && t_la && t_lb && t_cand && t_rng;
             if (!ok) {
 #ifdef _OPENMP
 #pragma omp atomic write
@@ -1480,6 +1566,8 @@ int orc_compose(const orc_graph *g, const uint32_t *membership,
                 const int64_t sz = csize[c];
                 if (skey) {
                     intra_sorted(verts, sz, cfg->intra_order, skey, local_ids, t_la);
+                } else if (cfg->intra_order == ORC_INTRA_RANDOM) {
+                    intra_random(verts, sz, c, local_ids, t_la, t_rng);
                 } else if (cfg->intra_order == ORC_INTRA_RCM || cfg->intra_order == ORC_INTRA_RCMPP) {
                     if (intra_rcm(g, verts, sz, c, membership, deg, v2l, local_ids, t_visited,
                                   t_queue, t_la, t_lb, t_cand, cfg->intra_order == ORC_INTRA_RCMPP) != ORC_OK) {
@@ -1502,7 +1590,7 @@ int orc_compose(const orc_graph *g, const uint32_t *membership,
                               t_queue);
                 }
             }
-            free(t_visited); free(t_queue); free(t_la); free(t_lb); free(t_cand);
+            free(t_visited); free(t_queue); free(t_la); free(t_lb); free(t_cand); free(t_rng);
             gorder_ws_free(&t_ws);
         }
         if (failed) goto done;

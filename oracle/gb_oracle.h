@@ -92,6 +92,7 @@ enum {
     ORC_INTRA_DEGREE_ASC = 7,
     ORC_INTRA_HUB2 = 8,
     ORC_INTRA_ALTERNATE = 9,
+    ORC_INTRA_RANDOM = 10,
     ORC_INTRA_BOUNDARY_LAST = 11,
     ORC_INTRA_CORE = 12
 };
@@ -99,6 +100,10 @@ enum {
 /* libstdc++ (GCC 13) std::sort of `count` element ids by comp(a, b) =
  * key[a] < key[b]: the tie order the sorted intra orders inherit. */
 int orc_libstdcxx_sort(uint32_t *elems, int64_t count, const uint64_t *key);
+/* intra_random's swap indices (RG:6825-6845): out[j] for j = count - 1 .. 1
+ * drawn in that order from std::mt19937(seed) by libstdc++'s
+ * uniform_int_distribution (Lemire's method); out[0] = 0. */
+int orc_random_draws(uint32_t seed, int64_t count, uint32_t *out);
 /* Its depth-limit fallback alone (__partial_sort(first, last, last)). */
 int orc_libstdcxx_heap_sort(uint32_t *elems, int64_t count, const uint64_t *key);
 

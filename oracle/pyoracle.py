@@ -33,7 +33,7 @@ DEFAULT_TOLERANCE_DROP = 10.0
 
 COMM_ORDERS = {"size-desc": 0, "size-asc": 1, "degree-desc": 2, "degree-asc": 3, "identity": 6}
 INTRA_ORDERS = {"bfs": 0, "rcm": 1, "rcmpp": 2, "gorder": 4, "hubsort": 6, "degree-asc": 7, "hub2": 8, "alternate": 9,
-                "boundary-last": 11, "core": 12}
+                "random": 10, "boundary-last": 11, "core": 12}
 _u64p = np.ctypeslib.ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")
 STDSORT_SO = os.path.join(HERE, "_build", "libstdsort.so")
 
@@ -121,6 +121,7 @@ def load():
         lib.orc_max_threads.restype = C.c_int
         lib.orc_libstdcxx_sort.argtypes = [_u32p, C.c_int64, _u64p]
         lib.orc_libstdcxx_heap_sort.argtypes = [_u32p, C.c_int64, _u64p]
+        lib.orc_random_draws.argtypes = [C.c_uint32, C.c_int64, _u32p]
         lib.orc_pagerank_gs.restype = C.c_double
         lib.orc_pagerank_gs.argtypes = [C.POINTER(Graph), C.c_int, C.c_double, _f32p, C.c_int,
                                         C.POINTER(C.c_int)]
@@ -159,6 +160,7 @@ def _stdsort_lib():
     lib = C.CDLL(STDSORT_SO)
     lib.pin_std_sort.argtypes = [_u32p, C.c_int64, _u64p]
     lib.pin_std_heap_sort.argtypes = [_u32p, C.c_int64, _u64p]
+    lib.pin_std_shuffle_draws.argtypes = [C.c_uint32, C.c_int64, _u32p]
     return lib
 
 
@@ -167,6 +169,22 @@ def std_sort(elems, key):
     e = np.array(elems, dtype=np.uint32)
     _stdsort_lib().pin_std_sort(e, len(e), np.ascontiguousarray(key, dtype=np.uint64))
     return e
+
+
+def random_draws(seed, count):
+    """The oracle's intra_random swap indices: out[j], j = count-1 .. 1."""
+    out = np.zeros(max(count, 1), dtype=np.uint32)
+    if load().orc_random_draws(seed, count, out) != 0:
+        raise RuntimeError("orc_random_draws failed")
+    return out[:count]
+
+
+def std_shuffle_draws(seed, count):
+    """The same indices from the toolchain's std::mt19937 and
+    std::uniform_int_distribution<size_t> (pin)."""
+    out = np.zeros(max(count, 1), dtype=np.uint32)
+    _stdsort_lib().pin_std_shuffle_draws(seed, count, out)
+    return out[:count]
 
 
 def std_heap_sort(elems, key):
