@@ -1418,17 +1418,356 @@ static void intra_random(const uint32_t *verts, int64_t sz, uint32_t c, uint32_t
 }
 
 /* ------------------------------------------------------------------------ */
+/* Super-graph orders of orderCompose, one thread: sg_super_rcm (RG:4990-5090 */
+/* buildCommunitySuperGraph, :5726-5871 runRCMOnSuperCSR) and sg_hilbert      */
+/* (:6421-6459).  Each gives stage1Perm, the tie-break of the community      */
+/* order (:6460-6462).                                                        */
+/* ------------------------------------------------------------------------ */
+
+/* Bucket counts a default-constructed libstdc++ std::unordered_map goes
+ * through as it grows (maximum load factor 1): the first insertion
+ * allocates 13 buckets, and inserting element B + 1 into B buckets rehashes
+ * to the next count.  Measured on the toolchain's own container; the tests
+ * check it again (pin_umap_bucket_count in stdsort_pin.cc). */
+static const int64_t kUmapBuckets[] = {13, 29, 59, 127, 257, 541, 1109, 2357, 5087, 10273, 20753, 42043, 85229,
+                                       172933, 351061, 712697, 1447153, 2938679, 5967347, 12117689, 24607243,
+                                       49969847, 101473717};
+#define ORC_UMAP_MAX 101473717ll
+
+/* Iteration order of a libstdc++ std::unordered_map keyed by an unsigned
+ * integer (identity hash) after the k distinct keys are inserted in order
+ * into an empty map.  The container keeps one singly linked list of all
+ * nodes, and each bucket points at the node before its first node.  A key
+ * whose bucket is empty goes to the front of the list (the bucket of the old
+ * front then starts after it); otherwise it goes right after its bucket's
+ * before-node.  A rehash walks the list in order and puts every node back by
+ * the same two rules into the new buckets. */
+int orc_umap_order(const uint32_t *keys, int64_t k, uint32_t *out)
+{
+    const int64_t END = -1, EMPTY = -1, BEFORE = -2;
+    if (k < 0 || k > ORC_UMAP_MAX) return ORC_EINVAL;
+    if (k == 0) return ORC_OK;
+    int64_t bmax = 0;
+    for (size_t i = 0; i < sizeof(kUmapBuckets) / sizeof(kUmapBuckets[0]); ++i)
+        if (kUmapBuckets[i] >= k) { bmax = kUmapBuckets[i]; break; }
+    int64_t *nxt = (int64_t *)malloc((size_t)k * sizeof(int64_t));
+    int64_t *bkt = (int64_t *)malloc((size_t)bmax * sizeof(int64_t));
+    if (!nxt || !bkt) { free(nxt); free(bkt); return ORC_ENOMEM; }
+    int64_t head = END, B = 0;
+    int gi = -1;
+    for (int64_t i = 0; i < k; ++i) {
+        if (i + 1 > B) {
+            B = kUmapBuckets[++gi];
+            for (int64_t b = 0; b < B; ++b) bkt[b] = EMPTY;
+            int64_t p = head, first_bkt = 0;
+            head = END;
+            while (p != END) {
+                const int64_t q = nxt[p];
+                const int64_t b = (int64_t)(keys[p] % (uint64_t)B);
+                if (bkt[b] == EMPTY) {
+                    nxt[p] = head;
+                    head = p;
+                    bkt[b] = BEFORE;
+                    if (nxt[p] != END) bkt[first_bkt] = p;
+                    first_bkt = b;
+                } else if (bkt[b] == BEFORE) {
+                    nxt[p] = head;
+                    head = p;
+                } else {
+                    nxt[p] = nxt[bkt[b]];
+                    nxt[bkt[b]] = p;
+                }
+                p = q;
+            }
+        }
+        const int64_t b = (int64_t)(keys[i] % (uint64_t)B);
+        if (bkt[b] == EMPTY) {
+            nxt[i] = head;
+            head = i;
+            if (nxt[i] != END) bkt[(int64_t)(keys[nxt[i]] % (uint64_t)B)] = i;
+            bkt[b] = BEFORE;
+        } else if (bkt[b] == BEFORE) {
+            nxt[i] = head;
+            head = i;
+        } else {
+            nxt[i] = nxt[bkt[b]];
+            nxt[bkt[b]] = i;
+        }
+    }
+    int64_t j = 0;
+    for (int64_t p = head; p != END; p = nxt[p]) out[j++] = keys[p];
+    free(nxt);
+    free(bkt);
+    return j == k ? ORC_OK : ORC_EINVAL;
+}
+
+/* Pair set for first occurrences of (community, neighbour community). */
+static int64_t pairset_insert(uint64_t *tab, int64_t mask, uint64_t key)
+{
+    uint64_t h = key * 0x9E3779B97F4A7C15ull;
+    int64_t i = (int64_t)(h >> 20) & mask;
+    while (tab[i] != UINT64_MAX) {
+        if (tab[i] == key) return 0;
+        i = (i + 1) & mask;
+    }
+    tab[i] = key;
+    return 1;
+}
+
+/* One FIFO BFS of the super-graph from root over active nodes (the
+ * reference's superBFS): returns the number of levels after the root and
+ * the widest level; the last level is left in last[0..*nlast). */
+static void super_bfs(const int64_t *aoff, const uint32_t *adj, const int64_t *csize, uint32_t C, uint32_t root,
+                      char *vis, uint32_t *cur, uint32_t *nxtl, int64_t *ecc, int64_t *maxw, uint32_t **last,
+                      int64_t *nlast)
+{
+    memset(vis, 0, C);
+    int64_t nc = 1;
+    cur[0] = root;
+    vis[root] = 1;
+    *ecc = 0;
+    *maxw = 1;
+    for (;;) {
+        int64_t nn = 0;
+        for (int64_t i = 0; i < nc; ++i)
+            for (int64_t e = aoff[cur[i]]; e < aoff[cur[i] + 1]; ++e) {
+                const uint32_t d = adj[e];
+                if (!vis[d] && csize[d] > 0) {
+                    vis[d] = 1;
+                    nxtl[nn++] = d;
+                }
+            }
+        if (nn == 0) break;
+        ++*ecc;
+        if (nn > *maxw) *maxw = nn;
+        uint32_t *t = cur;
+        cur = nxtl;
+        nxtl = t;
+        nc = nn;
+    }
+    *last = cur;
+    *nlast = nc;
+}
+
+/* stage1Perm of sg_super_rcm.  The super-graph of every community's
+ * non-isolated vertices: edges[c] is the reference's map of neighbour
+ * communities d >= c, filled one thread in vertex order and then copied
+ * into the merged map in the per-thread map's iteration order; superAdj[c]
+ * is edges[c] without c, then every c' < c with c in edges[c'] in c'
+ * order.  George-Liu picks the start (up to 20 BFS from the first
+ * minimum-degree node, keeping the narrowest), Cuthill-McKee runs from it
+ * and then from every seed in degree order (std::sort, unstable), each node's
+ * neighbours sorted by degree (std::sort) when it leaves the queue; the order
+ * is reversed, and communities it did not reach follow in id order. */
+static int super_rcm_perm(const orc_graph *g, const uint32_t *memb, const uint32_t *deg, const int64_t *csize,
+                          uint32_t C, uint32_t *perm)
+{
+    const int64_t n = g->n;
+    int rc = ORC_ENOMEM;
+    int64_t npairs = 0, cap = 0;
+    for (int64_t u = 0; u < n; ++u) if (deg[u]) cap += deg[u];
+    int64_t tabsz = 64;
+    while (tabsz < 2 * cap) tabsz <<= 1;
+    uint64_t *tab = (uint64_t *)malloc((size_t)tabsz * sizeof(uint64_t));
+    uint64_t *pairs = (uint64_t *)malloc((size_t)(cap > 0 ? cap : 1) * sizeof(uint64_t));
+    int64_t *moff = (int64_t *)calloc((size_t)C + 1, sizeof(int64_t));
+    uint32_t *mkeys = NULL, *ord1 = NULL, *ord2 = NULL, *adj = NULL, *cur = NULL, *nxtl = NULL, *seeds = NULL,
+             *queue = NULL, *order = NULL;
+    int64_t *aoff = NULL, *fill = NULL;
+    uint64_t *rdeg = NULL;
+    char *vis = NULL;
+    if (!tab || !pairs || !moff) goto out;
+    memset(tab, 0xFF, (size_t)tabsz * sizeof(uint64_t));
+    for (int64_t u = 0; u < n; ++u) {
+        if (!deg[u]) continue;
+        const uint32_t cu = memb[u];
+        for (int64_t e = g->row_ptr[u]; e < g->row_ptr[u + 1]; ++e) {
+            const uint32_t cv = memb[g->col[e]];
+            if (cu > cv) continue;
+            const uint64_t key = ((uint64_t)cu << 32) | cv;
+            if (pairset_insert(tab, tabsz - 1, key)) pairs[npairs++] = key;
+        }
+    }
+    /* Per-map insertion sequences (stable by community). */
+    mkeys = (uint32_t *)malloc((size_t)(npairs > 0 ? npairs : 1) * sizeof(uint32_t));
+    ord1 = (uint32_t *)malloc((size_t)(npairs > 0 ? npairs : 1) * sizeof(uint32_t));
+    ord2 = (uint32_t *)malloc((size_t)(npairs > 0 ? npairs : 1) * sizeof(uint32_t));
+    fill = (int64_t *)calloc((size_t)C + 1, sizeof(int64_t));
+    if (!mkeys || !ord1 || !ord2 || !fill) goto out;
+    for (int64_t i = 0; i < npairs; ++i) moff[(pairs[i] >> 32) + 1]++;
+    for (uint32_t c = 0; c < C; ++c) moff[c + 1] += moff[c];
+    for (int64_t i = 0; i < npairs; ++i) {
+        const uint32_t c = (uint32_t)(pairs[i] >> 32);
+        mkeys[moff[c] + fill[c]++] = (uint32_t)pairs[i];
+    }
+    for (uint32_t c = 0; c < C; ++c) {
+        const int64_t len = moff[c + 1] - moff[c];
+        if (orc_umap_order(mkeys + moff[c], len, ord1 + moff[c]) != ORC_OK ||
+            orc_umap_order(ord1 + moff[c], len, ord2 + moff[c]) != ORC_OK) {
+            rc = ORC_EINVAL;
+            goto out;
+        }
+    }
+    /* superAdj. */
+    aoff = (int64_t *)calloc((size_t)C + 1, sizeof(int64_t));
+    if (!aoff) goto out;
+    for (uint32_t c = 0; c < C; ++c)
+        for (int64_t i = moff[c]; i < moff[c + 1]; ++i)
+            if (ord2[i] != c) { aoff[c + 1]++; aoff[ord2[i] + 1]++; }
+    for (uint32_t c = 0; c < C; ++c) aoff[c + 1] += aoff[c];
+    adj = (uint32_t *)malloc((size_t)(aoff[C] > 0 ? aoff[C] : 1) * sizeof(uint32_t));
+    if (!adj) goto out;
+    memset(fill, 0, ((size_t)C + 1) * sizeof(int64_t));
+    for (uint32_t c = 0; c < C; ++c)
+        for (int64_t i = moff[c]; i < moff[c + 1]; ++i)
+            if (ord2[i] != c) adj[aoff[c] + fill[c]++] = ord2[i];
+    for (uint32_t c = 0; c < C; ++c)
+        for (int64_t i = moff[c]; i < moff[c + 1]; ++i)
+            if (ord2[i] != c) adj[aoff[ord2[i]] + fill[ord2[i]]++] = c;
+    rdeg = (uint64_t *)malloc(((size_t)C + 1) * sizeof(uint64_t));
+    vis = (char *)malloc((size_t)C + 1);
+    cur = (uint32_t *)malloc(((size_t)C + 1) * sizeof(uint32_t));
+    nxtl = (uint32_t *)malloc(((size_t)C + 1) * sizeof(uint32_t));
+    seeds = (uint32_t *)malloc(((size_t)C + 1) * sizeof(uint32_t));
+    queue = (uint32_t *)malloc(((size_t)C + 1) * sizeof(uint32_t));
+    order = (uint32_t *)malloc(((size_t)C + 1) * sizeof(uint32_t));
+    if (!rdeg || !vis || !cur || !nxtl || !seeds || !queue || !order) goto out;
+    for (uint32_t c = 0; c < C; ++c) rdeg[c] = (uint64_t)(aoff[c + 1] - aoff[c]);
+
+    /* George-Liu start. */
+    int64_t first_nonempty = -1;
+    uint32_t gl = 0;
+    uint64_t mind = UINT64_MAX;
+    for (uint32_t c = 0; c < C; ++c) {
+        if (!(csize[c] > 0 && rdeg[c] > 0)) continue;
+        if (first_nonempty < 0) { first_nonempty = c; gl = c; }
+        if (rdeg[c] < mind) { mind = rdeg[c]; gl = c; }
+    }
+    uint32_t best = gl;
+    if (first_nonempty >= 0 || C > 0) {
+        int64_t prev_ecc = 0, best_w = INT64_MAX;
+        for (int it = 0; it < 20; ++it) {
+            int64_t ecc, maxw, nlast;
+            uint32_t *last;
+            super_bfs(aoff, adj, csize, C, gl, vis, cur, nxtl, &ecc, &maxw, &last, &nlast);
+            if (maxw < best_w || (maxw == best_w && ecc > prev_ecc)) { best_w = maxw; best = gl; }
+            if (ecc <= prev_ecc) break;
+            prev_ecc = ecc;
+            uint32_t nx = last[0];
+            uint64_t nd = rdeg[last[0]];
+            for (int64_t i = 1; i < nlast; ++i)
+                if (rdeg[last[i]] < nd) { nd = rdeg[last[i]]; nx = last[i]; }
+            gl = nx;
+        }
+    }
+    /* Cuthill-McKee from the start, then from every seed in degree order. */
+    for (uint32_t c = 0; c < C; ++c) seeds[c] = c;
+    if (C > 0) ls_sort(seeds, seeds + C, rdeg);
+    memset(vis, 0, C);
+    int64_t norder = 0;
+    for (int64_t s = -1; s < (int64_t)C; ++s) {
+        const uint32_t seed = s < 0 ? best : seeds[s];
+        if (C == 0 || vis[seed] || !(csize[seed] > 0)) continue;
+        int64_t qh = 0, qt = 0;
+        queue[qt++] = seed;
+        vis[seed] = 1;
+        while (qh < qt) {
+            const uint32_t u = queue[qh++];
+            order[norder++] = u;
+            uint32_t *a = adj + aoff[u], *ae = adj + aoff[u + 1];
+            if (ae > a) ls_sort(a, ae, rdeg);
+            for (; a != ae; ++a)
+                if (!vis[*a] && csize[*a] > 0) {
+                    vis[*a] = 1;
+                    queue[qt++] = *a;
+                }
+        }
+    }
+    for (uint32_t c = 0; c < C; ++c) perm[c] = UINT32_MAX;
+    for (int64_t i = 0; i < norder; ++i) perm[order[norder - 1 - i]] = (uint32_t)i;
+    {
+        uint32_t next = (uint32_t)norder;
+        for (uint32_t c = 0; c < C; ++c) if (perm[c] == UINT32_MAX) perm[c] = next++;
+    }
+    rc = ORC_OK;
+out:
+    free(tab); free(pairs); free(moff); free(mkeys); free(ord1); free(ord2); free(fill); free(aoff); free(adj);
+    free(rdeg); free(vis); free(cur); free(nxtl); free(seeds); free(queue); free(order);
+    return rc;
+}
+
+/* The reference's Hilbert index of (x, y) on an n x n grid (xy2d with its
+ * own rotation, s - 1 - x, in 32-bit unsigned arithmetic). */
+static uint64_t hilbert_xy2d(uint32_t n, uint32_t x, uint32_t y)
+{
+    uint64_t d = 0;
+    for (uint32_t s = n / 2; s > 0; s /= 2) {
+        const uint32_t rx = (x & s) > 0, ry = (y & s) > 0;
+        d += (uint64_t)s * s * ((3u * rx) ^ ry);
+        if (ry == 0) {
+            if (rx == 1) {
+                x = s - 1 - x;
+                y = s - 1 - y;
+            }
+            const uint32_t t = x;
+            x = y;
+            y = t;
+        }
+    }
+    return d;
+}
+
+typedef struct { uint64_t d; uint32_t c; } orc_hrec;
+
+static int hrec_cmp(const void *a, const void *b)
+{
+    const orc_hrec *x = (const orc_hrec *)a, *y = (const orc_hrec *)b;
+    if (x->d != y->d) return x->d < y->d ? -1 : 1;
+    return x->c < y->c ? -1 : (x->c > y->c);
+}
+
+/* stage1Perm of sg_hilbert: communities by the Hilbert index of (size,
+ * average degree), each axis scaled to [0, 255] by its maximum (at least 1). */
+static int hilbert_perm(const uint32_t *deg, const uint32_t *cverts, const int64_t *cstart, const int64_t *csize,
+                        uint32_t C, uint32_t *perm)
+{
+    uint64_t *tot = (uint64_t *)calloc((size_t)C + 1, sizeof(uint64_t));
+    orc_hrec *rec = (orc_hrec *)malloc(((size_t)C + 1) * sizeof(orc_hrec));
+    if (!tot || !rec) { free(tot); free(rec); return ORC_ENOMEM; }
+    uint64_t max_sz = 1, max_avg = 1;
+    for (uint32_t c = 0; c < C; ++c) {
+        for (int64_t i = cstart[c]; i < cstart[c + 1]; ++i) tot[c] += deg[cverts[i]];
+        if ((uint64_t)csize[c] > max_sz) max_sz = (uint64_t)csize[c];
+        const uint64_t avg = csize[c] ? tot[c] / (uint64_t)csize[c] : 0;
+        if (avg > max_avg) max_avg = avg;
+    }
+    for (uint32_t c = 0; c < C; ++c) {
+        const uint64_t avg = csize[c] ? tot[c] / (uint64_t)csize[c] : 0;
+        const uint32_t bx = (uint32_t)(((uint64_t)csize[c] * 255u) / max_sz);
+        const uint32_t by = (uint32_t)((avg * 255u) / max_avg);
+        rec[c].d = hilbert_xy2d(256, bx, by);
+        rec[c].c = c;
+    }
+    qsort(rec, C, sizeof(orc_hrec), hrec_cmp);
+    for (uint32_t i = 0; i < C; ++i) perm[rec[i].c] = i;
+    free(tot);
+    free(rec);
+    return ORC_OK;
+}
+
+/* ------------------------------------------------------------------------ */
 /* orderCompose (RG:6286-7087), super-graph order "none".                    */
 /* ------------------------------------------------------------------------ */
-typedef struct { int64_t key; uint32_t c; } orc_sortrec;
+typedef struct { int64_t key; uint32_t c, tie; } orc_sortrec;
 
 static int sortrec_cmp(const void *a, const void *b)
 {
-    /* Ascending key; equal keys keep community-id order, which is what the
-     * reference's std::stable_sort over iota(0..C) yields. */
+    /* Ascending key; equal keys keep the order the reference's
+     * std::stable_sort starts from: community ids (iota), or stage1Perm's
+     * order when a super-graph order is set (:6460-6462). */
     const orc_sortrec *x = (const orc_sortrec *)a, *y = (const orc_sortrec *)b;
     if (x->key != y->key) return x->key < y->key ? -1 : 1;
-    return x->c < y->c ? -1 : (x->c > y->c);
+    return x->tie < y->tie ? -1 : (x->tie > y->tie);
 }
 
 int orc_compose(const orc_graph *g, const uint32_t *membership,
@@ -1446,6 +1785,9 @@ int orc_compose(const orc_graph *g, const uint32_t *membership,
         cfg->intra_order != ORC_INTRA_RCMPP && cfg->intra_order != ORC_INTRA_GORDER &&
         cfg->intra_order != ORC_INTRA_RANDOM && !is_sorted_intra(cfg->intra_order))
         return ORC_EUNSUPPORTED;
+    if (cfg->super_order != ORC_SUPER_NONE && cfg->super_order != ORC_SUPER_RCM &&
+        cfg->super_order != ORC_SUPER_HILBERT)
+        return ORC_EUNSUPPORTED;
 
     int rc = ORC_ENOMEM;
     uint32_t num_comm = 0;
@@ -1462,6 +1804,7 @@ int orc_compose(const orc_graph *g, const uint32_t *membership,
     int64_t *v2l = (int64_t *)malloc((size_t)n * sizeof(int64_t));
     uint32_t *local_ids = (uint32_t *)calloc((size_t)n, sizeof(uint32_t));
     uint64_t *skey = NULL;   /* sort keys of the sorted intra orders */
+    uint32_t *stage1 = NULL; /* stage1Perm of a super-graph order */
     if (!deg || !csize || !cstart || !cverts || !recs || !offsets || !v2l || !local_ids)
         goto done;
     for (int64_t v = 0; v < n; ++v) deg[v] = (uint32_t)degree_of(g, v);
@@ -1483,7 +1826,17 @@ int orc_compose(const orc_graph *g, const uint32_t *membership,
         free(cur);
     }
 
-    /* Community order: stable sort of 0..C-1 (RG:6438-6502). */
+    /* Super-graph order (stage1Perm), then the community order: stable sort
+     * of 0..C-1 (RG:6438-6502). */
+    if (cfg->super_order != ORC_SUPER_NONE) {
+        stage1 = (uint32_t *)malloc(((size_t)num_comm + 1) * sizeof(uint32_t));
+        if (!stage1) goto done;
+        rc = cfg->super_order == ORC_SUPER_RCM
+                 ? super_rcm_perm(g, membership, deg, csize, num_comm, stage1)
+                 : hilbert_perm(deg, cverts, cstart, csize, num_comm, stage1);
+        if (rc != ORC_OK) goto done;
+        rc = ORC_ENOMEM;
+    }
     for (uint32_t c = 0; c < num_comm; ++c) {
         int64_t key = 0;
         int64_t tdeg = 0;
@@ -1499,6 +1852,7 @@ int orc_compose(const orc_graph *g, const uint32_t *membership,
         }
         recs[c].key = key;
         recs[c].c = c;
+        recs[c].tie = stage1 ? stage1[c] : c;
     }
     qsort(recs, num_comm, sizeof(orc_sortrec), sortrec_cmp);
     for (uint32_t i = 0; i < num_comm; ++i) offsets[i + 1] = offsets[i] + csize[recs[i].c];
@@ -1612,7 +1966,7 @@ int orc_compose(const orc_graph *g, const uint32_t *membership,
     rc = ORC_OK;
 done:
     free(deg); free(csize); free(cstart); free(cverts); free(recs); free(offsets);
-    free(v2l); free(local_ids); free(skey);
+    free(v2l); free(local_ids); free(skey); free(stage1);
     return rc;
 }
 

@@ -113,7 +113,18 @@ typedef struct {
     int gorder_window;    /* gw<k> */
     int gorder_fallback;  /* gordf<k>; 0 = no fallback */
     int threads;          /* 1 = serial; otherwise the OpenMP default */
+    int super_order;      /* ORC_SUPER_*: stage1Perm, the community order's tie-break */
 } orc_compose_cfg;
+
+enum {
+    ORC_SUPER_NONE = 0,
+    ORC_SUPER_RCM = 2,      /* sg_super_rcm, the reference's one-thread result */
+    ORC_SUPER_HILBERT = 4   /* sg_hilbert */
+};
+
+/* Iteration order of a libstdc++ std::unordered_map keyed by an unsigned
+ * integer after the k distinct keys are inserted in order (k <= 101473717). */
+int orc_umap_order(const uint32_t *keys, int64_t k, uint32_t *out);
 
 typedef struct {
     int64_t num_communities;   /* max(membership) + 1 */

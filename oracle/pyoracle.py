@@ -62,7 +62,10 @@ class LeidenStats(C.Structure):
 class ComposeCfg(C.Structure):
     _fields_ = [("community_order", C.c_int), ("intra_order", C.c_int),
                 ("gorder_window", C.c_int), ("gorder_fallback", C.c_int),
-                ("threads", C.c_int)]
+                ("threads", C.c_int), ("super_order", C.c_int)]
+
+
+SUPER_ORDERS = {"none": 0, "super-rcm": 2, "hilbert": 4}
 
 
 class ComposeStats(C.Structure):
@@ -122,6 +125,7 @@ def load():
         lib.orc_libstdcxx_sort.argtypes = [_u32p, C.c_int64, _u64p]
         lib.orc_libstdcxx_heap_sort.argtypes = [_u32p, C.c_int64, _u64p]
         lib.orc_random_draws.argtypes = [C.c_uint32, C.c_int64, _u32p]
+        lib.orc_umap_order.argtypes = [_u32p, C.c_int64, _u32p]
         lib.orc_pagerank_gs.restype = C.c_double
         lib.orc_pagerank_gs.argtypes = [C.POINTER(Graph), C.c_int, C.c_double, _f32p, C.c_int,
                                         C.POINTER(C.c_int)]
@@ -161,6 +165,9 @@ def _stdsort_lib():
     lib.pin_std_sort.argtypes = [_u32p, C.c_int64, _u64p]
     lib.pin_std_heap_sort.argtypes = [_u32p, C.c_int64, _u64p]
     lib.pin_std_shuffle_draws.argtypes = [C.c_uint32, C.c_int64, _u32p]
+    lib.pin_umap_order.argtypes = [_u32p, C.c_int64, _u32p]
+    lib.pin_umap_bucket_count.restype = C.c_int64
+    lib.pin_umap_bucket_count.argtypes = [C.c_int64]
     return lib
 
 
@@ -185,6 +192,30 @@ def std_shuffle_draws(seed, count):
     out = np.zeros(max(count, 1), dtype=np.uint32)
     _stdsort_lib().pin_std_shuffle_draws(seed, count, out)
     return out[:count]
+
+
+def umap_order(keys):
+    """The oracle's libstdc++ unordered_map iteration order for distinct
+    keys inserted in order."""
+    k = np.ascontiguousarray(keys, dtype=np.uint32)
+    out = np.zeros(max(len(k), 1), dtype=np.uint32)
+    if load().orc_umap_order(k, len(k), out) != 0:
+        raise RuntimeError("orc_umap_order failed")
+    return out[:len(k)]
+
+
+def std_umap_order(keys):
+    """The same from the toolchain's std::unordered_map (pin)."""
+    k = np.ascontiguousarray(keys, dtype=np.uint32)
+    out = np.zeros(max(len(k), 1), dtype=np.uint32)
+    _stdsort_lib().pin_umap_order(k, len(k), out)
+    return out[:len(k)]
+
+
+def std_umap_bucket_count(count):
+    """bucket_count() of the toolchain's std::unordered_map after count
+    distinct insertions (pin of the growth table)."""
+    return int(_stdsort_lib().pin_umap_bucket_count(count))
 
 
 def std_heap_sort(elems, key):
@@ -256,10 +287,10 @@ def leiden(row_ptr, col, resolution, max_iterations=2, max_passes=2, super_move_
 
 
 def compose(row_ptr, col, membership, community_order="size-desc", intra_order="gorder",
-            gorder_window=8, gorder_fallback=5000, threads=0):
+            gorder_window=8, gorder_fallback=5000, threads=0, super_order="none"):
     g, keep = _as_graph(row_ptr, col)
     cfg = ComposeCfg(COMM_ORDERS[community_order], INTRA_ORDERS[intra_order], gorder_window,
-                     gorder_fallback, threads)
+                     gorder_fallback, threads, SUPER_ORDERS[super_order])
     memb = np.ascontiguousarray(membership, dtype=np.uint32)
     out = np.zeros(g.n, dtype=np.int32)
     st = ComposeStats()

@@ -8,6 +8,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <random>
+#include <unordered_map>
 
 extern "C" void pin_std_sort(uint32_t* elems, int64_t count, const uint64_t* key) {
     std::sort(elems, elems + count, [key](uint32_t a, uint32_t b) { return key[a] < key[b]; });
@@ -30,4 +31,20 @@ extern "C" void pin_std_shuffle_draws(uint32_t seed, int64_t count, uint32_t* ou
         std::uniform_int_distribution<std::size_t> dist(0, (std::size_t)j);
         out[j] = (uint32_t)dist(rng);
     }
+}
+
+// Iteration order of std::unordered_map<uint32_t, float> after the keys are
+// inserted in order with operator[] (distinct keys: out gets all of them).
+extern "C" void pin_umap_order(const uint32_t* keys, int64_t count, uint32_t* out) {
+    std::unordered_map<uint32_t, float> m;
+    for (int64_t i = 0; i < count; ++i) m[keys[i]] += 1.0f;
+    int64_t j = 0;
+    for (const auto& kv : m) out[j++] = kv.first;
+}
+
+// bucket_count() after `count` distinct insertions into an empty map.
+extern "C" int64_t pin_umap_bucket_count(int64_t count) {
+    std::unordered_map<uint32_t, float> m;
+    for (int64_t i = 0; i < count; ++i) m[(uint32_t)i] += 1.0f;
+    return (int64_t)m.bucket_count();
 }
