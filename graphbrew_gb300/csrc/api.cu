@@ -169,6 +169,7 @@ gb::ComposeParams compose_params(const gb::Config& c) {
     gb::ComposeParams p;
     p.community_order = static_cast<int>(c.communityOrder);
     p.intra_order = static_cast<int>(c.intraCommunityOrder);
+    p.super_order = static_cast<int>(c.superGraphOrder);
     p.gorder_window = c.gorderWindow;
     p.gorder_fallback = c.gorderFallback;
     return p;

@@ -70,9 +70,12 @@ __global__ void k_max_u32_u64(const uint32_t* __restrict__ a, const unsigned lon
     }
 }
 
+// stage1, when given (a super-graph order), places community c at position
+// stage1[c] before the stable sort, so equal keys keep stage1's order.
 __global__ void k_comm_keys(int order, const uint32_t* __restrict__ csize, const unsigned long long* __restrict__ cdeg,
                             int64_t C, uint32_t max_size, unsigned long long max_deg,
-                            uint64_t* __restrict__ keys, uint32_t* __restrict__ ids) {
+                            const uint32_t* __restrict__ stage1, uint64_t* __restrict__ keys,
+                            uint32_t* __restrict__ ids) {
     for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C; c += (int64_t)gridDim.x * blockDim.x) {
         uint64_t k = 0;
         switch (order) {
@@ -82,8 +85,9 @@ __global__ void k_comm_keys(int order, const uint32_t* __restrict__ csize, const
             case kDegreeAsc: k = cdeg[c]; break;
             default: k = 0; break;
         }
-        keys[c] = k;
-        ids[c] = (uint32_t)c;
+        const int64_t at = stage1 ? (int64_t)stage1[c] : c;
+        keys[at] = k;
+        ids[at] = (uint32_t)c;
     }
 }
 
@@ -1282,9 +1286,14 @@ void compose_device(const DeviceCSR& g, const uint32_t* memb, const ComposeParam
         GB_LAUNCH_CHECK();
         const uint32_t max_size = read_dev(scal.get(), s);
         const unsigned long long max_deg = read_dev(maxdeg.get(), s);
+        DevBuf<uint32_t> stage1;
+        if (p.super_order != 0) {
+            stage1.alloc(C, s);
+            super_order_device(g, memb, csize, C, p.super_order, stage1, s, &launches);
+        }
         DevBuf<uint64_t> keys(C, s);
         k_comm_keys<<<grid_for(C, kT), kT, 0, s>>>(co, csize, need_deg ? cdeg.get() : nullptr, C, max_size, max_deg,
-                                                   keys, comm_order);
+                                                   stage1.get(), keys, comm_order);
         GB_LAUNCH_CHECK();
         int kbits = 0;
         if (co == kSizeDesc || co == kSizeAsc) kbits = bits_for(max_size);

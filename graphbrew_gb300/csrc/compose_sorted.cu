@@ -683,9 +683,27 @@ int64_t sorted_communities(const DeviceCSR& g, const uint32_t* memb, int intra, 
         GB_CUDA(cudaMemcpyAsync(aux, core, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
     }
 
-    Segs sg{};
     DevBuf<uint32_t> E(nn, s);
-    DevBuf<uint64_t> K(nn, s), piv(nn, s);
+    DevBuf<uint64_t> K(nn, s);
+    const int grid = grid_for(nn, kT);
+    k_sorted_keys<<<grid, kT, 0, s>>>(order_v, nn, g.row_ptr, intra, score.get(), aux.get(), E, K);
+    GB_LAUNCH_CHECK();
+    nl += 1;
+    libstdcxx_sort_segments(E, K, ranks, offs, ssize, nn, s, &nl);
+    k_sorted_local<<<grid, kT, 0, s>>>(E, nn, ranks, offs, ssize, intra == kAlternate, local);
+    GB_LAUNCH_CHECK();
+    nl += 1;
+    if (launches) *launches += nl;
+    return 0;
+}
+
+void libstdcxx_sort_segments(uint32_t* E, uint64_t* K, const uint32_t* ranks, const int64_t* offs,
+                             const int64_t* ssize, int64_t nn, cudaStream_t s, int64_t* launches) {
+    if (nn == 0) return;
+    GB_REQUIRE(nn < (int64_t)INT32_MAX, GBGPU_E_INVALID, "segmented sort: too many elements");
+    int64_t nl = 0;
+    Segs sg{};
+    DevBuf<uint64_t> piv(nn, s);
     DevBuf<int32_t> S(nn, s), end(nn, s), depth(nn, s), kcnt(nn, s), cut(nn, s), ge(nn, s), le(nn, s), L(nn, s),
         R(nn, s);
     DevBuf<uint8_t> act(nn, s);
@@ -707,11 +725,9 @@ int64_t sorted_communities(const DeviceCSR& g, const uint32_t* memb, int intra, 
     sg.R = R;
     sg.nn = nn;
     const int grid = grid_for(nn, kT);
-    k_sorted_keys<<<grid, kT, 0, s>>>(order_v, nn, g.row_ptr, intra, score.get(), aux.get(), E, K);
-    GB_LAUNCH_CHECK();
     k_seg_init<<<grid, kT, 0, s>>>(ranks, offs, ssize, sg);
     GB_LAUNCH_CHECK();
-    nl += 2;
+    nl += 1;
     DevBuf<int> any(1, s);
     // Each level halves the largest active segment or spends one unit of its
     // depth limit (<= 2 log2 nn + 2 levels).
@@ -743,11 +759,8 @@ int64_t sorted_communities(const DeviceCSR& g, const uint32_t* memb, int intra, 
     GB_LAUNCH_CHECK();
     k_seg_final<<<grid, kT, 0, s>>>(sg);
     GB_LAUNCH_CHECK();
-    k_sorted_local<<<grid, kT, 0, s>>>(E, nn, ranks, offs, ssize, intra == kAlternate, local);
-    GB_LAUNCH_CHECK();
-    nl += 3;
+    nl += 2;
     if (launches) *launches += nl;
-    return 0;
 }
 
 }  // namespace gb

@@ -1,0 +1,921 @@
+// compose_super.cu -- the super-graph orders of orderCompose on the GPU.
+//
+// A super-graph order gives stage1Perm, the community order that the
+// community-order sort keeps for equal keys
+// (bench/include/graphbrew/reorder/reorder_graphbrew.h:6395-6462).
+//
+// sg_super_rcm (:4990-5090 buildCommunitySuperGraph, :5726-5871
+// runRCMOnSuperCSR).  The reference fills per-thread std::unordered_maps, so
+// its result depends on the thread count; this is its one-thread result.
+//
+// * edges[c], the map of neighbour communities d >= c, receives its keys in
+//   the order in which vertices (ascending) and their entries meet them; the
+//   merged map receives them in the first map's iteration order.  Both
+//   iteration orders are libstdc++'s (umap_sim below): one thread simulates
+//   a map, the maps run in parallel.  First occurrences come from one stable
+//   sort of the (c, d, entry) triples.
+// * superAdj[c] = edges[c] without c, then every c' < c with c in edges[c'],
+//   by c'.
+// * George-Liu: up to 20 FIFO BFS from the first community of minimum
+//   degree, the narrowest start kept.  Cuthill-McKee from it, then from every
+//   community in degree order (std::sort, unstable: libstdcxx_sort_segments),
+//   each community's neighbours sorted by degree (std::sort) when it leaves
+//   the queue.  Every BFS started from a seed covers the seed's component,
+//   so the seeds that start one are the components' first seeds: the
+//   components run as one multi-source BFS, in the order of their first
+//   seeds (the start's component first), and the visit order is then
+//   grouped by component.  A level is exact FIFO order: a node goes to the
+//   smallest (frontier position, adjacency offset) that reaches it.
+//   The order is reversed; communities it did not reach follow by id.
+//
+// sg_hilbert (:6421-6459): communities by the Hilbert index of (size,
+// average degree), each scaled to [0, 255] by its maximum (at least 1).
+#include <algorithm>
+#include <limits>
+#include <vector>
+
+#include "gb_chunks.cuh"
+#include "gb_common.cuh"
+#include "gb_stages.h"
+
+namespace gb {
+
+namespace {
+
+constexpr int kT = 256;
+constexpr int kSuperRCM = 2, kHilbert = 4;
+
+// Bucket counts a default-constructed libstdc++ std::unordered_map goes
+// through as it grows (maximum load factor 1): 13 at the first insertion,
+// then inserting element B + 1 into B buckets rehashes to the next count.
+// Measured on the toolchain's container; the oracle's copy is pinned to it
+// by the tests.
+constexpr int kUmapSteps = 23;
+__constant__ int64_t c_umap_buckets[kUmapSteps] = {
+    13, 29, 59, 127, 257, 541, 1109, 2357, 5087, 10273, 20753, 42043, 85229, 172933, 351061, 712697, 1447153,
+    2938679, 5967347, 12117689, 24607243, 49969847, 101473717};
+const int64_t kUmapHost[kUmapSteps] = {13, 29, 59, 127, 257, 541, 1109, 2357, 5087, 10273, 20753, 42043, 85229,
+                                       172933, 351061, 712697, 1447153, 2938679, 5967347, 12117689, 24607243,
+                                       49969847, 101473717};
+constexpr int kUmapSmall = 13;                 // maps that never rehash
+constexpr int kWarpMapInts = 2048;             // per-warp shared region (keys, next, buckets)
+constexpr int kMapWarps = 4;
+constexpr int kCtaMapInts = 48 * 1024;         // CTA tier: up to 192 KB of shared memory
+
+int64_t umap_buckets_host(int64_t k) {
+    for (int i = 0; i < kUmapSteps; ++i)
+        if (kUmapHost[i] >= k) return kUmapHost[i];
+    return -1;
+}
+
+template <typename T>
+T read_dev(const T* p, cudaStream_t s) {
+    T h;
+    GB_CUDA(cudaMemcpyAsync(&h, p, sizeof(T), cudaMemcpyDeviceToHost, s));
+    GB_CUDA(cudaStreamSynchronize(s));
+    return h;
+}
+
+__device__ __forceinline__ int64_t umap_buckets(int64_t k) {
+    for (int i = 0; i < kUmapSteps; ++i)
+        if (c_umap_buckets[i] >= k) return c_umap_buckets[i];
+    return -1;
+}
+
+// Iteration order of a libstdc++ std::unordered_map keyed by an unsigned
+// integer (identity hash) after the k distinct keys are inserted in order,
+// by one thread.  One singly linked list holds all nodes and a bucket points
+// at the node before its first node (kBefore: the list head).  A key whose
+// bucket is empty goes to the front of the list, and the bucket of the old
+// front then starts after it; otherwise it goes right after its bucket's
+// before-node.  A rehash walks the list in order and puts every node back by
+// the same rules.  nxt: k entries; bkt: umap_buckets(k) entries.
+constexpr int32_t kEnd = -1, kEmpty = -1, kBefore = -2;
+
+__device__ void umap_sim(const uint32_t* keys, int32_t k, uint32_t* out, int32_t* nxt, int32_t* bkt) {
+    int32_t head = kEnd;
+    uint32_t B = 0;
+    int gi = -1;
+    for (int32_t i = 0; i < k; ++i) {
+        if ((uint32_t)i + 1u > B) {
+            B = (uint32_t)c_umap_buckets[++gi];
+            for (uint32_t b = 0; b < B; ++b) bkt[b] = kEmpty;
+            int32_t p = head, first_bkt = 0;
+            head = kEnd;
+            while (p != kEnd) {
+                const int32_t q = nxt[p];
+                const int32_t b = (int32_t)(keys[p] % B);
+                const int32_t at = bkt[b];
+                if (at == kEmpty) {
+                    nxt[p] = head;
+                    head = p;
+                    bkt[b] = kBefore;
+                    if (nxt[p] != kEnd) bkt[first_bkt] = p;
+                    first_bkt = b;
+                } else if (at == kBefore) {
+                    nxt[p] = head;
+                    head = p;
+                } else {
+                    nxt[p] = nxt[at];
+                    nxt[at] = p;
+                }
+                p = q;
+            }
+        }
+        const int32_t b = (int32_t)(keys[i] % B);
+        const int32_t at = bkt[b];
+        if (at == kEmpty) {
+            nxt[i] = head;
+            head = i;
+            if (nxt[i] != kEnd) bkt[keys[nxt[i]] % B] = i;
+            bkt[b] = kBefore;
+        } else if (at == kBefore) {
+            nxt[i] = head;
+            head = i;
+        } else {
+            nxt[i] = nxt[at];
+            nxt[at] = i;
+        }
+    }
+    int32_t j = 0;
+    for (int32_t p = head; p != kEnd; p = nxt[p]) out[j++] = keys[p];
+}
+
+// ---------------------------------------------------------------------------
+// First occurrences of (c, d), c = membership of an entry's row <= d.
+// ---------------------------------------------------------------------------
+template <bool kEmit>
+__global__ void __launch_bounds__(kT)
+k_pairs(const int64_t* __restrict__ rp, const int32_t* __restrict__ col, const uint32_t* __restrict__ memb,
+        int64_t n, int64_t nnz, const int32_t* __restrict__ chunk_row, uint8_t* __restrict__ flag,
+        const int64_t* __restrict__ pos, int cb, uint64_t* __restrict__ key, uint32_t* __restrict__ val) {
+    constexpr int kPer = kEdgeChunk / kT;
+    __shared__ int32_t srow[kEdgeChunkPadded];
+    __shared__ int32_t wmax[kT / 32];
+    const int64_t chunks = (nnz + kEdgeChunk - 1) / kEdgeChunk;
+    for (int64_t c = blockIdx.x; c < chunks; c += gridDim.x) {
+        const int64_t e0 = c * kEdgeChunk, e1 = min(nnz, e0 + kEdgeChunk);
+        chunk_entry_rows<kT>(rp, n, chunk_row[c], e0, e1, srow, wmax);
+#pragma unroll 4
+        for (int q = 0; q < kPer; ++q) {
+            const int i = q * kT + threadIdx.x;
+            const int64_t e = e0 + i;
+            if (e >= e1) continue;
+            const uint32_t cu = memb[srow[chunk_pad(i)]], cv = memb[col[e]];
+            if (!kEmit) {
+                flag[e] = cu <= cv ? 1 : 0;
+            } else if (cu <= cv) {
+                const int64_t at = pos[e];
+                key[at] = ((uint64_t)cu << cb) | cv;
+                val[at] = (uint32_t)e;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_run_flags(const uint64_t* __restrict__ key, int64_t m, uint8_t* __restrict__ flag) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
+        flag[i] = (i == 0 || key[i] != key[i - 1]) ? 1 : 0;
+}
+
+// Unique pairs: key2 = (c, first entry) with d as value for the per-map
+// insertion order; map sizes; communities with a self pair; the reverse
+// pairs (d, c), c < d, flagged for their own list.
+__global__ void k_unique_emit(const uint64_t* __restrict__ key, const uint32_t* __restrict__ val, int64_t m,
+                              const uint8_t* __restrict__ flag, const int64_t* __restrict__ pos, int cb, int eb,
+                              uint64_t* __restrict__ key2, uint32_t* __restrict__ d2, uint32_t* __restrict__ msize,
+                              uint8_t* __restrict__ self_pair, uint8_t* __restrict__ rflag) {
+    const uint64_t dmask = (1ull << cb) - 1ull;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        if (!flag[i]) continue;
+        const int64_t j = pos[i];
+        const uint32_t c = (uint32_t)(key[i] >> cb), d = (uint32_t)(key[i] & dmask);
+        key2[j] = ((uint64_t)c << eb) | val[i];
+        d2[j] = d;
+        atomicAdd(&msize[c], 1u);
+        if (c == d) self_pair[c] = 1;
+        rflag[j] = c < d ? 1 : 0;
+    }
+}
+
+__global__ void k_reverse_emit(const uint64_t* __restrict__ key2, const uint32_t* __restrict__ d2, int64_t m, int eb,
+                               int cb, const uint8_t* __restrict__ rflag, const int64_t* __restrict__ rpos,
+                               uint64_t* __restrict__ rkey, uint32_t* __restrict__ rval) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+        if (!rflag[j]) continue;
+        const uint32_t c = (uint32_t)(key2[j] >> eb);
+        rkey[rpos[j]] = ((uint64_t)d2[j] << cb) | c;
+        rval[rpos[j]] = c;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Map simulations: edges[c]'s first map (keys in first-occurrence order)
+// and the merged map (keys in the first map's order) -> ord2.  Three tiers
+// by size: a thread per map that never rehashes, a warp per map in a
+// shared region, a CTA per map in up to 192 KB of shared memory, or global
+// scratch above that.
+// ---------------------------------------------------------------------------
+__global__ void k_umap_small(const int64_t* __restrict__ moff, const uint32_t* __restrict__ msize, int64_t C,
+                             const uint32_t* __restrict__ d2, uint32_t* __restrict__ ord1,
+                             uint32_t* __restrict__ ord2) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C; c += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t k = (int32_t)msize[c];
+        if (k == 0 || k > kUmapSmall) continue;
+        int32_t nxt[kUmapSmall], bkt[kUmapSmall];
+        const int64_t b = moff[c];
+        umap_sim(d2 + b, k, ord1 + b, nxt, bkt);
+        umap_sim(ord1 + b, k, ord2 + b, nxt, bkt);
+    }
+}
+
+__global__ void __launch_bounds__(kMapWarps * 32)
+k_umap_warp(const int32_t* __restrict__ list, int32_t cnt, const int64_t* __restrict__ moff,
+            const uint32_t* __restrict__ msize, const uint32_t* __restrict__ d2, uint32_t* __restrict__ ord1,
+            uint32_t* __restrict__ ord2) {
+    __shared__ int32_t region[kMapWarps][kWarpMapInts];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int64_t q = (int64_t)blockIdx.x * kMapWarps + w; q < cnt; q += (int64_t)gridDim.x * kMapWarps) {
+        const int32_t c = list[q];
+        const int32_t k = (int32_t)msize[c];
+        const int64_t b = moff[c];
+        uint32_t* keys = reinterpret_cast<uint32_t*>(region[w]);
+        int32_t* nxt = region[w] + k;
+        int32_t* bkt = region[w] + 2 * k;
+        for (int pass = 0; pass < 2; ++pass) {
+            const uint32_t* src = pass == 0 ? d2 + b : ord1 + b;
+            for (int32_t i = lane; i < k; i += 32) keys[i] = src[i];
+            __syncwarp();
+            if (lane == 0) umap_sim(keys, k, (pass == 0 ? ord1 : ord2) + b, nxt, bkt);
+            __syncwarp();
+        }
+    }
+}
+
+__global__ void k_umap_cta(const int32_t* __restrict__ list, int32_t cnt, const int64_t* __restrict__ moff,
+                           const uint32_t* __restrict__ msize, const uint32_t* __restrict__ d2,
+                           uint32_t* __restrict__ ord1, uint32_t* __restrict__ ord2, int32_t* __restrict__ gscratch,
+                           const int64_t* __restrict__ goff, int smem_ints) {
+    extern __shared__ int32_t dyn[];
+    for (int64_t q = blockIdx.x; q < cnt; q += gridDim.x) {
+        const int32_t c = list[q];
+        const int32_t k = (int32_t)msize[c];
+        const int64_t b = moff[c];
+        const int64_t need = 2 * (int64_t)k + umap_buckets(k);
+        int32_t* base = need <= smem_ints ? dyn : gscratch + goff[q];
+        uint32_t* keys = reinterpret_cast<uint32_t*>(base);
+        int32_t* nxt = base + k;
+        int32_t* bkt = base + 2 * k;
+        for (int pass = 0; pass < 2; ++pass) {
+            const uint32_t* src = pass == 0 ? d2 + b : ord1 + b;
+            for (int32_t i = threadIdx.x; i < k; i += blockDim.x) keys[i] = src[i];
+            __syncthreads();
+            if (threadIdx.x == 0) umap_sim(keys, k, (pass == 0 ? ord1 : ord2) + b, nxt, bkt);
+            __syncthreads();
+        }
+    }
+}
+
+// Maps above the small tier, by tier: 1 warp, 2 CTA.
+__global__ void k_map_tiers(const uint32_t* __restrict__ msize, int64_t C, int smem_ints, int32_t* __restrict__ lists,
+                            int32_t* __restrict__ counts) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C; c += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t k = msize[c];
+        if (k <= kUmapSmall) continue;
+        const int64_t need = 2 * k + umap_buckets(k);
+        const int tier = need <= kWarpMapInts ? 0 : 1;
+        const int32_t at = atomicAdd(&counts[tier], 1);
+        lists[(int64_t)tier * C + at] = (int32_t)c;
+    }
+}
+
+__global__ void k_cta_need(const int32_t* __restrict__ list, int32_t cnt, const uint32_t* __restrict__ msize,
+                           int smem_ints, int64_t* __restrict__ gneed) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < cnt; q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t k = msize[list[q]];
+        const int64_t need = 2 * k + umap_buckets(k);
+        gneed[q] = need <= smem_ints ? 0 : need;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// superAdj
+// ---------------------------------------------------------------------------
+// Position of c inside its merged map (k when absent) and own counts.
+__global__ void k_self_pos(const int64_t* __restrict__ moff, const uint32_t* __restrict__ msize,
+                           const uint8_t* __restrict__ self_pair, const uint32_t* __restrict__ ord2, int64_t C,
+                           uint32_t* __restrict__ spos, int64_t* __restrict__ adeg) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C; c += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t k = msize[c];
+        uint32_t at = k;
+        if (self_pair[c]) {
+            const int64_t b = moff[c];
+            for (uint32_t i = 0; i < k; ++i)
+                if (ord2[b + i] == (uint32_t)c) { at = i; break; }
+        }
+        spos[c] = at;
+        adeg[c] = (int64_t)k - (self_pair[c] ? 1 : 0);
+    }
+}
+
+__global__ void k_reverse_counts(const uint64_t* __restrict__ rkey, int64_t mr, int cb, int64_t* __restrict__ adeg,
+                                 uint32_t* __restrict__ rcnt) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < mr; r += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t d = (uint32_t)(rkey[r] >> cb);
+        atomicAdd(reinterpret_cast<unsigned long long*>(&adeg[d]), 1ull);
+        atomicAdd(&rcnt[d], 1u);
+    }
+}
+
+__global__ void k_adj_own(const uint64_t* __restrict__ key2, int64_t m, int eb, const int64_t* __restrict__ moff,
+                          const uint32_t* __restrict__ spos, const uint32_t* __restrict__ ord2,
+                          const int64_t* __restrict__ aoff, uint32_t* __restrict__ adj, uint32_t* __restrict__ asrc) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t c = (uint32_t)(key2[i] >> eb);
+        const uint32_t d = ord2[i];
+        if (d == c) continue;
+        const uint32_t j = (uint32_t)(i - moff[c]);
+        const int64_t at = aoff[c] + j - (spos[c] < j ? 1 : 0);
+        adj[at] = d;
+        asrc[at] = c;
+    }
+}
+
+__global__ void k_adj_rev(const uint64_t* __restrict__ rkey, const uint32_t* __restrict__ rval, int64_t mr, int cb,
+                          const int64_t* __restrict__ rstart, const int64_t* __restrict__ aoff,
+                          const uint32_t* __restrict__ msize, const uint8_t* __restrict__ self_pair,
+                          uint32_t* __restrict__ adj, uint32_t* __restrict__ asrc) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < mr; r += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t d = (uint32_t)(rkey[r] >> cb);
+        const int64_t own = (int64_t)msize[d] - (self_pair[d] ? 1 : 0);
+        const int64_t at = aoff[d] + own + (r - rstart[d]);
+        adj[at] = rval[r];
+        asrc[at] = d;
+    }
+}
+
+__global__ void k_deg_keys(const int64_t* __restrict__ aoff, int64_t C, const uint32_t* __restrict__ csize,
+                           uint64_t* __restrict__ rdeg, uint8_t* __restrict__ active,
+                           unsigned long long* __restrict__ first_min) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C; c += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t d = (uint64_t)(aoff[c + 1] - aoff[c]);
+        rdeg[c] = d;
+        active[c] = csize[c] > 0 ? 1 : 0;
+        if (csize[c] > 0 && d > 0) atomicMin(first_min, (d << 32) | (uint64_t)c);
+    }
+}
+
+// Sort keys of the adjacency entries: the neighbour's degree.
+__global__ void k_adj_keys(const uint32_t* __restrict__ adj, int64_t A, const uint64_t* __restrict__ rdeg,
+                           uint64_t* __restrict__ K) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < A; i += (int64_t)gridDim.x * blockDim.x)
+        K[i] = rdeg[adj[i]];
+}
+
+__global__ void k_iota_keys(int64_t C, const uint64_t* __restrict__ rdeg, uint32_t* __restrict__ E,
+                            uint64_t* __restrict__ K, uint32_t* __restrict__ zero_rank) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C; c += (int64_t)gridDim.x * blockDim.x) {
+        E[c] = (uint32_t)c;
+        K[c] = rdeg[c];
+        zero_rank[c] = 0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// FIFO BFS, one level at a time.  The frontier F (nf nodes, in order) expands
+// into T = sum of its degrees entries t; the entry's neighbour is claimed by
+// the smallest t that reaches it while unvisited and active; the claimed
+// nodes, in t order, are the next frontier.
+// ---------------------------------------------------------------------------
+__global__ void k_bfs_degrees(const uint32_t* __restrict__ F, int64_t nf, const int64_t* __restrict__ aoff,
+                              int64_t* __restrict__ D) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nf; i += (int64_t)gridDim.x * blockDim.x)
+        D[i] = aoff[F[i] + 1] - aoff[F[i]];
+}
+
+__device__ __forceinline__ int64_t frontier_of(const int64_t* __restrict__ D, int64_t nf, int64_t t) {
+    int64_t lo = 0, hi = nf - 1;   // last i with D[i] <= t
+    while (lo < hi) {
+        const int64_t mid = (lo + hi + 1) >> 1;
+        if (D[mid] <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int kPhase>
+__global__ void k_bfs_level(const uint32_t* __restrict__ F, int64_t nf, const int64_t* __restrict__ D, int64_t T,
+                            const int64_t* __restrict__ aoff, const uint32_t* __restrict__ adj,
+                            const uint8_t* __restrict__ active, uint8_t* __restrict__ vis,
+                            unsigned long long* __restrict__ claim, uint8_t* __restrict__ flag,
+                            const int64_t* __restrict__ P, uint32_t* __restrict__ NF, uint32_t* __restrict__ comp) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < T; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = frontier_of(D, nf, t);
+        const uint32_t u = F[i];
+        const uint32_t v = adj[aoff[u] + (t - D[i])];
+        if (kPhase == 0) {
+            if (!vis[v] && active[v]) atomicMin(&claim[v], (unsigned long long)t);
+        } else if (kPhase == 1) {
+            flag[t] = (!vis[v] && active[v] && claim[v] == (unsigned long long)t) ? 1 : 0;
+        } else if (flag[t]) {
+            NF[P[t]] = v;
+            vis[v] = 1;
+            if (comp) comp[v] = comp[u];
+        }
+    }
+}
+
+__global__ void k_mark_roots(const uint32_t* __restrict__ R, int64_t nr, uint8_t* __restrict__ vis,
+                             uint32_t* __restrict__ comp) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nr; i += (int64_t)gridDim.x * blockDim.x) {
+        vis[R[i]] = 1;
+        if (comp) comp[R[i]] = (uint32_t)i;
+    }
+}
+
+__global__ void k_level_first_min(const uint32_t* __restrict__ L, int64_t nl, const uint64_t* __restrict__ rdeg,
+                                  unsigned long long* __restrict__ best) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nl; i += (int64_t)gridDim.x * blockDim.x)
+        atomicMin(best, (rdeg[L[i]] << 32) | (uint64_t)i);
+}
+
+// ---------------------------------------------------------------------------
+// Components of the active communities (hook to the smaller label, then
+// pointer jumping, until nothing changes) and their first seeds.
+// ---------------------------------------------------------------------------
+__global__ void k_cc_init(uint32_t* __restrict__ label, int64_t C) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C; c += (int64_t)gridDim.x * blockDim.x)
+        label[c] = (uint32_t)c;
+}
+
+__global__ void k_cc_hook(const uint32_t* __restrict__ asrc, const uint32_t* __restrict__ adj, int64_t A,
+                          uint32_t* __restrict__ label, int* __restrict__ changed) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < A; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t a = label[asrc[i]], b = label[adj[i]];
+        if (a != b) {
+            atomicMin(&label[max(a, b)], min(a, b));
+            *changed = 1;
+        }
+    }
+}
+
+__global__ void k_cc_jump(uint32_t* __restrict__ label, int64_t C, int* __restrict__ changed) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C; c += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t l = label[c], ll = label[l];
+        if (ll != l) {
+            label[c] = ll;
+            *changed = 1;
+        }
+    }
+}
+
+// First seed of each component: seed position + 1, or 0 for the start's.
+__global__ void k_first_seed(const uint32_t* __restrict__ seeds, int64_t C, const uint8_t* __restrict__ active,
+                             const uint32_t* __restrict__ label, uint32_t start_label, uint32_t* __restrict__ first) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < C; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t c = seeds[i];
+        if (!active[c]) continue;
+        const uint32_t l = label[c];
+        atomicMin(&first[l], l == start_label ? 0u : (uint32_t)i + 1u);
+    }
+}
+
+// Roots (one per component, keyed by its first seed) for the sort.
+__global__ void k_root_keys(const uint32_t* __restrict__ first, const uint32_t* __restrict__ seeds, int64_t C,
+                            uint32_t start, int* __restrict__ cnt, uint64_t* __restrict__ rk,
+                            uint32_t* __restrict__ rv) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C; c += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t f = first[c];
+        if (f == 0xFFFFFFFFu) continue;   // not a component's label
+        const int at = atomicAdd(cnt, 1);
+        rk[at] = f;
+        rv[at] = f == 0 ? start : seeds[f - 1];
+    }
+}
+
+__global__ void k_comp_of_order(const uint32_t* __restrict__ order, int64_t no, const uint32_t* __restrict__ comp,
+                                uint32_t* __restrict__ key) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < no; i += (int64_t)gridDim.x * blockDim.x)
+        key[i] = comp[order[i]];
+}
+
+__global__ void k_rcm_perm(const uint32_t* __restrict__ order, int64_t no, uint32_t* __restrict__ perm) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < no; i += (int64_t)gridDim.x * blockDim.x)
+        perm[order[i]] = (uint32_t)(no - 1 - i);
+}
+
+__global__ void k_unreached_flags(const uint32_t* __restrict__ perm, int64_t C, int32_t* __restrict__ flag) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C; c += (int64_t)gridDim.x * blockDim.x)
+        flag[c] = perm[c] == 0xFFFFFFFFu ? 1 : 0;
+}
+
+__global__ void k_unreached_assign(const int32_t* __restrict__ flag, const int64_t* __restrict__ pos, int64_t C,
+                                   int64_t no, uint32_t* __restrict__ perm) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C; c += (int64_t)gridDim.x * blockDim.x)
+        if (flag[c]) perm[c] = (uint32_t)(no + pos[c]);
+}
+
+// ---------------------------------------------------------------------------
+// Hilbert
+// ---------------------------------------------------------------------------
+__global__ void k_comm_degree_sums(const int64_t* __restrict__ rp, const uint32_t* __restrict__ memb, int64_t n,
+                                   unsigned long long* __restrict__ tot) {
+    const int lane = threadIdx.x & 31;
+    for (int64_t v0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; v0 < n;
+         v0 += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t v = v0 + lane;
+        const int64_t d = v < n ? rp[v + 1] - rp[v] : 0;
+        warp_add_u64(tot, d ? memb[v] : 0u, (unsigned long long)d, d != 0);
+    }
+}
+
+__global__ void k_hilbert_max(const uint32_t* __restrict__ csize, const unsigned long long* __restrict__ tot,
+                              int64_t C, unsigned long long* __restrict__ mx) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C; c += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned long long sz = csize[c];
+        atomicMax(&mx[0], sz);
+        if (sz) atomicMax(&mx[1], tot[c] / sz);
+    }
+}
+
+// The reference's xy2d, with its rotation s - 1 - x in 32-bit arithmetic.
+__device__ uint64_t hilbert_xy2d(uint32_t n, uint32_t x, uint32_t y) {
+    uint64_t d = 0;
+    for (uint32_t s = n / 2; s > 0; s /= 2) {
+        const uint32_t rx = (x & s) > 0, ry = (y & s) > 0;
+        d += (uint64_t)s * s * ((3u * rx) ^ ry);
+        if (ry == 0) {
+            if (rx == 1) {
+                x = s - 1 - x;
+                y = s - 1 - y;
+            }
+            const uint32_t t = x;
+            x = y;
+            y = t;
+        }
+    }
+    return d;
+}
+
+__global__ void k_hilbert_keys(const uint32_t* __restrict__ csize, const unsigned long long* __restrict__ tot,
+                               int64_t C, const unsigned long long* __restrict__ mx, uint64_t* __restrict__ key,
+                               uint32_t* __restrict__ ids) {
+    const unsigned long long max_sz = max(mx[0], 1ull), max_avg = max(mx[1], 1ull);
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C; c += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned long long sz = csize[c];
+        const unsigned long long avg = sz ? tot[c] / sz : 0ull;
+        const uint32_t bx = (uint32_t)((sz * 255ull) / max_sz);
+        const uint32_t by = (uint32_t)((avg * 255ull) / max_avg);
+        key[c] = hilbert_xy2d(256, bx, by);
+        ids[c] = (uint32_t)c;
+    }
+}
+
+__global__ void k_perm_from_order(const uint32_t* __restrict__ ids, int64_t C, uint32_t* __restrict__ perm) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < C; i += (int64_t)gridDim.x * blockDim.x)
+        perm[ids[i]] = (uint32_t)i;
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+struct BfsResult {
+    int64_t visited = 0;                 // nodes written to order
+    std::vector<int64_t> level_start;    // offsets into order of each level
+};
+
+// FIFO BFS from roots (in order) over active nodes; visit order into order
+// (roots first).  comp, if given, gets the root's index for every node.
+BfsResult fifo_bfs(const uint32_t* roots, int64_t nr, int64_t C, const int64_t* aoff, const uint32_t* adj,
+                   const uint8_t* active, uint8_t* vis, unsigned long long* claim, uint32_t* order, uint32_t* comp,
+                   cudaStream_t s, int64_t* nl) {
+    BfsResult r;
+    GB_CUDA(cudaMemsetAsync(vis, 0, C, s));
+    GB_CUDA(cudaMemsetAsync(claim, 0xFF, C * sizeof(unsigned long long), s));
+    GB_CUDA(cudaMemcpyAsync(order, roots, nr * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+    k_mark_roots<<<grid_for(nr, kT), kT, 0, s>>>(roots, nr, vis, comp);
+    GB_LAUNCH_CHECK();
+    *nl += 1;
+    int64_t f0 = 0, nf = nr;
+    r.level_start.push_back(0);
+    DevBuf<int64_t> D;
+    while (nf > 0) {
+        const uint32_t* F = order + f0;
+        D.alloc(nf + 1, s);
+        k_bfs_degrees<<<grid_for(nf, kT), kT, 0, s>>>(F, nf, aoff, D);
+        GB_LAUNCH_CHECK();
+        exclusive_scan_i64_total(D, D, nf, D.get() + nf, s);
+        const int64_t T = read_dev(D.get() + nf, s);
+        *nl += 4;
+        int64_t next = 0;
+        if (T > 0) {
+            DevBuf<uint8_t> flag(T, s);
+            DevBuf<int64_t> P(T + 1, s);
+            const int grid = grid_for(T, kT);
+            k_bfs_level<0><<<grid, kT, 0, s>>>(F, nf, D, T, aoff, adj, active, vis, claim, nullptr, nullptr, nullptr,
+                                               nullptr);
+            GB_LAUNCH_CHECK();
+            k_bfs_level<1><<<grid, kT, 0, s>>>(F, nf, D, T, aoff, adj, active, vis, claim, flag, nullptr, nullptr,
+                                               nullptr);
+            GB_LAUNCH_CHECK();
+            exclusive_scan_u8_to_i64(flag, P, T, P.get() + T, s);
+            k_bfs_level<2><<<grid, kT, 0, s>>>(F, nf, D, T, aoff, adj, active, vis, claim, flag, P,
+                                               order + f0 + nf, comp);
+            GB_LAUNCH_CHECK();
+            next = read_dev(P.get() + T, s);
+            *nl += 6;
+        }
+        f0 += nf;
+        nf = next;
+        if (nf > 0) r.level_start.push_back(f0);
+    }
+    r.visited = f0;
+    return r;
+}
+
+void hilbert_perm(const DeviceCSR& g, const uint32_t* memb, const uint32_t* csize, int64_t C, uint32_t* perm,
+                  cudaStream_t s, int64_t* nl) {
+    DevBuf<unsigned long long> tot(C, s), mx(2, s);
+    GB_CUDA(cudaMemsetAsync(tot, 0, C * sizeof(unsigned long long), s));
+    GB_CUDA(cudaMemsetAsync(mx, 0, 2 * sizeof(unsigned long long), s));
+    k_comm_degree_sums<<<grid_for(g.n, kT), kT, 0, s>>>(g.row_ptr, memb, g.n, tot);
+    GB_LAUNCH_CHECK();
+    k_hilbert_max<<<grid_for(C, kT), kT, 0, s>>>(csize, tot, C, mx);
+    GB_LAUNCH_CHECK();
+    DevBuf<uint64_t> key(C, s);
+    DevBuf<uint32_t> ids(C, s);
+    k_hilbert_keys<<<grid_for(C, kT), kT, 0, s>>>(csize, tot, C, mx, key, ids);
+    GB_LAUNCH_CHECK();
+    radix_sort_pairs_u64(key, ids, C, 16, s);   // d < 2^16; stable: ties by id
+    k_perm_from_order<<<grid_for(C, kT), kT, 0, s>>>(ids, C, perm);
+    GB_LAUNCH_CHECK();
+    *nl += 4 + 3 * 2;
+}
+
+void super_rcm_perm(const DeviceCSR& g, const uint32_t* memb, const uint32_t* csize, int64_t C, uint32_t* perm,
+                    cudaStream_t s, int64_t* nl) {
+    const int64_t n = g.n, nnz = g.nnz;
+    GB_REQUIRE(nnz < (int64_t)0xFFFFFFFFll, GBGPU_E_UNSUPPORTED, "sg_super_rcm: more than 2^32 - 1 entries");
+    const int cb = std::max(1, bits_for((uint64_t)(C - 1)));
+    const int eb = std::max(1, bits_for((uint64_t)(nnz > 0 ? nnz - 1 : 0)));
+    DevBuf<uint32_t> msize(C, s);
+    DevBuf<uint8_t> self_pair(C, s);
+    GB_CUDA(cudaMemsetAsync(msize, 0, C * sizeof(uint32_t), s));
+    GB_CUDA(cudaMemsetAsync(self_pair, 0, C, s));
+    // ---- first occurrences ----
+    int64_t m = 0;
+    DevBuf<uint64_t> key2;
+    DevBuf<uint32_t> d2;
+    DevBuf<uint8_t> rflag;
+    if (nnz > 0) {
+        DevBuf<int32_t> crow(edge_chunks(nnz), s);
+        chunk_rows_device(g.row_ptr, n, nnz, crow, s);
+        DevBuf<uint8_t> flag(nnz, s);
+        DevBuf<int64_t> pos(nnz + 1, s);
+        const int egrid = (int)std::min<int64_t>(edge_chunks(nnz), (int64_t)kNumSMs * 8);
+        k_pairs<false><<<egrid, kT, 0, s>>>(g.row_ptr, g.col, memb, n, nnz, crow, flag, nullptr, cb, nullptr,
+                                            nullptr);
+        GB_LAUNCH_CHECK();
+        exclusive_scan_u8_to_i64(flag, pos, nnz, pos.get() + nnz, s);
+        const int64_t m0 = read_dev(pos.get() + nnz, s);
+        DevBuf<uint64_t> key(m0 > 0 ? m0 : 1, s);
+        DevBuf<uint32_t> val(m0 > 0 ? m0 : 1, s);
+        k_pairs<true><<<egrid, kT, 0, s>>>(g.row_ptr, g.col, memb, n, nnz, crow, flag, pos, cb, key, val);
+        GB_LAUNCH_CHECK();
+        *nl += 5;
+        if (m0 > 0) {
+            radix_sort_pairs_u64(key, val, m0, 2 * cb, s);   // stable: entries ascending inside a pair
+            DevBuf<uint8_t> uflag(m0, s);
+            DevBuf<int64_t> upos(m0 + 1, s);
+            k_run_flags<<<grid_for(m0, kT), kT, 0, s>>>(key, m0, uflag);
+            GB_LAUNCH_CHECK();
+            exclusive_scan_u8_to_i64(uflag, upos, m0, upos.get() + m0, s);
+            m = read_dev(upos.get() + m0, s);
+            key2.alloc(m, s);
+            d2.alloc(m, s);
+            rflag.alloc(m, s);
+            k_unique_emit<<<grid_for(m0, kT), kT, 0, s>>>(key, val, m0, uflag, upos, cb, eb, key2, d2, msize,
+                                                          self_pair, rflag);
+            GB_LAUNCH_CHECK();
+            *nl += 6 + 3 * ((2 * cb + 7) / 8);
+        }
+    }
+    // Reverse pairs (d, c), c < d, by d then c.
+    int64_t mr = 0;
+    DevBuf<uint64_t> rkey;
+    DevBuf<uint32_t> rval;
+    if (m > 0) {
+        DevBuf<int64_t> rpos(m + 1, s);
+        exclusive_scan_u8_to_i64(rflag, rpos, m, rpos.get() + m, s);
+        mr = read_dev(rpos.get() + m, s);
+        rkey.alloc(mr > 0 ? mr : 1, s);
+        rval.alloc(mr > 0 ? mr : 1, s);
+        k_reverse_emit<<<grid_for(m, kT), kT, 0, s>>>(key2, d2, m, eb, cb, rflag, rpos, rkey, rval);
+        GB_LAUNCH_CHECK();
+        if (mr > 0) radix_sort_pairs_u64(rkey, rval, mr, 2 * cb, s);
+        // Per-map insertion order: by community, then first entry.
+        radix_sort_pairs_u64(key2, d2, m, cb + eb, s);
+        *nl += 4 + 3 * ((2 * cb + 7) / 8) + 3 * ((cb + eb + 7) / 8);
+    }
+    DevBuf<int64_t> moff(C + 1, s);
+    {
+        DevBuf<int32_t> ms32(C, s);
+        GB_CUDA(cudaMemcpyAsync(ms32, msize, C * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+        exclusive_scan_i32_to_i64(ms32, moff, C, moff.get() + C, s);
+        *nl += 3;
+    }
+    // ---- map simulations ----
+    DevBuf<uint32_t> ord1(m > 0 ? m : 1, s), ord2(m > 0 ? m : 1, s);
+    if (m > 0) {
+        GB_REQUIRE(umap_buckets_host(m) > 0, GBGPU_E_UNSUPPORTED, "sg_super_rcm: a community map is too large");
+        k_umap_small<<<grid_for(C, kT), kT, 0, s>>>(moff, msize, C, d2, ord1, ord2);
+        GB_LAUNCH_CHECK();
+        DevBuf<int32_t> lists(2 * C, s);
+        DevBuf<int32_t> counts(2, s);
+        GB_CUDA(cudaMemsetAsync(counts, 0, 2 * sizeof(int32_t), s));
+        k_map_tiers<<<grid_for(C, kT), kT, 0, s>>>(msize, C, kCtaMapInts, lists, counts);
+        GB_LAUNCH_CHECK();
+        int32_t hc[2];
+        GB_CUDA(cudaMemcpyAsync(hc, counts, sizeof(hc), cudaMemcpyDeviceToHost, s));
+        GB_CUDA(cudaStreamSynchronize(s));
+        *nl += 2;
+        if (hc[0] > 0) {
+            const int grid = (int)std::min<int64_t>(ceil_div(hc[0], kMapWarps), (int64_t)kNumSMs * 8);
+            k_umap_warp<<<grid, kMapWarps * 32, 0, s>>>(lists, hc[0], moff, msize, d2, ord1, ord2);
+            GB_LAUNCH_CHECK();
+            *nl += 1;
+        }
+        if (hc[1] > 0) {
+            const int32_t* clist = lists.get() + C;
+            DevBuf<int64_t> goff(hc[1] + 1, s);
+            k_cta_need<<<grid_for(hc[1], kT), kT, 0, s>>>(clist, hc[1], msize, kCtaMapInts, goff);
+            GB_LAUNCH_CHECK();
+            exclusive_scan_i64_total(goff, goff, hc[1], goff.get() + hc[1], s);
+            const int64_t gtot = read_dev(goff.get() + hc[1], s);
+            DevBuf<int32_t> gscratch(gtot > 0 ? gtot : 1, s);
+            const int smem = kCtaMapInts * (int)sizeof(int32_t);
+            GB_CUDA(cudaFuncSetAttribute(k_umap_cta, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+            const int grid = (int)std::min<int64_t>(hc[1], (int64_t)kNumSMs);
+            k_umap_cta<<<grid, 32, smem, s>>>(clist, hc[1], moff, msize, d2, ord1, ord2, gscratch, goff, kCtaMapInts);
+            GB_LAUNCH_CHECK();
+            *nl += 4;
+        }
+    }
+    // ---- superAdj ----
+    DevBuf<uint32_t> spos(C, s), rcnt(C, s);
+    DevBuf<int64_t> adeg(C, s), aoff(C + 1, s), rstart(C + 1, s);
+    k_self_pos<<<grid_for(C, kT), kT, 0, s>>>(moff, msize, self_pair, ord2, C, spos, adeg);
+    GB_LAUNCH_CHECK();
+    GB_CUDA(cudaMemsetAsync(rcnt, 0, C * sizeof(uint32_t), s));
+    if (mr > 0) {
+        k_reverse_counts<<<grid_for(mr, kT), kT, 0, s>>>(rkey, mr, cb, adeg, rcnt);
+        GB_LAUNCH_CHECK();
+    }
+    exclusive_scan_i64_total(adeg, aoff, C, aoff.get() + C, s);
+    {
+        DevBuf<int32_t> r32(C, s);
+        GB_CUDA(cudaMemcpyAsync(r32, rcnt, C * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+        exclusive_scan_i32_to_i64(r32, rstart, C, rstart.get() + C, s);
+    }
+    const int64_t A = read_dev(aoff.get() + C, s);
+    GB_REQUIRE(A < (int64_t)INT32_MAX, GBGPU_E_UNSUPPORTED, "sg_super_rcm: super-graph too large");
+    DevBuf<uint32_t> adj(A > 0 ? A : 1, s), asrc(A > 0 ? A : 1, s);
+    if (m > 0) {
+        k_adj_own<<<grid_for(m, kT), kT, 0, s>>>(key2, m, eb, moff, spos, ord2, aoff, adj, asrc);
+        GB_LAUNCH_CHECK();
+    }
+    if (mr > 0) {
+        k_adj_rev<<<grid_for(mr, kT), kT, 0, s>>>(rkey, rval, mr, cb, rstart, aoff, msize, self_pair, adj, asrc);
+        GB_LAUNCH_CHECK();
+    }
+    DevBuf<uint64_t> rdeg(C, s);
+    DevBuf<uint8_t> active(C, s);
+    DevBuf<unsigned long long> first_min(1, s);
+    GB_CUDA(cudaMemsetAsync(first_min, 0xFF, sizeof(unsigned long long), s));
+    k_deg_keys<<<grid_for(C, kT), kT, 0, s>>>(aoff, C, csize, rdeg, active, first_min);
+    GB_LAUNCH_CHECK();
+    *nl += 12;
+
+    // ---- George-Liu ----
+    DevBuf<uint8_t> vis(C, s);
+    DevBuf<unsigned long long> claim(C, s), best_key(1, s);
+    DevBuf<uint32_t> order(C, s), root(1, s);
+    const unsigned long long fm = read_dev(first_min.get(), s);
+    uint32_t gl = fm == ~0ull ? 0u : (uint32_t)(fm & 0xFFFFFFFFull);
+    uint32_t best = gl;
+    {
+        int64_t prev_ecc = 0, best_w = std::numeric_limits<int64_t>::max();
+        for (int it = 0; it < 20; ++it) {
+            GB_CUDA(cudaMemcpyAsync(root, &gl, sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+            const BfsResult r = fifo_bfs(root, 1, C, aoff, adj, active, vis, claim, order, nullptr, s, nl);
+            const int64_t ecc = (int64_t)r.level_start.size() - 1;
+            int64_t maxw = 1;
+            for (size_t l = 0; l + 1 < r.level_start.size(); ++l)
+                maxw = std::max(maxw, r.level_start[l + 1] - r.level_start[l]);
+            maxw = std::max(maxw, r.visited - r.level_start.back());
+            if (maxw < best_w || (maxw == best_w && ecc > prev_ecc)) {
+                best_w = maxw;
+                best = gl;
+            }
+            if (ecc <= prev_ecc) break;
+            prev_ecc = ecc;
+            const int64_t l0 = r.level_start.back(), ln = r.visited - l0;
+            GB_CUDA(cudaMemsetAsync(best_key, 0xFF, sizeof(unsigned long long), s));
+            k_level_first_min<<<grid_for(ln, kT), kT, 0, s>>>(order.get() + l0, ln, rdeg, best_key);
+            GB_LAUNCH_CHECK();
+            const unsigned long long bk = read_dev(best_key.get(), s);
+            gl = read_dev(order.get() + l0 + (int64_t)(bk & 0xFFFFFFFFull), s);
+            *nl += 1;
+        }
+    }
+    // ---- seeds: std::sort of 0..C-1 by degree ----
+    DevBuf<uint32_t> seeds(C, s), zero_rank(C, s);
+    DevBuf<uint64_t> skey(C, s);
+    k_iota_keys<<<grid_for(C, kT), kT, 0, s>>>(C, rdeg, seeds, skey, zero_rank);
+    GB_LAUNCH_CHECK();
+    {
+        const int64_t zero = 0, cc = C;
+        DevBuf<int64_t> so(1, s), ss(1, s);
+        GB_CUDA(cudaMemcpyAsync(so, &zero, sizeof(int64_t), cudaMemcpyHostToDevice, s));
+        GB_CUDA(cudaMemcpyAsync(ss, &cc, sizeof(int64_t), cudaMemcpyHostToDevice, s));
+        libstdcxx_sort_segments(seeds, skey, zero_rank, so, ss, C, s, nl);
+    }
+    // ---- neighbours by degree (std::sort per community) ----
+    if (A > 0) {
+        DevBuf<uint64_t> akey(A, s);
+        k_adj_keys<<<grid_for(A, kT), kT, 0, s>>>(adj, A, rdeg, akey);
+        GB_LAUNCH_CHECK();
+        libstdcxx_sort_segments(adj, akey, asrc, aoff, adeg, A, s, nl);
+    }
+    // ---- components and their first seeds ----
+    DevBuf<uint32_t> label(C, s), first(C, s);
+    k_cc_init<<<grid_for(C, kT), kT, 0, s>>>(label, C);
+    GB_LAUNCH_CHECK();
+    {
+        DevBuf<int> changed(1, s);
+        for (int64_t it = 0;; ++it) {
+            GB_REQUIRE(it <= C + 1, GBGPU_E_CUDA, "sg_super_rcm: components did not settle");
+            GB_CUDA(cudaMemsetAsync(changed, 0, sizeof(int), s));
+            if (A > 0) {
+                k_cc_hook<<<grid_for(A, kT), kT, 0, s>>>(asrc, adj, A, label, changed);
+                GB_LAUNCH_CHECK();
+            }
+            k_cc_jump<<<grid_for(C, kT), kT, 0, s>>>(label, C, changed);
+            GB_LAUNCH_CHECK();
+            *nl += 2;
+            if (read_dev(changed.get(), s) == 0) break;
+        }
+    }
+    uint8_t best_active = 0;
+    GB_CUDA(cudaMemcpyAsync(&best_active, active.get() + best, 1, cudaMemcpyDeviceToHost, s));
+    const uint32_t best_label = read_dev(label.get() + best, s);
+    GB_CUDA(cudaMemsetAsync(first, 0xFF, C * sizeof(uint32_t), s));
+    k_first_seed<<<grid_for(C, kT), kT, 0, s>>>(seeds, C, active, label, best_active ? best_label : 0xFFFFFFFFu, first);
+    GB_LAUNCH_CHECK();
+    DevBuf<int> ncomp_d(1, s);
+    GB_CUDA(cudaMemsetAsync(ncomp_d, 0, sizeof(int), s));
+    DevBuf<uint64_t> rk(C, s);
+    DevBuf<uint32_t> roots(C, s);
+    k_root_keys<<<grid_for(C, kT), kT, 0, s>>>(first, seeds, C, best, ncomp_d, rk, roots);
+    GB_LAUNCH_CHECK();
+    const int64_t ncomp = read_dev(ncomp_d.get(), s);
+    *nl += 3;
+    // ---- Cuthill-McKee: all components at once, grouped afterwards ----
+    DevBuf<uint32_t> comp(C, s);
+    fill_u32(perm, 0xFFFFFFFFu, C, s);
+    int64_t no = 0;
+    if (ncomp > 0) {
+        radix_sort_pairs_u64(rk, roots, ncomp, bits_for((uint64_t)C + 1), s);
+        const BfsResult r = fifo_bfs(roots, ncomp, C, aoff, adj, active, vis, claim, order, comp, s, nl);
+        no = r.visited;
+        DevBuf<uint32_t> ck(no, s);
+        k_comp_of_order<<<grid_for(no, kT), kT, 0, s>>>(order, no, comp, ck);
+        GB_LAUNCH_CHECK();
+        radix_sort_pairs_u32(ck, order, no, bits_for((uint64_t)ncomp), s);   // stable: visit order inside
+        k_rcm_perm<<<grid_for(no, kT), kT, 0, s>>>(order, no, perm);
+        GB_LAUNCH_CHECK();
+        *nl += 2;
+    }
+    DevBuf<int32_t> uflag(C, s);
+    DevBuf<int64_t> upos(C + 1, s);
+    k_unreached_flags<<<grid_for(C, kT), kT, 0, s>>>(perm, C, uflag);
+    GB_LAUNCH_CHECK();
+    exclusive_scan_i32_to_i64(uflag, upos, C, upos.get() + C, s);
+    k_unreached_assign<<<grid_for(C, kT), kT, 0, s>>>(uflag, upos, C, no, perm);
+    GB_LAUNCH_CHECK();
+    *nl += 5;
+}
+
+}  // namespace
+
+void super_order_device(const DeviceCSR& g, const uint32_t* memb, const uint32_t* csize, int64_t C, int order,
+                        uint32_t* stage1, cudaStream_t s, int64_t* launches) {
+    int64_t nl = 0;
+    if (order == kSuperRCM) super_rcm_perm(g, memb, csize, C, stage1, s, &nl);
+    else if (order == kHilbert) hilbert_perm(g, memb, csize, C, stage1, s, &nl);
+    else throw Error(GBGPU_E_UNSUPPORTED, "super-graph order not available on the GPU path");
+    if (launches) *launches += nl;
+}
+
+}  // namespace gb

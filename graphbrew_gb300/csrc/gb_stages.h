@@ -22,6 +22,7 @@ struct ComposeParams {
     int intra_order = 4;       // IntraCommunityOrder ordinal
     int gorder_window = 8;
     int gorder_fallback = 5000;
+    int super_order = 0;       // SuperGraphOrder ordinal (stage1Perm); 0 = none
 };
 void compose_device(const DeviceCSR& g, const uint32_t* membership, const ComposeParams& p,
                     int32_t* new_ids, gbgpu_stats* st, cudaStream_t s);
@@ -34,6 +35,18 @@ bool is_sorted_intra_order(int intra);
 int64_t sorted_communities(const DeviceCSR& g, const uint32_t* memb, int intra, const uint32_t* order_v,
                            const uint32_t* ranks, const int64_t* offs, const int64_t* ssize, int64_t nn,
                            uint32_t* local, cudaStream_t s, int64_t* launches);
+
+// libstdc++'s std::sort (introsort: ties end where it leaves them) of every
+// segment of (E, K) by K ascending, E moving with its key.  ranks: segment
+// of each of the nn positions; offs / ssize: start and size of a segment.
+void libstdcxx_sort_segments(uint32_t* E, uint64_t* K, const uint32_t* ranks, const int64_t* offs,
+                             const int64_t* ssize, int64_t nn, cudaStream_t s, int64_t* launches);
+
+// ---- compose_super.cu: sg_super_rcm, sg_hilbert ----
+// stage1Perm of a super-graph order (SuperGraphOrder ordinal: 2 super_rcm,
+// 4 hilbert) into stage1[C]; csize: non-isolated vertices per community.
+void super_order_device(const DeviceCSR& g, const uint32_t* memb, const uint32_t* csize, int64_t C, int order,
+                        uint32_t* stage1, cudaStream_t s, int64_t* launches);
 
 // ---- compose_random.cu: intra_random ----
 // Local ids of every non-isolated vertex for intra_random: list / count_dev

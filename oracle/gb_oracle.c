@@ -1755,6 +1755,36 @@ static int hilbert_perm(const uint32_t *deg, const uint32_t *cverts, const int64
     return ORC_OK;
 }
 
+int orc_super_stage1(const orc_graph *g, const uint32_t *membership, int super_order, uint32_t *out)
+{
+    if (!g || !membership || !out) return ORC_EINVAL;
+    const int64_t n = g->n;
+    uint32_t C = 0;
+    for (int64_t v = 0; v < n; ++v)
+        if (membership[v] + 1 > C) C = membership[v] + 1;
+    int rc = ORC_ENOMEM;
+    uint32_t *deg = (uint32_t *)malloc(((size_t)n + 1) * sizeof(uint32_t));
+    int64_t *csize = (int64_t *)calloc((size_t)C + 1, sizeof(int64_t));
+    int64_t *cstart = (int64_t *)calloc((size_t)C + 1, sizeof(int64_t));
+    int64_t *cur = (int64_t *)calloc((size_t)C + 1, sizeof(int64_t));
+    uint32_t *cverts = (uint32_t *)malloc(((size_t)n + 1) * sizeof(uint32_t));
+    if (deg && csize && cstart && cur && cverts) {
+        for (int64_t v = 0; v < n; ++v) {
+            deg[v] = (uint32_t)degree_of(g, v);
+            if (deg[v]) csize[membership[v]]++;
+        }
+        for (uint32_t c = 0; c < C; ++c) cstart[c + 1] = cstart[c] + csize[c];
+        memcpy(cur, cstart, (size_t)C * sizeof(int64_t));
+        for (int64_t v = 0; v < n; ++v)
+            if (deg[v]) cverts[cur[membership[v]]++] = (uint32_t)v;
+        if (super_order == ORC_SUPER_RCM) rc = super_rcm_perm(g, membership, deg, csize, C, out);
+        else if (super_order == ORC_SUPER_HILBERT) rc = hilbert_perm(deg, cverts, cstart, csize, C, out);
+        else rc = ORC_EUNSUPPORTED;
+    }
+    free(deg); free(csize); free(cstart); free(cur); free(cverts);
+    return rc;
+}
+
 /* ------------------------------------------------------------------------ */
 /* orderCompose (RG:6286-7087), super-graph order "none".                    */
 /* ------------------------------------------------------------------------ */

@@ -125,6 +125,9 @@ enum {
 /* Iteration order of a libstdc++ std::unordered_map keyed by an unsigned
  * integer after the k distinct keys are inserted in order (k <= 101473717). */
 int orc_umap_order(const uint32_t *keys, int64_t k, uint32_t *out);
+/* stage1Perm of a super-graph order (ORC_SUPER_RCM / ORC_SUPER_HILBERT) for
+ * the membership; out has max(membership) + 1 entries. */
+int orc_super_stage1(const orc_graph *g, const uint32_t *membership, int super_order, uint32_t *out);
 
 typedef struct {
     int64_t num_communities;   /* max(membership) + 1 */

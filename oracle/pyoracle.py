@@ -126,6 +126,7 @@ def load():
         lib.orc_libstdcxx_heap_sort.argtypes = [_u32p, C.c_int64, _u64p]
         lib.orc_random_draws.argtypes = [C.c_uint32, C.c_int64, _u32p]
         lib.orc_umap_order.argtypes = [_u32p, C.c_int64, _u32p]
+        lib.orc_super_stage1.argtypes = [C.POINTER(Graph), _u32p, C.c_int, _u32p]
         lib.orc_pagerank_gs.restype = C.c_double
         lib.orc_pagerank_gs.argtypes = [C.POINTER(Graph), C.c_int, C.c_double, _f32p, C.c_int,
                                         C.POINTER(C.c_int)]
@@ -202,6 +203,16 @@ def umap_order(keys):
     if load().orc_umap_order(k, len(k), out) != 0:
         raise RuntimeError("orc_umap_order failed")
     return out[:len(k)]
+
+
+def super_stage1(row_ptr, col, membership, super_order):
+    """stage1Perm of a super-graph order ("super-rcm" / "hilbert")."""
+    g, keep = _as_graph(row_ptr, col)
+    memb = np.ascontiguousarray(membership, dtype=np.uint32)
+    out = np.zeros(int(memb.max()) + 1 if len(memb) else 1, dtype=np.uint32)
+    if load().orc_super_stage1(C.byref(g), memb, SUPER_ORDERS[super_order], out) != 0:
+        raise RuntimeError("orc_super_stage1 failed")
+    return out
 
 
 def std_umap_order(keys):

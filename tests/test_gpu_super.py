@@ -1,0 +1,72 @@
+"""Super-graph orders on the GPU (sg_super_rcm, sg_hilbert;
+reorder_graphbrew.h:4990-5090, 5726-5871, 6395-6462): the per-community
+std::unordered_map simulations, the George-Liu / Cuthill-McKee BFS and the
+Hilbert keys give the reference's one-thread permutation bit for bit, given
+the same membership; on the RMAT-18/19 pins and through the whole mapping
+against the oracle."""
+import json
+import os
+import sys
+
+import numpy as np
+import pytest
+import torch
+
+import pyoracle as po
+import graphbrew_gb300 as gb
+from graphbrew_gb300 import graphgen as gg
+from conftest import GOLDEN
+
+sys.path.insert(0, GOLDEN)
+from make_golden_super import BIG, COMM, SUPER, big_graph, digest, recipe  # noqa: E402
+from make_golden_sorted import generator_graphs  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+CASES = np.load(os.path.join(GOLDEN, "super_cases.npz"))
+NAMES = sorted({k.split("/")[0] for k in CASES.files})
+with open(os.path.join(GOLDEN, "super_pins.json")) as f:
+    PINS = json.load(f)
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    assert torch.cuda.is_available(), "GPU tests need CUDA"
+    c = gb.Context(0)
+    yield c
+    c.close()
+
+
+@pytest.mark.parametrize("sup", sorted(SUPER))
+def test_super_against_reference(ctx, sup, golden_arrays):
+    gen = generator_graphs()
+    for name in NAMES:
+        if name in gen:
+            rp, col = gen[name]
+            memb = CASES[f"{name}/membership"]
+        else:
+            rp, col = golden_arrays[f"{name}/row_ptr"], golden_arrays[f"{name}/col"]
+            memb = golden_arrays[f"{name}/membership_serial"]
+        for comm in COMM:
+            ids, _ = ctx.order_compose(rp, col, memb, recipe(sup, comm))
+            np.testing.assert_array_equal(ids, CASES[f"{name}/{sup}/{comm}"], err_msg=f"{name} {comm}")
+
+
+@pytest.mark.parametrize("name", sorted(BIG))
+def test_super_pinned(ctx, name):
+    rp, col, memb = big_graph(name)
+    for sup in SUPER:
+        ids, _ = ctx.order_compose(rp, col, memb, recipe(sup))
+        assert digest(ids) == PINS[name][sup], sup
+
+
+@pytest.mark.parametrize("sup", sorted(SUPER))
+def test_super_mapping_against_oracle(ctx, sup):
+    rp_t, col_t = gg.rmat(17, 16, seed=79, device="cuda")
+    rp, col = rp_t.cpu().numpy(), col_t.cpu().numpy()
+    ar = po.auto_resolution(rp, col)
+    rec = f"leiden:compose:{SUPER[sup]}:comm_size_desc:intra_gorder:gw8:cd_serial:sgmb4096:gordf5000:norefine:2:2"
+    ids, _ = ctx.generate_mapping(rp_t, col_t, rec, ar)
+    memb, _ = po.leiden(rp, col, ar)
+    ids_orc, _ = po.compose(rp, col, memb, "size-desc", "gorder", super_order=sup)
+    np.testing.assert_array_equal(ids.cpu().numpy(), ids_orc)
