@@ -334,7 +334,7 @@ def main():
             assert rc == 0, lib.gbgpu_last_error(ctx.handle)
             return s
 
-        for _ in range(2):
+        for _ in range(max(3, args.warmup)):
             host_step()
         t0 = time.perf_counter()
         host_stats, marks = [], [t0]
@@ -349,6 +349,7 @@ def main():
                 "d2h_bytes_per_step": 4 * n + 8 * (n + 1) + 4 * nnz,
                 "ms_per_step": e2e_s * 1e3, "host_buffers": "pinned" if pinned else "pageable",
                 "step_wall_ms": [round((b - a) * 1e3, 2) for a, b in zip(marks, marks[1:])],
+                "step_device_ms": [round(float(x.total_ms), 2) for x in host_stats],
                 "h2d_ms": float(np.median([x.h2d_ms for x in host_stats])),
                 "d2h_ms": float(np.median([x.d2h_ms for x in host_stats])),
                 "call_device_ms": float(np.median([x.total_ms for x in host_stats])),

@@ -170,6 +170,7 @@ gb::ComposeParams compose_params(const gb::Config& c) {
     p.community_order = static_cast<int>(c.communityOrder);
     p.intra_order = static_cast<int>(c.intraCommunityOrder);
     p.super_order = static_cast<int>(c.superGraphOrder);
+    p.super_gamma = static_cast<float>(c.superGraphResolution);
     p.gorder_window = c.gorderWindow;
     p.gorder_fallback = c.gorderFallback;
     return p;

@@ -1289,7 +1289,7 @@ void compose_device(const DeviceCSR& g, const uint32_t* memb, const ComposeParam
         DevBuf<uint32_t> stage1;
         if (p.super_order != 0) {
             stage1.alloc(C, s);
-            super_order_device(g, memb, csize, C, p.super_order, stage1, s, &launches);
+            super_order_device(g, memb, csize, C, p.super_order, p.super_gamma, stage1, s, &launches);
         }
         DevBuf<uint64_t> keys(C, s);
         k_comm_keys<<<grid_for(C, kT), kT, 0, s>>>(co, csize, need_deg ? cdeg.get() : nullptr, C, max_size, max_deg,

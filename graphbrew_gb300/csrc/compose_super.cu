@@ -43,7 +43,7 @@ namespace gb {
 namespace {
 
 constexpr int kT = 256;
-constexpr int kSuperRCM = 2, kHilbert = 4;
+constexpr int kSuperRabbit = 1, kSuperRCM = 2, kHilbert = 4;
 
 // Bucket counts a default-constructed libstdc++ std::unordered_map goes
 // through as it grows (maximum load factor 1): 13 at the first insertion,
@@ -185,17 +185,29 @@ __global__ void k_run_flags(const uint64_t* __restrict__ key, int64_t m, uint8_t
 __global__ void k_unique_emit(const uint64_t* __restrict__ key, const uint32_t* __restrict__ val, int64_t m,
                               const uint8_t* __restrict__ flag, const int64_t* __restrict__ pos, int cb, int eb,
                               uint64_t* __restrict__ key2, uint32_t* __restrict__ d2, uint32_t* __restrict__ msize,
-                              uint8_t* __restrict__ self_pair, uint8_t* __restrict__ rflag) {
+                              uint8_t* __restrict__ self_pair, uint8_t* __restrict__ rflag, uint64_t* __restrict__ ukey,
+                              int64_t* __restrict__ head) {
     const uint64_t dmask = (1ull << cb) - 1ull;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
         if (!flag[i]) continue;
         const int64_t j = pos[i];
         const uint32_t c = (uint32_t)(key[i] >> cb), d = (uint32_t)(key[i] & dmask);
+        ukey[j] = key[i];
+        head[j] = i;
         key2[j] = ((uint64_t)c << eb) | val[i];
         d2[j] = d;
         atomicAdd(&msize[c], 1u);
         if (c == d) self_pair[c] = 1;
         rflag[j] = c < d ? 1 : 0;
+    }
+}
+
+// Weight of a unique pair: the per-thread map's float sum of 1.0f per
+// entry, which stops growing at 2^24 (2^24 + 1 rounds back to 2^24).
+__global__ void k_unique_weights(const int64_t* __restrict__ head, int64_t m, int64_t m0, float* __restrict__ uw) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t k = (j + 1 < m ? head[j + 1] : m0) - head[j];
+        uw[j] = k >= (1ll << 24) ? 16777216.0f : (float)k;
     }
 }
 
@@ -342,15 +354,16 @@ __global__ void k_adj_own(const uint64_t* __restrict__ key2, int64_t m, int eb, 
     }
 }
 
-__global__ void k_adj_rev(const uint64_t* __restrict__ rkey, const uint32_t* __restrict__ rval, int64_t mr, int cb,
-                          const int64_t* __restrict__ rstart, const int64_t* __restrict__ aoff,
-                          const uint32_t* __restrict__ msize, const uint8_t* __restrict__ self_pair,
-                          uint32_t* __restrict__ adj, uint32_t* __restrict__ asrc) {
+__global__ void k_adj_rev(const uint64_t* __restrict__ rkey, int64_t mr, int cb, const int64_t* __restrict__ rstart,
+                          const int64_t* __restrict__ aoff, const uint32_t* __restrict__ msize,
+                          const uint8_t* __restrict__ self_pair, uint32_t* __restrict__ adj,
+                          uint32_t* __restrict__ asrc) {
+    const uint64_t cmask = (1ull << cb) - 1ull;
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < mr; r += (int64_t)gridDim.x * blockDim.x) {
         const uint32_t d = (uint32_t)(rkey[r] >> cb);
         const int64_t own = (int64_t)msize[d] - (self_pair[d] ? 1 : 0);
         const int64_t at = aoff[d] + own + (r - rstart[d]);
-        adj[at] = rval[r];
+        adj[at] = (uint32_t)(rkey[r] & cmask);
         asrc[at] = d;
     }
 }
@@ -517,6 +530,342 @@ __global__ void k_unreached_assign(const int32_t* __restrict__ flag, const int64
 }
 
 // ---------------------------------------------------------------------------
+// sg_super_rabbit (RG:5495-5715, its OpenMP loops run by one thread)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float pair_weight(const uint64_t* __restrict__ ukey, const float* __restrict__ uw, int64_t m,
+                                             uint64_t key) {
+    int64_t lo = 0, hi = m - 1;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (ukey[mid] < key) lo = mid + 1;
+        else hi = mid;
+    }
+    return uw[lo];
+}
+
+__global__ void k_rev_counts(const uint64_t* __restrict__ rkey, int64_t mr, int cb, uint32_t* __restrict__ rcnt) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < mr; r += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd(&rcnt[(uint32_t)(rkey[r] >> cb)], 1u);
+}
+
+__global__ void k_vtx_counts(const uint32_t* __restrict__ msize, const uint32_t* __restrict__ rcnt, int64_t C,
+                             int64_t* __restrict__ vcnt) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C; c += (int64_t)gridDim.x * blockDim.x)
+        vcnt[c] = (int64_t)msize[c] + rcnt[c];
+}
+
+// vtx[x]: (c', w) for every c' < x whose map holds x, by c', then x's own
+// map (self included) in iteration order -- the order in which the
+// reference's loop over c pushes them (RG:5515-5520).
+__global__ void k_vtx_fill_rev(const uint64_t* __restrict__ rkey, int64_t mr, int cb,
+                               const int64_t* __restrict__ rstart, const int64_t* __restrict__ voff,
+                               const uint64_t* __restrict__ ukey, const float* __restrict__ uw, int64_t m,
+                               uint32_t* __restrict__ ad, float* __restrict__ aw) {
+    const uint64_t cmask = (1ull << cb) - 1ull;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < mr; r += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t x = (uint32_t)(rkey[r] >> cb), c = (uint32_t)(rkey[r] & cmask);
+        const int64_t at = voff[x] + (r - rstart[x]);
+        ad[at] = c;
+        aw[at] = pair_weight(ukey, uw, m, ((uint64_t)c << cb) | x);
+    }
+}
+
+__global__ void k_vtx_fill_own(const uint64_t* __restrict__ key2, int64_t m, int eb, int cb,
+                               const int64_t* __restrict__ moff, const uint32_t* __restrict__ ord2,
+                               const uint32_t* __restrict__ rcnt, const int64_t* __restrict__ voff,
+                               const uint64_t* __restrict__ ukey, const float* __restrict__ uw,
+                               uint32_t* __restrict__ ad, float* __restrict__ aw) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t c = (uint32_t)(key2[i] >> eb), d = ord2[i];
+        const int64_t at = voff[c] + rcnt[c] + (i - moff[c]);
+        ad[at] = d;
+        aw[at] = pair_weight(ukey, uw, m, ((uint64_t)c << cb) | d);
+    }
+}
+
+// Degrees: each community's weights summed in list order (float), which is
+// the order the reference adds them; initial state of every community.
+__global__ void k_vtx_degrees(const int64_t* __restrict__ voff, const int64_t* __restrict__ vcnt, const float* aw,
+                              int64_t C, float* __restrict__ degc, int32_t* __restrict__ vlen,
+                              uint32_t* __restrict__ dest, uint32_t* __restrict__ child, uint32_t* __restrict__ sibling,
+                              uint32_t* __restrict__ united, float* __restrict__ str, int32_t* __restrict__ spos,
+                              float* __restrict__ sums, uint8_t* __restrict__ nz) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C; c += (int64_t)gridDim.x * blockDim.x) {
+        float d = 0.0f;
+        for (int64_t e = voff[c]; e < voff[c] + vcnt[c]; ++e) d = __fadd_rn(d, aw[e]);
+        degc[c] = d;
+        vlen[c] = (int32_t)vcnt[c];
+        dest[c] = (uint32_t)c;
+        child[c] = kNone;
+        sibling[c] = kNone;
+        united[c] = kNone;
+        str[c] = d;
+        spos[c] = -1;
+        sums[c] = 0.0f;
+        nz[c] = d != 0.0f ? 1 : 0;
+    }
+}
+
+__global__ void k_nz_emit(const uint8_t* __restrict__ nz, const int64_t* __restrict__ pos, const float* __restrict__ degc,
+                          int64_t C, uint32_t* __restrict__ keys, uint32_t* __restrict__ ids) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C; c += (int64_t)gridDim.x * blockDim.x) {
+        if (!nz[c]) continue;
+        keys[pos[c]] = __float_as_uint(degc[c]);   // non-negative: bits order like the float
+        ids[pos[c]] = (uint32_t)c;
+    }
+}
+
+// M: the degrees summed in community order, one thread (zeros add nothing).
+__global__ void k_total_weight(const float* __restrict__ degc, const uint32_t* __restrict__ ids_by_c, int64_t nnz_c,
+                               float* __restrict__ out) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    float M = 0.0f;
+    for (int64_t i = 0; i < nnz_c; ++i) M = __fadd_rn(M, degc[ids_by_c[i]]);
+    out[0] = M;
+}
+
+struct RabbitState {
+    const uint32_t* order;   // non-zero-degree communities by (degree, id)
+    int64_t norder;
+    uint32_t *dest, *child, *sibling, *united;
+    float* str;
+    int64_t* voff;
+    int32_t* vlen;
+    uint32_t* ad;            // arena: list entries
+    float* aw;
+    int64_t arena_cap;
+    int64_t* arena_len;      // [0]
+    int32_t* spos;           // scanner: position of a key, -1 absent
+    float* sums;
+    uint32_t* keys;
+    uint32_t* stack;
+    int64_t stack_cap;
+    uint32_t* upd;           // deferred united_child updates (c, value) pairs
+    float gamma, inv2M;
+    int64_t* progress;       // [0] next order index
+    int* status;             // [0] 0 done, 1 arena full, 2 error
+};
+
+// Adds a list's entries to the scanner in order: lanes find the roots of 32
+// entries at once; for each root the first lane holding it adds the group's
+// weights in lane order (float, sequential like the reference's scanner) and,
+// if the root is new, appends it in first-lane order.
+__device__ __forceinline__ void rabbit_scan_list(const RabbitState& s, uint32_t u, int64_t off, int32_t len,
+                                                 int64_t& nk) {
+    const int lane = threadIdx.x & 31;
+    for (int32_t b = 0; b < len; b += 32) {
+        const int32_t e = b + lane;
+        const bool valid = e < len;
+        uint32_t r = 0;
+        float w = 0.0f;
+        if (valid) {
+            r = s.ad[off + e];
+            w = s.aw[off + e];
+            while (s.dest[r] != r) r = s.dest[r];
+        }
+        const bool act = valid && r != u;
+        const unsigned am = __ballot_sync(0xFFFFFFFFu, act);
+        unsigned peers = 0;
+        if (act) peers = __match_any_sync(am, r);
+        const bool leader = act && (__ffs(peers) - 1) == lane;
+        float acc = leader ? s.sums[r] : 0.0f;
+        for (int t = 0; t < 32; ++t) {
+            const float wt = __shfl_sync(0xFFFFFFFFu, w, t);
+            if (leader && ((peers >> t) & 1u)) acc = __fadd_rn(acc, wt);
+        }
+        const bool isnew = leader && s.spos[r] < 0;
+        const unsigned nm = __ballot_sync(0xFFFFFFFFu, isnew);
+        if (leader) {
+            s.sums[r] = acc;
+            if (isnew) {
+                const int64_t at = nk + __popc(nm & ((1u << lane) - 1u));
+                s.keys[at] = r;
+                s.spos[r] = (int32_t)at;
+            }
+        }
+        nk += __popc(nm);
+        __syncwarp();
+    }
+}
+
+__device__ __forceinline__ bool rabbit_better(float a, uint32_t ia, float b, uint32_t ib) {
+    return a > b || (a == b && ia < ib);
+}
+
+// The merge chain, one warp: communities in (degree, id) order unite their
+// edges and merge into the best neighbour root.  Stops with status 1 when a
+// new list does not fit the arena (nothing of that community changed yet).
+__global__ void __launch_bounds__(32) k_rabbit_chain(RabbitState s) {
+    const int lane = threadIdx.x;
+    const float kInvalidStr = -1.0f;
+    int64_t alen = s.arena_len[0];
+    for (int64_t i = s.progress[0]; i < s.norder; ++i) {
+        const uint32_t u = s.order[i];
+        int64_t nk = 0;
+        rabbit_scan_list(s, u, s.voff[u], s.vlen[u], nk);
+        const uint32_t first_child = s.child[u], uc = s.united[u];
+        int64_t sp = 0, nupd = 0;
+        if (first_child != uc && first_child != kNone) {
+            if (lane == 0) s.stack[0] = first_child;
+            sp = 1;
+        }
+        bool bad = false;
+        while (sp > 0) {
+            __syncwarp();
+            const uint32_t c = s.stack[--sp];
+            if (c == uc || c == kNone) continue;
+            rabbit_scan_list(s, u, s.voff[c], s.vlen[c], nk);
+            const uint32_t sib = s.sibling[c], cf = s.child[c], ucc = s.united[c];
+            if (sp + 2 > s.stack_cap || nupd + 1 > s.stack_cap / 2) {
+                bad = true;
+                break;
+            }
+            if (sib != uc && sib != kNone) {
+                if (lane == 0) s.stack[sp] = sib;
+                ++sp;
+            }
+            if (cf != ucc && cf != kNone) {
+                if (lane == 0) s.stack[sp] = cf;
+                ++sp;
+            }
+            if (lane == 0) {
+                s.upd[2 * nupd] = c;
+                s.upd[2 * nupd + 1] = cf;
+            }
+            ++nupd;
+        }
+        __syncwarp();
+        if (bad || alen + nk > s.arena_cap) {
+            for (int64_t j = lane; j < nk; j += 32) {
+                s.spos[s.keys[j]] = -1;
+                s.sums[s.keys[j]] = 0.0f;
+            }
+            if (lane == 0) {
+                s.progress[0] = i;
+                s.arena_len[0] = alen;
+                s.status[0] = bad ? 2 : 1;
+            }
+            return;
+        }
+        // The new list, the deferred united_child updates.
+        for (int64_t j = lane; j < nk; j += 32) {
+            const uint32_t d = s.keys[j];
+            s.ad[alen + j] = d;
+            s.aw[alen + j] = s.sums[d];
+        }
+        for (int64_t q = lane; q < nupd; q += 32) s.united[s.upd[2 * q]] = s.upd[2 * q + 1];
+        __syncwarp();
+        if (lane == 0) {
+            s.voff[u] = alen;
+            s.vlen[u] = (int32_t)nk;
+            s.united[u] = first_child;
+        }
+        alen += nk;
+        // Best neighbour: largest w - gamma str_u str_d / 2M above 0, ties
+        // to the smaller id (the reference's scan keeps the same one).
+        const float str_u = s.str[u];
+        const float gu = __fmul_rn(s.gamma, str_u);
+        float bdq = 0.0f;
+        uint32_t bd = kNone;
+        for (int64_t j0 = 0; j0 < nk; j0 += 32) {
+            const int64_t j = j0 + lane;
+            float dq = 0.0f;
+            uint32_t d = kNone;
+            if (j < nk) {
+                const uint32_t cand = s.keys[j];
+                const float sd = s.str[cand];
+                if (sd != kInvalidStr) {
+                    const float q = __fsub_rn(s.sums[cand], __fmul_rn(__fmul_rn(gu, sd), s.inv2M));
+                    if (q > 0.0f) {
+                        dq = q;
+                        d = cand;
+                    }
+                }
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                const float odq = __shfl_xor_sync(0xFFFFFFFFu, dq, o);
+                const uint32_t od = __shfl_xor_sync(0xFFFFFFFFu, d, o);
+                if (od != kNone && (d == kNone || rabbit_better(odq, od, dq, d))) {
+                    dq = odq;
+                    d = od;
+                }
+            }
+            if (d != kNone && (bd == kNone || rabbit_better(dq, d, bdq, bd))) {
+                bdq = dq;
+                bd = d;
+            }
+        }
+        __syncwarp();
+        for (int64_t j = lane; j < nk; j += 32) {
+            s.spos[s.keys[j]] = -1;
+            s.sums[s.keys[j]] = 0.0f;
+        }
+        if (lane == 0 && bd != kNone) {
+            s.sibling[u] = s.child[bd];
+            s.str[bd] = __fadd_rn(s.str[bd], str_u);
+            s.child[bd] = u;
+            s.dest[u] = bd;
+        }
+        __syncwarp();
+    }
+    if (lane == 0) {
+        s.progress[0] = s.norder;
+        s.arena_len[0] = alen;
+        s.status[0] = 0;
+    }
+}
+
+// Dendrogram roots: non-empty ones first, then empty ones (no weight and no
+// vertices), each group by id.
+__global__ void k_root_flags(const uint32_t* __restrict__ dest, const float* __restrict__ degc,
+                             const uint32_t* __restrict__ csize, int64_t C, int32_t* __restrict__ fa,
+                             int32_t* __restrict__ fb) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C; c += (int64_t)gridDim.x * blockDim.x) {
+        const bool root = dest[c] == (uint32_t)c;
+        const bool empty = degc[c] == 0.0f && csize[c] == 0;
+        fa[c] = root && !empty ? 1 : 0;
+        fb[c] = root && empty ? 1 : 0;
+    }
+}
+
+__global__ void k_root_emit(const int32_t* __restrict__ fa, const int32_t* __restrict__ fb,
+                            const int64_t* __restrict__ pa, const int64_t* __restrict__ pb, int64_t na, int64_t C,
+                            uint32_t* __restrict__ roots) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C; c += (int64_t)gridDim.x * blockDim.x) {
+        if (fa[c]) roots[pa[c]] = (uint32_t)c;
+        if (fb[c]) roots[na + pb[c]] = (uint32_t)c;
+    }
+}
+
+// The dendrogram walk (RG:5696-5708), one thread: a root's child chain on a
+// stack, the deepest first; a popped community with a sibling pushes the
+// sibling's chain.
+__global__ void k_rabbit_walk(const uint32_t* __restrict__ roots, int64_t nr, const uint32_t* __restrict__ child,
+                              const uint32_t* __restrict__ sibling, uint32_t* __restrict__ stack, int64_t stack_cap,
+                              uint32_t* __restrict__ perm, int64_t* __restrict__ next_out, int* __restrict__ status) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    int64_t next = 0;
+    for (int64_t b = 0; b < nr; ++b) {
+        int64_t sp = 0;
+        for (uint32_t v = roots[b]; v != kNone; v = child[v]) {
+            if (sp >= stack_cap) { status[0] = 2; return; }
+            stack[sp++] = v;
+        }
+        while (sp > 0) {
+            const uint32_t c = stack[--sp];
+            if (perm[c] != kNone) continue;
+            perm[c] = (uint32_t)next++;
+            if (sibling[c] != kNone)
+                for (uint32_t v = sibling[c]; v != kNone; v = child[v]) {
+                    if (sp >= stack_cap) { status[0] = 2; return; }
+                    stack[sp++] = v;
+                }
+        }
+    }
+    next_out[0] = next;
+}
+
+// ---------------------------------------------------------------------------
 // Hilbert
 // ---------------------------------------------------------------------------
 __global__ void k_comm_degree_sums(const int64_t* __restrict__ rp, const uint32_t* __restrict__ memb, int64_t n,
@@ -653,20 +1002,38 @@ void hilbert_perm(const DeviceCSR& g, const uint32_t* memb, const uint32_t* csiz
     *nl += 4 + 3 * 2;
 }
 
-void super_rcm_perm(const DeviceCSR& g, const uint32_t* memb, const uint32_t* csize, int64_t C, uint32_t* perm,
-                    cudaStream_t s, int64_t* nl) {
+// The super-graph's maps (RG:5033-5072, one thread): sizes, offsets, the
+// merged maps' keys in iteration order (ord2, with key2 >> eb its map), the
+// reverse pairs (d, c), c < d, by d then c (rkey = d << cb | c), and every
+// unique pair (c << cb | d, ascending) with its weight.
+struct SuperMaps {
+    int cb = 1, eb = 1;
+    int64_t m = 0, mr = 0;
+    DevBuf<uint32_t> msize, d2, ord2;
+    DevBuf<uint8_t> self_pair;
+    DevBuf<int64_t> moff;
+    DevBuf<uint64_t> key2, rkey, ukey;
+    DevBuf<float> uw;
+};
+
+void build_super_maps(const DeviceCSR& g, const uint32_t* memb, int64_t C, SuperMaps& sm, cudaStream_t s,
+                      int64_t* nl) {
     const int64_t n = g.n, nnz = g.nnz;
-    GB_REQUIRE(nnz < (int64_t)0xFFFFFFFFll, GBGPU_E_UNSUPPORTED, "sg_super_rcm: more than 2^32 - 1 entries");
+    GB_REQUIRE(nnz < (int64_t)0xFFFFFFFFll, GBGPU_E_UNSUPPORTED, "super-graph order: more than 2^32 - 1 entries");
     const int cb = std::max(1, bits_for((uint64_t)(C - 1)));
     const int eb = std::max(1, bits_for((uint64_t)(nnz > 0 ? nnz - 1 : 0)));
-    DevBuf<uint32_t> msize(C, s);
-    DevBuf<uint8_t> self_pair(C, s);
+    sm.cb = cb;
+    sm.eb = eb;
+    sm.msize.alloc(C, s);
+    sm.self_pair.alloc(C, s);
+    DevBuf<uint32_t>& msize = sm.msize;
+    DevBuf<uint8_t>& self_pair = sm.self_pair;
     GB_CUDA(cudaMemsetAsync(msize, 0, C * sizeof(uint32_t), s));
     GB_CUDA(cudaMemsetAsync(self_pair, 0, C, s));
     // ---- first occurrences ----
     int64_t m = 0;
-    DevBuf<uint64_t> key2;
-    DevBuf<uint32_t> d2;
+    DevBuf<uint64_t>& key2 = sm.key2;
+    DevBuf<uint32_t>& d2 = sm.d2;
     DevBuf<uint8_t> rflag;
     if (nnz > 0) {
         DevBuf<int32_t> crow(edge_chunks(nnz), s);
@@ -695,30 +1062,37 @@ void super_rcm_perm(const DeviceCSR& g, const uint32_t* memb, const uint32_t* cs
             key2.alloc(m, s);
             d2.alloc(m, s);
             rflag.alloc(m, s);
+            sm.ukey.alloc(m, s);
+            sm.uw.alloc(m, s);
+            DevBuf<int64_t> head(m, s);
             k_unique_emit<<<grid_for(m0, kT), kT, 0, s>>>(key, val, m0, uflag, upos, cb, eb, key2, d2, msize,
-                                                          self_pair, rflag);
+                                                          self_pair, rflag, sm.ukey, head);
             GB_LAUNCH_CHECK();
-            *nl += 6 + 3 * ((2 * cb + 7) / 8);
+            k_unique_weights<<<grid_for(m, kT), kT, 0, s>>>(head, m, m0, sm.uw);
+            GB_LAUNCH_CHECK();
+            *nl += 7 + 3 * ((2 * cb + 7) / 8);
         }
     }
+    sm.m = m;
     // Reverse pairs (d, c), c < d, by d then c.
     int64_t mr = 0;
-    DevBuf<uint64_t> rkey;
-    DevBuf<uint32_t> rval;
+    DevBuf<uint64_t>& rkey = sm.rkey;
     if (m > 0) {
         DevBuf<int64_t> rpos(m + 1, s);
         exclusive_scan_u8_to_i64(rflag, rpos, m, rpos.get() + m, s);
         mr = read_dev(rpos.get() + m, s);
         rkey.alloc(mr > 0 ? mr : 1, s);
-        rval.alloc(mr > 0 ? mr : 1, s);
+        DevBuf<uint32_t> rval(mr > 0 ? mr : 1, s);
         k_reverse_emit<<<grid_for(m, kT), kT, 0, s>>>(key2, d2, m, eb, cb, rflag, rpos, rkey, rval);
         GB_LAUNCH_CHECK();
-        if (mr > 0) radix_sort_pairs_u64(rkey, rval, mr, 2 * cb, s);
+        if (mr > 0) radix_sort_keys_u64(rkey, mr, 2 * cb, s);
         // Per-map insertion order: by community, then first entry.
         radix_sort_pairs_u64(key2, d2, m, cb + eb, s);
         *nl += 4 + 3 * ((2 * cb + 7) / 8) + 3 * ((cb + eb + 7) / 8);
     }
-    DevBuf<int64_t> moff(C + 1, s);
+    sm.mr = mr;
+    sm.moff.alloc(C + 1, s);
+    DevBuf<int64_t>& moff = sm.moff;
     {
         DevBuf<int32_t> ms32(C, s);
         GB_CUDA(cudaMemcpyAsync(ms32, msize, C * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
@@ -726,7 +1100,9 @@ void super_rcm_perm(const DeviceCSR& g, const uint32_t* memb, const uint32_t* cs
         *nl += 3;
     }
     // ---- map simulations ----
-    DevBuf<uint32_t> ord1(m > 0 ? m : 1, s), ord2(m > 0 ? m : 1, s);
+    DevBuf<uint32_t> ord1(m > 0 ? m : 1, s);
+    sm.ord2.alloc(m > 0 ? m : 1, s);
+    DevBuf<uint32_t>& ord2 = sm.ord2;
     if (m > 0) {
         GB_REQUIRE(umap_buckets_host(m) > 0, GBGPU_E_UNSUPPORTED, "sg_super_rcm: a community map is too large");
         k_umap_small<<<grid_for(C, kT), kT, 0, s>>>(moff, msize, C, d2, ord1, ord2);
@@ -762,6 +1138,20 @@ void super_rcm_perm(const DeviceCSR& g, const uint32_t* memb, const uint32_t* cs
             *nl += 4;
         }
     }
+}
+
+void super_rcm_perm(const DeviceCSR& g, const uint32_t* memb, const uint32_t* csize, int64_t C, uint32_t* perm,
+                    cudaStream_t s, int64_t* nl) {
+    SuperMaps sm;
+    build_super_maps(g, memb, C, sm, s, nl);
+    const int cb = sm.cb, eb = sm.eb;
+    const int64_t m = sm.m, mr = sm.mr;
+    const DevBuf<uint32_t>& msize = sm.msize;
+    const DevBuf<uint8_t>& self_pair = sm.self_pair;
+    const DevBuf<int64_t>& moff = sm.moff;
+    const DevBuf<uint64_t>& key2 = sm.key2;
+    const DevBuf<uint64_t>& rkey = sm.rkey;
+    const DevBuf<uint32_t>& ord2 = sm.ord2;
     // ---- superAdj ----
     DevBuf<uint32_t> spos(C, s), rcnt(C, s);
     DevBuf<int64_t> adeg(C, s), aoff(C + 1, s), rstart(C + 1, s);
@@ -786,7 +1176,7 @@ void super_rcm_perm(const DeviceCSR& g, const uint32_t* memb, const uint32_t* cs
         GB_LAUNCH_CHECK();
     }
     if (mr > 0) {
-        k_adj_rev<<<grid_for(mr, kT), kT, 0, s>>>(rkey, rval, mr, cb, rstart, aoff, msize, self_pair, adj, asrc);
+        k_adj_rev<<<grid_for(mr, kT), kT, 0, s>>>(rkey, mr, cb, rstart, aoff, msize, self_pair, adj, asrc);
         GB_LAUNCH_CHECK();
     }
     DevBuf<uint64_t> rdeg(C, s);
@@ -907,12 +1297,147 @@ void super_rcm_perm(const DeviceCSR& g, const uint32_t* memb, const uint32_t* cs
     *nl += 5;
 }
 
+void super_rabbit_perm(const DeviceCSR& g, const uint32_t* memb, const uint32_t* csize, int64_t C, float gamma,
+                       uint32_t* perm, cudaStream_t s, int64_t* nl) {
+    SuperMaps sm;
+    build_super_maps(g, memb, C, sm, s, nl);
+    const int cb = sm.cb, eb = sm.eb;
+    const int64_t m = sm.m, mr = sm.mr;
+    // ---- vtx lists and degrees ----
+    DevBuf<uint32_t> rcnt(C, s);
+    DevBuf<int64_t> vcnt(C, s), voff(C + 1, s), rstart(C + 1, s);
+    GB_CUDA(cudaMemsetAsync(rcnt, 0, C * sizeof(uint32_t), s));
+    if (mr > 0) {
+        k_rev_counts<<<grid_for(mr, kT), kT, 0, s>>>(sm.rkey, mr, cb, rcnt);
+        GB_LAUNCH_CHECK();
+    }
+    k_vtx_counts<<<grid_for(C, kT), kT, 0, s>>>(sm.msize, rcnt, C, vcnt);
+    GB_LAUNCH_CHECK();
+    exclusive_scan_i64_total(vcnt, voff, C, voff.get() + C, s);
+    {
+        DevBuf<int32_t> r32(C, s);
+        GB_CUDA(cudaMemcpyAsync(r32, rcnt, C * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+        exclusive_scan_i32_to_i64(r32, rstart, C, rstart.get() + C, s);
+    }
+    const int64_t A0 = read_dev(voff.get() + C, s);
+    int64_t cap = 4 * A0 + 1024;
+    DevBuf<uint32_t> ad(cap, s);
+    DevBuf<float> aw(cap, s);
+    if (mr > 0) {
+        k_vtx_fill_rev<<<grid_for(mr, kT), kT, 0, s>>>(sm.rkey, mr, cb, rstart, voff, sm.ukey, sm.uw, m, ad, aw);
+        GB_LAUNCH_CHECK();
+    }
+    if (m > 0) {
+        k_vtx_fill_own<<<grid_for(m, kT), kT, 0, s>>>(sm.key2, m, eb, cb, sm.moff, sm.ord2, rcnt, voff, sm.ukey, sm.uw,
+                                                      ad, aw);
+        GB_LAUNCH_CHECK();
+    }
+    DevBuf<float> degc(C, s), str(C, s), sums(C, s), total(1, s);
+    DevBuf<int32_t> vlen(C, s), spos(C, s);
+    DevBuf<uint32_t> dest(C, s), child(C, s), sibling(C, s), united(C, s), keys(C, s);
+    DevBuf<uint8_t> nz(C, s);
+    k_vtx_degrees<<<grid_for(C, kT), kT, 0, s>>>(voff, vcnt, aw, C, degc, vlen, dest, child, sibling, united, str, spos,
+                                                 sums, nz);
+    GB_LAUNCH_CHECK();
+    // Non-zero-degree communities: by id for M, then by (degree, id).
+    DevBuf<int64_t> npos(C + 1, s);
+    exclusive_scan_u8_to_i64(nz, npos, C, npos.get() + C, s);
+    const int64_t nnzc = read_dev(npos.get() + C, s);
+    DevBuf<uint32_t> okey(nnzc > 0 ? nnzc : 1, s), order(nnzc > 0 ? nnzc : 1, s);
+    k_nz_emit<<<grid_for(C, kT), kT, 0, s>>>(nz, npos, degc, C, okey, order);
+    GB_LAUNCH_CHECK();
+    k_total_weight<<<1, 32, 0, s>>>(degc, order, nnzc, total);
+    GB_LAUNCH_CHECK();
+    const float Msum = read_dev(total.get(), s);
+    const float M = Msum / 2.0f;
+    const float inv2M = M > 0.0f ? 1.0f / (2.0f * M) : 0.0f;
+    if (nnzc > 0) radix_sort_pairs_u32(okey, order, nnzc, 32, s);   // stable: ties by id
+    *nl += 12;
+    // ---- the merge chain ----
+    const int64_t stack_cap = 2 * C + 2;
+    DevBuf<uint32_t> stack(stack_cap, s), upd(stack_cap, s);
+    DevBuf<int64_t> ctl(2, s);   // progress, arena length
+    DevBuf<int> status(1, s);
+    const int64_t zero_ctl[2] = {0, A0};
+    GB_CUDA(cudaMemcpyAsync(ctl, zero_ctl, sizeof(zero_ctl), cudaMemcpyHostToDevice, s));
+    for (;;) {
+        GB_CUDA(cudaMemsetAsync(status, 0xFF, sizeof(int), s));
+        RabbitState rs{};
+        rs.order = order;
+        rs.norder = nnzc;
+        rs.dest = dest;
+        rs.child = child;
+        rs.sibling = sibling;
+        rs.united = united;
+        rs.str = str;
+        rs.voff = voff;
+        rs.vlen = vlen;
+        rs.ad = ad;
+        rs.aw = aw;
+        rs.arena_cap = cap;
+        rs.arena_len = ctl.get() + 1;
+        rs.spos = spos;
+        rs.sums = sums;
+        rs.keys = keys;
+        rs.stack = stack;
+        rs.stack_cap = stack_cap;
+        rs.upd = upd;
+        rs.gamma = gamma;
+        rs.inv2M = inv2M;
+        rs.progress = ctl.get();
+        rs.status = status;
+        k_rabbit_chain<<<1, 32, 0, s>>>(rs);
+        GB_LAUNCH_CHECK();
+        ++*nl;
+        const int st = read_dev(status.get(), s);
+        if (st == 0) break;
+        GB_REQUIRE(st == 1, GBGPU_E_CUDA, "sg_super_rabbit: merge chain exceeded its stack");
+        // Grow the arena and continue from the community that did not fit.
+        const int64_t used = read_dev(ctl.get() + 1, s);
+        const int64_t ncap = 2 * cap + C;
+        DevBuf<uint32_t> nad(ncap, s);
+        DevBuf<float> naw(ncap, s);
+        GB_CUDA(cudaMemcpyAsync(nad, ad, used * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+        GB_CUDA(cudaMemcpyAsync(naw, aw, used * sizeof(float), cudaMemcpyDeviceToDevice, s));
+        ad = std::move(nad);
+        aw = std::move(naw);
+        cap = ncap;
+    }
+    // ---- dendrogram walk ----
+    DevBuf<int32_t> fa(C, s), fb(C, s);
+    DevBuf<int64_t> pa(C + 1, s), pb(C + 1, s);
+    k_root_flags<<<grid_for(C, kT), kT, 0, s>>>(dest, degc, csize, C, fa, fb);
+    GB_LAUNCH_CHECK();
+    exclusive_scan_i32_to_i64(fa, pa, C, pa.get() + C, s);
+    exclusive_scan_i32_to_i64(fb, pb, C, pb.get() + C, s);
+    const int64_t na = read_dev(pa.get() + C, s), nb = read_dev(pb.get() + C, s);
+    DevBuf<uint32_t> roots(na + nb > 0 ? na + nb : 1, s);
+    k_root_emit<<<grid_for(C, kT), kT, 0, s>>>(fa, fb, pa, pb, na, C, roots);
+    GB_LAUNCH_CHECK();
+    fill_u32(perm, 0xFFFFFFFFu, C, s);
+    DevBuf<int64_t> nextv(1, s);
+    GB_CUDA(cudaMemsetAsync(status, 0, sizeof(int), s));
+    k_rabbit_walk<<<1, 1, 0, s>>>(roots, na + nb, child, sibling, stack, stack_cap, perm, nextv, status);
+    GB_LAUNCH_CHECK();
+    GB_REQUIRE(read_dev(status.get(), s) == 0, GBGPU_E_CUDA, "sg_super_rabbit: dendrogram walk exceeded its stack");
+    const int64_t no = read_dev(nextv.get(), s);
+    DevBuf<int32_t> uflag(C, s);
+    DevBuf<int64_t> upos(C + 1, s);
+    k_unreached_flags<<<grid_for(C, kT), kT, 0, s>>>(perm, C, uflag);
+    GB_LAUNCH_CHECK();
+    exclusive_scan_i32_to_i64(uflag, upos, C, upos.get() + C, s);
+    k_unreached_assign<<<grid_for(C, kT), kT, 0, s>>>(uflag, upos, C, no, perm);
+    GB_LAUNCH_CHECK();
+    *nl += 12;
+}
+
 }  // namespace
 
 void super_order_device(const DeviceCSR& g, const uint32_t* memb, const uint32_t* csize, int64_t C, int order,
-                        uint32_t* stage1, cudaStream_t s, int64_t* launches) {
+                        float gamma, uint32_t* stage1, cudaStream_t s, int64_t* launches) {
     int64_t nl = 0;
     if (order == kSuperRCM) super_rcm_perm(g, memb, csize, C, stage1, s, &nl);
+    else if (order == kSuperRabbit) super_rabbit_perm(g, memb, csize, C, gamma, stage1, s, &nl);
     else if (order == kHilbert) hilbert_perm(g, memb, csize, C, stage1, s, &nl);
     else throw Error(GBGPU_E_UNSUPPORTED, "super-graph order not available on the GPU path");
     if (launches) *launches += nl;

@@ -715,9 +715,8 @@ std::string gpu_unsupported_reason(const Config& c) {
     if (c.aggregation != Aggregation::GveCSR) return "only gvecsr aggregation is on the GPU path";
     if (c.ordering != Ordering::Compose) return std::string("ordering '") + ordering_name(c.ordering) +
                                                 "' is not on the GPU path (use compose)";
-    if (c.superGraphOrder != SuperGraphOrder::None && c.superGraphOrder != SuperGraphOrder::SuperRCM &&
-        c.superGraphOrder != SuperGraphOrder::Hilbert)
-        return "super-graph orders sg_none, sg_super_rcm and sg_hilbert are on the GPU path";
+    if (c.superGraphOrder == SuperGraphOrder::TileRabbit)
+        return "super-graph order sg_tile_rabbit is not on the GPU path";
     switch (c.communityOrder) {
         case CommunityOrder::SizeDesc: case CommunityOrder::SizeAsc: case CommunityOrder::DegreeDesc:
         case CommunityOrder::DegreeAsc: case CommunityOrder::Identity: break;

@@ -23,6 +23,7 @@ struct ComposeParams {
     int gorder_window = 8;
     int gorder_fallback = 5000;
     int super_order = 0;       // SuperGraphOrder ordinal (stage1Perm); 0 = none
+    float super_gamma = 0.1f;  // superGraphResolution (sg_super_rabbit)
 };
 void compose_device(const DeviceCSR& g, const uint32_t* membership, const ComposeParams& p,
                     int32_t* new_ids, gbgpu_stats* st, cudaStream_t s);
@@ -42,11 +43,12 @@ int64_t sorted_communities(const DeviceCSR& g, const uint32_t* memb, int intra, 
 void libstdcxx_sort_segments(uint32_t* E, uint64_t* K, const uint32_t* ranks, const int64_t* offs,
                              const int64_t* ssize, int64_t nn, cudaStream_t s, int64_t* launches);
 
-// ---- compose_super.cu: sg_super_rcm, sg_hilbert ----
-// stage1Perm of a super-graph order (SuperGraphOrder ordinal: 2 super_rcm,
-// 4 hilbert) into stage1[C]; csize: non-isolated vertices per community.
+// ---- compose_super.cu: sg_super_rabbit, sg_super_rcm, sg_hilbert ----
+// stage1Perm of a super-graph order (SuperGraphOrder ordinal: 1 super_rabbit,
+// 2 super_rcm, 4 hilbert) into stage1[C]; csize: non-isolated vertices per
+// community; gamma: superGraphResolution (Rabbit).
 void super_order_device(const DeviceCSR& g, const uint32_t* memb, const uint32_t* csize, int64_t C, int order,
-                        uint32_t* stage1, cudaStream_t s, int64_t* launches);
+                        float gamma, uint32_t* stage1, cudaStream_t s, int64_t* launches);
 
 // ---- compose_random.cu: intra_random ----
 // Local ids of every non-isolated vertex for intra_random: list / count_dev

@@ -1696,6 +1696,298 @@ out:
     return rc;
 }
 
+/* edges[c] of the super-graph with weights, one thread (RG:5033-5072): moff
+ * (C + 1 offsets), the merged map's keys in iteration order (ord2) and
+ * their weights.  A weight is the per-thread map's float sum of 1.0f per
+ * entry, which stops growing at 2^24 (2^24 + 1 rounds back to 2^24). */
+static int super_maps(const orc_graph *g, const uint32_t *memb, const uint32_t *deg, uint32_t C, int64_t **moff_out,
+                      uint32_t **ord2_out, float **w_out)
+{
+    const int64_t n = g->n;
+    int rc = ORC_ENOMEM;
+    int64_t npairs = 0, cap = 0;
+    for (int64_t u = 0; u < n; ++u) cap += deg[u];
+    int64_t tabsz = 64;
+    while (tabsz < 2 * cap) tabsz <<= 1;
+    uint64_t *tab = (uint64_t *)malloc((size_t)tabsz * sizeof(uint64_t));
+    int64_t *tix = (int64_t *)malloc((size_t)tabsz * sizeof(int64_t));
+    uint64_t *pairs = (uint64_t *)malloc((size_t)(cap > 0 ? cap : 1) * sizeof(uint64_t));
+    int64_t *cnt = (int64_t *)calloc((size_t)(cap > 0 ? cap : 1), sizeof(int64_t));
+    int64_t *moff = (int64_t *)calloc((size_t)C + 1, sizeof(int64_t));
+    int64_t *fill = (int64_t *)calloc((size_t)C + 1, sizeof(int64_t));
+    uint32_t *mkeys = NULL, *ord1 = NULL, *ord2 = NULL;
+    float *w2 = NULL;
+    if (!tab || !tix || !pairs || !cnt || !moff || !fill) goto out;
+    memset(tab, 0xFF, (size_t)tabsz * sizeof(uint64_t));
+    for (int64_t u = 0; u < n; ++u) {
+        if (!deg[u]) continue;
+        const uint32_t cu = memb[u];
+        for (int64_t e = g->row_ptr[u]; e < g->row_ptr[u + 1]; ++e) {
+            const uint32_t cv = memb[g->col[e]];
+            if (cu > cv) continue;
+            const uint64_t key = ((uint64_t)cu << 32) | cv;
+            int64_t i = (int64_t)((key * 0x9E3779B97F4A7C15ull) >> 20) & (tabsz - 1);
+            while (tab[i] != UINT64_MAX && tab[i] != key) i = (i + 1) & (tabsz - 1);
+            if (tab[i] == UINT64_MAX) {
+                tab[i] = key;
+                tix[i] = npairs;
+                pairs[npairs++] = key;
+            }
+            cnt[tix[i]]++;
+        }
+    }
+    const int64_t np1 = npairs > 0 ? npairs : 1;
+    mkeys = (uint32_t *)malloc((size_t)np1 * sizeof(uint32_t));
+    ord1 = (uint32_t *)malloc((size_t)np1 * sizeof(uint32_t));
+    ord2 = (uint32_t *)malloc((size_t)np1 * sizeof(uint32_t));
+    w2 = (float *)malloc((size_t)np1 * sizeof(float));
+    if (!mkeys || !ord1 || !ord2 || !w2) goto out;
+    for (int64_t i = 0; i < npairs; ++i) moff[(pairs[i] >> 32) + 1]++;
+    for (uint32_t c = 0; c < C; ++c) moff[c + 1] += moff[c];
+    for (int64_t i = 0; i < npairs; ++i) {
+        const uint32_t c = (uint32_t)(pairs[i] >> 32);
+        mkeys[moff[c] + fill[c]++] = (uint32_t)pairs[i];
+    }
+    for (uint32_t c = 0; c < C; ++c) {
+        const int64_t len = moff[c + 1] - moff[c];
+        if (orc_umap_order(mkeys + moff[c], len, ord1 + moff[c]) != ORC_OK ||
+            orc_umap_order(ord1 + moff[c], len, ord2 + moff[c]) != ORC_OK) {
+            rc = ORC_EINVAL;
+            goto out;
+        }
+        for (int64_t i = moff[c]; i < moff[c + 1]; ++i) {
+            const uint64_t key = ((uint64_t)c << 32) | ord2[i];
+            int64_t j = (int64_t)((key * 0x9E3779B97F4A7C15ull) >> 20) & (tabsz - 1);
+            while (tab[j] != key) j = (j + 1) & (tabsz - 1);
+            const int64_t k = cnt[tix[j]];
+            w2[i] = k >= 16777216 ? 16777216.0f : (float)k;
+        }
+    }
+    *moff_out = moff;
+    *ord2_out = ord2;
+    *w_out = w2;
+    moff = NULL;
+    ord2 = NULL;
+    w2 = NULL;
+    rc = ORC_OK;
+out:
+    free(tab); free(tix); free(pairs); free(cnt); free(moff); free(fill); free(mkeys); free(ord1); free(ord2);
+    free(w2);
+    return rc;
+}
+
+typedef struct {
+    uint32_t d;
+    float w;
+} orc_sedge;
+
+static int u64_cmp(const void *a, const void *b)
+{
+    const uint64_t x = *(const uint64_t *)a, y = *(const uint64_t *)b;
+    return x < y ? -1 : (x > y);
+}
+
+/* stage1Perm of sg_super_rabbit, one thread (RG:5495-5715 runRabbitOnSuperCSR
+ * with its OpenMP loops run by one thread): RabbitOrder on the super-graph.
+ * vtx[c] lists the (d, w) of every c' < c whose map holds c, by c', then c's
+ * own map in iteration order; degrees are those weights summed in the same
+ * order.  Communities in ascending (degree, id) unite their own and their
+ * not yet aggregated children's edges (a scanner: keys in first-insertion
+ * order, float sums in traversal order), then merge into the neighbour
+ * root of the largest w - gamma str_u str_d / 2M (ties to the smaller id)
+ * when that is > 0.  The dendrogram is walked from the roots (non-empty
+ * ones first, each group by id), children chains before siblings. */
+static int super_rabbit_perm(const orc_graph *g, const uint32_t *memb, const uint32_t *deg, const int64_t *csize,
+                             uint32_t C, float gamma, uint32_t *perm)
+{
+    const uint32_t INV = UINT32_MAX;
+    const float INVALID_STR = -1.0f;
+    int rc = ORC_ENOMEM;
+    int64_t *moff = NULL, *voff = NULL, *vlen = NULL, *vcur = NULL, *spos = NULL;
+    uint32_t *ord2 = NULL, *order = NULL, *dest = NULL, *child = NULL, *sibling = NULL, *united = NULL,
+             *keys = NULL, *stack = NULL;
+    float *w2 = NULL, *degc = NULL, *str = NULL, *sums = NULL;
+    orc_sedge *arena = NULL;
+    int64_t arena_len = 0, arena_cap = 0;
+    if (super_maps(g, memb, deg, C, &moff, &ord2, &w2) != ORC_OK) goto out;
+    const int64_t m = moff[C];
+    voff = (int64_t *)calloc((size_t)C + 1, sizeof(int64_t));
+    vlen = (int64_t *)calloc((size_t)C + 1, sizeof(int64_t));
+    vcur = (int64_t *)calloc((size_t)C + 1, sizeof(int64_t));
+    degc = (float *)calloc((size_t)C + 1, sizeof(float));
+    if (!voff || !vlen || !vcur || !degc) goto out;
+    for (uint32_t c = 0; c < C; ++c)
+        for (int64_t i = moff[c]; i < moff[c + 1]; ++i) {
+            vlen[c]++;
+            if (ord2[i] != c) vlen[ord2[i]]++;
+        }
+    for (uint32_t c = 0; c < C; ++c) voff[c + 1] = voff[c] + vlen[c];
+    arena_cap = 2 * voff[C] + 64;
+    arena = (orc_sedge *)malloc((size_t)arena_cap * sizeof(orc_sedge));
+    if (!arena) goto out;
+    arena_len = voff[C];
+    memcpy(vcur, voff, (size_t)C * sizeof(int64_t));
+    for (uint32_t c = 0; c < C; ++c)
+        for (int64_t i = moff[c]; i < moff[c + 1]; ++i) {
+            const uint32_t d = ord2[i];
+            const float w = w2[i];
+            arena[vcur[c]].d = d;
+            arena[vcur[c]++].w = w;
+            degc[c] += w;
+            if (d != c) {
+                arena[vcur[d]].d = c;
+                arena[vcur[d]++].w = w;
+                degc[d] += w;
+            }
+        }
+    (void)m;
+    float M = 0.0f;
+    for (uint32_t c = 0; c < C; ++c) M += degc[c];
+    M /= 2.0f;
+    const float inv2M = M > 0.0f ? 1.0f / (2.0f * M) : 0.0f;
+
+    order = (uint32_t *)malloc(((size_t)C + 1) * sizeof(uint32_t));
+    dest = (uint32_t *)malloc(((size_t)C + 1) * sizeof(uint32_t));
+    child = (uint32_t *)malloc(((size_t)C + 1) * sizeof(uint32_t));
+    sibling = (uint32_t *)malloc(((size_t)C + 1) * sizeof(uint32_t));
+    united = (uint32_t *)malloc(((size_t)C + 1) * sizeof(uint32_t));
+    keys = (uint32_t *)malloc(((size_t)C + 1) * sizeof(uint32_t));
+    const int64_t stack_cap = 2 * (int64_t)C + 2;
+    stack = (uint32_t *)malloc((size_t)stack_cap * sizeof(uint32_t));
+    str = (float *)malloc(((size_t)C + 1) * sizeof(float));
+    sums = (float *)calloc((size_t)C + 1, sizeof(float));
+    spos = (int64_t *)malloc(((size_t)C + 1) * sizeof(int64_t));
+    if (!order || !dest || !child || !sibling || !united || !keys || !stack || !str || !sums || !spos) goto out;
+    for (uint32_t c = 0; c < C; ++c) {
+        order[c] = c;
+        dest[c] = c;
+        child[c] = INV;
+        sibling[c] = INV;
+        united[c] = INV;
+        str[c] = degc[c];
+        spos[c] = -1;
+    }
+    {
+        /* ascending (degree, id): the degree's bits order like the float */
+        uint64_t *k = (uint64_t *)malloc(((size_t)C + 1) * sizeof(uint64_t));
+        if (!k) goto out;
+        for (uint32_t c = 0; c < C; ++c) {
+            uint32_t b;
+            memcpy(&b, &degc[c], sizeof(b));
+            k[c] = ((uint64_t)b << 32) | c;
+        }
+        qsort(k, C, sizeof(uint64_t), u64_cmp);
+        for (uint32_t c = 0; c < C; ++c) order[c] = (uint32_t)k[c];
+        free(k);
+    }
+    for (uint32_t i = 0; i < C; ++i) {
+        const uint32_t u = order[i];
+        if (degc[u] == 0.0f) continue;
+        /* unite(u) */
+        int64_t nk = 0;
+#define ORC_SCAN_ADD(dd, ww)                                                                              \
+    do {                                                                                                  \
+        uint32_t r_ = (dd);                                                                               \
+        while (dest[r_] != r_) r_ = dest[r_];                                                             \
+        if (r_ != u) {                                                                                    \
+            if (spos[r_] < 0) { spos[r_] = nk; keys[nk++] = r_; }                                         \
+            sums[r_] += (ww);                                                                             \
+        }                                                                                                 \
+    } while (0)
+        for (int64_t e = voff[u]; e < voff[u] + vlen[u]; ++e) ORC_SCAN_ADD(arena[e].d, arena[e].w);
+        const uint32_t first_child = child[u], uc = united[u];
+        int64_t sp = 0;
+        if (first_child != uc && first_child != INV) stack[sp++] = first_child;
+        while (sp > 0) {
+            const uint32_t c = stack[--sp];
+            if (c == uc || c == INV) continue;
+            for (int64_t e = voff[c]; e < voff[c] + vlen[c]; ++e) ORC_SCAN_ADD(arena[e].d, arena[e].w);
+            if (sp + 2 > stack_cap) { rc = ORC_EINVAL; goto out; }
+            if (sibling[c] != uc && sibling[c] != INV) stack[sp++] = sibling[c];
+            const uint32_t cf = child[c];
+            if (cf != united[c] && cf != INV) stack[sp++] = cf;
+            united[c] = cf;
+        }
+#undef ORC_SCAN_ADD
+        if (arena_len + nk > arena_cap) {
+            arena_cap = 2 * (arena_len + nk) + 64;
+            orc_sedge *na = (orc_sedge *)realloc(arena, (size_t)arena_cap * sizeof(orc_sedge));
+            if (!na) goto out;
+            arena = na;
+        }
+        voff[u] = arena_len;
+        vlen[u] = nk;
+        for (int64_t j = 0; j < nk; ++j) {
+            arena[arena_len + j].d = keys[j];
+            arena[arena_len + j].w = sums[keys[j]];
+        }
+        arena_len += nk;
+        united[u] = first_child;
+        const float str_u = str[u];
+        str[u] = INVALID_STR;
+        uint32_t best = INV;
+        float best_dq = 0.0f;
+        const float gu = gamma * str_u;
+        for (int64_t j = 0; j < nk; ++j) {
+            const uint32_t d = keys[j];
+            const float str_d = str[d];
+            if (str_d == INVALID_STR) continue;
+            const float dq = sums[d] - gu * str_d * inv2M;
+            if (dq > best_dq || (dq == best_dq && (best == INV || d < best))) {
+                best_dq = dq;
+                best = d;
+            }
+        }
+        for (int64_t j = 0; j < nk; ++j) {
+            spos[keys[j]] = -1;
+            sums[keys[j]] = 0.0f;
+        }
+        if (best == INV || best_dq <= 0.0f) {
+            str[u] = str_u;
+            continue;
+        }
+        sibling[u] = child[best];
+        str[best] = str[best] + str_u;
+        child[best] = u;
+        dest[u] = best;
+    }
+    /* Dendrogram roots: non-empty ones by id, then empty ones by id. */
+    {
+        int64_t nr = 0, next = 0;
+        for (int pass = 0; pass < 2; ++pass)
+            for (uint32_t c = 0; c < C; ++c) {
+                if (dest[c] != c) continue;
+                const int empty = degc[c] == 0.0f && csize[c] == 0;
+                if (empty != pass) continue;
+                keys[nr++] = c;
+            }
+        for (uint32_t c = 0; c < C; ++c) perm[c] = INV;
+        for (int64_t b = 0; b < nr; ++b) {
+            int64_t sp = 0;
+            for (uint32_t v = keys[b]; v != INV; v = child[v]) {
+                if (sp >= stack_cap) { rc = ORC_EINVAL; goto out; }
+                stack[sp++] = v;
+            }
+            while (sp > 0) {
+                const uint32_t c = stack[--sp];
+                if (perm[c] != INV) continue;
+                perm[c] = (uint32_t)next++;
+                if (sibling[c] != INV)
+                    for (uint32_t v = sibling[c]; v != INV; v = child[v]) {
+                        if (sp >= stack_cap) { rc = ORC_EINVAL; goto out; }
+                        stack[sp++] = v;
+                    }
+            }
+        }
+        for (uint32_t c = 0; c < C; ++c) if (perm[c] == INV) perm[c] = (uint32_t)next++;
+    }
+    rc = ORC_OK;
+out:
+    free(moff); free(voff); free(vlen); free(vcur); free(spos); free(ord2); free(order); free(dest); free(child);
+    free(sibling); free(united); free(keys); free(stack); free(w2); free(degc); free(str); free(sums); free(arena);
+    return rc;
+}
+
 /* The reference's Hilbert index of (x, y) on an n x n grid (xy2d with its
  * own rotation, s - 1 - x, in 32-bit unsigned arithmetic). */
 static uint64_t hilbert_xy2d(uint32_t n, uint32_t x, uint32_t y)
@@ -1755,7 +2047,7 @@ static int hilbert_perm(const uint32_t *deg, const uint32_t *cverts, const int64
     return ORC_OK;
 }
 
-int orc_super_stage1(const orc_graph *g, const uint32_t *membership, int super_order, uint32_t *out)
+int orc_super_stage1(const orc_graph *g, const uint32_t *membership, int super_order, float gamma, uint32_t *out)
 {
     if (!g || !membership || !out) return ORC_EINVAL;
     const int64_t n = g->n;
@@ -1778,6 +2070,7 @@ int orc_super_stage1(const orc_graph *g, const uint32_t *membership, int super_o
         for (int64_t v = 0; v < n; ++v)
             if (deg[v]) cverts[cur[membership[v]]++] = (uint32_t)v;
         if (super_order == ORC_SUPER_RCM) rc = super_rcm_perm(g, membership, deg, csize, C, out);
+        else if (super_order == ORC_SUPER_RABBIT) rc = super_rabbit_perm(g, membership, deg, csize, C, gamma, out);
         else if (super_order == ORC_SUPER_HILBERT) rc = hilbert_perm(deg, cverts, cstart, csize, C, out);
         else rc = ORC_EUNSUPPORTED;
     }
@@ -1816,7 +2109,7 @@ int orc_compose(const orc_graph *g, const uint32_t *membership,
         cfg->intra_order != ORC_INTRA_RANDOM && !is_sorted_intra(cfg->intra_order))
         return ORC_EUNSUPPORTED;
     if (cfg->super_order != ORC_SUPER_NONE && cfg->super_order != ORC_SUPER_RCM &&
-        cfg->super_order != ORC_SUPER_HILBERT)
+        cfg->super_order != ORC_SUPER_HILBERT && cfg->super_order != ORC_SUPER_RABBIT)
         return ORC_EUNSUPPORTED;
 
     int rc = ORC_ENOMEM;
@@ -1863,7 +2156,9 @@ int orc_compose(const orc_graph *g, const uint32_t *membership,
         if (!stage1) goto done;
         rc = cfg->super_order == ORC_SUPER_RCM
                  ? super_rcm_perm(g, membership, deg, csize, num_comm, stage1)
-                 : hilbert_perm(deg, cverts, cstart, csize, num_comm, stage1);
+                 : cfg->super_order == ORC_SUPER_RABBIT
+                       ? super_rabbit_perm(g, membership, deg, csize, num_comm, cfg->super_gamma, stage1)
+                       : hilbert_perm(deg, cverts, cstart, csize, num_comm, stage1);
         if (rc != ORC_OK) goto done;
         rc = ORC_ENOMEM;
     }

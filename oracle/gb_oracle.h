@@ -114,10 +114,12 @@ typedef struct {
     int gorder_fallback;  /* gordf<k>; 0 = no fallback */
     int threads;          /* 1 = serial; otherwise the OpenMP default */
     int super_order;      /* ORC_SUPER_*: stage1Perm, the community order's tie-break */
+    float super_gamma;    /* superGraphResolution (sg_super_rabbit) */
 } orc_compose_cfg;
 
 enum {
     ORC_SUPER_NONE = 0,
+    ORC_SUPER_RABBIT = 1,   /* sg_super_rabbit, the reference's one-thread result */
     ORC_SUPER_RCM = 2,      /* sg_super_rcm, the reference's one-thread result */
     ORC_SUPER_HILBERT = 4   /* sg_hilbert */
 };
@@ -125,9 +127,9 @@ enum {
 /* Iteration order of a libstdc++ std::unordered_map keyed by an unsigned
  * integer after the k distinct keys are inserted in order (k <= 101473717). */
 int orc_umap_order(const uint32_t *keys, int64_t k, uint32_t *out);
-/* stage1Perm of a super-graph order (ORC_SUPER_RCM / ORC_SUPER_HILBERT) for
- * the membership; out has max(membership) + 1 entries. */
-int orc_super_stage1(const orc_graph *g, const uint32_t *membership, int super_order, uint32_t *out);
+/* stage1Perm of a super-graph order (ORC_SUPER_*) for the membership; out has
+ * max(membership) + 1 entries; gamma: superGraphResolution (Rabbit only). */
+int orc_super_stage1(const orc_graph *g, const uint32_t *membership, int super_order, float gamma, uint32_t *out);
 
 typedef struct {
     int64_t num_communities;   /* max(membership) + 1 */

@@ -62,10 +62,10 @@ class LeidenStats(C.Structure):
 class ComposeCfg(C.Structure):
     _fields_ = [("community_order", C.c_int), ("intra_order", C.c_int),
                 ("gorder_window", C.c_int), ("gorder_fallback", C.c_int),
-                ("threads", C.c_int), ("super_order", C.c_int)]
+                ("threads", C.c_int), ("super_order", C.c_int), ("super_gamma", C.c_float)]
 
 
-SUPER_ORDERS = {"none": 0, "super-rcm": 2, "hilbert": 4}
+SUPER_ORDERS = {"none": 0, "super-rabbit": 1, "super-rcm": 2, "hilbert": 4}
 
 
 class ComposeStats(C.Structure):
@@ -126,7 +126,7 @@ def load():
         lib.orc_libstdcxx_heap_sort.argtypes = [_u32p, C.c_int64, _u64p]
         lib.orc_random_draws.argtypes = [C.c_uint32, C.c_int64, _u32p]
         lib.orc_umap_order.argtypes = [_u32p, C.c_int64, _u32p]
-        lib.orc_super_stage1.argtypes = [C.POINTER(Graph), _u32p, C.c_int, _u32p]
+        lib.orc_super_stage1.argtypes = [C.POINTER(Graph), _u32p, C.c_int, C.c_float, _u32p]
         lib.orc_pagerank_gs.restype = C.c_double
         lib.orc_pagerank_gs.argtypes = [C.POINTER(Graph), C.c_int, C.c_double, _f32p, C.c_int,
                                         C.POINTER(C.c_int)]
@@ -205,12 +205,13 @@ def umap_order(keys):
     return out[:len(k)]
 
 
-def super_stage1(row_ptr, col, membership, super_order):
-    """stage1Perm of a super-graph order ("super-rcm" / "hilbert")."""
+def super_stage1(row_ptr, col, membership, super_order, gamma=0.1):
+    """stage1Perm of a super-graph order ("super-rcm" / "super-rabbit" /
+    "hilbert")."""
     g, keep = _as_graph(row_ptr, col)
     memb = np.ascontiguousarray(membership, dtype=np.uint32)
     out = np.zeros(int(memb.max()) + 1 if len(memb) else 1, dtype=np.uint32)
-    if load().orc_super_stage1(C.byref(g), memb, SUPER_ORDERS[super_order], out) != 0:
+    if load().orc_super_stage1(C.byref(g), memb, SUPER_ORDERS[super_order], gamma, out) != 0:
         raise RuntimeError("orc_super_stage1 failed")
     return out
 
@@ -298,10 +299,10 @@ def leiden(row_ptr, col, resolution, max_iterations=2, max_passes=2, super_move_
 
 
 def compose(row_ptr, col, membership, community_order="size-desc", intra_order="gorder",
-            gorder_window=8, gorder_fallback=5000, threads=0, super_order="none"):
+            gorder_window=8, gorder_fallback=5000, threads=0, super_order="none", super_gamma=0.1):
     g, keep = _as_graph(row_ptr, col)
     cfg = ComposeCfg(COMM_ORDERS[community_order], INTRA_ORDERS[intra_order], gorder_window,
-                     gorder_fallback, threads, SUPER_ORDERS[super_order])
+                     gorder_fallback, threads, SUPER_ORDERS[super_order], super_gamma)
     memb = np.ascontiguousarray(membership, dtype=np.uint32)
     out = np.zeros(g.n, dtype=np.int32)
     st = ComposeStats()

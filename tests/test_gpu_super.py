@@ -1,9 +1,9 @@
-"""Super-graph orders on the GPU (sg_super_rcm, sg_hilbert;
-reorder_graphbrew.h:4990-5090, 5726-5871, 6395-6462): the per-community
-std::unordered_map simulations, the George-Liu / Cuthill-McKee BFS and the
-Hilbert keys give the reference's one-thread permutation bit for bit, given
-the same membership; on the RMAT-18/19 pins and through the whole mapping
-against the oracle."""
+"""Super-graph orders on the GPU (sg_super_rcm, sg_super_rabbit, sg_hilbert;
+reorder_graphbrew.h:4990-5090, 5495-5871, 6395-6462): the per-community
+std::unordered_map simulations, the George-Liu / Cuthill-McKee BFS, the
+Rabbit merge chain and the Hilbert keys give the reference's one-thread
+permutation bit for bit, given the same membership; on the RMAT-18/19 and
+grid pins and through the whole mapping against the oracle."""
 import json
 import os
 import sys
@@ -56,8 +56,27 @@ def test_super_against_reference(ctx, sup, golden_arrays):
 def test_super_pinned(ctx, name):
     rp, col, memb = big_graph(name)
     for sup in SUPER:
+        for comm in COMM:
+            ids, _ = ctx.order_compose(rp, col, memb, recipe(sup, comm))
+            assert digest(ids) == PINS[name][sup][comm], (sup, comm)
+
+
+def test_super_rabbit_saturated_weights_against_oracle(ctx):
+    """RMAT-20 with its own mapping's membership: the giant community holds
+    more than 2^24 entries, so its pair weight stops at 2^24 and the float
+    sums of the Rabbit merge chain round in the reference's order."""
+    rp_t, col_t = gg.rmat(20, 16, seed=81, device="cuda")
+    rp, col = rp_t.cpu().numpy(), col_t.cpu().numpy()
+    ar = po.auto_resolution(rp, col)
+    memb, _ = ctx.run_graphbrew(rp_t, col_t, recipe("super-rabbit"), ar)
+    memb = memb.cpu().numpy().view(np.uint32)
+    src = np.repeat(np.arange(len(rp) - 1), np.diff(rp))
+    same = memb[src] == memb[col]
+    assert np.bincount(memb[src][same]).max() > (1 << 24)
+    for sup in ("super-rabbit", "super-rcm"):
         ids, _ = ctx.order_compose(rp, col, memb, recipe(sup))
-        assert digest(ids) == PINS[name][sup], sup
+        ids_orc, _ = po.compose(rp, col, memb, "size-desc", "bfs", super_order=sup)
+        np.testing.assert_array_equal(ids, ids_orc, err_msg=sup)
 
 
 @pytest.mark.parametrize("sup", sorted(SUPER))

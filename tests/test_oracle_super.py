@@ -78,5 +78,6 @@ def test_compose_super_against_reference(golden_arrays, sup):
 def test_compose_super_pinned(name):
     rp, col, memb = big_graph(name)
     for sup in SUPER:
-        ids, _ = po.compose(rp, col, memb, "size-desc", "bfs", super_order=sup)
-        assert digest(ids) == PINS[name][sup], sup
+        for comm in COMM:
+            ids, _ = po.compose(rp, col, memb, comm, "bfs", super_order=sup)
+            assert digest(ids) == PINS[name][sup][comm], (sup, comm)
