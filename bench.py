@@ -350,6 +350,9 @@ def main():
                 "ms_per_step": e2e_s * 1e3, "host_buffers": "pinned" if pinned else "pageable",
                 "step_wall_ms": [round((b - a) * 1e3, 2) for a, b in zip(marks, marks[1:])],
                 "step_device_ms": [round(float(x.total_ms), 2) for x in host_stats],
+                "step_h2d_ms": [round(float(x.h2d_ms), 2) for x in host_stats],
+                "step_relabel_ms": [round(float(x.relabel_ms), 2) for x in host_stats],
+                "step_local_move_ms": [round(float(x.local_move_ms), 2) for x in host_stats],
                 "h2d_ms": float(np.median([x.h2d_ms for x in host_stats])),
                 "d2h_ms": float(np.median([x.d2h_ms for x in host_stats])),
                 "call_device_ms": float(np.median([x.total_ms for x in host_stats])),

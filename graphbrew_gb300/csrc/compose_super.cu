@@ -659,9 +659,14 @@ __device__ __forceinline__ void rabbit_scan_list(const RabbitState& s, uint32_t 
         uint32_t r = 0;
         float w = 0.0f;
         if (valid) {
-            r = s.ad[off + e];
+            const uint32_t d = s.ad[off + e];
             w = s.aw[off + e];
+            r = d;
             while (s.dest[r] != r) r = s.dest[r];
+            // Path compression (the reference's findDest does the same for
+            // the queried node): lanes that read dest[d] meanwhile see an
+            // ancestor either way.
+            if (s.dest[d] != r) s.dest[d] = r;
         }
         const bool act = valid && r != u;
         const unsigned am = __ballot_sync(0xFFFFFFFFu, act);
