@@ -842,32 +842,52 @@ __global__ void k_root_emit(const int32_t* __restrict__ fa, const int32_t* __res
     }
 }
 
-// The dendrogram walk (RG:5696-5708), one thread: a root's child chain on a
-// stack, the deepest first; a popped community with a sibling pushes the
-// sibling's chain.
-__global__ void k_rabbit_walk(const uint32_t* __restrict__ roots, int64_t nr, const uint32_t* __restrict__ child,
-                              const uint32_t* __restrict__ sibling, uint32_t* __restrict__ stack, int64_t stack_cap,
-                              uint32_t* __restrict__ perm, int64_t* __restrict__ next_out, int* __restrict__ status) {
-    if (blockIdx.x != 0 || threadIdx.x != 0) return;
-    int64_t next = 0;
-    for (int64_t b = 0; b < nr; ++b) {
-        int64_t sp = 0;
-        for (uint32_t v = roots[b]; v != kNone; v = child[v]) {
-            if (sp >= stack_cap) { status[0] = 2; return; }
-            stack[sp++] = v;
+// The dendrogram walk (RG:5696-5708) numbers the roots' trees one after
+// another, so a tree's numbers start at the sum of the sizes of the trees
+// before it: the trees are walked side by side, a thread each.  Every
+// community of a merge tree is reachable from its root through child and
+// sibling links, and dest leads it to that root.
+__global__ void k_tree_of(const uint32_t* __restrict__ dest, int64_t C, const uint32_t* __restrict__ rank_of_root,
+                          int32_t* __restrict__ tsize) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < C; c += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t r = (uint32_t)c;
+        while (dest[r] != r) r = dest[r];
+        atomicAdd(&tsize[rank_of_root[r]], 1);
+    }
+}
+
+__global__ void k_rank_of_root(const uint32_t* __restrict__ roots, int64_t nr, uint32_t* __restrict__ rank_of_root) {
+    for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < nr; b += (int64_t)gridDim.x * blockDim.x)
+        rank_of_root[roots[b]] = (uint32_t)b;
+}
+
+// A root's child chain on a stack (its region: as many slots as the tree
+// has communities, each pushed at most once), the deepest first; a popped
+// community with a sibling pushes the sibling's chain.
+__global__ void k_rabbit_walk(const uint32_t* __restrict__ roots, int64_t nr, const int64_t* __restrict__ toff,
+                              const uint32_t* __restrict__ child, const uint32_t* __restrict__ sibling,
+                              uint32_t* __restrict__ stack, uint32_t* __restrict__ perm, int* __restrict__ status) {
+    for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < nr; b += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t base = toff[b], cap = toff[b + 1] - toff[b];
+        uint32_t* st = stack + base;
+        int64_t sp = 0, next = base;
+        bool ok = true;
+        for (uint32_t v = roots[b]; v != kNone && ok; v = child[v]) {
+            if (sp >= cap) ok = false;
+            else st[sp++] = v;
         }
-        while (sp > 0) {
-            const uint32_t c = stack[--sp];
+        while (ok && sp > 0) {
+            const uint32_t c = st[--sp];
             if (perm[c] != kNone) continue;
             perm[c] = (uint32_t)next++;
             if (sibling[c] != kNone)
-                for (uint32_t v = sibling[c]; v != kNone; v = child[v]) {
-                    if (sp >= stack_cap) { status[0] = 2; return; }
-                    stack[sp++] = v;
+                for (uint32_t v = sibling[c]; v != kNone && ok; v = child[v]) {
+                    if (sp >= cap) ok = false;
+                    else st[sp++] = v;
                 }
         }
+        if (!ok || next != toff[b + 1]) atomicExch(status, 2);
     }
-    next_out[0] = next;
 }
 
 // ---------------------------------------------------------------------------
@@ -1420,12 +1440,22 @@ void super_rabbit_perm(const DeviceCSR& g, const uint32_t* memb, const uint32_t*
     k_root_emit<<<grid_for(C, kT), kT, 0, s>>>(fa, fb, pa, pb, na, C, roots);
     GB_LAUNCH_CHECK();
     fill_u32(perm, 0xFFFFFFFFu, C, s);
-    DevBuf<int64_t> nextv(1, s);
-    GB_CUDA(cudaMemsetAsync(status, 0, sizeof(int), s));
-    k_rabbit_walk<<<1, 1, 0, s>>>(roots, na + nb, child, sibling, stack, stack_cap, perm, nextv, status);
+    const int64_t nr = na + nb;
+    DevBuf<uint32_t> rank_of_root(C, s);
+    DevBuf<int32_t> tsize(nr > 0 ? nr : 1, s);
+    DevBuf<int64_t> toff(nr + 1, s);
+    GB_CUDA(cudaMemsetAsync(tsize, 0, (nr > 0 ? nr : 1) * sizeof(int32_t), s));
+    k_rank_of_root<<<grid_for(nr, kT), kT, 0, s>>>(roots, nr, rank_of_root);
     GB_LAUNCH_CHECK();
-    GB_REQUIRE(read_dev(status.get(), s) == 0, GBGPU_E_CUDA, "sg_super_rabbit: dendrogram walk exceeded its stack");
-    const int64_t no = read_dev(nextv.get(), s);
+    k_tree_of<<<grid_for(C, kT), kT, 0, s>>>(dest, C, rank_of_root, tsize);
+    GB_LAUNCH_CHECK();
+    exclusive_scan_i32_to_i64(tsize, toff, nr, toff.get() + nr, s);
+    GB_CUDA(cudaMemsetAsync(status, 0, sizeof(int), s));
+    k_rabbit_walk<<<grid_for(nr, kT), kT, 0, s>>>(roots, nr, toff, child, sibling, stack, perm, status);
+    GB_LAUNCH_CHECK();
+    GB_REQUIRE(read_dev(status.get(), s) == 0, GBGPU_E_CUDA,
+               "sg_super_rabbit: a dendrogram walk did not cover its merge tree");
+    const int64_t no = read_dev(toff.get() + nr, s);
     DevBuf<int32_t> uflag(C, s);
     DevBuf<int64_t> upos(C + 1, s);
     k_unreached_flags<<<grid_for(C, kT), kT, 0, s>>>(perm, C, uflag);
