@@ -211,14 +211,14 @@ __global__ void k_unique_weights(const int64_t* __restrict__ head, int64_t m, in
     }
 }
 
+// Reverse pairs (d, c) of the unique pairs with c < d, keyed d << cb | c.
 __global__ void k_reverse_emit(const uint64_t* __restrict__ key2, const uint32_t* __restrict__ d2, int64_t m, int eb,
                                int cb, const uint8_t* __restrict__ rflag, const int64_t* __restrict__ rpos,
-                               uint64_t* __restrict__ rkey, uint32_t* __restrict__ rval) {
+                               uint64_t* __restrict__ rkey) {
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
         if (!rflag[j]) continue;
         const uint32_t c = (uint32_t)(key2[j] >> eb);
         rkey[rpos[j]] = ((uint64_t)d2[j] << cb) | c;
-        rval[rpos[j]] = c;
     }
 }
 
@@ -1107,8 +1107,7 @@ void build_super_maps(const DeviceCSR& g, const uint32_t* memb, int64_t C, Super
         exclusive_scan_u8_to_i64(rflag, rpos, m, rpos.get() + m, s);
         mr = read_dev(rpos.get() + m, s);
         rkey.alloc(mr > 0 ? mr : 1, s);
-        DevBuf<uint32_t> rval(mr > 0 ? mr : 1, s);
-        k_reverse_emit<<<grid_for(m, kT), kT, 0, s>>>(key2, d2, m, eb, cb, rflag, rpos, rkey, rval);
+        k_reverse_emit<<<grid_for(m, kT), kT, 0, s>>>(key2, d2, m, eb, cb, rflag, rpos, rkey);
         GB_LAUNCH_CHECK();
         if (mr > 0) radix_sort_keys_u64(rkey, mr, 2 * cb, s);
         // Per-map insertion order: by community, then first entry.
