@@ -89,3 +89,25 @@ def test_super_mapping_against_oracle(ctx, sup):
     memb, _ = po.leiden(rp, col, ar)
     ids_orc, _ = po.compose(rp, col, memb, "size-desc", "gorder", super_order=sup)
     np.testing.assert_array_equal(ids.cpu().numpy(), ids_orc)
+
+
+@pytest.mark.parametrize("layout", ["many-mid-maps", "one-huge-map"])
+def test_super_map_tiers_against_oracle(ctx, layout):
+    """Memberships that put communities' maps in every size tier of the map
+    simulations: 1,500 random communities of a uniform graph (maps of tens to
+    hundreds of keys: the warp tier and the shared-memory CTA tier), and half
+    the graph in community 0 beside 30,000 small ones (community 0's map has
+    about 24,000 keys, more than a CTA's shared memory holds: the global
+    tier)."""
+    rp_t, col_t = gg.uniform(16, 16, seed=82, device="cuda")
+    rp, col = rp_t.cpu().numpy(), col_t.cpu().numpy()
+    n = len(rp) - 1
+    h = (np.arange(n, dtype=np.uint64) * np.uint64(0x9E3779B97F4A7C15)) >> np.uint64(40)
+    if layout == "many-mid-maps":
+        memb = (h % np.uint64(1500)).astype(np.uint32)
+    else:
+        memb = np.where(np.arange(n) < n // 2, 0, 1 + h % np.uint64(30000)).astype(np.uint32)
+    for sup in ("super-rcm", "super-rabbit"):
+        ids, _ = ctx.order_compose(rp, col, memb, recipe(sup))
+        ids_orc, _ = po.compose(rp, col, memb, "size-desc", "bfs", super_order=sup)
+        np.testing.assert_array_equal(ids, ids_orc, err_msg=sup)
