@@ -31,6 +31,7 @@
 // sg_hilbert (:6421-6459): communities by the Hilbert index of (size,
 // average degree), each scaled to [0, 255] by its maximum (at least 1).
 #include <algorithm>
+#include <cstdlib>
 #include <limits>
 #include <vector>
 
@@ -1344,7 +1345,11 @@ void super_rabbit_perm(const DeviceCSR& g, const uint32_t* memb, const uint32_t*
         exclusive_scan_i32_to_i64(r32, rstart, C, rstart.get() + C, s);
     }
     const int64_t A0 = read_dev(voff.get() + C, s);
-    int64_t cap = 4 * A0 + 1024;
+    // Room for the aggregated lists: slack x the initial lists (4 unless
+    // GBGPU_RABBIT_ARENA_SLACK says otherwise); the arena grows when full.
+    int64_t slack = 4;
+    if (const char* v = std::getenv("GBGPU_RABBIT_ARENA_SLACK")) slack = std::max<int64_t>(1, std::atoll(v));
+    int64_t cap = slack * A0 + 64;
     DevBuf<uint32_t> ad(cap, s);
     DevBuf<float> aw(cap, s);
     if (mr > 0) {

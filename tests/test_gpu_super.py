@@ -111,3 +111,13 @@ def test_super_map_tiers_against_oracle(ctx, layout):
         ids, _ = ctx.order_compose(rp, col, memb, recipe(sup))
         ids_orc, _ = po.compose(rp, col, memb, "size-desc", "bfs", super_order=sup)
         np.testing.assert_array_equal(ids, ids_orc, err_msg=sup)
+
+
+def test_super_rabbit_arena_growth(ctx, monkeypatch):
+    """With no room beyond the initial lists the merge chain stops at the
+    first aggregated list that does not fit, the arena grows and the chain
+    resumes there: the permutation is unchanged (the RMAT-18 pin)."""
+    monkeypatch.setenv("GBGPU_RABBIT_ARENA_SLACK", "1")
+    rp, col, memb = big_graph("rmat18_s11")
+    ids, _ = ctx.order_compose(rp, col, memb, recipe("super-rabbit"))
+    assert digest(ids) == PINS["rmat18_s11"]["super-rabbit"]["size-desc"]
