@@ -50,3 +50,27 @@ def test_gapbs_g16_serial_fingerprint():
     ids, _, _, cst = po.map_graph(rp, col, ar)
     assert po.fingerprint(ids) == "9b52c0603aacbbdb"
     assert cst.fallback_communities == 1  # one community above 5000 -> BFS
+
+
+@pytest.mark.parametrize("seed", [11, 12, 13])
+def test_super_orders_and_random_intra_live(seed):
+    """sg_super_rcm / sg_super_rabbit / sg_hilbert and intra_random against
+    the reference run live with one thread, on random memberships (from a
+    few large communities to many small ones), community orders size-desc
+    and identity."""
+    rng = np.random.default_rng(seed)
+    rp, col = gg.rmat(12 + seed % 3, 12, seed=seed)
+    rp, col = rp.numpy(), col.numpy()
+    n = len(rp) - 1
+    k = [3, 40, 900][seed % 3]
+    memb = rng.integers(0, k, size=n).astype(np.uint32)
+    memb[rng.random(n) < 0.3] = 0   # one community far larger than the rest
+    for sup, tok in (("super-rcm", "sg_super_rcm"), ("super-rabbit", "sg_super_rabbit"), ("hilbert", "sg_hilbert")):
+        for comm, ctok in (("size-desc", "comm_size_desc"), ("identity", "comm_identity")):
+            opts = f"leiden:compose:{tok}:{ctok}:intra_bfs:cd_serial:norefine:2:2"
+            ref = po.ref_compose(rp, col, memb, opts, 1.0, threads=1)[0]
+            ids, _ = po.compose(rp, col, memb, comm, "bfs", super_order=sup)
+            np.testing.assert_array_equal(ids, ref, err_msg=f"{sup} {comm}")
+    opts = "leiden:compose:sg_none:comm_size_desc:intra_random:cd_serial:norefine:2:2"
+    ids, _ = po.compose(rp, col, memb, "size-desc", "random")
+    np.testing.assert_array_equal(ids, po.ref_compose(rp, col, memb, opts, 1.0, threads=1)[0])
